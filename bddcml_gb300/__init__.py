@@ -1,0 +1,258 @@
+"""GB300-native BDDC interface solver: Python binding over the C ABI.
+
+The functions below mirror the reference Fortran/C API of BDDCML
+(module_bddcml.f90, src/bddcml_interface_c.h): same names without the ``_c``
+suffix, same argument meaning, same call order.  They call the in-tree shared
+library ``libbddcgpu.so`` (built by :mod:`bddcml_gb300.build`) through ctypes;
+there is no CPU fallback - if the library or the GPU is missing, the calls
+raise :class:`BddcmlError`.
+
+Indices passed here use the ``numbase`` given to :func:`bddcml_init`.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIBPATH = os.path.join(_HERE, "libbddcgpu.so")
+_lib = None
+
+STATUS = {0: "OK", 1: "ARGUMENT", 2: "CUDA", 3: "NUMERIC", 4: "UNSUPPORTED", 5: "MEMORY"}
+
+# fields of bddcml_get_stats_c
+STAT_FIELDS = ["t_host_setup", "t_device_setup", "t_solve", "t_iterations", "t_postprocess", "num_iter",
+               "bytes_per_iteration", "ncorner", "nedge", "nface", "ndofc", "sum_ndofi", "sum_ndofo",
+               "ninterface", "precision"]
+
+EXPORTS = ["bddcml_init_c", "bddcml_upload_global_data_c", "bddcml_upload_subdomain_data_c",
+           "bddcml_setup_preconditioner_c", "bddcml_solve_c", "bddcml_download_local_solution_c",
+           "bddcml_download_global_solution_c", "bddcml_download_local_reactions_c",
+           "bddcml_download_global_reactions_c", "bddcml_change_global_data_c", "bddcml_change_subdomain_data_c",
+           "bddcml_setup_new_data_c", "bddcml_dotprod_subdomain_c", "bddcml_finalize_c",
+           "bddcml_get_last_error_c", "bddcml_set_precision_c", "bddcml_get_stats_c",
+           "bddcml_get_residual_history_c", "bddcml_get_interface_weights_c", "bddcml_get_coarse_info_c"]
+
+
+class BddcmlError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{STATUS.get(code, code)}] {msg}")
+        self.code = code
+
+
+def lib():
+    """Loads libbddcgpu.so (build it with ``python -m bddcml_gb300.build``)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIBPATH):
+            raise BddcmlError(2, f"{LIBPATH} is missing: run bddcml_gb300.build.build() first")
+        _lib = C.CDLL(LIBPATH)
+        _lib.bddcml_get_last_error_c.restype = C.c_int
+    return _lib
+
+
+def _i(v):
+    return C.byref(C.c_int(int(v)))
+
+
+def _d(v):
+    return C.byref(C.c_double(float(v)))
+
+
+def _pi(a):
+    a = np.ascontiguousarray(a, dtype=np.int32)
+    return a, a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def _pd(a):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a, a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def last_error():
+    buf = C.create_string_buffer(1024)
+    code = lib().bddcml_get_last_error_c(buf, _i(1024))
+    return code, buf.value.decode(errors="replace")
+
+
+def _check():
+    code, msg = last_error()
+    if code != 0:
+        raise BddcmlError(code, msg)
+
+
+# ------------------------------------------------------------- reference API
+def bddcml_init(nl: int, nsublev, nsub_loc_1: int = -1, comm_init: int = 0, verbose_level: int = 0,
+                numbase: int = 0, just_direct_solve_int: int = 0) -> int:
+    """module_bddcml.f90:36-101; returns nsub_loc_1 (all subdomains are local)."""
+    ns, pns = _pi(nsublev)
+    loc = C.c_int(nsub_loc_1)
+    lib().bddcml_init_c(_i(nl), pns, _i(len(ns)), C.byref(loc), _i(comm_init), _i(verbose_level), _i(numbase),
+                        _i(just_direct_solve_int))
+    _check()
+    return loc.value
+
+
+def bddcml_upload_subdomain_data(nelem, nnod, ndof, ndim, meshdim, isub, nelems, nnods, ndofs,
+                                 inet, nnet, nndf, isngn, isvgvn, isegn, xyz, ifix, fixv, rhs, is_rhs_complete,
+                                 sol, matrixtype, i_sparse, j_sparse, a_sparse, is_assembled,
+                                 find_components_int=1, use_dual_mesh_graph_int=1, neighbouring=3):
+    """module_bddcml.f90:186-356.  ``xyz`` is (nnods, ndim) or its Fortran
+    (column-major) flattening."""
+    xyz = np.asarray(xyz, dtype=np.float64)
+    if xyz.ndim == 2:
+        if xyz.shape == (ndim, nnods):
+            xyzf = np.ascontiguousarray(xyz).ravel()      # rows = coordinates -> already column-major order
+        else:
+            xyzf = np.ascontiguousarray(xyz.T).ravel()
+    else:
+        xyzf = xyz
+    keep = []
+
+    def P(a, f):
+        arr, ptr = f(a)
+        keep.append(arr)
+        return ptr, len(arr)
+
+    p_inet, l_inet = P(inet, _pi)
+    p_nnet, l_nnet = P(nnet, _pi)
+    p_nndf, l_nndf = P(nndf, _pi)
+    p_isngn, l_isngn = P(isngn, _pi)
+    p_isvgvn, l_isvgvn = P(isvgvn, _pi)
+    p_isegn, l_isegn = P(isegn, _pi)
+    p_xyz, _ = P(xyzf, _pd)
+    p_ifix, l_ifix = P(ifix, _pi)
+    p_fixv, l_fixv = P(fixv, _pd)
+    p_rhs, l_rhs = P(rhs, _pd)
+    p_sol, l_sol = P(sol, _pd)
+    p_i, la = P(i_sparse, _pi)
+    p_j, _ = P(j_sparse, _pi)
+    p_a, _ = P(a_sparse, _pd)
+    empty = (C.c_double * 1)()
+    lib().bddcml_upload_subdomain_data_c(
+        _i(nelem), _i(nnod), _i(ndof), _i(ndim), _i(meshdim), _i(isub), _i(nelems), _i(nnods), _i(ndofs),
+        p_inet, _i(l_inet), p_nnet, _i(l_nnet), p_nndf, _i(l_nndf), p_isngn, _i(l_isngn), p_isvgvn, _i(l_isvgvn),
+        p_isegn, _i(l_isegn), p_xyz, _i(nnods), _i(ndim), p_ifix, _i(l_ifix), p_fixv, _i(l_fixv), p_rhs, _i(l_rhs),
+        _i(is_rhs_complete), p_sol, _i(l_sol), _i(matrixtype), p_i, p_j, p_a, _i(la), _i(is_assembled),
+        empty, _i(0), _i(0), empty, _i(0), _i(0), empty, _i(0),
+        _i(find_components_int), _i(use_dual_mesh_graph_int), _i(neighbouring))
+    _check()
+
+
+def bddcml_setup_preconditioner(matrixtype=1, use_defaults_int=0, parallel_division_int=1,
+                                use_corner_constraints_int=1, use_arithmetic_constraints_int=1,
+                                use_adaptive_constraints_int=0, use_user_constraints_int=0, weights_type=0):
+    """module_bddcml.f90:359-455."""
+    lib().bddcml_setup_preconditioner_c(_i(matrixtype), _i(use_defaults_int), _i(parallel_division_int),
+                                        _i(use_corner_constraints_int), _i(use_arithmetic_constraints_int),
+                                        _i(use_adaptive_constraints_int), _i(use_user_constraints_int),
+                                        _i(weights_type))
+    _check()
+
+
+def bddcml_solve(comm_all=0, method=0, tol=1e-6, maxit=1000, ndecrmax=30, recycling_int=0,
+                 max_number_of_stored_vectors=100):
+    """module_bddcml.f90:459-567; returns (num_iter, converged_reason, condition_number)."""
+    it, reason, cond = C.c_int(), C.c_int(), C.c_double()
+    lib().bddcml_solve_c(_i(comm_all), _i(method), _d(tol), _i(maxit), _i(ndecrmax), _i(recycling_int),
+                         _i(max_number_of_stored_vectors), C.byref(it), C.byref(reason), C.byref(cond))
+    _check()
+    return it.value, reason.value, cond.value
+
+
+def bddcml_download_local_solution(isub: int, lsols: int) -> np.ndarray:
+    out = np.zeros(lsols)
+    lib().bddcml_download_local_solution_c(_i(isub), out.ctypes.data_as(C.POINTER(C.c_double)), _i(lsols))
+    _check()
+    return out
+
+
+def bddcml_dotprod_subdomain(isub: int, vec1, vec2) -> float:
+    a, pa = _pd(vec1)
+    b, pb = _pd(vec2)
+    d = C.c_double()
+    lib().bddcml_dotprod_subdomain_c(_i(isub), pa, _i(len(a)), pb, _i(len(b)), C.byref(d))
+    _check()
+    return d.value
+
+
+def bddcml_finalize():
+    lib().bddcml_finalize_c()
+    _check()
+
+
+# ---------------------------------------------------------------- extensions
+def set_precision(mode: int):
+    """0 = plain FP64, 1 = mixed precision (default)."""
+    lib().bddcml_set_precision_c(_i(mode))
+    _check()
+
+
+def get_stats() -> dict:
+    buf = (C.c_double * 32)()
+    n = C.c_int(32)
+    lib().bddcml_get_stats_c(buf, C.byref(n))
+    _check()
+    return {k: buf[i] for i, k in enumerate(STAT_FIELDS[: n.value])}
+
+
+def get_residual_history() -> np.ndarray:
+    n = C.c_int(0)
+    lib().bddcml_get_residual_history_c(None, C.byref(n))
+    _check()
+    out = np.zeros(n.value)
+    m = C.c_int(n.value)
+    lib().bddcml_get_residual_history_c(out.ctypes.data_as(C.POINTER(C.c_double)), C.byref(m))
+    _check()
+    return out
+
+
+def get_interface_weights(isub: int, ndofi: int) -> np.ndarray:
+    out = np.zeros(ndofi)
+    lib().bddcml_get_interface_weights_c(_i(isub), out.ctypes.data_as(C.POINTER(C.c_double)), _i(ndofi))
+    _check()
+    return out
+
+
+def get_coarse_info() -> dict:
+    buf = (C.c_int * 6)()
+    n = C.c_int(6)
+    lib().bddcml_get_coarse_info_c(buf, C.byref(n))
+    _check()
+    keys = ["ncorner", "nedge", "nface", "ndofc", "sum_ndofi", "sum_ndofo"]
+    return {k: int(buf[i]) for i, k in enumerate(keys)}
+
+
+# ------------------------------------------------------------ convenience
+def upload_problem(prob, numbase: int = 0, find_components_int: int = 1, neighbouring: int = 3):
+    """Uploads every subdomain of a :class:`bddcml_gb300.problems.Problem`
+    (0-based arrays) through the C ABI, shifting indices to ``numbase``."""
+    nb = numbase
+    for s in prob.subdomains:
+        bddcml_upload_subdomain_data(
+            prob.nelem, prob.nnod, prob.ndof, prob.ndim, prob.meshdim, s.isub + nb, s.nelems, s.nnods, s.ndofs,
+            s.inet + nb, s.nnet, s.nndf, s.isngn + nb, s.isvgvn + nb, s.isegn + nb, s.xyz, s.ifix, s.fixv,
+            s.rhs, s.is_rhs_complete, s.sol, prob.matrixtype, s.i_sparse + nb, s.j_sparse + nb, s.a_sparse,
+            s.is_assembled, find_components_int=find_components_int, neighbouring=neighbouring)
+
+
+def solve_problem(prob, precision: int = 1, tol: float = 1e-8, maxit: int = 500, ndecrmax: int = 50,
+                  weights_type: int = 0, numbase: int = 0, finalize: bool = True):
+    """init -> upload -> setup -> solve -> download (-> finalize) through the
+    C ABI, the sequence of the reference example poisson_on_cube.f90:373-672.
+    Returns (global solution, num_iter, reason, cond, stats)."""
+    bddcml_init(2, [prob.nsub, 1], -1, 0, 0, numbase, 0)
+    set_precision(precision)
+    upload_problem(prob, numbase=numbase)
+    bddcml_setup_preconditioner(prob.matrixtype, 0, 1, 1, 1, 0, 0, weights_type)
+    it, reason, cond = bddcml_solve(0, 0, tol, maxit, ndecrmax, 0, 0)
+    u = np.zeros(prob.ndof)
+    for s in prob.subdomains:
+        u[s.isvgvn] = bddcml_download_local_solution(s.isub + numbase, s.ndofs)
+    st = get_stats()
+    if finalize:
+        bddcml_finalize()
+    return u, it, reason, cond, st

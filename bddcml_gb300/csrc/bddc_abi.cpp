@@ -1,0 +1,375 @@
+// C ABI of the GB300 BDDC solver: the bddcml_*_c entry points of the
+// reference header src/bddcml_interface_c.h with identical signatures, over
+// one global solver instance (the reference keeps its state in module
+// variables, module_levels.f90:158-175, module_krylov.f90:33-43).
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+
+#include "../../include/bddcml_gb300.h"
+#include "bddc_internal.hpp"
+
+using namespace bddc;
+
+namespace {
+
+std::unique_ptr<Solver> g_solver;
+int g_status = BDDCML_OK;
+std::string g_msg;
+
+void set_error(int code, const std::string& msg) {
+  g_status = code;
+  g_msg = msg;
+}
+
+void clear_error() {
+  g_status = BDDCML_OK;
+  g_msg.clear();
+}
+
+Solver* need_solver(const char* who) {
+  if (!g_solver) {
+    set_error(BDDCML_ERR_ARGUMENT, std::string(who) + ": bddcml_init_c has not been called");
+    return nullptr;
+  }
+  return g_solver.get();
+}
+
+template <typename F>
+void guarded(const char* who, F&& f) {
+  clear_error();
+  try {
+    f();
+  } catch (Error& e) {
+    set_error(e.code, std::string(who) + ": " + e.msg);
+  } catch (std::bad_alloc&) {
+    set_error(BDDCML_ERR_MEMORY, std::string(who) + ": host allocation failed");
+  } catch (std::exception& e) {
+    set_error(BDDCML_ERR_ARGUMENT, std::string(who) + ": " + e.what());
+  }
+}
+
+int sub_index(Solver& S, int isub_in) {
+  int t = isub_in - S.prm.numbase;
+  if (t < 0 || t >= (int)S.subs.size())
+    throw Error{ERR_ARGUMENT, "subdomain index " + std::to_string(isub_in) + " out of range"};
+  return t;
+}
+
+}  // namespace
+
+extern "C" {
+
+void bddcml_init_c(int* nl, int* nsublev, int* lnsublev, int* nsub_loc_1, int* comm_init, int* verbose_level,
+                   int* numbase, int* just_direct_solve_int) {
+  guarded("bddcml_init_c", [&] {
+    (void)comm_init;
+    if (!nl || !nsublev || !lnsublev || !nsub_loc_1 || !numbase)
+      throw Error{ERR_ARGUMENT, "null argument"};
+    if (*nl < 2) throw Error{ERR_ARGUMENT, "number of levels must be at least 2"};
+    if (*lnsublev < *nl) throw Error{ERR_ARGUMENT, "lnsublev smaller than the number of levels"};
+    if (nsublev[*nl - 1] != 1) throw Error{ERR_ARGUMENT, "number of subdomains at the last level must be 1"};
+    if (*nl > 2) throw Error{ERR_UNSUPPORTED, "only 2 levels are implemented"};
+    if (just_direct_solve_int && *just_direct_solve_int)
+      throw Error{ERR_UNSUPPORTED, "the global direct solve (just_direct_solve) is not implemented"};
+    if (*nsub_loc_1 != -1 && *nsub_loc_1 != nsublev[0])
+      throw Error{ERR_ARGUMENT, "all subdomains live in this process: nsub_loc_1 must be -1 or nsublev[0]"};
+    if (g_solver) {
+      if (g_solver->dev) device_destroy(g_solver->dev);
+      g_solver.reset();
+    }
+    auto S = std::make_unique<Solver>();
+    S->prm.nlevels = *nl;
+    S->prm.nsub = nsublev[0];
+    S->prm.numbase = *numbase;
+    S->prm.verbose = verbose_level ? *verbose_level : 0;
+    S->subs.resize(nsublev[0]);
+    *nsub_loc_1 = nsublev[0];
+    g_solver = std::move(S);
+  });
+}
+
+void bddcml_upload_global_data_c(int*, int*, int*, int*, int*, int*, int*, int*, int*, int*, int*, double*, int*,
+                                 int*, int*, int*, double*, int*, double*, int*, double*, int*, int*, int*, int*) {
+  clear_error();
+  set_error(BDDCML_ERR_UNSUPPORTED, "bddcml_upload_global_data_c: global data loading is not implemented");
+}
+
+void bddcml_upload_subdomain_data_c(int* nelem, int* nnod, int* ndof, int* ndim, int* meshdim, int* isub,
+                                    int* nelems, int* nnods, int* ndofs, int* inet, int* linet, int* nnet,
+                                    int* lnnet, int* nndf, int* lnndf, int* isngn, int* lisngn, int* isvgvn,
+                                    int* lisvgvn, int* isegn, int* lisegn, double* xyz, int* lxyz1, int* lxyz2,
+                                    int* ifix, int* lifix, double* fixv, int* lfixv, double* rhs, int* lrhs,
+                                    int* is_rhs_complete, double* sol, int* lsol, int* matrixtype, int* i_sparse,
+                                    int* j_sparse, double* a_sparse, int* la, int* is_assembled_int,
+                                    double* user_constraints, int* luser_constraints1, int* luser_constraints2,
+                                    double* element_data, int* lelement_data1, int* lelement_data2,
+                                    double* dof_data, int* ldof_data, int* find_components_int,
+                                    int* use_dual_mesh_graph_int, int* neighbouring) {
+  guarded("bddcml_upload_subdomain_data_c", [&] {
+    Solver* S = need_solver("bddcml_upload_subdomain_data_c");
+    if (!S) return;
+    (void)user_constraints; (void)element_data; (void)dof_data; (void)meshdim;
+    (void)luser_constraints2; (void)lelement_data1; (void)lelement_data2; (void)ldof_data;
+    if (luser_constraints1 && *luser_constraints1 > 0)
+      throw Error{ERR_UNSUPPORTED, "user constraints are not implemented"};
+    int t = sub_index(*S, *isub);
+    Subdomain& s = S->subs[t];
+    if (s.loaded) throw Error{ERR_ARGUMENT, "mesh already loaded for this subdomain"};
+    const int nb = S->prm.numbase;
+    if (*lnnet != *nelems || *lnndf != *nnods || *lisngn != *nnods || *lisegn != *nelems || *lxyz1 != *nnods ||
+        *lxyz2 != *ndim || *lisvgvn != *ndofs || *lifix != *ndofs || *lfixv != *ndofs || *lrhs != *ndofs ||
+        *lsol != *ndofs)
+      throw Error{ERR_ARGUMENT, "array length does not match nelems/nnods/ndofs/ndim"};
+    long sum_nnet = 0;
+    for (int e = 0; e < *nelems; ++e) sum_nnet += nnet[e];
+    if (sum_nnet != *linet) throw Error{ERR_ARGUMENT, "NNET does not sum up to LINET"};
+    long sum_nndf = 0;
+    for (int i = 0; i < *nnods; ++i) sum_nndf += nndf[i];
+    if (sum_nndf != *ndofs) throw Error{ERR_ARGUMENT, "NNDF does not sum up to NDOFS"};
+    s.nelem = *nelems; s.nnod = *nnods; s.ndof = *ndofs; s.ndim = *ndim;
+    s.inet.resize(*linet);
+    for (int k = 0; k < *linet; ++k) s.inet[k] = inet[k] - nb;
+    s.nnet.assign(nnet, nnet + *nelems);
+    s.nndf.assign(nndf, nndf + *nnods);
+    s.isngn.resize(*nnods);
+    for (int i = 0; i < *nnods; ++i) s.isngn[i] = isngn[i] - nb;
+    s.isvgvn.resize(*ndofs);
+    for (int i = 0; i < *ndofs; ++i) s.isvgvn[i] = isvgvn[i] - nb;
+    s.isegn.resize(*nelems);
+    for (int e = 0; e < *nelems; ++e) s.isegn[e] = isegn[e] - nb;
+    s.xyz.assign(xyz, xyz + (size_t)(*nnods) * (*ndim));
+    s.ifix.assign(ifix, ifix + *ndofs);
+    s.fixv.assign(fixv, fixv + *ndofs);
+    s.rhs.assign(rhs, rhs + *ndofs);
+    s.rhs_complete = is_rhs_complete && *is_rhs_complete != 0;
+    s.sol.assign(sol, sol + *ndofs);
+    s.matrixtype = *matrixtype;
+    if (*matrixtype != 1 && *matrixtype != 2)
+      throw Error{ERR_UNSUPPORTED, "only symmetric matrices (matrixtype 1 or 2) are implemented"};
+    s.ia.resize(*la); s.ja.resize(*la);
+    for (int k = 0; k < *la; ++k) {
+      s.ia[k] = i_sparse[k] - nb;
+      s.ja[k] = j_sparse[k] - nb;
+      if (s.ia[k] > s.ja[k])
+        throw Error{ERR_ARGUMENT, "matrix in wrong format - only the upper triangle is expected for symmetric problems"};
+      if (s.ia[k] < 0 || s.ja[k] >= *ndofs) throw Error{ERR_ARGUMENT, "matrix index out of range"};
+    }
+    s.a.assign(a_sparse, a_sparse + *la);
+    (void)is_assembled_int;
+    host_assemble_upper(s.ia, s.ja, s.a);
+    s.find_components = find_components_int && *find_components_int != 0;
+    s.dual_graph = use_dual_mesh_graph_int && *use_dual_mesh_graph_int != 0;
+    s.neighbouring = neighbouring ? *neighbouring : 1;
+    host_nodal_components(s);
+    s.loaded = true;
+    (void)nelem; (void)nnod; (void)ndof;
+    S->nelem = *nelem; S->nnod = *nnod;
+    S->setup_done = false;
+  });
+}
+
+void bddcml_setup_preconditioner_c(int* matrixtype, int* use_defaults_int, int* parallel_division_int,
+                                   int* use_corner_constraints_int, int* use_arithmetic_constraints_int,
+                                   int* use_adaptive_constraints_int, int* use_user_constraints_int,
+                                   int* weights_type) {
+  guarded("bddcml_setup_preconditioner_c", [&] {
+    Solver* S = need_solver("bddcml_setup_preconditioner_c");
+    if (!S) return;
+    (void)parallel_division_int;
+    S->prm.matrixtype = *matrixtype;
+    if (use_defaults_int && *use_defaults_int) {  // module_bddcml.f90:411-416
+      S->prm.use_corner = true; S->prm.use_arith = true; S->prm.use_adaptive = false; S->prm.use_user = false;
+      S->prm.weights_type = 0;
+    } else {
+      S->prm.use_corner = *use_corner_constraints_int != 0;
+      S->prm.use_arith = *use_arithmetic_constraints_int != 0;
+      S->prm.use_adaptive = *use_adaptive_constraints_int != 0;
+      S->prm.use_user = *use_user_constraints_int != 0;
+      S->prm.weights_type = *weights_type;
+    }
+    if (S->prm.use_adaptive) throw Error{ERR_UNSUPPORTED, "adaptive constraints are not implemented"};
+    if (S->prm.use_user) throw Error{ERR_UNSUPPORTED, "user constraints are not implemented"};
+    double t0 = wall_time();
+    S->stats = Stats{};
+    host_setup(*S);
+    S->stats.t_host_setup = wall_time() - t0;
+    if (!S->dev) {
+      Error err{0, ""};
+      S->dev = device_create(err);
+      if (!S->dev) throw err;
+    }
+    Error err{0, ""};
+    if (!device_setup(*S, err)) throw err;
+    S->setup_done = true;
+  });
+}
+
+void bddcml_solve_c(int* comm_all, int* method, double* tol, int* maxit, int* ndecrmax, int* recycling_int,
+                    int* max_number_of_stored_vectors, int* num_iter, int* converged_reason,
+                    double* condition_number) {
+  guarded("bddcml_solve_c", [&] {
+    (void)comm_all; (void)recycling_int; (void)max_number_of_stored_vectors;
+    Solver* S = need_solver("bddcml_solve_c");
+    if (!S) return;
+    if (!S->setup_done) throw Error{ERR_ARGUMENT, "preconditioner is not set up"};
+    int m = *method;
+    double t = 1e-6;   // module_bddcml.f90:515-520 defaults
+    int mi = 1000, nd = 30;
+    if (m == -1) {
+      throw Error{ERR_UNSUPPORTED, "the default Krylov method of the reference is BiCGSTAB, which is not implemented; "
+                                  "use method 0 (PCG)"};
+    }
+    if (m != 0) throw Error{ERR_UNSUPPORTED, "only method 0 (PCG) is implemented"};
+    t = *tol; mi = *maxit; nd = *ndecrmax;
+    if (mi < 1) throw Error{ERR_ARGUMENT, "maxit must be positive"};
+    int it = 0, reason = 0;
+    double cond = 1.0;
+    Error err{0, ""};
+    if (!device_solve(*S, t, mi, nd, it, reason, cond, err)) throw err;
+    *num_iter = it;
+    *converged_reason = reason;
+    *condition_number = cond;
+  });
+}
+
+void bddcml_download_local_solution_c(int* isub, double* sols, int* lsols) {
+  guarded("bddcml_download_local_solution_c", [&] {
+    Solver* S = need_solver("bddcml_download_local_solution_c");
+    if (!S) return;
+    int t = sub_index(*S, *isub);
+    Subdomain& s = S->subs[t];
+    if (*lsols != s.ndof) throw Error{ERR_ARGUMENT, "lsols does not match the subdomain dof count"};
+    std::copy(s.sol.begin(), s.sol.end(), sols);
+  });
+}
+
+void bddcml_download_global_solution_c(double*, int*) {
+  clear_error();
+  set_error(BDDCML_ERR_UNSUPPORTED, "bddcml_download_global_solution_c: global data is not implemented");
+}
+
+void bddcml_download_local_reactions_c(int*, double*, int*) {
+  clear_error();
+  set_error(BDDCML_ERR_UNSUPPORTED, "bddcml_download_local_reactions_c: reactions are not implemented");
+}
+
+void bddcml_download_global_reactions_c(double*, int*) {
+  clear_error();
+  set_error(BDDCML_ERR_UNSUPPORTED, "bddcml_download_global_reactions_c: reactions are not implemented");
+}
+
+void bddcml_change_global_data_c(int*, int*, double*, int*, double*, int*, double*, int*) {
+  clear_error();
+  set_error(BDDCML_ERR_UNSUPPORTED, "bddcml_change_global_data_c: global data is not implemented");
+}
+
+void bddcml_change_subdomain_data_c(int* isub, int* ifix, int* lifix, double* fixv, int* lfixv, double* rhs,
+                                    int* lrhs, int* is_rhs_complete, double* sol, int* lsol) {
+  guarded("bddcml_change_subdomain_data_c", [&] {
+    (void)isub; (void)ifix; (void)lifix; (void)fixv; (void)lfixv; (void)rhs; (void)lrhs; (void)is_rhs_complete;
+    (void)sol; (void)lsol;
+    throw Error{ERR_UNSUPPORTED, "changing subdomain data after setup is not implemented"};
+  });
+}
+
+void bddcml_setup_new_data_c(void) {
+  guarded("bddcml_setup_new_data_c", [&] {
+    throw Error{ERR_UNSUPPORTED, "new data after setup is not implemented"};
+  });
+}
+
+void bddcml_dotprod_subdomain_c(int* isub, double* vec1, int* lvec1, double* vec2, int* lvec2, double* dotprod) {
+  guarded("bddcml_dotprod_subdomain_c", [&] {
+    Solver* S = need_solver("bddcml_dotprod_subdomain_c");
+    if (!S) return;
+    int t = sub_index(*S, *isub);
+    Subdomain& s = S->subs[t];
+    if (s.wi.empty() && s.ndofi > 0) throw Error{ERR_ARGUMENT, "weights are not ready"};
+    if (*lvec1 != *lvec2 || *lvec1 != s.ndof) throw Error{ERR_ARGUMENT, "dimension mismatch"};
+    double d = 0.0;  // module_dd.f90:12736-12788
+    for (int i = 0; i < s.ndofi; ++i) d += vec1[s.iivsvn[i]] * s.wi[i] * vec2[s.iivsvn[i]];
+    for (int i = 0; i < s.ndofo; ++i) d += vec1[s.iovsvn[i]] * vec2[s.iovsvn[i]];
+    *dotprod = d;
+  });
+}
+
+void bddcml_finalize_c(void) {
+  guarded("bddcml_finalize_c", [&] {
+    if (g_solver) {
+      if (g_solver->dev) device_destroy(g_solver->dev);
+      g_solver.reset();
+    }
+  });
+}
+
+int bddcml_get_last_error_c(char* msg, int* lmsg) {
+  if (msg && lmsg && *lmsg > 0) {
+    int n = std::min<int>((int)g_msg.size(), *lmsg - 1);
+    std::memcpy(msg, g_msg.data(), n);
+    msg[n] = '\0';
+  }
+  return g_status;
+}
+
+void bddcml_set_precision_c(int* mode) {
+  guarded("bddcml_set_precision_c", [&] {
+    Solver* S = need_solver("bddcml_set_precision_c");
+    if (!S) return;
+    if (*mode != 0 && *mode != 1) throw Error{ERR_ARGUMENT, "precision mode must be 0 (FP64) or 1 (mixed)"};
+    S->prm.precision = *mode;
+  });
+}
+
+void bddcml_get_stats_c(double* stats, int* lstats) {
+  guarded("bddcml_get_stats_c", [&] {
+    Solver* S = need_solver("bddcml_get_stats_c");
+    if (!S) return;
+    const Stats& q = S->stats;
+    double v[] = {q.t_host_setup, q.t_device_setup, q.t_solve, q.t_iterations, q.t_postprocess,
+                  (double)q.num_iter, q.bytes_per_iteration, (double)q.ncorner, (double)q.nedge, (double)q.nface,
+                  (double)q.ndofc, (double)q.sum_ndofi, (double)q.sum_ndofo, (double)q.ninterface,
+                  (double)S->prm.precision};
+    int n = std::min<int>(*lstats, (int)(sizeof(v) / sizeof(v[0])));
+    for (int i = 0; i < n; ++i) stats[i] = v[i];
+    *lstats = n;
+  });
+}
+
+void bddcml_get_residual_history_c(double* hist, int* lhist) {
+  guarded("bddcml_get_residual_history_c", [&] {
+    Solver* S = need_solver("bddcml_get_residual_history_c");
+    if (!S) return;
+    int n = std::min<int>(*lhist, (int)S->relres_history.size());
+    for (int i = 0; i < n; ++i) hist[i] = S->relres_history[i];
+    *lhist = (int)S->relres_history.size();
+  });
+}
+
+void bddcml_get_interface_weights_c(int* isub, double* wi, int* lwi) {
+  guarded("bddcml_get_interface_weights_c", [&] {
+    Solver* S = need_solver("bddcml_get_interface_weights_c");
+    if (!S) return;
+    int t = sub_index(*S, *isub);
+    Subdomain& s = S->subs[t];
+    if (*lwi != (int)s.wi.size()) throw Error{ERR_ARGUMENT, "lwi does not match ndofi"};
+    std::copy(s.wi.begin(), s.wi.end(), wi);
+  });
+}
+
+void bddcml_get_coarse_info_c(int* out, int* lout) {
+  guarded("bddcml_get_coarse_info_c", [&] {
+    Solver* S = need_solver("bddcml_get_coarse_info_c");
+    if (!S) return;
+    long si = 0, so = 0;
+    for (auto& s : S->subs) { si += s.ndofi; so += s.ndofo; }
+    int v[] = {S->ncorner, S->nedge, S->nface, S->ndofc, (int)si, (int)so};
+    int n = std::min<int>(*lout, 6);
+    for (int i = 0; i < n; ++i) out[i] = v[i];
+    *lout = n;
+  });
+}
+
+}  // extern "C"

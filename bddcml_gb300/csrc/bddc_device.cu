@@ -1,0 +1,775 @@
+// GPU side of the BDDC solver: data layout in HBM, setup orchestration and
+// the PCG driver.  See bddc_setup_kernels.cuh and bddc_pcg_kernels.cuh for
+// the kernels and their reference counterparts.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "bddc_internal.hpp"
+#include "bddc_pcg_kernels.cuh"
+
+namespace bddc {
+
+#define CK(call)                                                                                \
+  do {                                                                                          \
+    cudaError_t e_ = (call);                                                                    \
+    if (e_ != cudaSuccess)                                                                      \
+      throw Error{ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)};                \
+  } while (0)
+
+#define CKL()                                                                                   \
+  do {                                                                                          \
+    cudaError_t e_ = cudaGetLastError();                                                        \
+    if (e_ != cudaSuccess) throw Error{ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e_)}; \
+  } while (0)
+
+static inline int roundup(int x, int m) { return (x + m - 1) / m * m; }
+
+template <typename T>
+static T* dalloc(size_t n, std::vector<void*>& owned) {
+  T* p = nullptr;
+  if (n == 0) n = 1;
+  cudaError_t e = cudaMalloc(&p, n * sizeof(T));
+  if (e != cudaSuccess)
+    throw Error{ERR_MEMORY, "cudaMalloc of " + std::to_string(n * sizeof(T)) + " bytes: " + cudaGetErrorString(e)};
+  owned.push_back(p);
+  return p;
+}
+
+template <typename T>
+static T* upload(const std::vector<T>& v, std::vector<void*>& owned, cudaStream_t st) {
+  T* p = dalloc<T>(v.size(), owned);
+  if (!v.empty()) CK(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+  return p;
+}
+
+class Device {
+ public:
+  cudaStream_t st = nullptr;
+  std::vector<void*> owned;    // freed on destruction / re-setup
+  bool mixed = true;
+  int nsub = 0;
+  std::vector<DevSub> hs;
+  DevSub* ds = nullptr;
+  // pools
+  void* poolT = nullptr;   // factor precision
+  void* poolPC = nullptr;  // preconditioner precision
+  void* poolS = nullptr;   // Schur operator (float2 pairs or double)
+  double* small = nullptr;
+  // CSR blocks
+  CsrView koo{}, koi{}, kio{}, kii{};
+  int *c_ptr = nullptr, *c_col = nullptr;
+  double* c_val = nullptr;
+  int* cmap = nullptr;
+  int *co_ptr = nullptr, *co_sub = nullptr, *co_loc = nullptr;
+  // interface numbering
+  int n = 0, nrep = 0;
+  int* uniq = nullptr;
+  Owners own{};
+  int* fixed = nullptr;
+  double *wsum = nullptr, *wrep = nullptr;
+  // vectors
+  double *x = nullptr, *r = nullptr, *p = nullptr, *ap = nullptr, *z = nullptr, *g = nullptr;
+  double *yrep = nullptr, *zrep = nullptr, *grep = nullptr, *fi = nullptr, *fo = nullptr;
+  long long* fo_off = nullptr;
+  double *rcpart = nullptr, *rc = nullptr, *uc = nullptr, *cpool = nullptr, *ainv = nullptr;
+  int ndofc = 0, ldc = 0, nrb = 0, ncpmax = 0, maxNI = 0, maxNO = 0;
+  double* part = nullptr;
+  int npart = 0;
+  PcgCtl* ctl = nullptr;
+  PcgCtl* hctl = nullptr;  // pinned
+  double *hist = nullptr, *diag = nullptr, *subdiag = nullptr;
+  int maxit_alloc = 0;
+  double* uo = nullptr;
+  long long* uo_off = nullptr;
+  std::vector<long long> huo_off;
+  int* err = nullptr;
+  double* scal = nullptr;  // scratch scalar
+  BandDesc* bd_oo = nullptr;
+  std::vector<BandDesc> hbd_oo;
+  int maxnbo = 0, maxw = 0, maxNR = 0;
+  int nref = 0;
+
+  ~Device() { release(); if (hctl) cudaFreeHost(hctl); if (st) cudaStreamDestroy(st); }
+  void release() {
+    for (void* q : owned) cudaFree(q);
+    owned.clear();
+    maxit_alloc = 0;
+  }
+};
+
+Device* device_create(Error& err) {
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) {
+    err = Error{ERR_CUDA, std::string("no CUDA device: ") + (e == cudaSuccess ? "device count 0" : cudaGetErrorString(e))};
+    return nullptr;
+  }
+  auto* d = new Device;
+  if (cudaStreamCreateWithFlags(&d->st, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaMallocHost(&d->hctl, sizeof(PcgCtl)) != cudaSuccess) {
+    err = Error{ERR_CUDA, "stream or pinned allocation failed"};
+    delete d;
+    return nullptr;
+  }
+  return d;
+}
+
+void device_destroy(Device* d) { delete d; }
+
+// ------------------------------------------------------------ band phases
+template <typename T>
+static void run_factor(Device& D, const BandDesc* bd, int nbatch, int maxnb, int maxw, T* pool) {
+  size_t smem = (2 * NB * (NB + 1) + 2 * KC * NB) * sizeof(T);
+  CK(cudaFuncSetAttribute(k_chol_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  for (int k = 0; k < maxnb; ++k) {
+    k_chol_diag<T><<<nbatch, NT, smem, D.st>>>(bd, pool, k, D.err);
+    CKL();
+    if (maxw > 0) {
+      k_chol_off<T><<<dim3(maxw, nbatch), NT, 0, D.st>>>(bd, pool, k);
+      CKL();
+    }
+  }
+}
+
+template <typename T>
+static void run_solve(Device& D, const BandDesc* bd, int nbatch, int maxnb, int maxncol, const T* L, T* B) {
+  dim3 grid(maxncol / NB, nbatch);
+  for (int k = 0; k < maxnb; ++k) {
+    k_trsm_fwd<T><<<grid, NT, 0, D.st>>>(bd, L, B, k);
+    CKL();
+  }
+  for (int k = maxnb - 1; k >= 0; --k) {
+    k_trsm_bwd<T><<<grid, NT, 0, D.st>>>(bd, L, B, k);
+    CKL();
+  }
+}
+
+// ------------------------------------------------------- host preparation
+struct SubBlocks {
+  vector<int> oo_ptr, oo_col, oi_ptr, oi_col, io_ptr, io_col, ii_ptr, ii_col;
+  vector<double> oo_val, oi_val, io_val, ii_val;
+  vector<double> fo, fi;  // interior rhs (new order), interface rhs (weighted)
+  int w = 0;
+  double rho = 1.0;
+  int maxrow_oo = 0, maxrow_oi = 0, maxrow_io = 0, maxrow_ii = 0;
+};
+
+static void prepare_blocks(Subdomain& s, SubBlocks& b) {
+  vector<int> fptr, fcol;
+  vector<double> fval;
+  full_symmetric_csr(s, fptr, fcol, fval);
+  host_interior_ordering(s, fptr, fcol);
+  int no = s.ndofo, ni = s.ndofi;
+  vector<int> onew(s.ndof, -1), iidx(s.ndof, -1);
+  for (int q = 0; q < no; ++q) onew[s.iovsvn[s.operm[q]]] = q;
+  for (int i = 0; i < ni; ++i) iidx[s.iivsvn[i]] = i;
+  auto build = [&](int nrow, auto rowdof, const vector<int>& colmap, vector<int>& ptr, vector<int>& col,
+                   vector<double>& val, int& maxrow) {
+    ptr.assign(nrow + 1, 0);
+    col.clear(); val.clear();
+    maxrow = 0;
+    for (int r = 0; r < nrow; ++r) {
+      int d = rowdof(r);
+      for (int k = fptr[d]; k < fptr[d + 1]; ++k) {
+        int c = colmap[fcol[k]];
+        if (c >= 0) { col.push_back(c); val.push_back(fval[k]); }
+      }
+      ptr[r + 1] = (int)col.size();
+      maxrow = std::max(maxrow, ptr[r + 1] - ptr[r]);
+    }
+  };
+  auto orow = [&](int r) { return s.iovsvn[s.operm[r]]; };
+  auto irow = [&](int r) { return s.iivsvn[r]; };
+  build(no, orow, onew, b.oo_ptr, b.oo_col, b.oo_val, b.maxrow_oo);
+  build(no, orow, iidx, b.oi_ptr, b.oi_col, b.oi_val, b.maxrow_oi);
+  build(ni, irow, onew, b.io_ptr, b.io_col, b.io_val, b.maxrow_io);
+  build(ni, irow, iidx, b.ii_ptr, b.ii_col, b.ii_val, b.maxrow_ii);
+  b.w = 0;
+  for (int r = 0; r < no; ++r)
+    for (int k = b.oo_ptr[r]; k < b.oo_ptr[r + 1]; ++k)
+      if (b.oo_col[k] <= r) b.w = std::max(b.w, r / NB - b.oo_col[k] / NB);
+  // reduced-rhs input: weighted rhs, Dirichlet rows zeroed, weighted bc added
+  // (module_dd.f90:7040-7075 and sm_prepare_rhs, module_sm.f90:603-628)
+  vector<double> f = s.rhs;
+  vector<double> bcw = s.bc;
+  if (s.rhs_complete) for (int i = 0; i < ni; ++i) f[s.iivsvn[i]] *= s.wi[i];
+  for (int i = 0; i < ni; ++i) bcw[s.iivsvn[i]] *= s.wi[i];
+  if (s.bc_present)
+    for (int i = 0; i < s.ndof; ++i) { if (s.ifix[i]) f[i] = 0.0; f[i] += bcw[i]; }
+  b.fo.resize(no);
+  for (int q = 0; q < no; ++q) b.fo[q] = f[orow(q)];
+  b.fi.resize(ni);
+  for (int i = 0; i < ni; ++i) b.fi[i] = f[s.iivsvn[i]];
+  double sd = 0.0;
+  int cnt = 0;
+  for (int i = 0; i < ni; ++i)
+    for (int k = b.ii_ptr[i]; k < b.ii_ptr[i + 1]; ++k)
+      if (b.ii_col[k] == i) { sd += std::fabs(b.ii_val[k]); cnt++; }
+  b.rho = cnt ? sd / cnt : 1.0;
+  if (!(b.rho > 0.0)) b.rho = 1.0;
+}
+
+template <typename T>
+static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk);
+
+bool device_setup(Solver& S, Error& err) {
+  Device& D = *S.dev;
+  try {
+    D.release();
+    D.mixed = S.prm.precision != 0;
+    double t0 = wall_time();
+    int nsub = (int)S.subs.size();
+    D.nsub = nsub;
+    vector<SubBlocks> blk(nsub);
+#pragma omp parallel for schedule(dynamic)
+    for (int t = 0; t < nsub; ++t) prepare_blocks(S.subs[t], blk[t]);
+    for (int t = 0; t < nsub; ++t) {
+      auto& b = blk[t];
+      if (b.maxrow_oo > 96 || b.maxrow_oi > 95 || b.maxrow_io > 128 || b.maxrow_ii > 128)
+        throw Error{ERR_UNSUPPORTED, "subdomain matrix rows longer than the staging buffers (96/128 entries)"};
+      if (S.subs[t].nconstr > 119) throw Error{ERR_UNSUPPORTED, "more than 119 constraints on a subdomain"};
+      if (S.subs[t].ndofi == 0) throw Error{ERR_ARGUMENT, "subdomain without interface"};
+    }
+    S.stats.t_host_setup += wall_time() - t0;
+    double t1 = wall_time();
+    if (D.mixed) setup_numeric<float>(S, D, blk);
+    else setup_numeric<double>(S, D, blk);
+    // check device error flags
+    int herr = 0;
+    CK(cudaMemcpyAsync(&herr, D.err, sizeof(int), cudaMemcpyDeviceToHost, D.st));
+    CK(cudaStreamSynchronize(D.st));
+    if (herr) throw Error{ERR_NUMERIC, "non-positive pivot in a subdomain or coarse factorisation (flags " +
+                                            std::to_string(herr) + ")"};
+    S.stats.t_device_setup = wall_time() - t1;
+  } catch (Error& e) {
+    err = e;
+    return false;
+  }
+  return true;
+}
+
+template <typename T>
+static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
+  const int nsub = D.nsub;
+  cudaStream_t st = D.st;
+  auto& own = D.owned;
+  D.nref = D.mixed ? 2 : 0;
+
+  // ---- sizes and offsets
+  D.hs.assign(nsub, DevSub{});
+  long long oT = 0, oS = 0, oPC = 0, oSm = 0;
+  int rep = 0, koo = 0, koi = 0, kio = 0, kii = 0, cptr = 0, coff = 0;
+  D.maxnbo = 0; D.maxw = 0; D.maxNR = 0; D.maxNI = 0; D.maxNO = 0; D.ncpmax = 4;
+  int maxnbi = 0, maxNRC = 0, maxnc = 0;
+  for (int t = 0; t < nsub; ++t) {
+    auto& s = S.subs[t];
+    auto& b = blk[t];
+    DevSub d{};
+    d.no = s.ndofo; d.ni = s.ndofi; d.nc = s.nconstr;
+    d.ncp = roundup(std::max(1, d.nc), 4);
+    d.NO = roundup(d.no, NB); d.NI = roundup(d.ni, NB);
+    d.NR = roundup(d.ni + 1, NB);
+    d.NRC = d.NI + roundup(std::max(1, d.nc), NB);
+    d.nbo = d.NO / NB; d.w = b.w; d.nbi = d.NI / NB; d.nref = D.nref;
+    d.oL = oT; oT += (long long)d.nbo * (d.w + 1) * NB * NB;
+    d.oLinv = oT; oT += (long long)d.nbo * NB * NB;
+    d.oXc = oT; oT += (long long)(d.nref + 1) * d.NO * d.NR;
+    d.oLs = oT; oT += (long long)d.nbi * d.nbi * NB * NB;
+    d.oLsinv = oT; oT += (long long)d.nbi * NB * NB;
+    d.oBs = oT; oT += (long long)d.NI * d.NRC;
+    d.oS = oS; oS += (long long)d.NI * d.NI;
+    d.oZ = oPC; oPC += (long long)d.NI * d.NI;
+    d.oPhi = oPC; oPC += (long long)d.NI * d.ncp;
+    d.oGinv = oSm; oSm += (long long)d.ncp * d.ncp;
+    d.oAc = oSm; oSm += (long long)d.ncp * d.ncp;
+    d.rep = rep; rep += d.NI;
+    d.koo = koo; koo += d.no + 1;
+    d.koi = koi; koi += d.no + 1;
+    d.kio = kio; kio += d.ni + 1;
+    d.kii = kii; kii += d.ni + 1;
+    d.cptr = cptr; cptr += d.nc + 1;
+    d.coff = coff; coff += d.nc;
+    d.rho = b.rho;
+    D.hs[t] = d;
+    D.maxnbo = std::max(D.maxnbo, d.nbo); D.maxw = std::max(D.maxw, d.w);
+    D.maxNR = std::max(D.maxNR, d.NR); D.maxNI = std::max(D.maxNI, d.NI); D.maxNO = std::max(D.maxNO, d.NO);
+    D.ncpmax = std::max(D.ncpmax, d.ncp);
+    maxnbi = std::max(maxnbi, d.nbi); maxNRC = std::max(maxNRC, d.NRC); maxnc = std::max(maxnc, d.nc);
+  }
+  D.nrep = rep;
+  S.stats.bytes_per_iteration = 0;
+  for (auto& d : D.hs)
+    S.stats.bytes_per_iteration += (double)d.NI * d.NI * (D.mixed ? (8.0 + 4.0) : 16.0);
+
+  // ---- allocations
+  D.poolT = dalloc<T>(oT, own);
+  D.poolS = D.mixed ? (void*)dalloc<float2>(oS, own) : (void*)dalloc<double>(oS, own);
+  D.poolPC = dalloc<T>(oPC, own);
+  D.small = dalloc<double>(oSm, own);
+  D.err = dalloc<int>(1, own);
+  CK(cudaMemsetAsync(D.err, 0, sizeof(int), st));
+  CK(cudaMemsetAsync(D.poolT, 0, oT * sizeof(T), st));
+  D.ds = upload(D.hs, own, st);
+
+  // ---- CSR blocks
+  auto concat = [&](auto get_ptr, auto get_col, auto get_val, CsrView& view) {
+    vector<int> ptr, col;
+    vector<double> val;
+    for (int t = 0; t < nsub; ++t) {
+      const vector<int>& p = get_ptr(blk[t]);
+      int base = (int)col.size();
+      for (size_t i = 0; i < p.size(); ++i) ptr.push_back(base + p[i]);
+      const vector<int>& c = get_col(blk[t]);
+      const vector<double>& v = get_val(blk[t]);
+      col.insert(col.end(), c.begin(), c.end());
+      val.insert(val.end(), v.begin(), v.end());
+    }
+    view.ptr = upload(ptr, own, st);
+    view.col = upload(col, own, st);
+    view.val = upload(val, own, st);
+  };
+  concat([](SubBlocks& b) -> vector<int>& { return b.oo_ptr; }, [](SubBlocks& b) -> vector<int>& { return b.oo_col; },
+         [](SubBlocks& b) -> vector<double>& { return b.oo_val; }, D.koo);
+  concat([](SubBlocks& b) -> vector<int>& { return b.oi_ptr; }, [](SubBlocks& b) -> vector<int>& { return b.oi_col; },
+         [](SubBlocks& b) -> vector<double>& { return b.oi_val; }, D.koi);
+  concat([](SubBlocks& b) -> vector<int>& { return b.io_ptr; }, [](SubBlocks& b) -> vector<int>& { return b.io_col; },
+         [](SubBlocks& b) -> vector<double>& { return b.io_val; }, D.kio);
+  concat([](SubBlocks& b) -> vector<int>& { return b.ii_ptr; }, [](SubBlocks& b) -> vector<int>& { return b.ii_col; },
+         [](SubBlocks& b) -> vector<double>& { return b.ii_val; }, D.kii);
+  {
+    vector<int> cp, cc, cm;
+    vector<double> cv;
+    for (int t = 0; t < nsub; ++t) {
+      auto& s = S.subs[t];
+      int base = (int)cc.size();
+      for (int q = 0; q <= s.nconstr; ++q) cp.push_back(base + s.c_ptr[q]);
+      cc.insert(cc.end(), s.c_col.begin(), s.c_col.end());
+      cv.insert(cv.end(), s.c_val.begin(), s.c_val.end());
+      cm.insert(cm.end(), s.indrowc.begin(), s.indrowc.end());
+    }
+    D.c_ptr = upload(cp, own, st);
+    D.c_col = upload(cc, own, st);
+    D.c_val = upload(cv, own, st);
+    D.cmap = upload(cm, own, st);
+  }
+  // ---- interface vectors and owner lists
+  D.n = S.ninterface;
+  {
+    vector<int> uq(D.nrep, 0);
+    vector<double> wr(D.nrep, 0.0), fir(D.nrep, 0.0), fov;
+    vector<long long> fooff(nsub), uooff(nsub);
+    long long fpos = 0;
+    for (int t = 0; t < nsub; ++t) {
+      auto& s = S.subs[t];
+      auto& d = D.hs[t];
+      for (int i = 0; i < s.ndofi; ++i) { uq[d.rep + i] = s.uniq[i]; wr[d.rep + i] = s.wi[i]; fir[d.rep + i] = blk[t].fi[i]; }
+      fooff[t] = fpos;
+      uooff[t] = fpos;
+      fov.insert(fov.end(), blk[t].fo.begin(), blk[t].fo.end());
+      fpos += s.ndofo;
+    }
+    D.uniq = upload(uq, own, st);
+    D.wrep = upload(wr, own, st);
+    D.fi = upload(fir, own, st);
+    D.fo = upload(fov, own, st);
+    D.fo_off = upload(fooff, own, st);
+    D.uo_off = upload(uooff, own, st);
+    D.huo_off = uooff;
+    D.uo = dalloc<double>(fpos, own);
+    vector<int> optr(D.n + 1, 0), orep, osub, oloc;
+    for (int t = 0; t < nsub; ++t) for (int u : S.subs[t].uniq) optr[u + 1]++;
+    for (int u = 0; u < D.n; ++u) optr[u + 1] += optr[u];
+    orep.resize(optr[D.n]); osub.resize(optr[D.n]); oloc.resize(optr[D.n]);
+    vector<int> pos(optr.begin(), optr.end() - 1);
+    for (int t = 0; t < nsub; ++t)
+      for (int i = 0; i < S.subs[t].ndofi; ++i) {
+        int u = S.subs[t].uniq[i];
+        orep[pos[u]] = D.hs[t].rep + i; osub[pos[u]] = t; oloc[pos[u]++] = i;
+      }
+    D.own.ptr = upload(optr, own, st);
+    D.own.rep = upload(orep, own, st);
+    D.own.sub = upload(osub, own, st);
+    D.own.loc = upload(oloc, own, st);
+    D.fixed = upload(S.iface_fixed, own, st);
+    D.wsum = upload(S.iface_wsum, own, st);
+    // coarse dof owners
+    D.ndofc = S.ndofc;
+    vector<int> cptrv(D.ndofc + 1, 0), csub, cloc;
+    for (int t = 0; t < nsub; ++t) for (int q : S.subs[t].indrowc) cptrv[q + 1]++;
+    for (int q = 0; q < D.ndofc; ++q) cptrv[q + 1] += cptrv[q];
+    csub.resize(cptrv[D.ndofc]); cloc.resize(cptrv[D.ndofc]);
+    vector<int> cpos(cptrv.begin(), cptrv.end() - 1);
+    for (int t = 0; t < nsub; ++t)
+      for (int c = 0; c < S.subs[t].nconstr; ++c) {
+        int q = S.subs[t].indrowc[c];
+        csub[cpos[q]] = t; cloc[cpos[q]++] = c;
+      }
+    D.co_ptr = upload(cptrv, own, st);
+    D.co_sub = upload(csub, own, st);
+    D.co_loc = upload(cloc, own, st);
+  }
+  D.x = dalloc<double>(D.n, own); D.r = dalloc<double>(D.n, own); D.p = dalloc<double>(D.n, own);
+  D.ap = dalloc<double>(D.n, own); D.z = dalloc<double>(D.n, own); D.g = dalloc<double>(D.n, own);
+  D.yrep = dalloc<double>(D.nrep, own); D.zrep = dalloc<double>(D.nrep, own); D.grep = dalloc<double>(D.nrep, own);
+  CK(cudaMemsetAsync(D.yrep, 0, D.nrep * sizeof(double), st));
+  CK(cudaMemsetAsync(D.zrep, 0, D.nrep * sizeof(double), st));
+  CK(cudaMemsetAsync(D.grep, 0, D.nrep * sizeof(double), st));
+  D.nrb = (D.maxNI + AROWS - 1) / AROWS;
+  D.rcpart = dalloc<double>((size_t)nsub * D.nrb * D.ncpmax, own);
+  CK(cudaMemsetAsync(D.rcpart, 0, (size_t)nsub * D.nrb * D.ncpmax * sizeof(double), st));
+  D.rc = dalloc<double>(std::max(1, D.ndofc), own);
+  D.uc = dalloc<double>(std::max(1, D.ndofc), own);
+  D.npart = std::min(MAXPART, std::max(1, (D.n + RT - 1) / RT));
+  D.part = dalloc<double>(MAXPART, own);
+  D.ctl = dalloc<PcgCtl>(1, own);
+  D.scal = dalloc<double>(4, own);
+
+  T* poolT = static_cast<T*>(D.poolT);
+  T* poolPC = static_cast<T*>(D.poolPC);
+  if (D.mixed)
+    CK(cudaFuncSetAttribute(k_schur_apply_df, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)(D.maxNI * sizeof(float2))));
+  else
+    CK(cudaFuncSetAttribute(k_schur_apply_f64, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)(D.maxNI * sizeof(double))));
+  CK(cudaFuncSetAttribute(k_pc_local<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(D.maxNI * sizeof(T))));
+
+  // ---- interior band factor
+  D.hbd_oo.resize(nsub);
+  for (int t = 0; t < nsub; ++t) {
+    auto& d = D.hs[t];
+    D.hbd_oo[t] = BandDesc{d.nbo, d.w, d.NR, 0, d.oL, d.oLinv, d.oXc};
+  }
+  D.bd_oo = upload(D.hbd_oo, own, st);
+  k_fill_band<T><<<dim3((D.maxNO + 127) / 128, nsub), 128, 0, st>>>(D.ds, D.koo, poolT, D.bd_oo);
+  CKL();
+  run_factor<T>(D, D.bd_oo, nsub, D.maxnbo, D.maxw, poolT);
+  // ---- interior solves [X | v] = A_oo^-1 [A_oi | f_o], refined in mixed precision
+  k_fill_rhs<T><<<dim3((D.maxNO + 127) / 128, nsub), 128, 0, st>>>(D.ds, D.koi, D.fo, D.fo_off, poolT);
+  CKL();
+  run_solve<T>(D, D.bd_oo, nsub, D.maxnbo, D.maxNR, poolT, poolT);
+  for (int rr = 1; rr <= D.nref; ++rr) {
+    k_residual_df<<<dim3(D.maxNO, nsub), 128, 0, st>>>(D.ds, D.koo, D.koi, D.fo, D.fo_off,
+                                                       reinterpret_cast<float*>(poolT), rr);
+    CKL();
+    vector<BandDesc> hb = D.hbd_oo;
+    for (int t = 0; t < nsub; ++t) hb[t].oB = D.hs[t].oXc + (long long)rr * D.hs[t].NO * D.hs[t].NR;
+    BandDesc* bdr = upload(hb, own, st);
+    run_solve<T>(D, bdr, nsub, D.maxnbo, D.maxNR, poolT, poolT);
+  }
+  // ---- Schur complements and the subdomain reduced rhs
+  if (D.mixed) {
+    k_schur_df<<<dim3(D.maxNI, nsub), 128, 0, st>>>(D.ds, D.kio, D.kii, reinterpret_cast<const float*>(poolT),
+                                                    static_cast<float2*>(D.poolS), D.fi, D.grep);
+    CKL();
+    k_symmetrize_df<<<dim3(D.maxNI / 16, D.maxNI / 16, nsub), dim3(16, 16), 0, st>>>(D.ds,
+                                                                                     static_cast<float2*>(D.poolS));
+    CKL();
+  } else {
+    k_schur_f64<<<dim3(D.maxNI, nsub), 128, 0, st>>>(D.ds, D.kio, D.kii, reinterpret_cast<const double*>(poolT),
+                                                     static_cast<double*>(D.poolS), D.fi, D.grep);
+    CKL();
+    k_symmetrize_f64<<<dim3(D.maxNI / 16, D.maxNI / 16, nsub), dim3(16, 16), 0, st>>>(D.ds,
+                                                                                      static_cast<double*>(D.poolS));
+    CKL();
+  }
+  // ---- preconditioner blocks: Srho factor, [Srho^-1 | Y], G^-1, Phi, Z, local coarse matrices
+  vector<BandDesc> hbs(nsub);
+  for (int t = 0; t < nsub; ++t) {
+    auto& d = D.hs[t];
+    hbs[t] = BandDesc{d.nbi, d.nbi - 1, d.NRC, 0, d.oLs, d.oLsinv, d.oBs};
+  }
+  BandDesc* bd_s = upload(hbs, own, st);
+  if constexpr (std::is_same_v<T, float>)
+    k_fill_srho<T, float2><<<dim3(D.maxNI / 16, D.maxNI / 16, nsub), dim3(16, 16), 0, st>>>(
+        D.ds, static_cast<const float2*>(D.poolS), poolT, bd_s);
+  else
+    k_fill_srho<T, double><<<dim3(D.maxNI / 16, D.maxNI / 16, nsub), dim3(16, 16), 0, st>>>(
+        D.ds, reinterpret_cast<const double*>(D.poolS), poolT, bd_s);
+  CKL();
+  if (maxnc > 0) {
+    k_add_penalty<T><<<dim3(maxnc, nsub), 256, 0, st>>>(D.ds, D.c_ptr, D.c_col, D.c_val, poolT, bd_s);
+    CKL();
+  }
+  run_factor<T>(D, bd_s, nsub, maxnbi, maxnbi - 1, poolT);
+  k_fill_rhs_srho<T><<<dim3((D.maxNI + 127) / 128, nsub), 128, 0, st>>>(D.ds, D.c_ptr, D.c_col, D.c_val, poolT);
+  CKL();
+  run_solve<T>(D, bd_s, nsub, maxnbi, maxNRC, poolT, poolT);
+  {
+    size_t smem = 2 * (size_t)std::max(1, maxnc) * std::max(1, maxnc) * sizeof(double);
+    CK(cudaFuncSetAttribute(k_small_g<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_small_g<T><<<nsub, 256, smem, st>>>(D.ds, D.c_ptr, D.c_col, D.c_val, poolT, D.small, D.err);
+    CKL();
+  }
+  k_phi<T><<<dim3((D.maxNI * D.ncpmax + 255) / 256, nsub), 256, 0, st>>>(D.ds, poolT, D.small, poolPC);
+  CKL();
+  k_z<T><<<dim3(D.maxNI / 16, D.maxNI / 16, nsub), dim3(16, 16), 0, st>>>(D.ds, poolT, poolPC);
+  CKL();
+  k_symmetrize_t<T><<<dim3(D.maxNI / 16, D.maxNI / 16, nsub), dim3(16, 16), 0, st>>>(D.ds, poolPC);
+  CKL();
+  if constexpr (std::is_same_v<T, float>)
+    k_sphi<T, float2><<<dim3(D.maxNI, nsub), 64, 0, st>>>(D.ds, static_cast<const float2*>(D.poolS), poolPC, poolT);
+  else
+    k_sphi<T, double><<<dim3(D.maxNI, nsub), 64, 0, st>>>(D.ds, reinterpret_cast<const double*>(D.poolS), poolPC,
+                                                          poolT);
+  CKL();
+  k_ac<T><<<dim3((maxnc * maxnc + 255) / 256 + 1, nsub), 256, 0, st>>>(D.ds, poolT, poolPC, D.small);
+  CKL();
+
+  // ---- coarse problem: assemble on the host, dense FP64 factor and inverse on the device
+  // (levels_prepare_last_level, module_levels.f90:3001-3170)
+  {
+    vector<double> hsm(oSm);
+    CK(cudaMemcpyAsync(hsm.data(), D.small, oSm * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    int nc_g = D.ndofc;
+    int nbc = std::max(1, (nc_g + NB - 1) / NB);
+    D.ldc = nbc * NB;
+    vector<double> A((size_t)D.ldc * D.ldc, 0.0);
+    for (int t = 0; t < nsub; ++t) {
+      auto& s = S.subs[t];
+      auto& d = D.hs[t];
+      for (int a = 0; a < d.nc; ++a)
+        for (int b2 = 0; b2 < d.nc; ++b2)
+          A[(size_t)s.indrowc[a] * D.ldc + s.indrowc[b2]] += hsm[d.oAc + (size_t)a * d.ncp + b2];
+    }
+    for (int q = nc_g; q < D.ldc; ++q) A[(size_t)q * D.ldc + q] = 1.0;
+    // block layout: nbc x nbc lower blocks, then inverted diagonal blocks, then the identity RHS
+    BandDesc cb{nbc, nbc - 1, D.ldc, 0, 0, (long long)nbc * nbc * NB * NB,
+                (long long)nbc * nbc * NB * NB + (long long)nbc * NB * NB};
+    size_t csize = (size_t)cb.oB + (size_t)D.ldc * D.ldc;
+    vector<double> hc(csize, 0.0);
+    for (int i = 0; i < D.ldc; ++i)
+      for (int j = 0; j <= i; ++j) {
+        double v = 0.5 * (A[(size_t)i * D.ldc + j] + A[(size_t)j * D.ldc + i]);
+        hc[band_block(cb, i / NB, j / NB) + (i % NB) * NB + j % NB] = v;
+      }
+    for (int i = 0; i < D.ldc; ++i) hc[cb.oB + (size_t)i * D.ldc + i] = 1.0;
+    D.cpool = upload(hc, own, st);
+    vector<BandDesc> hcb{cb};
+    BandDesc* dcb = upload(hcb, own, st);
+    run_factor<double>(D, dcb, 1, nbc, nbc - 1, D.cpool);
+    run_solve<double>(D, dcb, 1, nbc, D.ldc, D.cpool, D.cpool);
+    D.ainv = D.cpool + cb.oB;
+  }
+  // ---- assembled reduced rhs (module_dd.f90:7090-7135)
+  k_assemble_plain<<<(D.n + 255) / 256, 256, 0, st>>>(D.n, D.own, D.grep, nullptr, D.g);
+  CKL();
+  CK(cudaStreamSynchronize(st));
+}
+
+// ------------------------------------------------------------ PCG driver
+template <typename T>
+static void launch_schur(Device& D, const double* vin, double* vout, bool zero_fixed, const PcgCtl* ctl,
+                         const double* dotvec) {
+  dim3 grid(D.nrb, D.nsub);
+  if (D.mixed) {
+    size_t smem = (size_t)D.maxNI * sizeof(float2);
+    k_schur_apply_df<<<grid, AT, smem, D.st>>>(D.ds, static_cast<const float2*>(D.poolS), vin, D.uniq, D.yrep, ctl);
+  } else {
+    size_t smem = (size_t)D.maxNI * sizeof(double);
+    k_schur_apply_f64<<<grid, AT, smem, D.st>>>(D.ds, static_cast<const double*>(D.poolS), vin, D.uniq, D.yrep, ctl);
+  }
+  CKL();
+  k_assemble_dot<<<D.npart, RT, 0, D.st>>>(D.n, D.own, D.yrep, D.fixed, D.wsum, dotvec, vout, D.part, ctl,
+                                           zero_fixed ? 1 : 0);
+  CKL();
+}
+
+template <typename T>
+static void launch_pc(Device& D, const double* rin, double* zout, const PcgCtl* ctl) {
+  dim3 grid(D.nrb, D.nsub);
+  size_t smem = (size_t)D.maxNI * sizeof(T);
+  k_pc_local<T><<<grid, AT, smem, D.st>>>(D.ds, static_cast<const T*>(D.poolPC), rin, D.uniq, D.wrep, D.zrep,
+                                          D.rcpart, D.nrb, D.ncpmax, ctl);
+  CKL();
+  if (D.ndofc > 0) {
+    k_coarse_gather<<<(D.ndofc + 255) / 256, 256, 0, D.st>>>(D.ndofc, D.co_ptr, D.co_sub, D.co_loc, D.ds, D.rcpart,
+                                                           D.nrb, D.ncpmax, D.rc, ctl);
+    CKL();
+    k_coarse_solve<<<(D.ndofc + 7) / 8, 256, 0, D.st>>>(D.ndofc, D.ldc, D.ainv, D.rc, D.uc, ctl);
+    CKL();
+  }
+  k_assemble_z<T><<<D.npart, RT, 0, D.st>>>(D.n, D.own, D.ds, static_cast<const T*>(D.poolPC), D.zrep, D.wrep,
+                                            D.cmap, D.uc, D.wsum, rin, zout, D.part, ctl);
+  CKL();
+}
+
+static double host_sum_parts(Device& D) {
+  k_sum_parts<<<1, RT, 0, D.st>>>(D.part, D.npart, D.scal);
+  double v = 0.0;
+  CK(cudaMemcpyAsync(&v, D.scal, sizeof(double), cudaMemcpyDeviceToHost, D.st));
+  CK(cudaStreamSynchronize(D.st));
+  return v;
+}
+
+// largest eigenvalue of the Lanczos tridiagonal matrix by Sturm bisection
+// (stands in for LAPACK DSTEV in krylov_condsparse, module_krylov.f90:2061-2118)
+static double lanczos_max_eig(const vector<double>& d, const vector<double>& e) {
+  int n = (int)d.size();
+  if (n <= 1) return 1.0;
+  double lo = 1e300, hi = -1e300;
+  for (int i = 0; i < n; ++i) {
+    double rr = (i > 0 ? std::fabs(e[i - 1]) : 0.0) + (i < n - 1 ? std::fabs(e[i]) : 0.0);
+    lo = std::min(lo, d[i] - rr);
+    hi = std::max(hi, d[i] + rr);
+  }
+  auto below = [&](double xv) {
+    int cnt = 0;
+    double q = 1.0;
+    for (int i = 0; i < n; ++i) {
+      q = d[i] - xv - (i > 0 ? e[i - 1] * e[i - 1] / q : 0.0);
+      if (q == 0.0) q = -1e-300;
+      if (q < 0) cnt++;
+    }
+    return cnt;
+  };
+  for (int it = 0; it < 200 && hi - lo > 1e-15 * std::max(1.0, std::fabs(hi)); ++it) {
+    double mid = 0.5 * (lo + hi);
+    if (below(mid) >= n) hi = mid; else lo = mid;
+  }
+  return 0.5 * (lo + hi);
+}
+
+template <typename T>
+static bool solve_impl(Solver& S, double tol, int maxit, int ndecrmax, int& num_iter, int& reason, double& cond) {
+  Device& D = *S.dev;
+  cudaStream_t st = D.st;
+  auto& own = D.owned;
+  double t0 = wall_time();
+  if (maxit + 2 > D.maxit_alloc) {
+    D.maxit_alloc = maxit + 2;
+    D.hist = dalloc<double>(D.maxit_alloc, own);
+    D.diag = dalloc<double>(D.maxit_alloc, own);
+    D.subdiag = dalloc<double>(D.maxit_alloc, own);
+  }
+  CK(cudaMemsetAsync(D.diag, 0, D.maxit_alloc * sizeof(double), st));
+  CK(cudaMemsetAsync(D.subdiag, 0, D.maxit_alloc * sizeof(double), st));
+  // initial guess restricted to the interface with Dirichlet values (module_levels.f90:4374-4440)
+  {
+    vector<double> x0(D.n, 0.0);
+    vector<char> seen(D.n, 0);
+    for (auto& s : S.subs)
+      for (int i = 0; i < s.ndofi; ++i) {
+        int u = s.uniq[i];
+        if (seen[u]) continue;
+        seen[u] = 1;
+        int d = s.iivsvn[i];
+        x0[u] = (s.bc_present && s.ifix[d]) ? s.fixv[d] : s.sol[d];
+      }
+    CK(cudaMemcpyAsync(D.x, x0.data(), D.n * sizeof(double), cudaMemcpyHostToDevice, st));
+    CK(cudaStreamSynchronize(st));
+  }
+  // r = g with fixed interface dofs zeroed (module_krylov.f90:222-236)
+  k_assemble_plain<<<(D.n + 255) / 256, 256, 0, st>>>(D.n, D.own, D.grep, D.fixed, D.r);
+  CKL();
+  k_dot<<<D.npart, RT, 0, st>>>(D.n, D.r, D.r, D.wsum, D.part);
+  double normrhs2 = host_sum_parts(D);
+  num_iter = 0; reason = 0; cond = 1.0;
+  S.relres_history.clear();
+  bool postprocess = true;
+  if (normrhs2 == 0.0) {
+    postprocess = false;
+  } else {
+    launch_schur<T>(D, D.x, D.ap, true, nullptr, nullptr);
+    k_axpy<<<(D.n + 255) / 256, 256, 0, st>>>(D.n, -1.0, D.ap, D.r);
+    CKL();
+    k_dot<<<D.npart, RT, 0, st>>>(D.n, D.r, D.r, D.wsum, D.part);
+    double normres0 = std::sqrt(host_sum_parts(D));
+    if (normres0 == 0.0) {
+      postprocess = false;
+    } else {
+      launch_pc<T>(D, D.r, D.p, nullptr);
+      double rmp = host_sum_parts(D);
+      PcgCtl c{};
+      c.rmp = rmp; c.normres0 = normres0; c.tol = tol; c.lastres = 1.0;
+      c.iter = 1; c.maxit = maxit; c.ndecrmax = ndecrmax;
+      CK(cudaMemcpyAsync(D.ctl, &c, sizeof(PcgCtl), cudaMemcpyHostToDevice, st));
+      double tl = wall_time();
+      const int chunk = 4;
+      int launched = 0;
+      while (true) {
+        for (int q = 0; q < chunk; ++q) {
+          launch_schur<T>(D, D.p, D.ap, false, D.ctl, D.p);
+          k_sc_alpha<<<1, RT, 0, st>>>(D.ctl, D.part, D.npart);
+          k_update_xr<<<D.npart, RT, 0, st>>>(D.n, D.ctl, D.x, D.r, D.p, D.ap, D.wsum, D.part);
+          k_sc_res<<<1, RT, 0, st>>>(D.ctl, D.part, D.npart, D.hist);
+          launch_pc<T>(D, D.r, D.z, D.ctl);
+          k_sc_beta<<<1, RT, 0, st>>>(D.ctl, D.part, D.npart, D.diag, D.subdiag);
+          k_update_p<<<D.npart, RT, 0, st>>>(D.n, D.ctl, D.p, D.z);
+          CKL();
+        }
+        launched += chunk;
+        CK(cudaMemcpyAsync(D.hctl, D.ctl, sizeof(PcgCtl), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (D.hctl->done || launched > maxit + chunk) break;
+      }
+      S.stats.t_iterations = wall_time() - tl;
+      PcgCtl c2 = *D.hctl;
+      num_iter = c2.num_iter;
+      reason = c2.reason;
+      S.relres_history.resize(num_iter);
+      if (num_iter > 0)
+        CK(cudaMemcpy(S.relres_history.data(), D.hist, num_iter * sizeof(double), cudaMemcpyDeviceToHost));
+      int nw = c2.nw;
+      if (nw > 1) {
+        vector<double> dg(nw), sd(nw);
+        CK(cudaMemcpy(dg.data(), D.diag, nw * sizeof(double), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(sd.data(), D.subdiag, nw * sizeof(double), cudaMemcpyDeviceToHost));
+        sd.resize(nw - 1);
+        cond = lanczos_max_eig(dg, sd);
+      } else {
+        cond = 1.0;
+      }
+    }
+  }
+  // interior values (module_levels.f90:4510-4576)
+  double tp = wall_time();
+  if (postprocess) {
+    if (D.mixed)
+      k_post_df<<<dim3((D.maxNO + 7) / 8, D.nsub), 256, 0, st>>>(D.ds, static_cast<const float*>(D.poolT), D.x, D.uniq,
+                                                                 D.uo, D.uo_off);
+    else
+      k_post_f64<<<dim3((D.maxNO + 7) / 8, D.nsub), 256, 0, st>>>(D.ds, static_cast<const double*>(D.poolT), D.x,
+                                                                  D.uniq, D.uo, D.uo_off);
+    CKL();
+    // pull the solution into the subdomain arrays (dd_upload_solution semantics)
+    vector<double> hx(D.n);
+    size_t nuo = 0;
+    for (auto& s : S.subs) nuo += s.ndofo;
+    vector<double> huo(nuo);
+    CK(cudaMemcpyAsync(hx.data(), D.x, D.n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(huo.data(), D.uo, nuo * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    for (int t = 0; t < D.nsub; ++t) {
+      auto& s = S.subs[t];
+      vector<double> u(s.ndof, 0.0);
+      for (int q = 0; q < s.ndofo; ++q) u[s.iovsvn[s.operm[q]]] = huo[D.huo_off[t] + q];
+      for (int i = 0; i < s.ndofi; ++i) u[s.iivsvn[i]] = hx[s.uniq[i]];
+      s.sol = u;
+    }
+  }
+  S.stats.t_postprocess = wall_time() - tp;
+  S.stats.t_solve = wall_time() - t0;
+  S.stats.num_iter = num_iter;
+  return true;
+}
+
+bool device_solve(Solver& S, double tol, int maxit, int ndecrmax, int& num_iter, int& reason, double& cond,
+                  Error& err) {
+  try {
+    if (S.dev->mixed) return solve_impl<float>(S, tol, maxit, ndecrmax, num_iter, reason, cond);
+    return solve_impl<double>(S, tol, maxit, ndecrmax, num_iter, reason, cond);
+  } catch (Error& e) {
+    err = e;
+    return false;
+  }
+}
+
+}  // namespace bddc

@@ -1,0 +1,655 @@
+// Host part of the BDDC setup: the integer and geometric work that decides
+// the coarse space, plus Dirichlet elimination and interface weights.
+//
+// All subdomains are in this process, so sharing information comes from one
+// global node -> subdomains table instead of the neighbour exchanges the
+// reference performs over MPI.  The decisions themselves follow the reference
+// rule by rule because they fix the coarse space, and with it the iteration
+// count:
+//   interface = nodes shared with another subdomain ........ module_dd.f90:8360-8470
+//   glob classification by sharing signature ............... module_dd.f90:9210-9276
+//   corner selection on faces (farthest / largest area) .... module_dd.f90:10017-10327
+//   corner union over neighbours ........................... module_dd.f90:9296-9385
+//   edges and faces, Dirichlet node removal ................ module_dd.f90:9387-9587
+//   coarse numbering, owner = lowest subdomain index ....... module_dd.f90:10329-10555
+//   arithmetic constraints (unscaled sums) ................. module_dd.f90:4298-4384
+//   coarse dof numbering ................................... module_dd.f90:11011-11235
+//   Dirichlet elimination .................................. module_sm.f90:431-600, module_dd.f90:1081-1256
+//   weights rho_i / sum rho ................................ module_dd.f90:11554-11722
+#include <algorithm>
+#include <array>
+#include <chrono>
+#include <cmath>
+#include <map>
+#include <numeric>
+#include <stdexcept>
+#include <functional>
+#include <unordered_map>
+
+#include "bddc_internal.hpp"
+
+namespace bddc {
+
+double wall_time() {
+  using namespace std::chrono;
+  return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+// sort + merge duplicate (i,j) entries (the effect of sm_assembly, module_sm.f90:630-684)
+void host_assemble_upper(vector<int>& ia, vector<int>& ja, vector<double>& a) {
+  size_t n = ia.size();
+  vector<uint64_t> key(n);
+  for (size_t k = 0; k < n; ++k) key[k] = ((uint64_t)(uint32_t)ia[k] << 32) | (uint32_t)ja[k];
+  vector<uint32_t> p(n);
+  std::iota(p.begin(), p.end(), 0u);
+  std::stable_sort(p.begin(), p.end(), [&](uint32_t x, uint32_t y) { return key[x] < key[y]; });
+  vector<int> ni, nj;
+  vector<double> na;
+  ni.reserve(n); nj.reserve(n); na.reserve(n);
+  for (size_t q = 0; q < n; ++q) {
+    uint32_t k = p[q];
+    if (!ni.empty() && ni.back() == ia[k] && nj.back() == ja[k]) na.back() += a[k];
+    else { ni.push_back(ia[k]); nj.push_back(ja[k]); na.push_back(a[k]); }
+  }
+  ia.swap(ni); ja.swap(nj); a.swap(na);
+}
+
+// components of the dual mesh graph: elements are connected when they share
+// at least `neighbouring` nodes; a node takes the component of the last
+// element that contains it (module_dd.f90:2680-2720)
+void host_nodal_components(Subdomain& s) {
+  s.comp.assign(s.nnod, 1);
+  if (!s.find_components || s.nelem == 0) return;
+  vector<int> kinet(s.nelem + 1, 0);
+  for (int e = 0; e < s.nelem; ++e) kinet[e + 1] = kinet[e] + s.nnet[e];
+  vector<int> nptr(s.nnod + 1, 0);
+  for (int k = 0; k < kinet[s.nelem]; ++k) nptr[s.inet[k] + 1]++;
+  for (int i = 0; i < s.nnod; ++i) nptr[i + 1] += nptr[i];
+  vector<int> nel(nptr[s.nnod]);
+  {
+    vector<int> pos(nptr.begin(), nptr.end() - 1);
+    for (int e = 0; e < s.nelem; ++e)
+      for (int k = kinet[e]; k < kinet[e + 1]; ++k) nel[pos[s.inet[k]]++] = e;
+  }
+  int thr = s.dual_graph ? std::max(1, s.neighbouring) : 1;
+  vector<int> ec(s.nelem, 0), cnt(s.nelem, 0), touched, stack;
+  int nc = 0;
+  for (int e0 = 0; e0 < s.nelem; ++e0) {
+    if (ec[e0]) continue;
+    ec[e0] = ++nc;
+    stack.assign(1, e0);
+    while (!stack.empty()) {
+      int e = stack.back();
+      stack.pop_back();
+      touched.clear();
+      for (int k = kinet[e]; k < kinet[e + 1]; ++k)
+        for (int q = nptr[s.inet[k]]; q < nptr[s.inet[k] + 1]; ++q) {
+          int f = nel[q];
+          if (f != e && cnt[f]++ == 0) touched.push_back(f);
+        }
+      for (int f : touched) {
+        if (cnt[f] >= thr && !ec[f]) { ec[f] = nc; stack.push_back(f); }
+        cnt[f] = 0;
+      }
+    }
+  }
+  for (int e = 0; e < s.nelem; ++e)
+    for (int k = kinet[e]; k < kinet[e + 1]; ++k) s.comp[s.inet[k]] = ec[e];
+}
+
+void full_symmetric_csr(const Subdomain& s, vector<int>& ptr, vector<int>& col, vector<double>& val) {
+  int n = s.ndof;
+  ptr.assign(n + 1, 0);
+  for (size_t k = 0; k < s.ia.size(); ++k) {
+    ptr[s.ia[k] + 1]++;
+    if (s.ia[k] != s.ja[k]) ptr[s.ja[k] + 1]++;
+  }
+  for (int i = 0; i < n; ++i) ptr[i + 1] += ptr[i];
+  col.assign(ptr[n], 0);
+  val.assign(ptr[n], 0.0);
+  vector<int> pos(ptr.begin(), ptr.end() - 1);
+  for (size_t k = 0; k < s.ia.size(); ++k) {
+    int i = s.ia[k], j = s.ja[k];
+    col[pos[i]] = j; val[pos[i]++] = s.a[k];
+    if (i != j) { col[pos[j]] = i; val[pos[j]++] = s.a[k]; }
+  }
+  // rows sorted by column
+  for (int i = 0; i < n; ++i) {
+    vector<std::pair<int, double>> r;
+    for (int k = ptr[i]; k < ptr[i + 1]; ++k) r.emplace_back(col[k], val[k]);
+    std::sort(r.begin(), r.end(), [](auto& x, auto& y) { return x.first < y.first; });
+    for (int k = ptr[i]; k < ptr[i + 1]; ++k) { col[k] = r[k - ptr[i]].first; val[k] = r[k - ptr[i]].second; }
+  }
+}
+
+// Interior ordering for the band factor: natural order or reverse
+// Cuthill-McKee, whichever has the smaller half bandwidth.
+void host_interior_ordering(Subdomain& s, const vector<int>& f_ptr, const vector<int>& f_col) {
+  int no = s.ndofo;
+  vector<int> mo(s.ndof, -1);
+  for (int i = 0; i < no; ++i) mo[s.iovsvn[i]] = i;
+  vector<vector<int>> g(no);
+  for (int i = 0; i < no; ++i) {
+    int r = s.iovsvn[i];
+    for (int k = f_ptr[r]; k < f_ptr[r + 1]; ++k) {
+      int c = mo[f_col[k]];
+      if (c >= 0 && c != i) g[i].push_back(c);
+    }
+  }
+  auto bandwidth = [&](const vector<int>& perm) {
+    vector<int> inv(no);
+    for (int i = 0; i < no; ++i) inv[perm[i]] = i;
+    int b = 0;
+    for (int i = 0; i < no; ++i)
+      for (int c : g[i]) b = std::max(b, std::abs(inv[i] - inv[c]));
+    return b;
+  };
+  vector<int> natural(no);
+  std::iota(natural.begin(), natural.end(), 0);
+  int bn = bandwidth(natural);
+  // reverse Cuthill-McKee from a minimum-degree start node
+  vector<int> rcm;
+  rcm.reserve(no);
+  vector<char> seen(no, 0);
+  for (int st = 0; st < no; ++st) {
+    if (seen[st]) continue;
+    int start = st, mind = (int)g[st].size();
+    // choose a low-degree node of this component as the root
+    {
+      vector<int> comp{st};
+      vector<char> vis(no, 0);
+      vis[st] = 1;
+      for (size_t q = 0; q < comp.size(); ++q)
+        for (int c : g[comp[q]]) if (!vis[c] && !seen[c]) { vis[c] = 1; comp.push_back(c); }
+      for (int v : comp) if ((int)g[v].size() < mind) { mind = (int)g[v].size(); start = v; }
+    }
+    size_t head = rcm.size();
+    rcm.push_back(start);
+    seen[start] = 1;
+    while (head < rcm.size()) {
+      int v = rcm[head++];
+      vector<int> nb;
+      for (int c : g[v]) if (!seen[c]) { seen[c] = 1; nb.push_back(c); }
+      std::sort(nb.begin(), nb.end(), [&](int x, int y) { return g[x].size() < g[y].size(); });
+      rcm.insert(rcm.end(), nb.begin(), nb.end());
+    }
+  }
+  std::reverse(rcm.begin(), rcm.end());
+  int br = no ? bandwidth(rcm) : 0;
+  if (br < bn) { s.operm = rcm; s.band = br; }
+  else { s.operm = natural; s.band = bn; }
+}
+
+namespace {
+
+// global node -> list of (subdomain, local node) in ascending subdomain order
+struct Sharing {
+  vector<int> ptr;       // size nnod_global + 1
+  vector<int> sub, loc;  // entries
+  int count(int g) const { return ptr[g + 1] - ptr[g]; }
+};
+
+Sharing build_sharing(const Solver& S, int nnod_global) {
+  Sharing sh;
+  sh.ptr.assign(nnod_global + 1, 0);
+  for (auto& s : S.subs)
+    for (int g : s.isngn) sh.ptr[g + 1]++;
+  for (int g = 0; g < nnod_global; ++g) sh.ptr[g + 1] += sh.ptr[g];
+  sh.sub.resize(sh.ptr[nnod_global]);
+  sh.loc.resize(sh.ptr[nnod_global]);
+  vector<int> pos(sh.ptr.begin(), sh.ptr.end() - 1);
+  for (int t = 0; t < (int)S.subs.size(); ++t) {
+    auto& s = S.subs[t];
+    for (int i = 0; i < s.nnod; ++i) {
+      int g = s.isngn[i];
+      sh.sub[pos[g]] = t;
+      sh.loc[pos[g]++] = i;
+    }
+  }
+  return sh;
+}
+
+// sharing signature of a node as seen from subdomain t: for every other
+// subdomain holding the node (ascending), its index, its component of the node
+// and t's own component (module_dd.f90:9160-9175 globsubs)
+using Sig = vector<std::array<int, 3>>;
+
+Sig signature(const Solver& S, const Sharing& sh, int t, int g) {
+  Sig sig;
+  int mycomp = 0;
+  for (int q = sh.ptr[g]; q < sh.ptr[g + 1]; ++q)
+    if (sh.sub[q] == t) mycomp = S.subs[t].comp[sh.loc[q]];
+  for (int q = sh.ptr[g]; q < sh.ptr[g + 1]; ++q) {
+    int u = sh.sub[q];
+    if (u == t) continue;
+    sig.push_back({u, S.subs[u].comp[sh.loc[q]], mycomp});
+  }
+  return sig;
+}
+
+struct SigHash {
+  size_t operator()(const Sig& s) const {
+    size_t h = s.size();
+    for (auto& a : s) h = h * 1000003u ^ (size_t)(a[0] * 31 + a[1] * 7 + a[2]);
+    return h;
+  }
+};
+
+}  // namespace
+
+void host_setup(Solver& S) {
+  int nsub = (int)S.subs.size();
+  for (int t = 0; t < nsub; ++t)
+    if (!S.subs[t].loaded) throw Error{ERR_ARGUMENT, "subdomain " + std::to_string(t) + " was not uploaded"};
+  int nnod_global = 0, ndof_global = 0;
+  for (auto& s : S.subs) {
+    for (int g : s.isngn) nnod_global = std::max(nnod_global, g + 1);
+    for (int g : s.isvgvn) ndof_global = std::max(ndof_global, g + 1);
+  }
+
+  // ---- Dirichlet elimination on each subdomain matrix (module_sm.f90:431-600)
+  for (auto& s : S.subs) {
+    s.bc.assign(s.ndof, 0.0);
+    s.bc_present = false;
+    for (int i = 0; i < s.ndof; ++i) if (s.ifix[i] != 0) s.bc_present = true;
+    if (!s.bc_present) continue;
+    vector<char> diag_fixed(s.ndof, 0);
+    for (size_t k = 0; k < s.ia.size(); ++k) {
+      int i = s.ia[k], j = s.ja[k];
+      if (i != j) {
+        if (s.ifix[i] && s.fixv[i] != 0.0 && s.a[k] != 0.0 && !s.ifix[j]) s.bc[j] -= s.a[k] * s.fixv[i];
+        if (s.ifix[j] && s.fixv[j] != 0.0 && s.a[k] != 0.0 && !s.ifix[i]) s.bc[i] -= s.a[k] * s.fixv[j];
+        if (s.ifix[i] || s.ifix[j]) s.a[k] = 0.0;
+      } else if (s.ifix[i]) {
+        if (std::fabs(s.a[k]) < 1e-16) s.a[k] = 1.0;
+        if (s.fixv[i] != 0.0) s.bc[i] += s.a[k] * s.fixv[i];
+        diag_fixed[i] = 1;
+      }
+    }
+    for (int i = 0; i < s.ndof; ++i)
+      if (s.ifix[i] > 0 && !diag_fixed[i]) {
+        s.ia.push_back(i); s.ja.push_back(i); s.a.push_back(1.0);
+        s.bc[i] += s.fixv[i];
+      }
+    host_assemble_upper(s.ia, s.ja, s.a);
+  }
+
+  // ---- interface and neighbours
+  Sharing sh = build_sharing(S, nnod_global);
+  for (int t = 0; t < nsub; ++t) {
+    auto& s = S.subs[t];
+    s.kdof.assign(s.nnod, 0);
+    for (int i = 1; i < s.nnod; ++i) s.kdof[i] = s.kdof[i - 1] + s.nndf[i - 1];
+    s.iin.clear(); s.iivsvn.clear(); s.iovsvn.clear();
+    std::vector<char> isadj(nsub, 0);
+    for (int i = 0; i < s.nnod; ++i) {
+      int g = s.isngn[i];
+      if (sh.count(g) > 1) {
+        s.iin.push_back(i);
+        for (int d = 0; d < s.nndf[i]; ++d) s.iivsvn.push_back(s.kdof[i] + d);
+        for (int q = sh.ptr[g]; q < sh.ptr[g + 1]; ++q) if (sh.sub[q] != t) isadj[sh.sub[q]] = 1;
+      } else {
+        for (int d = 0; d < s.nndf[i]; ++d) s.iovsvn.push_back(s.kdof[i] + d);
+      }
+    }
+    s.nnodi = (int)s.iin.size();
+    s.ndofi = (int)s.iivsvn.size();
+    s.ndofo = (int)s.iovsvn.size();
+    s.kdofi.assign(s.nnodi + 1, 0);
+    for (int i = 0; i < s.nnodi; ++i) s.kdofi[i + 1] = s.kdofi[i] + s.nndf[s.iin[i]];
+    s.adj.clear();
+    for (int u = 0; u < nsub; ++u) if (isadj[u]) s.adj.push_back(u);
+  }
+
+  // ---- pass 1: glob classification and corner selection, per subdomain
+  vector<char> corner_node(nnod_global, 0);  // union of all subdomains' corner choices
+  int meshdim = S.subs.empty() ? 3 : S.subs[0].ndim;
+  for (int t = 0; t < nsub; ++t) {
+    auto& s = S.subs[t];
+    int nnodi = s.nnodi;
+    vector<Sig> sig(nnodi);
+    for (int i = 0; i < nnodi; ++i) sig[i] = signature(S, sh, t, s.isngn[s.iin[i]]);
+    vector<int> type(nnodi, 0);
+    {
+      std::unordered_map<Sig, int, SigHash> first;  // signature -> first node
+      vector<int> size(nnodi, 0), head(nnodi, -1);
+      for (int i = 0; i < nnodi; ++i) {
+        auto it = first.find(sig[i]);
+        if (it == first.end()) { first.emplace(sig[i], i); head[i] = i; }
+        else head[i] = it->second;
+        size[head[i]]++;
+      }
+      for (int i = 0; i < nnodi; ++i) {
+        int h = head[i];
+        if (sig[i].size() == 1) type[i] = 1;
+        else type[i] = size[h] > 1 ? 2 : 3;
+      }
+    }
+    if (S.prm.use_corner) {
+      // per neighbour sharing a face: up to four extreme points of each
+      // component of the shared node set (module_dd.f90:10017-10327)
+      for (int u : s.adj) {
+        // shared nodes with u, ascending global id
+        vector<std::pair<int, int>> shn;  // (global id, inodi)
+        for (int i = 0; i < nnodi; ++i)
+          for (auto& e : sig[i]) if (e[0] == u) { shn.emplace_back(s.isngn[s.iin[i]], i); break; }
+        std::sort(shn.begin(), shn.end());
+        bool face = false;
+        for (auto& p : shn) if (type[p.second] == 1) { face = true; break; }
+        if (!face) continue;
+        int m = (int)shn.size();
+        vector<int> myc(m), adc(m);
+        for (int q = 0; q < m; ++q) {
+          int i = shn[q].second;
+          for (auto& e : sig[i]) if (e[0] == u) { adc[q] = e[1]; myc[q] = e[2]; }
+        }
+        auto renumber = [](vector<int>& v) {
+          std::map<int, int> mp;
+          for (int x : v) mp[x] = 0;
+          int k = 0;
+          for (auto& kv : mp) kv.second = ++k;
+          for (int& x : v) x = mp[x];
+          return k;
+        };
+        renumber(myc);
+        int nadc = renumber(adc);
+        vector<int> ic(m);
+        for (int q = 0; q < m; ++q) ic[q] = (myc[q] - 1) * nadc + adc[q];
+        int nic = renumber(ic);
+        for (int c = 1; c <= nic; ++c) {
+          vector<int> members;
+          for (int q = 0; q < m; ++q) if (ic[q] == c) members.push_back(q);
+          int mm = (int)members.size();
+          vector<double> x(3 * mm, 0.0);
+          for (int q = 0; q < mm; ++q) {
+            int nd = s.iin[shn[members[q]].second];
+            for (int d = 0; d < s.ndim; ++d) x[3 * q + d] = s.xyz[(size_t)d * s.nnod + nd];
+          }
+          int pick[4] = {-1, -1, -1, -1};
+          auto farthest = [&](int base) {
+            double best = -1.0;
+            int loc = 0;
+            for (int q = 0; q < mm; ++q) {
+              double dd = 0.0;
+              for (int d = 0; d < s.ndim; ++d) { double df = x[3 * q + d] - x[3 * base + d]; dd += df * df; }
+              if (dd > best) { best = dd; loc = q; }
+            }
+            return loc;
+          };
+          if (mm > 0) pick[0] = farthest(0);
+          if (meshdim > 1 && mm > 1) {
+            pick[1] = farthest(pick[0]);
+            if (pick[1] == pick[0])
+              for (int q = 0; q < mm; ++q) if (q != pick[0]) { pick[1] = q; break; }
+          }
+          if (meshdim > 2 && mm > 2) {
+            const double *p1 = &x[3 * pick[0]], *p2 = &x[3 * pick[1]];
+            vector<double> area(mm);
+            for (int q = 0; q < mm; ++q) {
+              const double* pi = &x[3 * q];
+              double t1 = (p2[1] - p1[1]) * (pi[2] - p1[2]) - (pi[1] - p1[1]) * (p2[2] - p1[2]);
+              double t2 = (p2[0] - p1[0]) * (pi[2] - p1[2]) - (pi[0] - p1[0]) * (p2[2] - p1[2]);
+              double t3 = (p2[0] - p1[0]) * (pi[1] - p1[1]) - (pi[0] - p1[0]) * (p2[1] - p1[1]);
+              area[q] = t1 * t1 + t2 * t2 + t3 * t3;
+            }
+            double mv = 0.0;
+            int ml = -1;
+            for (int q = 0; q < mm; ++q) if (area[q] > mv) { mv = area[q]; ml = q; }
+            pick[2] = ml;
+            mv = 0.0; ml = -1;
+            for (int q = mm - 1; q >= 0; --q) if (area[q] > mv) { mv = area[q]; ml = q; }
+            pick[3] = ml;
+            if ((pick[2] == pick[0] && pick[3] == pick[0]) || (pick[2] == pick[1] && pick[3] == pick[1])) {
+              for (int q = 0; q < mm; ++q) if (q != pick[0] && q != pick[1]) { pick[2] = q; break; }
+              for (int q = 0; q < mm; ++q) if (q != pick[0] && q != pick[1] && q != pick[2]) { pick[3] = q; break; }
+            }
+          }
+          int nb = meshdim <= 2 ? 2 : 4;
+          for (int k = 0; k < nb; ++k)
+            if (pick[k] >= 0) type[shn[members[pick[k]]].second] = 3;
+        }
+      }
+    }
+    for (int i = 0; i < nnodi; ++i) if (type[i] == 3) corner_node[s.isngn[s.iin[i]]] = 1;
+  }
+
+  // ---- coarse numbering of a class of entities identified by a global node id:
+  // owner = lowest subdomain index holding the node; numbers run over
+  // subdomains in order, inside a subdomain in interface node order.
+  auto number_entities = [&](int shift, const vector<vector<int>>& ent_gid, vector<vector<int>>& ent_num) {
+    std::unordered_map<int, int> num;
+    int next = 1;
+    for (int t = 0; t < nsub; ++t) {
+      auto& s = S.subs[t];
+      std::unordered_map<int, int> mine;
+      for (size_t e = 0; e < ent_gid[t].size(); ++e) mine.emplace(ent_gid[t][e], (int)e);
+      for (int i = 0; i < s.nnodi; ++i) {
+        int g = s.isngn[s.iin[i]];
+        if (!mine.count(g)) continue;
+        if (sh.sub[sh.ptr[g]] == t) num[g] = shift + next++;
+      }
+    }
+    ent_num.resize(nsub);
+    for (int t = 0; t < nsub; ++t) {
+      ent_num[t].resize(ent_gid[t].size());
+      for (size_t e = 0; e < ent_gid[t].size(); ++e) {
+        auto it = num.find(ent_gid[t][e]);
+        if (it == num.end()) throw Error{ERR_NUMERIC, "coarse entity without owner"};
+        ent_num[t][e] = it->second;
+      }
+    }
+    return next - 1;
+  };
+
+  // corners of each subdomain, ascending global id
+  vector<vector<int>> corner_gid(nsub), corner_num;
+  for (int t = 0; t < nsub; ++t) {
+    auto& s = S.subs[t];
+    for (int i = 0; i < s.nnodi; ++i)
+      if (corner_node[s.isngn[s.iin[i]]]) corner_gid[t].push_back(s.isngn[s.iin[i]]);
+    std::sort(corner_gid[t].begin(), corner_gid[t].end());
+  }
+  S.ncorner = number_entities(0, corner_gid, corner_num);
+
+  // ---- pass 2: edges and faces, Dirichlet node removal
+  vector<vector<vector<int>>> edges(nsub), faces(nsub);  // node lists (inodi)
+  vector<vector<int>> edge_gid(nsub), face_gid(nsub), edge_num, face_num;
+  for (int t = 0; t < nsub; ++t) {
+    auto& s = S.subs[t];
+    std::unordered_map<Sig, int, SigHash> eidx, fidx;
+    for (int i = 0; i < s.nnodi; ++i) {
+      int g = s.isngn[s.iin[i]];
+      if (corner_node[g]) continue;
+      Sig sg = signature(S, sh, t, g);
+      if (sg.size() > 1) {
+        auto it = eidx.find(sg);
+        if (it == eidx.end()) { eidx.emplace(sg, (int)edges[t].size()); edges[t].push_back({i}); }
+        else edges[t][it->second].push_back(i);
+      } else {
+        auto it = fidx.find(sg);
+        if (it == fidx.end()) { fidx.emplace(sg, (int)faces[t].size()); faces[t].push_back({i}); }
+        else faces[t][it->second].push_back(i);
+      }
+    }
+    if (s.bc_present) {  // remove_bc_nodes on the first level (module_levels.f90:2233-2237)
+      auto strip = [&](vector<vector<int>>& globs) {
+        vector<vector<int>> kept;
+        for (auto& gl : globs) {
+          vector<int> k2;
+          for (int i : gl) {
+            int nd = s.iin[i];
+            bool fixed = false;
+            for (int d = 0; d < s.nndf[nd]; ++d) if (s.ifix[s.kdof[nd] + d] > 0) fixed = true;
+            if (!fixed) k2.push_back(i);
+          }
+          if (!k2.empty()) kept.push_back(k2);
+        }
+        globs.swap(kept);
+      };
+      strip(edges[t]);
+      strip(faces[t]);
+    }
+    for (auto& gl : edges[t]) {
+      int mn = INT32_MAX;
+      for (int i : gl) mn = std::min(mn, s.isngn[s.iin[i]]);
+      edge_gid[t].push_back(mn);
+    }
+    for (auto& gl : faces[t]) {
+      int mn = INT32_MAX;
+      for (int i : gl) mn = std::min(mn, s.isngn[s.iin[i]]);
+      face_gid[t].push_back(mn);
+    }
+  }
+  S.nedge = number_entities(S.ncorner, edge_gid, edge_num);
+  S.nface = number_entities(S.ncorner + S.nedge, face_gid, face_num);
+
+  // ---- coarse nodes and constraints
+  int ncnode = S.ncorner + S.nedge + S.nface;
+  vector<int> nndfc(ncnode, -1);
+  for (int t = 0; t < nsub; ++t) {
+    auto& s = S.subs[t];
+    s.cnodes.clear();
+    std::unordered_map<int, int> inodi_of;
+    for (int i = 0; i < s.nnodi; ++i) inodi_of.emplace(s.isngn[s.iin[i]], i);
+    auto add = [&](int itype, int num, const vector<int>& nodes, bool used) {
+      CoarseNode cn;
+      cn.itype = itype;
+      cn.global_number = num;
+      cn.inodi = nodes;
+      int ncd = 0;
+      for (int i : nodes) {
+        int nd = s.iin[i];
+        ncd = std::max(ncd, s.nndf[nd]);
+        for (int d = 0; d < s.nndf[nd]; ++d) cn.idofi.push_back(s.kdofi[i] + d);
+      }
+      cn.ncdof = used ? (itype == 3 ? s.nndf[s.iin[nodes[0]]] : ncd) : 0;
+      cn.used = used;
+      s.cnodes.push_back(cn);
+    };
+    for (size_t c = 0; c < corner_gid[t].size(); ++c)
+      add(3, corner_num[t][c], {inodi_of.at(corner_gid[t][c])}, S.prm.use_corner);
+    for (size_t e = 0; e < edges[t].size(); ++e) add(2, edge_num[t][e], edges[t][e], S.prm.use_arith);
+    for (size_t f = 0; f < faces[t].size(); ++f) add(1, face_num[t][f], faces[t][f], S.prm.use_arith);
+    for (auto& cn : s.cnodes) {
+      int& slot = nndfc[cn.global_number - 1];
+      if (slot >= 0 && slot != cn.ncdof) throw Error{ERR_NUMERIC, "inconsistent coarse node dof count"};
+      slot = cn.ncdof;
+    }
+  }
+  vector<int> kdofc(ncnode + 1, 0);
+  for (int c = 0; c < ncnode; ++c) kdofc[c + 1] = kdofc[c] + std::max(0, nndfc[c]);
+  S.ndofc = kdofc[ncnode];
+  for (auto& s : S.subs) {
+    s.c_ptr.assign(1, 0); s.c_col.clear(); s.c_val.clear(); s.indrowc.clear();
+    for (auto& cn : s.cnodes) {
+      if (!cn.used) continue;
+      if (cn.itype == 3) {
+        for (int d = 0; d < cn.ncdof; ++d) {
+          s.c_col.push_back(cn.idofi[d]); s.c_val.push_back(1.0);
+          s.c_ptr.push_back((int)s.c_col.size());
+          s.indrowc.push_back(kdofc[cn.global_number - 1] + d);
+        }
+      } else {
+        for (int d = 0; d < cn.ncdof; ++d) {  // row d: ones on the d-th dof of every node
+          for (int i : cn.inodi) {
+            int nd = s.iin[i];
+            if (d < s.nndf[nd]) { s.c_col.push_back(s.kdofi[i] + d); s.c_val.push_back(1.0); }
+          }
+          s.c_ptr.push_back((int)s.c_col.size());
+          s.indrowc.push_back(kdofc[cn.global_number - 1] + d);
+        }
+      }
+    }
+    s.nconstr = (int)s.indrowc.size();
+  }
+
+  // ---- unique interface dofs (by global dof id) and per-dof sharing lists
+  vector<int> gdof_uniq(ndof_global, -1);
+  vector<int> gid_list;
+  for (auto& s : S.subs)
+    for (int i = 0; i < s.ndofi; ++i) gid_list.push_back(s.isvgvn[s.iivsvn[i]]);
+  std::sort(gid_list.begin(), gid_list.end());
+  gid_list.erase(std::unique(gid_list.begin(), gid_list.end()), gid_list.end());
+  for (size_t k = 0; k < gid_list.size(); ++k) gdof_uniq[gid_list[k]] = (int)k;
+  S.ninterface = (int)gid_list.size();
+  for (auto& s : S.subs) {
+    s.uniq.resize(s.ndofi);
+    for (int i = 0; i < s.ndofi; ++i) s.uniq[i] = gdof_uniq[s.isvgvn[s.iivsvn[i]]];
+  }
+  // owners of each unique dof, ascending subdomain
+  vector<int> optr(S.ninterface + 1, 0);
+  for (auto& s : S.subs) for (int u : s.uniq) optr[u + 1]++;
+  for (int u = 0; u < S.ninterface; ++u) optr[u + 1] += optr[u];
+  vector<int> osub(optr[S.ninterface]), oloc(optr[S.ninterface]);
+  {
+    vector<int> pos(optr.begin(), optr.end() - 1);
+    for (int t = 0; t < nsub; ++t)
+      for (int i = 0; i < S.subs[t].ndofi; ++i) { int u = S.subs[t].uniq[i]; osub[pos[u]] = t; oloc[pos[u]++] = i; }
+  }
+  // own value plus the other holders' values in ascending order (the
+  // upload / swap / download sum of module_dd.f90:11236-11551)
+  auto neighbour_sum = [&](int t, int i, const std::function<double(int, int)>& val) {
+    int u = S.subs[t].uniq[i];
+    double own = val(t, i), acc = 0.0;
+    for (int q = optr[u]; q < optr[u + 1]; ++q) if (osub[q] != t) acc += val(osub[q], oloc[q]);
+    return std::make_pair(own, acc);
+  };
+
+  // ---- assembled Dirichlet contributions on the interface (module_dd.f90:1200-1255)
+  {
+    vector<vector<double>> bci(nsub);
+    for (int t = 0; t < nsub; ++t) {
+      auto& s = S.subs[t];
+      bci[t].resize(s.ndofi);
+      for (int i = 0; i < s.ndofi; ++i) bci[t][i] = s.bc[s.iivsvn[i]];
+    }
+    for (int t = 0; t < nsub; ++t) {
+      auto& s = S.subs[t];
+      for (int i = 0; i < s.ndofi; ++i) {
+        auto pr = neighbour_sum(t, i, [&](int a, int b) { return bci[a][b]; });
+        s.bc[s.iivsvn[i]] += pr.second;
+      }
+    }
+  }
+
+  // ---- weights (module_dd.f90:11554-11722)
+  {
+    vector<vector<double>> rho(nsub);
+    for (int t = 0; t < nsub; ++t) {
+      auto& s = S.subs[t];
+      rho[t].assign(s.ndofi, 1.0);
+      if (S.prm.weights_type == 1) {
+        vector<double> dg(s.ndof, 0.0);
+        for (size_t k = 0; k < s.ia.size(); ++k) if (s.ia[k] == s.ja[k]) dg[s.ia[k]] += s.a[k];
+        for (int i = 0; i < s.ndofi; ++i) { rho[t][i] = dg[s.iivsvn[i]]; if (rho[t][i] == 0.0) rho[t][i] = 1.0; }
+      } else if (S.prm.weights_type != 0) {
+        throw Error{ERR_UNSUPPORTED, "weights_type " + std::to_string(S.prm.weights_type) + " is not implemented"};
+      }
+    }
+    for (int t = 0; t < nsub; ++t) {
+      auto& s = S.subs[t];
+      s.wi.resize(s.ndofi);
+      for (int i = 0; i < s.ndofi; ++i) {
+        auto pr = neighbour_sum(t, i, [&](int a, int b) { return rho[a][b]; });
+        double den = pr.first + pr.second;
+        if (den == 0.0) throw Error{ERR_NUMERIC, "zero denominator in interface weights"};
+        s.wi[i] = pr.first / den;
+      }
+    }
+  }
+  S.iface_fixed.assign(S.ninterface, 0);
+  S.iface_wsum.assign(S.ninterface, 0.0);
+  for (auto& s : S.subs)
+    for (int i = 0; i < s.ndofi; ++i) {
+      if (s.ifix[s.iivsvn[i]]) S.iface_fixed[s.uniq[i]] = 1;
+      S.iface_wsum[s.uniq[i]] += s.wi[i];
+    }
+
+  S.stats.ncorner = S.ncorner; S.stats.nedge = S.nedge; S.stats.nface = S.nface; S.stats.ndofc = S.ndofc;
+  S.stats.sum_ndofi = 0; S.stats.sum_ndofo = 0;
+  for (auto& s : S.subs) { S.stats.sum_ndofi += s.ndofi; S.stats.sum_ndofo += s.ndofo; }
+  S.stats.ninterface = S.ninterface;
+  S.ndof_global = ndof_global;
+}
+
+}  // namespace bddc

@@ -1,0 +1,135 @@
+// Internal data model of the GB300 BDDC solver (host side).
+//
+// One process, one GPU, every subdomain resident on the device.  The host
+// keeps the uploaded subdomain data (module_dd.f90:65-372 subdomain_type is the
+// reference's equivalent) and runs the integer/geometric part of the setup:
+// interface detection, globs and corners, coarse numbering, Dirichlet
+// elimination and weights.  Everything numeric after that runs on the GPU.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace bddc {
+
+using std::vector;
+
+// status codes (mirror include/bddcml_gb300.h)
+enum Status { OK = 0, ERR_ARGUMENT = 1, ERR_CUDA = 2, ERR_NUMERIC = 3, ERR_UNSUPPORTED = 4, ERR_MEMORY = 5 };
+
+struct Error {
+  int code;
+  std::string msg;
+};
+
+// one coarse node of a subdomain: a corner, an edge or a face
+// (module_dd.f90:43-62 cnode_type)
+struct CoarseNode {
+  int itype = 0;          // 3 corner, 2 edge, 1 face
+  int global_number = 0;  // 1-based over corners, then edges, then faces
+  vector<int> inodi;      // interface nodes of the glob
+  vector<int> idofi;      // interface dofs of the glob
+  int ncdof = 0;          // number of constraint rows it contributes
+  bool used = false;
+};
+
+struct Subdomain {
+  // ---------------- uploaded (0-based local numbering)
+  int nelem = 0, nnod = 0, ndof = 0, ndim = 0;
+  vector<int> inet, nnet, nndf, isngn, isvgvn, isegn, ifix;
+  vector<double> xyz;  // column-major (nnod x ndim)
+  vector<double> fixv, rhs, sol;
+  bool rhs_complete = true;
+  int matrixtype = 1;
+  vector<int> ia, ja;  // assembled upper triangle
+  vector<double> a;
+  bool loaded = false;
+  bool find_components = true;
+  bool dual_graph = true;
+  int neighbouring = 1;
+
+  // ---------------- derived on the host
+  bool bc_present = false;
+  vector<int> comp;          // nodal components, 1-based
+  vector<int> kdof;          // first dof of each node
+  vector<int> iin;           // interface nodes (local order)
+  vector<int> kdofi;         // first interface dof of each interface node (nnodi+1)
+  vector<int> iivsvn;        // interface dofs (local dof index)
+  vector<int> iovsvn;        // interior dofs (local dof index)
+  int nnodi = 0, ndofi = 0, ndofo = 0;
+  vector<int> adj;           // neighbour subdomains, ascending (0-based)
+  vector<CoarseNode> cnodes;
+  // constraints in CSR over interface dofs; indrowc = global coarse dof (0-based)
+  vector<int> c_ptr, c_col;
+  vector<double> c_val;
+  vector<int> indrowc;
+  int nconstr = 0;
+  vector<double> bc;         // eliminated Dirichlet contributions, interface assembled
+  vector<double> wi;         // interface weights
+  vector<int> uniq;          // interface dof -> unique interface index
+  // interior ordering used for the band factor: perm[new] = index into iovsvn
+  vector<int> operm;
+  int band = 0;              // half bandwidth of the reordered interior block
+  double rho = 1.0;          // scale of the constraint penalty in the preconditioner
+};
+
+struct Params {
+  int nlevels = 2;
+  int nsub = 0;
+  int numbase = 0;
+  int verbose = 0;
+  int precision = 1;          // 0 plain FP64, 1 mixed
+  // preconditioner options
+  bool use_corner = true, use_arith = true, use_adaptive = false, use_user = false;
+  int weights_type = 0;
+  int matrixtype = 1;
+};
+
+struct Stats {
+  double t_host_setup = 0, t_device_setup = 0, t_solve = 0, t_factor = 0, t_schur = 0, t_precond = 0,
+         t_coarse = 0, t_iterations = 0, t_postprocess = 0;
+  double bytes_per_iteration = 0;
+  int ncorner = 0, nedge = 0, nface = 0, ndofc = 0;
+  long long sum_ndofi = 0, sum_ndofo = 0, ninterface = 0;
+  int num_iter = 0;
+  double setup_flops = 0;
+  double schur_refine_residual = 0;
+};
+
+class Device;  // GPU side (bddc_device.cu)
+
+struct Solver {
+  Params prm;
+  vector<Subdomain> subs;
+  int nelem = 0, nnod = 0, ndof_global = 0;
+  // coarse space
+  int ncorner = 0, nedge = 0, nface = 0, ndofc = 0;
+  // unique interface numbering
+  int ninterface = 0;                 // number of unique interface dofs
+  vector<int> iface_fixed;            // per unique dof: 1 if Dirichlet-fixed
+  vector<double> iface_wsum;          // per unique dof: sum of subdomain weights
+  bool setup_done = false;
+  Device* dev = nullptr;
+  Stats stats;
+  vector<double> relres_history;
+};
+
+// host setup (bddc_host.cpp)
+void host_assemble_upper(vector<int>& ia, vector<int>& ja, vector<double>& a);
+void host_nodal_components(Subdomain& s);
+void host_setup(Solver& S);              // everything integer/geometric + BC + weights + constraints
+void host_interior_ordering(Subdomain& s, const vector<int>& f_ptr, const vector<int>& f_col);
+void full_symmetric_csr(const Subdomain& s, vector<int>& ptr, vector<int>& col, vector<double>& val);
+
+// device (bddc_device.cu)
+Device* device_create(Error& err);
+void device_destroy(Device* d);
+bool device_setup(Solver& S, Error& err);
+bool device_solve(Solver& S, double tol, int maxit, int ndecrmax, int& num_iter, int& reason, double& cond,
+                  Error& err);
+bool device_download(Solver& S, int isub, double* out, Error& err);
+
+double wall_time();
+
+}  // namespace bddc

@@ -1,0 +1,80 @@
+// Device kernels of the BDDC solver (sm_103a).
+//
+// Blocked dense linear algebra on 64 x 64 tiles, batched over subdomains of
+// different sizes through per-subdomain descriptors.  Each subdomain's
+// interior stiffness block is a band matrix after reordering; it is stored as
+// block rows of (w+1) dense 64 x 64 tiles ("block band"), so the same
+// kernels serve the band factor of the interior block (small w) and the dense
+// factor of the interface-sized preconditioner block (w = nb - 1).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace bddc {
+
+constexpr int NB = 64;      // tile edge
+constexpr int NT = 256;     // threads of the tile kernels (16 x 16, 4 x 4 outputs each)
+constexpr int KC = 16;      // K chunk of the SIMT tile product
+
+// error flags written by kernels (bit field), read by the host after setup
+enum DevErr : int { DE_PIVOT = 1, DE_NAN = 2, DE_SMALL = 4 };
+
+struct BandDesc {
+  int nb;            // block rows (0 = nothing to do for this entry)
+  int w;             // band width in blocks
+  int ncol;          // RHS columns (multiple of NB)
+  int pad;
+  long long oL;      // offset of the block band (elements)
+  long long oLinv;   // offset of the inverted diagonal blocks
+  long long oB;      // offset of the RHS block (row-major, ld = ncol)
+};
+
+__host__ __device__ inline long long band_block(const BandDesc& d, int i, int j) {
+  return d.oL + ((long long)i * (d.w + 1) + (j - i + d.w)) * (NB * NB);
+}
+
+// --------------------------------------------------------------- SIMT tile
+// acc(4x4 per thread) += op(A) * op(B) over K (multiple of KC), 64 x 64 output.
+// A: !TA -> A[r*lda + k], TA -> A[k*lda + r];  B: !TB -> B[k*ldb + c], TB -> B[c*ldb + k]
+template <typename T, bool TA, bool TB>
+__device__ __forceinline__ void tile_gemm(T (&acc)[4][4], const T* __restrict__ A, int lda,
+                                          const T* __restrict__ B, int ldb, int K, T* smA, T* smB) {
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+  for (int k0 = 0; k0 < K; k0 += KC) {
+    // stage A chunk as smA[k][r], B chunk as smB[k][c]  (KC x 64 each)
+    for (int e = tid; e < KC * NB; e += NT) {
+      int r, k;
+      if (!TA) { k = e % KC; r = e / KC; } else { r = e % NB; k = e / NB; }
+      T v = TA ? A[(long long)(k0 + k) * lda + r] : A[(long long)r * lda + k0 + k];
+      smA[k * NB + r] = v;
+      int c, kk;
+      if (!TB) { c = e % NB; kk = e / NB; } else { kk = e % KC; c = e / KC; }
+      T u = TB ? B[(long long)c * ldb + k0 + kk] : B[(long long)(k0 + kk) * ldb + c];
+      smB[kk * NB + c] = u;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < KC; ++k) {
+      T a[4], b[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) { a[q] = smA[k * NB + ty * 4 + q]; b[q] = smB[k * NB + tx * 4 + q]; }
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int p = 0; p < 4; ++p) acc[q][p] += a[q] * b[p];
+    }
+    __syncthreads();
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void tile_zero(T (&acc)[4][4]) {
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+#pragma unroll
+    for (int p = 0; p < 4; ++p) acc[q][p] = T(0);
+}
+
+}  // namespace bddc

@@ -1,0 +1,602 @@
+// Setup kernels: block-band Cholesky, multi-RHS triangular solves, FP64-
+// accurate Schur complements by refinement, constrained-Neumann
+// preconditioner blocks and local coarse matrices.
+//
+// Reference counterparts (what is computed, not how):
+//   interior factor A11 ............... module_dd.f90:4175-4295 (MUMPS there)
+//   S = A22 - A21 A11^-1 A12 .......... module_dd.f90:6564-6699 (applied implicitly there)
+//   [A C^T; C 0] factor ............... module_dd.f90:5211-5486 (MUMPS SYM=2 there)
+//   coarse basis Phi, Ac = -lambda .... module_dd.f90:5489-5799
+//   reduced rhs g = f2 - A21 A11^-1 f1  module_dd.f90:7138-7257
+#pragma once
+
+#include "bddc_df.cuh"
+#include "bddc_kernels.cuh"
+
+namespace bddc {
+
+struct DevSub {
+  int no, ni, nc, ncp;     // interior dofs, interface dofs, constraints, padded constraints
+  int NO, NI, NR, NRC;     // padded: interior, interface, interior-RHS columns, Srho-RHS columns
+  int nbo, w, nbi, nref;   // interior block rows, band blocks, interface block rows, refinement steps
+  long long oL, oLinv;     // factor pool: interior band factor, inverted diagonal blocks
+  long long oXc;           // factor pool: (nref+1) solution components, NO x NR each
+  long long oLs, oLsinv;   // factor pool: preconditioner block factor
+  long long oBs;           // factor pool: NI x NRC  [Srho^-1 | Y]
+  long long oS;            // Schur pool: NI x NI
+  long long oZ, oPhi;      // preconditioner pool: NI x NI, NI x ncp
+  long long oGinv, oAc;    // small FP64 pool: ncp x ncp each
+  int rep;                 // offset into replicated interface vectors
+  int koo, koi, kio, kii;  // row-pointer offsets of the four CSR blocks
+  int cptr;                // constraint row-pointer offset
+  int coff;                // offset into per-constraint arrays (coarse map)
+  double rho;              // penalty scale of the preconditioner block
+};
+
+// ------------------------------------------------------------ band factor
+// dynamic smem: a[NB][NB+1], inv[NB][NB+1], smA[KC*NB], smB[KC*NB]
+template <typename T>
+__global__ void __launch_bounds__(NT) k_chol_diag(const BandDesc* __restrict__ bd, T* __restrict__ pool, int k,
+                                                  int* __restrict__ err) {
+  const BandDesc d = bd[blockIdx.x];
+  if (k >= d.nb) return;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T* a = reinterpret_cast<T*>(smraw);          // NB x (NB+1)
+  T* inv = a + NB * (NB + 1);                  // NB x (NB+1)
+  T* smA = inv + NB * (NB + 1);
+  T* smB = smA + KC * NB;
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  T acc[4][4];
+  tile_zero(acc);
+  for (int j = max(0, k - d.w); j < k; ++j) {
+    const T* Lkj = pool + band_block(d, k, j);
+    tile_gemm<T, false, true>(acc, Lkj, NB, Lkj, NB, NB, smA, smB);
+  }
+  const T* Akk = pool + band_block(d, k, k);
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+#pragma unroll
+    for (int p = 0; p < 4; ++p) {
+      int r = ty * 4 + q, c = tx * 4 + p;
+      a[r * (NB + 1) + c] = Akk[r * NB + c] - acc[q][p];
+    }
+  __syncthreads();
+  for (int c = 0; c < NB; ++c) {
+    if (tid == 0) {
+      T v = a[c * (NB + 1) + c];
+      if (!(v > T(0))) {
+        atomicOr(err, (v != v) ? DE_NAN : DE_PIVOT);
+        v = T(1);
+      }
+      a[c * (NB + 1) + c] = sqrt(v);
+    }
+    __syncthreads();
+    T dc = a[c * (NB + 1) + c];
+    for (int r = c + 1 + tid; r < NB; r += NT) a[r * (NB + 1) + c] /= dc;
+    __syncthreads();
+    int m = NB - c - 1;
+    for (int e = tid; e < m * m; e += NT) {
+      int r = c + 1 + e / m, q = c + 1 + e % m;
+      if (q <= r) a[r * (NB + 1) + q] -= a[r * (NB + 1) + c] * a[q * (NB + 1) + c];
+    }
+    __syncthreads();
+  }
+  // inverse of the lower triangular factor, one column per thread
+  if (tid < NB) {
+    const int j = tid;
+    for (int i = 0; i < j; ++i) inv[i * (NB + 1) + j] = T(0);
+    inv[j * (NB + 1) + j] = T(1) / a[j * (NB + 1) + j];
+    for (int i = j + 1; i < NB; ++i) {
+      T s = T(0);
+      for (int m = j; m < i; ++m) s += a[i * (NB + 1) + m] * inv[m * (NB + 1) + j];
+      inv[i * (NB + 1) + j] = -s / a[i * (NB + 1) + i];
+    }
+  }
+  __syncthreads();
+  T* Lkk = pool + band_block(d, k, k);
+  T* Li = pool + d.oLinv + (long long)k * NB * NB;
+  for (int e = tid; e < NB * NB; e += NT) {
+    int r = e / NB, c = e % NB;
+    Lkk[e] = c <= r ? a[r * (NB + 1) + c] : T(0);
+    Li[e] = inv[r * (NB + 1) + c];
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(NT) k_chol_off(const BandDesc* __restrict__ bd, T* __restrict__ pool, int k) {
+  const BandDesc d = bd[blockIdx.y];
+  const int i = k + 1 + blockIdx.x;
+  if (k >= d.nb || i >= d.nb || i - k > d.w) return;
+  __shared__ __align__(16) T smA[KC * NB];
+  __shared__ __align__(16) T smB[KC * NB];
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  T acc[4][4];
+  tile_zero(acc);
+  for (int j = max(0, i - d.w); j < k; ++j)
+    tile_gemm<T, false, true>(acc, pool + band_block(d, i, j), NB, pool + band_block(d, k, j), NB, NB, smA, smB);
+  T* Aik = pool + band_block(d, i, k);
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+#pragma unroll
+    for (int p = 0; p < 4; ++p) Aik[(ty * 4 + q) * NB + tx * 4 + p] -= acc[q][p];
+  __syncthreads();
+  tile_zero(acc);
+  tile_gemm<T, false, true>(acc, Aik, NB, pool + d.oLinv + (long long)k * NB * NB, NB, NB, smA, smB);
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+#pragma unroll
+    for (int p = 0; p < 4; ++p) Aik[(ty * 4 + q) * NB + tx * 4 + p] = acc[q][p];
+}
+
+// forward step k: B_k = Linv_kk (B_k - sum_j L_kj B_j), one 64-column tile per CTA
+template <typename T>
+__global__ void __launch_bounds__(NT) k_trsm_fwd(const BandDesc* __restrict__ bd, const T* __restrict__ Lpool,
+                                                 T* __restrict__ Bpool, int k) {
+  const BandDesc d = bd[blockIdx.y];
+  const int c0 = blockIdx.x * NB;
+  if (k >= d.nb || c0 >= d.ncol) return;
+  __shared__ __align__(16) T smA[KC * NB];
+  __shared__ __align__(16) T smB[KC * NB];
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const int ld = d.ncol;
+  T* B = Bpool + d.oB;
+  T acc[4][4];
+  tile_zero(acc);
+  for (int j = max(0, k - d.w); j < k; ++j)
+    tile_gemm<T, false, false>(acc, Lpool + band_block(d, k, j), NB, B + (long long)j * NB * ld + c0, ld, NB, smA, smB);
+  T* Bk = B + (long long)k * NB * ld + c0;
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+#pragma unroll
+    for (int p = 0; p < 4; ++p) Bk[(long long)(ty * 4 + q) * ld + tx * 4 + p] -= acc[q][p];
+  __syncthreads();
+  tile_zero(acc);
+  tile_gemm<T, false, false>(acc, Lpool + d.oLinv + (long long)k * NB * NB, NB, Bk, ld, NB, smA, smB);
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+#pragma unroll
+    for (int p = 0; p < 4; ++p) Bk[(long long)(ty * 4 + q) * ld + tx * 4 + p] = acc[q][p];
+}
+
+// backward step k: B_k = Linv_kk^T (B_k - sum_{i>k} L_ik^T B_i)
+template <typename T>
+__global__ void __launch_bounds__(NT) k_trsm_bwd(const BandDesc* __restrict__ bd, const T* __restrict__ Lpool,
+                                                 T* __restrict__ Bpool, int k) {
+  const BandDesc d = bd[blockIdx.y];
+  const int c0 = blockIdx.x * NB;
+  if (k >= d.nb || c0 >= d.ncol) return;
+  __shared__ __align__(16) T smA[KC * NB];
+  __shared__ __align__(16) T smB[KC * NB];
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const int ld = d.ncol;
+  T* B = Bpool + d.oB;
+  T acc[4][4];
+  tile_zero(acc);
+  int iend = min(d.nb - 1, k + d.w);
+  for (int i = k + 1; i <= iend; ++i)
+    tile_gemm<T, true, false>(acc, Lpool + band_block(d, i, k), NB, B + (long long)i * NB * ld + c0, ld, NB, smA, smB);
+  T* Bk = B + (long long)k * NB * ld + c0;
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+#pragma unroll
+    for (int p = 0; p < 4; ++p) Bk[(long long)(ty * 4 + q) * ld + tx * 4 + p] -= acc[q][p];
+  __syncthreads();
+  tile_zero(acc);
+  tile_gemm<T, true, false>(acc, Lpool + d.oLinv + (long long)k * NB * NB, NB, Bk, ld, NB, smA, smB);
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+#pragma unroll
+    for (int p = 0; p < 4; ++p) Bk[(long long)(ty * 4 + q) * ld + tx * 4 + p] = acc[q][p];
+}
+
+// --------------------------------------------------- matrix construction
+struct CsrView {
+  const int* ptr;     // global row pointers (absolute indices into col/val)
+  const int* col;
+  const double* val;
+};
+
+// interior block into block-band storage; padding rows get a unit diagonal
+template <typename T>
+__global__ void k_fill_band(const DevSub* __restrict__ ds, CsrView koo, T* __restrict__ pool,
+                            const BandDesc* __restrict__ bd) {
+  const DevSub s = ds[blockIdx.y];
+  const BandDesc d = bd[blockIdx.y];
+  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= s.NO) return;
+  if (r >= s.no) {
+    pool[band_block(d, r / NB, r / NB) + (r % NB) * NB + r % NB] = T(1);
+    return;
+  }
+  const int* ptr = koo.ptr + s.koo;
+  for (int q = ptr[r]; q < ptr[r + 1]; ++q) {
+    int c = koo.col[q];
+    if (c <= r) pool[band_block(d, r / NB, c / NB) + (r % NB) * NB + c % NB] = T(koo.val[q]);
+  }
+}
+
+// RHS of the interior solves: [A_oi | f_o | 0], NO x NR
+template <typename T>
+__global__ void k_fill_rhs(const DevSub* __restrict__ ds, CsrView koi, const double* __restrict__ fo,
+                           const long long* __restrict__ fo_off, T* __restrict__ pool) {
+  const DevSub s = ds[blockIdx.y];
+  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= s.no) return;
+  T* B = pool + s.oXc + (long long)r * s.NR;
+  const int* ptr = koi.ptr + s.koi;
+  for (int q = ptr[r]; q < ptr[r + 1]; ++q) B[koi.col[q]] = T(koi.val[q]);
+  B[s.ni] = T(fo[fo_off[blockIdx.y] + r]);
+}
+
+// Refinement residual of the interior solves, FP64-accurate on FP32 pipes:
+// R = [A_oi | f_o] - A_oo (X_0 + ... + X_{ncomp-1}), written as FP32 into component ncomp.
+// One CTA per interior row; the row's matrix entries are staged in shared memory.
+__global__ void __launch_bounds__(128) k_residual_df(const DevSub* __restrict__ ds, CsrView koo, CsrView koi,
+                                                     const double* __restrict__ fo,
+                                                     const long long* __restrict__ fo_off, float* __restrict__ pool,
+                                                     int ncomp) {
+  const DevSub s = ds[blockIdx.y];
+  const int r = blockIdx.x;
+  if (r >= s.NO) return;
+  __shared__ int scol[96];
+  __shared__ dfloat sval[96];
+  __shared__ int bcol[96];
+  __shared__ dfloat bval[96];
+  __shared__ int nnz, nb0;
+  float* out = pool + s.oXc + (long long)ncomp * s.NO * s.NR + (long long)r * s.NR;
+  if (r >= s.no) {
+    for (int c = threadIdx.x; c < s.NR; c += blockDim.x) out[c] = 0.f;
+    return;
+  }
+  if (threadIdx.x == 0) {
+    const int* p = koo.ptr + s.koo;
+    int n = min(96, p[r + 1] - p[r]);
+    nnz = n;
+    const int* pb = koi.ptr + s.koi;
+    nb0 = min(95, pb[r + 1] - pb[r]);
+  }
+  __syncthreads();
+  {
+    const int* p = koo.ptr + s.koo;
+    for (int q = threadIdx.x; q < nnz; q += blockDim.x) {
+      scol[q] = koo.col[p[r] + q];
+      sval[q] = df_from_double(-koo.val[p[r] + q]);
+    }
+    const int* pb = koi.ptr + s.koi;
+    for (int q = threadIdx.x; q < nb0; q += blockDim.x) {
+      bcol[q] = koi.col[pb[r] + q];
+      bval[q] = df_from_double(koi.val[pb[r] + q]);
+    }
+    if (threadIdx.x == 0) {
+      bcol[nb0] = s.ni;
+      bval[nb0] = df_from_double(fo[fo_off[blockIdx.y] + r]);
+    }
+  }
+  __syncthreads();
+  const long long comp = (long long)s.NO * s.NR;
+  const float* X = pool + s.oXc;
+  for (int c = threadIdx.x; c < s.NR; c += blockDim.x) {
+    dfacc acc;
+    for (int q = 0; q <= nb0; ++q)
+      if (bcol[q] == c) acc.add_df(bval[q]);
+    for (int q = 0; q < nnz; ++q) {
+      const float* xr = X + (long long)scol[q] * s.NR + c;
+      for (int m = 0; m < ncomp; ++m) acc.fma_df(sval[q], xr[m * comp]);
+    }
+    out[c] = acc.value().hi;
+  }
+}
+
+// Schur complement S = A_ii - A_io (X_0 + ...), FP64-accurate, plus the
+// subdomain part of the reduced rhs g = f_i - A_io X(:, ni).
+// Mixed precision stores S as FP32 (hi, lo) pairs.
+__global__ void __launch_bounds__(128) k_schur_df(const DevSub* __restrict__ ds, CsrView kio, CsrView kii,
+                                                  const float* __restrict__ pool, float2* __restrict__ Spool,
+                                                  const double* __restrict__ fi, double* __restrict__ grep) {
+  const DevSub s = ds[blockIdx.y];
+  const int i = blockIdx.x;
+  if (i >= s.NI) return;
+  float2* Srow = Spool + s.oS + (long long)i * s.NI;
+  if (i >= s.ni) {
+    for (int c = threadIdx.x; c < s.NI; c += blockDim.x) Srow[c] = make_float2(0.f, 0.f);
+    return;
+  }
+  __shared__ int scol[128];
+  __shared__ dfloat sval[128];
+  __shared__ int dcol[128];
+  __shared__ dfloat dval[128];
+  __shared__ int nnz, nd;
+  if (threadIdx.x == 0) {
+    const int* p = kio.ptr + s.kio;
+    nnz = min(128, p[i + 1] - p[i]);
+    const int* pd = kii.ptr + s.kii;
+    nd = min(128, pd[i + 1] - pd[i]);
+  }
+  __syncthreads();
+  {
+    const int* p = kio.ptr + s.kio;
+    for (int q = threadIdx.x; q < nnz; q += blockDim.x) {
+      scol[q] = kio.col[p[i] + q];
+      sval[q] = df_from_double(-kio.val[p[i] + q]);
+    }
+    const int* pd = kii.ptr + s.kii;
+    for (int q = threadIdx.x; q < nd; q += blockDim.x) {
+      dcol[q] = kii.col[pd[i] + q];
+      dval[q] = df_from_double(kii.val[pd[i] + q]);
+    }
+  }
+  __syncthreads();
+  const long long comp = (long long)s.NO * s.NR;
+  const int ncomp = s.nref + 1;
+  for (int c = threadIdx.x; c <= s.ni; c += blockDim.x) {
+    dfacc acc;
+    if (c < s.ni) {
+      for (int q = 0; q < nd; ++q)
+        if (dcol[q] == c) acc.add_df(dval[q]);
+    } else {
+      acc.add_df(df_from_double(fi[s.rep + i]));
+    }
+    for (int q = 0; q < nnz; ++q) {
+      const float* xr = pool + s.oXc + (long long)scol[q] * s.NR + c;
+      for (int m = 0; m < ncomp; ++m) acc.fma_df(sval[q], xr[m * comp]);
+    }
+    if (c < s.ni) {
+      dfloat v = acc.value();
+      Srow[c] = make_float2(v.hi, v.lo);
+    } else {
+      grep[s.rep + i] = acc.to_double();
+    }
+  }
+  for (int c = s.ni + threadIdx.x; c < s.NI; c += blockDim.x) Srow[c] = make_float2(0.f, 0.f);
+}
+
+// plain FP64 counterpart of k_schur_df (single solution component)
+__global__ void __launch_bounds__(128) k_schur_f64(const DevSub* __restrict__ ds, CsrView kio, CsrView kii,
+                                                   const double* __restrict__ pool, double* __restrict__ Spool,
+                                                   const double* __restrict__ fi, double* __restrict__ grep) {
+  const DevSub s = ds[blockIdx.y];
+  const int i = blockIdx.x;
+  if (i >= s.NI) return;
+  double* Srow = Spool + s.oS + (long long)i * s.NI;
+  if (i >= s.ni) {
+    for (int c = threadIdx.x; c < s.NI; c += blockDim.x) Srow[c] = 0.0;
+    return;
+  }
+  const int* p = kio.ptr + s.kio;
+  const int* pd = kii.ptr + s.kii;
+  for (int c = threadIdx.x; c <= s.ni; c += blockDim.x) {
+    double acc = 0.0;
+    if (c < s.ni) {
+      for (int q = pd[i]; q < pd[i + 1]; ++q)
+        if (kii.col[q] == c) acc += kii.val[q];
+    } else {
+      acc = fi[s.rep + i];
+    }
+    for (int q = p[i]; q < p[i + 1]; ++q) acc -= kio.val[q] * pool[s.oXc + (long long)kio.col[q] * s.NR + c];
+    if (c < s.ni) Srow[c] = acc;
+    else grep[s.rep + i] = acc;
+  }
+  for (int c = s.ni + threadIdx.x; c < s.NI; c += blockDim.x) Srow[c] = 0.0;
+}
+
+// S = (S + S^T) / 2 (the computed Schur complement is symmetric only up to rounding)
+__global__ void k_symmetrize_df(const DevSub* __restrict__ ds, float2* __restrict__ Spool) {
+  const DevSub s = ds[blockIdx.z];
+  int i = blockIdx.y * 16 + threadIdx.y, j = blockIdx.x * 16 + threadIdx.x;
+  if (i >= s.ni || j >= s.ni || j <= i) return;
+  float2* S = Spool + s.oS;
+  float2 a = S[(long long)i * s.NI + j], b = S[(long long)j * s.NI + i];
+  dfacc acc;
+  acc.add(a.x); acc.add(b.x); acc.c += a.y + b.y;
+  dfloat v = acc.value();
+  float2 m = make_float2(0.5f * v.hi, 0.5f * v.lo);
+  S[(long long)i * s.NI + j] = m;
+  S[(long long)j * s.NI + i] = m;
+}
+
+__global__ void k_symmetrize_f64(const DevSub* __restrict__ ds, double* __restrict__ Spool) {
+  const DevSub s = ds[blockIdx.z];
+  int i = blockIdx.y * 16 + threadIdx.y, j = blockIdx.x * 16 + threadIdx.x;
+  if (i >= s.ni || j >= s.ni || j <= i) return;
+  double* S = Spool + s.oS;
+  double m = 0.5 * (S[(long long)i * s.NI + j] + S[(long long)j * s.NI + i]);
+  S[(long long)i * s.NI + j] = m;
+  S[(long long)j * s.NI + i] = m;
+}
+
+template <typename T, typename ST>
+__device__ __forceinline__ T schur_entry(const ST* S, long long idx);
+template <>
+__device__ __forceinline__ float schur_entry<float, float2>(const float2* S, long long idx) { return S[idx].x; }
+template <>
+__device__ __forceinline__ double schur_entry<double, double>(const double* S, long long idx) { return S[idx]; }
+
+// Preconditioner block Srho = S + rho * C~^T C~ (rows of C scaled to unit norm),
+// lower blocks in dense-block storage; unit diagonal on the padding.  On the
+// constraint set C z = 0 it equals S, so the constrained solve is unchanged.
+template <typename T, typename ST>
+__global__ void k_fill_srho(const DevSub* __restrict__ ds, const ST* __restrict__ Spool, T* __restrict__ pool,
+                            const BandDesc* __restrict__ bd) {
+  const DevSub s = ds[blockIdx.z];
+  const BandDesc d = bd[blockIdx.z];
+  int i = blockIdx.y * 16 + threadIdx.y, j = blockIdx.x * 16 + threadIdx.x;
+  if (i >= s.NI || j > i) return;
+  T v;
+  if (i < s.ni && j < s.ni) v = schur_entry<T, ST>(Spool + s.oS, (long long)i * s.NI + j);
+  else v = (i == j) ? T(1) : T(0);
+  pool[band_block(d, i / NB, j / NB) + (i % NB) * NB + j % NB] = v;
+}
+
+template <typename T>
+__global__ void k_add_penalty(const DevSub* __restrict__ ds, const int* __restrict__ cptr, const int* __restrict__ ccol,
+                              const double* __restrict__ cval, T* __restrict__ pool, const BandDesc* __restrict__ bd) {
+  const DevSub s = ds[blockIdx.y];
+  const BandDesc d = bd[blockIdx.y];
+  const int r = blockIdx.x;
+  if (r >= s.nc) return;
+  const int* p = cptr + s.cptr;
+  int q0 = p[r], n = p[r + 1] - q0;
+  double nrm = 0.0;
+  for (int q = 0; q < n; ++q) nrm += cval[q0 + q] * cval[q0 + q];
+  double sc = s.rho / nrm;
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    int a = e / n, b = e % n;
+    int i = ccol[q0 + a], j = ccol[q0 + b];
+    if (j > i) continue;
+    pool[band_block(d, i / NB, j / NB) + (i % NB) * NB + j % NB] += T(sc * cval[q0 + a] * cval[q0 + b]);
+  }
+}
+
+// RHS [I | C^T | 0] of the preconditioner solves
+template <typename T>
+__global__ void k_fill_rhs_srho(const DevSub* __restrict__ ds, const int* __restrict__ cptr,
+                                const int* __restrict__ ccol, const double* __restrict__ cval, T* __restrict__ pool) {
+  const DevSub s = ds[blockIdx.y];
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < s.NI) pool[s.oBs + (long long)i * s.NRC + i] = T(1);
+  if (i < s.nc) {
+    const int* p = cptr + s.cptr;
+    for (int q = p[i]; q < p[i + 1]; ++q) pool[s.oBs + (long long)ccol[q] * s.NRC + s.NI + i] = T(cval[q]);
+  }
+}
+
+// G = C Y (nc x nc), its Cholesky factor and inverse, FP64 (one CTA per subdomain)
+template <typename T>
+__global__ void __launch_bounds__(256) k_small_g(const DevSub* __restrict__ ds, const int* __restrict__ cptr,
+                                                 const int* __restrict__ ccol, const double* __restrict__ cval,
+                                                 const T* __restrict__ pool, double* __restrict__ small,
+                                                 int* __restrict__ err) {
+  const DevSub s = ds[blockIdx.x];
+  const int nc = s.nc, ld = max(1, s.nc);
+  extern __shared__ __align__(16) unsigned char smraw[];
+  double* g = reinterpret_cast<double*>(smraw);  // nc x nc
+  double* inv = g + ld * ld;
+  const int* p = cptr + s.cptr;
+  for (int e = threadIdx.x; e < nc * nc; e += blockDim.x) {
+    int r = e / nc, q = e % nc;
+    double t = 0.0;
+    for (int k = p[r]; k < p[r + 1]; ++k) t += cval[k] * (double)pool[s.oBs + (long long)ccol[k] * s.NRC + s.NI + q];
+    g[r * ld + q] = t;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < nc * nc; e += blockDim.x) {
+    int r = e / nc, q = e % nc;
+    if (q > r) {
+      double m = 0.5 * (g[r * ld + q] + g[q * ld + r]);
+      g[r * ld + q] = m;
+      g[q * ld + r] = m;
+    }
+  }
+  __syncthreads();
+  for (int c = 0; c < nc; ++c) {
+    if (threadIdx.x == 0) {
+      double v = g[c * ld + c];
+      if (!(v > 0.0)) { atomicOr(err, DE_PIVOT); v = 1.0; }
+      g[c * ld + c] = sqrt(v);
+    }
+    __syncthreads();
+    for (int r = c + 1 + threadIdx.x; r < nc; r += blockDim.x) g[r * ld + c] /= g[c * ld + c];
+    __syncthreads();
+    int m = nc - c - 1;
+    for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
+      int r = c + 1 + e / m, q = c + 1 + e % m;
+      if (q <= r) g[r * ld + q] -= g[r * ld + c] * g[q * ld + c];
+    }
+    __syncthreads();
+  }
+  // L^-1 column by column, then Ginv = L^-T L^-1
+  if (threadIdx.x < nc) {
+    int j = threadIdx.x;
+    for (int i = 0; i < j; ++i) inv[i * ld + j] = 0.0;
+    inv[j * ld + j] = 1.0 / g[j * ld + j];
+    for (int i = j + 1; i < nc; ++i) {
+      double t = 0.0;
+      for (int m = j; m < i; ++m) t += g[i * ld + m] * inv[m * ld + j];
+      inv[i * ld + j] = -t / g[i * ld + i];
+    }
+  }
+  __syncthreads();
+  double* Gi = small + s.oGinv;
+  for (int e = threadIdx.x; e < s.ncp * s.ncp; e += blockDim.x) {
+    int r = e / s.ncp, q = e % s.ncp;
+    double t = 0.0;
+    if (r < nc && q < nc)
+      for (int m = max(r, q); m < nc; ++m) t += inv[m * ld + r] * inv[m * ld + q];
+    Gi[e] = t;
+  }
+}
+
+// Phi = Y Ginv  (NI x ncp, preconditioner precision)
+template <typename T>
+__global__ void k_phi(const DevSub* __restrict__ ds, const T* __restrict__ pool, const double* __restrict__ small,
+                      T* __restrict__ pcpool) {
+  const DevSub s = ds[blockIdx.y];
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= s.NI * s.ncp) return;
+  int i = e / s.ncp, c = e % s.ncp;
+  double t = 0.0;
+  if (c < s.nc && i < s.ni) {
+    const T* y = pool + s.oBs + (long long)i * s.NRC + s.NI;
+    const double* gi = small + s.oGinv;
+    for (int q = 0; q < s.nc; ++q) t += (double)y[q] * gi[q * s.ncp + c];
+  }
+  pcpool[s.oPhi + e] = T(t);
+}
+
+// Z = Srho^-1 - Phi Y^T on the interface block (dense, preconditioner precision)
+template <typename T>
+__global__ void k_z(const DevSub* __restrict__ ds, const T* __restrict__ pool, T* __restrict__ pcpool) {
+  const DevSub s = ds[blockIdx.z];
+  int i = blockIdx.y * 16 + threadIdx.y, j = blockIdx.x * 16 + threadIdx.x;
+  if (i >= s.NI || j >= s.NI) return;
+  T v = T(0);
+  if (i < s.ni && j < s.ni) {
+    v = pool[s.oBs + (long long)i * s.NRC + j];
+    const T* ph = pcpool + s.oPhi + (long long)i * s.ncp;
+    const T* y = pool + s.oBs + (long long)j * s.NRC + s.NI;
+    for (int c = 0; c < s.nc; ++c) v -= ph[c] * y[c];
+  }
+  pcpool[s.oZ + (long long)i * s.NI + j] = v;
+}
+
+template <typename T>
+__global__ void k_symmetrize_t(const DevSub* __restrict__ ds, T* __restrict__ pcpool) {
+  const DevSub s = ds[blockIdx.z];
+  int i = blockIdx.y * 16 + threadIdx.y, j = blockIdx.x * 16 + threadIdx.x;
+  if (i >= s.ni || j >= s.ni || j <= i) return;
+  T* Z = pcpool + s.oZ;
+  T m = T(0.5) * (Z[(long long)i * s.NI + j] + Z[(long long)j * s.NI + i]);
+  Z[(long long)i * s.NI + j] = m;
+  Z[(long long)j * s.NI + i] = m;
+}
+
+// S Phi (into the Y columns of the preconditioner RHS block, which are no
+// longer needed), then Ac = Phi^T S Phi in FP64 accumulation
+template <typename T, typename ST>
+__global__ void k_sphi(const DevSub* __restrict__ ds, const ST* __restrict__ Spool, const T* __restrict__ pcpool,
+                       T* __restrict__ pool) {
+  const DevSub s = ds[blockIdx.y];
+  const int i = blockIdx.x;
+  if (i >= s.ni) return;
+  for (int c = threadIdx.x; c < s.nc; c += blockDim.x) {
+    T t = T(0);
+    for (int j = 0; j < s.ni; ++j)
+      t += schur_entry<T, ST>(Spool + s.oS, (long long)i * s.NI + j) * pcpool[s.oPhi + (long long)j * s.ncp + c];
+    pool[s.oBs + (long long)i * s.NRC + s.NI + c] = t;
+  }
+}
+
+template <typename T>
+__global__ void k_ac(const DevSub* __restrict__ ds, const T* __restrict__ pool, const T* __restrict__ pcpool,
+                     double* __restrict__ small) {
+  const DevSub s = ds[blockIdx.y];
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= s.nc * s.nc) return;
+  int a = e / s.nc, b = e % s.nc;
+  double t = 0.0;
+  for (int i = 0; i < s.ni; ++i)
+    t += (double)pcpool[s.oPhi + (long long)i * s.ncp + a] * (double)pool[s.oBs + (long long)i * s.NRC + s.NI + b];
+  small[s.oAc + a * s.ncp + b] = t;
+}
+
+}  // namespace bddc

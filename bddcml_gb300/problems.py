@@ -1,0 +1,239 @@
+"""Synthetic subdomain data generators for the BDDC interface solve.
+
+These build, per subdomain, exactly the arrays a caller of the
+``bddcml_upload_subdomain_data_c`` entry point hands over: element
+connectivity, local-to-global node/dof/element maps, coordinates, Dirichlet
+flags and values, the right-hand side, the initial guess and the upper-triangle
+COO triplets of the subdomain stiffness matrix.
+
+The Poisson generator restates the reference example program
+``examples/poisson_on_cube.f90``:
+
+* element matrix of the Q1 Laplacian on the reference cube, scaled by the
+  element size h (``poisson_on_cube.f90:169-177`` and ``:447``);
+* lexicographic node numbering inside a subdomain, x fastest
+  (``poisson_on_cube.f90:778-826``), element node order n1..n8 (``:836-870``);
+* homogeneous Dirichlet condition on the whole boundary of the unit cube
+  (``:812-820``);
+* right-hand side h^3 at every node, zero at fixed nodes, marked complete so
+  that interface weights are applied to it (``:433-437``);
+* upper-triangle triplets element by element, unassembled
+  (``:449-475``).
+
+A per-element coefficient ``kappa`` multiplies each element matrix; it is 1 in
+the reference example and random for the heterogeneous workloads.
+"""
+from __future__ import annotations
+
+import dataclasses
+from typing import List, Optional
+
+import numpy as np
+
+# Q1 Laplacian element matrix on [0,1]^3 with the node order of the reference
+# example (n1=(0,0,0), n2=(1,0,0), n3=(1,1,0), n4=(0,1,0), n5..n8 = +z).
+# Entries: 1/3 on the diagonal, 0 for nodes differing in one coordinate,
+# -1/12 for nodes differing in two or three coordinates.
+_NODE_OFFSETS = np.array(
+    [[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0],
+     [0, 0, 1], [1, 0, 1], [1, 1, 1], [0, 1, 1]], dtype=np.int64)
+
+
+def q1_laplace_reference_matrix() -> np.ndarray:
+    km = np.zeros((8, 8))
+    for i in range(8):
+        for j in range(8):
+            d = int(np.abs(_NODE_OFFSETS[i] - _NODE_OFFSETS[j]).sum())
+            if d == 0:
+                km[i, j] = 1.0 / 3.0
+            elif d == 1:
+                km[i, j] = 0.0
+            else:
+                km[i, j] = -1.0 / 12.0
+    return km
+
+
+@dataclasses.dataclass
+class Subdomain:
+    """Arrays of one subdomain, 0-based (numbase = 0)."""
+    isub: int
+    nelems: int
+    nnods: int
+    ndofs: int
+    inet: np.ndarray      # int32, nelems*8
+    nnet: np.ndarray      # int32, nelems
+    nndf: np.ndarray      # int32, nnods
+    isngn: np.ndarray     # int32, nnods
+    isvgvn: np.ndarray    # int32, ndofs
+    isegn: np.ndarray     # int32, nelems
+    xyz: np.ndarray       # float64, (ndim, nnods) column-major as Fortran xyz(lxyz1,lxyz2)
+    ifix: np.ndarray      # int32, ndofs
+    fixv: np.ndarray      # float64, ndofs
+    rhs: np.ndarray       # float64, ndofs
+    sol: np.ndarray       # float64, ndofs
+    i_sparse: np.ndarray  # int32, la
+    j_sparse: np.ndarray  # int32, la
+    a_sparse: np.ndarray  # float64, la
+    is_rhs_complete: int = 1
+    is_assembled: int = 0
+
+
+@dataclasses.dataclass
+class Problem:
+    name: str
+    nelem: int
+    nnod: int
+    ndof: int
+    ndim: int
+    meshdim: int
+    subdomains: List[Subdomain]
+    matrixtype: int = 1
+    # geometric description used by the checks (global structured grid)
+    n_el_edge: int = 0
+    kappa: Optional[np.ndarray] = None   # per global element (lexicographic), or None
+
+    @property
+    def nsub(self) -> int:
+        return len(self.subdomains)
+
+
+def _sub_ranges_uniform(num_el_per_sub_edge: int, num_sub_per_cube_edge: int):
+    """Box partition of the cube into equal subdomain cubes, subdomain index
+    x fastest, as ``prepare_subdomain_data`` (poisson_on_cube.f90:764-768)."""
+    boxes = []
+    for kz in range(num_sub_per_cube_edge):
+        for ky in range(num_sub_per_cube_edge):
+            for kx in range(num_sub_per_cube_edge):
+                lo = np.array([kx, ky, kz]) * num_el_per_sub_edge
+                hi = lo + num_el_per_sub_edge
+                boxes.append((lo, hi))
+    return boxes
+
+
+def box_subdomain(isub: int, lo, hi, n_el_edge: int, kappa: Optional[np.ndarray],
+                  km_ref: np.ndarray) -> Subdomain:
+    """Subdomain on the element box [lo, hi) of a structured n_el_edge^3 grid
+    of the unit cube, numbered like the reference example (x fastest)."""
+    lo = np.asarray(lo, dtype=np.int64)
+    hi = np.asarray(hi, dtype=np.int64)
+    ne = hi - lo                       # elements per direction
+    nn = ne + 1                        # nodes per direction
+    h = 1.0 / n_el_edge
+    nng = n_el_edge + 1                # global nodes per edge
+    nelems = int(np.prod(ne))
+    nnods = int(np.prod(nn))
+
+    # nodes, x fastest
+    k, j, i = np.meshgrid(np.arange(nn[2]), np.arange(nn[1]), np.arange(nn[0]), indexing="ij")
+    ig = (lo[0] + i).ravel()
+    jg = (lo[1] + j).ravel()
+    kg = (lo[2] + k).ravel()
+    isngn = (ig + jg * nng + kg * nng * nng).astype(np.int32)
+    xyz = np.empty((3, nnods))
+    xyz[0] = ig * h
+    xyz[1] = jg * h
+    xyz[2] = kg * h
+    onb = (ig == 0) | (ig == n_el_edge) | (jg == 0) | (jg == n_el_edge) | (kg == 0) | (kg == n_el_edge)
+    ifix = onb.astype(np.int32)
+    fixv = np.zeros(nnods)
+
+    # elements, x fastest
+    ek, ej, ei = np.meshgrid(np.arange(ne[2]), np.arange(ne[1]), np.arange(ne[0]), indexing="ij")
+    ei = ei.ravel(); ej = ej.ravel(); ek = ek.ravel()
+    n1 = ei + ej * nn[0] + ek * nn[0] * nn[1]
+    sx, sy = 1, nn[0]
+    sz = nn[0] * nn[1]
+    inet_e = np.stack([n1, n1 + sx, n1 + sx + sy, n1 + sy,
+                       n1 + sz, n1 + sx + sz, n1 + sx + sy + sz, n1 + sy + sz], axis=1)
+    isegn = ((lo[0] + ei) + (lo[1] + ej) * n_el_edge + (lo[2] + ek) * n_el_edge * n_el_edge).astype(np.int32)
+
+    # element matrices: upper triangle, element by element, j outer, i <= j inner
+    pairs = [(i_, j_) for j_ in range(8) for i_ in range(j_ + 1)]
+    pi = np.array([p[0] for p in pairs])
+    pj = np.array([p[1] for p in pairs])
+    idof = inet_e[:, pi]
+    jdof = inet_e[:, pj]
+    i_sp = np.minimum(idof, jdof).astype(np.int32).ravel()
+    j_sp = np.maximum(idof, jdof).astype(np.int32).ravel()
+    scale = h * (kappa[isegn] if kappa is not None else np.ones(nelems))
+    a_sp = (scale[:, None] * km_ref[pi, pj][None, :]).ravel()
+
+    rhs = np.full(nnods, h ** 3)
+    rhs[onb] = 0.0
+    return Subdomain(
+        isub=isub, nelems=nelems, nnods=nnods, ndofs=nnods,
+        inet=inet_e.astype(np.int32).ravel(), nnet=np.full(nelems, 8, dtype=np.int32),
+        nndf=np.ones(nnods, dtype=np.int32), isngn=isngn, isvgvn=isngn.copy(),
+        isegn=isegn, xyz=xyz, ifix=ifix, fixv=fixv, rhs=rhs, sol=np.zeros(nnods),
+        i_sparse=i_sp, j_sparse=j_sp, a_sparse=a_sp)
+
+
+def poisson_on_cube(num_el_per_sub_edge: int, num_sub_per_cube_edge: int,
+                    kappa: Optional[np.ndarray] = None) -> Problem:
+    """The reference example: -Laplace(u) = 1 on the unit cube, u = 0 on the
+    boundary, Q1 hexahedra, num_sub_per_cube_edge^3 cubic subdomains."""
+    n = num_el_per_sub_edge * num_sub_per_cube_edge
+    km = q1_laplace_reference_matrix()
+    subs = [box_subdomain(isub, lo, hi, n, kappa, km)
+            for isub, (lo, hi) in enumerate(_sub_ranges_uniform(num_el_per_sub_edge, num_sub_per_cube_edge))]
+    return Problem(name=f"poisson_{n}^3_{num_sub_per_cube_edge}^3subs", nelem=n ** 3,
+                   nnod=(n + 1) ** 3, ndof=(n + 1) ** 3, ndim=3, meshdim=3, subdomains=subs,
+                   n_el_edge=n, kappa=kappa)
+
+
+def poisson_boxes(n_el_edge: int, boxes, kappa: Optional[np.ndarray] = None, name="poisson_boxes") -> Problem:
+    """Poisson on the unit cube with an arbitrary box partition (list of
+    (lo, hi) element ranges that tile the grid)."""
+    km = q1_laplace_reference_matrix()
+    subs = [box_subdomain(isub, lo, hi, n_el_edge, kappa, km) for isub, (lo, hi) in enumerate(boxes)]
+    return Problem(name=name, nelem=n_el_edge ** 3, nnod=(n_el_edge + 1) ** 3, ndof=(n_el_edge + 1) ** 3,
+                   ndim=3, meshdim=3, subdomains=subs, n_el_edge=n_el_edge, kappa=kappa)
+
+
+def random_box_partition(n_el_edge: int, lo_side: int, hi_side: int, seed: int):
+    """Tensor-product box partition with side lengths drawn uniformly in
+    [lo_side, hi_side] per axis (the last box of each axis absorbs the rest)."""
+    rng = np.random.default_rng(seed)
+    cuts = []
+    for _ in range(3):
+        c = [0]
+        while c[-1] < n_el_edge:
+            s = int(rng.integers(lo_side, hi_side + 1))
+            if n_el_edge - (c[-1] + s) < lo_side:
+                s = n_el_edge - c[-1]
+            c.append(min(n_el_edge, c[-1] + s))
+        cuts.append(c)
+    boxes = []
+    for kz in range(len(cuts[2]) - 1):
+        for ky in range(len(cuts[1]) - 1):
+            for kx in range(len(cuts[0]) - 1):
+                boxes.append((np.array([cuts[0][kx], cuts[1][ky], cuts[2][kz]]),
+                              np.array([cuts[0][kx + 1], cuts[1][ky + 1], cuts[2][kz + 1]])))
+    return boxes
+
+
+def lognormal_kappa(n_el_edge: int, sigma: float, seed: int) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    return np.exp(sigma * rng.standard_normal(n_el_edge ** 3))
+
+
+def global_matrix_and_rhs(prob: Problem):
+    """Assembled global stiffness matrix and load vector with the Dirichlet
+    rows/columns eliminated (scipy CSR), used as an independent check."""
+    import scipy.sparse as sp
+    rows, cols, vals = [], [], []
+    f = np.zeros(prob.ndof)
+    fixed = np.zeros(prob.ndof, dtype=bool)
+    cnt = np.zeros(prob.ndof)
+    for s in prob.subdomains:
+        g = s.isvgvn
+        rows.append(g[s.i_sparse]); cols.append(g[s.j_sparse]); vals.append(s.a_sparse)
+        off = s.i_sparse != s.j_sparse
+        rows.append(g[s.j_sparse[off]]); cols.append(g[s.i_sparse[off]]); vals.append(s.a_sparse[off])
+        fixed[g[s.ifix != 0]] = True
+        np.add.at(f, g, s.rhs)
+        np.add.at(cnt, g, 1.0)
+    K = sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))),
+                      shape=(prob.ndof, prob.ndof))
+    f = f / np.maximum(cnt, 1.0)   # rhs is a restriction of the global rhs (complete)
+    return K, f, fixed

@@ -1,0 +1,159 @@
+/*
+ * bddcml_gb300 -- GB300-native BDDC interface solver, C ABI.
+ *
+ * Drop-in replacement for the C interface of BDDCML (reference header
+ * src/bddcml_interface_c.h).  Every entry point below has the signature of the
+ * reference function it replaces: all arguments are pointers (Fortran
+ * by-reference convention), int = c_int, double = c_double.  A Fortran caller
+ * binds them through iso_c_binding exactly as the reference's
+ * module_bddcml_c_wrapper.f90 does.
+ *
+ * Semantics follow the reference (module_bddcml.f90):
+ *   - one global solver instance per process, not thread-safe, not re-entrant
+ *     (module_levels.f90:158-175);
+ *   - call order: init -> upload_subdomain_data (every subdomain) ->
+ *     setup_preconditioner -> solve -> download_local_solution, optionally
+ *     change_subdomain_data + setup_new_data + solve, then finalize;
+ *   - numbase (0 for C, 1 for Fortran) shifts every index array and isub
+ *     (module_levels.f90:249, 718);
+ *   - inputs are copied; the caller keeps ownership of every array.
+ *
+ * Differences, all additive:
+ *   - All subdomains live on one GPU in one process: comm_init/comm_all are
+ *     accepted and ignored, nsub_loc_1 = -1 returns nsublev[0].
+ *   - The reference aborts the process on errors (module_utils.f90:296-298).
+ *     Here a failing call returns early and records a status that
+ *     bddcml_get_last_error_c() reports; the process is not aborted.
+ *   - There is no CPU fallback: without a usable CUDA device every call fails
+ *     with status BDDCML_ERR_CUDA.
+ */
+#ifndef BDDCML_GB300_H
+#define BDDCML_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+#define BDDCML_OK 0
+#define BDDCML_ERR_ARGUMENT 1    /* bad size / index / order of calls          */
+#define BDDCML_ERR_CUDA 2        /* CUDA runtime failure or no device          */
+#define BDDCML_ERR_NUMERIC 3     /* non-positive pivot, NaN, singular coarse   */
+#define BDDCML_ERR_UNSUPPORTED 4 /* feature outside the implemented scope      */
+#define BDDCML_ERR_MEMORY 5      /* device or host allocation failed           */
+
+/* ------------------------------------------------ reference entry points */
+
+/* replaces bddcml_init_c, src/bddcml_interface_c.h:6-7 (module_bddcml.f90:36-101) */
+void bddcml_init_c(int *nl, int *nsublev, int *lnsublev, int *nsub_loc_1, int *comm_init,
+                   int *verbose_level, int *numbase, int *just_direct_solve_int);
+
+/* replaces bddcml_upload_global_data_c, src/bddcml_interface_c.h:9-13.
+ * Global loading is outside the implemented path: sets BDDCML_ERR_UNSUPPORTED. */
+void bddcml_upload_global_data_c(int *nelem, int *nnod, int *ndof, int *ndim, int *meshdim,
+                                 int *inet, int *linet, int *nnet, int *lnnet, int *nndf, int *lnndf,
+                                 double *xyz, int *lxyz1, int *lxyz2,
+                                 int *ifix, int *lifix, double *fixv, int *lfixv, double *rhs, int *lrhs,
+                                 double *sol, int *lsol, int *idelm,
+                                 int *neighbouring, int *load_division_int);
+
+/* replaces bddcml_upload_subdomain_data_c, src/bddcml_interface_c.h:15-27
+ * (module_bddcml.f90:186-356, module_levels.f90:615-782) */
+void bddcml_upload_subdomain_data_c(int *nelem, int *nnod, int *ndof, int *ndim, int *meshdim,
+                                    int *isub, int *nelems, int *nnods, int *ndofs,
+                                    int *inet, int *linet, int *nnet, int *lnnet, int *nndf, int *lnndf,
+                                    int *isngn, int *lisngn, int *isvgvn, int *lisvgvn, int *isegn, int *lisegn,
+                                    double *xyz, int *lxyz1, int *lxyz2,
+                                    int *ifix, int *lifix, double *fixv, int *lfixv,
+                                    double *rhs, int *lrhs, int *is_rhs_complete,
+                                    double *sol, int *lsol,
+                                    int *matrixtype, int *i_sparse, int *j_sparse, double *a_sparse, int *la,
+                                    int *is_assembled_int,
+                                    double *user_constraints, int *luser_constraints1, int *luser_constraints2,
+                                    double *element_data, int *lelement_data1, int *lelement_data2,
+                                    double *dof_data, int *ldof_data,
+                                    int *find_components_int, int *use_dual_mesh_graph_int, int *neighbouring);
+
+/* replaces bddcml_setup_preconditioner_c, src/bddcml_interface_c.h:29-35
+ * (module_bddcml.f90:359-455, module_levels.f90:905-1069) */
+void bddcml_setup_preconditioner_c(int *matrixtype, int *use_defaults_int, int *parallel_division_int,
+                                   int *use_corner_constraints_int, int *use_arithmetic_constraints_int,
+                                   int *use_adaptive_constraints_int, int *use_user_constraints_int,
+                                   int *weights_type);
+
+/* replaces bddcml_solve_c, src/bddcml_interface_c.h:37-39 (module_bddcml.f90:459-567).
+ * method 0 (PCG) is implemented; -1 selects the reference defaults, whose
+ * method is BiCGSTAB (module_bddcml.f90:515) and is reported unsupported. */
+void bddcml_solve_c(int *comm_all, int *method, double *tol, int *maxit, int *ndecrmax,
+                    int *recycling_int, int *max_number_of_stored_vectors,
+                    int *num_iter, int *converged_reason, double *condition_number);
+
+/* replaces bddcml_download_local_solution_c, src/bddcml_interface_c.h:41 */
+void bddcml_download_local_solution_c(int *isub, double *sols, int *lsols);
+
+/* replaces bddcml_download_global_solution_c, src/bddcml_interface_c.h:43 (unsupported) */
+void bddcml_download_global_solution_c(double *sol, int *lsol);
+
+/* replaces bddcml_download_local_reactions_c, src/bddcml_interface_c.h:45 (unsupported) */
+void bddcml_download_local_reactions_c(int *isub, double *reas, int *lreas);
+
+/* replaces bddcml_download_global_reactions_c, src/bddcml_interface_c.h:47 (unsupported) */
+void bddcml_download_global_reactions_c(double *rea, int *lrea);
+
+/* replaces bddcml_change_global_data_c, src/bddcml_interface_c.h:49 (unsupported) */
+void bddcml_change_global_data_c(int *ifix, int *lifix, double *fixv, int *lfixv, double *rhs, int *lrhs,
+                                 double *sol, int *lsol);
+
+/* replaces bddcml_change_subdomain_data_c, src/bddcml_interface_c.h:51-54
+ * (module_levels.f90:785-849) */
+void bddcml_change_subdomain_data_c(int *isub, int *ifix, int *lifix, double *fixv, int *lfixv,
+                                    double *rhs, int *lrhs, int *is_rhs_complete, double *sol, int *lsol);
+
+/* replaces bddcml_setup_new_data_c, src/bddcml_interface_c.h:56 (module_levels.f90:852-903) */
+void bddcml_setup_new_data_c(void);
+
+/* replaces bddcml_dotprod_subdomain_c, src/bddcml_interface_c.h:58 (module_dd.f90:12736-12788) */
+void bddcml_dotprod_subdomain_c(int *isub, double *vec1, int *lvec1, double *vec2, int *lvec2, double *dotprod);
+
+/* replaces bddcml_finalize_c, src/bddcml_interface_c.h:60 */
+void bddcml_finalize_c(void);
+
+/* ------------------------------------------------------------ extensions */
+
+/* Status of the last call (BDDCML_OK ... BDDCML_ERR_MEMORY); copies a
+ * NUL-terminated message into msg (at most *lmsg bytes, may be NULL).  The
+ * reference aborts instead (module_utils.f90:265-298); this has no
+ * counterpart there. */
+int bddcml_get_last_error_c(char *msg, int *lmsg);
+
+/* Arithmetic of the subdomain factors, Schur-complement preconditioner blocks
+ * and coarse basis: 0 = plain FP64 everywhere, 1 = mixed (FP32 factors and
+ * preconditioner blocks with FP64 refinement of the Schur operator; FP64 PCG
+ * vectors, dot products, weights and coarse solve).  Default 1.  Must be set
+ * before bddcml_setup_preconditioner_c.  No counterpart in the reference. */
+void bddcml_set_precision_c(int *mode);
+
+/* Timing and size report of the last setup and solve, filled into stats
+ * (length *lstats, up to 32 doubles; see bddcml_gb300/__init__.py for the
+ * field list).  No counterpart in the reference. */
+void bddcml_get_stats_c(double *stats, int *lstats);
+
+/* Relative residual history of the last PCG solve (at most *lhist values);
+ * *lhist returns the number of iterations recorded.  Corresponds to the
+ * per-iteration residual print of module_krylov.f90:769-772. */
+void bddcml_get_residual_history_c(double *hist, int *lhist);
+
+/* Copies the interface weights of subdomain *isub (ndofi values, subdomain
+ * interface order) for checking; no counterpart in the reference. */
+void bddcml_get_interface_weights_c(int *isub, double *wi, int *lwi);
+
+/* Structural summary of the coarse space: out = {ncorner, nedge, nface,
+ * ndofc, sum ndofi, sum ndofo}.  Corresponds to the level summary of
+ * module_levels.f90:2240-2300 (printed there, returned here). */
+void bddcml_get_coarse_info_c(int *out, int *lout);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BDDCML_GB300_H */

@@ -1,0 +1,1326 @@
+// BDDC oracle: CPU restatement of the reference BDDC interface-PCG path.
+//
+// TEST INFRASTRUCTURE ONLY.  This file is the checker for the GPU library in
+// bddcml_gb300/: only tests/, __graft_entry__.smoke() and bench.py's
+// cpu_baseline / reference legs may load it.  The product never links it.
+//
+// Parity status: unpinned against the reference's own outputs.  The reference
+// (Fortran 95 + MPI + MUMPS + METIS + LAPACK) cannot be compiled here and ships
+// no golden solver numbers; this restatement is pinned instead against direct
+// sparse solves of the assembled global system (tests/test_oracle.py) and
+// against structural invariants of the coarse space.
+//
+// What it restates (file:line in the reference project):
+//   upload + matrix assembly ....... module_levels.f90:615-782, module_sm.f90:630-684
+//   neighbours / interface ......... module_dd.f90:8071-8648 (dd_create_neighbouring),
+//                                    module_utils.f90:878-945 (sorted intersection)
+//   globs, corners, BC removal ..... module_dd.f90:8925-10016 (dd_create_globs),
+//                                    10017-10327 (select_corners), 10329-10555 (coarse numbering)
+//   BC elimination ................. module_dd.f90:1081-1256, module_sm.f90:431-600
+//   interior factor (A11) .......... module_dd.f90:3983-4295 (blocking + factorisation)
+//   weights ........................ module_dd.f90:11554-11722, 11800-11878
+//   arithmetic constraints, C ...... module_dd.f90:4298-4384, 4869-5144, 11011-11235
+//   augmented factor, coarse basis . module_dd.f90:5211-5799
+//   reduced rhs, interior resolve .. module_dd.f90:6995-7257, 6811-6932
+//   Schur apply .................... module_dd.f90:6564-6699
+//   exchange (upload/download) ..... module_dd.f90:11236-11551
+//   BDDC apply ..................... module_levels.f90:3627-4346
+//   PCG + Lanczos estimate ......... module_krylov.f90:48-945, 2061-2118
+//   coarse problem ................. module_levels.f90:3001-3170, 4029-4061
+//
+// The direct solver MUMPS is replaced by band Cholesky factorisations in the
+// subdomain's own dof order.  The saddle-point system [A C^T; C 0] that the
+// reference factors with a symmetric indefinite MUMPS (SYM=2) is solved here by
+// an equivalent exact formulation: with A_r = A + sum_corner_dofs d_k e_k e_k^T
+// (SPD once the corner constraints remove the kernel of A, and still banded),
+// z = A_r^{-1}(f - C^T mu), mu = (C A_r^{-1} C^T)^{-1} C A_r^{-1} f.  On the
+// constraint set C z = 0, A_r z = A z, so the solution is that of the
+// reference system.  The coarse matrix is Phi^T A Phi, which equals the
+// reference's -lambda (module_dd.f90:5615-5625) in exact arithmetic.
+#include <algorithm>
+#include <array>
+#include <climits>
+#include <cstdint>
+#include <functional>
+#include <unordered_map>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <numeric>
+#include <stdexcept>
+#include <string>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+using std::vector;
+
+namespace {
+
+struct Band {
+  // lower band Cholesky factor: L(i,j) for i-b <= j <= i stored at v[i*(b+1) + (j-i+b)]
+  int n = 0, b = 0;
+  vector<double> v;
+  double& at(int i, int j) { return v[(size_t)i * (b + 1) + (j - i + b)]; }
+  double at(int i, int j) const { return v[(size_t)i * (b + 1) + (j - i + b)]; }
+  void factor() {
+    for (int i = 0; i < n; ++i) {
+      int j0 = std::max(0, i - b);
+      for (int j = j0; j <= i; ++j) {
+        double s = at(i, j);
+        int k0 = std::max(j0, j - b);
+        const double* li = &v[(size_t)i * (b + 1) + (k0 - i + b)];
+        const double* lj = &v[(size_t)j * (b + 1) + (k0 - j + b)];
+        for (int k = 0; k < j - k0; ++k) s -= li[k] * lj[k];
+        if (i == j) {
+          if (!(s > 0.0)) throw std::runtime_error("band Cholesky: non-positive pivot");
+          at(i, i) = std::sqrt(s);
+        } else {
+          at(i, j) = s / at(j, j);
+        }
+      }
+    }
+  }
+  void solve(double* x) const {  // L L^T x = rhs, in place
+    for (int i = 0; i < n; ++i) {
+      double s = x[i];
+      int j0 = std::max(0, i - b);
+      for (int j = j0; j < i; ++j) s -= at(i, j) * x[j];
+      x[i] = s / at(i, i);
+    }
+    for (int i = n - 1; i >= 0; --i) {
+      x[i] /= at(i, i);
+      double xi = x[i];
+      int j0 = std::max(0, i - b);
+      for (int j = j0; j < i; ++j) x[j] -= at(i, j) * xi;
+    }
+  }
+};
+
+// dense symmetric positive definite (small): Cholesky in place, row-major n x n
+static void dense_chol(vector<double>& a, int n, int nthreads = 1) {
+  for (int j = 0; j < n; ++j) {
+    double s = a[(size_t)j * n + j];
+    for (int k = 0; k < j; ++k) s -= a[(size_t)j * n + k] * a[(size_t)j * n + k];
+    if (!(s > 0.0)) throw std::runtime_error("dense Cholesky: non-positive pivot");
+    double d = std::sqrt(s);
+    a[(size_t)j * n + j] = d;
+#pragma omp parallel for schedule(static) num_threads(nthreads) if (n - j > 256 && nthreads > 1)
+    for (int i = j + 1; i < n; ++i) {
+      double t = a[(size_t)i * n + j];
+      for (int k = 0; k < j; ++k) t -= a[(size_t)i * n + k] * a[(size_t)j * n + k];
+      a[(size_t)i * n + j] = t / d;
+    }
+  }
+}
+static void dense_chol_solve(const vector<double>& l, int n, double* x) {
+  for (int i = 0; i < n; ++i) {
+    double s = x[i];
+    for (int k = 0; k < i; ++k) s -= l[(size_t)i * n + k] * x[k];
+    x[i] = s / l[(size_t)i * n + i];
+  }
+  for (int i = n - 1; i >= 0; --i) {
+    double s = x[i];
+    for (int k = i + 1; k < n; ++k) s -= l[(size_t)k * n + i] * x[k];
+    x[i] = s / l[(size_t)i * n + i];
+  }
+}
+
+// COO sort + merge of duplicates (module_sm.f90:630-684 sm_assembly)
+static void coo_assemble(vector<int>& ia, vector<int>& ja, vector<double>& a) {
+  size_t n = ia.size();
+  vector<size_t> p(n);
+  std::iota(p.begin(), p.end(), 0);
+  std::sort(p.begin(), p.end(), [&](size_t x, size_t y) {
+    return ia[x] != ia[y] ? ia[x] < ia[y] : ja[x] < ja[y];
+  });
+  vector<int> ni, nj;
+  vector<double> na;
+  ni.reserve(n); nj.reserve(n); na.reserve(n);
+  for (size_t k = 0; k < n; ++k) {
+    size_t q = p[k];
+    if (!ni.empty() && ni.back() == ia[q] && nj.back() == ja[q]) na.back() += a[q];
+    else { ni.push_back(ia[q]); nj.push_back(ja[q]); na.push_back(a[q]); }
+  }
+  ia.swap(ni); ja.swap(nj); a.swap(na);
+}
+
+static int find_index(const vector<int>& v, int x) {  // first position, -1 if absent
+  for (size_t i = 0; i < v.size(); ++i) if (v[i] == x) return (int)i;
+  return -1;
+}
+
+struct Cnode {
+  int itype = 0;            // 3 corner, 2 edge, 1 face
+  int global_cnode = 0;     // 1-based global coarse node number
+  vector<int> insin;        // interface node indices
+  vector<int> ivsivn;       // interface dof indices
+  int nvar = 0;
+  int ncdof = 0;            // constraints loaded
+  vector<double> matrix;    // ncdof x nvar row-major
+  bool used = false;
+  vector<int> igcdof;       // global coarse dofs (1-based)
+};
+
+struct Sub {
+  int isub = 0;  // 1-based
+  int nelem = 0, nnod = 0, ndof = 0, ndim = 0;
+  vector<int> inet, nnet, nndf, isngn, isvgvn, isegn, ifix;
+  vector<double> xyz;  // xyz[d*nnod + i]
+  vector<double> fixv, rhs, sol;
+  bool rhs_complete = true;
+  int matrixtype = 1;
+  vector<int> ia, ja;  // 0-based, upper triangle
+  vector<double> a;
+  bool bc_present = false;
+  vector<int> comp;  // nodal components (1-based)
+  // neighbours / interface
+  vector<int> iadj, nshnadj, ishnadj, ishnncadj;
+  vector<int> iin, iivsvn, iovsvn;
+  int nnodi = 0, ndofi = 0, ndofo = 0;
+  vector<int> kdof;  // first dof of each node
+  vector<int> kdofi; // first interface dof of each interface node (size nnodi+1)
+  vector<int> xch_mine, xch_theirs, xch_ptr;  // exchange lists per neighbour (interface dof positions)
+  // coarse space
+  vector<int> icnsin;  // interface node index of corners (sorted by global id)
+  vector<int> global_corner_number;
+  vector<Cnode> cnodes;
+  int nconstr = 0;
+  vector<int> crow_ptr, crow_col;  // C in CSR over interface dofs
+  vector<double> crow_val;
+  vector<int> indrowc;             // global coarse dof of each row (1-based)
+  // weights
+  vector<double> wi;
+  // BC
+  vector<double> bc;
+  // factors
+  Band a11;                 // interior block in iovsvn order
+  vector<int> c11_ptr, c11_col; vector<double> c11_val;  // full symmetric CSR of interior block (for checks)
+  vector<int> a12_ptr, a12_col; vector<double> a12_val;  // CSR rows = interior, cols = interface
+  vector<int> a22_ptr, a22_col; vector<double> a22_val;  // full symmetric CSR on interface
+  Band aug;                 // A + corner shifts, full subdomain order
+  vector<double> yaug;      // ndof x nconstr (column-major: yaug[c*ndof + i])
+  vector<double> gchol;     // nconstr x nconstr Cholesky of C A_r^-1 C^T
+  vector<double> phisi;     // ndofi x nconstr (column-major)
+  vector<double> coarsem;   // nconstr x nconstr dense Phi^T A Phi
+  vector<double> g, solo;
+  // full symmetric CSR of the whole (BC-eliminated) matrix
+  vector<int> f_ptr, f_col; vector<double> f_val;
+};
+
+struct Oracle {
+  int nsub = 0;
+  int nthreads = 1;
+  vector<Sub> subs;
+  bool setup_done = false;
+  int ncorner = 0, nedge = 0, nface = 0, ndofc = 0;
+  vector<double> coarse_chol;  // dense Cholesky of the coarse matrix
+  vector<int> ncdof_of_cnode;  // nndfc
+  std::string err;
+  // PCG results
+  vector<double> relres_hist;
+};
+
+// ---------------------------------------------------------------- helpers
+static void sym_csr_from_upper(int n, const vector<int>& ia, const vector<int>& ja, const vector<double>& a,
+                               vector<int>& ptr, vector<int>& col, vector<double>& val) {
+  vector<int> cnt(n + 1, 0);
+  for (size_t k = 0; k < ia.size(); ++k) {
+    cnt[ia[k] + 1]++;
+    if (ia[k] != ja[k]) cnt[ja[k] + 1]++;
+  }
+  for (int i = 0; i < n; ++i) cnt[i + 1] += cnt[i];
+  ptr = cnt;
+  col.assign(ptr[n], 0);
+  val.assign(ptr[n], 0.0);
+  vector<int> pos(ptr.begin(), ptr.end() - 1);
+  for (size_t k = 0; k < ia.size(); ++k) {
+    col[pos[ia[k]]] = ja[k]; val[pos[ia[k]]++] = a[k];
+    if (ia[k] != ja[k]) { col[pos[ja[k]]] = ia[k]; val[pos[ja[k]]++] = a[k]; }
+  }
+}
+
+static void csr_mult(const vector<int>& ptr, const vector<int>& col, const vector<double>& val,
+                     const double* x, double* y, int nrow) {
+  for (int i = 0; i < nrow; ++i) {
+    double s = 0.0;
+    for (int k = ptr[i]; k < ptr[i + 1]; ++k) s += val[k] * x[col[k]];
+    y[i] = s;
+  }
+}
+
+// nodal components from the dual mesh graph (module_dd.f90:2516-2770):
+// elements sharing at least `neighbouring` nodes are connected.
+static void nodal_components(Sub& s, bool find_components, int neighbouring) {
+  s.comp.assign(s.nnod, 1);
+  if (!find_components || s.nelem == 0) return;
+  vector<int> kinet(s.nelem + 1, 0);
+  for (int e = 0; e < s.nelem; ++e) kinet[e + 1] = kinet[e] + s.nnet[e];
+  vector<vector<int>> node_elems(s.nnod);
+  for (int e = 0; e < s.nelem; ++e)
+    for (int k = kinet[e]; k < kinet[e + 1]; ++k) node_elems[s.inet[k]].push_back(e);
+  vector<int> ecomp(s.nelem, 0);
+  int ncomp = 0;
+  vector<int> cntshared(s.nelem, 0), touched;
+  for (int e0 = 0; e0 < s.nelem; ++e0) {
+    if (ecomp[e0]) continue;
+    ++ncomp;
+    vector<int> stack{e0};
+    ecomp[e0] = ncomp;
+    while (!stack.empty()) {
+      int e = stack.back(); stack.pop_back();
+      touched.clear();
+      for (int k = kinet[e]; k < kinet[e + 1]; ++k)
+        for (int f : node_elems[s.inet[k]]) {
+          if (f == e) continue;
+          if (cntshared[f]++ == 0) touched.push_back(f);
+        }
+      for (int f : touched) {
+        if (cntshared[f] >= neighbouring && !ecomp[f]) { ecomp[f] = ncomp; stack.push_back(f); }
+        cntshared[f] = 0;
+      }
+    }
+  }
+  for (int e = 0; e < s.nelem; ++e)
+    for (int k = kinet[e]; k < kinet[e + 1]; ++k) s.comp[s.inet[k]] = ecomp[e];
+}
+
+static vector<int> sorted_intersection(vector<int> a, vector<int> b) {
+  std::sort(a.begin(), a.end());
+  std::sort(b.begin(), b.end());
+  vector<int> out;
+  std::set_intersection(a.begin(), a.end(), b.begin(), b.end(), std::back_inserter(out));
+  return out;
+}
+
+}  // namespace
+
+// ============================================================ neighbours
+static void create_neighbouring(Oracle& o) {
+  int nsub = o.nsub;
+  // guess by node-id ranges and coordinate bounding boxes (module_dd.f90:8649-8924);
+  // the guess only has to be a superset, the intersection decides.
+  vector<int> lo(nsub), hi(nsub);
+  vector<double> bmin(3 * nsub), bmax(3 * nsub);
+  for (int s = 0; s < nsub; ++s) {
+    auto& S = o.subs[s];
+    lo[s] = *std::min_element(S.isngn.begin(), S.isngn.end());
+    hi[s] = *std::max_element(S.isngn.begin(), S.isngn.end());
+    for (int d = 0; d < S.ndim; ++d) {
+      const double* x = &S.xyz[(size_t)d * S.nnod];
+      bmin[3 * s + d] = *std::min_element(x, x + S.nnod);
+      bmax[3 * s + d] = *std::max_element(x, x + S.nnod);
+    }
+  }
+  vector<vector<int>> sorted_ids(nsub);
+  for (int s = 0; s < nsub; ++s) { sorted_ids[s] = o.subs[s].isngn; std::sort(sorted_ids[s].begin(), sorted_ids[s].end()); }
+#pragma omp parallel for schedule(dynamic) num_threads(o.nthreads)
+  for (int s = 0; s < nsub; ++s) {
+    auto& S = o.subs[s];
+    std::map<int, int> gid2loc;
+    for (int i = 0; i < S.nnod; ++i) gid2loc.emplace(S.isngn[i], i);
+    vector<int> kinodes(S.nnod, 0);
+    vector<vector<int>> shared_g;  // per actual neighbour, sorted global ids
+    vector<int> adj;
+    for (int t = 0; t < nsub; ++t) {
+      if (t == s) continue;
+      if (lo[s] > hi[t] || hi[s] < lo[t]) continue;
+      bool bb = true;
+      for (int d = 0; d < S.ndim; ++d) {
+        double tol = 1e-9 * (1.0 + std::fabs(bmax[3 * s + d]) + std::fabs(bmax[3 * t + d]));
+        if (bmin[3 * s + d] > bmax[3 * t + d] + tol || bmax[3 * s + d] < bmin[3 * t + d] - tol) bb = false;
+      }
+      if (!bb) continue;
+      vector<int> inter;
+      std::set_intersection(sorted_ids[s].begin(), sorted_ids[s].end(), sorted_ids[t].begin(), sorted_ids[t].end(),
+                            std::back_inserter(inter));
+      if (inter.empty()) continue;
+      adj.push_back(t + 1);
+      for (int g : inter) kinodes[gid2loc[g]]++;
+      shared_g.push_back(std::move(inter));
+    }
+    // interface: nodes shared with anybody, in local order (module_dd.f90:8410-8470)
+    S.kdof.assign(S.nnod, 0);
+    for (int i = 1; i < S.nnod; ++i) S.kdof[i] = S.kdof[i - 1] + S.nndf[i - 1];
+    S.iin.clear(); S.iivsvn.clear(); S.iovsvn.clear();
+    vector<int> inodi_of(S.nnod, -1);
+    for (int i = 0; i < S.nnod; ++i) {
+      if (kinodes[i] > 0) {
+        inodi_of[i] = (int)S.iin.size();
+        S.iin.push_back(i);
+        for (int d = 0; d < S.nndf[i]; ++d) S.iivsvn.push_back(S.kdof[i] + d);
+      } else {
+        for (int d = 0; d < S.nndf[i]; ++d) S.iovsvn.push_back(S.kdof[i] + d);
+      }
+    }
+    S.nnodi = (int)S.iin.size();
+    S.ndofi = (int)S.iivsvn.size();
+    S.ndofo = (int)S.iovsvn.size();
+    S.iadj = adj;
+    S.nshnadj.clear(); S.ishnadj.clear(); S.ishnncadj.clear();
+    for (size_t a = 0; a < adj.size(); ++a) {
+      auto& T = o.subs[adj[a] - 1];
+      S.nshnadj.push_back((int)shared_g[a].size());
+      std::unordered_map<int, int> tloc;
+      for (int i = 0; i < T.nnod; ++i) tloc.emplace(T.isngn[i], i);
+      for (int g : shared_g[a]) {
+        S.ishnadj.push_back(inodi_of[gid2loc[g]]);
+        S.ishnncadj.push_back(T.comp[tloc.at(g)]);
+      }
+    }
+  }
+}
+
+// ================================================================ globs
+static void create_globs(Oracle& o, bool use_corner_constraints, int meshdim) {
+  int nsub = o.nsub;
+  struct Aux {
+    vector<int> nsubnode;                // per interface node
+    vector<vector<std::array<int, 3>>> globsubs;
+    vector<int> globtypes, kglobs;
+    vector<int> icgn;                    // corners by global node id
+    int ncorners = 0, nedges = 0, nfaces = 0;
+    vector<int> iegn, ifgn;
+    vector<int> icgcn, iegcn, ifgcn;
+    vector<int> iingns;
+  };
+  vector<Aux> aux(nsub);
+  // ---- pass 1: classification + corner selection (module_dd.f90:9099-9276, 10017-10327)
+  for (int s = 0; s < nsub; ++s) {
+    auto& S = o.subs[s];
+    auto& A = aux[s];
+    int nnodi = S.nnodi;
+    A.nsubnode.assign(nnodi, 0);
+    A.globsubs.assign(nnodi, {});
+    int k = 0;
+    for (size_t ia = 0; ia < S.iadj.size(); ++ia) {
+      for (int ish = 0; ish < S.nshnadj[ia]; ++ish) {
+        int inodi = S.ishnadj[k + ish];
+        int mycomp = S.comp[S.iin[inodi]];
+        A.nsubnode[inodi]++;
+        A.globsubs[inodi].push_back({S.iadj[ia], S.ishnncadj[k + ish], mycomp});
+      }
+      k += S.nshnadj[ia];
+    }
+    for (int i = 0; i < nnodi; ++i)
+      if (A.nsubnode[i] == 0) throw std::runtime_error("interface coverage by globs failed");
+    A.globtypes.assign(nnodi, 0);
+    A.kglobs.assign(nnodi, -1);
+    int iglobs = 0;
+    for (int i = 0; i < nnodi; ++i) {
+      if (A.kglobs[i] != -1) continue;
+      ++iglobs;
+      A.kglobs[i] = iglobs;
+      int nsubn = A.nsubnode[i];
+      int nglobn = 1;
+      for (int j = i + 1; j < nnodi; ++j) {
+        if (A.kglobs[j] == -1 && A.globtypes[j] != 3 && A.nsubnode[j] == nsubn && A.globsubs[j] == A.globsubs[i]) {
+          A.kglobs[j] = iglobs;
+          nglobn++;
+          A.globtypes[j] = (nsubn == 1) ? 1 : 2;
+        }
+      }
+      if (nsubn == 1) A.globtypes[i] = 1;
+      else A.globtypes[i] = (nglobn > 1) ? 2 : 3;
+    }
+    for (int i = 0; i < nnodi; ++i) if (A.nsubnode[i] == 1) A.globtypes[i] = 1;
+    if (use_corner_constraints) {
+      int kk = 0;
+      for (size_t ia = 0; ia < S.iadj.size(); ++ia) {
+        int nshn = S.nshnadj[ia];
+        bool face = false;
+        for (int ish = 0; ish < nshn; ++ish)
+          if (A.globtypes[S.ishnadj[kk + ish]] == 1) { face = true; break; }
+        if (face) {
+          // interface components (check_face_components = .true.)
+          vector<int> myc(nshn), adjc(nshn);
+          for (int ish = 0; ish < nshn; ++ish) {
+            myc[ish] = S.comp[S.iin[S.ishnadj[kk + ish]]];
+            adjc[ish] = S.ishnncadj[kk + ish];
+          }
+          auto compress = [](vector<int>& v) {
+            int mx = *std::max_element(v.begin(), v.end());
+            int nw = 0;
+            for (int old = 1; old <= mx; ++old) {
+              if (std::find(v.begin(), v.end(), old) != v.end()) {
+                ++nw;
+                for (auto& x : v) if (x == old) x = nw;
+              }
+            }
+            return nw;
+          };
+          compress(myc);
+          int nadjc = compress(adjc);
+          vector<int> ic(nshn);
+          for (int ish = 0; ish < nshn; ++ish) ic[ish] = (myc[ish] - 1) * nadjc + adjc[ish];
+          int nic = compress(ic);
+          for (int icomp = 1; icomp <= nic; ++icomp) {
+            vector<int> compind;
+            for (int ish = 0; ish < nshn; ++ish) if (ic[ish] == icomp) compind.push_back(ish);
+            int m = (int)compind.size();
+            int ndim = S.ndim;
+            vector<double> xs(m * 3, 0.0);
+            for (int c = 0; c < m; ++c) {
+              int nd = S.iin[S.ishnadj[kk + compind[c]]];
+              for (int d = 0; d < ndim; ++d) xs[c * 3 + d] = S.xyz[(size_t)d * S.nnod + nd];
+            }
+            int inodcf[4] = {0, 0, 0, 0};  // 1-based positions, 0 = none
+            auto farthest_from = [&](int base) {
+              double best = -1.0; int loc = 0;
+              for (int c = 0; c < m; ++c) {
+                double dist = 0.0;
+                for (int d = 0; d < ndim; ++d) { double t = xs[c * 3 + d] - xs[base * 3 + d]; dist += t * t; }
+                if (dist > best) { best = dist; loc = c; }  // maxloc: first maximum
+              }
+              return loc + 1;
+            };
+            if (m > 0) inodcf[0] = farthest_from(0);
+            if (meshdim > 1 && m > 1) {
+              inodcf[1] = farthest_from(inodcf[0] - 1);
+              if (inodcf[1] == inodcf[0]) {
+                for (int c = 1; c <= m; ++c) if (c != inodcf[0]) { inodcf[1] = c; break; }
+              }
+            }
+            if (meshdim > 2 && m > 2) {
+              double x1 = xs[(inodcf[0] - 1) * 3], y1 = xs[(inodcf[0] - 1) * 3 + 1], z1 = xs[(inodcf[0] - 1) * 3 + 2];
+              double x2 = xs[(inodcf[1] - 1) * 3], y2 = xs[(inodcf[1] - 1) * 3 + 1], z2 = xs[(inodcf[1] - 1) * 3 + 2];
+              vector<double> area(m);
+              for (int c = 0; c < m; ++c) {
+                double xi = xs[c * 3], yi = xs[c * 3 + 1], zi = xs[c * 3 + 2];
+                double t1 = (y2 - y1) * (zi - z1) - (yi - y1) * (z2 - z1);
+                double t2 = (x2 - x1) * (zi - z1) - (xi - x1) * (z2 - z1);
+                double t3 = (x2 - x1) * (yi - y1) - (xi - x1) * (y2 - y1);
+                area[c] = t1 * t1 + t2 * t2 + t3 * t3;
+              }
+              for (int round = 1; round <= 2; ++round) {
+                double maxv = 0.0; int maxl = 0;
+                if (round == 1) { for (int c = 0; c < m; ++c) if (area[c] > maxv) { maxv = area[c]; maxl = c + 1; } }
+                else { for (int c = m - 1; c >= 0; --c) if (area[c] > maxv) { maxv = area[c]; maxl = c + 1; } }
+                inodcf[1 + round] = maxl;
+              }
+              if ((inodcf[2] == inodcf[0] && inodcf[3] == inodcf[0]) || (inodcf[2] == inodcf[1] && inodcf[3] == inodcf[1])) {
+                for (int c = 1; c <= m; ++c) if (c != inodcf[0] && c != inodcf[1]) { inodcf[2] = c; break; }
+                for (int c = 1; c <= m; ++c) if (c != inodcf[0] && c != inodcf[1] && c != inodcf[2]) { inodcf[3] = c; break; }
+              }
+            }
+            int end_bound = meshdim <= 2 ? 2 : 4;
+            for (int i = 0; i < end_bound; ++i)
+              if (inodcf[i] != 0) A.globtypes[S.ishnadj[kk + compind[inodcf[i] - 1]]] = 3;
+          }
+        }
+        kk += nshn;
+      }
+    }
+    A.icgn.clear();
+    for (int i = 0; i < nnodi; ++i) if (A.globtypes[i] == 3) A.icgn.push_back(S.isngn[S.iin[i]]);
+    A.iingns.resize(nnodi);
+    for (int i = 0; i < nnodi; ++i) A.iingns[i] = S.isngn[S.iin[i]];
+  }
+  // ---- corner merge across neighbours (module_dd.f90:9296-9385)
+  vector<vector<int>> newicgn(nsub);
+  for (int s = 0; s < nsub; ++s) {
+    auto& S = o.subs[s];
+    vector<int> merge = aux[s].icgn;
+    for (int t : S.iadj) merge.insert(merge.end(), aux[t - 1].icgn.begin(), aux[t - 1].icgn.end());
+    std::sort(merge.begin(), merge.end());
+    merge.erase(std::unique(merge.begin(), merge.end()), merge.end());
+    newicgn[s] = sorted_intersection(aux[s].iingns, merge);
+  }
+  for (int s = 0; s < nsub; ++s) {
+    aux[s].icgn = newicgn[s];
+    aux[s].ncorners = (int)aux[s].icgn.size();
+    for (int g : aux[s].icgn) aux[s].globtypes[find_index(aux[s].iingns, g)] = 3;
+  }
+  // ---- coarse numbering of a class of entities (module_dd.f90:10329-10555)
+  auto number = [&](int shift, std::function<vector<int>&(Aux&)> gidx, std::function<vector<int>&(Aux&)> gcidx) {
+    vector<int> nuniq(nsub + 1, 0);
+    for (int s = 0; s < nsub; ++s) {
+      auto& A = aux[s];
+      int isub = s + 1, cnt = 0;
+      for (int g : gidx(A)) {
+        int inodi = find_index(A.iingns, g);
+        int mn = isub;
+        for (auto& t : A.globsubs[inodi]) mn = std::min(mn, t[0]);
+        if (mn == isub) cnt++;
+      }
+      nuniq[s] = cnt;
+    }
+    vector<int> start(nsub + 1);
+    start[0] = 1;
+    for (int s = 0; s < nsub; ++s) start[s + 1] = start[s] + nuniq[s];
+    int ncoarse = start[nsub] - 1;
+    std::map<int, int> owned;  // global entity id -> coarse number
+    for (int s = 0; s < nsub; ++s) {
+      auto& A = aux[s];
+      auto& S = o.subs[s];
+      auto& gi = gidx(A);
+      auto& gc = gcidx(A);
+      gc.assign(gi.size(), 0);
+      int indcg = start[s];
+      int isub = s + 1;
+      for (int inodi = 0; inodi < S.nnodi; ++inodi) {
+        int g = A.iingns[inodi];
+        int pos = find_index(gi, g);
+        if (pos < 0) continue;
+        int mn = isub;
+        for (auto& t : A.globsubs[inodi]) mn = std::min(mn, t[0]);
+        if (mn == isub) { gc[pos] = shift + indcg; owned[g] = shift + indcg; indcg++; }
+      }
+    }
+    for (int s = 0; s < nsub; ++s) {
+      auto& gi = gidx(aux[s]);
+      auto& gc = gcidx(aux[s]);
+      for (size_t k = 0; k < gi.size(); ++k)
+        if (gc[k] == 0) {
+          auto it = owned.find(gi[k]);
+          if (it == owned.end()) throw std::runtime_error("coarse entity without owner");
+          gc[k] = it->second;
+        }
+    }
+    return ncoarse;
+  };
+  o.ncorner = number(0, [](Aux& A) -> vector<int>& { return A.icgn; }, [](Aux& A) -> vector<int>& { return A.icgcn; });
+  for (int s = 0; s < nsub; ++s) {
+    auto& S = o.subs[s];
+    auto& A = aux[s];
+    S.icnsin.assign(A.ncorners, -1);
+    for (int c = 0; c < A.ncorners; ++c) S.icnsin[c] = find_index(A.iingns, A.icgn[c]);
+    S.global_corner_number = A.icgcn;
+  }
+  // ---- pass 2: edges, faces, BC removal (module_dd.f90:9387-9587)
+  for (int s = 0; s < nsub; ++s) {
+    auto& S = o.subs[s];
+    auto& A = aux[s];
+    int nnodi = S.nnodi;
+    A.kglobs.assign(nnodi, -1);
+    A.globtypes.assign(nnodi, 0);
+    int nc = A.ncorners;
+    for (int c = 0; c < nc; ++c) { A.kglobs[S.icnsin[c]] = c + 1; A.globtypes[S.icnsin[c]] = 3; }
+    int iedges = 0;
+    for (int i = 0; i < nnodi; ++i) {
+      if (A.kglobs[i] != -1) continue;
+      int nsubn = A.nsubnode[i];
+      if (nsubn > 1) {
+        ++iedges;
+        A.kglobs[i] = nc + iedges; A.globtypes[i] = 2;
+        for (int j = i + 1; j < nnodi; ++j)
+          if (A.kglobs[j] == -1 && A.nsubnode[j] == nsubn && A.globsubs[j] == A.globsubs[i]) {
+            A.kglobs[j] = nc + iedges; A.globtypes[j] = 2;
+          }
+      }
+    }
+    int nedges = iedges, ifaces = 0;
+    for (int i = 0; i < nnodi; ++i) {
+      if (A.kglobs[i] != -1) continue;
+      int nsubn = A.nsubnode[i];
+      if (nsubn != 1) throw std::runtime_error("unassigned non-face node");
+      ++ifaces;
+      A.kglobs[i] = nc + nedges + ifaces; A.globtypes[i] = 1;
+      for (int j = i + 1; j < nnodi; ++j)
+        if (A.kglobs[j] == -1 && A.nsubnode[j] == nsubn && A.globsubs[j] == A.globsubs[i]) {
+          A.kglobs[j] = nc + nedges + ifaces; A.globtypes[j] = 1;
+        }
+    }
+    int nfaces = ifaces;
+    if (S.bc_present) {  // remove_bc_nodes on level 1
+      for (int i = 0; i < nnodi; ++i) {
+        if (A.globtypes[i] == 3) continue;
+        int nd = S.iin[i];
+        bool fixed = false;
+        for (int d = 0; d < S.nndf[nd]; ++d) if (S.ifix[S.kdof[nd] + d] > 0) fixed = true;
+        if (fixed) { A.kglobs[i] = -2; A.globtypes[i] = -2; }
+      }
+      int ie = 0;
+      for (int e = 1; e <= nedges; ++e) {
+        int old = nc + e;
+        if (std::find(A.kglobs.begin(), A.kglobs.end(), old) != A.kglobs.end()) {
+          ++ie;
+          for (auto& x : A.kglobs) if (x == old) x = nc + ie;
+        }
+      }
+      int iff = 0;
+      for (int f = 1; f <= nfaces; ++f) {
+        int old = nc + nedges + f;
+        if (std::find(A.kglobs.begin(), A.kglobs.end(), old) != A.kglobs.end()) {
+          ++iff;
+          for (auto& x : A.kglobs) if (x == old) x = nc + ie + iff;
+        }
+      }
+      nedges = ie; nfaces = iff;
+    }
+    A.nedges = nedges; A.nfaces = nfaces;
+    A.iegn.assign(nedges, 0);
+    A.ifgn.assign(nfaces, 0);
+    for (int e = 0; e < nedges; ++e) {
+      int mn = INT32_MAX;
+      for (int i = 0; i < nnodi; ++i) if (A.kglobs[i] == nc + e + 1) mn = std::min(mn, A.iingns[i]);
+      A.iegn[e] = mn;
+    }
+    for (int f = 0; f < nfaces; ++f) {
+      int mn = INT32_MAX;
+      for (int i = 0; i < nnodi; ++i) if (A.kglobs[i] == nc + nedges + f + 1) mn = std::min(mn, A.iingns[i]);
+      A.ifgn[f] = mn;
+    }
+  }
+  o.nedge = number(o.ncorner, [](Aux& A) -> vector<int>& { return A.iegn; }, [](Aux& A) -> vector<int>& { return A.iegcn; });
+  o.nface = number(o.ncorner + o.nedge, [](Aux& A) -> vector<int>& { return A.ifgn; }, [](Aux& A) -> vector<int>& { return A.ifgcn; });
+  // ---- cnodes (module_dd.f90:4869-5016)
+  for (int s = 0; s < nsub; ++s) {
+    auto& S = o.subs[s];
+    auto& A = aux[s];
+    vector<int> kdofi(S.nnodi, 0);
+    for (int i = 1; i < S.nnodi; ++i) kdofi[i] = kdofi[i - 1] + S.nndf[S.iin[i - 1]];
+    S.cnodes.clear();
+    for (int c = 0; c < A.ncorners; ++c) {
+      Cnode cn;
+      cn.itype = 3;
+      cn.global_cnode = S.global_corner_number[c];
+      int in = S.icnsin[c];
+      cn.insin = {in};
+      cn.nvar = S.nndf[S.iin[in]];
+      for (int d = 0; d < cn.nvar; ++d) cn.ivsivn.push_back(kdofi[in] + d);
+      S.cnodes.push_back(cn);
+    }
+    int nc = A.ncorners;
+    for (int gl = 0; gl < A.nedges + A.nfaces; ++gl) {
+      Cnode cn;
+      bool edge = gl < A.nedges;
+      cn.itype = edge ? 2 : 1;
+      cn.global_cnode = edge ? A.iegcn[gl] : A.ifgcn[gl - A.nedges];
+      for (int i = 0; i < S.nnodi; ++i)
+        if (A.kglobs[i] == nc + gl + 1) {
+          cn.insin.push_back(i);
+          for (int d = 0; d < S.nndf[S.iin[i]]; ++d) cn.ivsivn.push_back(kdofi[i] + d);
+        }
+      cn.nvar = (int)cn.ivsivn.size();
+      S.cnodes.push_back(cn);
+    }
+  }
+}
+
+// arithmetic constraints of one glob type (module_dd.f90:4298-4384)
+static void load_arithmetic_constraints(Sub& S, int itype) {
+  for (auto& cn : S.cnodes) {
+    if (cn.itype != itype) continue;
+    int ncdof = 0;
+    for (int in : cn.insin) ncdof = std::max(ncdof, S.nndf[S.iin[in]]);
+    vector<double> m((size_t)ncdof * cn.nvar, 0.0);
+    int p = 0;
+    for (int in : cn.insin) {
+      int nd = S.nndf[S.iin[in]];
+      for (int d = 0; d < nd; ++d) m[(size_t)d * cn.nvar + p + d] = 1.0;
+      p += nd;
+    }
+    cn.matrix.insert(cn.matrix.end(), m.begin(), m.end());
+    cn.ncdof += ncdof;
+    cn.used = true;
+  }
+}
+
+// ================================================================ API
+extern "C" {
+
+void* oracle_create(int nsub, int nthreads) {
+  auto* o = new Oracle;
+  o->nsub = nsub;
+  o->nthreads = std::max(1, nthreads);
+  o->subs.resize(nsub);
+  return o;
+}
+
+void oracle_destroy(void* h) { delete static_cast<Oracle*>(h); }
+
+const char* oracle_error(void* h) { return static_cast<Oracle*>(h)->err.c_str(); }
+
+// All index arrays 0-based.  xyz is (nnod x ndim) column-major as in the ABI.
+int oracle_upload(void* h, int isub, int nelem, int nnod, int ndof, int ndim,
+                  const int* inet, int linet, const int* nnet, const int* nndf,
+                  const int* isngn, const int* isvgvn, const int* isegn, const double* xyz,
+                  const int* ifix, const double* fixv, const double* rhs, int is_rhs_complete,
+                  const double* sol, int matrixtype, int la, const int* i_sparse, const int* j_sparse,
+                  const double* a_sparse, int find_components, int neighbouring) {
+  auto* o = static_cast<Oracle*>(h);
+  if (isub < 0 || isub >= o->nsub) { o->err = "bad isub"; return 1; }
+  Sub& S = o->subs[isub];
+  S.isub = isub + 1;
+  S.nelem = nelem; S.nnod = nnod; S.ndof = ndof; S.ndim = ndim;
+  S.inet.assign(inet, inet + linet);
+  S.nnet.assign(nnet, nnet + nelem);
+  S.nndf.assign(nndf, nndf + nnod);
+  S.isngn.assign(isngn, isngn + nnod);
+  S.isvgvn.assign(isvgvn, isvgvn + ndof);
+  S.isegn.assign(isegn, isegn + nelem);
+  S.xyz.assign(xyz, xyz + (size_t)nnod * ndim);
+  S.ifix.assign(ifix, ifix + ndof);
+  S.fixv.assign(fixv, fixv + ndof);
+  S.rhs.assign(rhs, rhs + ndof);
+  S.rhs_complete = is_rhs_complete != 0;
+  S.sol.assign(sol, sol + ndof);
+  S.matrixtype = matrixtype;
+  S.ia.assign(i_sparse, i_sparse + la);
+  S.ja.assign(j_sparse, j_sparse + la);
+  S.a.assign(a_sparse, a_sparse + la);
+  for (int k = 0; k < la; ++k)
+    if (S.ia[k] > S.ja[k]) { o->err = "only the upper triangle is expected"; return 2; }
+  coo_assemble(S.ia, S.ja, S.a);
+  S.bc_present = false;
+  for (int i = 0; i < ndof; ++i) if (S.ifix[i] != 0) S.bc_present = true;
+  nodal_components(S, find_components != 0, neighbouring);
+  return 0;
+}
+
+static void comm_exchange_add(Oracle& o, vector<vector<double>>& v) {
+  // upload / swap / download (module_dd.f90:11236-11551): own value plus the
+  // neighbours' values on shared dofs, neighbours in ascending order.
+  int nsub = o.nsub;
+  vector<vector<double>> out(nsub);
+  for (int s = 0; s < nsub; ++s) out[s] = v[s];
+#pragma omp parallel for schedule(dynamic) num_threads(o.nthreads)
+  for (int s = 0; s < nsub; ++s) {
+    auto& S = o.subs[s];
+    for (size_t a = 0; a < S.iadj.size(); ++a) {
+      const vector<double>& vt = v[S.iadj[a] - 1];
+      for (int k = S.xch_ptr[a]; k < S.xch_ptr[a + 1]; ++k) out[s][S.xch_mine[k]] += vt[S.xch_theirs[k]];
+    }
+  }
+  v.swap(out);
+}
+
+static void build_exchange_lists(Oracle& o) {
+  for (auto& S : o.subs) {
+    S.kdofi.assign(S.nnodi + 1, 0);
+    for (int i = 0; i < S.nnodi; ++i) S.kdofi[i + 1] = S.kdofi[i] + S.nndf[S.iin[i]];
+  }
+#pragma omp parallel for schedule(dynamic) num_threads(o.nthreads)
+  for (int s = 0; s < o.nsub; ++s) {
+    auto& S = o.subs[s];
+    S.xch_mine.clear(); S.xch_theirs.clear(); S.xch_ptr.assign(1, 0);
+    int k = 0;
+    for (size_t a = 0; a < S.iadj.size(); ++a) {
+      auto& T = o.subs[S.iadj[a] - 1];
+      std::unordered_map<int, int> tpos;  // global node id -> neighbour interface node index
+      for (int i = 0; i < T.nnodi; ++i) tpos.emplace(T.isngn[T.iin[i]], i);
+      for (int ish = 0; ish < S.nshnadj[a]; ++ish) {
+        int inodi = S.ishnadj[k + ish];
+        int tinodi = tpos.at(S.isngn[S.iin[inodi]]);
+        int nd = S.kdofi[inodi + 1] - S.kdofi[inodi];
+        for (int d = 0; d < nd; ++d) { S.xch_mine.push_back(S.kdofi[inodi] + d); S.xch_theirs.push_back(T.kdofi[tinodi] + d); }
+      }
+      S.xch_ptr.push_back((int)S.xch_mine.size());
+      k += S.nshnadj[a];
+    }
+  }
+}
+
+int oracle_setup(void* h, int use_corner_constraints, int use_arithmetic_constraints, int weights_type) {
+  auto* o = static_cast<Oracle*>(h);
+  try {
+    int nsub = o->nsub;
+    int meshdim = o->subs[0].ndim;
+    create_neighbouring(*o);
+    build_exchange_lists(*o);
+    create_globs(*o, use_corner_constraints != 0, meshdim);
+    // ---- BC elimination (module_dd.f90:1081-1256, module_sm.f90:431-600)
+    vector<vector<double>> bci(nsub);
+    for (int s = 0; s < nsub; ++s) {
+      auto& S = o->subs[s];
+      S.bc.assign(S.ndof, 0.0);
+      if (S.bc_present) {
+        vector<char> diag_fixed(S.ndof, 0);
+        for (size_t k = 0; k < S.ia.size(); ++k) {
+          int i = S.ia[k], j = S.ja[k];
+          if (i != j) {
+            if (S.ifix[i] && S.fixv[i] != 0.0 && S.a[k] != 0.0 && !S.ifix[j]) S.bc[j] -= S.a[k] * S.fixv[i];
+            if (S.ifix[j] && S.fixv[j] != 0.0 && S.a[k] != 0.0 && !S.ifix[i]) S.bc[i] -= S.a[k] * S.fixv[j];
+            if (S.ifix[i] || S.ifix[j]) S.a[k] = 0.0;
+          } else if (S.ifix[i]) {
+            if (std::fabs(S.a[k]) < 1e-16) S.a[k] = 1.0;
+            if (S.fixv[i] != 0.0) S.bc[i] += S.a[k] * S.fixv[i];
+            diag_fixed[i] = 1;
+          }
+        }
+        for (int i = 0; i < S.ndof; ++i)
+          if (S.ifix[i] > 0 && !diag_fixed[i]) {
+            S.ia.push_back(i); S.ja.push_back(i); S.a.push_back(1.0);
+            S.bc[i] += S.fixv[i];
+          }
+        coo_assemble(S.ia, S.ja, S.a);
+      }
+      bci[s].assign(S.ndofi, 0.0);
+      for (int i = 0; i < S.ndofi; ++i) bci[s][i] = S.bc[S.iivsvn[i]];
+    }
+    {
+      vector<vector<double>> summed = bci;
+      comm_exchange_add(*o, summed);
+      for (int s = 0; s < nsub; ++s) {
+        auto& S = o->subs[s];
+        for (int i = 0; i < S.ndofi; ++i) S.bc[S.iivsvn[i]] += summed[s][i] - bci[s][i];
+      }
+    }
+    // ---- weights (module_dd.f90:11554-11722)
+    vector<vector<double>> rho(nsub);
+    for (int s = 0; s < nsub; ++s) {
+      auto& S = o->subs[s];
+      rho[s].assign(S.ndofi, 1.0);
+      if (weights_type == 1) {
+        vector<double> dg(S.ndof, 0.0);
+        for (size_t k = 0; k < S.ia.size(); ++k) if (S.ia[k] == S.ja[k]) dg[S.ia[k]] += S.a[k];
+        for (int i = 0; i < S.ndofi; ++i) { rho[s][i] = dg[S.iivsvn[i]]; if (rho[s][i] == 0.0) rho[s][i] = 1.0; }
+      } else if (weights_type != 0) {
+        throw std::runtime_error("weights type not supported by the oracle");
+      }
+    }
+    {
+      vector<vector<double>> tot = rho;
+      comm_exchange_add(*o, tot);
+      for (int s = 0; s < nsub; ++s) {
+        auto& S = o->subs[s];
+        S.wi.resize(S.ndofi);
+        for (int i = 0; i < S.ndofi; ++i) S.wi[i] = rho[s][i] / tot[s][i];  // rho/(rho + sum neighbours)
+      }
+    }
+    // ---- constraints and coarse dofs (module_levels.f90:2690-2740, module_dd.f90:11011-11235, 5018-5144)
+    for (int s = 0; s < nsub; ++s) {
+      auto& S = o->subs[s];
+      if (use_corner_constraints) load_arithmetic_constraints(S, 3);
+      if (use_arithmetic_constraints) { load_arithmetic_constraints(S, 2); load_arithmetic_constraints(S, 1); }
+    }
+    int ncnode = o->ncorner + o->nedge + o->nface;
+    o->ncdof_of_cnode.assign(ncnode, 0);
+    for (auto& S : o->subs)
+      for (auto& cn : S.cnodes) o->ncdof_of_cnode[cn.global_cnode - 1] = cn.ncdof;
+    vector<int> kdofc(ncnode + 1, 0);
+    for (int c = 0; c < ncnode; ++c) kdofc[c + 1] = kdofc[c] + o->ncdof_of_cnode[c];
+    o->ndofc = kdofc[ncnode];
+    for (auto& S : o->subs) {
+      S.crow_ptr.assign(1, 0); S.crow_col.clear(); S.crow_val.clear(); S.indrowc.clear();
+      for (auto& cn : S.cnodes) {
+        cn.igcdof.clear();
+        for (int d = 0; d < cn.ncdof; ++d) cn.igcdof.push_back(kdofc[cn.global_cnode - 1] + d + 1);
+        if (!cn.used) continue;
+        for (int r = 0; r < cn.ncdof; ++r) {
+          for (int v = 0; v < cn.nvar; ++v) {
+            double val = cn.matrix[(size_t)r * cn.nvar + v];
+            if (std::fabs(val) > 0.0) { S.crow_col.push_back(cn.ivsivn[v]); S.crow_val.push_back(val); }
+          }
+          S.crow_ptr.push_back((int)S.crow_col.size());
+          S.indrowc.push_back(cn.igcdof[r]);
+        }
+      }
+      S.nconstr = (int)S.indrowc.size();
+    }
+    // ---- per-subdomain factorisations (module_dd.f90:3983-4295, 5211-5799)
+    std::string errs;
+#pragma omp parallel for schedule(dynamic) num_threads(o->nthreads)
+    for (int s = 0; s < nsub; ++s) {
+      try {
+        auto& S = o->subs[s];
+        sym_csr_from_upper(S.ndof, S.ia, S.ja, S.a, S.f_ptr, S.f_col, S.f_val);
+        // blocks
+        vector<int> mo(S.ndof, -1), mi(S.ndof, -1);
+        for (int i = 0; i < S.ndofo; ++i) mo[S.iovsvn[i]] = i;
+        for (int i = 0; i < S.ndofi; ++i) mi[S.iivsvn[i]] = i;
+        S.a12_ptr.assign(S.ndofo + 1, 0); S.a12_col.clear(); S.a12_val.clear();
+        S.a22_ptr.assign(S.ndofi + 1, 0); S.a22_col.clear(); S.a22_val.clear();
+        int b11 = 0;
+        for (int io = 0; io < S.ndofo; ++io) {
+          int r = S.iovsvn[io];
+          for (int k = S.f_ptr[r]; k < S.f_ptr[r + 1]; ++k) {
+            int c = S.f_col[k];
+            if (mi[c] >= 0) { S.a12_col.push_back(mi[c]); S.a12_val.push_back(S.f_val[k]); }
+            else b11 = std::max(b11, std::abs(io - mo[c]));
+          }
+          S.a12_ptr[io + 1] = (int)S.a12_col.size();
+        }
+        for (int ii = 0; ii < S.ndofi; ++ii) {
+          int r = S.iivsvn[ii];
+          for (int k = S.f_ptr[r]; k < S.f_ptr[r + 1]; ++k) {
+            int c = S.f_col[k];
+            if (mi[c] >= 0) { S.a22_col.push_back(mi[c]); S.a22_val.push_back(S.f_val[k]); }
+          }
+          S.a22_ptr[ii + 1] = (int)S.a22_col.size();
+        }
+        S.a11.n = S.ndofo; S.a11.b = b11;
+        S.a11.v.assign((size_t)S.ndofo * (b11 + 1), 0.0);
+        for (int io = 0; io < S.ndofo; ++io) {
+          int r = S.iovsvn[io];
+          for (int k = S.f_ptr[r]; k < S.f_ptr[r + 1]; ++k) {
+            int c = S.f_col[k];
+            if (mo[c] >= 0 && mo[c] <= io) S.a11.at(io, mo[c]) += S.f_val[k];
+          }
+        }
+        if (S.ndofo > 0) S.a11.factor();
+        // augmented system: corner dofs shifted by their own diagonal
+        int baug = 0;
+        for (int r = 0; r < S.ndof; ++r)
+          for (int k = S.f_ptr[r]; k < S.f_ptr[r + 1]; ++k) baug = std::max(baug, std::abs(r - S.f_col[k]));
+        S.aug.n = S.ndof; S.aug.b = baug;
+        S.aug.v.assign((size_t)S.ndof * (baug + 1), 0.0);
+        for (int r = 0; r < S.ndof; ++r)
+          for (int k = S.f_ptr[r]; k < S.f_ptr[r + 1]; ++k)
+            if (S.f_col[k] <= r) S.aug.at(r, S.f_col[k]) += S.f_val[k];
+        for (auto& cn : S.cnodes)
+          if (cn.itype == 3 && cn.used)
+            for (int v : cn.ivsivn) { int d = S.iivsvn[v]; S.aug.at(d, d) *= 2.0; }
+        S.aug.factor();
+        int nc = S.nconstr;
+        S.yaug.assign((size_t)S.ndof * nc, 0.0);
+        for (int c = 0; c < nc; ++c) {
+          double* y = &S.yaug[(size_t)c * S.ndof];
+          for (int k = S.crow_ptr[c]; k < S.crow_ptr[c + 1]; ++k) y[S.iivsvn[S.crow_col[k]]] += S.crow_val[k];
+          S.aug.solve(y);
+        }
+        S.gchol.assign((size_t)nc * nc, 0.0);
+        for (int r = 0; r < nc; ++r)
+          for (int c = 0; c < nc; ++c) {
+            double t = 0.0;
+            for (int k = S.crow_ptr[r]; k < S.crow_ptr[r + 1]; ++k) t += S.crow_val[k] * S.yaug[(size_t)c * S.ndof + S.iivsvn[S.crow_col[k]]];
+            S.gchol[(size_t)r * nc + c] = t;
+          }
+        for (int r = 0; r < nc; ++r)
+          for (int c = r + 1; c < nc; ++c) {
+            double m = 0.5 * (S.gchol[(size_t)r * nc + c] + S.gchol[(size_t)c * nc + r]);
+            S.gchol[(size_t)r * nc + c] = S.gchol[(size_t)c * nc + r] = m;
+          }
+        if (nc > 0) dense_chol(S.gchol, nc);
+        // coarse basis: Phi = Y G^{-1}   (solve with RHS [0; I], module_dd.f90:5592-5607)
+        vector<double> phi((size_t)S.ndof * nc, 0.0);
+        for (int c = 0; c < nc; ++c) {
+          vector<double> e(nc, 0.0); e[c] = 1.0;
+          dense_chol_solve(S.gchol, nc, e.data());
+          for (int i = 0; i < S.ndof; ++i) {
+            double t = 0.0;
+            for (int q = 0; q < nc; ++q) t += S.yaug[(size_t)q * S.ndof + i] * e[q];
+            phi[(size_t)c * S.ndof + i] = t;
+          }
+        }
+        S.phisi.assign((size_t)S.ndofi * nc, 0.0);
+        for (int c = 0; c < nc; ++c)
+          for (int i = 0; i < S.ndofi; ++i) S.phisi[(size_t)c * S.ndofi + i] = phi[(size_t)c * S.ndof + S.iivsvn[i]];
+        // coarse matrix Phi^T A Phi
+        S.coarsem.assign((size_t)nc * nc, 0.0);
+        vector<double> aphi(S.ndof);
+        for (int c = 0; c < nc; ++c) {
+          csr_mult(S.f_ptr, S.f_col, S.f_val, &phi[(size_t)c * S.ndof], aphi.data(), S.ndof);
+          for (int r = 0; r < nc; ++r) {
+            double t = 0.0;
+            for (int i = 0; i < S.ndof; ++i) t += phi[(size_t)r * S.ndof + i] * aphi[i];
+            S.coarsem[(size_t)r * nc + c] = t;
+          }
+        }
+      } catch (std::exception& e) {
+#pragma omp critical
+        errs = e.what();
+      }
+    }
+    if (!errs.empty()) throw std::runtime_error(errs);
+    // ---- coarse problem (module_levels.f90:3001-3170): assemble upper triangle, factor
+    int n = o->ndofc;
+    o->coarse_chol.assign((size_t)n * n, 0.0);
+    for (auto& S : o->subs) {
+      int nc = S.nconstr;
+      for (int j = 0; j < nc; ++j)
+        for (int i = 0; i <= j; ++i) {
+          int gi = S.indrowc[i] - 1, gj = S.indrowc[j] - 1;
+          double v = S.coarsem[(size_t)i * nc + j];
+          int r = std::max(gi, gj), c = std::min(gi, gj);
+          o->coarse_chol[(size_t)r * n + c] += v;
+        }
+    }
+    for (int r = 0; r < n; ++r)
+      for (int c = r + 1; c < n; ++c) o->coarse_chol[(size_t)r * n + c] = o->coarse_chol[(size_t)c * n + r];
+    if (n > 0) dense_chol(o->coarse_chol, n, o->nthreads);
+    // ---- reduced rhs (module_dd.f90:6995-7257)
+    vector<vector<double>> g(nsub);
+#pragma omp parallel for schedule(dynamic) num_threads(o->nthreads)
+    for (int s = 0; s < nsub; ++s) {
+      auto& S = o->subs[s];
+      vector<double> rhs = S.rhs;
+      if (S.rhs_complete) for (int i = 0; i < S.ndofi; ++i) rhs[S.iivsvn[i]] *= S.wi[i];
+      if (S.bc_present) {
+        vector<double> bcw = S.bc;
+        for (int i = 0; i < S.ndofi; ++i) bcw[S.iivsvn[i]] *= S.wi[i];
+        for (int i = 0; i < S.ndof; ++i) { if (S.ifix[i]) rhs[i] = 0.0; rhs[i] += bcw[i]; }
+      }
+      S.solo.assign(S.ndofo, 0.0);
+      for (int i = 0; i < S.ndofo; ++i) S.solo[i] = rhs[S.iovsvn[i]];
+      if (S.ndofo > 0) S.a11.solve(S.solo.data());
+      g[s].assign(S.ndofi, 0.0);
+      for (int io = 0; io < S.ndofo; ++io)
+        for (int k = S.a12_ptr[io]; k < S.a12_ptr[io + 1]; ++k) g[s][S.a12_col[k]] += S.a12_val[k] * S.solo[io];
+      for (int i = 0; i < S.ndofi; ++i) g[s][i] = rhs[S.iivsvn[i]] - g[s][i];
+    }
+    comm_exchange_add(*o, g);
+    for (int s = 0; s < nsub; ++s) o->subs[s].g = g[s];
+    o->setup_done = true;
+  } catch (std::exception& e) {
+    o->err = e.what();
+    return 1;
+  }
+  return 0;
+}
+
+// y = S x per subdomain (module_dd.f90:6564-6699), then exchange
+static void sm_apply(Oracle& o, vector<vector<double>>& x, vector<vector<double>>& y) {
+#pragma omp parallel for schedule(dynamic) num_threads(o.nthreads)
+  for (int s = 0; s < o.nsub; ++s) {
+    auto& S = o.subs[s];
+    vector<double> aux1(S.ndofo, 0.0);
+    for (int io = 0; io < S.ndofo; ++io) {
+      double t = 0.0;
+      for (int k = S.a12_ptr[io]; k < S.a12_ptr[io + 1]; ++k) t += S.a12_val[k] * x[s][S.a12_col[k]];
+      aux1[io] = t;
+    }
+    if (S.ndofo > 0) S.a11.solve(aux1.data());
+    vector<double> aux2(S.ndofi, 0.0);
+    for (int io = 0; io < S.ndofo; ++io)
+      for (int k = S.a12_ptr[io]; k < S.a12_ptr[io + 1]; ++k) aux2[S.a12_col[k]] += S.a12_val[k] * aux1[io];
+    y[s].assign(S.ndofi, 0.0);
+    for (int i = 0; i < S.ndofi; ++i) {
+      double t = 0.0;
+      for (int k = S.a22_ptr[i]; k < S.a22_ptr[i + 1]; ++k) t += S.a22_val[k] * x[s][S.a22_col[k]];
+      y[s][i] = t - aux2[i];
+    }
+  }
+  comm_exchange_add(o, y);
+}
+
+// z = M r (module_levels.f90:3627-3703, 3707-3846, 4029-4061, 4252-4346)
+static void pc_apply(Oracle& o, vector<vector<double>>& r, vector<vector<double>>& z) {
+  int n = o.ndofc;
+  vector<double> rc(n, 0.0);
+  vector<vector<double>> rcs(o.nsub);
+#pragma omp parallel for schedule(dynamic) num_threads(o.nthreads)
+  for (int s = 0; s < o.nsub; ++s) {
+    auto& S = o.subs[s];
+    int nc = S.nconstr;
+    vector<double> aux(S.ndofi);
+    for (int i = 0; i < S.ndofi; ++i) aux[i] = S.wi[i] * r[s][i];
+    rcs[s].assign(nc, 0.0);
+    for (int c = 0; c < nc; ++c) {
+      double t = 0.0;
+      for (int i = 0; i < S.ndofi; ++i) t += S.phisi[(size_t)c * S.ndofi + i] * aux[i];
+      rcs[s][c] = t;
+    }
+    // constrained Neumann solve with interface RHS, interior zero
+    vector<double> f(S.ndof, 0.0);
+    for (int i = 0; i < S.ndofi; ++i) f[S.iivsvn[i]] = aux[i];
+    S.aug.solve(f.data());
+    vector<double> mu(nc, 0.0);
+    for (int c = 0; c < nc; ++c) {
+      double t = 0.0;
+      for (int k = S.crow_ptr[c]; k < S.crow_ptr[c + 1]; ++k) t += S.crow_val[k] * f[S.iivsvn[S.crow_col[k]]];
+      mu[c] = t;
+    }
+    if (nc > 0) dense_chol_solve(S.gchol, nc, mu.data());
+    z[s].assign(S.ndofi, 0.0);
+    for (int i = 0; i < S.ndofi; ++i) {
+      int d = S.iivsvn[i];
+      double t = f[d];
+      for (int c = 0; c < nc; ++c) t -= S.yaug[(size_t)c * S.ndof + d] * mu[c];
+      z[s][i] = t;
+    }
+  }
+  for (int s = 0; s < o.nsub; ++s) {
+    auto& S = o.subs[s];
+    for (int c = 0; c < S.nconstr; ++c) rc[S.indrowc[c] - 1] += rcs[s][c];
+  }
+  if (n > 0) dense_chol_solve(o.coarse_chol, n, rc.data());
+#pragma omp parallel for schedule(dynamic) num_threads(o.nthreads)
+  for (int s = 0; s < o.nsub; ++s) {
+    auto& S = o.subs[s];
+    for (int c = 0; c < S.nconstr; ++c) {
+      double u = rc[S.indrowc[c] - 1];
+      for (int i = 0; i < S.ndofi; ++i) z[s][i] += S.phisi[(size_t)c * S.ndofi + i] * u;
+    }
+    for (int i = 0; i < S.ndofi; ++i) z[s][i] *= S.wi[i];
+  }
+  comm_exchange_add(o, z);
+}
+
+static double dotw(Oracle& o, vector<vector<double>>& a, vector<vector<double>>& b) {
+  double t = 0.0;
+  for (int s = 0; s < o.nsub; ++s) {
+    auto& S = o.subs[s];
+    double ts = 0.0;
+    for (int i = 0; i < S.ndofi; ++i) ts += a[s][i] * S.wi[i] * b[s][i];
+    t += ts;
+  }
+  return t;
+}
+
+static void fix_bc_dual(Oracle& o, vector<vector<double>>& v) {
+  for (int s = 0; s < o.nsub; ++s) {
+    auto& S = o.subs[s];
+    if (!S.bc_present) continue;
+    for (int i = 0; i < S.ndofi; ++i) if (S.ifix[S.iivsvn[i]]) v[s][i] = 0.0;
+  }
+}
+
+// largest eigenvalue of a symmetric tridiagonal matrix by Sturm bisection
+// (stands in for LAPACK DSTEV in module_krylov.f90:2061-2118)
+static double tridiag_max_eig(const vector<double>& d, const vector<double>& e) {
+  int n = (int)d.size();
+  double lo = 1e300, hi = -1e300;
+  for (int i = 0; i < n; ++i) {
+    double r = (i > 0 ? std::fabs(e[i - 1]) : 0.0) + (i < n - 1 ? std::fabs(e[i]) : 0.0);
+    lo = std::min(lo, d[i] - r); hi = std::max(hi, d[i] + r);
+  }
+  auto count_below = [&](double x) {
+    int cnt = 0; double q = 1.0;
+    for (int i = 0; i < n; ++i) {
+      q = d[i] - x - (i > 0 ? e[i - 1] * e[i - 1] / q : 0.0);
+      if (q == 0.0) q = -1e-300;
+      if (q < 0) cnt++;
+    }
+    return cnt;
+  };
+  for (int it = 0; it < 200; ++it) {
+    double mid = 0.5 * (lo + hi);
+    if (count_below(mid) >= n) hi = mid; else lo = mid;
+    if (hi - lo <= 1e-15 * std::max(1.0, std::fabs(hi))) break;
+  }
+  return 0.5 * (lo + hi);
+}
+
+int oracle_solve(void* h, double tol, int maxit, int ndecrmax, int* num_iter, int* converged_reason,
+                 double* condition_number) {
+  auto* o = static_cast<Oracle*>(h);
+  if (!o->setup_done) { o->err = "setup not done"; return 1; }
+  int nsub = o->nsub;
+  vector<vector<double>> x(nsub), r(nsub), p(nsub), ap(nsub), z(nsub);
+  // initial data (module_levels.f90:4374-4440)
+  for (int s = 0; s < nsub; ++s) {
+    auto& S = o->subs[s];
+    vector<double> sol = S.sol;
+    if (S.bc_present) for (int i = 0; i < S.ndof; ++i) if (S.ifix[i]) sol[i] = S.fixv[i];
+    x[s].resize(S.ndofi);
+    for (int i = 0; i < S.ndofi; ++i) x[s][i] = sol[S.iivsvn[i]];
+    r[s] = S.g;
+  }
+  fix_bc_dual(*o, r);
+  o->relres_hist.clear();
+  *num_iter = 0; *converged_reason = 0; *condition_number = 1.0;
+  double normrhs = std::sqrt(dotw(*o, r, r));
+  if (normrhs == 0.0) return 0;
+  sm_apply(*o, x, ap);
+  fix_bc_dual(*o, ap);
+  for (int s = 0; s < nsub; ++s) for (size_t i = 0; i < r[s].size(); ++i) r[s][i] -= ap[s][i];
+  double normres0 = std::sqrt(dotw(*o, r, r));
+  if (normres0 == 0.0) return 0;
+  vector<double> diag(maxit + 1, 0.0), subdiag(maxit, 0.0);
+  int nw = 0;
+  if (normres0 != 0.0) {
+    pc_apply(*o, r, p);
+    double rmp = dotw(*o, r, p);
+    int ndecr = 0;
+    double lastres = 1.0;
+    for (int iter = 1; iter <= maxit; ++iter) {
+      sm_apply(*o, p, ap);
+      double pap = dotw(*o, p, ap);
+      double alpha = rmp / pap;
+      for (int s = 0; s < nsub; ++s)
+        for (size_t i = 0; i < x[s].size(); ++i) { x[s][i] += alpha * p[s][i]; r[s][i] -= alpha * ap[s][i]; }
+      double normres = std::sqrt(dotw(*o, r, r));
+      double relres = normres / normres0;
+      o->relres_hist.push_back(relres);
+      if (relres < tol) { nw = iter - 1; *num_iter = iter; *converged_reason = 0; break; }
+      if (iter == maxit) { nw = iter - 1; *num_iter = iter; *converged_reason = -1; break; }
+      if (relres < lastres) ndecr = 0;
+      else if (++ndecr >= ndecrmax) { nw = iter - 1; *num_iter = iter; *converged_reason = -2; break; }
+      lastres = relres;
+      pc_apply(*o, r, z);
+      double rmpold = rmp;
+      rmp = dotw(*o, r, z);
+      double beta = rmp / rmpold;
+      for (int s = 0; s < nsub; ++s)
+        for (size_t i = 0; i < p[s].size(); ++i) p[s][i] = z[s][i] + beta * p[s][i];
+      diag[iter - 1] += 1.0 / alpha;
+      diag[iter] = beta / alpha;
+      subdiag[iter - 1] = beta >= 0.0 ? -std::sqrt(beta) / alpha : 0.0;
+    }
+    if (nw > 1) {
+      vector<double> d(diag.begin(), diag.begin() + nw), e(subdiag.begin(), subdiag.begin() + nw - 1);
+      *condition_number = tridiag_max_eig(d, e);
+    } else {
+      *condition_number = 1.0;
+    }
+  }
+  // post-processing (module_levels.f90:4510-4576, module_dd.f90:6811-6932)
+#pragma omp parallel for schedule(dynamic) num_threads(o->nthreads)
+  for (int s = 0; s < nsub; ++s) {
+    auto& S = o->subs[s];
+    vector<double> u(S.ndof, 0.0);
+    if (S.ndofo > 0) {
+      vector<double> rhs = S.rhs;
+      if (S.bc_present) for (int i = 0; i < S.ndof; ++i) { if (S.ifix[i]) rhs[i] = 0.0; rhs[i] += S.bc[i]; }
+      vector<double> aux1(S.ndofo);
+      for (int io = 0; io < S.ndofo; ++io) {
+        double t = 0.0;
+        for (int k = S.a12_ptr[io]; k < S.a12_ptr[io + 1]; ++k) t += S.a12_val[k] * x[s][S.a12_col[k]];
+        aux1[io] = rhs[S.iovsvn[io]] - t;
+      }
+      S.a11.solve(aux1.data());
+      for (int io = 0; io < S.ndofo; ++io) u[S.iovsvn[io]] += aux1[io];
+    }
+    for (int i = 0; i < S.ndofi; ++i) u[S.iivsvn[i]] += x[s][i];
+    S.sol = u;
+  }
+  return 0;
+}
+
+int oracle_download(void* h, int isub, double* sols, int lsols) {
+  auto* o = static_cast<Oracle*>(h);
+  auto& S = o->subs[isub];
+  if (lsols != S.ndof) return 1;
+  std::copy(S.sol.begin(), S.sol.end(), sols);
+  return 0;
+}
+
+// structure summary: [ncorner, nedge, nface, ndofc, sum ndofi, sum ndofo]
+void oracle_stats(void* h, int* out) {
+  auto* o = static_cast<Oracle*>(h);
+  long si = 0, so = 0;
+  for (auto& S : o->subs) { si += S.ndofi; so += S.ndofo; }
+  out[0] = o->ncorner; out[1] = o->nedge; out[2] = o->nface; out[3] = o->ndofc;
+  out[4] = (int)si; out[5] = (int)so;
+}
+
+// per-subdomain: [ndofi, ndofo, nconstr, ncorner_nodes, nadj]
+void oracle_sub_stats(void* h, int isub, int* out) {
+  auto* o = static_cast<Oracle*>(h);
+  auto& S = o->subs[isub];
+  int nco = 0;
+  for (auto& cn : S.cnodes) if (cn.itype == 3) nco++;
+  out[0] = S.ndofi; out[1] = S.ndofo; out[2] = S.nconstr; out[3] = nco; out[4] = (int)S.iadj.size();
+}
+
+int oracle_relres_history(void* h, double* out, int lout) {
+  auto* o = static_cast<Oracle*>(h);
+  int n = std::min<int>(lout, (int)o->relres_hist.size());
+  for (int i = 0; i < n; ++i) out[i] = o->relres_hist[i];
+  return (int)o->relres_hist.size();
+}
+
+// interface weights of one subdomain (ndofi values)
+int oracle_weights(void* h, int isub, double* out, int lout) {
+  auto* o = static_cast<Oracle*>(h);
+  auto& S = o->subs[isub];
+  if (lout != S.ndofi) return 1;
+  std::copy(S.wi.begin(), S.wi.end(), out);
+  return 0;
+}
+
+// sum_i v1 w v2 over interface + plain sum over interior (module_dd.f90:12736-12788)
+double oracle_dotprod_subdomain(void* h, int isub, const double* v1, const double* v2) {
+  auto* o = static_cast<Oracle*>(h);
+  auto& S = o->subs[isub];
+  double t = 0.0;
+  for (int i = 0; i < S.ndofi; ++i) t += v1[S.iivsvn[i]] * S.wi[i] * v2[S.iivsvn[i]];
+  for (int i = 0; i < S.ndofo; ++i) t += v1[S.iovsvn[i]] * v2[S.iovsvn[i]];
+  return t;
+}
+
+}  // extern "C"

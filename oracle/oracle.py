@@ -1,0 +1,137 @@
+"""ctypes wrapper of the CPU oracle (liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by ``__graft_entry__.smoke()``
+and by the CPU legs of ``bench.py``.  The GPU library never imports this.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+
+def build(force: bool = False) -> str:
+    path = os.path.join(_HERE, "liboracle.so")
+    src = os.path.join(_HERE, "bddc_oracle.cpp")
+    if force or not os.path.exists(path) or os.path.getmtime(path) < os.path.getmtime(src):
+        subprocess.run(["make", "-s", "-C", _HERE, "liboracle.so"], check=True)
+    return path
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        _LIB = C.CDLL(build())
+        L = _LIB
+        L.oracle_create.restype = C.c_void_p
+        L.oracle_create.argtypes = [C.c_int, C.c_int]
+        L.oracle_destroy.argtypes = [C.c_void_p]
+        L.oracle_error.restype = C.c_char_p
+        L.oracle_error.argtypes = [C.c_void_p]
+        L.oracle_setup.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int]
+        L.oracle_solve.argtypes = [C.c_void_p, C.c_double, C.c_int, C.c_int,
+                                   C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_double)]
+        L.oracle_download.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int]
+        L.oracle_stats.argtypes = [C.c_void_p, C.c_void_p]
+        L.oracle_sub_stats.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+        L.oracle_relres_history.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
+        L.oracle_weights.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int]
+        L.oracle_dotprod_subdomain.restype = C.c_double
+        L.oracle_dotprod_subdomain.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+    return _LIB
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Oracle:
+    """BDDC interface PCG restated on the CPU (see bddc_oracle.cpp)."""
+
+    def __init__(self, prob, nthreads: int | None = None, find_components: int = 1, neighbouring: int = 3):
+        self.L = lib()
+        self.prob = prob
+        self.h = self.L.oracle_create(prob.nsub, int(nthreads or os.cpu_count() or 1))
+        self._keep = []
+        for s in prob.subdomains:
+            arrs = dict(
+                inet=np.ascontiguousarray(s.inet, np.int32), nnet=np.ascontiguousarray(s.nnet, np.int32),
+                nndf=np.ascontiguousarray(s.nndf, np.int32), isngn=np.ascontiguousarray(s.isngn, np.int32),
+                isvgvn=np.ascontiguousarray(s.isvgvn, np.int32), isegn=np.ascontiguousarray(s.isegn, np.int32),
+                xyz=np.ascontiguousarray(s.xyz, np.float64), ifix=np.ascontiguousarray(s.ifix, np.int32),
+                fixv=np.ascontiguousarray(s.fixv, np.float64), rhs=np.ascontiguousarray(s.rhs, np.float64),
+                sol=np.ascontiguousarray(s.sol, np.float64), i=np.ascontiguousarray(s.i_sparse, np.int32),
+                j=np.ascontiguousarray(s.j_sparse, np.int32), a=np.ascontiguousarray(s.a_sparse, np.float64))
+            rc = self.L.oracle_upload(
+                C.c_void_p(self.h), C.c_int(s.isub), C.c_int(s.nelems), C.c_int(s.nnods), C.c_int(s.ndofs),
+                C.c_int(prob.ndim), _p(arrs["inet"]), C.c_int(len(s.inet)), _p(arrs["nnet"]), _p(arrs["nndf"]),
+                _p(arrs["isngn"]), _p(arrs["isvgvn"]), _p(arrs["isegn"]), _p(arrs["xyz"]), _p(arrs["ifix"]),
+                _p(arrs["fixv"]), _p(arrs["rhs"]), C.c_int(s.is_rhs_complete), _p(arrs["sol"]),
+                C.c_int(prob.matrixtype), C.c_int(len(s.a_sparse)), _p(arrs["i"]), _p(arrs["j"]), _p(arrs["a"]),
+                C.c_int(find_components), C.c_int(neighbouring))
+            if rc != 0:
+                raise RuntimeError(self.L.oracle_error(self.h).decode())
+
+    def __del__(self):
+        try:
+            self.L.oracle_destroy(self.h)
+        except Exception:
+            pass
+
+    def setup(self, use_corner_constraints=1, use_arithmetic_constraints=1, weights_type=0):
+        rc = self.L.oracle_setup(self.h, use_corner_constraints, use_arithmetic_constraints, weights_type)
+        if rc != 0:
+            raise RuntimeError(self.L.oracle_error(self.h).decode())
+
+    def solve(self, tol=1e-8, maxit=500, ndecrmax=50):
+        it, reason, cond = C.c_int(), C.c_int(), C.c_double()
+        rc = self.L.oracle_solve(self.h, tol, maxit, ndecrmax, C.byref(it), C.byref(reason), C.byref(cond))
+        if rc != 0:
+            raise RuntimeError(self.L.oracle_error(self.h).decode())
+        return it.value, reason.value, cond.value
+
+    def download(self, isub):
+        s = self.prob.subdomains[isub]
+        out = np.zeros(s.ndofs)
+        if self.L.oracle_download(self.h, isub, _p(out), s.ndofs) != 0:
+            raise RuntimeError("download size mismatch")
+        return out
+
+    def global_solution(self):
+        u = np.zeros(self.prob.ndof)
+        for s in self.prob.subdomains:
+            u[s.isvgvn] = self.download(s.isub)
+        return u
+
+    def stats(self):
+        out = np.zeros(6, dtype=np.int32)
+        self.L.oracle_stats(self.h, _p(out))
+        return dict(ncorner=int(out[0]), nedge=int(out[1]), nface=int(out[2]), ndofc=int(out[3]),
+                    sum_ndofi=int(out[4]), sum_ndofo=int(out[5]))
+
+    def sub_stats(self, isub):
+        out = np.zeros(5, dtype=np.int32)
+        self.L.oracle_sub_stats(self.h, isub, _p(out))
+        return dict(ndofi=int(out[0]), ndofo=int(out[1]), nconstr=int(out[2]), ncorner=int(out[3]), nadj=int(out[4]))
+
+    def relres_history(self):
+        n = self.L.oracle_relres_history(self.h, None, 0)
+        out = np.zeros(n)
+        self.L.oracle_relres_history(self.h, _p(out), n)
+        return out
+
+    def weights(self, isub):
+        st = self.sub_stats(isub)
+        out = np.zeros(st["ndofi"])
+        self.L.oracle_weights(self.h, isub, _p(out), st["ndofi"])
+        return out
+
+    def dotprod_subdomain(self, isub, v1, v2):
+        v1 = np.ascontiguousarray(v1, np.float64)
+        v2 = np.ascontiguousarray(v2, np.float64)
+        return self.L.oracle_dotprod_subdomain(self.h, isub, _p(v1), _p(v2))
