@@ -26,7 +26,7 @@ STATUS = {0: "OK", 1: "ARGUMENT", 2: "CUDA", 3: "NUMERIC", 4: "UNSUPPORTED", 5: 
 # fields of bddcml_get_stats_c
 STAT_FIELDS = ["t_host_setup", "t_device_setup", "t_solve", "t_iterations", "t_postprocess", "num_iter",
                "bytes_per_iteration", "ncorner", "nedge", "nface", "ndofc", "sum_ndofi", "sum_ndofo",
-               "ninterface", "precision"]
+               "ninterface", "precision", "h2d_bytes", "d2h_bytes"]
 
 EXPORTS = ["bddcml_init_c", "bddcml_upload_global_data_c", "bddcml_upload_subdomain_data_c",
            "bddcml_setup_preconditioner_c", "bddcml_solve_c", "bddcml_download_local_solution_c",
@@ -34,7 +34,13 @@ EXPORTS = ["bddcml_init_c", "bddcml_upload_global_data_c", "bddcml_upload_subdom
            "bddcml_download_global_reactions_c", "bddcml_change_global_data_c", "bddcml_change_subdomain_data_c",
            "bddcml_setup_new_data_c", "bddcml_dotprod_subdomain_c", "bddcml_finalize_c",
            "bddcml_get_last_error_c", "bddcml_set_precision_c", "bddcml_get_stats_c",
-           "bddcml_get_residual_history_c", "bddcml_get_interface_weights_c", "bddcml_get_coarse_info_c"]
+           "bddcml_get_residual_history_c", "bddcml_get_interface_weights_c", "bddcml_get_coarse_info_c",
+           "bddcml_set_profiling_c", "bddcml_get_profile_c"]
+
+# phases of bddcml_get_profile_c (CUDA events on the solver stream)
+PHASES = ["numeric_total", "solve_total", "factor_interior", "solve_interior", "refine_residual", "schur",
+          "precond_factor", "precond_solve", "precond_blocks", "coarse", "pcg", "schur_apply", "precond_local",
+          "postprocess"]
 
 
 class BddcmlError(RuntimeError):
@@ -215,6 +221,21 @@ def get_interface_weights(isub: int, ndofi: int) -> np.ndarray:
     lib().bddcml_get_interface_weights_c(_i(isub), out.ctypes.data_as(C.POINTER(C.c_double)), _i(ndofi))
     _check()
     return out
+
+
+def set_profiling(on: bool):
+    lib().bddcml_set_profiling_c(_i(1 if on else 0))
+    _check()
+
+
+def get_profile() -> dict:
+    """{phase: (total ms, launches)} from the library's CUDA-event timers."""
+    ms = (C.c_double * 64)()
+    cnt = (C.c_int * 64)()
+    n = C.c_int(64)
+    lib().bddcml_get_profile_c(ms, cnt, C.byref(n))
+    _check()
+    return {k: (ms[i], cnt[i]) for i, k in enumerate(PHASES[: n.value])}
 
 
 def get_coarse_info() -> dict:

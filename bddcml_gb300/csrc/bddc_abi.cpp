@@ -201,6 +201,7 @@ void bddcml_setup_preconditioner_c(int* matrixtype, int* use_defaults_int, int* 
       S->dev = device_create(err);
       if (!S->dev) throw err;
     }
+    device_set_profiling(S->dev, S->profiling);
     Error err{0, ""};
     if (!device_setup(*S, err)) throw err;
     S->setup_done = true;
@@ -331,7 +332,7 @@ void bddcml_get_stats_c(double* stats, int* lstats) {
     double v[] = {q.t_host_setup, q.t_device_setup, q.t_solve, q.t_iterations, q.t_postprocess,
                   (double)q.num_iter, q.bytes_per_iteration, (double)q.ncorner, (double)q.nedge, (double)q.nface,
                   (double)q.ndofc, (double)q.sum_ndofi, (double)q.sum_ndofo, (double)q.ninterface,
-                  (double)S->prm.precision};
+                  (double)S->prm.precision, q.h2d_bytes, q.d2h_bytes};
     int n = std::min<int>(*lstats, (int)(sizeof(v) / sizeof(v[0])));
     for (int i = 0; i < n; ++i) stats[i] = v[i];
     *lstats = n;
@@ -356,6 +357,28 @@ void bddcml_get_interface_weights_c(int* isub, double* wi, int* lwi) {
     Subdomain& s = S->subs[t];
     if (*lwi != (int)s.wi.size()) throw Error{ERR_ARGUMENT, "lwi does not match ndofi"};
     std::copy(s.wi.begin(), s.wi.end(), wi);
+  });
+}
+
+void bddcml_set_profiling_c(int* on) {
+  guarded("bddcml_set_profiling_c", [&] {
+    Solver* S = need_solver("bddcml_set_profiling_c");
+    if (!S) return;
+    S->profiling = *on != 0;
+    if (S->dev) device_set_profiling(S->dev, S->profiling);
+  });
+}
+
+void bddcml_get_profile_c(double* ms, int* counts, int* lphase) {
+  guarded("bddcml_get_profile_c", [&] {
+    Solver* S = need_solver("bddcml_get_profile_c");
+    if (!S) return;
+    double m[NPHASE] = {0};
+    int c[NPHASE] = {0};
+    if (S->dev) device_get_profile(S->dev, m, c);
+    int n = std::min<int>(*lphase, NPHASE);
+    for (int i = 0; i < n; ++i) { ms[i] = m[i]; counts[i] = c[i]; }
+    *lphase = NPHASE;
   });
 }
 

@@ -30,6 +30,62 @@ namespace bddc {
 
 static inline int roundup(int x, int m) { return (x + m - 1) / m * m; }
 
+// Phase timers: CUDA events recorded on the solver's stream.  The two totals
+// are always recorded; the per-phase and per-kernel slots only when profiling
+// is switched on (bddcml_set_profiling_c).
+struct Profiler {
+  bool on = false;
+  struct Rec { int ph; cudaEvent_t a, b; };
+  std::vector<Rec> open, done;
+  std::vector<cudaEvent_t> pool;
+  double ms[NPHASE] = {0};
+  int cnt[NPHASE] = {0};
+  cudaEvent_t get() {
+    cudaEvent_t e;
+    if (!pool.empty()) { e = pool.back(); pool.pop_back(); }
+    else cudaEventCreate(&e);
+    return e;
+  }
+  void begin(int ph, cudaStream_t st, bool always = false) {
+    if (!on && !always) return;
+    Rec r{ph, get(), nullptr};
+    cudaEventRecord(r.a, st);
+    open.push_back(r);
+  }
+  void end(int ph, cudaStream_t st) {
+    for (size_t i = open.size(); i-- > 0;)
+      if (open[i].ph == ph) {
+        Rec r = open[i];
+        open.erase(open.begin() + i);
+        r.b = get();
+        cudaEventRecord(r.b, st);
+        done.push_back(r);
+        return;
+      }
+  }
+  void collect() {
+    for (auto& r : done) {
+      cudaEventSynchronize(r.b);
+      float t = 0.f;
+      cudaEventElapsedTime(&t, r.a, r.b);
+      ms[r.ph] += t;
+      cnt[r.ph] += 1;
+      pool.push_back(r.a);
+      pool.push_back(r.b);
+    }
+    done.clear();
+  }
+  void reset() {
+    collect();
+    for (int i = 0; i < NPHASE; ++i) { ms[i] = 0; cnt[i] = 0; }
+  }
+  ~Profiler() {
+    for (auto& r : open) { cudaEventDestroy(r.a); }
+    for (auto& r : done) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
+    for (auto e : pool) cudaEventDestroy(e);
+  }
+};
+
 template <typename T>
 static T* dalloc(size_t n, std::vector<void*>& owned) {
   T* p = nullptr;
@@ -41,10 +97,14 @@ static T* dalloc(size_t n, std::vector<void*>& owned) {
   return p;
 }
 
+// host<->device traffic of the current setup + solve (reported in the stats)
+static double g_h2d_bytes = 0.0, g_d2h_bytes = 0.0;
+
 template <typename T>
 static T* upload(const std::vector<T>& v, std::vector<void*>& owned, cudaStream_t st) {
   T* p = dalloc<T>(v.size(), owned);
   if (!v.empty()) CK(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+  g_h2d_bytes += (double)v.size() * sizeof(T);
   return p;
 }
 
@@ -94,6 +154,7 @@ class Device {
   std::vector<BandDesc> hbd_oo;
   int maxnbo = 0, maxw = 0, maxNR = 0;
   int nref = 0;
+  Profiler prof;
 
   ~Device() { release(); if (hctl) cudaFreeHost(hctl); if (st) cudaStreamDestroy(st); }
   void release() {
@@ -222,6 +283,9 @@ bool device_setup(Solver& S, Error& err) {
   Device& D = *S.dev;
   try {
     D.release();
+    D.prof.reset();
+    g_h2d_bytes = 0.0;
+    g_d2h_bytes = 0.0;
     D.mixed = S.prm.precision != 0;
     double t0 = wall_time();
     int nsub = (int)S.subs.size();
@@ -246,6 +310,7 @@ bool device_setup(Solver& S, Error& err) {
     CK(cudaStreamSynchronize(D.st));
     if (herr) throw Error{ERR_NUMERIC, "non-positive pivot in a subdomain or coarse factorisation (flags " +
                                             std::to_string(herr) + ")"};
+    D.prof.collect();
     S.stats.t_device_setup = wall_time() - t1;
   } catch (Error& e) {
     err = e;
@@ -447,23 +512,33 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
     D.hbd_oo[t] = BandDesc{d.nbo, d.w, d.NR, 0, d.oL, d.oLinv, d.oXc};
   }
   D.bd_oo = upload(D.hbd_oo, own, st);
+  D.prof.begin(PH_NUMERIC_TOTAL, st, true);
+  D.prof.begin(PH_FACTOR_OO, st);
   k_fill_band<T><<<dim3((D.maxNO + 127) / 128, nsub), 128, 0, st>>>(D.ds, D.koo, poolT, D.bd_oo);
   CKL();
   run_factor<T>(D, D.bd_oo, nsub, D.maxnbo, D.maxw, poolT);
+  D.prof.end(PH_FACTOR_OO, st);
   // ---- interior solves [X | v] = A_oo^-1 [A_oi | f_o], refined in mixed precision
+  D.prof.begin(PH_SOLVE_OO, st);
   k_fill_rhs<T><<<dim3((D.maxNO + 127) / 128, nsub), 128, 0, st>>>(D.ds, D.koi, D.fo, D.fo_off, poolT);
   CKL();
   run_solve<T>(D, D.bd_oo, nsub, D.maxnbo, D.maxNR, poolT, poolT);
+  D.prof.end(PH_SOLVE_OO, st);
   for (int rr = 1; rr <= D.nref; ++rr) {
-    k_residual_df<<<dim3(D.maxNO, nsub), 128, 0, st>>>(D.ds, D.koo, D.koi, D.fo, D.fo_off,
-                                                       reinterpret_cast<float*>(poolT), rr);
-    CKL();
     vector<BandDesc> hb = D.hbd_oo;
     for (int t = 0; t < nsub; ++t) hb[t].oB = D.hs[t].oXc + (long long)rr * D.hs[t].NO * D.hs[t].NR;
     BandDesc* bdr = upload(hb, own, st);
+    D.prof.begin(PH_RESIDUAL, st);
+    k_residual_df<<<dim3(D.maxNO, nsub), 128, 0, st>>>(D.ds, D.koo, D.koi, D.fo, D.fo_off,
+                                                       reinterpret_cast<float*>(poolT), rr);
+    CKL();
+    D.prof.end(PH_RESIDUAL, st);
+    D.prof.begin(PH_SOLVE_OO, st);
     run_solve<T>(D, bdr, nsub, D.maxnbo, D.maxNR, poolT, poolT);
+    D.prof.end(PH_SOLVE_OO, st);
   }
   // ---- Schur complements and the subdomain reduced rhs
+  D.prof.begin(PH_SCHUR, st);
   if (D.mixed) {
     k_schur_df<<<dim3(D.maxNI, nsub), 128, 0, st>>>(D.ds, D.kio, D.kii, reinterpret_cast<const float*>(poolT),
                                                     static_cast<float2*>(D.poolS), D.fi, D.grep);
@@ -479,6 +554,7 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
                                                                                       static_cast<double*>(D.poolS));
     CKL();
   }
+  D.prof.end(PH_SCHUR, st);
   // ---- preconditioner blocks: Srho factor, [Srho^-1 | Y], G^-1, Phi, Z, local coarse matrices
   vector<BandDesc> hbs(nsub);
   for (int t = 0; t < nsub; ++t) {
@@ -486,6 +562,7 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
     hbs[t] = BandDesc{d.nbi, d.nbi - 1, d.NRC, 0, d.oLs, d.oLsinv, d.oBs};
   }
   BandDesc* bd_s = upload(hbs, own, st);
+  D.prof.begin(PH_SRHO_FACTOR, st);
   if constexpr (std::is_same_v<T, float>)
     k_fill_srho<T, float2><<<dim3(D.maxNI / 16, D.maxNI / 16, nsub), dim3(16, 16), 0, st>>>(
         D.ds, static_cast<const float2*>(D.poolS), poolT, bd_s);
@@ -498,9 +575,13 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
     CKL();
   }
   run_factor<T>(D, bd_s, nsub, maxnbi, maxnbi - 1, poolT);
+  D.prof.end(PH_SRHO_FACTOR, st);
+  D.prof.begin(PH_SRHO_SOLVE, st);
   k_fill_rhs_srho<T><<<dim3((D.maxNI + 127) / 128, nsub), 128, 0, st>>>(D.ds, D.c_ptr, D.c_col, D.c_val, poolT);
   CKL();
   run_solve<T>(D, bd_s, nsub, maxnbi, maxNRC, poolT, poolT);
+  D.prof.end(PH_SRHO_SOLVE, st);
+  D.prof.begin(PH_PC_BLOCKS, st);
   {
     size_t smem = 2 * (size_t)std::max(1, maxnc) * std::max(1, maxnc) * sizeof(double);
     CK(cudaFuncSetAttribute(k_small_g<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -521,12 +602,15 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
   CKL();
   k_ac<T><<<dim3((maxnc * maxnc + 255) / 256 + 1, nsub), 256, 0, st>>>(D.ds, poolT, poolPC, D.small);
   CKL();
+  D.prof.end(PH_PC_BLOCKS, st);
+  D.prof.begin(PH_COARSE, st);
 
   // ---- coarse problem: assemble on the host, dense FP64 factor and inverse on the device
   // (levels_prepare_last_level, module_levels.f90:3001-3170)
   {
     vector<double> hsm(oSm);
     CK(cudaMemcpyAsync(hsm.data(), D.small, oSm * sizeof(double), cudaMemcpyDeviceToHost, st));
+    g_d2h_bytes += oSm * sizeof(double);
     CK(cudaStreamSynchronize(st));
     int nc_g = D.ndofc;
     int nbc = std::max(1, (nc_g + NB - 1) / NB);
@@ -558,9 +642,11 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
     run_solve<double>(D, dcb, 1, nbc, D.ldc, D.cpool, D.cpool);
     D.ainv = D.cpool + cb.oB;
   }
+  D.prof.end(PH_COARSE, st);
   // ---- assembled reduced rhs (module_dd.f90:7090-7135)
   k_assemble_plain<<<(D.n + 255) / 256, 256, 0, st>>>(D.n, D.own, D.grep, nullptr, D.g);
   CKL();
+  D.prof.end(PH_NUMERIC_TOTAL, st);
   CK(cudaStreamSynchronize(st));
 }
 
@@ -569,6 +655,7 @@ template <typename T>
 static void launch_schur(Device& D, const double* vin, double* vout, bool zero_fixed, const PcgCtl* ctl,
                          const double* dotvec) {
   dim3 grid(D.nrb, D.nsub);
+  D.prof.begin(PH_SCHUR_APPLY, D.st);
   if (D.mixed) {
     size_t smem = (size_t)D.maxNI * sizeof(float2);
     k_schur_apply_df<<<grid, AT, smem, D.st>>>(D.ds, static_cast<const float2*>(D.poolS), vin, D.uniq, D.yrep, ctl);
@@ -577,6 +664,7 @@ static void launch_schur(Device& D, const double* vin, double* vout, bool zero_f
     k_schur_apply_f64<<<grid, AT, smem, D.st>>>(D.ds, static_cast<const double*>(D.poolS), vin, D.uniq, D.yrep, ctl);
   }
   CKL();
+  D.prof.end(PH_SCHUR_APPLY, D.st);
   k_assemble_dot<<<D.npart, RT, 0, D.st>>>(D.n, D.own, D.yrep, D.fixed, D.wsum, dotvec, vout, D.part, ctl,
                                            zero_fixed ? 1 : 0);
   CKL();
@@ -586,9 +674,11 @@ template <typename T>
 static void launch_pc(Device& D, const double* rin, double* zout, const PcgCtl* ctl) {
   dim3 grid(D.nrb, D.nsub);
   size_t smem = (size_t)D.maxNI * sizeof(T);
+  D.prof.begin(PH_PC_LOCAL, D.st);
   k_pc_local<T><<<grid, AT, smem, D.st>>>(D.ds, static_cast<const T*>(D.poolPC), rin, D.uniq, D.wrep, D.zrep,
                                           D.rcpart, D.nrb, D.ncpmax, ctl);
   CKL();
+  D.prof.end(PH_PC_LOCAL, D.st);
   if (D.ndofc > 0) {
     k_coarse_gather<<<(D.ndofc + 255) / 256, 256, 0, D.st>>>(D.ndofc, D.co_ptr, D.co_sub, D.co_loc, D.ds, D.rcpart,
                                                            D.nrb, D.ncpmax, D.rc, ctl);
@@ -664,8 +754,10 @@ static bool solve_impl(Solver& S, double tol, int maxit, int ndecrmax, int& num_
         x0[u] = (s.bc_present && s.ifix[d]) ? s.fixv[d] : s.sol[d];
       }
     CK(cudaMemcpyAsync(D.x, x0.data(), D.n * sizeof(double), cudaMemcpyHostToDevice, st));
+    g_h2d_bytes += D.n * sizeof(double);
     CK(cudaStreamSynchronize(st));
   }
+  D.prof.begin(PH_SOLVE_TOTAL, st, true);
   // r = g with fixed interface dofs zeroed (module_krylov.f90:222-236)
   k_assemble_plain<<<(D.n + 255) / 256, 256, 0, st>>>(D.n, D.own, D.grep, D.fixed, D.r);
   CKL();
@@ -692,6 +784,7 @@ static bool solve_impl(Solver& S, double tol, int maxit, int ndecrmax, int& num_
       c.iter = 1; c.maxit = maxit; c.ndecrmax = ndecrmax;
       CK(cudaMemcpyAsync(D.ctl, &c, sizeof(PcgCtl), cudaMemcpyHostToDevice, st));
       double tl = wall_time();
+      D.prof.begin(PH_PCG, st);
       const int chunk = 4;
       int launched = 0;
       while (true) {
@@ -710,6 +803,7 @@ static bool solve_impl(Solver& S, double tol, int maxit, int ndecrmax, int& num_
         CK(cudaStreamSynchronize(st));
         if (D.hctl->done || launched > maxit + chunk) break;
       }
+      D.prof.end(PH_PCG, st);
       S.stats.t_iterations = wall_time() - tl;
       PcgCtl c2 = *D.hctl;
       num_iter = c2.num_iter;
@@ -732,6 +826,7 @@ static bool solve_impl(Solver& S, double tol, int maxit, int ndecrmax, int& num_
   // interior values (module_levels.f90:4510-4576)
   double tp = wall_time();
   if (postprocess) {
+    D.prof.begin(PH_POST, st);
     if (D.mixed)
       k_post_df<<<dim3((D.maxNO + 7) / 8, D.nsub), 256, 0, st>>>(D.ds, static_cast<const float*>(D.poolT), D.x, D.uniq,
                                                                  D.uo, D.uo_off);
@@ -739,6 +834,7 @@ static bool solve_impl(Solver& S, double tol, int maxit, int ndecrmax, int& num_
       k_post_f64<<<dim3((D.maxNO + 7) / 8, D.nsub), 256, 0, st>>>(D.ds, static_cast<const double*>(D.poolT), D.x,
                                                                   D.uniq, D.uo, D.uo_off);
     CKL();
+    D.prof.end(PH_POST, st);
     // pull the solution into the subdomain arrays (dd_upload_solution semantics)
     vector<double> hx(D.n);
     size_t nuo = 0;
@@ -746,6 +842,7 @@ static bool solve_impl(Solver& S, double tol, int maxit, int ndecrmax, int& num_
     vector<double> huo(nuo);
     CK(cudaMemcpyAsync(hx.data(), D.x, D.n * sizeof(double), cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(huo.data(), D.uo, nuo * sizeof(double), cudaMemcpyDeviceToHost, st));
+    g_d2h_bytes += (D.n + nuo) * sizeof(double);
     CK(cudaStreamSynchronize(st));
     for (int t = 0; t < D.nsub; ++t) {
       auto& s = S.subs[t];
@@ -755,10 +852,21 @@ static bool solve_impl(Solver& S, double tol, int maxit, int ndecrmax, int& num_
       s.sol = u;
     }
   }
+  D.prof.end(PH_SOLVE_TOTAL, st);
+  D.prof.collect();
+  S.stats.h2d_bytes = g_h2d_bytes;
+  S.stats.d2h_bytes = g_d2h_bytes;
   S.stats.t_postprocess = wall_time() - tp;
   S.stats.t_solve = wall_time() - t0;
   S.stats.num_iter = num_iter;
   return true;
+}
+
+void device_set_profiling(Device* d, bool on) { d->prof.on = on; }
+
+void device_get_profile(Device* d, double* ms, int* cnt) {
+  d->prof.collect();
+  for (int i = 0; i < NPHASE; ++i) { ms[i] = d->prof.ms[i]; cnt[i] = d->prof.cnt[i]; }
 }
 
 bool device_solve(Solver& S, double tol, int maxit, int ndecrmax, int& num_iter, int& reason, double& cond,

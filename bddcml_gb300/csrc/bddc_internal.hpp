@@ -18,6 +18,13 @@ using std::vector;
 // status codes (mirror include/bddcml_gb300.h)
 enum Status { OK = 0, ERR_ARGUMENT = 1, ERR_CUDA = 2, ERR_NUMERIC = 3, ERR_UNSUPPORTED = 4, ERR_MEMORY = 5 };
 
+// timed phases (CUDA events on the solver stream); order is part of the
+// bddcml_get_profile_c extension
+enum Phase {
+  PH_NUMERIC_TOTAL = 0, PH_SOLVE_TOTAL, PH_FACTOR_OO, PH_SOLVE_OO, PH_RESIDUAL, PH_SCHUR, PH_SRHO_FACTOR,
+  PH_SRHO_SOLVE, PH_PC_BLOCKS, PH_COARSE, PH_PCG, PH_SCHUR_APPLY, PH_PC_LOCAL, PH_POST, NPHASE
+};
+
 struct Error {
   int code;
   std::string msg;
@@ -94,7 +101,7 @@ struct Stats {
   long long sum_ndofi = 0, sum_ndofo = 0, ninterface = 0;
   int num_iter = 0;
   double setup_flops = 0;
-  double schur_refine_residual = 0;
+  double h2d_bytes = 0, d2h_bytes = 0;
 };
 
 class Device;  // GPU side (bddc_device.cu)
@@ -113,6 +120,7 @@ struct Solver {
   Device* dev = nullptr;
   Stats stats;
   vector<double> relres_history;
+  bool profiling = false;
 };
 
 // host setup (bddc_host.cpp)
@@ -129,6 +137,8 @@ bool device_setup(Solver& S, Error& err);
 bool device_solve(Solver& S, double tol, int maxit, int ndecrmax, int& num_iter, int& reason, double& cond,
                   Error& err);
 bool device_download(Solver& S, int isub, double* out, Error& err);
+void device_set_profiling(Device* d, bool on);
+void device_get_profile(Device* d, double* ms, int* cnt);
 
 double wall_time();
 

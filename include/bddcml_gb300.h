@@ -152,6 +152,16 @@ void bddcml_get_interface_weights_c(int *isub, double *wi, int *lwi);
  * module_levels.f90:2240-2300 (printed there, returned here). */
 void bddcml_get_coarse_info_c(int *out, int *lout);
 
+/* Switches the per-phase CUDA-event timers on (1) or off (0).  The two totals
+ * (numeric setup, solve) are always timed.  No counterpart in the reference
+ * (its verbosity-2 profiling prints wall times, module_bddcml.f90:91-93). */
+void bddcml_set_profiling_c(int *on);
+
+/* Accumulated milliseconds and counts per timed phase since the last
+ * setup_preconditioner (see bddcml_gb300/__init__.py PHASES for the order);
+ * *lphase in: capacity, out: number of phases. */
+void bddcml_get_profile_c(double *ms, int *counts, int *lphase);
+
 #ifdef __cplusplus
 }
 #endif
