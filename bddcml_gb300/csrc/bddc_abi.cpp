@@ -108,6 +108,7 @@ void bddcml_upload_subdomain_data_c(int* nelem, int* nnod, int* ndof, int* ndim,
                                     double* element_data, int* lelement_data1, int* lelement_data2,
                                     double* dof_data, int* ldof_data, int* find_components_int,
                                     int* use_dual_mesh_graph_int, int* neighbouring) {
+  double tup = wall_time();
   guarded("bddcml_upload_subdomain_data_c", [&] {
     Solver* S = need_solver("bddcml_upload_subdomain_data_c");
     if (!S) return;
@@ -158,16 +159,18 @@ void bddcml_upload_subdomain_data_c(int* nelem, int* nnod, int* ndof, int* ndim,
       if (s.ia[k] < 0 || s.ja[k] >= *ndofs) throw Error{ERR_ARGUMENT, "matrix index out of range"};
     }
     s.a.assign(a_sparse, a_sparse + *la);
+    // assembly (merge of repeated entries) and mesh components are computed
+    // for all subdomains in parallel at setup
+    s.assembled = false;
     (void)is_assembled_int;
-    host_assemble_upper(s.ia, s.ja, s.a);
     s.find_components = find_components_int && *find_components_int != 0;
     s.dual_graph = use_dual_mesh_graph_int && *use_dual_mesh_graph_int != 0;
     s.neighbouring = neighbouring ? *neighbouring : 1;
-    host_nodal_components(s);
     s.loaded = true;
     (void)nelem; (void)nnod; (void)ndof;
     S->nelem = *nelem; S->nnod = *nnod;
     S->setup_done = false;
+    S->t_upload += wall_time() - tup;
   });
 }
 
@@ -194,6 +197,7 @@ void bddcml_setup_preconditioner_c(int* matrixtype, int* use_defaults_int, int* 
     if (S->prm.use_user) throw Error{ERR_UNSUPPORTED, "user constraints are not implemented"};
     double t0 = wall_time();
     S->stats = Stats{};
+    S->stats.t_upload = S->t_upload;
     host_setup(*S);
     S->stats.t_host_setup = wall_time() - t0;
     if (!S->dev) {
@@ -332,7 +336,8 @@ void bddcml_get_stats_c(double* stats, int* lstats) {
     double v[] = {q.t_host_setup, q.t_device_setup, q.t_solve, q.t_iterations, q.t_postprocess,
                   (double)q.num_iter, q.bytes_per_iteration, (double)q.ncorner, (double)q.nedge, (double)q.nface,
                   (double)q.ndofc, (double)q.sum_ndofi, (double)q.sum_ndofo, (double)q.ninterface,
-                  (double)S->prm.precision, q.h2d_bytes, q.d2h_bytes};
+                  (double)S->prm.precision, q.h2d_bytes, q.d2h_bytes, q.t_upload, q.t_host_assemble,
+                  q.t_host_iface, q.t_host_globs, q.t_host_blocks};
     int n = std::min<int>(*lstats, (int)(sizeof(v) / sizeof(v[0])));
     for (int i = 0; i < n; ++i) stats[i] = v[i];
     *lstats = n;

@@ -2,6 +2,7 @@
 // the PCG driver.  See bddc_setup_kernels.cuh and bddc_pcg_kernels.cuh for
 // the kernels and their reference counterparts.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -137,7 +138,10 @@ class Device {
   double *x = nullptr, *r = nullptr, *p = nullptr, *ap = nullptr, *z = nullptr, *g = nullptr;
   double *yrep = nullptr, *zrep = nullptr, *grep = nullptr, *fi = nullptr, *fo = nullptr;
   long long* fo_off = nullptr;
-  double *rcpart = nullptr, *rc = nullptr, *uc = nullptr, *cpool = nullptr, *ainv = nullptr;
+  double *rcpart = nullptr, *rc = nullptr, *uc = nullptr, *cres = nullptr;
+  void* cinv = nullptr;            // explicit coarse inverse (factor precision), ldc x ldc
+  int *ac_ptr = nullptr, *ac_col = nullptr;
+  double* ac_val = nullptr;        // coarse matrix, FP64 CSR
   int ndofc = 0, ldc = 0, nrb = 0, ncpmax = 0, maxNI = 0, maxNO = 0;
   double* part = nullptr;
   int npart = 0;
@@ -211,71 +215,6 @@ static void run_solve(Device& D, const BandDesc* bd, int nbatch, int maxnb, int 
   }
 }
 
-// ------------------------------------------------------- host preparation
-struct SubBlocks {
-  vector<int> oo_ptr, oo_col, oi_ptr, oi_col, io_ptr, io_col, ii_ptr, ii_col;
-  vector<double> oo_val, oi_val, io_val, ii_val;
-  vector<double> fo, fi;  // interior rhs (new order), interface rhs (weighted)
-  int w = 0;
-  double rho = 1.0;
-  int maxrow_oo = 0, maxrow_oi = 0, maxrow_io = 0, maxrow_ii = 0;
-};
-
-static void prepare_blocks(Subdomain& s, SubBlocks& b) {
-  vector<int> fptr, fcol;
-  vector<double> fval;
-  full_symmetric_csr(s, fptr, fcol, fval);
-  host_interior_ordering(s, fptr, fcol);
-  int no = s.ndofo, ni = s.ndofi;
-  vector<int> onew(s.ndof, -1), iidx(s.ndof, -1);
-  for (int q = 0; q < no; ++q) onew[s.iovsvn[s.operm[q]]] = q;
-  for (int i = 0; i < ni; ++i) iidx[s.iivsvn[i]] = i;
-  auto build = [&](int nrow, auto rowdof, const vector<int>& colmap, vector<int>& ptr, vector<int>& col,
-                   vector<double>& val, int& maxrow) {
-    ptr.assign(nrow + 1, 0);
-    col.clear(); val.clear();
-    maxrow = 0;
-    for (int r = 0; r < nrow; ++r) {
-      int d = rowdof(r);
-      for (int k = fptr[d]; k < fptr[d + 1]; ++k) {
-        int c = colmap[fcol[k]];
-        if (c >= 0) { col.push_back(c); val.push_back(fval[k]); }
-      }
-      ptr[r + 1] = (int)col.size();
-      maxrow = std::max(maxrow, ptr[r + 1] - ptr[r]);
-    }
-  };
-  auto orow = [&](int r) { return s.iovsvn[s.operm[r]]; };
-  auto irow = [&](int r) { return s.iivsvn[r]; };
-  build(no, orow, onew, b.oo_ptr, b.oo_col, b.oo_val, b.maxrow_oo);
-  build(no, orow, iidx, b.oi_ptr, b.oi_col, b.oi_val, b.maxrow_oi);
-  build(ni, irow, onew, b.io_ptr, b.io_col, b.io_val, b.maxrow_io);
-  build(ni, irow, iidx, b.ii_ptr, b.ii_col, b.ii_val, b.maxrow_ii);
-  b.w = 0;
-  for (int r = 0; r < no; ++r)
-    for (int k = b.oo_ptr[r]; k < b.oo_ptr[r + 1]; ++k)
-      if (b.oo_col[k] <= r) b.w = std::max(b.w, r / NB - b.oo_col[k] / NB);
-  // reduced-rhs input: weighted rhs, Dirichlet rows zeroed, weighted bc added
-  // (module_dd.f90:7040-7075 and sm_prepare_rhs, module_sm.f90:603-628)
-  vector<double> f = s.rhs;
-  vector<double> bcw = s.bc;
-  if (s.rhs_complete) for (int i = 0; i < ni; ++i) f[s.iivsvn[i]] *= s.wi[i];
-  for (int i = 0; i < ni; ++i) bcw[s.iivsvn[i]] *= s.wi[i];
-  if (s.bc_present)
-    for (int i = 0; i < s.ndof; ++i) { if (s.ifix[i]) f[i] = 0.0; f[i] += bcw[i]; }
-  b.fo.resize(no);
-  for (int q = 0; q < no; ++q) b.fo[q] = f[orow(q)];
-  b.fi.resize(ni);
-  for (int i = 0; i < ni; ++i) b.fi[i] = f[s.iivsvn[i]];
-  double sd = 0.0;
-  int cnt = 0;
-  for (int i = 0; i < ni; ++i)
-    for (int k = b.ii_ptr[i]; k < b.ii_ptr[i + 1]; ++k)
-      if (b.ii_col[k] == i) { sd += std::fabs(b.ii_val[k]); cnt++; }
-  b.rho = cnt ? sd / cnt : 1.0;
-  if (!(b.rho > 0.0)) b.rho = 1.0;
-}
-
 template <typename T>
 static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk);
 
@@ -290,9 +229,7 @@ bool device_setup(Solver& S, Error& err) {
     double t0 = wall_time();
     int nsub = (int)S.subs.size();
     D.nsub = nsub;
-    vector<SubBlocks> blk(nsub);
-#pragma omp parallel for schedule(dynamic)
-    for (int t = 0; t < nsub; ++t) prepare_blocks(S.subs[t], blk[t]);
+    vector<SubBlocks>& blk = S.blocks;
     for (int t = 0; t < nsub; ++t) {
       auto& b = blk[t];
       if (b.maxrow_oo > 96 || b.maxrow_oi > 95 || b.maxrow_io > 128 || b.maxrow_ii > 128)
@@ -304,6 +241,7 @@ bool device_setup(Solver& S, Error& err) {
     double t1 = wall_time();
     if (D.mixed) setup_numeric<float>(S, D, blk);
     else setup_numeric<double>(S, D, blk);
+    vector<SubBlocks>().swap(S.blocks);
     // check device error flags
     int herr = 0;
     CK(cudaMemcpyAsync(&herr, D.err, sizeof(int), cudaMemcpyDeviceToHost, D.st));
@@ -605,42 +543,59 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
   D.prof.end(PH_PC_BLOCKS, st);
   D.prof.begin(PH_COARSE, st);
 
-  // ---- coarse problem: assemble on the host, dense FP64 factor and inverse on the device
-  // (levels_prepare_last_level, module_levels.f90:3001-3170)
+  // ---- coarse problem (levels_prepare_last_level, module_levels.f90:3001-3170):
+  // sparse FP64 matrix assembled on the device in a fixed order, factor and
+  // explicit inverse in factor precision; the solve is refined in FP64.
   {
-    vector<double> hsm(oSm);
-    CK(cudaMemcpyAsync(hsm.data(), D.small, oSm * sizeof(double), cudaMemcpyDeviceToHost, st));
-    g_d2h_bytes += oSm * sizeof(double);
-    CK(cudaStreamSynchronize(st));
     int nc_g = D.ndofc;
     int nbc = std::max(1, (nc_g + NB - 1) / NB);
     D.ldc = nbc * NB;
-    vector<double> A((size_t)D.ldc * D.ldc, 0.0);
+    // sparsity and contribution lists (integer work only)
+    vector<std::array<long long, 3>> ent;  // (row, col, contribution index)
     for (int t = 0; t < nsub; ++t) {
-      auto& s = S.subs[t];
+      auto& sb = S.subs[t];
       auto& d = D.hs[t];
       for (int a = 0; a < d.nc; ++a)
         for (int b2 = 0; b2 < d.nc; ++b2)
-          A[(size_t)s.indrowc[a] * D.ldc + s.indrowc[b2]] += hsm[d.oAc + (size_t)a * d.ncp + b2];
+          ent.push_back({(long long)sb.indrowc[a], (long long)sb.indrowc[b2], d.oAc + (long long)a * d.ncp + b2});
     }
-    for (int q = nc_g; q < D.ldc; ++q) A[(size_t)q * D.ldc + q] = 1.0;
-    // block layout: nbc x nbc lower blocks, then inverted diagonal blocks, then the identity RHS
+    std::sort(ent.begin(), ent.end());
+    vector<int> aptr(nc_g + 1, 0), acol, acptr(1, 0);
+    vector<long long> acontrib;
+    for (size_t k = 0; k < ent.size(); ++k) {
+      bool fresh = k == 0 || ent[k][0] != ent[k - 1][0] || ent[k][1] != ent[k - 1][1];
+      if (fresh) {
+        if (k) acptr.push_back((int)acontrib.size());
+        acol.push_back((int)ent[k][1]);
+        aptr[ent[k][0] + 1]++;
+      }
+      acontrib.push_back(ent[k][2]);
+    }
+    acptr.push_back((int)acontrib.size());
+    for (int q = 0; q < nc_g; ++q) aptr[q + 1] += aptr[q];
+    D.ac_ptr = upload(aptr, own, st);
+    D.ac_col = upload(acol, own, st);
+    int* dcptr = upload(acptr, own, st);
+    long long* dcontrib = upload(acontrib, own, st);
+    D.ac_val = dalloc<double>(acol.size(), own);
     BandDesc cb{nbc, nbc - 1, D.ldc, 0, 0, (long long)nbc * nbc * NB * NB,
                 (long long)nbc * nbc * NB * NB + (long long)nbc * NB * NB};
     size_t csize = (size_t)cb.oB + (size_t)D.ldc * D.ldc;
-    vector<double> hc(csize, 0.0);
-    for (int i = 0; i < D.ldc; ++i)
-      for (int j = 0; j <= i; ++j) {
-        double v = 0.5 * (A[(size_t)i * D.ldc + j] + A[(size_t)j * D.ldc + i]);
-        hc[band_block(cb, i / NB, j / NB) + (i % NB) * NB + j % NB] = v;
-      }
-    for (int i = 0; i < D.ldc; ++i) hc[cb.oB + (size_t)i * D.ldc + i] = 1.0;
-    D.cpool = upload(hc, own, st);
+    T* cpool = dalloc<T>(csize, own);
+    CK(cudaMemsetAsync(cpool, 0, csize * sizeof(T), st));
+    if (nc_g > 0) {
+      k_coarse_assemble<T><<<nc_g, 128, 0, st>>>(nc_g, D.ac_ptr, D.ac_col, dcptr, dcontrib, D.small, D.ac_val,
+                                                  cpool, cb);
+      CKL();
+    }
+    k_coarse_pad<T><<<(D.ldc + 255) / 256, 256, 0, st>>>(nc_g, D.ldc, cpool, cb);
+    CKL();
     vector<BandDesc> hcb{cb};
     BandDesc* dcb = upload(hcb, own, st);
-    run_factor<double>(D, dcb, 1, nbc, nbc - 1, D.cpool);
-    run_solve<double>(D, dcb, 1, nbc, D.ldc, D.cpool, D.cpool);
-    D.ainv = D.cpool + cb.oB;
+    run_factor<T>(D, dcb, 1, nbc, nbc - 1, cpool);
+    run_solve<T>(D, dcb, 1, nbc, D.ldc, cpool, cpool);
+    D.cinv = cpool + cb.oB;
+    D.cres = dalloc<double>(std::max(1, nc_g), own);
   }
   D.prof.end(PH_COARSE, st);
   // ---- assembled reduced rhs (module_dd.f90:7090-7135)
@@ -683,7 +638,14 @@ static void launch_pc(Device& D, const double* rin, double* zout, const PcgCtl* 
     k_coarse_gather<<<(D.ndofc + 255) / 256, 256, 0, D.st>>>(D.ndofc, D.co_ptr, D.co_sub, D.co_loc, D.ds, D.rcpart,
                                                            D.nrb, D.ncpmax, D.rc, ctl);
     CKL();
-    k_coarse_solve<<<(D.ndofc + 7) / 8, 256, 0, D.st>>>(D.ndofc, D.ldc, D.ainv, D.rc, D.uc, ctl);
+    const T* minv = static_cast<const T*>(D.cinv);
+    int gb = (D.ndofc + 7) / 8;
+    k_coarse_gemv<T><<<gb, 256, 0, D.st>>>(D.ndofc, D.ldc, minv, D.rc, D.uc, 0, ctl);
+    for (int rr = 0; rr < 2; ++rr) {
+      k_coarse_residual<<<(D.ndofc + 255) / 256, 256, 0, D.st>>>(D.ndofc, D.ac_ptr, D.ac_col, D.ac_val, D.rc, D.uc,
+                                                               D.cres, ctl);
+      k_coarse_gemv<T><<<gb, 256, 0, D.st>>>(D.ndofc, D.ldc, minv, D.cres, D.uc, 1, ctl);
+    }
     CKL();
   }
   k_assemble_z<T><<<D.npart, RT, 0, D.st>>>(D.n, D.own, D.ds, static_cast<const T*>(D.poolPC), D.zrep, D.wrep,

@@ -247,8 +247,14 @@ void host_setup(Solver& S) {
     for (int g : s.isvgvn) ndof_global = std::max(ndof_global, g + 1);
   }
 
-  // ---- Dirichlet elimination on each subdomain matrix (module_sm.f90:431-600)
-  for (auto& s : S.subs) {
+  // ---- assembly of the uploaded triplets, mesh components and Dirichlet
+  // elimination on each subdomain matrix (module_sm.f90:431-600, 630-684)
+  double tt = wall_time();
+#pragma omp parallel for schedule(dynamic)
+  for (int t = 0; t < nsub; ++t) {
+    auto& s = S.subs[t];
+    if (!s.assembled) { host_assemble_upper(s.ia, s.ja, s.a); s.assembled = true; }
+    host_nodal_components(s);
     s.bc.assign(s.ndof, 0.0);
     s.bc_present = false;
     for (int i = 0; i < s.ndof; ++i) if (s.ifix[i] != 0) s.bc_present = true;
@@ -266,16 +272,21 @@ void host_setup(Solver& S) {
         diag_fixed[i] = 1;
       }
     }
+    bool added = false;
     for (int i = 0; i < s.ndof; ++i)
       if (s.ifix[i] > 0 && !diag_fixed[i]) {
         s.ia.push_back(i); s.ja.push_back(i); s.a.push_back(1.0);
         s.bc[i] += s.fixv[i];
+        added = true;
       }
-    host_assemble_upper(s.ia, s.ja, s.a);
+    if (added) host_assemble_upper(s.ia, s.ja, s.a);
   }
+  S.stats.t_host_assemble = wall_time() - tt;
+  tt = wall_time();
 
   // ---- interface and neighbours
   Sharing sh = build_sharing(S, nnod_global);
+#pragma omp parallel for schedule(dynamic)
   for (int t = 0; t < nsub; ++t) {
     auto& s = S.subs[t];
     s.kdof.assign(s.nnod, 0);
@@ -301,9 +312,13 @@ void host_setup(Solver& S) {
     for (int u = 0; u < nsub; ++u) if (isadj[u]) s.adj.push_back(u);
   }
 
+  S.stats.t_host_iface = wall_time() - tt;
+  tt = wall_time();
   // ---- pass 1: glob classification and corner selection, per subdomain
   vector<char> corner_node(nnod_global, 0);  // union of all subdomains' corner choices
+  vector<vector<int>> pass1_corners(nsub);
   int meshdim = S.subs.empty() ? 3 : S.subs[0].ndim;
+#pragma omp parallel for schedule(dynamic)
   for (int t = 0; t < nsub; ++t) {
     auto& s = S.subs[t];
     int nnodi = s.nnodi;
@@ -410,8 +425,10 @@ void host_setup(Solver& S) {
         }
       }
     }
-    for (int i = 0; i < nnodi; ++i) if (type[i] == 3) corner_node[s.isngn[s.iin[i]]] = 1;
+    for (int i = 0; i < nnodi; ++i) if (type[i] == 3) pass1_corners[t].push_back(s.isngn[s.iin[i]]);
   }
+  for (auto& v : pass1_corners)
+    for (int g : v) corner_node[g] = 1;
 
   // ---- coarse numbering of a class of entities identified by a global node id:
   // owner = lowest subdomain index holding the node; numbers run over
@@ -443,6 +460,7 @@ void host_setup(Solver& S) {
 
   // corners of each subdomain, ascending global id
   vector<vector<int>> corner_gid(nsub), corner_num;
+#pragma omp parallel for schedule(dynamic)
   for (int t = 0; t < nsub; ++t) {
     auto& s = S.subs[t];
     for (int i = 0; i < s.nnodi; ++i)
@@ -454,6 +472,7 @@ void host_setup(Solver& S) {
   // ---- pass 2: edges and faces, Dirichlet node removal
   vector<vector<vector<int>>> edges(nsub), faces(nsub);  // node lists (inodi)
   vector<vector<int>> edge_gid(nsub), face_gid(nsub), edge_num, face_num;
+#pragma omp parallel for schedule(dynamic)
   for (int t = 0; t < nsub; ++t) {
     auto& s = S.subs[t];
     std::unordered_map<Sig, int, SigHash> eidx, fidx;
@@ -506,6 +525,7 @@ void host_setup(Solver& S) {
   // ---- coarse nodes and constraints
   int ncnode = S.ncorner + S.nedge + S.nface;
   vector<int> nndfc(ncnode, -1);
+#pragma omp parallel for schedule(dynamic)
   for (int t = 0; t < nsub; ++t) {
     auto& s = S.subs[t];
     s.cnodes.clear();
@@ -530,16 +550,19 @@ void host_setup(Solver& S) {
       add(3, corner_num[t][c], {inodi_of.at(corner_gid[t][c])}, S.prm.use_corner);
     for (size_t e = 0; e < edges[t].size(); ++e) add(2, edge_num[t][e], edges[t][e], S.prm.use_arith);
     for (size_t f = 0; f < faces[t].size(); ++f) add(1, face_num[t][f], faces[t][f], S.prm.use_arith);
+  }
+  for (auto& s : S.subs)
     for (auto& cn : s.cnodes) {
       int& slot = nndfc[cn.global_number - 1];
       if (slot >= 0 && slot != cn.ncdof) throw Error{ERR_NUMERIC, "inconsistent coarse node dof count"};
       slot = cn.ncdof;
     }
-  }
   vector<int> kdofc(ncnode + 1, 0);
   for (int c = 0; c < ncnode; ++c) kdofc[c + 1] = kdofc[c] + std::max(0, nndfc[c]);
   S.ndofc = kdofc[ncnode];
-  for (auto& s : S.subs) {
+#pragma omp parallel for schedule(dynamic)
+  for (int t = 0; t < nsub; ++t) {
+    auto& s = S.subs[t];
     s.c_ptr.assign(1, 0); s.c_col.clear(); s.c_val.clear(); s.indrowc.clear();
     for (auto& cn : s.cnodes) {
       if (!cn.used) continue;
@@ -603,6 +626,7 @@ void host_setup(Solver& S) {
       bci[t].resize(s.ndofi);
       for (int i = 0; i < s.ndofi; ++i) bci[t][i] = s.bc[s.iivsvn[i]];
     }
+#pragma omp parallel for schedule(dynamic)
     for (int t = 0; t < nsub; ++t) {
       auto& s = S.subs[t];
       for (int i = 0; i < s.ndofi; ++i) {
@@ -626,6 +650,7 @@ void host_setup(Solver& S) {
         throw Error{ERR_UNSUPPORTED, "weights_type " + std::to_string(S.prm.weights_type) + " is not implemented"};
       }
     }
+#pragma omp parallel for schedule(dynamic)
     for (int t = 0; t < nsub; ++t) {
       auto& s = S.subs[t];
       s.wi.resize(s.ndofi);
@@ -650,6 +675,72 @@ void host_setup(Solver& S) {
   for (auto& s : S.subs) { S.stats.sum_ndofi += s.ndofi; S.stats.sum_ndofo += s.ndofo; }
   S.stats.ninterface = S.ninterface;
   S.ndof_global = ndof_global;
+  S.stats.t_host_globs = wall_time() - tt;
+  // ---- device-ready blocks (interior reordering, CSR splits, reduced-rhs inputs)
+  tt = wall_time();
+  S.blocks.assign(nsub, SubBlocks{});
+#pragma omp parallel for schedule(dynamic)
+  for (int t = 0; t < nsub; ++t) host_prepare_blocks(S.subs[t], S.blocks[t]);
+  S.stats.t_host_blocks = wall_time() - tt;
 }
+
+// ---------------------------------------------------- device-ready blocks
+
+void host_prepare_blocks(Subdomain& s, SubBlocks& b) {
+  constexpr int NB = 64;
+  vector<int> fptr, fcol;
+  vector<double> fval;
+  full_symmetric_csr(s, fptr, fcol, fval);
+  host_interior_ordering(s, fptr, fcol);
+  int no = s.ndofo, ni = s.ndofi;
+  vector<int> onew(s.ndof, -1), iidx(s.ndof, -1);
+  for (int q = 0; q < no; ++q) onew[s.iovsvn[s.operm[q]]] = q;
+  for (int i = 0; i < ni; ++i) iidx[s.iivsvn[i]] = i;
+  auto build = [&](int nrow, auto rowdof, const vector<int>& colmap, vector<int>& ptr, vector<int>& col,
+                   vector<double>& val, int& maxrow) {
+    ptr.assign(nrow + 1, 0);
+    col.clear(); val.clear();
+    maxrow = 0;
+    for (int r = 0; r < nrow; ++r) {
+      int d = rowdof(r);
+      for (int k = fptr[d]; k < fptr[d + 1]; ++k) {
+        int c = colmap[fcol[k]];
+        if (c >= 0) { col.push_back(c); val.push_back(fval[k]); }
+      }
+      ptr[r + 1] = (int)col.size();
+      maxrow = std::max(maxrow, ptr[r + 1] - ptr[r]);
+    }
+  };
+  auto orow = [&](int r) { return s.iovsvn[s.operm[r]]; };
+  auto irow = [&](int r) { return s.iivsvn[r]; };
+  build(no, orow, onew, b.oo_ptr, b.oo_col, b.oo_val, b.maxrow_oo);
+  build(no, orow, iidx, b.oi_ptr, b.oi_col, b.oi_val, b.maxrow_oi);
+  build(ni, irow, onew, b.io_ptr, b.io_col, b.io_val, b.maxrow_io);
+  build(ni, irow, iidx, b.ii_ptr, b.ii_col, b.ii_val, b.maxrow_ii);
+  b.w = 0;
+  for (int r = 0; r < no; ++r)
+    for (int k = b.oo_ptr[r]; k < b.oo_ptr[r + 1]; ++k)
+      if (b.oo_col[k] <= r) b.w = std::max(b.w, r / NB - b.oo_col[k] / NB);
+  // reduced-rhs input: weighted rhs, Dirichlet rows zeroed, weighted bc added
+  // (module_dd.f90:7040-7075 and sm_prepare_rhs, module_sm.f90:603-628)
+  vector<double> f = s.rhs;
+  vector<double> bcw = s.bc;
+  if (s.rhs_complete) for (int i = 0; i < ni; ++i) f[s.iivsvn[i]] *= s.wi[i];
+  for (int i = 0; i < ni; ++i) bcw[s.iivsvn[i]] *= s.wi[i];
+  if (s.bc_present)
+    for (int i = 0; i < s.ndof; ++i) { if (s.ifix[i]) f[i] = 0.0; f[i] += bcw[i]; }
+  b.fo.resize(no);
+  for (int q = 0; q < no; ++q) b.fo[q] = f[orow(q)];
+  b.fi.resize(ni);
+  for (int i = 0; i < ni; ++i) b.fi[i] = f[s.iivsvn[i]];
+  double sd = 0.0;
+  int cnt = 0;
+  for (int i = 0; i < ni; ++i)
+    for (int k = b.ii_ptr[i]; k < b.ii_ptr[i + 1]; ++k)
+      if (b.ii_col[k] == i) { sd += std::fabs(b.ii_val[k]); cnt++; }
+  b.rho = cnt ? sd / cnt : 1.0;
+  if (!(b.rho > 0.0)) b.rho = 1.0;
+}
+
 
 }  // namespace bddc

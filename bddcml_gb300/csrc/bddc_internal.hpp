@@ -49,9 +49,10 @@ struct Subdomain {
   vector<double> fixv, rhs, sol;
   bool rhs_complete = true;
   int matrixtype = 1;
-  vector<int> ia, ja;  // assembled upper triangle
+  vector<int> ia, ja;  // upper triangle (merged at setup)
   vector<double> a;
   bool loaded = false;
+  bool assembled = false;
   bool find_components = true;
   bool dual_graph = true;
   int neighbouring = 1;
@@ -102,6 +103,19 @@ struct Stats {
   int num_iter = 0;
   double setup_flops = 0;
   double h2d_bytes = 0, d2h_bytes = 0;
+  double t_upload = 0, t_host_assemble = 0, t_host_iface = 0, t_host_globs = 0, t_host_blocks = 0;
+};
+
+// Per-subdomain matrix blocks in device-ready form (interior rows in the
+// band-reducing order): A_oo, A_oi, A_io, A_ii as CSR, the reduced-rhs inputs
+// and the band width of A_oo in 64-row blocks.
+struct SubBlocks {
+  vector<int> oo_ptr, oo_col, oi_ptr, oi_col, io_ptr, io_col, ii_ptr, ii_col;
+  vector<double> oo_val, oi_val, io_val, ii_val;
+  vector<double> fo, fi;  // interior rhs (new order), interface rhs (weighted)
+  int w = 0;
+  double rho = 1.0;
+  int maxrow_oo = 0, maxrow_oi = 0, maxrow_io = 0, maxrow_ii = 0;
 };
 
 class Device;  // GPU side (bddc_device.cu)
@@ -121,6 +135,8 @@ struct Solver {
   Stats stats;
   vector<double> relres_history;
   bool profiling = false;
+  double t_upload = 0;              // accumulated time inside the upload calls
+  vector<SubBlocks> blocks;         // device-ready blocks, freed after upload
 };
 
 // host setup (bddc_host.cpp)
@@ -129,6 +145,7 @@ void host_nodal_components(Subdomain& s);
 void host_setup(Solver& S);              // everything integer/geometric + BC + weights + constraints
 void host_interior_ordering(Subdomain& s, const vector<int>& f_ptr, const vector<int>& f_col);
 void full_symmetric_csr(const Subdomain& s, vector<int>& ptr, vector<int>& col, vector<double>& val);
+void host_prepare_blocks(Subdomain& s, SubBlocks& b);
 
 // device (bddc_device.cu)
 Device* device_create(Error& err);

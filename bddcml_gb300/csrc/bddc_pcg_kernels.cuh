@@ -179,18 +179,63 @@ __global__ void k_coarse_gather(int ndofc, const int* __restrict__ cptr, const i
   rc[q] = t;
 }
 
-// u_c = Ac^-1 r_c (dense FP64, warp per row)
-__global__ void __launch_bounds__(256) k_coarse_solve(int n, int ld, const double* __restrict__ ainv,
-                                                      const double* __restrict__ rc, double* __restrict__ uc,
-                                                      const PcgCtl* __restrict__ ctl) {
+// Coarse solve u_c = Ac^-1 r_c by an explicit inverse M of the coarse matrix
+// (factor precision) with FP64 refinement against the FP64 coarse matrix:
+//   u = M r;  repeat: u += M (r - Ac u).
+// mode 0: u = M v;  mode 1: u += M v  (warp per row, FP64 accumulation)
+template <typename T>
+__global__ void __launch_bounds__(256) k_coarse_gemv(int n, int ld, const T* __restrict__ m,
+                                                     const double* __restrict__ v, double* __restrict__ u, int mode,
+                                                     const PcgCtl* __restrict__ ctl) {
   if (ctl && ctl->done) return;
   int row = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   if (row >= n) return;
-  const double* a = ainv + (long long)row * ld;
+  const T* a = m + (long long)row * ld;
   double t = 0.0;
-  for (int j = lane; j < n; j += 32) t += a[j] * rc[j];
+  for (int j = lane; j < n; j += 32) t += (double)a[j] * v[j];
   for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-  if (lane == 0) uc[row] = t;
+  if (lane == 0) u[row] = mode ? u[row] + t : t;
+}
+
+// res = r - Ac u with the sparse FP64 coarse matrix
+__global__ void k_coarse_residual(int n, const int* __restrict__ ptr, const int* __restrict__ col,
+                                  const double* __restrict__ val, const double* __restrict__ r,
+                                  const double* __restrict__ u, double* __restrict__ res,
+                                  const PcgCtl* __restrict__ ctl) {
+  if (ctl && ctl->done) return;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double t = r[i];
+  for (int q = ptr[i]; q < ptr[i + 1]; ++q) t -= val[q] * u[col[q]];
+  res[i] = t;
+}
+
+// deterministic assembly of the coarse matrix: every nonzero sums its
+// subdomain contributions in a fixed order (levels_prepare_last_level,
+// module_levels.f90:3075-3090); the lower part is also written, in factor
+// precision, into the dense block layout that the factor kernels use
+template <typename T>
+__global__ void k_coarse_assemble(int n, const int* __restrict__ ptr, const int* __restrict__ col,
+                                  const int* __restrict__ cptr, const long long* __restrict__ contrib,
+                                  const double* __restrict__ small, double* __restrict__ val, T* __restrict__ fpool,
+                                  BandDesc d) {
+  int i = blockIdx.x;
+  if (i >= n) return;
+  for (int q = ptr[i] + threadIdx.x; q < ptr[i + 1]; q += blockDim.x) {
+    double t = 0.0;
+    for (int e = cptr[q]; e < cptr[q + 1]; ++e) t += small[contrib[e]];
+    val[q] = t;
+    int j = col[q];
+    if (j <= i) fpool[band_block(d, i / NB, j / NB) + (i % NB) * NB + j % NB] = T(t);
+  }
+}
+
+template <typename T>
+__global__ void k_coarse_pad(int n, int ld, T* __restrict__ fpool, BandDesc d) {
+  int i = n + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < ld) fpool[band_block(d, i / NB, i / NB) + (i % NB) * NB + i % NB] = T(1);
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < ld) fpool[d.oB + (long long)k * ld + k] = T(1);  // identity right-hand side
 }
 
 // z[g] = sum_s w_s (z_s + Phi_s u_c|_s); partial (r, z)
