@@ -13,6 +13,7 @@
 
 #include "bddc_internal.hpp"
 #include "bddc_pcg_kernels.cuh"
+#include "bddc_tc.cuh"
 
 namespace bddc {
 
@@ -202,6 +203,32 @@ static void run_factor(Device& D, const BandDesc* bd, int nbatch, int maxnb, int
   }
 }
 
+// FP32 factors: panels for the tensor-core sweeps (after the factorisation)
+static void run_panels(Device& D, const BandDesc* bd, const TcDesc* td, int nbatch, int maxnb, int maxw,
+                       const float* L, float* P) {
+  k_make_panels<<<dim3(maxw + 1, maxnb, nbatch), NT, 0, D.st>>>(bd, td, L, P);
+  CKL();
+}
+
+// forward + backward sweeps on the tensor cores (3xTF32, TMEM accumulation)
+static void run_solve_tc(Device& D, const TcDesc* td, int nbatch, int maxnb, int maxncol, const float* P, float* B) {
+  static bool attr = false;
+  const size_t smem = tc_smem_bytes();
+  if (!attr) {
+    CK(cudaFuncSetAttribute(k_band_step_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = true;
+  }
+  dim3 grid(maxncol / TC_M, nbatch);
+  for (int k = 0; k < maxnb; ++k) {
+    k_band_step_tc<<<grid, TC_THREADS, smem, D.st>>>(td, P, B, k, 0, D.err);
+    CKL();
+  }
+  for (int k = maxnb - 1; k >= 0; --k) {
+    k_band_step_tc<<<grid, TC_THREADS, smem, D.st>>>(td, P, B, k, 1, D.err);
+    CKL();
+  }
+}
+
 template <typename T>
 static void run_solve(Device& D, const BandDesc* bd, int nbatch, int maxnb, int maxncol, const T* L, T* B) {
   dim3 grid(maxncol / NB, nbatch);
@@ -266,7 +293,8 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
 
   // ---- sizes and offsets
   D.hs.assign(nsub, DevSub{});
-  long long oT = 0, oS = 0, oPC = 0, oSm = 0;
+  long long oT = 0, oS = 0, oPC = 0, oSm = 0, oPan = 0;
+  vector<std::array<long long, 4>> poff(nsub, {0, 0, 0, 0});
   int rep = 0, koo = 0, koi = 0, kio = 0, kii = 0, cptr = 0, coff = 0;
   D.maxnbo = 0; D.maxw = 0; D.maxNR = 0; D.maxNI = 0; D.maxNO = 0; D.ncpmax = 4;
   int maxnbi = 0, maxNRC = 0, maxnc = 0;
@@ -277,8 +305,8 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
     d.no = s.ndofo; d.ni = s.ndofi; d.nc = s.nconstr;
     d.ncp = roundup(std::max(1, d.nc), 4);
     d.NO = roundup(d.no, NB); d.NI = roundup(d.ni, NB);
-    d.NR = roundup(d.ni + 1, NB);
-    d.NRC = d.NI + roundup(std::max(1, d.nc), NB);
+    d.NR = roundup(d.ni + 1, TC_M);
+    d.NRC = roundup(d.NI + std::max(1, d.nc), TC_M);
     d.nbo = d.NO / NB; d.w = b.w; d.nbi = d.NI / NB; d.nref = D.nref;
     d.oL = oT; oT += (long long)d.nbo * (d.w + 1) * NB * NB;
     d.oLinv = oT; oT += (long long)d.nbo * NB * NB;
@@ -286,6 +314,12 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
     d.oLs = oT; oT += (long long)d.nbi * d.nbi * NB * NB;
     d.oLsinv = oT; oT += (long long)d.nbi * NB * NB;
     d.oBs = oT; oT += (long long)d.NI * d.NRC;
+    if (std::is_same_v<T, float>) {
+      poff[t][0] = oPan; oPan += (long long)d.nbo * (d.w + 1) * 2 * TC_PCHUNK;
+      poff[t][1] = oPan; oPan += (long long)d.nbo * (d.w + 1) * 2 * TC_PCHUNK;
+      poff[t][2] = oPan; oPan += (long long)d.nbi * d.nbi * 2 * TC_PCHUNK;
+      poff[t][3] = oPan; oPan += (long long)d.nbi * d.nbi * 2 * TC_PCHUNK;
+    }
     d.oS = oS; oS += (long long)d.NI * d.NI;
     d.oZ = oPC; oPC += (long long)d.NI * d.NI;
     d.oPhi = oPC; oPC += (long long)d.NI * d.ncp;
@@ -312,6 +346,7 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
 
   // ---- allocations
   D.poolT = dalloc<T>(oT, own);
+  float* ppool = std::is_same_v<T, float> ? dalloc<float>(oPan, own) : nullptr;
   D.poolS = D.mixed ? (void*)dalloc<float2>(oS, own) : (void*)dalloc<double>(oS, own);
   D.poolPC = dalloc<T>(oPC, own);
   D.small = dalloc<double>(oSm, own);
@@ -442,6 +477,7 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
     CK(cudaFuncSetAttribute(k_schur_apply_f64, cudaFuncAttributeMaxDynamicSharedMemorySize,
                             (int)(D.maxNI * sizeof(double))));
   CK(cudaFuncSetAttribute(k_pc_local<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(D.maxNI * sizeof(T))));
+  (void)ppool;
 
   // ---- interior band factor
   D.hbd_oo.resize(nsub);
@@ -455,12 +491,23 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
   k_fill_band<T><<<dim3((D.maxNO + 127) / 128, nsub), 128, 0, st>>>(D.ds, D.koo, poolT, D.bd_oo);
   CKL();
   run_factor<T>(D, D.bd_oo, nsub, D.maxnbo, D.maxw, poolT);
+  vector<TcDesc> htd(nsub);
+  TcDesc* td_oo = nullptr;
+  if constexpr (std::is_same_v<T, float>) {
+    for (int t = 0; t < nsub; ++t) {
+      auto& d = D.hs[t];
+      htd[t] = TcDesc{d.nbo, d.w, d.NR, 0, d.oXc, poff[t][0], poff[t][1]};
+    }
+    td_oo = upload(htd, own, st);
+    run_panels(D, D.bd_oo, td_oo, nsub, D.maxnbo, D.maxw, poolT, ppool);
+  }
   D.prof.end(PH_FACTOR_OO, st);
   // ---- interior solves [X | v] = A_oo^-1 [A_oi | f_o], refined in mixed precision
   D.prof.begin(PH_SOLVE_OO, st);
   k_fill_rhs<T><<<dim3((D.maxNO + 127) / 128, nsub), 128, 0, st>>>(D.ds, D.koi, D.fo, D.fo_off, poolT);
   CKL();
-  run_solve<T>(D, D.bd_oo, nsub, D.maxnbo, D.maxNR, poolT, poolT);
+  if constexpr (std::is_same_v<T, float>) run_solve_tc(D, td_oo, nsub, D.maxnbo, D.maxNR, ppool, poolT);
+  else run_solve<T>(D, D.bd_oo, nsub, D.maxnbo, D.maxNR, poolT, poolT);
   D.prof.end(PH_SOLVE_OO, st);
   for (int rr = 1; rr <= D.nref; ++rr) {
     vector<BandDesc> hb = D.hbd_oo;
@@ -472,7 +519,14 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
     CKL();
     D.prof.end(PH_RESIDUAL, st);
     D.prof.begin(PH_SOLVE_OO, st);
-    run_solve<T>(D, bdr, nsub, D.maxnbo, D.maxNR, poolT, poolT);
+    if constexpr (std::is_same_v<T, float>) {
+      vector<TcDesc> h2 = htd;
+      for (int t = 0; t < nsub; ++t) h2[t].oB = hb[t].oB;
+      TcDesc* tdr = upload(h2, own, st);
+      run_solve_tc(D, tdr, nsub, D.maxnbo, D.maxNR, ppool, poolT);
+    } else {
+      run_solve<T>(D, bdr, nsub, D.maxnbo, D.maxNR, poolT, poolT);
+    }
     D.prof.end(PH_SOLVE_OO, st);
   }
   // ---- Schur complements and the subdomain reduced rhs
@@ -513,11 +567,22 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
     CKL();
   }
   run_factor<T>(D, bd_s, nsub, maxnbi, maxnbi - 1, poolT);
+  TcDesc* td_s = nullptr;
+  if constexpr (std::is_same_v<T, float>) {
+    vector<TcDesc> hts(nsub);
+    for (int t = 0; t < nsub; ++t) {
+      auto& d = D.hs[t];
+      hts[t] = TcDesc{d.nbi, d.nbi - 1, d.NRC, 0, d.oBs, poff[t][2], poff[t][3]};
+    }
+    td_s = upload(hts, own, st);
+    run_panels(D, bd_s, td_s, nsub, maxnbi, maxnbi - 1, poolT, ppool);
+  }
   D.prof.end(PH_SRHO_FACTOR, st);
   D.prof.begin(PH_SRHO_SOLVE, st);
   k_fill_rhs_srho<T><<<dim3((D.maxNI + 127) / 128, nsub), 128, 0, st>>>(D.ds, D.c_ptr, D.c_col, D.c_val, poolT);
   CKL();
-  run_solve<T>(D, bd_s, nsub, maxnbi, maxNRC, poolT, poolT);
+  if constexpr (std::is_same_v<T, float>) run_solve_tc(D, td_s, nsub, maxnbi, maxNRC, ppool, poolT);
+  else run_solve<T>(D, bd_s, nsub, maxnbi, maxNRC, poolT, poolT);
   D.prof.end(PH_SRHO_SOLVE, st);
   D.prof.begin(PH_PC_BLOCKS, st);
   {
@@ -548,7 +613,7 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
   // explicit inverse in factor precision; the solve is refined in FP64.
   {
     int nc_g = D.ndofc;
-    int nbc = std::max(1, (nc_g + NB - 1) / NB);
+    int nbc = std::max(2, (nc_g + TC_M - 1) / TC_M * 2);  // even number of 64-blocks: ld multiple of 128
     D.ldc = nbc * NB;
     // sparsity and contribution lists (integer work only)
     vector<std::array<long long, 3>> ent;  // (row, col, contribution index)
@@ -593,7 +658,16 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
     vector<BandDesc> hcb{cb};
     BandDesc* dcb = upload(hcb, own, st);
     run_factor<T>(D, dcb, 1, nbc, nbc - 1, cpool);
-    run_solve<T>(D, dcb, 1, nbc, D.ldc, cpool, cpool);
+    if constexpr (std::is_same_v<T, float>) {
+      // identity right-hand side needs a column count that is a multiple of the MMA tile
+      vector<TcDesc> htc{TcDesc{nbc, nbc - 1, D.ldc, 0, cb.oB, 0, (long long)nbc * nbc * 2 * TC_PCHUNK}};
+      TcDesc* tdc = upload(htc, own, st);
+      float* cpan = dalloc<float>((size_t)2 * nbc * nbc * 2 * TC_PCHUNK, own);
+      run_panels(D, dcb, tdc, 1, nbc, nbc - 1, cpool, cpan);
+      run_solve_tc(D, tdc, 1, nbc, D.ldc, cpan, cpool);
+    } else {
+      run_solve<T>(D, dcb, 1, nbc, D.ldc, cpool, cpool);
+    }
     D.cinv = cpool + cb.oB;
     D.cres = dalloc<double>(std::max(1, nc_g), own);
   }

@@ -1,0 +1,355 @@
+// 5th-generation tensor-core path (tcgen05, TMEM, bulk TMA) for the block-band
+// triangular sweeps of the subdomain solves.
+//
+// One sweep step computes, for every subdomain and every 128-column tile of
+// the right-hand-side block B (row-major, FP32):
+//     B[k-block rows, tile] = P_k  x  B[window rows, tile]
+// where the window is the band of block rows that block row k depends on and
+// P_k (64 x window) is a precomputed panel with the inverted diagonal block
+// folded in:
+//     forward : P_k = [-Linv_kk L_k,j0 ... -Linv_kk L_k,k-1 | Linv_kk]
+//     backward: Q_k = [Linv_kk^T | -Linv_kk^T L_k+1,k^T ... -Linv_kk^T L_k+w,k^T]
+// so that each step is one contraction on the tensor cores.
+//
+// Precision: 3xTF32 (Ootomo & Yokota's split a = hi + lo with hi = tf32(a);
+// a*b ~ hi*hi + hi*lo + lo*hi), FP32 accumulation in TMEM.  This is the
+// FP32-class inner solve of the refinement loop in the setup.
+//
+// MMA shape: M = 128 (columns of B), N = 64 (rows of the output block),
+// K = 8 per instruction, both operands K-major in the canonical no-swizzle
+// layout (core matrices of 8 rows x 16 bytes).  The panel operand is stored
+// in global memory already split and laid out per 32-wide K chunk and is
+// moved by cp.async.bulk; the window operand is read from global memory,
+// split into hi/lo and written into the canonical layout by all threads.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "bddc_kernels.cuh"
+
+namespace bddc {
+
+constexpr int TC_M = 128;            // columns of B per CTA (MMA M)
+constexpr int TC_N = 64;             // output rows (MMA N)
+constexpr int TC_KC = 32;            // K chunk staged per pipeline stage
+constexpr int TC_THREADS = 128;
+constexpr int TC_STAGES = 2;
+constexpr int TC_PCHUNK = TC_N * TC_KC * 2;     // floats per panel chunk (hi + lo)
+constexpr int TC_ACHUNK = TC_M * TC_KC;         // floats per window-operand half (hi or lo)
+constexpr uint32_t TC_LBO = 128;                // bytes between K-adjacent core matrices
+constexpr uint32_t TC_SBO = (TC_KC / 4) * 128;  // bytes between 8-row groups
+constexpr long long TC_SPIN_LIMIT = 1LL << 26;  // bounded waits
+enum { DE_TIMEOUT = 8 };
+
+// offset (floats) of element (row r, k) inside one canonical K-major operand
+// tile of TC_KC columns
+__host__ __device__ __forceinline__ int canon_off(int r, int k) {
+  return (r >> 3) * (TC_SBO / 4) + (k >> 2) * (TC_LBO / 4) + (r & 7) * 4 + (k & 3);
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// bounded wait: returns false after the spin limit
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (long long i = 0; i < TC_SPIN_LIMIT; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// shared-memory matrix descriptor: canonical K-major, no swizzle
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)((TC_LBO >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((TC_SBO >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;  // descriptor version of the 5th-generation tensor core
+  return d;
+}
+
+// instruction descriptor: kind::tf32, D = F32, A = B = TF32, both K-major
+__host__ __device__ constexpr uint32_t tc_idesc(int M, int N) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ float tf32_rna(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
+struct TcDesc {
+  int nb, w, ncol, pad;
+  long long oB;      // RHS block (row-major, ld = ncol) in the work pool
+  long long oPf;     // forward panels in the panel pool
+  long long oPb;     // backward panels
+};
+
+// panel storage: block row k, chunk q at ((k * (w+1)*2) + q) * TC_PCHUNK
+__host__ __device__ __forceinline__ long long panel_chunk(long long base, int w, int k, int q) {
+  return base + ((long long)k * (w + 1) * 2 + q) * TC_PCHUNK;
+}
+
+// one sweep step for all subdomains: grid (max column tiles, batch)
+// dir = 0 forward, 1 backward
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_band_step_tc(const TcDesc* __restrict__ td, const float* __restrict__ ppool, float* __restrict__ bpool, int k,
+                   int dir, int* __restrict__ err) {
+  const TcDesc d = td[blockIdx.y];
+  const int c0 = blockIdx.x * TC_M;
+  if (k >= d.nb || c0 >= d.ncol) return;
+  // window of block rows
+  int j0, nblk;
+  if (dir == 0) { j0 = k - min(k, d.w); nblk = k - j0 + 1; }
+  else { j0 = k; nblk = min(d.w, d.nb - 1 - k) + 1; }
+  const int nchunk = nblk * (NB / TC_KC);
+  const int ld = d.ncol;
+  float* B = bpool + d.oB;
+  const float* P = ppool + (dir == 0 ? d.oPf : d.oPb);
+
+  extern __shared__ __align__(1024) unsigned char smraw[];
+  float* sA = reinterpret_cast<float*>(smraw);                  // [stage][hi|lo][TC_ACHUNK]
+  float* sP = sA + TC_STAGES * 2 * TC_ACHUNK;                    // [stage][TC_PCHUNK]
+  __shared__ __align__(8) uint64_t bar_p[TC_STAGES], bar_mma[TC_STAGES];
+  __shared__ uint32_t tmem_base;
+  __shared__ int abort_flag;
+  __shared__ int last_commit, tma_pending[TC_STAGES];
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid == 0) {
+    for (int s = 0; s < TC_STAGES; ++s) {
+      mbar_init(&bar_p[s], 1);
+      mbar_init(&bar_mma[s], 1);
+      tma_pending[s] = -1;
+    }
+    abort_flag = 0;
+    last_commit = -1;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                 "r"(TC_N));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_base;
+  constexpr uint32_t idesc = tc_idesc(TC_M, TC_N);
+
+  int committed = 0;  // number of commits issued (thread 0)
+  for (int q = 0; q < nchunk; ++q) {
+    const int st = q & 1;
+    if (q >= TC_STAGES) {
+      // stage reuse: the MMAs of chunk q-2 must have finished reading it
+      if (!mbar_wait(&bar_mma[st], ((q - TC_STAGES) >> 1) & 1)) { if (tid == 0) abort_flag = 1; }
+    }
+    __syncthreads();
+    if (abort_flag) break;
+    if (tid == 0) {
+      mbar_expect_tx(&bar_p[st], TC_PCHUNK * 4);
+      bulk_g2s(sP + st * TC_PCHUNK, P + panel_chunk(0, d.w, k, q), TC_PCHUNK * 4, &bar_p[st]);
+      tma_pending[st] = q;
+    }
+    // window operand: rows r = j0*64 + q*32 + t, columns c0 + tid -> A[m = tid][k = t]
+    {
+      float* ahi = sA + (st * 2 + 0) * TC_ACHUNK;
+      float* alo = sA + (st * 2 + 1) * TC_ACHUNK;
+      const float* src = B + (long long)(j0 * NB + q * TC_KC) * ld + c0 + tid;
+      float v[TC_KC];
+#pragma unroll
+      for (int t = 0; t < TC_KC; ++t) v[t] = src[(long long)t * ld];
+#pragma unroll
+      for (int t4 = 0; t4 < TC_KC / 4; ++t4) {
+        float4 h, l;
+        h.x = tf32_rna(v[4 * t4 + 0]); l.x = v[4 * t4 + 0] - h.x;
+        h.y = tf32_rna(v[4 * t4 + 1]); l.y = v[4 * t4 + 1] - h.y;
+        h.z = tf32_rna(v[4 * t4 + 2]); l.z = v[4 * t4 + 2] - h.z;
+        h.w = tf32_rna(v[4 * t4 + 3]); l.w = v[4 * t4 + 3] - h.w;
+        int off = canon_off(tid, 4 * t4);
+        *reinterpret_cast<float4*>(ahi + off) = h;
+        *reinterpret_cast<float4*>(alo + off) = l;
+      }
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    if (tid == 0) {
+      tc_fence_after();
+      if (!mbar_wait(&bar_p[st], (q >> 1) & 1)) {
+        abort_flag = 1;
+      } else {
+        tma_pending[st] = -1;
+        const uint32_t a_hi = smem_u32(sA + (st * 2 + 0) * TC_ACHUNK);
+        const uint32_t a_lo = smem_u32(sA + (st * 2 + 1) * TC_ACHUNK);
+        const uint32_t p_hi = smem_u32(sP + st * TC_PCHUNK);
+        const uint32_t p_lo = p_hi + TC_N * TC_KC * 4;
+#pragma unroll
+        for (int kk = 0; kk < TC_KC / 8; ++kk) {
+          const uint32_t koff = kk * 2 * TC_LBO;
+          uint32_t acc = (q > 0 || kk > 0) ? 1u : 0u;
+          mma_tf32(tmem, tc_desc(a_lo + koff), tc_desc(p_hi + koff), idesc, acc);
+          mma_tf32(tmem, tc_desc(a_hi + koff), tc_desc(p_lo + koff), idesc, 1u);
+          mma_tf32(tmem, tc_desc(a_hi + koff), tc_desc(p_hi + koff), idesc, 1u);
+        }
+        mma_commit(&bar_mma[st]);
+        last_commit = q;
+        committed++;
+      }
+    }
+  }
+  // wait for the last commit (and, after an abort, for copies still in
+  // flight), then read the accumulator out of TMEM
+  __syncthreads();
+  bool ok = abort_flag == 0;
+  if (tid == 0) {
+    int ql = last_commit;
+    if (ql >= 0 && !mbar_wait(&bar_mma[ql & 1], (ql >> 1) & 1)) abort_flag = 1;
+    for (int s2 = 0; s2 < TC_STAGES; ++s2)
+      if (tma_pending[s2] >= 0 && !mbar_wait(&bar_p[s2], (tma_pending[s2] >> 1) & 1)) abort_flag = 1;
+    if (ok && ql != nchunk - 1) abort_flag = 1;
+  }
+  __syncthreads();
+  ok = abort_flag == 0;
+  tc_fence_after();
+  if (ok) {
+    // warp w holds TMEM lanes 32w..32w+31 = columns c0 + 32w + lane; 64 accumulator columns = output rows
+    const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+    float* dst = B + (long long)(k * NB) * ld + c0 + warp * 32 + lane;
+#pragma unroll
+    for (int part = 0; part < TC_N / 16; ++part) {
+      float v[16];
+      tmem_ld16(taddr + part * 16, v);
+#pragma unroll
+      for (int i = 0; i < 16; ++i) dst[(long long)(part * 16 + i) * ld] = v[i];
+    }
+  } else if (tid == 0) {
+    atomicOr(err, DE_TIMEOUT);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_N));
+  (void)committed;
+}
+
+constexpr size_t tc_smem_bytes() { return (size_t)TC_STAGES * (2 * TC_ACHUNK + TC_PCHUNK) * sizeof(float); }
+
+// ------------------------------------------------------------- panels
+// Builds the forward and backward panels of a block-band factor (FP32):
+// P_k[:, jj-th block] for block j = j0 + jj and Q_k[:, ii-th block] for block
+// i = k + ii, each written as two 32-wide K chunks in canonical hi/lo form.
+// grid (w+1, nb, batch), 256 threads; 64x64 SIMT products in FP32.
+__global__ void __launch_bounds__(NT) k_make_panels(const BandDesc* __restrict__ bd, const TcDesc* __restrict__ td,
+                                                    const float* __restrict__ lpool, float* __restrict__ ppool) {
+  const BandDesc d = bd[blockIdx.z];
+  const TcDesc t = td[blockIdx.z];
+  const int k = blockIdx.y, jj = blockIdx.x;
+  if (k >= d.nb) return;
+  __shared__ __align__(16) float smA[KC * NB];
+  __shared__ __align__(16) float smB[KC * NB];
+  __shared__ float tile[NB][NB + 1];
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const float* Li = lpool + d.oLinv + (long long)k * NB * NB;
+  for (int dir = 0; dir < 2; ++dir) {
+    int nblk = dir == 0 ? (k - (k - min(k, d.w)) + 1) : (min(d.w, d.nb - 1 - k) + 1);
+    if (jj >= nblk) continue;
+    float acc[4][4];
+    tile_zero(acc);
+    if (dir == 0) {
+      int j = k - min(k, d.w) + jj;
+      if (j == k) {
+        for (int e = tid; e < NB * NB; e += NT) tile[e / NB][e % NB] = Li[e];
+      } else {
+        tile_gemm<float, false, false>(acc, Li, NB, lpool + band_block(d, k, j), NB, NB, smA, smB);
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+#pragma unroll
+          for (int p = 0; p < 4; ++p) tile[ty * 4 + q][tx * 4 + p] = -acc[q][p];
+      }
+    } else {
+      int i = k + jj;
+      if (i == k) {
+        for (int e = tid; e < NB * NB; e += NT) tile[e % NB][e / NB] = Li[e];  // transpose
+      } else {
+        // -Linv_kk^T L_ik^T = -(L_ik Linv_kk)^T
+        tile_gemm<float, false, false>(acc, lpool + band_block(d, i, k), NB, Li, NB, NB, smA, smB);
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+#pragma unroll
+          for (int p = 0; p < 4; ++p) tile[tx * 4 + p][ty * 4 + q] = -acc[q][p];
+      }
+    }
+    __syncthreads();
+    float* dst0 = ppool + panel_chunk(dir == 0 ? t.oPf : t.oPb, d.w, k, 2 * jj);
+    for (int e = tid; e < NB * NB; e += NT) {
+      int r = e / NB, c = e % NB;  // r = output row (N), c = K index within this block
+      float v = tile[r][c];
+      float h = tf32_rna(v);
+      float* dst = dst0 + (c / TC_KC) * TC_PCHUNK;
+      int off = canon_off(r, c % TC_KC);
+      dst[off] = h;
+      dst[TC_N * TC_KC + off] = v - h;
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace bddc
