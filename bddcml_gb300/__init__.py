@@ -27,7 +27,8 @@ STATUS = {0: "OK", 1: "ARGUMENT", 2: "CUDA", 3: "NUMERIC", 4: "UNSUPPORTED", 5: 
 STAT_FIELDS = ["t_host_setup", "t_device_setup", "t_solve", "t_iterations", "t_postprocess", "num_iter",
                "bytes_per_iteration", "ncorner", "nedge", "nface", "ndofc", "sum_ndofi", "sum_ndofo",
                "ninterface", "precision", "h2d_bytes", "d2h_bytes", "t_upload", "t_host_assemble",
-               "t_host_iface", "t_host_globs", "t_host_blocks"]
+               "t_host_iface", "t_host_globs", "t_host_blocks", "refine1", "refine2",
+               "flop_sweep_oo", "flop_sweep_s", "bytes_residual", "bytes_schur_apply", "bytes_pc_local"]
 
 EXPORTS = ["bddcml_init_c", "bddcml_upload_global_data_c", "bddcml_upload_subdomain_data_c",
            "bddcml_setup_preconditioner_c", "bddcml_solve_c", "bddcml_download_local_solution_c",

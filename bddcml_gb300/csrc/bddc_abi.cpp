@@ -337,7 +337,8 @@ void bddcml_get_stats_c(double* stats, int* lstats) {
                   (double)q.num_iter, q.bytes_per_iteration, (double)q.ncorner, (double)q.nedge, (double)q.nface,
                   (double)q.ndofc, (double)q.sum_ndofi, (double)q.sum_ndofo, (double)q.ninterface,
                   (double)S->prm.precision, q.h2d_bytes, q.d2h_bytes, q.t_upload, q.t_host_assemble,
-                  q.t_host_iface, q.t_host_globs, q.t_host_blocks};
+                  q.t_host_iface, q.t_host_globs, q.t_host_blocks, q.refine1, q.refine2,
+                  q.flop_sweep_oo, q.flop_sweep_s, q.bytes_residual, q.bytes_schur_apply, q.bytes_pc_local};
     int n = std::min<int>(*lstats, (int)(sizeof(v) / sizeof(v[0])));
     for (int i = 0; i < n; ++i) stats[i] = v[i];
     *lstats = n;

@@ -310,7 +310,7 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
     d.nbo = d.NO / NB; d.w = b.w; d.nbi = d.NI / NB; d.nref = D.nref;
     d.oL = oT; oT += (long long)d.nbo * (d.w + 1) * NB * NB;
     d.oLinv = oT; oT += (long long)d.nbo * NB * NB;
-    d.oXc = oT; oT += (long long)(d.nref + 1) * d.NO * d.NR;
+    d.oXc = oT; oT += (long long)(d.nref == 0 ? 1 : (d.nref == 1 ? 2 : 3)) * d.NO * d.NR;
     d.oLs = oT; oT += (long long)d.nbi * d.nbi * NB * NB;
     d.oLsinv = oT; oT += (long long)d.nbi * NB * NB;
     d.oBs = oT; oT += (long long)d.NI * d.NRC;
@@ -340,6 +340,23 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
     maxnbi = std::max(maxnbi, d.nbi); maxNRC = std::max(maxNRC, d.NRC); maxnc = std::max(maxnc, d.nc);
   }
   D.nrep = rep;
+  {
+    auto sweep = [](int nb, int w, int ncol) {
+      double f = 0.0;
+      for (int k = 0; k < nb; ++k)
+        f += 2.0 * NB * ncol * NB * ((std::min(k, w) + 1) + (std::min(w, nb - 1 - k) + 1));
+      return f;
+    };
+    S.stats.flop_sweep_oo = S.stats.flop_sweep_s = S.stats.bytes_residual = 0;
+    S.stats.bytes_schur_apply = S.stats.bytes_pc_local = 0;
+    for (auto& d : D.hs) {
+      S.stats.flop_sweep_oo += sweep(d.nbo, d.w, d.NR);
+      S.stats.flop_sweep_s += sweep(d.nbi, d.nbi - 1, d.NRC);
+      S.stats.bytes_residual += (double)d.NO * d.NR * 4.0 * 3.0;
+      S.stats.bytes_schur_apply += (double)d.ni * d.NI * 8.0 + d.ni * 16.0;
+      S.stats.bytes_pc_local += (double)d.ni * d.NI * sizeof(T) + (double)d.ni * d.ncp * sizeof(T) + d.ni * 24.0;
+    }
+  }
   S.stats.bytes_per_iteration = 0;
   for (auto& d : D.hs)
     S.stats.bytes_per_iteration += (double)d.NI * d.NI * (D.mixed ? (8.0 + 4.0) : 16.0);
@@ -509,13 +526,25 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
   if constexpr (std::is_same_v<T, float>) run_solve_tc(D, td_oo, nsub, D.maxnbo, D.maxNR, ppool, poolT);
   else run_solve<T>(D, D.bd_oo, nsub, D.maxnbo, D.maxNR, poolT, poolT);
   D.prof.end(PH_SOLVE_OO, st);
+  // iterative refinement of [X | v] with FP64-accurate residuals: X is kept
+  // as a double-float pair in components 0 and 1, corrections land in the
+  // next free component and are merged
+  int* dmax = nullptr;
+  vector<int> hmax;
+  if (D.prof.on && D.mixed) {
+    dmax = dalloc<int>((size_t)nsub * 3, own);
+    CK(cudaMemsetAsync(dmax, 0, (size_t)nsub * 3 * sizeof(int), st));
+    k_comp_maxabs<<<dim3(64, nsub), 256, 0, st>>>(D.ds, reinterpret_cast<const float*>(poolT), 0, dmax);
+    CKL();
+  }
   for (int rr = 1; rr <= D.nref; ++rr) {
+    const int outc = rr == 1 ? 1 : 2;
     vector<BandDesc> hb = D.hbd_oo;
-    for (int t = 0; t < nsub; ++t) hb[t].oB = D.hs[t].oXc + (long long)rr * D.hs[t].NO * D.hs[t].NR;
+    for (int t = 0; t < nsub; ++t) hb[t].oB = D.hs[t].oXc + (long long)outc * D.hs[t].NO * D.hs[t].NR;
     BandDesc* bdr = upload(hb, own, st);
     D.prof.begin(PH_RESIDUAL, st);
     k_residual_df<<<dim3(D.maxNO, nsub), 128, 0, st>>>(D.ds, D.koo, D.koi, D.fo, D.fo_off,
-                                                       reinterpret_cast<float*>(poolT), rr);
+                                                       reinterpret_cast<float*>(poolT), rr > 1 ? 1 : 0, outc);
     CKL();
     D.prof.end(PH_RESIDUAL, st);
     D.prof.begin(PH_SOLVE_OO, st);
@@ -528,6 +557,31 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
       run_solve<T>(D, bdr, nsub, D.maxnbo, D.maxNR, poolT, poolT);
     }
     D.prof.end(PH_SOLVE_OO, st);
+    if (dmax && rr <= 2) {
+      k_comp_maxabs<<<dim3(64, nsub), 256, 0, st>>>(D.ds, reinterpret_cast<const float*>(poolT), outc,
+                                                     dmax + (size_t)rr * nsub);
+      CKL();
+    }
+    D.prof.begin(PH_RESIDUAL, st);
+    k_merge_df<<<dim3(256, nsub), 256, 0, st>>>(D.ds, reinterpret_cast<float*>(poolT), outc);
+    CKL();
+    D.prof.end(PH_RESIDUAL, st);
+  }
+  if (dmax) {
+    hmax.resize((size_t)nsub * 3);
+    CK(cudaMemcpyAsync(hmax.data(), dmax, hmax.size() * sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    float r1 = 0.f, r2 = 0.f;
+    for (int t = 0; t < nsub; ++t) {
+      float x0;
+      std::memcpy(&x0, &hmax[t], 4);
+      float d1, d2;
+      std::memcpy(&d1, &hmax[nsub + t], 4);
+      std::memcpy(&d2, &hmax[2 * nsub + t], 4);
+      if (x0 > 0) { r1 = std::max(r1, d1 / x0); r2 = std::max(r2, d2 / x0); }
+    }
+    S.stats.refine1 = r1;
+    S.stats.refine2 = r2;
   }
   // ---- Schur complements and the subdomain reduced rhs
   D.prof.begin(PH_SCHUR, st);
@@ -535,15 +589,15 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
     k_schur_df<<<dim3(D.maxNI, nsub), 128, 0, st>>>(D.ds, D.kio, D.kii, reinterpret_cast<const float*>(poolT),
                                                     static_cast<float2*>(D.poolS), D.fi, D.grep);
     CKL();
-    k_symmetrize_df<<<dim3(D.maxNI / 16, D.maxNI / 16, nsub), dim3(16, 16), 0, st>>>(D.ds,
-                                                                                     static_cast<float2*>(D.poolS));
+    k_symmetrize<float2><<<dim3(D.maxNI / 32, D.maxNI / 32, nsub), dim3(32, 8), 0, st>>>(
+        D.ds, static_cast<float2*>(D.poolS), 0);
     CKL();
   } else {
     k_schur_f64<<<dim3(D.maxNI, nsub), 128, 0, st>>>(D.ds, D.kio, D.kii, reinterpret_cast<const double*>(poolT),
                                                      static_cast<double*>(D.poolS), D.fi, D.grep);
     CKL();
-    k_symmetrize_f64<<<dim3(D.maxNI / 16, D.maxNI / 16, nsub), dim3(16, 16), 0, st>>>(D.ds,
-                                                                                      static_cast<double*>(D.poolS));
+    k_symmetrize<double><<<dim3(D.maxNI / 32, D.maxNI / 32, nsub), dim3(32, 8), 0, st>>>(
+        D.ds, static_cast<double*>(D.poolS), 0);
     CKL();
   }
   D.prof.end(PH_SCHUR, st);
@@ -595,15 +649,7 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
   CKL();
   k_z<T><<<dim3(D.maxNI / 16, D.maxNI / 16, nsub), dim3(16, 16), 0, st>>>(D.ds, poolT, poolPC);
   CKL();
-  k_symmetrize_t<T><<<dim3(D.maxNI / 16, D.maxNI / 16, nsub), dim3(16, 16), 0, st>>>(D.ds, poolPC);
-  CKL();
-  if constexpr (std::is_same_v<T, float>)
-    k_sphi<T, float2><<<dim3(D.maxNI, nsub), 64, 0, st>>>(D.ds, static_cast<const float2*>(D.poolS), poolPC, poolT);
-  else
-    k_sphi<T, double><<<dim3(D.maxNI, nsub), 64, 0, st>>>(D.ds, reinterpret_cast<const double*>(D.poolS), poolPC,
-                                                          poolT);
-  CKL();
-  k_ac<T><<<dim3((maxnc * maxnc + 255) / 256 + 1, nsub), 256, 0, st>>>(D.ds, poolT, poolPC, D.small);
+  k_symmetrize<T><<<dim3(D.maxNI / 32, D.maxNI / 32, nsub), dim3(32, 8), 0, st>>>(D.ds, poolPC, 1);
   CKL();
   D.prof.end(PH_PC_BLOCKS, st);
   D.prof.begin(PH_COARSE, st);

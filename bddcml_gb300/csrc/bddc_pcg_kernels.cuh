@@ -398,11 +398,12 @@ __global__ void __launch_bounds__(256) k_post_df(const DevSub* __restrict__ ds, 
   int row = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   if (row >= s.no) return;
   const long long comp = (long long)s.NO * s.NR;
-  const float* X = pool + s.oXc + (long long)row * s.NR;
+  const float* X0 = pool + s.oXc + (long long)row * s.NR;
+  const float* X1 = X0 + comp;
   dfacc acc;
   for (int j = lane; j <= s.ni; j += 32) {
     dfloat xv = j < s.ni ? df_from_double(-x[uniq[s.rep + j]]) : dfloat{1.f, 0.f};
-    for (int m = 0; m <= s.nref; ++m) acc.fma_df(xv, X[m * comp + j]);
+    acc.fma_df(xv, dfloat{X0[j], X1[j]});
   }
   for (int o = 16; o > 0; o >>= 1) {
     dfacc other;

@@ -229,12 +229,14 @@ __global__ void k_fill_rhs(const DevSub* __restrict__ ds, CsrView koi, const dou
 }
 
 // Refinement residual of the interior solves, FP64-accurate on FP32 pipes:
-// R = [A_oi | f_o] - A_oo (X_0 + ... + X_{ncomp-1}), written as FP32 into component ncomp.
-// One CTA per interior row; the row's matrix entries are staged in shared memory.
+// R = [A_oi | f_o] - A_oo X, written as FP32 into component `outcomp`.  X is
+// component 0 (an exact FP32 value, xpair = 0) or the double-float pair held
+// in components 0 and 1 (xpair = 1).  One CTA per interior row; the row's
+// matrix entries are staged in shared memory; padding columns are zero.
 __global__ void __launch_bounds__(128) k_residual_df(const DevSub* __restrict__ ds, CsrView koo, CsrView koi,
                                                      const double* __restrict__ fo,
                                                      const long long* __restrict__ fo_off, float* __restrict__ pool,
-                                                     int ncomp) {
+                                                     int xpair, int outcomp) {
   const DevSub s = ds[blockIdx.y];
   const int r = blockIdx.x;
   if (r >= s.NO) return;
@@ -243,15 +245,15 @@ __global__ void __launch_bounds__(128) k_residual_df(const DevSub* __restrict__ 
   __shared__ int bcol[96];
   __shared__ dfloat bval[96];
   __shared__ int nnz, nb0;
-  float* out = pool + s.oXc + (long long)ncomp * s.NO * s.NR + (long long)r * s.NR;
+  const long long comp = (long long)s.NO * s.NR;
+  float* out = pool + s.oXc + (long long)outcomp * comp + (long long)r * s.NR;
   if (r >= s.no) {
     for (int c = threadIdx.x; c < s.NR; c += blockDim.x) out[c] = 0.f;
     return;
   }
   if (threadIdx.x == 0) {
     const int* p = koo.ptr + s.koo;
-    int n = min(96, p[r + 1] - p[r]);
-    nnz = n;
+    nnz = min(96, p[r + 1] - p[r]);
     const int* pb = koi.ptr + s.koi;
     nb0 = min(95, pb[r + 1] - pb[r]);
   }
@@ -273,18 +275,56 @@ __global__ void __launch_bounds__(128) k_residual_df(const DevSub* __restrict__ 
     }
   }
   __syncthreads();
-  const long long comp = (long long)s.NO * s.NR;
-  const float* X = pool + s.oXc;
+  const float* X0 = pool + s.oXc;
+  const float* X1 = X0 + comp;
   for (int c = threadIdx.x; c < s.NR; c += blockDim.x) {
+    if (c > s.ni) { out[c] = 0.f; continue; }
     dfacc acc;
     for (int q = 0; q <= nb0; ++q)
       if (bcol[q] == c) acc.add_df(bval[q]);
-    for (int q = 0; q < nnz; ++q) {
-      const float* xr = X + (long long)scol[q] * s.NR + c;
-      for (int m = 0; m < ncomp; ++m) acc.fma_df(sval[q], xr[m * comp]);
+    if (xpair) {
+      for (int q = 0; q < nnz; ++q) {
+        long long o = (long long)scol[q] * s.NR + c;
+        acc.fma_df(sval[q], dfloat{X0[o], X1[o]});
+      }
+    } else {
+      for (int q = 0; q < nnz; ++q) acc.fma_df(sval[q], X0[(long long)scol[q] * s.NR + c]);
     }
     out[c] = acc.value().hi;
   }
+}
+
+// X <- X + D: components (0, 1) hold X as a double-float pair (component 1
+// is taken as zero when addcomp == 1), D is component `addcomp`
+__global__ void k_merge_df(const DevSub* __restrict__ ds, float* __restrict__ pool, int addcomp) {
+  const DevSub s = ds[blockIdx.y];
+  const long long comp = (long long)s.NO * s.NR;
+  float* X0 = pool + s.oXc;
+  float* X1 = X0 + comp;
+  const float* D = X0 + (long long)addcomp * comp;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < comp; e += (long long)gridDim.x * blockDim.x) {
+    float hi = X0[e], lo = addcomp == 1 ? 0.f : X1[e], d = D[e];
+    float t, err;
+    two_sum(hi, d, t, err);
+    lo += err;
+    float h2 = t + lo;
+    X0[e] = h2;
+    X1[e] = lo - (h2 - t);
+  }
+}
+
+// largest |component| per subdomain (refinement diagnostics; FP32 bit patterns
+// of non-negative values order like integers)
+__global__ void k_comp_maxabs(const DevSub* __restrict__ ds, const float* __restrict__ pool, int comp_id,
+                              int* __restrict__ out) {
+  const DevSub s = ds[blockIdx.y];
+  const long long comp = (long long)s.NO * s.NR;
+  const float* X = pool + s.oXc + (long long)comp_id * comp;
+  float m = 0.f;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < comp; e += (long long)gridDim.x * blockDim.x)
+    m = fmaxf(m, fabsf(X[e]));
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out + blockIdx.y, __float_as_int(m));
 }
 
 // Schur complement S = A_ii - A_io (X_0 + ...), FP64-accurate, plus the
@@ -327,7 +367,8 @@ __global__ void __launch_bounds__(128) k_schur_df(const DevSub* __restrict__ ds,
   }
   __syncthreads();
   const long long comp = (long long)s.NO * s.NR;
-  const int ncomp = s.nref + 1;
+  const float* X0 = pool + s.oXc;
+  const float* X1 = X0 + comp;
   for (int c = threadIdx.x; c <= s.ni; c += blockDim.x) {
     dfacc acc;
     if (c < s.ni) {
@@ -337,8 +378,8 @@ __global__ void __launch_bounds__(128) k_schur_df(const DevSub* __restrict__ ds,
       acc.add_df(df_from_double(fi[s.rep + i]));
     }
     for (int q = 0; q < nnz; ++q) {
-      const float* xr = pool + s.oXc + (long long)scol[q] * s.NR + c;
-      for (int m = 0; m < ncomp; ++m) acc.fma_df(sval[q], xr[m * comp]);
+      long long o = (long long)scol[q] * s.NR + c;
+      acc.fma_df(sval[q], dfloat{X0[o], X1[o]});
     }
     if (c < s.ni) {
       dfloat v = acc.value();
@@ -379,29 +420,39 @@ __global__ void __launch_bounds__(128) k_schur_f64(const DevSub* __restrict__ ds
   for (int c = s.ni + threadIdx.x; c < s.NI; c += blockDim.x) Srow[c] = 0.0;
 }
 
-// S = (S + S^T) / 2 (the computed Schur complement is symmetric only up to rounding)
-__global__ void k_symmetrize_df(const DevSub* __restrict__ ds, float2* __restrict__ Spool) {
-  const DevSub s = ds[blockIdx.z];
-  int i = blockIdx.y * 16 + threadIdx.y, j = blockIdx.x * 16 + threadIdx.x;
-  if (i >= s.ni || j >= s.ni || j <= i) return;
-  float2* S = Spool + s.oS;
-  float2 a = S[(long long)i * s.NI + j], b = S[(long long)j * s.NI + i];
+// M = (M + M^T) / 2 on the leading n x n block of a row-major NI x NI
+// matrix (the computed Schur complement and preconditioner block are
+// symmetric only up to rounding).  Tile pairs (I, J) and (J, I) go through
+// shared memory so both reads and writes are coalesced.
+template <typename E>
+__device__ __forceinline__ E sym_avg(E a, E b) { return E(0.5) * (a + b); }
+template <>
+__device__ __forceinline__ float2 sym_avg<float2>(float2 a, float2 b) {
   dfacc acc;
   acc.add(a.x); acc.add(b.x); acc.c += a.y + b.y;
   dfloat v = acc.value();
-  float2 m = make_float2(0.5f * v.hi, 0.5f * v.lo);
-  S[(long long)i * s.NI + j] = m;
-  S[(long long)j * s.NI + i] = m;
+  return make_float2(0.5f * v.hi, 0.5f * v.lo);
 }
 
-__global__ void k_symmetrize_f64(const DevSub* __restrict__ ds, double* __restrict__ Spool) {
+template <typename E>
+__global__ void k_symmetrize(const DevSub* __restrict__ ds, E* __restrict__ pool, int which) {
   const DevSub s = ds[blockIdx.z];
-  int i = blockIdx.y * 16 + threadIdx.y, j = blockIdx.x * 16 + threadIdx.x;
-  if (i >= s.ni || j >= s.ni || j <= i) return;
-  double* S = Spool + s.oS;
-  double m = 0.5 * (S[(long long)i * s.NI + j] + S[(long long)j * s.NI + i]);
-  S[(long long)i * s.NI + j] = m;
-  S[(long long)j * s.NI + i] = m;
+  const int bi = blockIdx.y, bj = blockIdx.x;
+  if (bj < bi || bi * 32 >= s.NI || bj * 32 >= s.NI) return;
+  E* M = pool + (which == 0 ? s.oS : s.oZ);
+  __shared__ E ta[32][33], tb[32][33];
+  const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
+  for (int r = ty; r < 32; r += 8) {
+    ta[r][tx] = M[(long long)(bi * 32 + r) * s.NI + bj * 32 + tx];
+    tb[r][tx] = M[(long long)(bj * 32 + r) * s.NI + bi * 32 + tx];
+  }
+  __syncthreads();
+  for (int r = ty; r < 32; r += 8) {
+    int gi = bi * 32 + r, gj = bj * 32 + tx;
+    if (gi < s.ni && gj < s.ni) M[(long long)gi * s.NI + gj] = sym_avg(ta[r][tx], tb[tx][r]);
+    int hi = bj * 32 + r, hj = bi * 32 + tx;
+    if (bi != bj && hi < s.ni && hj < s.ni) M[(long long)hi * s.NI + hj] = sym_avg(tb[r][tx], ta[tx][r]);
+  }
 }
 
 template <typename T, typename ST>
@@ -516,13 +567,24 @@ __global__ void __launch_bounds__(256) k_small_g(const DevSub* __restrict__ ds, 
     }
   }
   __syncthreads();
+  // G^-1 and the local coarse matrix.  With Srho = S + C^T (rho D^2) C
+  // (D = diag(1/|c_r|)), Y = Srho^-1 C^T and Phi = Y G^-1:  Srho Phi = C^T G^-1
+  // and C Phi = I, hence Phi^T S Phi = G^-1 - rho D^2 (= -lambda of the
+  // reference's augmented solve, module_dd.f90:5615-5625).
   double* Gi = small + s.oGinv;
+  double* Ac = small + s.oAc;
   for (int e = threadIdx.x; e < s.ncp * s.ncp; e += blockDim.x) {
     int r = e / s.ncp, q = e % s.ncp;
     double t = 0.0;
     if (r < nc && q < nc)
       for (int m = max(r, q); m < nc; ++m) t += inv[m * ld + r] * inv[m * ld + q];
     Gi[e] = t;
+    if (r < nc && r == q) {
+      double nrm = 0.0;
+      for (int k = p[r]; k < p[r + 1]; ++k) nrm += cval[k] * cval[k];
+      t -= s.rho / nrm;
+    }
+    Ac[e] = t;
   }
 }
 
@@ -543,60 +605,30 @@ __global__ void k_phi(const DevSub* __restrict__ ds, const T* __restrict__ pool,
   pcpool[s.oPhi + e] = T(t);
 }
 
-// Z = Srho^-1 - Phi Y^T on the interface block (dense, preconditioner precision)
+// Z = Srho^-1 - Phi Y^T on the interface block (dense, preconditioner
+// precision); 16 x 16 output tiles with the Phi and Y rows staged in shared
+// memory
+constexpr int NCMAX = 120;
 template <typename T>
 __global__ void k_z(const DevSub* __restrict__ ds, const T* __restrict__ pool, T* __restrict__ pcpool) {
   const DevSub s = ds[blockIdx.z];
-  int i = blockIdx.y * 16 + threadIdx.y, j = blockIdx.x * 16 + threadIdx.x;
-  if (i >= s.NI || j >= s.NI) return;
+  const int i0 = blockIdx.y * 16, j0 = blockIdx.x * 16;
+  if (i0 >= s.NI || j0 >= s.NI) return;
+  __shared__ T ph[16][NCMAX + 1], yy[16][NCMAX + 1];
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * 16 + tx;
+  for (int e = tid; e < 16 * s.nc; e += 256) {
+    int r = e / s.nc, c = e % s.nc;
+    ph[r][c] = pcpool[s.oPhi + (long long)(i0 + r) * s.ncp + c];
+    yy[r][c] = pool[s.oBs + (long long)(j0 + r) * s.NRC + s.NI + c];
+  }
+  __syncthreads();
+  const int i = i0 + ty, j = j0 + tx;
   T v = T(0);
   if (i < s.ni && j < s.ni) {
     v = pool[s.oBs + (long long)i * s.NRC + j];
-    const T* ph = pcpool + s.oPhi + (long long)i * s.ncp;
-    const T* y = pool + s.oBs + (long long)j * s.NRC + s.NI;
-    for (int c = 0; c < s.nc; ++c) v -= ph[c] * y[c];
+    for (int c = 0; c < s.nc; ++c) v -= ph[ty][c] * yy[tx][c];
   }
   pcpool[s.oZ + (long long)i * s.NI + j] = v;
-}
-
-template <typename T>
-__global__ void k_symmetrize_t(const DevSub* __restrict__ ds, T* __restrict__ pcpool) {
-  const DevSub s = ds[blockIdx.z];
-  int i = blockIdx.y * 16 + threadIdx.y, j = blockIdx.x * 16 + threadIdx.x;
-  if (i >= s.ni || j >= s.ni || j <= i) return;
-  T* Z = pcpool + s.oZ;
-  T m = T(0.5) * (Z[(long long)i * s.NI + j] + Z[(long long)j * s.NI + i]);
-  Z[(long long)i * s.NI + j] = m;
-  Z[(long long)j * s.NI + i] = m;
-}
-
-// S Phi (into the Y columns of the preconditioner RHS block, which are no
-// longer needed), then Ac = Phi^T S Phi in FP64 accumulation
-template <typename T, typename ST>
-__global__ void k_sphi(const DevSub* __restrict__ ds, const ST* __restrict__ Spool, const T* __restrict__ pcpool,
-                       T* __restrict__ pool) {
-  const DevSub s = ds[blockIdx.y];
-  const int i = blockIdx.x;
-  if (i >= s.ni) return;
-  for (int c = threadIdx.x; c < s.nc; c += blockDim.x) {
-    T t = T(0);
-    for (int j = 0; j < s.ni; ++j)
-      t += schur_entry<T, ST>(Spool + s.oS, (long long)i * s.NI + j) * pcpool[s.oPhi + (long long)j * s.ncp + c];
-    pool[s.oBs + (long long)i * s.NRC + s.NI + c] = t;
-  }
-}
-
-template <typename T>
-__global__ void k_ac(const DevSub* __restrict__ ds, const T* __restrict__ pool, const T* __restrict__ pcpool,
-                     double* __restrict__ small) {
-  const DevSub s = ds[blockIdx.y];
-  int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= s.nc * s.nc) return;
-  int a = e / s.nc, b = e % s.nc;
-  double t = 0.0;
-  for (int i = 0; i < s.ni; ++i)
-    t += (double)pcpool[s.oPhi + (long long)i * s.ncp + a] * (double)pool[s.oBs + (long long)i * s.NRC + s.NI + b];
-  small[s.oAc + a * s.ncp + b] = t;
 }
 
 }  // namespace bddc
