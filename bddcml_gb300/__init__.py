@@ -254,11 +254,14 @@ def upload_problem(prob, numbase: int = 0, find_components_int: int = 1, neighbo
     """Uploads every subdomain of a :class:`bddcml_gb300.problems.Problem`
     (0-based arrays) through the C ABI, shifting indices to ``numbase``."""
     nb = numbase
+
+    def sh(a):  # index arrays in the caller's numbering (no copy for numbase 0)
+        return a + nb if nb else a
     for s in prob.subdomains:
         bddcml_upload_subdomain_data(
             prob.nelem, prob.nnod, prob.ndof, prob.ndim, prob.meshdim, s.isub + nb, s.nelems, s.nnods, s.ndofs,
-            s.inet + nb, s.nnet, s.nndf, s.isngn + nb, s.isvgvn + nb, s.isegn + nb, s.xyz, s.ifix, s.fixv,
-            s.rhs, s.is_rhs_complete, s.sol, prob.matrixtype, s.i_sparse + nb, s.j_sparse + nb, s.a_sparse,
+            sh(s.inet), s.nnet, s.nndf, sh(s.isngn), sh(s.isvgvn), sh(s.isegn), s.xyz, s.ifix, s.fixv,
+            s.rhs, s.is_rhs_complete, s.sol, prob.matrixtype, sh(s.i_sparse), sh(s.j_sparse), s.a_sparse,
             s.is_assembled, find_components_int=find_components_int, neighbouring=neighbouring)
 
 

@@ -210,23 +210,21 @@ static void run_panels(Device& D, const BandDesc* bd, const TcDesc* td, int nbat
   CKL();
 }
 
-// forward + backward sweeps on the tensor cores (3xTF32, TMEM accumulation)
+// forward + backward sweeps on the tensor cores (3xTF32, TMEM accumulation):
+// one launch per direction, one CTA per (system, 128-column tile)
 static void run_solve_tc(Device& D, const TcDesc* td, int nbatch, int maxnb, int maxncol, const float* P, float* B) {
   static bool attr = false;
   const size_t smem = tc_smem_bytes();
   if (!attr) {
-    CK(cudaFuncSetAttribute(k_band_step_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_band_sweep_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr = true;
   }
+  (void)maxnb;
   dim3 grid(maxncol / TC_M, nbatch);
-  for (int k = 0; k < maxnb; ++k) {
-    k_band_step_tc<<<grid, TC_THREADS, smem, D.st>>>(td, P, B, k, 0, D.err);
-    CKL();
-  }
-  for (int k = maxnb - 1; k >= 0; --k) {
-    k_band_step_tc<<<grid, TC_THREADS, smem, D.st>>>(td, P, B, k, 1, D.err);
-    CKL();
-  }
+  k_band_sweep_tc<<<grid, TC_THREADS, smem, D.st>>>(td, P, B, 0, D.err);
+  CKL();
+  k_band_sweep_tc<<<grid, TC_THREADS, smem, D.st>>>(td, P, B, 1, D.err);
+  CKL();
 }
 
 template <typename T>
@@ -494,6 +492,8 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
     CK(cudaFuncSetAttribute(k_schur_apply_f64, cudaFuncAttributeMaxDynamicSharedMemorySize,
                             (int)(D.maxNI * sizeof(double))));
   CK(cudaFuncSetAttribute(k_pc_local<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(D.maxNI * sizeof(T))));
+  CK(cudaFuncSetAttribute(k_post_df, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                          (int)((D.maxNI + 1) * sizeof(float2))));
   (void)ppool;
 
   // ---- interior band factor
@@ -910,8 +910,8 @@ static bool solve_impl(Solver& S, double tol, int maxit, int ndecrmax, int& num_
   if (postprocess) {
     D.prof.begin(PH_POST, st);
     if (D.mixed)
-      k_post_df<<<dim3((D.maxNO + 7) / 8, D.nsub), 256, 0, st>>>(D.ds, static_cast<const float*>(D.poolT), D.x, D.uniq,
-                                                                 D.uo, D.uo_off);
+      k_post_df<<<dim3((D.maxNO + POST_ROWS - 1) / POST_ROWS, D.nsub), 256, (D.maxNI + 1) * sizeof(float2), st>>>(
+          D.ds, static_cast<const float*>(D.poolT), D.x, D.uniq, D.uo, D.uo_off);
     else
       k_post_f64<<<dim3((D.maxNO + 7) / 8, D.nsub), 256, 0, st>>>(D.ds, static_cast<const double*>(D.poolT), D.x,
                                                                   D.uniq, D.uo, D.uo_off);

@@ -390,28 +390,42 @@ __global__ void k_axpy(int n, double a, const double* __restrict__ x, double* __
   if (g < n) y[g] += a * x[g];
 }
 
-// interior values u_o = v - X(:, 0:ni) x_s  (module_dd.f90:6811-6932), warp per row
+// interior values u_o = v - X(:, 0:ni) x_s  (module_dd.f90:6811-6932): 64
+// rows per CTA, the gathered interface solution staged once in shared memory
+// as double-float, X read as its double-float pair
+constexpr int POST_ROWS = 64;
 __global__ void __launch_bounds__(256) k_post_df(const DevSub* __restrict__ ds, const float* __restrict__ pool,
                                                  const double* __restrict__ x, const int* __restrict__ uniq,
                                                  double* __restrict__ uo, const long long* __restrict__ uo_off) {
   const DevSub s = ds[blockIdx.y];
-  int row = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-  if (row >= s.no) return;
+  const int r0 = blockIdx.x * POST_ROWS;
+  if (r0 >= s.no) return;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  float2* xs = reinterpret_cast<float2*>(smraw);
+  for (int j = threadIdx.x; j <= s.ni; j += blockDim.x) {
+    dfloat v = j < s.ni ? df_from_double(-x[uniq[s.rep + j]]) : dfloat{1.f, 0.f};
+    xs[j] = make_float2(v.hi, v.lo);
+  }
+  __syncthreads();
   const long long comp = (long long)s.NO * s.NR;
-  const float* X0 = pool + s.oXc + (long long)row * s.NR;
-  const float* X1 = X0 + comp;
-  dfacc acc;
-  for (int j = lane; j <= s.ni; j += 32) {
-    dfloat xv = j < s.ni ? df_from_double(-x[uniq[s.rep + j]]) : dfloat{1.f, 0.f};
-    acc.fma_df(xv, dfloat{X0[j], X1[j]});
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int rend = min(r0 + POST_ROWS, s.no);
+  for (int row = r0 + warp; row < rend; row += 8) {
+    const float* X0 = pool + s.oXc + (long long)row * s.NR;
+    const float* X1 = X0 + comp;
+    dfacc acc;
+    for (int j = lane; j <= s.ni; j += 32) {
+      float2 xv = xs[j];
+      acc.fma_df(dfloat{xv.x, xv.y}, dfloat{X0[j], X1[j]});
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      dfacc other;
+      other.s = __shfl_xor_sync(0xffffffffu, acc.s, o);
+      other.c = __shfl_xor_sync(0xffffffffu, acc.c, o);
+      acc.merge(other);
+    }
+    if (lane == 0) uo[uo_off[blockIdx.y] + row] = acc.to_double();
   }
-  for (int o = 16; o > 0; o >>= 1) {
-    dfacc other;
-    other.s = __shfl_xor_sync(0xffffffffu, acc.s, o);
-    other.c = __shfl_xor_sync(0xffffffffu, acc.c, o);
-    acc.merge(other);
-  }
-  if (lane == 0) uo[uo_off[blockIdx.y] + row] = acc.to_double();
 }
 
 __global__ void __launch_bounds__(256) k_post_f64(const DevSub* __restrict__ ds, const double* __restrict__ pool,

@@ -148,19 +148,17 @@ __host__ __device__ __forceinline__ long long panel_chunk(long long base, int w,
   return base + ((long long)k * (w + 1) * 2 + q) * TC_PCHUNK;
 }
 
-// one sweep step for all subdomains: grid (max column tiles, batch)
-// dir = 0 forward, 1 backward
+// Complete forward (dir = 0) or backward (dir = 1) sweep: one CTA owns one
+// 128-column tile of one system's right-hand side and walks all block rows;
+// tiles are independent, so no grid-wide synchronisation is needed and the
+// band window of a tile (w+1 block rows x 128 columns) stays in L2 between
+// consecutive block rows.  grid (max column tiles, batch).
 __global__ void __launch_bounds__(TC_THREADS, 1)
-    k_band_step_tc(const TcDesc* __restrict__ td, const float* __restrict__ ppool, float* __restrict__ bpool, int k,
-                   int dir, int* __restrict__ err) {
+    k_band_sweep_tc(const TcDesc* __restrict__ td, const float* __restrict__ ppool, float* __restrict__ bpool,
+                    int dir, int* __restrict__ err) {
   const TcDesc d = td[blockIdx.y];
   const int c0 = blockIdx.x * TC_M;
-  if (k >= d.nb || c0 >= d.ncol) return;
-  // window of block rows
-  int j0, nblk;
-  if (dir == 0) { j0 = k - min(k, d.w); nblk = k - j0 + 1; }
-  else { j0 = k; nblk = min(d.w, d.nb - 1 - k) + 1; }
-  const int nchunk = nblk * (NB / TC_KC);
+  if (c0 >= d.ncol || d.nb == 0) return;
   const int ld = d.ncol;
   float* B = bpool + d.oB;
   const float* P = ppool + (dir == 0 ? d.oPf : d.oPb);
@@ -171,7 +169,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   __shared__ __align__(8) uint64_t bar_p[TC_STAGES], bar_mma[TC_STAGES];
   __shared__ uint32_t tmem_base;
   __shared__ int abort_flag;
-  __shared__ int last_commit, tma_pending[TC_STAGES];
+  __shared__ long long last_commit, tma_pending[TC_STAGES];
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid == 0) {
@@ -195,99 +193,113 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   const uint32_t tmem = tmem_base;
   constexpr uint32_t idesc = tc_idesc(TC_M, TC_N);
 
-  int committed = 0;  // number of commits issued (thread 0)
-  for (int q = 0; q < nchunk; ++q) {
-    const int st = q & 1;
-    if (q >= TC_STAGES) {
-      // stage reuse: the MMAs of chunk q-2 must have finished reading it
-      if (!mbar_wait(&bar_mma[st], ((q - TC_STAGES) >> 1) & 1)) { if (tid == 0) abort_flag = 1; }
+  long long g = 0;  // chunk counter over the whole sweep (mbarrier phases)
+  for (int sidx = 0; sidx < d.nb; ++sidx) {
+    const int k = dir == 0 ? sidx : d.nb - 1 - sidx;
+    int j0, nblk;
+    if (dir == 0) { j0 = k - min(k, d.w); nblk = k - j0 + 1; }
+    else { j0 = k; nblk = min(d.w, d.nb - 1 - k) + 1; }
+    const int nchunk = nblk * (NB / TC_KC);
+    const float* src0 = B + (long long)(j0 * NB) * ld + c0 + tid;
+    float vn[TC_KC];
+#pragma unroll
+    for (int t = 0; t < TC_KC; ++t) vn[t] = src0[(long long)t * ld];
+    for (int q = 0; q < nchunk; ++q, ++g) {
+      const int st = (int)(g & 1);
+      float v[TC_KC];
+#pragma unroll
+      for (int t = 0; t < TC_KC; ++t) v[t] = vn[t];
+      if (q + 1 < nchunk) {  // prefetch the next chunk of the window
+        const float* src = src0 + (long long)((q + 1) * TC_KC) * ld;
+#pragma unroll
+        for (int t = 0; t < TC_KC; ++t) vn[t] = src[(long long)t * ld];
+      }
+      if (g >= TC_STAGES) {
+        if (!mbar_wait(&bar_mma[st], (uint32_t)(((g - TC_STAGES) >> 1) & 1))) { if (tid == 0) abort_flag = 1; }
+      }
+      __syncthreads();
+      if (abort_flag) break;
+      if (tid == 0) {
+        mbar_expect_tx(&bar_p[st], TC_PCHUNK * 4);
+        bulk_g2s(sP + st * TC_PCHUNK, P + panel_chunk(0, d.w, k, q), TC_PCHUNK * 4, &bar_p[st]);
+        tma_pending[st] = g;
+      }
+      {
+        float* ahi = sA + (st * 2 + 0) * TC_ACHUNK;
+        float* alo = sA + (st * 2 + 1) * TC_ACHUNK;
+#pragma unroll
+        for (int t4 = 0; t4 < TC_KC / 4; ++t4) {
+          float4 h, l;
+          h.x = tf32_rna(v[4 * t4 + 0]); l.x = v[4 * t4 + 0] - h.x;
+          h.y = tf32_rna(v[4 * t4 + 1]); l.y = v[4 * t4 + 1] - h.y;
+          h.z = tf32_rna(v[4 * t4 + 2]); l.z = v[4 * t4 + 2] - h.z;
+          h.w = tf32_rna(v[4 * t4 + 3]); l.w = v[4 * t4 + 3] - h.w;
+          int off = canon_off(tid, 4 * t4);
+          *reinterpret_cast<float4*>(ahi + off) = h;
+          *reinterpret_cast<float4*>(alo + off) = l;
+        }
+      }
+      fence_async_smem();
+      tc_fence_before();
+      __syncthreads();
+      if (tid == 0) {
+        tc_fence_after();
+        if (!mbar_wait(&bar_p[st], (uint32_t)((g >> 1) & 1))) {
+          abort_flag = 1;
+        } else {
+          tma_pending[st] = -1;
+          const uint32_t a_hi = smem_u32(sA + (st * 2 + 0) * TC_ACHUNK);
+          const uint32_t a_lo = smem_u32(sA + (st * 2 + 1) * TC_ACHUNK);
+          const uint32_t p_hi = smem_u32(sP + st * TC_PCHUNK);
+          const uint32_t p_lo = p_hi + TC_N * TC_KC * 4;
+#pragma unroll
+          for (int kk = 0; kk < TC_KC / 8; ++kk) {
+            const uint32_t koff = kk * 2 * TC_LBO;
+            uint32_t acc = (q > 0 || kk > 0) ? 1u : 0u;
+            mma_tf32(tmem, tc_desc(a_lo + koff), tc_desc(p_hi + koff), idesc, acc);
+            mma_tf32(tmem, tc_desc(a_hi + koff), tc_desc(p_lo + koff), idesc, 1u);
+            mma_tf32(tmem, tc_desc(a_hi + koff), tc_desc(p_hi + koff), idesc, 1u);
+          }
+          mma_commit(&bar_mma[st]);
+          last_commit = g;
+        }
+      }
+    }
+    // block row k done: wait for its MMAs, move the accumulator to global memory
+    __syncthreads();
+    if (tid == 0 && !abort_flag) {
+      long long ql = last_commit;
+      if (ql != g - 1 || !mbar_wait(&bar_mma[ql & 1], (uint32_t)((ql >> 1) & 1))) abort_flag = 1;
     }
     __syncthreads();
     if (abort_flag) break;
-    if (tid == 0) {
-      mbar_expect_tx(&bar_p[st], TC_PCHUNK * 4);
-      bulk_g2s(sP + st * TC_PCHUNK, P + panel_chunk(0, d.w, k, q), TC_PCHUNK * 4, &bar_p[st]);
-      tma_pending[st] = q;
-    }
-    // window operand: rows r = j0*64 + q*32 + t, columns c0 + tid -> A[m = tid][k = t]
+    tc_fence_after();
     {
-      float* ahi = sA + (st * 2 + 0) * TC_ACHUNK;
-      float* alo = sA + (st * 2 + 1) * TC_ACHUNK;
-      const float* src = B + (long long)(j0 * NB + q * TC_KC) * ld + c0 + tid;
-      float v[TC_KC];
+      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+      float* dst = B + (long long)(k * NB) * ld + c0 + warp * 32 + lane;
 #pragma unroll
-      for (int t = 0; t < TC_KC; ++t) v[t] = src[(long long)t * ld];
+      for (int part = 0; part < TC_N / 16; ++part) {
+        float vv[16];
+        tmem_ld16(taddr + part * 16, vv);
 #pragma unroll
-      for (int t4 = 0; t4 < TC_KC / 4; ++t4) {
-        float4 h, l;
-        h.x = tf32_rna(v[4 * t4 + 0]); l.x = v[4 * t4 + 0] - h.x;
-        h.y = tf32_rna(v[4 * t4 + 1]); l.y = v[4 * t4 + 1] - h.y;
-        h.z = tf32_rna(v[4 * t4 + 2]); l.z = v[4 * t4 + 2] - h.z;
-        h.w = tf32_rna(v[4 * t4 + 3]); l.w = v[4 * t4 + 3] - h.w;
-        int off = canon_off(tid, 4 * t4);
-        *reinterpret_cast<float4*>(ahi + off) = h;
-        *reinterpret_cast<float4*>(alo + off) = l;
+        for (int i = 0; i < 16; ++i) dst[(long long)(part * 16 + i) * ld] = vv[i];
       }
     }
-    fence_async_smem();
     tc_fence_before();
-    __syncthreads();
-    if (tid == 0) {
-      tc_fence_after();
-      if (!mbar_wait(&bar_p[st], (q >> 1) & 1)) {
-        abort_flag = 1;
-      } else {
-        tma_pending[st] = -1;
-        const uint32_t a_hi = smem_u32(sA + (st * 2 + 0) * TC_ACHUNK);
-        const uint32_t a_lo = smem_u32(sA + (st * 2 + 1) * TC_ACHUNK);
-        const uint32_t p_hi = smem_u32(sP + st * TC_PCHUNK);
-        const uint32_t p_lo = p_hi + TC_N * TC_KC * 4;
-#pragma unroll
-        for (int kk = 0; kk < TC_KC / 8; ++kk) {
-          const uint32_t koff = kk * 2 * TC_LBO;
-          uint32_t acc = (q > 0 || kk > 0) ? 1u : 0u;
-          mma_tf32(tmem, tc_desc(a_lo + koff), tc_desc(p_hi + koff), idesc, acc);
-          mma_tf32(tmem, tc_desc(a_hi + koff), tc_desc(p_lo + koff), idesc, 1u);
-          mma_tf32(tmem, tc_desc(a_hi + koff), tc_desc(p_hi + koff), idesc, 1u);
-        }
-        mma_commit(&bar_mma[st]);
-        last_commit = q;
-        committed++;
-      }
-    }
+    __syncthreads();  // the next block row reads these rows
   }
-  // wait for the last commit (and, after an abort, for copies still in
-  // flight), then read the accumulator out of TMEM
-  __syncthreads();
-  bool ok = abort_flag == 0;
-  if (tid == 0) {
-    int ql = last_commit;
-    if (ql >= 0 && !mbar_wait(&bar_mma[ql & 1], (ql >> 1) & 1)) abort_flag = 1;
+  // after an abort: wait (bounded) for work still in flight before freeing TMEM
+  if (tid == 0 && abort_flag) {
+    long long ql = last_commit;
+    if (ql >= 0) mbar_wait(&bar_mma[ql & 1], (uint32_t)((ql >> 1) & 1));
     for (int s2 = 0; s2 < TC_STAGES; ++s2)
-      if (tma_pending[s2] >= 0 && !mbar_wait(&bar_p[s2], (tma_pending[s2] >> 1) & 1)) abort_flag = 1;
-    if (ok && ql != nchunk - 1) abort_flag = 1;
-  }
-  __syncthreads();
-  ok = abort_flag == 0;
-  tc_fence_after();
-  if (ok) {
-    // warp w holds TMEM lanes 32w..32w+31 = columns c0 + 32w + lane; 64 accumulator columns = output rows
-    const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
-    float* dst = B + (long long)(k * NB) * ld + c0 + warp * 32 + lane;
-#pragma unroll
-    for (int part = 0; part < TC_N / 16; ++part) {
-      float v[16];
-      tmem_ld16(taddr + part * 16, v);
-#pragma unroll
-      for (int i = 0; i < 16; ++i) dst[(long long)(part * 16 + i) * ld] = v[i];
-    }
-  } else if (tid == 0) {
+      if (tma_pending[s2] >= 0) mbar_wait(&bar_p[s2], (uint32_t)((tma_pending[s2] >> 1) & 1));
     atomicOr(err, DE_TIMEOUT);
   }
   tc_fence_before();
   __syncthreads();
+  tc_fence_after();
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_N));
-  (void)committed;
 }
 
 constexpr size_t tc_smem_bytes() { return (size_t)TC_STAGES * (2 * TC_ACHUNK + TC_PCHUNK) * sizeof(float); }
