@@ -35,23 +35,51 @@ double wall_time() {
   return duration<double>(steady_clock::now().time_since_epoch()).count();
 }
 
-// sort + merge duplicate (i,j) entries (the effect of sm_assembly, module_sm.f90:630-684)
+// sort + merge duplicate (i,j) entries (the effect of sm_assembly,
+// module_sm.f90:630-684): counting sort by row, insertion sort of the short
+// rows by column, then merge of repeated pairs in their original order
 void host_assemble_upper(vector<int>& ia, vector<int>& ja, vector<double>& a) {
-  size_t n = ia.size();
-  vector<uint64_t> key(n);
-  for (size_t k = 0; k < n; ++k) key[k] = ((uint64_t)(uint32_t)ia[k] << 32) | (uint32_t)ja[k];
-  vector<uint32_t> p(n);
-  std::iota(p.begin(), p.end(), 0u);
-  std::stable_sort(p.begin(), p.end(), [&](uint32_t x, uint32_t y) { return key[x] < key[y]; });
-  vector<int> ni, nj;
-  vector<double> na;
-  ni.reserve(n); nj.reserve(n); na.reserve(n);
-  for (size_t q = 0; q < n; ++q) {
-    uint32_t k = p[q];
-    if (!ni.empty() && ni.back() == ia[k] && nj.back() == ja[k]) na.back() += a[k];
-    else { ni.push_back(ia[k]); nj.push_back(ja[k]); na.push_back(a[k]); }
+  const size_t n = ia.size();
+  int nrow = 0;
+  for (size_t k = 0; k < n; ++k) nrow = std::max(nrow, ia[k] + 1);
+  vector<int> ptr(nrow + 1, 0);
+  for (size_t k = 0; k < n; ++k) ptr[ia[k] + 1]++;
+  for (int r = 0; r < nrow; ++r) ptr[r + 1] += ptr[r];
+  vector<int> col(n);
+  vector<double> val(n);
+  {
+    vector<int> pos(ptr.begin(), ptr.end() - 1);
+    for (size_t k = 0; k < n; ++k) {
+      int q = pos[ia[k]]++;
+      col[q] = ja[k];
+      val[q] = a[k];
+    }
   }
-  ia.swap(ni); ja.swap(nj); a.swap(na);
+  size_t out = 0;
+  for (int r = 0; r < nrow; ++r) {
+    int b = ptr[r], e = ptr[r + 1];
+    for (int i = b + 1; i < e; ++i) {  // stable insertion sort by column
+      int c = col[i];
+      double v = val[i];
+      int j = i - 1;
+      while (j >= b && col[j] > c) { col[j + 1] = col[j]; val[j + 1] = val[j]; --j; }
+      col[j + 1] = c;
+      val[j + 1] = v;
+    }
+    for (int i = b; i < e; ++i) {
+      if (out > 0 && ia[out - 1] == r && ja[out - 1] == col[i]) {
+        a[out - 1] += val[i];
+      } else {
+        ia[out] = r;
+        ja[out] = col[i];
+        a[out] = val[i];
+        ++out;
+      }
+    }
+  }
+  ia.resize(out);
+  ja.resize(out);
+  a.resize(out);
 }
 
 // components of the dual mesh graph: elements are connected when they share
@@ -98,6 +126,9 @@ void host_nodal_components(Subdomain& s) {
 }
 
 void full_symmetric_csr(const Subdomain& s, vector<int>& ptr, vector<int>& col, vector<double>& val) {
+  // the assembled upper triangle is sorted by (row, column): scanning it in
+  // order appends the mirrored entries of every row in increasing column
+  // order, and the row's own entries follow, so no row needs sorting
   int n = s.ndof;
   ptr.assign(n + 1, 0);
   for (size_t k = 0; k < s.ia.size(); ++k) {
@@ -108,18 +139,9 @@ void full_symmetric_csr(const Subdomain& s, vector<int>& ptr, vector<int>& col, 
   col.assign(ptr[n], 0);
   val.assign(ptr[n], 0.0);
   vector<int> pos(ptr.begin(), ptr.end() - 1);
-  for (size_t k = 0; k < s.ia.size(); ++k) {
-    int i = s.ia[k], j = s.ja[k];
-    col[pos[i]] = j; val[pos[i]++] = s.a[k];
-    if (i != j) { col[pos[j]] = i; val[pos[j]++] = s.a[k]; }
-  }
-  // rows sorted by column
-  for (int i = 0; i < n; ++i) {
-    vector<std::pair<int, double>> r;
-    for (int k = ptr[i]; k < ptr[i + 1]; ++k) r.emplace_back(col[k], val[k]);
-    std::sort(r.begin(), r.end(), [](auto& x, auto& y) { return x.first < y.first; });
-    for (int k = ptr[i]; k < ptr[i + 1]; ++k) { col[k] = r[k - ptr[i]].first; val[k] = r[k - ptr[i]].second; }
-  }
+  for (size_t k = 0; k < s.ia.size(); ++k)
+    if (s.ia[k] != s.ja[k]) { int j = s.ja[k]; col[pos[j]] = s.ia[k]; val[pos[j]++] = s.a[k]; }
+  for (size_t k = 0; k < s.ia.size(); ++k) { int i = s.ia[k]; col[pos[i]] = s.ja[k]; val[pos[i]++] = s.a[k]; }
 }
 
 // Interior ordering for the band factor: natural order or reverse

@@ -128,19 +128,27 @@ def make_problem(workload):
 def e2e_solve(B, prob, precision, profile=False):
     """The reference-facing sequence through the C ABI with host buffers
     (poisson_on_cube.f90:373-672)."""
-    t0 = time.perf_counter()
+    tp = [time.perf_counter()]
     B.bddcml_init(2, [prob.nsub, 1], -1, 0, 0, 0, 0)
     B.set_precision(precision)
     if profile:
         B.set_profiling(True)
+    tp.append(time.perf_counter())
     B.upload_problem(prob)
+    tp.append(time.perf_counter())
     B.bddcml_setup_preconditioner(1, 0, 1, 1, 1, 0, 0, 0)
+    tp.append(time.perf_counter())
     it, reason, cond = B.bddcml_solve(0, 0, 1e-8, 500, 50, 0, 0)
+    tp.append(time.perf_counter())
     sols = [B.bddcml_download_local_solution(s.isub, s.ndofs) for s in prob.subdomains]
+    tp.append(time.perf_counter())
     st = B.get_stats()
     prof = B.get_profile()
     B.bddcml_finalize()
-    return time.perf_counter() - t0, it, reason, cond, st, prof, sols
+    tp.append(time.perf_counter())
+    names = ["init", "upload", "setup", "solve", "download", "finalize"]
+    st["e2e_phases_ms"] = {n: 1e3 * (tp[i + 1] - tp[i]) for i, n in enumerate(names)}
+    return tp[-1] - tp[0], it, reason, cond, st, prof, sols
 
 
 def phase_roofline(phase, prof, st, hbm, tensor, peak_kind):
@@ -268,6 +276,7 @@ def run_gpu(args):
         "refinement": {"max_correction_ratio_1": st_p["refine1"], "max_correction_ratio_2": st_p["refine2"]},
         "host_ms": {k: 1e3 * st_p[k] for k in ("t_upload", "t_host_assemble", "t_host_iface", "t_host_globs",
                                                 "t_host_blocks")},
+        "e2e_phases_ms": st["e2e_phases_ms"],
         "clocks": clocks,
     }
     print(json.dumps(out))

@@ -133,7 +133,7 @@ static void coo_assemble(vector<int>& ia, vector<int>& ja, vector<double>& a) {
   size_t n = ia.size();
   vector<size_t> p(n);
   std::iota(p.begin(), p.end(), 0);
-  std::sort(p.begin(), p.end(), [&](size_t x, size_t y) {
+  std::stable_sort(p.begin(), p.end(), [&](size_t x, size_t y) {
     return ia[x] != ia[y] ? ia[x] < ia[y] : ja[x] < ja[y];
   });
   vector<int> ni, nj;
@@ -771,12 +771,13 @@ int oracle_upload(void* h, int isub, int nelem, int nnod, int ndof, int ndim,
   return 0;
 }
 
-static void comm_exchange_add(Oracle& o, vector<vector<double>>& v) {
-  // upload / swap / download (module_dd.f90:11236-11551): own value plus the
-  // neighbours' values on shared dofs, neighbours in ascending order.
+static void comm_exchange(Oracle& o, vector<vector<double>>& v, bool keep_own) {
+  // upload / swap / download (module_dd.f90:11236-11551): the neighbours'
+  // values on shared dofs summed in ascending neighbour order, either onto the
+  // own value (keep_own) or into a zeroed buffer, as dd_comm_download does.
   int nsub = o.nsub;
   vector<vector<double>> out(nsub);
-  for (int s = 0; s < nsub; ++s) out[s] = v[s];
+  for (int s = 0; s < nsub; ++s) out[s] = keep_own ? v[s] : vector<double>(v[s].size(), 0.0);
 #pragma omp parallel for schedule(dynamic) num_threads(o.nthreads)
   for (int s = 0; s < nsub; ++s) {
     auto& S = o.subs[s];
@@ -787,6 +788,8 @@ static void comm_exchange_add(Oracle& o, vector<vector<double>>& v) {
   }
   v.swap(out);
 }
+
+static void comm_exchange_add(Oracle& o, vector<vector<double>>& v) { comm_exchange(o, v, true); }
 
 static void build_exchange_lists(Oracle& o) {
   for (auto& S : o.subs) {
@@ -852,11 +855,11 @@ int oracle_setup(void* h, int use_corner_constraints, int use_arithmetic_constra
       for (int i = 0; i < S.ndofi; ++i) bci[s][i] = S.bc[S.iivsvn[i]];
     }
     {
-      vector<vector<double>> summed = bci;
-      comm_exchange_add(*o, summed);
+      vector<vector<double>> nb = bci;
+      comm_exchange(*o, nb, false);
       for (int s = 0; s < nsub; ++s) {
         auto& S = o->subs[s];
-        for (int i = 0; i < S.ndofi; ++i) S.bc[S.iivsvn[i]] += summed[s][i] - bci[s][i];
+        for (int i = 0; i < S.ndofi; ++i) S.bc[S.iivsvn[i]] += nb[s][i];
       }
     }
     // ---- weights (module_dd.f90:11554-11722)
@@ -873,12 +876,12 @@ int oracle_setup(void* h, int use_corner_constraints, int use_arithmetic_constra
       }
     }
     {
-      vector<vector<double>> tot = rho;
-      comm_exchange_add(*o, tot);
+      vector<vector<double>> aux = rho;
+      comm_exchange(*o, aux, false);
       for (int s = 0; s < nsub; ++s) {
         auto& S = o->subs[s];
         S.wi.resize(S.ndofi);
-        for (int i = 0; i < S.ndofi; ++i) S.wi[i] = rho[s][i] / tot[s][i];  // rho/(rho + sum neighbours)
+        for (int i = 0; i < S.ndofi; ++i) S.wi[i] = rho[s][i] / (rho[s][i] + aux[s][i]);
       }
     }
     // ---- constraints and coarse dofs (module_levels.f90:2690-2740, module_dd.f90:11011-11235, 5018-5144)
@@ -1311,6 +1314,26 @@ int oracle_weights(void* h, int isub, double* out, int lout) {
   if (lout != S.ndofi) return 1;
   std::copy(S.wi.begin(), S.wi.end(), out);
   return 0;
+}
+
+// sorted intersection and union of two integer arrays (module_utils.f90:
+// get_array_intersection 878-945, get_array_union 831-876): inputs unsorted,
+// outputs sorted and without repetition; returns the number of entries.
+int oracle_array_intersection(const int* a, int la, const int* b, int lb, int* out) {
+  vector<int> x(a, a + la), y(b, b + lb);
+  vector<int> r = sorted_intersection(x, y);
+  r.erase(std::unique(r.begin(), r.end()), r.end());
+  std::copy(r.begin(), r.end(), out);
+  return (int)r.size();
+}
+
+int oracle_array_union(const int* a, int la, const int* b, int lb, int* out) {
+  vector<int> r(a, a + la);
+  r.insert(r.end(), b, b + lb);
+  std::sort(r.begin(), r.end());
+  r.erase(std::unique(r.begin(), r.end()), r.end());
+  std::copy(r.begin(), r.end(), out);
+  return (int)r.size();
 }
 
 // sum_i v1 w v2 over interface + plain sum over interior (module_dd.f90:12736-12788)

@@ -43,7 +43,26 @@ def lib():
         L.oracle_weights.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int]
         L.oracle_dotprod_subdomain.restype = C.c_double
         L.oracle_dotprod_subdomain.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+        for fn in (L.oracle_array_intersection, L.oracle_array_union):
+            fn.restype = C.c_int
+            fn.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p]
     return _LIB
+
+
+def array_intersection(a, b):
+    a = np.ascontiguousarray(a, np.int32)
+    b = np.ascontiguousarray(b, np.int32)
+    out = np.zeros(len(a) + len(b), np.int32)
+    n = lib().oracle_array_intersection(_p(a), len(a), _p(b), len(b), _p(out))
+    return out[:n]
+
+
+def array_union(a, b):
+    a = np.ascontiguousarray(a, np.int32)
+    b = np.ascontiguousarray(b, np.int32)
+    out = np.zeros(len(a) + len(b), np.int32)
+    n = lib().oracle_array_union(_p(a), len(a), _p(b), len(b), _p(out))
+    return out[:n]
 
 
 def _p(a):

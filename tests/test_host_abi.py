@@ -1,0 +1,131 @@
+"""C ABI and host-side logic without a GPU: the library loads and exports every
+entry point the header declares, the integer/geometric setup (interface,
+globs, corners, coarse numbering, weights) equals the oracle's, and errors are
+reported through status codes instead of aborting."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_symbols():
+    src = open(os.path.join(ROOT, "include", "bddcml_gb300.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:void|int)\s+(bddcml_\w+)\s*\(", src, re.M)))
+
+
+def test_exports_every_header_symbol(built_lib):
+    lib = C.CDLL(built_lib)
+    syms = header_symbols()
+    assert len(syms) >= 22
+    for name in syms:
+        assert hasattr(lib, name), name
+    import bddcml_gb300 as B
+    assert sorted(B.EXPORTS) == syms
+
+
+def test_reference_signatures_present():
+    """Every function of the reference header src/bddcml_interface_c.h is
+    declared with the same argument list."""
+    src = open(os.path.join(ROOT, "include", "bddcml_gb300.h")).read()
+    for name, nargs in [("bddcml_init_c", 8), ("bddcml_upload_global_data_c", 25),
+                        ("bddcml_upload_subdomain_data_c", 50), ("bddcml_setup_preconditioner_c", 8),
+                        ("bddcml_solve_c", 10), ("bddcml_download_local_solution_c", 3),
+                        ("bddcml_download_global_solution_c", 2), ("bddcml_download_local_reactions_c", 3),
+                        ("bddcml_download_global_reactions_c", 2), ("bddcml_change_global_data_c", 8),
+                        ("bddcml_change_subdomain_data_c", 10), ("bddcml_setup_new_data_c", 0),
+                        ("bddcml_dotprod_subdomain_c", 6), ("bddcml_finalize_c", 0)]:
+        m = re.search(name + r"\s*\(([^)]*)\)", src)
+        assert m, name
+        args = [a for a in m.group(1).split(",") if a.strip() and a.strip() != "void"]
+        assert len(args) == nargs, (name, len(args))
+
+
+@pytest.mark.parametrize("ne,ns,numbase", [(4, 2, 0), (4, 3, 1), (5, 4, 0)])
+def test_host_coarse_space_equals_oracle(built_lib, oracle_mod, ne, ns, numbase):
+    import bddcml_gb300 as B
+    from bddcml_gb300 import problems
+    prob = problems.poisson_on_cube(ne, ns)
+    B.bddcml_init(2, [prob.nsub, 1], -1, 0, 0, numbase, 0)
+    B.upload_problem(prob, numbase=numbase)
+    try:
+        B.bddcml_setup_preconditioner(1, 0, 1, 1, 1, 0, 0, 0)
+    except B.BddcmlError as e:  # no GPU in this container: the host part has run
+        assert e.code == 2
+    info = B.get_coarse_info()
+    o = oracle_mod.Oracle(prob)
+    o.setup(1, 1, 0)
+    assert info == o.stats()
+    for s in prob.subdomains:
+        w_o = o.weights(s.isub)
+        w_g = B.get_interface_weights(s.isub + numbase, len(w_o))
+        assert np.array_equal(w_o, w_g)
+    B.bddcml_finalize()
+
+
+def test_host_uneven_partition_stiffness_weights(built_lib, oracle_mod):
+    import bddcml_gb300 as B
+    from bddcml_gb300 import problems
+    prob = problems.poisson_boxes(24, problems.random_box_partition(24, 5, 10, seed=17),
+                                  kappa=problems.lognormal_kappa(24, 1.0, seed=2))
+    B.bddcml_init(2, [prob.nsub, 1], -1, 0, 0, 0, 0)
+    B.upload_problem(prob)
+    try:
+        B.bddcml_setup_preconditioner(1, 0, 1, 1, 1, 0, 0, 1)
+    except B.BddcmlError as e:
+        assert e.code == 2
+    o = oracle_mod.Oracle(prob)
+    o.setup(1, 1, 1)
+    assert B.get_coarse_info() == o.stats()
+    for s in prob.subdomains:
+        w_o = o.weights(s.isub)
+        assert np.array_equal(w_o, B.get_interface_weights(s.isub, len(w_o)))
+    B.bddcml_finalize()
+
+
+def test_errors_are_status_codes(built_lib):
+    import bddcml_gb300 as B
+    from bddcml_gb300 import problems
+    with pytest.raises(B.BddcmlError) as ei:
+        B.bddcml_init(1, [1], -1, 0, 0, 0, 0)         # fewer than 2 levels
+    assert ei.value.code == 1
+    with pytest.raises(B.BddcmlError) as ei:
+        B.bddcml_init(2, [4, 2], -1, 0, 0, 0, 0)      # last level must have 1 subdomain
+    assert ei.value.code == 1
+    prob = problems.poisson_on_cube(4, 2)
+    B.bddcml_init(2, [prob.nsub, 1], -1, 0, 0, 0, 0)
+    s = prob.subdomains[0]
+    bad_i = s.i_sparse.copy()
+    bad_i[0], bad_j = s.j_sparse[0] + 1, s.j_sparse.copy()
+    with pytest.raises(B.BddcmlError) as ei:              # lower-triangle entry for a symmetric matrix
+        B.bddcml_upload_subdomain_data(prob.nelem, prob.nnod, prob.ndof, 3, 3, 0, s.nelems, s.nnods, s.ndofs,
+                                       s.inet, s.nnet, s.nndf, s.isngn, s.isvgvn, s.isegn, s.xyz, s.ifix, s.fixv,
+                                       s.rhs, 1, s.sol, 1, bad_i, bad_j, s.a_sparse, 0)
+    assert ei.value.code == 1
+    with pytest.raises(B.BddcmlError) as ei:              # solve before setup
+        B.bddcml_solve(0, 0, 1e-8, 10, 10, 0, 0)
+    assert ei.value.code == 1
+    with pytest.raises(B.BddcmlError) as ei:              # subdomain not uploaded
+        B.bddcml_setup_preconditioner(1, 0, 1, 1, 1, 0, 0, 0)
+    assert ei.value.code == 1
+    with pytest.raises(B.BddcmlError) as ei:
+        B.bddcml_setup_preconditioner(1, 0, 1, 1, 1, 1, 0, 0)  # adaptive constraints
+    assert ei.value.code in (1, 4)
+    B.bddcml_finalize()
+    # global-data entry points are reported unsupported, not aborted
+    B.lib().bddcml_download_global_solution_c(None, None)
+    assert B.last_error()[0] == 4
+
+
+def test_solve_defaults_report_unsupported_bicgstab(built_lib):
+    import bddcml_gb300 as B
+    from bddcml_gb300 import problems
+    prob = problems.poisson_on_cube(4, 2)
+    B.bddcml_init(2, [prob.nsub, 1], -1, 0, 0, 0, 0)
+    B.upload_problem(prob)
+    with pytest.raises(B.BddcmlError):
+        B.bddcml_setup_preconditioner(1, 0, 1, 1, 1, 0, 0, 0)  # no GPU here -> CUDA error after host setup
+    B.bddcml_finalize()

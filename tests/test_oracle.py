@@ -1,0 +1,131 @@
+"""CPU oracle: pinned against the reference's known-answer vectors for the set
+operations it uses, against direct sparse solves of the assembled global
+system, against structural invariants of the coarse space, and against its own
+golden regression fixtures (tests/golden/)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def test_reference_set_operations_known_answers(oracle_mod):
+    """test/test_module_utils.f90:29-47 / :154-166 of the reference."""
+    with open(os.path.join(GOLDEN, "reference_utils_known_answers.json")) as f:
+        ka = json.load(f)
+    inter = oracle_mod.array_intersection(ka["array1"], ka["array2"])
+    assert list(inter) == ka["intersection_check"]
+    uni = oracle_mod.array_union(ka["array1"], ka["array2"])
+    assert list(uni) == ka["union_check"]
+    # get_array_norepeat on a sorted array = union with an empty array
+    assert list(oracle_mod.array_union(ka["array3"], [])) == ka["array3_check"]
+
+
+def _direct(prob):
+    import scipy.sparse.linalg as spla
+    from bddcml_gb300 import problems
+    K, f, fixed = problems.global_matrix_and_rhs(prob)
+    free = ~fixed
+    u = np.zeros(prob.ndof)
+    u[free] = spla.spsolve(K[free][:, free].tocsc(), f[free])
+    return u
+
+
+@pytest.mark.parametrize("ne,ns", [(4, 2), (4, 3), (5, 4)])
+def test_oracle_matches_direct_solve(oracle_mod, ne, ns):
+    from bddcml_gb300 import problems
+    prob = problems.poisson_on_cube(ne, ns)
+    o = oracle_mod.Oracle(prob)
+    o.setup(1, 1, 0)
+    it, reason, cond = o.solve(1e-10, 300, 50)
+    assert reason == 0
+    u = o.global_solution()
+    ud = _direct(prob)
+    assert np.linalg.norm(u - ud) / np.linalg.norm(ud) < 1e-9
+
+
+def test_oracle_heterogeneous_uneven_matches_direct(oracle_mod):
+    from bddcml_gb300 import problems
+    boxes = problems.random_box_partition(20, 4, 9, seed=5)
+    kappa = problems.lognormal_kappa(20, 1.0, seed=7)
+    prob = problems.poisson_boxes(20, boxes, kappa=kappa)
+    o = oracle_mod.Oracle(prob)
+    o.setup(1, 1, 1)
+    it, reason, cond = o.solve(1e-10, 300, 50)
+    assert reason == 0
+    u = o.global_solution()
+    ud = _direct(prob)
+    assert np.linalg.norm(u - ud) / np.linalg.norm(ud) < 1e-9
+
+
+def test_coarse_space_hand_count(oracle_mod):
+    """2 x 2 x 2 subdomains: 19 corners (1 centre vertex, 6 boundary-edge
+    vertices, 12 face-corner selections merged) + 6 edges + 12 faces = 37."""
+    from bddcml_gb300 import problems
+    o = oracle_mod.Oracle(problems.poisson_on_cube(4, 2))
+    o.setup(1, 1, 0)
+    st = o.stats()
+    assert (st["ncorner"], st["nedge"], st["nface"], st["ndofc"]) == (19, 6, 12, 37)
+
+
+def test_weights_partition_of_unity(oracle_mod):
+    from bddcml_gb300 import problems
+    prob = problems.poisson_on_cube(4, 3, kappa=problems.lognormal_kappa(12, 1.0, seed=1))
+    for wt in (0, 1):
+        o = oracle_mod.Oracle(prob)
+        o.setup(1, 1, wt)
+        tot = {}
+        cnt = np.zeros(prob.nnod, dtype=int)
+        for s in prob.subdomains:
+            cnt[s.isngn] += 1
+        for s in prob.subdomains:
+            w = o.weights(s.isub)
+            iface = [g for g in s.isvgvn if cnt[g] > 1]
+            for g, wi in zip(iface, w):
+                tot[g] = tot.get(g, 0.0) + wi
+        assert max(abs(v - 1.0) for v in tot.values()) < 1e-14
+
+
+def test_zero_rhs_returns_without_iterations(oracle_mod):
+    from bddcml_gb300 import problems
+    prob = problems.poisson_on_cube(4, 2)
+    for s in prob.subdomains:
+        s.rhs[:] = 0.0
+    o = oracle_mod.Oracle(prob)
+    o.setup(1, 1, 0)
+    it, reason, cond = o.solve(1e-8, 100, 50)
+    assert it == 0 and reason == 0
+
+
+def test_maxit_reason(oracle_mod):
+    """maxit reached -> converged_reason -1 (module_krylov.f90:785-795)."""
+    from bddcml_gb300 import problems
+    o = oracle_mod.Oracle(problems.poisson_on_cube(5, 4))
+    o.setup(1, 1, 0)
+    it, reason, cond = o.solve(1e-14, 3, 50)
+    assert it == 3 and reason == -1
+
+
+def test_oracle_golden_regression(oracle_mod):
+    from bddcml_gb300 import problems
+    with open(os.path.join(GOLDEN, "oracle_small.json")) as f:
+        gold = json.load(f)
+    specs = {
+        "cube_4x2": lambda: problems.poisson_on_cube(4, 2),
+        "cube_4x3": lambda: problems.poisson_on_cube(4, 3),
+        "cube_5x4": lambda: problems.poisson_on_cube(5, 4),
+        "boxes_24_seed17": lambda: problems.poisson_boxes(24, problems.random_box_partition(24, 5, 10, seed=17)),
+        "lognormal_16_seed3_w1": lambda: problems.poisson_on_cube(4, 4, kappa=problems.lognormal_kappa(16, 1.0, 3)),
+    }
+    for name, mk in specs.items():
+        g = gold[name]
+        o = oracle_mod.Oracle(mk())
+        o.setup(1, 1, g["weights_type"])
+        it, reason, cond = o.solve(1e-8, 300, 50)
+        assert it == g["iterations"] and reason == g["reason"], name
+        assert abs(cond - g["cond"]) < 1e-8 * g["cond"], name
+        assert o.stats() == g["coarse"], name
+        u = o.global_solution()
+        assert abs(np.linalg.norm(u) - g["solution_norm2"]) < 1e-10 * g["solution_norm2"], name
