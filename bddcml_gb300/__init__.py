@@ -28,7 +28,8 @@ STAT_FIELDS = ["t_host_setup", "t_device_setup", "t_solve", "t_iterations", "t_p
                "bytes_per_iteration", "ncorner", "nedge", "nface", "ndofc", "sum_ndofi", "sum_ndofo",
                "ninterface", "precision", "h2d_bytes", "d2h_bytes", "t_upload", "t_host_assemble",
                "t_host_iface", "t_host_globs", "t_host_blocks", "refine1", "refine2",
-               "flop_sweep_oo", "flop_sweep_s", "bytes_residual", "bytes_schur_apply", "bytes_pc_local"]
+               "flop_sweep_oo", "flop_sweep_s", "bytes_residual", "bytes_schur_apply", "bytes_pc_local",
+               "launches_setup", "launches_solve", "t_dev_alloc", "t_dev_h2d"]
 
 EXPORTS = ["bddcml_init_c", "bddcml_upload_global_data_c", "bddcml_upload_subdomain_data_c",
            "bddcml_setup_preconditioner_c", "bddcml_solve_c", "bddcml_download_local_solution_c",
@@ -37,7 +38,7 @@ EXPORTS = ["bddcml_init_c", "bddcml_upload_global_data_c", "bddcml_upload_subdom
            "bddcml_setup_new_data_c", "bddcml_dotprod_subdomain_c", "bddcml_finalize_c",
            "bddcml_get_last_error_c", "bddcml_set_precision_c", "bddcml_get_stats_c",
            "bddcml_get_residual_history_c", "bddcml_get_interface_weights_c", "bddcml_get_coarse_info_c",
-           "bddcml_set_profiling_c", "bddcml_get_profile_c"]
+           "bddcml_set_profiling_c", "bddcml_get_profile_c", "bddcml_release_device_memory_c"]
 
 # phases of bddcml_get_profile_c (CUDA events on the solver stream)
 PHASES = ["numeric_total", "solve_total", "factor_interior", "solve_interior", "refine_residual", "schur",
@@ -200,8 +201,8 @@ def set_precision(mode: int):
 
 
 def get_stats() -> dict:
-    buf = (C.c_double * 32)()
-    n = C.c_int(32)
+    buf = (C.c_double * 64)()
+    n = C.c_int(64)
     lib().bddcml_get_stats_c(buf, C.byref(n))
     _check()
     return {k: buf[i] for i, k in enumerate(STAT_FIELDS[: n.value])}
@@ -223,6 +224,12 @@ def get_interface_weights(isub: int, ndofi: int) -> np.ndarray:
     lib().bddcml_get_interface_weights_c(_i(isub), out.ctypes.data_as(C.POINTER(C.c_double)), _i(ndofi))
     _check()
     return out
+
+
+def release_device_memory():
+    """Hand the pooled device memory that no solver uses back to the driver."""
+    lib().bddcml_release_device_memory_c()
+    _check()
 
 
 def set_profiling(on: bool):

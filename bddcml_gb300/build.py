@@ -22,7 +22,7 @@ SOURCES = [
     ("bddc_device.cu", "nvcc"),
 ]
 HEADERS = ["bddc_internal.hpp", "bddc_kernels.cuh", "bddc_df.cuh", "bddc_setup_kernels.cuh",
-           "bddc_pcg_kernels.cuh"]
+           "bddc_pcg_kernels.cuh", "bddc_tc.cuh"]
 
 
 def _nvcc() -> str:

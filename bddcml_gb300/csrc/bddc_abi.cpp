@@ -150,15 +150,26 @@ void bddcml_upload_subdomain_data_c(int* nelem, int* nnod, int* ndof, int* ndim,
     s.matrixtype = *matrixtype;
     if (*matrixtype != 1 && *matrixtype != 2)
       throw Error{ERR_UNSUPPORTED, "only symmetric matrices (matrixtype 1 or 2) are implemented"};
-    s.ia.resize(*la); s.ja.resize(*la);
-    for (int k = 0; k < *la; ++k) {
-      s.ia[k] = i_sparse[k] - nb;
-      s.ja[k] = j_sparse[k] - nb;
-      if (s.ia[k] > s.ja[k])
-        throw Error{ERR_ARGUMENT, "matrix in wrong format - only the upper triangle is expected for symmetric problems"};
-      if (s.ia[k] < 0 || s.ja[k] >= *ndofs) throw Error{ERR_ARGUMENT, "matrix index out of range"};
+    // the triplets are most of the uploaded bytes: copy them with several
+    // threads (first touch of the new buffers included)
+    const int nla = *la, nd = *ndofs;
+    s.ia.resize(nla); s.ja.resize(nla); s.a.resize(nla);
+    int* ia = s.ia.data();
+    int* ja = s.ja.data();
+    double* av = s.a.data();
+    int bad_order = 0, bad_range = 0;
+#pragma omp parallel for schedule(static) reduction(| : bad_order, bad_range) if (nla > 65536)
+    for (int k = 0; k < nla; ++k) {
+      int i = i_sparse[k] - nb, j = j_sparse[k] - nb;
+      ia[k] = i;
+      ja[k] = j;
+      av[k] = a_sparse[k];
+      bad_order |= i > j;
+      bad_range |= (i < 0) | (j >= nd);
     }
-    s.a.assign(a_sparse, a_sparse + *la);
+    if (bad_order)
+      throw Error{ERR_ARGUMENT, "matrix in wrong format - only the upper triangle is expected for symmetric problems"};
+    if (bad_range) throw Error{ERR_ARGUMENT, "matrix index out of range"};
     // assembly (merge of repeated entries) and mesh components are computed
     // for all subdomains in parallel at setup
     s.assembled = false;
@@ -310,6 +321,13 @@ void bddcml_finalize_c(void) {
   });
 }
 
+void bddcml_release_device_memory_c(void) {
+  guarded("bddcml_release_device_memory_c", [&] {
+    Error err{BDDCML_OK, ""};
+    if (!device_release_memory(err)) throw err;
+  });
+}
+
 int bddcml_get_last_error_c(char* msg, int* lmsg) {
   if (msg && lmsg && *lmsg > 0) {
     int n = std::min<int>((int)g_msg.size(), *lmsg - 1);
@@ -338,7 +356,8 @@ void bddcml_get_stats_c(double* stats, int* lstats) {
                   (double)q.ndofc, (double)q.sum_ndofi, (double)q.sum_ndofo, (double)q.ninterface,
                   (double)S->prm.precision, q.h2d_bytes, q.d2h_bytes, q.t_upload, q.t_host_assemble,
                   q.t_host_iface, q.t_host_globs, q.t_host_blocks, q.refine1, q.refine2,
-                  q.flop_sweep_oo, q.flop_sweep_s, q.bytes_residual, q.bytes_schur_apply, q.bytes_pc_local};
+                  q.flop_sweep_oo, q.flop_sweep_s, q.bytes_residual, q.bytes_schur_apply, q.bytes_pc_local,
+                  q.launches_setup, q.launches_solve, q.t_dev_alloc, q.t_dev_h2d};
     int n = std::min<int>(*lstats, (int)(sizeof(v) / sizeof(v[0])));
     for (int i = 0; i < n; ++i) stats[i] = v[i];
     *lstats = n;

@@ -5,7 +5,9 @@
 #include <array>
 #include <cmath>
 #include <cstdio>
+#include <cstdint>
 #include <cstring>
+#include <memory>
 #include <numeric>
 #include <string>
 #include <type_traits>
@@ -24,8 +26,12 @@ namespace bddc {
       throw Error{ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)};                \
   } while (0)
 
+// Every kernel launch of the library is followed by CKL(), which also counts it.
+static long long g_launches = 0;
+
 #define CKL()                                                                                   \
   do {                                                                                          \
+    ++g_launches;                                                                               \
     cudaError_t e_ = cudaGetLastError();                                                        \
     if (e_ != cudaSuccess) throw Error{ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e_)}; \
   } while (0)
@@ -88,19 +94,53 @@ struct Profiler {
   }
 };
 
+// Device memory comes from one stream-ordered CUDA memory pool per device and
+// process.  The pool keeps what is freed (unlimited release threshold), so a
+// later setup in the same process allocates without new mappings; memory is
+// handed back to the driver by bddcml_release_device_memory_c or at exit.
+// Allocations and frees are ordered on the solver's stream.
+static constexpr int MAX_DEVICES = 64;
+static cudaMemPool_t g_pools[MAX_DEVICES] = {};
+static cudaStream_t g_alloc_st = nullptr;
+
+static cudaMemPool_t device_pool() {
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= MAX_DEVICES) throw Error{ERR_CUDA, "device index out of range for the memory pool table"};
+  if (!g_pools[dev]) {
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    CK(cudaMemPoolCreate(&g_pools[dev], &props));
+    uint64_t keep = UINT64_MAX;
+    CK(cudaMemPoolSetAttribute(g_pools[dev], cudaMemPoolAttrReleaseThreshold, &keep));
+  }
+  return g_pools[dev];
+}
+
 template <typename T>
 static T* dalloc(size_t n, std::vector<void*>& owned) {
   T* p = nullptr;
   if (n == 0) n = 1;
-  cudaError_t e = cudaMalloc(&p, n * sizeof(T));
+  cudaError_t e = cudaMallocFromPoolAsync(reinterpret_cast<void**>(&p), n * sizeof(T), device_pool(), g_alloc_st);
   if (e != cudaSuccess)
-    throw Error{ERR_MEMORY, "cudaMalloc of " + std::to_string(n * sizeof(T)) + " bytes: " + cudaGetErrorString(e)};
+    throw Error{ERR_MEMORY, "device allocation of " + std::to_string(n * sizeof(T)) + " bytes: " +
+                                cudaGetErrorString(e)};
   owned.push_back(p);
   return p;
 }
 
 // host<->device traffic of the current setup + solve (reported in the stats)
 static double g_h2d_bytes = 0.0, g_d2h_bytes = 0.0;
+
+template <typename T>
+static T* upload(const T* v, size_t n, std::vector<void*>& owned, cudaStream_t st) {
+  T* p = dalloc<T>(n, owned);
+  if (n) CK(cudaMemcpyAsync(p, v, n * sizeof(T), cudaMemcpyHostToDevice, st));
+  g_h2d_bytes += (double)n * sizeof(T);
+  return p;
+}
 
 template <typename T>
 static T* upload(const std::vector<T>& v, std::vector<void*>& owned, cudaStream_t st) {
@@ -161,9 +201,17 @@ class Device {
   int nref = 0;
   Profiler prof;
 
-  ~Device() { release(); if (hctl) cudaFreeHost(hctl); if (st) cudaStreamDestroy(st); }
+  ~Device() {
+    release();
+    if (hctl) cudaFreeHost(hctl);
+    if (st) {
+      cudaStreamSynchronize(st);
+      cudaStreamDestroy(st);
+    }
+    if (g_alloc_st == st) g_alloc_st = nullptr;
+  }
   void release() {
-    for (void* q : owned) cudaFree(q);
+    for (void* q : owned) cudaFreeAsync(q, st);
     owned.clear();
     maxit_alloc = 0;
   }
@@ -183,7 +231,20 @@ Device* device_create(Error& err) {
     delete d;
     return nullptr;
   }
+  g_alloc_st = d->st;
   return d;
+}
+
+bool device_release_memory(Error& err) {
+  try {
+    CK(cudaDeviceSynchronize());
+    for (auto& pool : g_pools)
+      if (pool) CK(cudaMemPoolTrimTo(pool, 0));
+  } catch (Error& e) {
+    err = e;
+    return false;
+  }
+  return true;
 }
 
 void device_destroy(Device* d) { delete d; }
@@ -212,18 +273,21 @@ static void run_panels(Device& D, const BandDesc* bd, const TcDesc* td, int nbat
 
 // forward + backward sweeps on the tensor cores (3xTF32, TMEM accumulation):
 // one launch per direction, one CTA per (system, 128-column tile)
-static void run_solve_tc(Device& D, const TcDesc* td, int nbatch, int maxnb, int maxncol, const float* P, float* B) {
+// forward + backward tensor-core sweep; passes 3 (3xTF32) or 1 (TF32)
+static void run_solve_tc(Device& D, const TcDesc* td, int nbatch, int maxnb, int maxncol, const float* P, float* B,
+                         int passes = 3) {
   static bool attr = false;
   const size_t smem = tc_smem_bytes();
   if (!attr) {
     CK(cudaFuncSetAttribute(k_band_sweep_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_band_sweep_tc, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
     attr = true;
   }
   (void)maxnb;
   dim3 grid(maxncol / TC_M, nbatch);
-  k_band_sweep_tc<<<grid, TC_THREADS, smem, D.st>>>(td, P, B, 0, D.err);
+  k_band_sweep_tc<<<grid, TC_THREADS, smem, D.st>>>(td, P, B, 0, passes, D.err);
   CKL();
-  k_band_sweep_tc<<<grid, TC_THREADS, smem, D.st>>>(td, P, B, 1, D.err);
+  k_band_sweep_tc<<<grid, TC_THREADS, smem, D.st>>>(td, P, B, 1, passes, D.err);
   CKL();
 }
 
@@ -250,6 +314,7 @@ bool device_setup(Solver& S, Error& err) {
     D.prof.reset();
     g_h2d_bytes = 0.0;
     g_d2h_bytes = 0.0;
+    g_launches = 0;
     D.mixed = S.prm.precision != 0;
     double t0 = wall_time();
     int nsub = (int)S.subs.size();
@@ -275,6 +340,7 @@ bool device_setup(Solver& S, Error& err) {
                                             std::to_string(herr) + ")"};
     D.prof.collect();
     S.stats.t_device_setup = wall_time() - t1;
+    S.stats.launches_setup = (double)g_launches;
   } catch (Error& e) {
     err = e;
     return false;
@@ -360,32 +426,50 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
     S.stats.bytes_per_iteration += (double)d.NI * d.NI * (D.mixed ? (8.0 + 4.0) : 16.0);
 
   // ---- allocations
+  double tw0 = wall_time();
   D.poolT = dalloc<T>(oT, own);
   float* ppool = std::is_same_v<T, float> ? dalloc<float>(oPan, own) : nullptr;
   D.poolS = D.mixed ? (void*)dalloc<float2>(oS, own) : (void*)dalloc<double>(oS, own);
   D.poolPC = dalloc<T>(oPC, own);
   D.small = dalloc<double>(oSm, own);
   D.err = dalloc<int>(1, own);
+  S.stats.t_dev_alloc = wall_time() - tw0;
   CK(cudaMemsetAsync(D.err, 0, sizeof(int), st));
   CK(cudaMemsetAsync(D.poolT, 0, oT * sizeof(T), st));
   D.ds = upload(D.hs, own, st);
 
-  // ---- CSR blocks
+  // ---- CSR blocks: every subdomain's rows (ptr with nrow + 1 entries,
+  // shifted by the subdomain's first entry) concatenated into one staging
+  // buffer, filled by all host threads (first touch included), then copied
+  // in one transfer.  The per-subdomain arrays are released as they are copied.
   auto concat = [&](auto get_ptr, auto get_col, auto get_val, CsrView& view) {
-    vector<int> ptr, col;
-    vector<double> val;
+    vector<long long> po(nsub + 1, 0), co(nsub + 1, 0);
     for (int t = 0; t < nsub; ++t) {
-      const vector<int>& p = get_ptr(blk[t]);
-      int base = (int)col.size();
-      for (size_t i = 0; i < p.size(); ++i) ptr.push_back(base + p[i]);
-      const vector<int>& c = get_col(blk[t]);
-      const vector<double>& v = get_val(blk[t]);
-      col.insert(col.end(), c.begin(), c.end());
-      val.insert(val.end(), v.begin(), v.end());
+      po[t + 1] = po[t] + (long long)get_ptr(blk[t]).size();
+      co[t + 1] = co[t] + (long long)get_col(blk[t]).size();
     }
-    view.ptr = upload(ptr, own, st);
-    view.col = upload(col, own, st);
-    view.val = upload(val, own, st);
+    if (co[nsub] > INT32_MAX) throw Error{ERR_UNSUPPORTED, "more than 2^31 matrix entries in one block type"};
+    std::unique_ptr<int[]> ptr(new int[std::max<long long>(1, po[nsub])]);
+    std::unique_ptr<int[]> col(new int[std::max<long long>(1, co[nsub])]);
+    std::unique_ptr<double[]> val(new double[std::max<long long>(1, co[nsub])]);
+#pragma omp parallel for schedule(dynamic)
+    for (int t = 0; t < nsub; ++t) {
+      vector<int>& p = get_ptr(blk[t]);
+      vector<int>& c = get_col(blk[t]);
+      vector<double>& v = get_val(blk[t]);
+      const int base = (int)co[t];
+      for (size_t i = 0; i < p.size(); ++i) ptr[po[t] + i] = base + p[i];
+      if (!c.empty()) {
+        std::memcpy(col.get() + co[t], c.data(), c.size() * sizeof(int));
+        std::memcpy(val.get() + co[t], v.data(), v.size() * sizeof(double));
+      }
+      vector<int>().swap(p);
+      vector<int>().swap(c);
+      vector<double>().swap(v);
+    }
+    view.ptr = upload(ptr.get(), (size_t)po[nsub], own, st);
+    view.col = upload(col.get(), (size_t)co[nsub], own, st);
+    view.val = upload(val.get(), (size_t)co[nsub], own, st);
   };
   concat([](SubBlocks& b) -> vector<int>& { return b.oo_ptr; }, [](SubBlocks& b) -> vector<int>& { return b.oo_col; },
          [](SubBlocks& b) -> vector<double>& { return b.oo_val; }, D.koo);
@@ -503,6 +587,7 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
     D.hbd_oo[t] = BandDesc{d.nbo, d.w, d.NR, 0, d.oL, d.oLinv, d.oXc};
   }
   D.bd_oo = upload(D.hbd_oo, own, st);
+  S.stats.t_dev_h2d = wall_time() - tw0 - S.stats.t_dev_alloc;
   D.prof.begin(PH_NUMERIC_TOTAL, st, true);
   D.prof.begin(PH_FACTOR_OO, st);
   k_fill_band<T><<<dim3((D.maxNO + 127) / 128, nsub), 128, 0, st>>>(D.ds, D.koo, poolT, D.bd_oo);
@@ -513,7 +598,7 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
   if constexpr (std::is_same_v<T, float>) {
     for (int t = 0; t < nsub; ++t) {
       auto& d = D.hs[t];
-      htd[t] = TcDesc{d.nbo, d.w, d.NR, 0, d.oXc, poff[t][0], poff[t][1]};
+      htd[t] = TcDesc{d.nbo, d.w, d.NR, 0, d.oXc, poff[t][0], poff[t][1], -1};
     }
     td_oo = upload(htd, own, st);
     run_panels(D, D.bd_oo, td_oo, nsub, D.maxnbo, D.maxw, poolT, ppool);
@@ -526,56 +611,51 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
   if constexpr (std::is_same_v<T, float>) run_solve_tc(D, td_oo, nsub, D.maxnbo, D.maxNR, ppool, poolT);
   else run_solve<T>(D, D.bd_oo, nsub, D.maxnbo, D.maxNR, poolT, poolT);
   D.prof.end(PH_SOLVE_OO, st);
-  // iterative refinement of [X | v] with FP64-accurate residuals: X is kept
-  // as a double-float pair in components 0 and 1, corrections land in the
-  // next free component and are merged
+  // Mixed precision: two refinement steps with FP64-accurate residuals.
+  //   R0 = [A_oi | f_o] - A_oo X0 -> component 1, D1 = A_oo^-1 R0 in place (3xTF32)
+  //   R1 = [A_oi | f_o] - A_oo (X0 + D1) -> component 2, D2 = A_oo^-1 R1 in place
+  //        with one TF32 pass (D2 is ~1e-10 of X, so its ~1e-3 relative error
+  //        stays far below the FP32 pair's resolution), added into D1 by the
+  //        backward sweep.
+  // X is then the unnormalised FP32 pair (X0, D1 + D2) in components 0 and 1.
   int* dmax = nullptr;
-  vector<int> hmax;
   if (D.prof.on && D.mixed) {
     dmax = dalloc<int>((size_t)nsub * 3, own);
     CK(cudaMemsetAsync(dmax, 0, (size_t)nsub * 3 * sizeof(int), st));
     k_comp_maxabs<<<dim3(64, nsub), 256, 0, st>>>(D.ds, reinterpret_cast<const float*>(poolT), 0, dmax);
     CKL();
   }
-  for (int rr = 1; rr <= D.nref; ++rr) {
-    const int outc = rr == 1 ? 1 : 2;
-    vector<BandDesc> hb = D.hbd_oo;
-    for (int t = 0; t < nsub; ++t) hb[t].oB = D.hs[t].oXc + (long long)outc * D.hs[t].NO * D.hs[t].NR;
-    BandDesc* bdr = upload(hb, own, st);
-    D.prof.begin(PH_RESIDUAL, st);
-    k_residual_df<<<dim3(D.maxNO, nsub), 128, 0, st>>>(D.ds, D.koo, D.koi, D.fo, D.fo_off,
-                                                       reinterpret_cast<float*>(poolT), rr > 1 ? 1 : 0, outc);
-    CKL();
-    D.prof.end(PH_RESIDUAL, st);
-    D.prof.begin(PH_SOLVE_OO, st);
-    if constexpr (std::is_same_v<T, float>) {
-      vector<TcDesc> h2 = htd;
-      for (int t = 0; t < nsub; ++t) h2[t].oB = hb[t].oB;
-      TcDesc* tdr = upload(h2, own, st);
-      run_solve_tc(D, tdr, nsub, D.maxnbo, D.maxNR, ppool, poolT);
-    } else {
-      run_solve<T>(D, bdr, nsub, D.maxnbo, D.maxNR, poolT, poolT);
-    }
-    D.prof.end(PH_SOLVE_OO, st);
-    if (dmax && rr <= 2) {
-      k_comp_maxabs<<<dim3(64, nsub), 256, 0, st>>>(D.ds, reinterpret_cast<const float*>(poolT), outc,
-                                                     dmax + (size_t)rr * nsub);
+  if constexpr (std::is_same_v<T, float>) {
+    for (int rr = 1; rr <= D.nref; ++rr) {
+      D.prof.begin(PH_RESIDUAL, st);
+      k_residual_df<<<dim3((D.maxNO + RES_ROWS - 1) / RES_ROWS, nsub), 128, 0, st>>>(
+          D.ds, D.koo, D.koi, D.fo, D.fo_off, poolT, rr > 1 ? 1 : 0, rr);
       CKL();
+      D.prof.end(PH_RESIDUAL, st);
+      D.prof.begin(PH_SOLVE_OO, st);
+      vector<TcDesc> h2 = htd;
+      for (int t = 0; t < nsub; ++t) {
+        const long long comp = (long long)D.hs[t].NO * D.hs[t].NR;
+        h2[t].oB = D.hs[t].oXc + rr * comp;
+        h2[t].oAcc = rr == 2 ? D.hs[t].oXc + comp : -1;  // D2 is added into D1
+      }
+      TcDesc* tdr = upload(h2, own, st);
+      run_solve_tc(D, tdr, nsub, D.maxnbo, D.maxNR, ppool, poolT, rr == 1 ? 3 : 1);
+      D.prof.end(PH_SOLVE_OO, st);
+      if (dmax && rr <= 2) {
+        k_comp_maxabs<<<dim3(64, nsub), 256, 0, st>>>(D.ds, poolT, rr, dmax + (size_t)rr * nsub);
+        CKL();
+      }
     }
-    D.prof.begin(PH_RESIDUAL, st);
-    k_merge_df<<<dim3(256, nsub), 256, 0, st>>>(D.ds, reinterpret_cast<float*>(poolT), outc);
-    CKL();
-    D.prof.end(PH_RESIDUAL, st);
   }
   if (dmax) {
-    hmax.resize((size_t)nsub * 3);
+    vector<int> hmax((size_t)nsub * 3);
     CK(cudaMemcpyAsync(hmax.data(), dmax, hmax.size() * sizeof(int), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     float r1 = 0.f, r2 = 0.f;
     for (int t = 0; t < nsub; ++t) {
-      float x0;
+      float x0, d1, d2;
       std::memcpy(&x0, &hmax[t], 4);
-      float d1, d2;
       std::memcpy(&d1, &hmax[nsub + t], 4);
       std::memcpy(&d2, &hmax[2 * nsub + t], 4);
       if (x0 > 0) { r1 = std::max(r1, d1 / x0); r2 = std::max(r2, d2 / x0); }
@@ -626,7 +706,7 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
     vector<TcDesc> hts(nsub);
     for (int t = 0; t < nsub; ++t) {
       auto& d = D.hs[t];
-      hts[t] = TcDesc{d.nbi, d.nbi - 1, d.NRC, 0, d.oBs, poff[t][2], poff[t][3]};
+      hts[t] = TcDesc{d.nbi, d.nbi - 1, d.NRC, 0, d.oBs, poff[t][2], poff[t][3], -1};
     }
     td_s = upload(hts, own, st);
     run_panels(D, bd_s, td_s, nsub, maxnbi, maxnbi - 1, poolT, ppool);
@@ -706,7 +786,7 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
     run_factor<T>(D, dcb, 1, nbc, nbc - 1, cpool);
     if constexpr (std::is_same_v<T, float>) {
       // identity right-hand side needs a column count that is a multiple of the MMA tile
-      vector<TcDesc> htc{TcDesc{nbc, nbc - 1, D.ldc, 0, cb.oB, 0, (long long)nbc * nbc * 2 * TC_PCHUNK}};
+      vector<TcDesc> htc{TcDesc{nbc, nbc - 1, D.ldc, 0, cb.oB, 0, (long long)nbc * nbc * 2 * TC_PCHUNK, -1}};
       TcDesc* tdc = upload(htc, own, st);
       float* cpan = dalloc<float>((size_t)2 * nbc * nbc * 2 * TC_PCHUNK, own);
       run_panels(D, dcb, tdc, 1, nbc, nbc - 1, cpool, cpan);
@@ -775,6 +855,7 @@ static void launch_pc(Device& D, const double* rin, double* zout, const PcgCtl* 
 
 static double host_sum_parts(Device& D) {
   k_sum_parts<<<1, RT, 0, D.st>>>(D.part, D.npart, D.scal);
+  CKL();
   double v = 0.0;
   CK(cudaMemcpyAsync(&v, D.scal, sizeof(double), cudaMemcpyDeviceToHost, D.st));
   CK(cudaStreamSynchronize(D.st));
@@ -839,11 +920,13 @@ static bool solve_impl(Solver& S, double tol, int maxit, int ndecrmax, int& num_
     g_h2d_bytes += D.n * sizeof(double);
     CK(cudaStreamSynchronize(st));
   }
+  long long launches0 = g_launches;
   D.prof.begin(PH_SOLVE_TOTAL, st, true);
   // r = g with fixed interface dofs zeroed (module_krylov.f90:222-236)
   k_assemble_plain<<<(D.n + 255) / 256, 256, 0, st>>>(D.n, D.own, D.grep, D.fixed, D.r);
   CKL();
   k_dot<<<D.npart, RT, 0, st>>>(D.n, D.r, D.r, D.wsum, D.part);
+  CKL();
   double normrhs2 = host_sum_parts(D);
   num_iter = 0; reason = 0; cond = 1.0;
   S.relres_history.clear();
@@ -855,6 +938,8 @@ static bool solve_impl(Solver& S, double tol, int maxit, int ndecrmax, int& num_
     k_axpy<<<(D.n + 255) / 256, 256, 0, st>>>(D.n, -1.0, D.ap, D.r);
     CKL();
     k_dot<<<D.npart, RT, 0, st>>>(D.n, D.r, D.r, D.wsum, D.part);
+    CKL();
+  CKL();
     double normres0 = std::sqrt(host_sum_parts(D));
     if (normres0 == 0.0) {
       postprocess = false;
@@ -892,12 +977,15 @@ static bool solve_impl(Solver& S, double tol, int maxit, int ndecrmax, int& num_
       reason = c2.reason;
       S.relres_history.resize(num_iter);
       if (num_iter > 0)
-        CK(cudaMemcpy(S.relres_history.data(), D.hist, num_iter * sizeof(double), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpyAsync(S.relres_history.data(), D.hist, num_iter * sizeof(double), cudaMemcpyDeviceToHost, st));
       int nw = c2.nw;
+      vector<double> dg(std::max(nw, 1)), sd(std::max(nw, 1));
       if (nw > 1) {
-        vector<double> dg(nw), sd(nw);
-        CK(cudaMemcpy(dg.data(), D.diag, nw * sizeof(double), cudaMemcpyDeviceToHost));
-        CK(cudaMemcpy(sd.data(), D.subdiag, nw * sizeof(double), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpyAsync(dg.data(), D.diag, nw * sizeof(double), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(sd.data(), D.subdiag, nw * sizeof(double), cudaMemcpyDeviceToHost, st));
+      }
+      CK(cudaStreamSynchronize(st));
+      if (nw > 1) {
         sd.resize(nw - 1);
         cond = lanczos_max_eig(dg, sd);
       } else {
@@ -941,6 +1029,7 @@ static bool solve_impl(Solver& S, double tol, int maxit, int ndecrmax, int& num_
   S.stats.t_postprocess = wall_time() - tp;
   S.stats.t_solve = wall_time() - t0;
   S.stats.num_iter = num_iter;
+  S.stats.launches_solve = (double)(g_launches - launches0);
   return true;
 }
 

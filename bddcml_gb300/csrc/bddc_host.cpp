@@ -36,50 +36,56 @@ double wall_time() {
 }
 
 // sort + merge duplicate (i,j) entries (the effect of sm_assembly,
-// module_sm.f90:630-684): counting sort by row, insertion sort of the short
-// rows by column, then merge of repeated pairs in their original order
+// module_sm.f90:630-684): counting sort by row keeps the upload order inside
+// a row, repeated columns are summed in that order (as a stable sort followed
+// by a merge would), and the distinct columns of each short row are then
+// sorted.  Scratch buffers are per thread and reused across subdomains.
 void host_assemble_upper(vector<int>& ia, vector<int>& ja, vector<double>& a) {
+  static thread_local vector<int> ptr, col, slot;
+  static thread_local vector<double> val;
   const size_t n = ia.size();
-  int nrow = 0;
-  for (size_t k = 0; k < n; ++k) nrow = std::max(nrow, ia[k] + 1);
-  vector<int> ptr(nrow + 1, 0);
+  int nrow = 0, ncol = 0;
+  for (size_t k = 0; k < n; ++k) { nrow = std::max(nrow, ia[k] + 1); ncol = std::max(ncol, ja[k] + 1); }
+  ptr.assign(nrow + 1, 0);
   for (size_t k = 0; k < n; ++k) ptr[ia[k] + 1]++;
   for (int r = 0; r < nrow; ++r) ptr[r + 1] += ptr[r];
-  vector<int> col(n);
-  vector<double> val(n);
-  {
-    vector<int> pos(ptr.begin(), ptr.end() - 1);
-    for (size_t k = 0; k < n; ++k) {
-      int q = pos[ia[k]]++;
-      col[q] = ja[k];
-      val[q] = a[k];
-    }
+  col.resize(n);
+  val.resize(n);
+  for (size_t k = 0; k < n; ++k) {
+    int q = ptr[ia[k]]++;
+    col[q] = ja[k];
+    val[q] = a[k];
   }
-  size_t out = 0;
+  for (int r = nrow; r > 0; --r) ptr[r] = ptr[r - 1];
+  ptr[0] = 0;
+  slot.assign(ncol, -1);
+  int out = 0;
   for (int r = 0; r < nrow; ++r) {
-    int b = ptr[r], e = ptr[r + 1];
-    for (int i = b + 1; i < e; ++i) {  // stable insertion sort by column
+    const int rs = out;
+    for (int i = ptr[r]; i < ptr[r + 1]; ++i) {
       int c = col[i];
-      double v = val[i];
-      int j = i - 1;
-      while (j >= b && col[j] > c) { col[j + 1] = col[j]; val[j + 1] = val[j]; --j; }
-      col[j + 1] = c;
-      val[j + 1] = v;
-    }
-    for (int i = b; i < e; ++i) {
-      if (out > 0 && ia[out - 1] == r && ja[out - 1] == col[i]) {
-        a[out - 1] += val[i];
+      if (slot[c] >= rs) {
+        a[slot[c]] += val[i];
       } else {
+        slot[c] = out;
         ia[out] = r;
-        ja[out] = col[i];
+        ja[out] = c;
         a[out] = val[i];
         ++out;
       }
     }
+    for (int i = rs + 1; i < out; ++i) {  // insertion sort of the distinct columns
+      int c = ja[i];
+      double v = a[i];
+      int j = i - 1;
+      while (j >= rs && ja[j] > c) { ja[j + 1] = ja[j]; a[j + 1] = a[j]; --j; }
+      ja[j + 1] = c;
+      a[j + 1] = v;
+    }
   }
-  ia.resize(out);
-  ja.resize(out);
-  a.resize(out);
+  ia.resize(out); ia.shrink_to_fit();
+  ja.resize(out); ja.shrink_to_fit();
+  a.resize(out); a.shrink_to_fit();
 }
 
 // components of the dual mesh graph: elements are connected when they share
@@ -145,55 +151,69 @@ void full_symmetric_csr(const Subdomain& s, vector<int>& ptr, vector<int>& col, 
 }
 
 // Interior ordering for the band factor: natural order or reverse
-// Cuthill-McKee, whichever has the smaller half bandwidth.
+// Cuthill-McKee, whichever has the smaller half bandwidth.  The interior
+// graph is kept as flat arrays; neighbours of a visited node are queued by
+// increasing degree (stable, so ties keep the matrix order).
 void host_interior_ordering(Subdomain& s, const vector<int>& f_ptr, const vector<int>& f_col) {
-  int no = s.ndofo;
+  const int no = s.ndofo;
   vector<int> mo(s.ndof, -1);
   for (int i = 0; i < no; ++i) mo[s.iovsvn[i]] = i;
-  vector<vector<int>> g(no);
+  vector<int> gptr(no + 1, 0), gcol;
+  gcol.reserve((size_t)no * 27);
   for (int i = 0; i < no; ++i) {
     int r = s.iovsvn[i];
     for (int k = f_ptr[r]; k < f_ptr[r + 1]; ++k) {
       int c = mo[f_col[k]];
-      if (c >= 0 && c != i) g[i].push_back(c);
+      if (c >= 0 && c != i) gcol.push_back(c);
     }
+    gptr[i + 1] = (int)gcol.size();
   }
+  auto deg = [&](int v) { return gptr[v + 1] - gptr[v]; };
+  vector<int> inv(no);
   auto bandwidth = [&](const vector<int>& perm) {
-    vector<int> inv(no);
     for (int i = 0; i < no; ++i) inv[perm[i]] = i;
     int b = 0;
     for (int i = 0; i < no; ++i)
-      for (int c : g[i]) b = std::max(b, std::abs(inv[i] - inv[c]));
+      for (int k = gptr[i]; k < gptr[i + 1]; ++k) b = std::max(b, std::abs(inv[i] - inv[gcol[k]]));
     return b;
   };
   vector<int> natural(no);
   std::iota(natural.begin(), natural.end(), 0);
   int bn = bandwidth(natural);
-  // reverse Cuthill-McKee from a minimum-degree start node
+  // reverse Cuthill-McKee, each component rooted at its first node of
+  // minimum degree
   vector<int> rcm;
   rcm.reserve(no);
-  vector<char> seen(no, 0);
+  vector<char> seen(no, 0), vis(no, 0);
+  vector<int> comp;
+  comp.reserve(no);
   for (int st = 0; st < no; ++st) {
     if (seen[st]) continue;
-    int start = st, mind = (int)g[st].size();
-    // choose a low-degree node of this component as the root
-    {
-      vector<int> comp{st};
-      vector<char> vis(no, 0);
-      vis[st] = 1;
-      for (size_t q = 0; q < comp.size(); ++q)
-        for (int c : g[comp[q]]) if (!vis[c] && !seen[c]) { vis[c] = 1; comp.push_back(c); }
-      for (int v : comp) if ((int)g[v].size() < mind) { mind = (int)g[v].size(); start = v; }
-    }
+    int start = st, mind = deg(st);
+    comp.assign(1, st);
+    vis[st] = 1;
+    for (size_t q = 0; q < comp.size(); ++q)
+      for (int k = gptr[comp[q]]; k < gptr[comp[q] + 1]; ++k) {
+        int c = gcol[k];
+        if (!vis[c] && !seen[c]) { vis[c] = 1; comp.push_back(c); }
+      }
+    for (int v : comp) if (deg(v) < mind) { mind = deg(v); start = v; }
     size_t head = rcm.size();
     rcm.push_back(start);
     seen[start] = 1;
     while (head < rcm.size()) {
       int v = rcm[head++];
-      vector<int> nb;
-      for (int c : g[v]) if (!seen[c]) { seen[c] = 1; nb.push_back(c); }
-      std::sort(nb.begin(), nb.end(), [&](int x, int y) { return g[x].size() < g[y].size(); });
-      rcm.insert(rcm.end(), nb.begin(), nb.end());
+      size_t b = rcm.size();
+      for (int k = gptr[v]; k < gptr[v + 1]; ++k) {
+        int c = gcol[k];
+        if (!seen[c]) { seen[c] = 1; rcm.push_back(c); }
+      }
+      for (size_t i = b + 1; i < rcm.size(); ++i) {  // stable insertion sort by degree
+        int x = rcm[i], dx = deg(x);
+        size_t j = i;
+        while (j > b && deg(rcm[j - 1]) > dx) { rcm[j] = rcm[j - 1]; --j; }
+        rcm[j] = x;
+      }
     }
   }
   std::reverse(rcm.begin(), rcm.end());
@@ -721,16 +741,21 @@ void host_prepare_blocks(Subdomain& s, SubBlocks& b) {
   auto build = [&](int nrow, auto rowdof, const vector<int>& colmap, vector<int>& ptr, vector<int>& col,
                    vector<double>& val, int& maxrow) {
     ptr.assign(nrow + 1, 0);
-    col.clear(); val.clear();
     maxrow = 0;
     for (int r = 0; r < nrow; ++r) {
-      int d = rowdof(r);
+      int d = rowdof(r), cnt = 0;
+      for (int k = fptr[d]; k < fptr[d + 1]; ++k) cnt += colmap[fcol[k]] >= 0;
+      ptr[r + 1] = ptr[r] + cnt;
+      maxrow = std::max(maxrow, cnt);
+    }
+    col.resize(ptr[nrow]);
+    val.resize(ptr[nrow]);
+    for (int r = 0; r < nrow; ++r) {
+      int d = rowdof(r), q = ptr[r];
       for (int k = fptr[d]; k < fptr[d + 1]; ++k) {
         int c = colmap[fcol[k]];
-        if (c >= 0) { col.push_back(c); val.push_back(fval[k]); }
+        if (c >= 0) { col[q] = c; val[q++] = fval[k]; }
       }
-      ptr[r + 1] = (int)col.size();
-      maxrow = std::max(maxrow, ptr[r + 1] - ptr[r]);
     }
   };
   auto orow = [&](int r) { return s.iovsvn[s.operm[r]]; };

@@ -104,13 +104,15 @@ struct Stats {
   double setup_flops = 0;
   double h2d_bytes = 0, d2h_bytes = 0;
   double t_upload = 0, t_host_assemble = 0, t_host_iface = 0, t_host_globs = 0, t_host_blocks = 0;
-  double refine1 = 0, refine2 = 0;  // max |correction| / max |X| after refinement steps 1, 2
+  double refine1 = 0, refine2 = 0;  // max |correction| / max |X| of refinement steps 1, 2
   // algorithmic work per launch of the main phases (for roofline reporting)
   double flop_sweep_oo = 0;     // one forward + backward interior sweep, all subdomains (FP32 flop)
   double flop_sweep_s = 0;      // one forward + backward preconditioner-block sweep
   double bytes_residual = 0;    // one refinement residual (X read once, R written)
   double bytes_schur_apply = 0; // one Schur operator apply
   double bytes_pc_local = 0;    // one local preconditioner apply
+  double launches_setup = 0, launches_solve = 0;  // kernel launches of the last set-up / solve
+  double t_dev_alloc = 0, t_dev_h2d = 0;  // device set-up: allocations, staging + host->device copies
 };
 
 // Per-subdomain matrix blocks in device-ready form (interior rows in the
@@ -156,6 +158,7 @@ void host_prepare_blocks(Subdomain& s, SubBlocks& b);
 
 // device (bddc_device.cu)
 Device* device_create(Error& err);
+bool device_release_memory(Error& err);
 void device_destroy(Device* d);
 bool device_setup(Solver& S, Error& err);
 bool device_solve(Solver& S, double tol, int maxit, int ndecrmax, int& num_iter, int& reason, double& cond,

@@ -230,88 +230,115 @@ __global__ void k_fill_rhs(const DevSub* __restrict__ ds, CsrView koi, const dou
 
 // Refinement residual of the interior solves, FP64-accurate on FP32 pipes:
 // R = [A_oi | f_o] - A_oo X, written as FP32 into component `outcomp`.  X is
-// component 0 (an exact FP32 value, xpair = 0) or the double-float pair held
-// in components 0 and 1 (xpair = 1).  One CTA per interior row; the row's
-// matrix entries are staged in shared memory; padding columns are zero.
+// component 0 (an exact FP32 value, xpair = 0) or the FP32 pair held in
+// components 0 and 1 (xpair = 1).  One CTA per RES_ROWS interior rows; each
+// thread owns groups of 4 adjacent columns (float4 loads of X), the rows'
+// matrix entries are staged in shared memory with their X row offsets, and
+// the CTA walks its rows in order so that the band neighbours they share are
+// served from L1.  Padding columns and rows are written as zero.
+constexpr int RES_ROWS = 8;
+constexpr int RES_MAXNZ = 96;
 __global__ void __launch_bounds__(128) k_residual_df(const DevSub* __restrict__ ds, CsrView koo, CsrView koi,
                                                      const double* __restrict__ fo,
                                                      const long long* __restrict__ fo_off, float* __restrict__ pool,
                                                      int xpair, int outcomp) {
   const DevSub s = ds[blockIdx.y];
-  const int r = blockIdx.x;
-  if (r >= s.NO) return;
-  __shared__ int scol[96];
-  __shared__ dfloat sval[96];
-  __shared__ int bcol[96];
-  __shared__ dfloat bval[96];
-  __shared__ int nnz, nb0;
+  const int r0 = blockIdx.x * RES_ROWS;
+  if (r0 >= s.NO) return;
+  __shared__ int soff[RES_ROWS][RES_MAXNZ];       // X row offsets (row * NR) of the A_oo entries
+  __shared__ dfloat sval[RES_ROWS][RES_MAXNZ];    // -A_oo entries
+  __shared__ int bcol[RES_ROWS][RES_MAXNZ];       // columns of [A_oi | f_o]
+  __shared__ dfloat bval[RES_ROWS][RES_MAXNZ];
+  __shared__ int nnz[RES_ROWS], nb[RES_ROWS];
+  const int nrow = min(RES_ROWS, s.NO - r0);
+  const int tid = threadIdx.x;
+  if (tid < RES_ROWS) {
+    const int r = r0 + tid;
+    if (tid < nrow && r < s.no) {
+      const int* p = koo.ptr + s.koo;
+      const int* pb = koi.ptr + s.koi;
+      nnz[tid] = min(RES_MAXNZ, p[r + 1] - p[r]);
+      nb[tid] = min(RES_MAXNZ - 1, pb[r + 1] - pb[r]) + 1;
+    } else {
+      nnz[tid] = 0;
+      nb[tid] = 0;
+    }
+  }
+  __syncthreads();
+  for (int rr = 0; rr < nrow; ++rr) {
+    const int r = r0 + rr;
+    if (r >= s.no) break;
+    const int* p = koo.ptr + s.koo;
+    for (int q = tid; q < nnz[rr]; q += blockDim.x) {
+      soff[rr][q] = koo.col[p[r] + q] * s.NR;
+      sval[rr][q] = df_from_double(-koo.val[p[r] + q]);
+    }
+    const int* pb = koi.ptr + s.koi;
+    for (int q = tid; q < nb[rr] - 1; q += blockDim.x) {
+      bcol[rr][q] = koi.col[pb[r] + q];
+      bval[rr][q] = df_from_double(koi.val[pb[r] + q]);
+    }
+    if (tid == 0) {
+      bcol[rr][nb[rr] - 1] = s.ni;
+      bval[rr][nb[rr] - 1] = df_from_double(fo[fo_off[blockIdx.y] + r]);
+    }
+  }
+  __syncthreads();
   const long long comp = (long long)s.NO * s.NR;
-  float* out = pool + s.oXc + (long long)outcomp * comp + (long long)r * s.NR;
-  if (r >= s.no) {
-    for (int c = threadIdx.x; c < s.NR; c += blockDim.x) out[c] = 0.f;
-    return;
-  }
-  if (threadIdx.x == 0) {
-    const int* p = koo.ptr + s.koo;
-    nnz = min(96, p[r + 1] - p[r]);
-    const int* pb = koi.ptr + s.koi;
-    nb0 = min(95, pb[r + 1] - pb[r]);
-  }
-  __syncthreads();
-  {
-    const int* p = koo.ptr + s.koo;
-    for (int q = threadIdx.x; q < nnz; q += blockDim.x) {
-      scol[q] = koo.col[p[r] + q];
-      sval[q] = df_from_double(-koo.val[p[r] + q]);
-    }
-    const int* pb = koi.ptr + s.koi;
-    for (int q = threadIdx.x; q < nb0; q += blockDim.x) {
-      bcol[q] = koi.col[pb[r] + q];
-      bval[q] = df_from_double(koi.val[pb[r] + q]);
-    }
-    if (threadIdx.x == 0) {
-      bcol[nb0] = s.ni;
-      bval[nb0] = df_from_double(fo[fo_off[blockIdx.y] + r]);
-    }
-  }
-  __syncthreads();
   const float* X0 = pool + s.oXc;
   const float* X1 = X0 + comp;
-  for (int c = threadIdx.x; c < s.NR; c += blockDim.x) {
-    if (c > s.ni) { out[c] = 0.f; continue; }
-    dfacc acc;
-    for (int q = 0; q <= nb0; ++q)
-      if (bcol[q] == c) acc.add_df(bval[q]);
-    if (xpair) {
-      for (int q = 0; q < nnz; ++q) {
-        long long o = (long long)scol[q] * s.NR + c;
-        acc.fma_df(sval[q], dfloat{X0[o], X1[o]});
+  float* out = pool + s.oXc + (long long)outcomp * comp;
+  const int ngrp = s.NR / 4;
+  for (int gidx = tid; gidx < ngrp; gidx += blockDim.x) {
+    const int c = 4 * gidx;
+    for (int rr = 0; rr < nrow; ++rr) {
+      const int r = r0 + rr;
+      float4 res = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (r < s.no && c <= s.ni) {
+        dfacc a0, a1, a2, a3;
+        for (int q = 0; q < nb[rr]; ++q) {
+          const int d = bcol[rr][q] - c;
+          if ((unsigned)d < 4u) {
+            const dfloat v = bval[rr][q];
+            if (d == 0) a0.add_df(v);
+            else if (d == 1) a1.add_df(v);
+            else if (d == 2) a2.add_df(v);
+            else a3.add_df(v);
+          }
+        }
+        const int n = nnz[rr];
+        if (xpair) {
+          for (int q = 0; q < n; ++q) {
+            const dfloat a = sval[rr][q];
+            const int o = soff[rr][q] + c;
+            const float4 h = *reinterpret_cast<const float4*>(X0 + o);
+            const float4 l = *reinterpret_cast<const float4*>(X1 + o);
+            a0.fma_df(a, dfloat{h.x, l.x});
+            a1.fma_df(a, dfloat{h.y, l.y});
+            a2.fma_df(a, dfloat{h.z, l.z});
+            a3.fma_df(a, dfloat{h.w, l.w});
+          }
+        } else {
+          for (int q = 0; q < n; ++q) {
+            const dfloat a = sval[rr][q];
+            const float4 h = *reinterpret_cast<const float4*>(X0 + soff[rr][q] + c);
+            a0.fma_df(a, h.x);
+            a1.fma_df(a, h.y);
+            a2.fma_df(a, h.z);
+            a3.fma_df(a, h.w);
+          }
+        }
+        res = make_float4(a0.value().hi, a1.value().hi, a2.value().hi, a3.value().hi);
+        // columns beyond the rhs column are padding
+        if (c + 1 > s.ni) res.y = 0.f;
+        if (c + 2 > s.ni) res.z = 0.f;
+        if (c + 3 > s.ni) res.w = 0.f;
       }
-    } else {
-      for (int q = 0; q < nnz; ++q) acc.fma_df(sval[q], X0[(long long)scol[q] * s.NR + c]);
+      *reinterpret_cast<float4*>(out + (long long)r * s.NR + c) = res;
     }
-    out[c] = acc.value().hi;
   }
 }
 
-// X <- X + D: components (0, 1) hold X as a double-float pair (component 1
-// is taken as zero when addcomp == 1), D is component `addcomp`
-__global__ void k_merge_df(const DevSub* __restrict__ ds, float* __restrict__ pool, int addcomp) {
-  const DevSub s = ds[blockIdx.y];
-  const long long comp = (long long)s.NO * s.NR;
-  float* X0 = pool + s.oXc;
-  float* X1 = X0 + comp;
-  const float* D = X0 + (long long)addcomp * comp;
-  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < comp; e += (long long)gridDim.x * blockDim.x) {
-    float hi = X0[e], lo = addcomp == 1 ? 0.f : X1[e], d = D[e];
-    float t, err;
-    two_sum(hi, d, t, err);
-    lo += err;
-    float h2 = t + lo;
-    X0[e] = h2;
-    X1[e] = lo - (h2 - t);
-  }
-}
 
 // largest |component| per subdomain (refinement diagnostics; FP32 bit patterns
 // of non-negative values order like integers)
@@ -327,8 +354,9 @@ __global__ void k_comp_maxabs(const DevSub* __restrict__ ds, const float* __rest
   if ((threadIdx.x & 31) == 0) atomicMax(out + blockIdx.y, __float_as_int(m));
 }
 
-// Schur complement S = A_ii - A_io (X_0 + ...), FP64-accurate, plus the
-// subdomain part of the reduced rhs g = f_i - A_io X(:, ni).
+// Schur complement S = A_ii - A_io (X_0 + X_1), FP64-accurate, plus the
+// subdomain part of the reduced rhs g = f_i - A_io X(:, ni), where X_0 + X_1
+// is the refined interior solution held as an (unnormalised) FP32 pair.
 // Mixed precision stores S as FP32 (hi, lo) pairs.
 __global__ void __launch_bounds__(128) k_schur_df(const DevSub* __restrict__ ds, CsrView kio, CsrView kii,
                                                   const float* __restrict__ pool, float2* __restrict__ Spool,

@@ -141,6 +141,7 @@ struct TcDesc {
   long long oB;      // RHS block (row-major, ld = ncol) in the work pool
   long long oPf;     // forward panels in the panel pool
   long long oPb;     // backward panels
+  long long oAcc;    // < 0, or a block (same shape as B) the backward sweep adds its result into
 };
 
 // panel storage: block row k, chunk q at ((k * (w+1)*2) + q) * TC_PCHUNK
@@ -153,15 +154,20 @@ __host__ __device__ __forceinline__ long long panel_chunk(long long base, int w,
 // tiles are independent, so no grid-wide synchronisation is needed and the
 // band window of a tile (w+1 block rows x 128 columns) stays in L2 between
 // consecutive block rows.  grid (max column tiles, batch).
-__global__ void __launch_bounds__(TC_THREADS, 1)
+// passes = 3: 3xTF32 (FP32-class result); passes = 1: one TF32 product
+// (hi x hi, relative error ~1e-3), for a refinement correction that is
+// itself ~1e-10 of the solution.  With oAcc >= 0 the backward sweep also
+// adds each finished block row into the block at oAcc.
+__global__ void __launch_bounds__(TC_THREADS, 2)
     k_band_sweep_tc(const TcDesc* __restrict__ td, const float* __restrict__ ppool, float* __restrict__ bpool,
-                    int dir, int* __restrict__ err) {
+                    int dir, int passes, int* __restrict__ err) {
   const TcDesc d = td[blockIdx.y];
   const int c0 = blockIdx.x * TC_M;
   if (c0 >= d.ncol || d.nb == 0) return;
   const int ld = d.ncol;
   float* B = bpool + d.oB;
   const float* P = ppool + (dir == 0 ? d.oPf : d.oPb);
+  const uint32_t pbytes = (passes == 1 ? TC_PCHUNK / 2 : TC_PCHUNK) * 4;  // hi half first in a chunk
 
   extern __shared__ __align__(1024) unsigned char smraw[];
   float* sA = reinterpret_cast<float*>(smraw);                  // [stage][hi|lo][TC_ACHUNK]
@@ -172,6 +178,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   __shared__ long long last_commit, tma_pending[TC_STAGES];
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  // sweep order: step s handles block row k(s); its window is nblk(s) blocks from j0(s)
+  auto row_of = [&](int sidx) { return dir == 0 ? sidx : d.nb - 1 - sidx; };
+  auto window = [&](int k, int& j0, int& nblk) {
+    if (dir == 0) { j0 = k - min(k, d.w); nblk = k - j0 + 1; }
+    else { j0 = k; nblk = min(d.w, d.nb - 1 - k) + 1; }
+  };
+  auto issue_panel = [&](int st, int k, int q, long long gg) {  // thread 0
+    mbar_expect_tx(&bar_p[st], pbytes);
+    bulk_g2s(sP + st * TC_PCHUNK, P + panel_chunk(0, d.w, k, q), pbytes, &bar_p[st]);
+    tma_pending[st] = gg;
+  };
   if (tid == 0) {
     for (int s = 0; s < TC_STAGES; ++s) {
       mbar_init(&bar_p[s], 1);
@@ -193,17 +210,36 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   const uint32_t tmem = tmem_base;
   constexpr uint32_t idesc = tc_idesc(TC_M, TC_N);
 
-  long long g = 0;  // chunk counter over the whole sweep (mbarrier phases)
-  for (int sidx = 0; sidx < d.nb; ++sidx) {
-    const int k = dir == 0 ? sidx : d.nb - 1 - sidx;
+  // the window rows of the first chunk, and its panel chunk
+  float vn[TC_KC];
+  {
     int j0, nblk;
-    if (dir == 0) { j0 = k - min(k, d.w); nblk = k - j0 + 1; }
-    else { j0 = k; nblk = min(d.w, d.nb - 1 - k) + 1; }
+    window(row_of(0), j0, nblk);
+    const float* src = B + (long long)(j0 * NB) * ld + c0 + tid;
+#pragma unroll
+    for (int t = 0; t < TC_KC; ++t) vn[t] = src[(long long)t * ld];
+    if (tid == 0) issue_panel(0, row_of(0), 0, 0);
+  }
+  bool pending_load = false;  // the next row's first chunk waits for this row's results
+  long long g = 0;            // chunk counter over the whole sweep (stage = g & 1)
+  for (int sidx = 0; sidx < d.nb; ++sidx) {
+    const int k = row_of(sidx);
+    int j0, nblk;
+    window(k, j0, nblk);
     const int nchunk = nblk * (NB / TC_KC);
     const float* src0 = B + (long long)(j0 * NB) * ld + c0 + tid;
-    float vn[TC_KC];
+    if (pending_load) {
 #pragma unroll
-    for (int t = 0; t < TC_KC; ++t) vn[t] = src0[(long long)t * ld];
+      for (int t = 0; t < TC_KC; ++t) vn[t] = src0[(long long)t * ld];
+      pending_load = false;
+    }
+    // the chunk after the last one of this row: first chunk of the next row
+    int nk = -1, nj0 = 0;
+    if (sidx + 1 < d.nb) {
+      int nnblk;
+      nk = row_of(sidx + 1);
+      window(nk, nj0, nnblk);
+    }
     for (int q = 0; q < nchunk; ++q, ++g) {
       const int st = (int)(g & 1);
       float v[TC_KC];
@@ -213,30 +249,41 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         const float* src = src0 + (long long)((q + 1) * TC_KC) * ld;
 #pragma unroll
         for (int t = 0; t < TC_KC; ++t) vn[t] = src[(long long)t * ld];
+      } else if (nk >= 0) {
+        if (nj0 != k) {  // rows already final: fetch them now
+          const float* src = B + (long long)(nj0 * NB) * ld + c0 + tid;
+#pragma unroll
+          for (int t = 0; t < TC_KC; ++t) vn[t] = src[(long long)t * ld];
+        } else {
+          pending_load = true;
+        }
       }
       if (g >= TC_STAGES) {
         if (!mbar_wait(&bar_mma[st], (uint32_t)(((g - TC_STAGES) >> 1) & 1))) { if (tid == 0) abort_flag = 1; }
       }
       __syncthreads();
       if (abort_flag) break;
-      if (tid == 0) {
-        mbar_expect_tx(&bar_p[st], TC_PCHUNK * 4);
-        bulk_g2s(sP + st * TC_PCHUNK, P + panel_chunk(0, d.w, k, q), TC_PCHUNK * 4, &bar_p[st]);
-        tma_pending[st] = g;
-      }
       {
         float* ahi = sA + (st * 2 + 0) * TC_ACHUNK;
         float* alo = sA + (st * 2 + 1) * TC_ACHUNK;
+        if (passes == 1) {
 #pragma unroll
-        for (int t4 = 0; t4 < TC_KC / 4; ++t4) {
-          float4 h, l;
-          h.x = tf32_rna(v[4 * t4 + 0]); l.x = v[4 * t4 + 0] - h.x;
-          h.y = tf32_rna(v[4 * t4 + 1]); l.y = v[4 * t4 + 1] - h.y;
-          h.z = tf32_rna(v[4 * t4 + 2]); l.z = v[4 * t4 + 2] - h.z;
-          h.w = tf32_rna(v[4 * t4 + 3]); l.w = v[4 * t4 + 3] - h.w;
-          int off = canon_off(tid, 4 * t4);
-          *reinterpret_cast<float4*>(ahi + off) = h;
-          *reinterpret_cast<float4*>(alo + off) = l;
+          for (int t4 = 0; t4 < TC_KC / 4; ++t4)
+            *reinterpret_cast<float4*>(ahi + canon_off(tid, 4 * t4)) =
+                make_float4(tf32_rna(v[4 * t4]), tf32_rna(v[4 * t4 + 1]), tf32_rna(v[4 * t4 + 2]),
+                            tf32_rna(v[4 * t4 + 3]));
+        } else {
+#pragma unroll
+          for (int t4 = 0; t4 < TC_KC / 4; ++t4) {
+            float4 h, l;
+            h.x = tf32_rna(v[4 * t4 + 0]); l.x = v[4 * t4 + 0] - h.x;
+            h.y = tf32_rna(v[4 * t4 + 1]); l.y = v[4 * t4 + 1] - h.y;
+            h.z = tf32_rna(v[4 * t4 + 2]); l.z = v[4 * t4 + 2] - h.z;
+            h.w = tf32_rna(v[4 * t4 + 3]); l.w = v[4 * t4 + 3] - h.w;
+            int off = canon_off(tid, 4 * t4);
+            *reinterpret_cast<float4*>(ahi + off) = h;
+            *reinterpret_cast<float4*>(alo + off) = l;
+          }
         }
       }
       fence_async_smem();
@@ -252,20 +299,44 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           const uint32_t a_lo = smem_u32(sA + (st * 2 + 1) * TC_ACHUNK);
           const uint32_t p_hi = smem_u32(sP + st * TC_PCHUNK);
           const uint32_t p_lo = p_hi + TC_N * TC_KC * 4;
+          if (passes == 1) {
 #pragma unroll
-          for (int kk = 0; kk < TC_KC / 8; ++kk) {
-            const uint32_t koff = kk * 2 * TC_LBO;
-            uint32_t acc = (q > 0 || kk > 0) ? 1u : 0u;
-            mma_tf32(tmem, tc_desc(a_lo + koff), tc_desc(p_hi + koff), idesc, acc);
-            mma_tf32(tmem, tc_desc(a_hi + koff), tc_desc(p_lo + koff), idesc, 1u);
-            mma_tf32(tmem, tc_desc(a_hi + koff), tc_desc(p_hi + koff), idesc, 1u);
+            for (int kk = 0; kk < TC_KC / 8; ++kk) {
+              const uint32_t koff = kk * 2 * TC_LBO;
+              mma_tf32(tmem, tc_desc(a_hi + koff), tc_desc(p_hi + koff), idesc, (q > 0 || kk > 0) ? 1u : 0u);
+            }
+          } else {
+#pragma unroll
+            for (int kk = 0; kk < TC_KC / 8; ++kk) {
+              const uint32_t koff = kk * 2 * TC_LBO;
+              uint32_t acc = (q > 0 || kk > 0) ? 1u : 0u;
+              mma_tf32(tmem, tc_desc(a_lo + koff), tc_desc(p_hi + koff), idesc, acc);
+              mma_tf32(tmem, tc_desc(a_hi + koff), tc_desc(p_lo + koff), idesc, 1u);
+              mma_tf32(tmem, tc_desc(a_hi + koff), tc_desc(p_hi + koff), idesc, 1u);
+            }
           }
           mma_commit(&bar_mma[st]);
           last_commit = g;
+          // panel of the next chunk into the other stage, once the MMAs of
+          // chunk g-1 (which read that stage) are done
+          const int pk = q + 1 < nchunk ? k : nk;
+          const int pq = q + 1 < nchunk ? q + 1 : 0;
+          if (pk >= 0) {
+            if (g >= 1 && !mbar_wait(&bar_mma[st ^ 1], (uint32_t)(((g - 1) >> 1) & 1))) abort_flag = 1;
+            else issue_panel(st ^ 1, pk, pq, g + 1);
+          }
         }
       }
     }
     // block row k done: wait for its MMAs, move the accumulator to global memory
+    // (the rows of an accumulation target are fetched before the wait)
+    float* dst2 = (dir == 1 && d.oAcc >= 0) ? bpool + d.oAcc + (long long)(k * NB) * ld + c0 + warp * 32 + lane
+                                            : nullptr;
+    float accin[TC_N];
+    if (dst2) {
+#pragma unroll
+      for (int i = 0; i < TC_N; ++i) accin[i] = dst2[(long long)i * ld];
+    }
     __syncthreads();
     if (tid == 0 && !abort_flag) {
       long long ql = last_commit;
@@ -283,6 +354,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         tmem_ld16(taddr + part * 16, vv);
 #pragma unroll
         for (int i = 0; i < 16; ++i) dst[(long long)(part * 16 + i) * ld] = vv[i];
+        if (dst2) {
+#pragma unroll
+          for (int i = 0; i < 16; ++i) dst2[(long long)(part * 16 + i) * ld] = accin[part * 16 + i] + vv[i];
+        }
       }
     }
     tc_fence_before();

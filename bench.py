@@ -271,11 +271,12 @@ def run_gpu(args):
         "iterations": it, "converged_reason": reason, "condition_number": cond,
         "phases_ms": {k: v[0] for k, v in prof_p.items()},
         "phase_launches": {k: v[1] for k, v in prof_p.items()},
-        "gpu_launches": None,
+        "gpu_launches": int(args.steps * (st["launches_setup"] + st["launches_solve"])),
+        "gpu_launches_per_step": {"setup": int(st["launches_setup"]), "solve": int(st["launches_solve"])},
         "roofline": roof, "phase_rooflines": all_roof, "fp64_plain": fp64, "cpu_baseline": cpu,
         "refinement": {"max_correction_ratio_1": st_p["refine1"], "max_correction_ratio_2": st_p["refine2"]},
         "host_ms": {k: 1e3 * st_p[k] for k in ("t_upload", "t_host_assemble", "t_host_iface", "t_host_globs",
-                                                "t_host_blocks")},
+                                                "t_host_blocks", "t_device_setup", "t_dev_alloc", "t_dev_h2d")},
         "e2e_phases_ms": st["e2e_phases_ms"],
         "clocks": clocks,
     }

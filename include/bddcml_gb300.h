@@ -134,7 +134,7 @@ int bddcml_get_last_error_c(char *msg, int *lmsg);
 void bddcml_set_precision_c(int *mode);
 
 /* Timing and size report of the last setup and solve, filled into stats
- * (length *lstats, up to 32 doubles; see bddcml_gb300/__init__.py for the
+ * (length *lstats, up to 64 doubles; see bddcml_gb300/__init__.py for the
  * field list).  No counterpart in the reference. */
 void bddcml_get_stats_c(double *stats, int *lstats);
 
@@ -161,6 +161,13 @@ void bddcml_set_profiling_c(int *on);
  * setup_preconditioner (see bddcml_gb300/__init__.py PHASES for the order);
  * *lphase in: capacity, out: number of phases. */
 void bddcml_get_profile_c(double *ms, int *counts, int *lphase);
+
+/* Device memory of a solver is taken from a per-process CUDA memory pool
+ * that keeps freed memory for the next setup (bddcml_finalize_c returns the
+ * solver's memory to that pool, not to the driver).  This call hands all
+ * unused pooled memory back to the driver; it may be called at any time.
+ * No counterpart in the reference. */
+void bddcml_release_device_memory_c(void);
 
 #ifdef __cplusplus
 }
