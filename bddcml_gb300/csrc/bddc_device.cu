@@ -273,22 +273,32 @@ static void run_panels(Device& D, const BandDesc* bd, const TcDesc* td, int nbat
 
 // forward + backward sweeps on the tensor cores (3xTF32, TMEM accumulation):
 // one launch per direction, one CTA per (system, 128-column tile)
-// forward + backward tensor-core sweep; passes 3 (3xTF32) or 1 (TF32)
-static void run_solve_tc(Device& D, const TcDesc* td, int nbatch, int maxnb, int maxncol, const float* P, float* B,
-                         int passes = 3) {
+// forward + backward tensor-core sweep; passes 3 (3xTF32) or 1 (TF32); with
+// acc the backward sweep also adds its result into each system's oAcc block
+template <int PASSES, bool ACC>
+static void sweep_pair(Device& D, dim3 grid, const TcDesc* td, const float* P, float* B) {
   static bool attr = false;
   const size_t smem = tc_smem_bytes();
-  if (!attr) {
-    CK(cudaFuncSetAttribute(k_band_sweep_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    CK(cudaFuncSetAttribute(k_band_sweep_tc, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+  if (!attr) {  // both instances launched here need the large shared-memory window
+    CK(cudaFuncSetAttribute(k_band_sweep_tc<PASSES, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_band_sweep_tc<PASSES, false>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    CK(cudaFuncSetAttribute(k_band_sweep_tc<PASSES, ACC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_band_sweep_tc<PASSES, ACC>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
     attr = true;
   }
+  k_band_sweep_tc<PASSES, false><<<grid, SW_THREADS, smem, D.st>>>(td, P, B, 0, D.err);
+  CKL();
+  k_band_sweep_tc<PASSES, ACC><<<grid, SW_THREADS, smem, D.st>>>(td, P, B, 1, D.err);
+  CKL();
+}
+
+static void run_solve_tc(Device& D, const TcDesc* td, int nbatch, int maxnb, int maxncol, const float* P, float* B,
+                         int passes = 3, bool acc = false) {
   (void)maxnb;
   dim3 grid(maxncol / TC_M, nbatch);
-  k_band_sweep_tc<<<grid, TC_THREADS, smem, D.st>>>(td, P, B, 0, passes, D.err);
-  CKL();
-  k_band_sweep_tc<<<grid, TC_THREADS, smem, D.st>>>(td, P, B, 1, passes, D.err);
-  CKL();
+  if (passes == 3) sweep_pair<3, false>(D, grid, td, P, B);
+  else if (acc) sweep_pair<1, true>(D, grid, td, P, B);
+  else sweep_pair<1, false>(D, grid, td, P, B);
 }
 
 template <typename T>
@@ -640,7 +650,7 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
         h2[t].oAcc = rr == 2 ? D.hs[t].oXc + comp : -1;  // D2 is added into D1
       }
       TcDesc* tdr = upload(h2, own, st);
-      run_solve_tc(D, tdr, nsub, D.maxnbo, D.maxNR, ppool, poolT, rr == 1 ? 3 : 1);
+      run_solve_tc(D, tdr, nsub, D.maxnbo, D.maxNR, ppool, poolT, rr == 1 ? 3 : 1, rr == 2);
       D.prof.end(PH_SOLVE_OO, st);
       if (dmax && rr <= 2) {
         k_comp_maxabs<<<dim3(64, nsub), 256, 0, st>>>(D.ds, poolT, rr, dmax + (size_t)rr * nsub);

@@ -154,13 +154,66 @@ __host__ __device__ __forceinline__ long long panel_chunk(long long base, int w,
 // tiles are independent, so no grid-wide synchronisation is needed and the
 // band window of a tile (w+1 block rows x 128 columns) stays in L2 between
 // consecutive block rows.  grid (max column tiles, batch).
+//
+// Warp roles: warps 0-3 (one thread per column of the tile) stage the window
+// chunks (global -> registers -> TF32 split -> canonical shared layout) and
+// move finished block rows from TMEM to global memory; lane 0 of warp 4
+// issues the panel copies (cp.async.bulk) and the MMAs.  Stages are handed
+// over with mbarriers, so the staging warps run ahead of the tensor core.
+// Two TMEM accumulators alternate between block rows; the block row finished
+// last (the only part of a window that depends on the previous step) is
+// placed at the end of the next window, and the previous row's results are
+// written out after the first chunks of the next row are queued.
+//
 // passes = 3: 3xTF32 (FP32-class result); passes = 1: one TF32 product
 // (hi x hi, relative error ~1e-3), for a refinement correction that is
 // itself ~1e-10 of the solution.  With oAcc >= 0 the backward sweep also
 // adds each finished block row into the block at oAcc.
-__global__ void __launch_bounds__(TC_THREADS, 2)
+constexpr int SW_THREADS = TC_THREADS + 32;
+
+struct SweepChunk {
+  int jb;    // block row of B read by this chunk
+  int pq;    // panel chunk index (2 * block position in the panel + half)
+  int half;  // which 32-row half of the block
+  bool dep;  // reads the block row finished by the previous step
+};
+
+// q-th chunk of the window of block row k (the freshest block last)
+__device__ __forceinline__ SweepChunk sweep_chunk(int dir, int nb, int w, int k, int q) {
+  int j0, nblk;
+  if (dir == 0) { j0 = k - min(k, w); nblk = k - j0 + 1; }
+  else { j0 = k; nblk = min(w, nb - 1 - k) + 1; }
+  const int p = q >> 1;
+  SweepChunk c;
+  c.half = q & 1;
+  c.dep = false;
+  if (nblk == 1) {
+    c.jb = k;
+  } else if (p == nblk - 1) {
+    c.jb = dir == 0 ? k - 1 : k + 1;
+    c.dep = true;
+  } else if (dir == 0) {
+    c.jb = p < nblk - 2 ? j0 + p : k;
+  } else {
+    c.jb = p == 0 ? k : k + 1 + p;
+  }
+  c.pq = 2 * (c.jb - j0) + c.half;
+  return c;
+}
+
+__device__ __forceinline__ int sweep_nchunk(int dir, int nb, int w, int k) {
+  return 2 * (dir == 0 ? min(k, w) + 1 : min(w, nb - 1 - k) + 1);
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+template <int PASSES, bool ACC>
+__global__ void __launch_bounds__(SW_THREADS, 2)
     k_band_sweep_tc(const TcDesc* __restrict__ td, const float* __restrict__ ppool, float* __restrict__ bpool,
-                    int dir, int passes, int* __restrict__ err) {
+                    int dir, int* __restrict__ err) {
+  constexpr int passes = PASSES;
   const TcDesc d = td[blockIdx.y];
   const int c0 = blockIdx.x * TC_M;
   if (c0 >= d.ncol || d.nb == 0) return;
@@ -169,31 +222,26 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
   const float* P = ppool + (dir == 0 ? d.oPf : d.oPb);
   const uint32_t pbytes = (passes == 1 ? TC_PCHUNK / 2 : TC_PCHUNK) * 4;  // hi half first in a chunk
 
-  extern __shared__ __align__(1024) unsigned char smraw[];
-  float* sA = reinterpret_cast<float*>(smraw);                  // [stage][hi|lo][TC_ACHUNK]
+  extern __shared__ __align__(128) unsigned char sw_smem[];
+  float* sA = reinterpret_cast<float*>(sw_smem);                // [stage][hi|lo][TC_ACHUNK]
   float* sP = sA + TC_STAGES * 2 * TC_ACHUNK;                    // [stage][TC_PCHUNK]
-  __shared__ __align__(8) uint64_t bar_p[TC_STAGES], bar_mma[TC_STAGES];
+  __shared__ __align__(8) uint64_t bar_a[TC_STAGES], bar_p[TC_STAGES], bar_mma[TC_STAGES], bar_acc[2], bar_tfree[2];
   __shared__ uint32_t tmem_base;
-  __shared__ int abort_flag;
+  __shared__ volatile int abort_flag;
   __shared__ long long last_commit, tma_pending[TC_STAGES];
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  // sweep order: step s handles block row k(s); its window is nblk(s) blocks from j0(s)
   auto row_of = [&](int sidx) { return dir == 0 ? sidx : d.nb - 1 - sidx; };
-  auto window = [&](int k, int& j0, int& nblk) {
-    if (dir == 0) { j0 = k - min(k, d.w); nblk = k - j0 + 1; }
-    else { j0 = k; nblk = min(d.w, d.nb - 1 - k) + 1; }
-  };
-  auto issue_panel = [&](int st, int k, int q, long long gg) {  // thread 0
-    mbar_expect_tx(&bar_p[st], pbytes);
-    bulk_g2s(sP + st * TC_PCHUNK, P + panel_chunk(0, d.w, k, q), pbytes, &bar_p[st]);
-    tma_pending[st] = gg;
-  };
   if (tid == 0) {
     for (int s = 0; s < TC_STAGES; ++s) {
+      mbar_init(&bar_a[s], TC_THREADS);
       mbar_init(&bar_p[s], 1);
       mbar_init(&bar_mma[s], 1);
       tma_pending[s] = -1;
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&bar_acc[b], 1);
+      mbar_init(&bar_tfree[b], TC_THREADS);
     }
     abort_flag = 0;
     last_commit = -1;
@@ -201,69 +249,150 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
-                 "r"(TC_N));
+                 "r"(2 * TC_N));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = tmem_base;
-  constexpr uint32_t idesc = tc_idesc(TC_M, TC_N);
 
-  // the window rows of the first chunk, and its panel chunk
-  float vn[TC_KC];
-  {
-    int j0, nblk;
-    window(row_of(0), j0, nblk);
-    const float* src = B + (long long)(j0 * NB) * ld + c0 + tid;
+  if (warp == TC_THREADS / 32) {
+    // ------------------------------------------------ issuer (one thread)
+    if (lane == 0) {
+      constexpr uint32_t idesc = tc_idesc(TC_M, TC_N);
+      auto issue_panel = [&](int st, int k, int pq, long long gg) {
+        mbar_expect_tx(&bar_p[st], pbytes);
+        bulk_g2s(sP + st * TC_PCHUNK, P + panel_chunk(0, d.w, k, pq), pbytes, &bar_p[st]);
+        tma_pending[st] = gg;
+      };
+      issue_panel(0, row_of(0), sweep_chunk(dir, d.nb, d.w, row_of(0), 0).pq, 0);
+      long long g = 0;
+      for (int sidx = 0; sidx < d.nb && !abort_flag; ++sidx) {
+        const int k = row_of(sidx), b = sidx & 1;
+        const int nchunk = sweep_nchunk(dir, d.nb, d.w, k);
+        const uint32_t dacc = tmem + (uint32_t)(b * TC_N);
+        if (sidx >= 2 && !mbar_wait(&bar_tfree[b], (uint32_t)(((sidx - 2) >> 1) & 1))) { abort_flag = 1; break; }
+        for (int q = 0; q < nchunk; ++q, ++g) {
+          const int st = (int)(g % TC_STAGES);
+          const uint32_t ph = (uint32_t)((g / TC_STAGES) & 1);
+          if (!mbar_wait(&bar_a[st], ph) || !mbar_wait(&bar_p[st], ph)) { abort_flag = 1; break; }
+          tma_pending[st] = -1;
+          tc_fence_after();
+          const uint32_t a_hi = smem_u32(sA + (st * 2 + 0) * TC_ACHUNK);
+          const uint32_t a_lo = smem_u32(sA + (st * 2 + 1) * TC_ACHUNK);
+          const uint32_t p_hi = smem_u32(sP + st * TC_PCHUNK);
+          const uint32_t p_lo = p_hi + TC_N * TC_KC * 4;
+          if (passes == 1) {
 #pragma unroll
-    for (int t = 0; t < TC_KC; ++t) vn[t] = src[(long long)t * ld];
-    if (tid == 0) issue_panel(0, row_of(0), 0, 0);
-  }
-  bool pending_load = false;  // the next row's first chunk waits for this row's results
-  long long g = 0;            // chunk counter over the whole sweep (stage = g & 1)
-  for (int sidx = 0; sidx < d.nb; ++sidx) {
-    const int k = row_of(sidx);
-    int j0, nblk;
-    window(k, j0, nblk);
-    const int nchunk = nblk * (NB / TC_KC);
-    const float* src0 = B + (long long)(j0 * NB) * ld + c0 + tid;
-    if (pending_load) {
+            for (int kk = 0; kk < TC_KC / 8; ++kk) {
+              const uint32_t koff = kk * 2 * TC_LBO;
+              mma_tf32(dacc, tc_desc(a_hi + koff), tc_desc(p_hi + koff), idesc, (q > 0 || kk > 0) ? 1u : 0u);
+            }
+          } else {
 #pragma unroll
-      for (int t = 0; t < TC_KC; ++t) vn[t] = src0[(long long)t * ld];
-      pending_load = false;
-    }
-    // the chunk after the last one of this row: first chunk of the next row
-    int nk = -1, nj0 = 0;
-    if (sidx + 1 < d.nb) {
-      int nnblk;
-      nk = row_of(sidx + 1);
-      window(nk, nj0, nnblk);
-    }
-    for (int q = 0; q < nchunk; ++q, ++g) {
-      const int st = (int)(g & 1);
-      float v[TC_KC];
-#pragma unroll
-      for (int t = 0; t < TC_KC; ++t) v[t] = vn[t];
-      if (q + 1 < nchunk) {  // prefetch the next chunk of the window
-        const float* src = src0 + (long long)((q + 1) * TC_KC) * ld;
-#pragma unroll
-        for (int t = 0; t < TC_KC; ++t) vn[t] = src[(long long)t * ld];
-      } else if (nk >= 0) {
-        if (nj0 != k) {  // rows already final: fetch them now
-          const float* src = B + (long long)(nj0 * NB) * ld + c0 + tid;
-#pragma unroll
-          for (int t = 0; t < TC_KC; ++t) vn[t] = src[(long long)t * ld];
-        } else {
-          pending_load = true;
+            for (int kk = 0; kk < TC_KC / 8; ++kk) {
+              const uint32_t koff = kk * 2 * TC_LBO;
+              const uint32_t acc = (q > 0 || kk > 0) ? 1u : 0u;
+              mma_tf32(dacc, tc_desc(a_lo + koff), tc_desc(p_hi + koff), idesc, acc);
+              mma_tf32(dacc, tc_desc(a_hi + koff), tc_desc(p_lo + koff), idesc, 1u);
+              mma_tf32(dacc, tc_desc(a_hi + koff), tc_desc(p_hi + koff), idesc, 1u);
+            }
+          }
+          mma_commit(&bar_mma[st]);
+          if (q == nchunk - 1) mma_commit(&bar_acc[b]);
+          last_commit = g;
+          // panel of the next chunk, once the stage it goes to is free
+          int nk = k, nq = q + 1;
+          if (nq == nchunk) { nk = sidx + 1 < d.nb ? row_of(sidx + 1) : -1; nq = 0; }
+          if (nk >= 0) {
+            const long long gn = g + 1;
+            const int st2 = (int)(gn % TC_STAGES);
+            if (gn >= TC_STAGES &&
+                !mbar_wait(&bar_mma[st2], (uint32_t)(((gn - TC_STAGES) / TC_STAGES) & 1))) { abort_flag = 1; break; }
+            issue_panel(st2, nk, sweep_chunk(dir, d.nb, d.w, nk, nq).pq, gn);
+          }
         }
       }
-      if (g >= TC_STAGES) {
-        if (!mbar_wait(&bar_mma[st], (uint32_t)(((g - TC_STAGES) >> 1) & 1))) { if (tid == 0) abort_flag = 1; }
+    }
+  } else {
+    // ------------------------------------------------ staging + epilogue (128 threads)
+    const uint32_t trow = (uint32_t)(warp * 32) << 16;
+    auto load_chunk = [&](int jb, int half, float (&r)[TC_KC]) {
+      const float* src = B + (long long)(jb * NB + half * TC_KC) * ld + c0 + tid;
+#pragma unroll
+      for (int t = 0; t < TC_KC; ++t) r[t] = src[(long long)t * ld];
+    };
+    // move block row `sr` from its TMEM buffer to global memory
+    auto epilogue = [&](int sr) -> bool {
+      const int k = row_of(sr), b = sr & 1;
+      // the row stride is made opaque so that the 64 row offsets are formed
+      // here rather than kept live in registers across the sweep
+      long long lds = ld;
+      asm volatile("" : "+l"(lds));
+      float* dst = B + (long long)(k * NB) * lds + c0 + tid;
+      float* dst2 = (ACC && dir == 1 && d.oAcc >= 0) ? bpool + d.oAcc + (long long)(k * NB) * lds + c0 + tid : nullptr;
+      if (!mbar_wait(&bar_acc[b], (uint32_t)((sr >> 1) & 1))) { abort_flag = 1; return false; }
+      tc_fence_after();
+#pragma unroll
+      for (int part = 0; part < TC_N / 16; ++part) {
+        float vv[16];
+        tmem_ld16(tmem + trow + (uint32_t)(b * TC_N + part * 16), vv);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) dst[(long long)(part * 16 + i) * lds] = vv[i];
+        if (ACC && dst2) {
+          float a[16];
+#pragma unroll
+          for (int i = 0; i < 16; ++i) a[i] = dst2[(long long)(part * 16 + i) * lds];
+#pragma unroll
+          for (int i = 0; i < 16; ++i) dst2[(long long)(part * 16 + i) * lds] = a[i] + vv[i];
+        }
       }
-      __syncthreads();
-      if (abort_flag) break;
-      {
+      tc_fence_before();
+      mbar_arrive(&bar_tfree[b]);
+      return true;
+    };
+    float vn[TC_KC];
+    bool have_next = true;
+    {
+      const SweepChunk c = sweep_chunk(dir, d.nb, d.w, row_of(0), 0);
+      load_chunk(c.jb, c.half, vn);
+    }
+    int epi_done = -1;  // last block row written to global memory
+    long long g = 0;
+    bool ok = true;
+    for (int sidx = 0; sidx < d.nb && ok; ++sidx) {
+      const int k = row_of(sidx);
+      const int nchunk = sweep_nchunk(dir, d.nb, d.w, k);
+      for (int q = 0; q < nchunk; ++q, ++g) {
+        if (abort_flag) { ok = false; break; }
+        // the previous row's results go out once two chunks of this row are queued
+        // (and always before a chunk that reads them)
+        const SweepChunk c = sweep_chunk(dir, d.nb, d.w, k, q);
+        if (sidx > 0 && epi_done < sidx - 1 && (q == 2 || c.dep)) {
+          if (!epilogue(sidx - 1)) { ok = false; break; }
+          epi_done = sidx - 1;
+        }
+        if (!have_next) load_chunk(c.jb, c.half, vn);
+        float v[TC_KC];
+#pragma unroll
+        for (int t = 0; t < TC_KC; ++t) v[t] = vn[t];
+        // prefetch the next chunk unless it reads rows not yet written
+        {
+          int nk = k, nq = q + 1, ns = sidx;
+          if (nq == nchunk) { ns = sidx + 1; nk = ns < d.nb ? row_of(ns) : -1; nq = 0; }
+          have_next = false;
+          if (nk >= 0) {
+            const SweepChunk cn = sweep_chunk(dir, d.nb, d.w, nk, nq);
+            if (!cn.dep || epi_done >= ns - 1) {
+              load_chunk(cn.jb, cn.half, vn);
+              have_next = true;
+            }
+          }
+        }
+        const int st = (int)(g % TC_STAGES);
+        if (g >= TC_STAGES &&
+            !mbar_wait(&bar_mma[st], (uint32_t)(((g - TC_STAGES) / TC_STAGES) & 1))) { abort_flag = 1; ok = false; break; }
         float* ahi = sA + (st * 2 + 0) * TC_ACHUNK;
         float* alo = sA + (st * 2 + 1) * TC_ACHUNK;
         if (passes == 1) {
@@ -280,101 +409,35 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
             h.y = tf32_rna(v[4 * t4 + 1]); l.y = v[4 * t4 + 1] - h.y;
             h.z = tf32_rna(v[4 * t4 + 2]); l.z = v[4 * t4 + 2] - h.z;
             h.w = tf32_rna(v[4 * t4 + 3]); l.w = v[4 * t4 + 3] - h.w;
-            int off = canon_off(tid, 4 * t4);
+            const int off = canon_off(tid, 4 * t4);
             *reinterpret_cast<float4*>(ahi + off) = h;
             *reinterpret_cast<float4*>(alo + off) = l;
           }
         }
+        fence_async_smem();
+        mbar_arrive(&bar_a[st]);
       }
-      fence_async_smem();
-      tc_fence_before();
-      __syncthreads();
-      if (tid == 0) {
-        tc_fence_after();
-        if (!mbar_wait(&bar_p[st], (uint32_t)((g >> 1) & 1))) {
-          abort_flag = 1;
-        } else {
-          tma_pending[st] = -1;
-          const uint32_t a_hi = smem_u32(sA + (st * 2 + 0) * TC_ACHUNK);
-          const uint32_t a_lo = smem_u32(sA + (st * 2 + 1) * TC_ACHUNK);
-          const uint32_t p_hi = smem_u32(sP + st * TC_PCHUNK);
-          const uint32_t p_lo = p_hi + TC_N * TC_KC * 4;
-          if (passes == 1) {
-#pragma unroll
-            for (int kk = 0; kk < TC_KC / 8; ++kk) {
-              const uint32_t koff = kk * 2 * TC_LBO;
-              mma_tf32(tmem, tc_desc(a_hi + koff), tc_desc(p_hi + koff), idesc, (q > 0 || kk > 0) ? 1u : 0u);
-            }
-          } else {
-#pragma unroll
-            for (int kk = 0; kk < TC_KC / 8; ++kk) {
-              const uint32_t koff = kk * 2 * TC_LBO;
-              uint32_t acc = (q > 0 || kk > 0) ? 1u : 0u;
-              mma_tf32(tmem, tc_desc(a_lo + koff), tc_desc(p_hi + koff), idesc, acc);
-              mma_tf32(tmem, tc_desc(a_hi + koff), tc_desc(p_lo + koff), idesc, 1u);
-              mma_tf32(tmem, tc_desc(a_hi + koff), tc_desc(p_hi + koff), idesc, 1u);
-            }
-          }
-          mma_commit(&bar_mma[st]);
-          last_commit = g;
-          // panel of the next chunk into the other stage, once the MMAs of
-          // chunk g-1 (which read that stage) are done
-          const int pk = q + 1 < nchunk ? k : nk;
-          const int pq = q + 1 < nchunk ? q + 1 : 0;
-          if (pk >= 0) {
-            if (g >= 1 && !mbar_wait(&bar_mma[st ^ 1], (uint32_t)(((g - 1) >> 1) & 1))) abort_flag = 1;
-            else issue_panel(st ^ 1, pk, pq, g + 1);
-          }
-        }
+      // a row with fewer than three chunks and no dependent chunk
+      if (ok && sidx > 0 && epi_done < sidx - 1) {
+        if (!epilogue(sidx - 1)) ok = false;
+        else epi_done = sidx - 1;
       }
     }
-    // block row k done: wait for its MMAs, move the accumulator to global memory
-    // (the rows of an accumulation target are fetched before the wait)
-    float* dst2 = (dir == 1 && d.oAcc >= 0) ? bpool + d.oAcc + (long long)(k * NB) * ld + c0 + warp * 32 + lane
-                                            : nullptr;
-    float accin[TC_N];
-    if (dst2) {
-#pragma unroll
-      for (int i = 0; i < TC_N; ++i) accin[i] = dst2[(long long)i * ld];
-    }
-    __syncthreads();
-    if (tid == 0 && !abort_flag) {
-      long long ql = last_commit;
-      if (ql != g - 1 || !mbar_wait(&bar_mma[ql & 1], (uint32_t)((ql >> 1) & 1))) abort_flag = 1;
-    }
-    __syncthreads();
-    if (abort_flag) break;
-    tc_fence_after();
-    {
-      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
-      float* dst = B + (long long)(k * NB) * ld + c0 + warp * 32 + lane;
-#pragma unroll
-      for (int part = 0; part < TC_N / 16; ++part) {
-        float vv[16];
-        tmem_ld16(taddr + part * 16, vv);
-#pragma unroll
-        for (int i = 0; i < 16; ++i) dst[(long long)(part * 16 + i) * ld] = vv[i];
-        if (dst2) {
-#pragma unroll
-          for (int i = 0; i < 16; ++i) dst2[(long long)(part * 16 + i) * ld] = accin[part * 16 + i] + vv[i];
-        }
-      }
-    }
-    tc_fence_before();
-    __syncthreads();  // the next block row reads these rows
+    if (ok && epi_done < d.nb - 1) epilogue(d.nb - 1);
   }
-  // after an abort: wait (bounded) for work still in flight before freeing TMEM
+  // wind-down: after an abort, wait (bounded) for work still in flight before freeing TMEM
+  __syncthreads();
   if (tid == 0 && abort_flag) {
-    long long ql = last_commit;
-    if (ql >= 0) mbar_wait(&bar_mma[ql & 1], (uint32_t)((ql >> 1) & 1));
+    const long long ql = last_commit;
+    if (ql >= 0) mbar_wait(&bar_mma[ql % TC_STAGES], (uint32_t)((ql / TC_STAGES) & 1));
     for (int s2 = 0; s2 < TC_STAGES; ++s2)
-      if (tma_pending[s2] >= 0) mbar_wait(&bar_p[s2], (uint32_t)((tma_pending[s2] >> 1) & 1));
+      if (tma_pending[s2] >= 0) mbar_wait(&bar_p[s2], (uint32_t)((tma_pending[s2] / TC_STAGES) & 1));
     atomicOr(err, DE_TIMEOUT);
   }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_N));
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * TC_N));
 }
 
 constexpr size_t tc_smem_bytes() { return (size_t)TC_STAGES * (2 * TC_ACHUNK + TC_PCHUNK) * sizeof(float); }
