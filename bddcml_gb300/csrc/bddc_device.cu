@@ -716,7 +716,7 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
     vector<TcDesc> hts(nsub);
     for (int t = 0; t < nsub; ++t) {
       auto& d = D.hs[t];
-      hts[t] = TcDesc{d.nbi, d.nbi - 1, d.NRC, 0, d.oBs, poff[t][2], poff[t][3], -1};
+      hts[t] = TcDesc{d.nbi, d.nbi - 1, d.NRC, d.NI, d.oBs, poff[t][2], poff[t][3], -1};  // [I | C^T]
     }
     td_s = upload(hts, own, st);
     run_panels(D, bd_s, td_s, nsub, maxnbi, maxnbi - 1, poolT, ppool);
@@ -796,7 +796,7 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
     run_factor<T>(D, dcb, 1, nbc, nbc - 1, cpool);
     if constexpr (std::is_same_v<T, float>) {
       // identity right-hand side needs a column count that is a multiple of the MMA tile
-      vector<TcDesc> htc{TcDesc{nbc, nbc - 1, D.ldc, 0, cb.oB, 0, (long long)nbc * nbc * 2 * TC_PCHUNK, -1}};
+      vector<TcDesc> htc{TcDesc{nbc, nbc - 1, D.ldc, D.ldc, cb.oB, 0, (long long)nbc * nbc * 2 * TC_PCHUNK, -1}};
       TcDesc* tdc = upload(htc, own, st);
       float* cpan = dalloc<float>((size_t)2 * nbc * nbc * 2 * TC_PCHUNK, own);
       run_panels(D, dcb, tdc, 1, nbc, nbc - 1, cpool, cpan);

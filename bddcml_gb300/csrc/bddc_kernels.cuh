@@ -34,6 +34,17 @@ __host__ __device__ inline long long band_block(const BandDesc& d, int i, int j)
   return d.oL + ((long long)i * (d.w + 1) + (j - i + d.w)) * (NB * NB);
 }
 
+// four consecutive elements from 16-byte aligned shared memory
+__device__ __forceinline__ void load4(float (&v)[4], const float* p) {
+  const float4 t = *reinterpret_cast<const float4*>(p);
+  v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+}
+__device__ __forceinline__ void load4(double (&v)[4], const double* p) {
+  const double2 t0 = *reinterpret_cast<const double2*>(p);
+  const double2 t1 = *reinterpret_cast<const double2*>(p + 2);
+  v[0] = t0.x; v[1] = t0.y; v[2] = t1.x; v[3] = t1.y;
+}
+
 // --------------------------------------------------------------- SIMT tile
 // acc(4x4 per thread) += op(A) * op(B) over K (multiple of KC), 64 x 64 output.
 // A: !TA -> A[r*lda + k], TA -> A[k*lda + r];  B: !TB -> B[k*ldb + c], TB -> B[c*ldb + k]
@@ -58,8 +69,8 @@ __device__ __forceinline__ void tile_gemm(T (&acc)[4][4], const T* __restrict__ 
 #pragma unroll
     for (int k = 0; k < KC; ++k) {
       T a[4], b[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) { a[q] = smA[k * NB + ty * 4 + q]; b[q] = smB[k * NB + tx * 4 + q]; }
+      load4(a, smA + k * NB + ty * 4);  // vector shared-memory loads
+      load4(b, smB + k * NB + tx * 4);
 #pragma unroll
       for (int q = 0; q < 4; ++q)
 #pragma unroll

@@ -34,17 +34,13 @@ struct DevSub {
 };
 
 // ------------------------------------------------------------ band factor
-// dynamic smem: a[NB][NB+1], inv[NB][NB+1], smA[KC*NB], smB[KC*NB]
+// Left-looking block Cholesky of a block-band matrix, step k:
+//   diagonal: L_kk = chol(A_kk - sum_j L_kj L_kj^T), Linv_kk = L_kk^-1
+//   below:    L_ik = (A_ik - sum_{j<k} L_ij L_kj^T) Linv_kk^T,  k < i <= k + w
+// Shared memory of the diagonal step: a[NB][NB+1], inv[NB][NB+1], smA, smB.
 template <typename T>
-__global__ void __launch_bounds__(NT) k_chol_diag(const BandDesc* __restrict__ bd, T* __restrict__ pool, int k,
-                                                  int* __restrict__ err) {
-  const BandDesc d = bd[blockIdx.x];
-  if (k >= d.nb) return;
-  extern __shared__ __align__(16) unsigned char smraw[];
-  T* a = reinterpret_cast<T*>(smraw);          // NB x (NB+1)
-  T* inv = a + NB * (NB + 1);                  // NB x (NB+1)
-  T* smA = inv + NB * (NB + 1);
-  T* smB = smA + KC * NB;
+__device__ void chol_diag_step(const BandDesc& d, T* __restrict__ pool, int k, int* __restrict__ err, T* a, T* inv,
+                               T* smA, T* smB) {
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   T acc[4][4];
   tile_zero(acc);
@@ -103,12 +99,7 @@ __global__ void __launch_bounds__(NT) k_chol_diag(const BandDesc* __restrict__ b
 }
 
 template <typename T>
-__global__ void __launch_bounds__(NT) k_chol_off(const BandDesc* __restrict__ bd, T* __restrict__ pool, int k) {
-  const BandDesc d = bd[blockIdx.y];
-  const int i = k + 1 + blockIdx.x;
-  if (k >= d.nb || i >= d.nb || i - k > d.w) return;
-  __shared__ __align__(16) T smA[KC * NB];
-  __shared__ __align__(16) T smB[KC * NB];
+__device__ void chol_off_step(const BandDesc& d, T* __restrict__ pool, int k, int i, T* smA, T* smB) {
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   T acc[4][4];
   tile_zero(acc);
@@ -126,6 +117,30 @@ __global__ void __launch_bounds__(NT) k_chol_off(const BandDesc* __restrict__ bd
   for (int q = 0; q < 4; ++q)
 #pragma unroll
     for (int p = 0; p < 4; ++p) Aik[(ty * 4 + q) * NB + tx * 4 + p] = acc[q][p];
+  __syncthreads();
+}
+
+// one step for every system (one CTA per system)
+template <typename T>
+__global__ void __launch_bounds__(NT) k_chol_diag(const BandDesc* __restrict__ bd, T* __restrict__ pool, int k,
+                                                  int* __restrict__ err) {
+  const BandDesc d = bd[blockIdx.x];
+  if (k >= d.nb) return;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T* a = reinterpret_cast<T*>(smraw);
+  T* inv = a + NB * (NB + 1);
+  T* smA = inv + NB * (NB + 1);
+  chol_diag_step<T>(d, pool, k, err, a, inv, smA, smA + KC * NB);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(NT) k_chol_off(const BandDesc* __restrict__ bd, T* __restrict__ pool, int k) {
+  const BandDesc d = bd[blockIdx.y];
+  const int i = k + 1 + blockIdx.x;
+  if (k >= d.nb || i >= d.nb || i - k > d.w) return;
+  __shared__ __align__(16) T smA[KC * NB];
+  __shared__ __align__(16) T smB[KC * NB];
+  chol_off_step<T>(d, pool, k, i, smA, smB);
 }
 
 // forward step k: B_k = Linv_kk (B_k - sum_j L_kj B_j), one 64-column tile per CTA

@@ -137,7 +137,8 @@ __device__ __forceinline__ float tf32_rna(float x) {
 }
 
 struct TcDesc {
-  int nb, w, ncol, pad;
+  int nb, w, ncol;
+  int pad;           // leading identity columns of B (forward sweeps skip the zero rows above them)
   long long oB;      // RHS block (row-major, ld = ncol) in the work pool
   long long oPf;     // forward panels in the panel pool
   long long oPb;     // backward panels
@@ -231,7 +232,11 @@ __global__ void __launch_bounds__(SW_THREADS, 2)
   __shared__ long long last_commit, tma_pending[TC_STAGES];
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  auto row_of = [&](int sidx) { return dir == 0 ? sidx : d.nb - 1 - sidx; };
+  // a forward sweep of a tile inside the identity columns (pad = their
+  // count) starts at the tile's diagonal block row: the rows above stay zero
+  const int s0 = (dir == 0 && c0 + TC_M <= d.pad) ? c0 / NB : 0;
+  const int nsteps = d.nb - s0;
+  auto row_of = [&](int sidx) { return dir == 0 ? s0 + sidx : d.nb - 1 - sidx; };
   if (tid == 0) {
     for (int s = 0; s < TC_STAGES; ++s) {
       mbar_init(&bar_a[s], TC_THREADS);
@@ -268,7 +273,7 @@ __global__ void __launch_bounds__(SW_THREADS, 2)
       };
       issue_panel(0, row_of(0), sweep_chunk(dir, d.nb, d.w, row_of(0), 0).pq, 0);
       long long g = 0;
-      for (int sidx = 0; sidx < d.nb && !abort_flag; ++sidx) {
+      for (int sidx = 0; sidx < nsteps && !abort_flag; ++sidx) {
         const int k = row_of(sidx), b = sidx & 1;
         const int nchunk = sweep_nchunk(dir, d.nb, d.w, k);
         const uint32_t dacc = tmem + (uint32_t)(b * TC_N);
@@ -304,7 +309,7 @@ __global__ void __launch_bounds__(SW_THREADS, 2)
           last_commit = g;
           // panel of the next chunk, once the stage it goes to is free
           int nk = k, nq = q + 1;
-          if (nq == nchunk) { nk = sidx + 1 < d.nb ? row_of(sidx + 1) : -1; nq = 0; }
+          if (nq == nchunk) { nk = sidx + 1 < nsteps ? row_of(sidx + 1) : -1; nq = 0; }
           if (nk >= 0) {
             const long long gn = g + 1;
             const int st2 = (int)(gn % TC_STAGES);
@@ -361,7 +366,7 @@ __global__ void __launch_bounds__(SW_THREADS, 2)
     int epi_done = -1;  // last block row written to global memory
     long long g = 0;
     bool ok = true;
-    for (int sidx = 0; sidx < d.nb && ok; ++sidx) {
+    for (int sidx = 0; sidx < nsteps && ok; ++sidx) {
       const int k = row_of(sidx);
       const int nchunk = sweep_nchunk(dir, d.nb, d.w, k);
       for (int q = 0; q < nchunk; ++q, ++g) {
@@ -380,7 +385,7 @@ __global__ void __launch_bounds__(SW_THREADS, 2)
         // prefetch the next chunk unless it reads rows not yet written
         {
           int nk = k, nq = q + 1, ns = sidx;
-          if (nq == nchunk) { ns = sidx + 1; nk = ns < d.nb ? row_of(ns) : -1; nq = 0; }
+          if (nq == nchunk) { ns = sidx + 1; nk = ns < nsteps ? row_of(ns) : -1; nq = 0; }
           have_next = false;
           if (nk >= 0) {
             const SweepChunk cn = sweep_chunk(dir, d.nb, d.w, nk, nq);
@@ -423,7 +428,7 @@ __global__ void __launch_bounds__(SW_THREADS, 2)
         else epi_done = sidx - 1;
       }
     }
-    if (ok && epi_done < d.nb - 1) epilogue(d.nb - 1);
+    if (ok && epi_done < nsteps - 1) epilogue(nsteps - 1);
   }
   // wind-down: after an abort, wait (bounded) for work still in flight before freeing TMEM
   __syncthreads();
