@@ -38,7 +38,8 @@ EXPORTS = ["bddcml_init_c", "bddcml_upload_global_data_c", "bddcml_upload_subdom
            "bddcml_setup_new_data_c", "bddcml_dotprod_subdomain_c", "bddcml_finalize_c",
            "bddcml_get_last_error_c", "bddcml_set_precision_c", "bddcml_get_stats_c",
            "bddcml_get_residual_history_c", "bddcml_get_interface_weights_c", "bddcml_get_coarse_info_c",
-           "bddcml_set_profiling_c", "bddcml_get_profile_c", "bddcml_release_device_memory_c"]
+           "bddcml_set_profiling_c", "bddcml_get_profile_c", "bddcml_release_device_memory_c",
+           "bddcml_dotprod_subdomain_dev_c"]
 
 # phases of bddcml_get_profile_c (CUDA events on the solver stream)
 PHASES = ["numeric_total", "solve_total", "factor_interior", "solve_interior", "refine_residual", "schur",
@@ -224,6 +225,16 @@ def get_interface_weights(isub: int, ndofi: int) -> np.ndarray:
     lib().bddcml_get_interface_weights_c(_i(isub), out.ctypes.data_as(C.POINTER(C.c_double)), _i(ndofi))
     _check()
     return out
+
+
+def dotprod_subdomain_dev(isub: int, vec1_ptr: int, vec2_ptr: int, lvec: int) -> float:
+    """Weighted subdomain dot product of two device-resident vectors (raw
+    device addresses, float64, length lvec); allocates nothing."""
+    out = C.c_double()
+    lib().bddcml_dotprod_subdomain_dev_c(_i(isub), C.c_void_p(vec1_ptr), C.c_void_p(vec2_ptr), _i(lvec),
+                                         C.byref(out))
+    _check()
+    return out.value
 
 
 def release_device_memory():

@@ -321,6 +321,19 @@ void bddcml_finalize_c(void) {
   });
 }
 
+void bddcml_dotprod_subdomain_dev_c(int* isub, const double* vec1, const double* vec2, int* lvec, double* dotprod) {
+  guarded("bddcml_dotprod_subdomain_dev_c", [&] {
+    Solver* S = need_solver("bddcml_dotprod_subdomain_dev_c");
+    if (!S) return;
+    int t = sub_index(*S, *isub);
+    Subdomain& s = S->subs[t];
+    if (s.wi.empty() && s.ndofi > 0) throw Error{ERR_ARGUMENT, "weights are not ready"};
+    if (*lvec != s.ndof) throw Error{ERR_ARGUMENT, "dimension mismatch"};
+    Error err{BDDCML_OK, ""};
+    if (!device_dotprod_noalloc(s.iivsvn.data(), s.wi.data(), s.ndofi, vec1, vec2, s.ndof, dotprod, err)) throw err;
+  });
+}
+
 void bddcml_release_device_memory_c(void) {
   guarded("bddcml_release_device_memory_c", [&] {
     Error err{BDDCML_OK, ""};

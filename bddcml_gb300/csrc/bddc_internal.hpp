@@ -159,6 +159,10 @@ void host_prepare_blocks(Subdomain& s, SubBlocks& b);
 // device (bddc_device.cu)
 Device* device_create(Error& err);
 bool device_release_memory(Error& err);
+// largest subdomain interface the allocation-free dot product's fixed scratch holds
+constexpr int NOALLOC_MAX_IFACE = 65536;
+bool device_dotprod_noalloc(const int* iface_dofs, const double* weights, int nif, const double* v1,
+                            const double* v2, int ndof, double* out, Error& err);
 void device_destroy(Device* d);
 bool device_setup(Solver& S, Error& err);
 bool device_solve(Solver& S, double tol, int maxit, int ndecrmax, int& num_iter, int& reason, double& cond,

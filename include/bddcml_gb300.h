@@ -169,6 +169,29 @@ void bddcml_get_profile_c(double *ms, int *counts, int *lphase);
  * No counterpart in the reference. */
 void bddcml_release_device_memory_c(void);
 
+/* The weighted dot product of bddcml_dotprod_subdomain_c for vectors that
+ * already live in device memory (vec1, vec2: device pointers, length *lvec =
+ * the subdomain's ndof, subdomain dof order); the result is written to the
+ * host double *dotprod.  No counterpart in the reference.
+ *
+ * It allocates nothing, on the device or through any library: its scratch
+ * (the subdomain's interface weights and indices, block partial sums, the
+ * result) is one fixed array in static device memory of about 0.8 MB, which
+ * holds subdomains with at most 65536 interface dofs; a larger interface is
+ * rejected with BDDCML_ERR_ARGUMENT.  It is meant for callers that keep their
+ * vectors on the GPU and may not allocate at that point: an application that
+ * reserves all device memory up front, or one whose own allocator forbids
+ * device allocations (and the implicit device synchronisation of cudaMalloc
+ * and cudaFree) inside its time-stepping loop.
+ *
+ * The first call on each device looks up the scratch address
+ * (cudaGetSymbolAddress), so make one call before any stream capture.  Work
+ * runs on the legacy default stream; the vectors must be ready there.  Calls
+ * must not overlap in time (several host threads, several streams): they share
+ * the scratch and would race.  Needs a finished bddcml_setup_preconditioner_c. */
+void bddcml_dotprod_subdomain_dev_c(int *isub, const double *vec1, const double *vec2, int *lvec,
+                                    double *dotprod);
+
 #ifdef __cplusplus
 }
 #endif
