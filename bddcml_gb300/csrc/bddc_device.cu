@@ -252,7 +252,7 @@ void device_destroy(Device* d) { delete d; }
 // ------------------------------------------------------------ band phases
 template <typename T>
 static void run_factor(Device& D, const BandDesc* bd, int nbatch, int maxnb, int maxw, T* pool) {
-  size_t smem = (2 * NB * (NB + 1) + 2 * KC * NB) * sizeof(T);
+  size_t smem = (2 * NB * (NB + 1) + 2 * SM_TILE) * sizeof(T);
   CK(cudaFuncSetAttribute(k_chol_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   for (int k = 0; k < maxnb; ++k) {
     k_chol_diag<T><<<nbatch, NT, smem, D.st>>>(bd, pool, k, D.err);

@@ -16,6 +16,8 @@ namespace bddc {
 constexpr int NB = 64;      // tile edge
 constexpr int NT = 256;     // threads of the tile kernels (16 x 16, 4 x 4 outputs each)
 constexpr int KC = 16;      // K chunk of the SIMT tile product
+constexpr int KCS = NB + 4;  // row stride of a staged K chunk (spreads the transposing stores over banks)
+constexpr int SM_TILE = KC * KCS;  // elements of one staged operand chunk
 
 // error flags written by kernels (bit field), read by the host after setup
 enum DevErr : int { DE_PIVOT = 1, DE_NAN = 2, DE_SMALL = 4 };
@@ -59,18 +61,18 @@ __device__ __forceinline__ void tile_gemm(T (&acc)[4][4], const T* __restrict__ 
       int r, k;
       if (!TA) { k = e % KC; r = e / KC; } else { r = e % NB; k = e / NB; }
       T v = TA ? A[(long long)(k0 + k) * lda + r] : A[(long long)r * lda + k0 + k];
-      smA[k * NB + r] = v;
+      smA[k * KCS + r] = v;
       int c, kk;
       if (!TB) { c = e % NB; kk = e / NB; } else { kk = e % KC; c = e / KC; }
       T u = TB ? B[(long long)c * ldb + k0 + kk] : B[(long long)(k0 + kk) * ldb + c];
-      smB[kk * NB + c] = u;
+      smB[kk * KCS + c] = u;
     }
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < KC; ++k) {
       T a[4], b[4];
-      load4(a, smA + k * NB + ty * 4);  // vector shared-memory loads
-      load4(b, smB + k * NB + tx * 4);
+      load4(a, smA + k * KCS + ty * 4);  // vector shared-memory loads
+      load4(b, smB + k * KCS + tx * 4);
 #pragma unroll
       for (int q = 0; q < 4; ++q)
 #pragma unroll

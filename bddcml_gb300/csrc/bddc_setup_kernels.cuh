@@ -70,25 +70,31 @@ __device__ void chol_diag_step(const BandDesc& d, T* __restrict__ pool, int k, i
     T dc = a[c * (NB + 1) + c];
     for (int r = c + 1 + tid; r < NB; r += NT) a[r * (NB + 1) + c] /= dc;
     __syncthreads();
-    int m = NB - c - 1;
-    for (int e = tid; e < m * m; e += NT) {
-      int r = c + 1 + e / m, q = c + 1 + e % m;
-      if (q <= r) a[r * (NB + 1) + q] -= a[r * (NB + 1) + c] * a[q * (NB + 1) + c];
+    // trailing update of the lower triangle, 16 x 16 thread grid
+    for (int r = c + 1 + ty; r < NB; r += 16) {
+      const T lr = a[r * (NB + 1) + c];
+      for (int q = c + 1 + tx; q <= r; q += 16) a[r * (NB + 1) + q] -= lr * a[q * (NB + 1) + c];
     }
     __syncthreads();
   }
-  // inverse of the lower triangular factor, one column per thread
-  if (tid < NB) {
-    const int j = tid;
-    for (int i = 0; i < j; ++i) inv[i * (NB + 1) + j] = T(0);
-    inv[j * (NB + 1) + j] = T(1) / a[j * (NB + 1) + j];
-    for (int i = j + 1; i < NB; ++i) {
-      T s = T(0);
-      for (int m = j; m < i; ++m) s += a[i * (NB + 1) + m] * inv[m * (NB + 1) + j];
-      inv[i * (NB + 1) + j] = -s / a[i * (NB + 1) + i];
-    }
+  // inverse of the lower triangular factor by elimination on the identity:
+  // row k of the inverse is final once scaled, then it is eliminated from the
+  // rows below, all (row, column) pairs of a step in parallel
+  for (int e = tid; e < NB * NB; e += NT) {
+    const int r = e / NB, c = e % NB;
+    inv[r * (NB + 1) + c] = r == c ? T(1) : T(0);
   }
   __syncthreads();
+  for (int k = 0; k < NB; ++k) {
+    const T dk = a[k * (NB + 1) + k];
+    for (int j = tid; j <= k; j += NT) inv[k * (NB + 1) + j] /= dk;
+    __syncthreads();
+    for (int i = k + 1 + ty; i < NB; i += 16) {
+      const T lik = a[i * (NB + 1) + k];
+      for (int j = tx; j <= k; j += 16) inv[i * (NB + 1) + j] -= lik * inv[k * (NB + 1) + j];
+    }
+    __syncthreads();
+  }
   T* Lkk = pool + band_block(d, k, k);
   T* Li = pool + d.oLinv + (long long)k * NB * NB;
   for (int e = tid; e < NB * NB; e += NT) {
@@ -130,7 +136,7 @@ __global__ void __launch_bounds__(NT) k_chol_diag(const BandDesc* __restrict__ b
   T* a = reinterpret_cast<T*>(smraw);
   T* inv = a + NB * (NB + 1);
   T* smA = inv + NB * (NB + 1);
-  chol_diag_step<T>(d, pool, k, err, a, inv, smA, smA + KC * NB);
+  chol_diag_step<T>(d, pool, k, err, a, inv, smA, smA + SM_TILE);
 }
 
 template <typename T>
@@ -138,8 +144,8 @@ __global__ void __launch_bounds__(NT) k_chol_off(const BandDesc* __restrict__ bd
   const BandDesc d = bd[blockIdx.y];
   const int i = k + 1 + blockIdx.x;
   if (k >= d.nb || i >= d.nb || i - k > d.w) return;
-  __shared__ __align__(16) T smA[KC * NB];
-  __shared__ __align__(16) T smB[KC * NB];
+  __shared__ __align__(16) T smA[SM_TILE];
+  __shared__ __align__(16) T smB[SM_TILE];
   chol_off_step<T>(d, pool, k, i, smA, smB);
 }
 
@@ -150,8 +156,8 @@ __global__ void __launch_bounds__(NT) k_trsm_fwd(const BandDesc* __restrict__ bd
   const BandDesc d = bd[blockIdx.y];
   const int c0 = blockIdx.x * NB;
   if (k >= d.nb || c0 >= d.ncol) return;
-  __shared__ __align__(16) T smA[KC * NB];
-  __shared__ __align__(16) T smB[KC * NB];
+  __shared__ __align__(16) T smA[SM_TILE];
+  __shared__ __align__(16) T smB[SM_TILE];
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   const int ld = d.ncol;
   T* B = Bpool + d.oB;
@@ -180,8 +186,8 @@ __global__ void __launch_bounds__(NT) k_trsm_bwd(const BandDesc* __restrict__ bd
   const BandDesc d = bd[blockIdx.y];
   const int c0 = blockIdx.x * NB;
   if (k >= d.nb || c0 >= d.ncol) return;
-  __shared__ __align__(16) T smA[KC * NB];
-  __shared__ __align__(16) T smB[KC * NB];
+  __shared__ __align__(16) T smA[SM_TILE];
+  __shared__ __align__(16) T smB[SM_TILE];
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   const int ld = d.ncol;
   T* B = Bpool + d.oB;

@@ -458,8 +458,8 @@ __global__ void __launch_bounds__(NT) k_make_panels(const BandDesc* __restrict__
   const TcDesc t = td[blockIdx.z];
   const int k = blockIdx.y, jj = blockIdx.x;
   if (k >= d.nb) return;
-  __shared__ __align__(16) float smA[KC * NB];
-  __shared__ __align__(16) float smB[KC * NB];
+  __shared__ __align__(16) float smA[SM_TILE];
+  __shared__ __align__(16) float smB[SM_TILE];
   __shared__ float tile[NB][NB + 1];
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   const float* Li = lpool + d.oLinv + (long long)k * NB * NB;
