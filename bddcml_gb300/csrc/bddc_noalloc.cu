@@ -32,7 +32,15 @@ constexpr size_t OFF_RESULT = OFF_PART + sizeof(double) * NOALLOC_BLOCKS;
 constexpr size_t OFF_TICKET = OFF_RESULT + sizeof(double);
 constexpr size_t SCRATCH_BYTES = OFF_TICKET + 256;
 
-__device__ __align__(256) unsigned char g_dot_scratch[SCRATCH_BYTES];  // zero-initialised at load
+}  // namespace
+
+// The scratch itself: every GPU that loads the library holds this array
+// (about 0.8 MB) until the process exits.  Zero-initialised at load.  Host
+// code must not pass its name to a kernel (on the host it names a stand-in,
+// not device memory); the device address comes from cudaGetSymbolAddress.
+static __device__ __align__(256) unsigned char g_dot_scratch[SCRATCH_BYTES];
+
+namespace {
 
 constexpr int MAX_DEVICES = 64;
 unsigned char* g_scratch_ptr[MAX_DEVICES] = {};  // device address of g_dot_scratch, per device

@@ -177,8 +177,10 @@ void bddcml_release_device_memory_c(void);
  * It allocates nothing, on the device or through any library: its scratch
  * (the subdomain's interface weights and indices, block partial sums, the
  * result) is one fixed array in static device memory of about 0.8 MB, which
- * holds subdomains with at most 65536 interface dofs; a larger interface is
- * rejected with BDDCML_ERR_ARGUMENT.  It is meant for callers that keep their
+ * every GPU that loads the library keeps until the process exits.  It holds
+ * subdomains with at most 65536 interface dofs; a larger interface is
+ * rejected with BDDCML_ERR_ARGUMENT.  The array keeps the previous call's
+ * contents; the one counter that must start at zero is reset by each call.  It is meant for callers that keep their
  * vectors on the GPU and may not allocate at that point: an application that
  * reserves all device memory up front, or one whose own allocator forbids
  * device allocations (and the implicit device synchronisation of cudaMalloc
