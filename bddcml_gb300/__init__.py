@@ -189,6 +189,21 @@ def bddcml_dotprod_subdomain(isub: int, vec1, vec2) -> float:
     return d.value
 
 
+def bddcml_change_subdomain_data(isub: int, ifix, fixv, rhs, is_rhs_complete: int, sol):
+    i, pi = _pi(ifix)
+    f, pf = _pd(fixv)
+    r, pr = _pd(rhs)
+    x, px = _pd(sol)
+    lib().bddcml_change_subdomain_data_c(_i(isub), pi, _i(len(i)), pf, _i(len(f)), pr, _i(len(r)),
+                                         _i(is_rhs_complete), px, _i(len(x)))
+    _check()
+
+
+def bddcml_setup_new_data():
+    lib().bddcml_setup_new_data_c()
+    _check()
+
+
 def bddcml_finalize():
     lib().bddcml_finalize_c()
     _check()

@@ -285,15 +285,35 @@ void bddcml_change_global_data_c(int*, int*, double*, int*, double*, int*, doubl
 void bddcml_change_subdomain_data_c(int* isub, int* ifix, int* lifix, double* fixv, int* lfixv, double* rhs,
                                     int* lrhs, int* is_rhs_complete, double* sol, int* lsol) {
   guarded("bddcml_change_subdomain_data_c", [&] {
-    (void)isub; (void)ifix; (void)lifix; (void)fixv; (void)lfixv; (void)rhs; (void)lrhs; (void)is_rhs_complete;
-    (void)sol; (void)lsol;
-    throw Error{ERR_UNSUPPORTED, "changing subdomain data after setup is not implemented"};
+    Solver* S = need_solver("bddcml_change_subdomain_data_c");
+    if (!S) return;
+    if (!S->setup_done) throw Error{ERR_ARGUMENT, "data can be changed only after bddcml_setup_preconditioner"};
+    int t = sub_index(*S, *isub);
+    Subdomain& s = S->subs[t];
+    if (*lifix != s.ndof || *lfixv != s.ndof || *lrhs != s.ndof || *lsol != s.ndof)
+      throw Error{ERR_ARGUMENT, "array length does not match ndofs of the subdomain"};
+    // the eliminated matrix and the coarse space depend on which dofs are
+    // fixed; only the values may change (module_levels.f90:785-853)
+    for (int i = 0; i < s.ndof; ++i)
+      if ((ifix[i] != 0) != (s.ifix[i] != 0))
+        throw Error{ERR_UNSUPPORTED, "the set of fixed dofs changed; that needs a new setup"};
+    s.fixv.assign(fixv, fixv + s.ndof);
+    s.rhs.assign(rhs, rhs + s.ndof);
+    s.rhs_complete = is_rhs_complete && *is_rhs_complete != 0;
+    s.sol.assign(sol, sol + s.ndof);
+    S->new_data_pending = true;
   });
 }
 
 void bddcml_setup_new_data_c(void) {
   guarded("bddcml_setup_new_data_c", [&] {
-    throw Error{ERR_UNSUPPORTED, "new data after setup is not implemented"};
+    Solver* S = need_solver("bddcml_setup_new_data_c");
+    if (!S) return;
+    if (!S->setup_done) throw Error{ERR_ARGUMENT, "bddcml_setup_preconditioner must come first"};
+    host_new_data(*S);
+    Error err{BDDCML_OK, ""};
+    if (!device_new_data(*S, err)) throw err;
+    S->new_data_pending = false;
   });
 }
 

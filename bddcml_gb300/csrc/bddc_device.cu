@@ -197,6 +197,11 @@ class Device {
   double* scal = nullptr;  // scratch scalar
   BandDesc* bd_oo = nullptr;
   std::vector<BandDesc> hbd_oo;
+  // one-vector interior solves for new loads after setup (allocated on first use)
+  void* nv_v0 = nullptr;
+  void* nv_v1 = nullptr;
+  void* nv_r = nullptr;
+  long long* nv_off = nullptr;
   int maxnbo = 0, maxw = 0, maxNR = 0;
   int nref = 0;
   Profiler prof;
@@ -211,6 +216,8 @@ class Device {
     if (g_alloc_st == st) g_alloc_st = nullptr;
   }
   void release() {
+    nv_v0 = nv_v1 = nv_r = nullptr;
+    nv_off = nullptr;
     for (void* q : owned) cudaFreeAsync(q, st);
     owned.clear();
     maxit_alloc = 0;
@@ -1048,6 +1055,92 @@ void device_set_profiling(Device* d, bool on) { d->prof.on = on; }
 void device_get_profile(Device* d, double* ms, int* cnt) {
   d->prof.collect();
   for (int i = 0; i < NPHASE; ++i) { ms[i] = d->prof.ms[i]; cnt[i] = d->prof.cnt[i]; }
+}
+
+// New loads and boundary values after setup (module_levels.f90:855-903): the
+// reduced-rhs inputs are uploaded again, v = A_oo^-1 f_o is recomputed with the
+// existing factors (refined to FP64 accuracy in mixed mode) and written into
+// the right-hand-side column of X, and g = f_i - A_io v is formed.  Factors,
+// Schur complements and preconditioner stay as they are.
+template <typename T>
+static void new_data_impl(Solver& S) {
+  Device& D = *S.dev;
+  const int nsub = D.nsub;
+  cudaStream_t st = D.st;
+  auto& own = D.owned;
+  vector<long long> fooff(nsub), voff(nsub);
+  long long nfo = 0, nv = 0;
+  for (int t = 0; t < nsub; ++t) {
+    fooff[t] = nfo; nfo += S.subs[t].ndofo;
+    voff[t] = nv; nv += D.hs[t].NO;
+  }
+  vector<double> fov((size_t)std::max(1LL, nfo)), fir((size_t)std::max(1, D.nrep), 0.0);
+#pragma omp parallel for schedule(dynamic)
+  for (int t = 0; t < nsub; ++t) {
+    vector<double> fo, fi;
+    host_reduced_rhs_inputs(S.subs[t], fo, fi);
+    std::copy(fo.begin(), fo.end(), fov.begin() + fooff[t]);
+    std::copy(fi.begin(), fi.end(), fir.begin() + D.hs[t].rep);
+  }
+  CK(cudaMemcpyAsync(D.fo, fov.data(), nfo * sizeof(double), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(D.fi, fir.data(), D.nrep * sizeof(double), cudaMemcpyHostToDevice, st));
+  g_h2d_bytes += (double)(nfo + D.nrep) * sizeof(double);
+  if (!D.nv_v0) {
+    D.nv_v0 = dalloc<T>(nv, own);
+    D.nv_v1 = dalloc<T>(nv, own);
+    D.nv_r = dalloc<T>(nv, own);
+    D.nv_off = upload(voff, own, st);
+  }
+  T* v0 = static_cast<T*>(D.nv_v0);
+  T* v1 = static_cast<T*>(D.nv_v1);
+  T* rv = static_cast<T*>(D.nv_r);
+  T* poolT = static_cast<T*>(D.poolT);
+  const dim3 gv((D.maxNO + 127) / 128, nsub);
+  const size_t smem = (size_t)(D.maxnbo * NB + 5 * NB) * sizeof(T);
+  CK(cudaFuncSetAttribute(k_band_solve1<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  auto solve1 = [&](T* x) {
+    k_band_solve1<T><<<nsub, NT, smem, st>>>(D.bd_oo, poolT, x, D.nv_off);
+    CKL();
+  };
+  k_fill_vec1<T><<<gv, 128, 0, st>>>(D.ds, D.fo, D.fo_off, v0, D.nv_off);
+  CKL();
+  solve1(v0);
+  if constexpr (std::is_same_v<T, float>) {
+    // two refinement steps with FP64-accurate residuals: v = v0 + (d1 + d2)
+    k_residual1_df<<<gv, 128, 0, st>>>(D.ds, D.koo, D.fo, D.fo_off, v0, nullptr, v1, D.nv_off);
+    CKL();
+    solve1(v1);
+    k_residual1_df<<<gv, 128, 0, st>>>(D.ds, D.koo, D.fo, D.fo_off, v0, v1, rv, D.nv_off);
+    CKL();
+    solve1(rv);
+    k_add_vec1<float><<<gv, 128, 0, st>>>(D.ds, rv, v1, D.nv_off);
+    CKL();
+    k_put_rhs_column<float><<<gv, 128, 0, st>>>(D.ds, poolT, v0, v1, D.nv_off);
+    CKL();
+    k_reduced_rhs_df<<<dim3((D.maxNI + 127) / 128, nsub), 128, 0, st>>>(D.ds, D.kio, poolT, D.fi, D.grep);
+    CKL();
+  } else {
+    k_put_rhs_column<double><<<gv, 128, 0, st>>>(D.ds, poolT, v0, nullptr, D.nv_off);
+    CKL();
+    k_reduced_rhs_f64<<<dim3((D.maxNI + 127) / 128, nsub), 128, 0, st>>>(D.ds, D.kio, poolT, D.fi, D.grep);
+    CKL();
+  }
+  int herr = 0;
+  CK(cudaMemcpyAsync(&herr, D.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (herr) throw Error{ERR_NUMERIC, "device error flags " + std::to_string(herr) + " after new data"};
+}
+
+bool device_new_data(Solver& S, Error& err) {
+  try {
+    if (!S.dev || !S.dev->ds) throw Error{ERR_ARGUMENT, "the preconditioner is not set up"};
+    if (S.dev->mixed) new_data_impl<float>(S);
+    else new_data_impl<double>(S);
+  } catch (Error& e) {
+    err = e;
+    return false;
+  }
+  return true;
 }
 
 bool device_solve(Solver& S, double tol, int maxit, int ndecrmax, int& num_iter, int& reason, double& cond,

@@ -279,6 +279,57 @@ struct SigHash {
 
 }  // namespace
 
+// bc = the recorded elimination applied to the current fixed values
+static void host_replay_bc(Subdomain& s) {
+  s.bc.assign(s.ndof, 0.0);
+  for (size_t e = 0; e < s.bcx_tgt.size(); ++e) {
+    const double f = s.fixv[s.bcx_src[e]];
+    if (f != 0.0) s.bc[s.bcx_tgt[e]] += s.bcx_val[e] * f;
+  }
+}
+
+// interface values of bc: own value plus the other holders' values in
+// ascending subdomain order (upload / swap / download, module_dd.f90:1200-1255)
+static void host_interface_bc(Solver& S) {
+  const int nsub = (int)S.subs.size();
+  vector<int> optr(S.ninterface + 1, 0);
+  for (auto& s : S.subs) for (int u : s.uniq) optr[u + 1]++;
+  for (int u = 0; u < S.ninterface; ++u) optr[u + 1] += optr[u];
+  vector<int> osub(optr[S.ninterface]), oloc(optr[S.ninterface]);
+  {
+    vector<int> pos(optr.begin(), optr.end() - 1);
+    for (int t = 0; t < nsub; ++t)
+      for (int i = 0; i < S.subs[t].ndofi; ++i) { int u = S.subs[t].uniq[i]; osub[pos[u]] = t; oloc[pos[u]++] = i; }
+  }
+  vector<vector<double>> bci(nsub);
+  for (int t = 0; t < nsub; ++t) {
+    auto& s = S.subs[t];
+    bci[t].resize(s.ndofi);
+    for (int i = 0; i < s.ndofi; ++i) bci[t][i] = s.bc[s.iivsvn[i]];
+  }
+#pragma omp parallel for schedule(dynamic)
+  for (int t = 0; t < nsub; ++t) {
+    auto& s = S.subs[t];
+    for (int i = 0; i < s.ndofi; ++i) {
+      const int u = s.uniq[i];
+      double acc = 0.0;
+      for (int q = optr[u]; q < optr[u + 1]; ++q) if (osub[q] != t) acc += bci[osub[q]][oloc[q]];
+      s.bc[s.iivsvn[i]] += acc;
+    }
+  }
+}
+
+void host_new_data(Solver& S) {
+  const int nsub = (int)S.subs.size();
+#pragma omp parallel for schedule(dynamic)
+  for (int t = 0; t < nsub; ++t) {
+    auto& s = S.subs[t];
+    if (s.bc_present) host_replay_bc(s);
+    else s.bc.assign(s.ndof, 0.0);
+  }
+  host_interface_bc(S);
+}
+
 void host_setup(Solver& S) {
   int nsub = (int)S.subs.size();
   for (int t = 0; t < nsub; ++t)
@@ -298,19 +349,25 @@ void host_setup(Solver& S) {
     if (!s.assembled) { host_assemble_upper(s.ia, s.ja, s.a); s.assembled = true; }
     host_nodal_components(s);
     s.bc.assign(s.ndof, 0.0);
+    s.bcx_tgt.clear(); s.bcx_src.clear(); s.bcx_val.clear();
     s.bc_present = false;
     for (int i = 0; i < s.ndof; ++i) if (s.ifix[i] != 0) s.bc_present = true;
     if (!s.bc_present) continue;
+    // fixed rows and columns are removed, the diagonal kept (set to 1 when
+    // below 1e-16, module_sm.f90:547-561); what they contributed is recorded
+    auto record = [&](int tgt, int src, double v) {
+      s.bcx_tgt.push_back(tgt); s.bcx_src.push_back(src); s.bcx_val.push_back(v);
+    };
     vector<char> diag_fixed(s.ndof, 0);
     for (size_t k = 0; k < s.ia.size(); ++k) {
       int i = s.ia[k], j = s.ja[k];
       if (i != j) {
-        if (s.ifix[i] && s.fixv[i] != 0.0 && s.a[k] != 0.0 && !s.ifix[j]) s.bc[j] -= s.a[k] * s.fixv[i];
-        if (s.ifix[j] && s.fixv[j] != 0.0 && s.a[k] != 0.0 && !s.ifix[i]) s.bc[i] -= s.a[k] * s.fixv[j];
+        if (s.ifix[i] && s.a[k] != 0.0 && !s.ifix[j]) record(j, i, -s.a[k]);
+        if (s.ifix[j] && s.a[k] != 0.0 && !s.ifix[i]) record(i, j, -s.a[k]);
         if (s.ifix[i] || s.ifix[j]) s.a[k] = 0.0;
       } else if (s.ifix[i]) {
         if (std::fabs(s.a[k]) < 1e-16) s.a[k] = 1.0;
-        if (s.fixv[i] != 0.0) s.bc[i] += s.a[k] * s.fixv[i];
+        record(i, i, s.a[k]);
         diag_fixed[i] = 1;
       }
     }
@@ -318,9 +375,10 @@ void host_setup(Solver& S) {
     for (int i = 0; i < s.ndof; ++i)
       if (s.ifix[i] > 0 && !diag_fixed[i]) {
         s.ia.push_back(i); s.ja.push_back(i); s.a.push_back(1.0);
-        s.bc[i] += s.fixv[i];
+        record(i, i, 1.0);
         added = true;
       }
+    host_replay_bc(s);
     if (added) host_assemble_upper(s.ia, s.ja, s.a);
   }
   S.stats.t_host_assemble = wall_time() - tt;
@@ -661,22 +719,7 @@ void host_setup(Solver& S) {
   };
 
   // ---- assembled Dirichlet contributions on the interface (module_dd.f90:1200-1255)
-  {
-    vector<vector<double>> bci(nsub);
-    for (int t = 0; t < nsub; ++t) {
-      auto& s = S.subs[t];
-      bci[t].resize(s.ndofi);
-      for (int i = 0; i < s.ndofi; ++i) bci[t][i] = s.bc[s.iivsvn[i]];
-    }
-#pragma omp parallel for schedule(dynamic)
-    for (int t = 0; t < nsub; ++t) {
-      auto& s = S.subs[t];
-      for (int i = 0; i < s.ndofi; ++i) {
-        auto pr = neighbour_sum(t, i, [&](int a, int b) { return bci[a][b]; });
-        s.bc[s.iivsvn[i]] += pr.second;
-      }
-    }
-  }
+  host_interface_bc(S);
 
   // ---- weights (module_dd.f90:11554-11722)
   {
@@ -728,6 +771,22 @@ void host_setup(Solver& S) {
 
 // ---------------------------------------------------- device-ready blocks
 
+// reduced-rhs input: weighted rhs, Dirichlet rows zeroed, weighted bc added
+// (module_dd.f90:7040-7075 and sm_prepare_rhs, module_sm.f90:603-628)
+void host_reduced_rhs_inputs(const Subdomain& s, vector<double>& fo, vector<double>& fi) {
+  const int no = s.ndofo, ni = s.ndofi;
+  vector<double> f = s.rhs;
+  vector<double> bcw = s.bc;
+  if (s.rhs_complete) for (int i = 0; i < ni; ++i) f[s.iivsvn[i]] *= s.wi[i];
+  for (int i = 0; i < ni; ++i) bcw[s.iivsvn[i]] *= s.wi[i];
+  if (s.bc_present)
+    for (int i = 0; i < s.ndof; ++i) { if (s.ifix[i]) f[i] = 0.0; f[i] += bcw[i]; }
+  fo.resize(no);
+  for (int q = 0; q < no; ++q) fo[q] = f[s.iovsvn[s.operm[q]]];
+  fi.resize(ni);
+  for (int i = 0; i < ni; ++i) fi[i] = f[s.iivsvn[i]];
+}
+
 void host_prepare_blocks(Subdomain& s, SubBlocks& b) {
   constexpr int NB = 64;
   vector<int> fptr, fcol;
@@ -768,18 +827,7 @@ void host_prepare_blocks(Subdomain& s, SubBlocks& b) {
   for (int r = 0; r < no; ++r)
     for (int k = b.oo_ptr[r]; k < b.oo_ptr[r + 1]; ++k)
       if (b.oo_col[k] <= r) b.w = std::max(b.w, r / NB - b.oo_col[k] / NB);
-  // reduced-rhs input: weighted rhs, Dirichlet rows zeroed, weighted bc added
-  // (module_dd.f90:7040-7075 and sm_prepare_rhs, module_sm.f90:603-628)
-  vector<double> f = s.rhs;
-  vector<double> bcw = s.bc;
-  if (s.rhs_complete) for (int i = 0; i < ni; ++i) f[s.iivsvn[i]] *= s.wi[i];
-  for (int i = 0; i < ni; ++i) bcw[s.iivsvn[i]] *= s.wi[i];
-  if (s.bc_present)
-    for (int i = 0; i < s.ndof; ++i) { if (s.ifix[i]) f[i] = 0.0; f[i] += bcw[i]; }
-  b.fo.resize(no);
-  for (int q = 0; q < no; ++q) b.fo[q] = f[orow(q)];
-  b.fi.resize(ni);
-  for (int i = 0; i < ni; ++i) b.fi[i] = f[s.iivsvn[i]];
+  host_reduced_rhs_inputs(s, b.fo, b.fi);
   double sd = 0.0;
   int cnt = 0;
   for (int i = 0; i < ni; ++i)

@@ -74,6 +74,11 @@ struct Subdomain {
   vector<int> indrowc;
   int nconstr = 0;
   vector<double> bc;         // eliminated Dirichlet contributions, interface assembled
+  // the elimination as a replayable list: bc[bcx_tgt] += bcx_val * fixv[bcx_src],
+  // in the order the first elimination applied them (the reference keeps the
+  // fixed rows of the matrix for the same purpose, module_dd.f90:1081-1180)
+  vector<int> bcx_tgt, bcx_src;
+  vector<double> bcx_val;
   vector<double> wi;         // interface weights
   vector<int> uniq;          // interface dof -> unique interface index
   // interior ordering used for the band factor: perm[new] = index into iovsvn
@@ -140,6 +145,7 @@ struct Solver {
   vector<int> iface_fixed;            // per unique dof: 1 if Dirichlet-fixed
   vector<double> iface_wsum;          // per unique dof: sum of subdomain weights
   bool setup_done = false;
+  bool new_data_pending = false;  // changed subdomain data not yet through setup_new_data
   Device* dev = nullptr;
   Stats stats;
   vector<double> relres_history;
@@ -155,10 +161,17 @@ void host_setup(Solver& S);              // everything integer/geometric + BC + 
 void host_interior_ordering(Subdomain& s, const vector<int>& f_ptr, const vector<int>& f_col);
 void full_symmetric_csr(const Subdomain& s, vector<int>& ptr, vector<int>& col, vector<double>& val);
 void host_prepare_blocks(Subdomain& s, SubBlocks& b);
+// reduced-rhs inputs of a subdomain: weighted rhs with Dirichlet rows replaced by the
+// weighted eliminated contributions; fo in the band order of the interior, fi per interface dof
+void host_reduced_rhs_inputs(const Subdomain& s, vector<double>& fo, vector<double>& fi);
+// new boundary values / loads after setup: recompute bc on every subdomain and
+// assemble it over the interface (module_levels.f90:855-903)
+void host_new_data(Solver& S);
 
 // device (bddc_device.cu)
 Device* device_create(Error& err);
 bool device_release_memory(Error& err);
+bool device_new_data(Solver& S, Error& err);
 // largest subdomain interface the allocation-free dot product's fixed scratch holds
 constexpr int NOALLOC_MAX_IFACE = 65536;
 bool device_dotprod_noalloc(const int* iface_dofs, const double* weights, int nif, const double* v1,

@@ -680,4 +680,158 @@ __global__ void k_z(const DevSub* __restrict__ ds, const T* __restrict__ pool, T
   pcpool[s.oZ + (long long)i * s.NI + j] = v;
 }
 
+// ---------------------------------------------------- one right-hand side
+// New loads after setup (bddcml_setup_new_data_c) need v = A_oo^-1 f_o and
+// g = f_i - A_io v per subdomain, with the factors already in place.
+
+// In-place solve (L L^T) x = b of one vector per system with the block-band
+// factor; grid = systems, NT threads.  x lives in shared memory during the
+// sweeps; forward rows are warp dot products along the band row, backward
+// columns are summed over four 16-row groups of the blocks below.
+// Dynamic shared memory: (nb*NB + 5*NB) elements of T.
+template <typename T>
+__global__ void __launch_bounds__(NT) k_band_solve1(const BandDesc* __restrict__ bd, const T* __restrict__ pool,
+                                                    T* __restrict__ xv, const long long* __restrict__ xoff) {
+  const BandDesc d = bd[blockIdx.x];
+  if (d.nb == 0) return;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T* xs = reinterpret_cast<T*>(smraw);  // nb * NB
+  T* ts = xs + d.nb * NB;                // NB
+  T* part = ts + NB;                     // 4 * NB
+  T* x = xv + xoff[blockIdx.x];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int n = d.nb * NB;
+  for (int i = tid; i < n; i += NT) xs[i] = x[i];
+  __syncthreads();
+  for (int k = 0; k < d.nb; ++k) {
+    const int j0 = max(0, k - d.w);
+    for (int r = warp; r < NB; r += NT / 32) {  // t = x_k - sum_j L_kj x_j
+      T acc = T(0);
+      for (int j = j0; j < k; ++j) {
+        const T* Lr = pool + band_block(d, k, j) + r * NB;
+        acc += Lr[lane] * xs[j * NB + lane] + Lr[lane + 32] * xs[j * NB + lane + 32];
+      }
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+      if (lane == 0) ts[r] = xs[k * NB + r] - acc;
+    }
+    __syncthreads();
+    const T* Li = pool + d.oLinv + (long long)k * NB * NB;
+    for (int r = warp; r < NB; r += NT / 32) {  // x_k = Linv_kk t
+      T acc = Li[r * NB + lane] * ts[lane] + Li[r * NB + lane + 32] * ts[lane + 32];
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+      if (lane == 0) xs[k * NB + r] = acc;
+    }
+    __syncthreads();
+  }
+  const int c = tid & (NB - 1), grp = tid / NB;
+  for (int k = d.nb - 1; k >= 0; --k) {
+    T acc = T(0);  // sum_{i>k} L_ik^T x_i, rows of this thread's group
+    for (int i = k + 1; i <= min(d.nb - 1, k + d.w); ++i) {
+      const T* L = pool + band_block(d, i, k);
+      for (int r = grp * 16; r < grp * 16 + 16; ++r) acc += L[r * NB + c] * xs[i * NB + r];
+    }
+    part[grp * NB + c] = acc;
+    __syncthreads();
+    if (tid < NB) ts[tid] = xs[k * NB + tid] - ((part[tid] + part[NB + tid]) + (part[2 * NB + tid] + part[3 * NB + tid]));
+    __syncthreads();
+    const T* Li = pool + d.oLinv + (long long)k * NB * NB;
+    T a2 = T(0);  // x_k = Linv_kk^T t
+    for (int r = grp * 16; r < grp * 16 + 16; ++r) a2 += Li[r * NB + c] * ts[r];
+    part[grp * NB + c] = a2;
+    __syncthreads();
+    if (tid < NB) xs[k * NB + tid] = (part[tid] + part[NB + tid]) + (part[2 * NB + tid] + part[3 * NB + tid]);
+    __syncthreads();
+  }
+  for (int i = tid; i < n; i += NT) x[i] = xs[i];
+}
+
+// x = f_o in the factor precision (padding rows zero); one vector per system
+template <typename T>
+__global__ void k_fill_vec1(const DevSub* __restrict__ ds, const double* __restrict__ fo,
+                            const long long* __restrict__ fo_off, T* __restrict__ xv,
+                            const long long* __restrict__ xoff) {
+  const DevSub s = ds[blockIdx.y];
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= s.NO) return;
+  xv[xoff[blockIdx.y] + r] = r < s.no ? T(fo[fo_off[blockIdx.y] + r]) : T(0);
+}
+
+// r = f_o - A_oo (v0 + v1), FP64-accurate in double-float, written as FP32;
+// v1 may be null (v0 is then an exact FP32 value)
+__global__ void k_residual1_df(const DevSub* __restrict__ ds, CsrView koo, const double* __restrict__ fo,
+                               const long long* __restrict__ fo_off, const float* __restrict__ v0,
+                               const float* __restrict__ v1, float* __restrict__ rv,
+                               const long long* __restrict__ xoff) {
+  const DevSub s = ds[blockIdx.y];
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= s.NO) return;
+  const long long off = xoff[blockIdx.y];
+  if (r >= s.no) { rv[off + r] = 0.f; return; }
+  dfacc acc;
+  acc.add_df(df_from_double(fo[fo_off[blockIdx.y] + r]));
+  const int* p = koo.ptr + s.koo;
+  for (int q = p[r]; q < p[r + 1]; ++q) {
+    const int col = koo.col[q];
+    const dfloat a = df_from_double(-koo.val[q]);
+    if (v1) acc.fma_df(a, dfloat{v0[off + col], v1[off + col]});
+    else acc.fma_df(a, v0[off + col]);
+  }
+  rv[off + r] = acc.value().hi;
+}
+
+// y += x (one vector per system)
+template <typename T>
+__global__ void k_add_vec1(const DevSub* __restrict__ ds, const T* __restrict__ x, T* __restrict__ y,
+                           const long long* __restrict__ xoff) {
+  const DevSub s = ds[blockIdx.y];
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= s.NO) return;
+  y[xoff[blockIdx.y] + r] += x[xoff[blockIdx.y] + r];
+}
+
+// column ni of the interior solution block X: component 0 = v0 and, for the
+// double-float pair, component 1 = v1
+template <typename T>
+__global__ void k_put_rhs_column(const DevSub* __restrict__ ds, T* __restrict__ pool, const T* __restrict__ v0,
+                                 const T* __restrict__ v1, const long long* __restrict__ xoff) {
+  const DevSub s = ds[blockIdx.y];
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= s.NO) return;
+  const long long off = xoff[blockIdx.y];
+  T* X0 = pool + s.oXc;
+  X0[(long long)r * s.NR + s.ni] = r < s.no ? v0[off + r] : T(0);
+  if (v1) X0[(long long)s.NO * s.NR + (long long)r * s.NR + s.ni] = r < s.no ? v1[off + r] : T(0);
+}
+
+// g = f_i - A_io X(:, ni): the reduced-rhs column of k_schur_df / k_schur_f64
+// alone, in the same operation order
+__global__ void k_reduced_rhs_df(const DevSub* __restrict__ ds, CsrView kio, const float* __restrict__ pool,
+                                 const double* __restrict__ fi, double* __restrict__ grep) {
+  const DevSub s = ds[blockIdx.y];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= s.ni) return;
+  const long long comp = (long long)s.NO * s.NR;
+  const float* X0 = pool + s.oXc;
+  const float* X1 = X0 + comp;
+  dfacc acc;
+  acc.add_df(df_from_double(fi[s.rep + i]));
+  const int* p = kio.ptr + s.kio;
+  for (int q = p[i]; q < p[i + 1]; ++q) {
+    const long long o = (long long)kio.col[q] * s.NR + s.ni;
+    acc.fma_df(df_from_double(-kio.val[q]), dfloat{X0[o], X1[o]});
+  }
+  grep[s.rep + i] = acc.to_double();
+}
+
+__global__ void k_reduced_rhs_f64(const DevSub* __restrict__ ds, CsrView kio, const double* __restrict__ pool,
+                                  const double* __restrict__ fi, double* __restrict__ grep) {
+  const DevSub s = ds[blockIdx.y];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= s.ni) return;
+  double acc = fi[s.rep + i];
+  const int* p = kio.ptr + s.kio;
+  for (int q = p[i]; q < p[i + 1]; ++q) acc -= kio.val[q] * pool[s.oXc + (long long)kio.col[q] * s.NR + s.ni];
+  grep[s.rep + i] = acc;
+}
+
 }  // namespace bddc

@@ -105,11 +105,17 @@ void bddcml_change_global_data_c(int *ifix, int *lifix, double *fixv, int *lfixv
                                  double *sol, int *lsol);
 
 /* replaces bddcml_change_subdomain_data_c, src/bddcml_interface_c.h:51-54
- * (module_levels.f90:785-849) */
+ * (module_levels.f90:785-849).  New fixed values, loads and initial guess of a
+ * subdomain after setup; the set of fixed dofs must stay the same
+ * (BDDCML_ERR_UNSUPPORTED otherwise, since the eliminated matrix and the
+ * coarse space depend on it).  Takes effect at bddcml_setup_new_data_c. */
 void bddcml_change_subdomain_data_c(int *isub, int *ifix, int *lifix, double *fixv, int *lfixv,
                                     double *rhs, int *lrhs, int *is_rhs_complete, double *sol, int *lsol);
 
-/* replaces bddcml_setup_new_data_c, src/bddcml_interface_c.h:56 (module_levels.f90:852-903) */
+/* replaces bddcml_setup_new_data_c, src/bddcml_interface_c.h:56 (module_levels.f90:852-903).
+ * Recomputes the eliminated Dirichlet contributions and the reduced
+ * right-hand side with the factors, Schur complements and preconditioner of
+ * the last setup; the next bddcml_solve_c solves the new problem. */
 void bddcml_setup_new_data_c(void);
 
 /* replaces bddcml_dotprod_subdomain_c, src/bddcml_interface_c.h:58 (module_dd.f90:12736-12788) */

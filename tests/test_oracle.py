@@ -129,3 +129,19 @@ def test_oracle_golden_regression(oracle_mod):
         assert o.stats() == g["coarse"], name
         u = o.global_solution()
         assert abs(np.linalg.norm(u) - g["solution_norm2"]) < 1e-10 * g["solution_norm2"], name
+
+
+def test_oracle_inhomogeneous_dirichlet_matches_direct(oracle_mod):
+    """Nonzero boundary values and a varying load: the eliminated Dirichlet
+    contributions (module_sm.f90:431-600, module_dd.f90:1081-1256) against a
+    direct solve of the assembled system."""
+    from bddcml_gb300 import problems
+    from newdata_util import changed_data, direct_solution
+    prob = changed_data(problems.poisson_on_cube(4, 3), seed=3)
+    o = oracle_mod.Oracle(prob)
+    o.setup(1, 1, 0)
+    it, reason, cond = o.solve(1e-10, 300, 50)
+    assert reason == 0
+    u = o.global_solution()
+    ud = direct_solution(prob)
+    assert np.linalg.norm(u - ud) / np.linalg.norm(ud) < 1e-9
