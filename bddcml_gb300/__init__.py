@@ -39,7 +39,7 @@ EXPORTS = ["bddcml_init_c", "bddcml_upload_global_data_c", "bddcml_upload_subdom
            "bddcml_get_last_error_c", "bddcml_set_precision_c", "bddcml_get_stats_c",
            "bddcml_get_residual_history_c", "bddcml_get_interface_weights_c", "bddcml_get_coarse_info_c",
            "bddcml_set_profiling_c", "bddcml_get_profile_c", "bddcml_release_device_memory_c",
-           "bddcml_dotprod_subdomain_dev_c"]
+           "bddcml_dotprod_subdomain_dev_c", "bddcml_element_gradient_dev_c"]
 
 # phases of bddcml_get_profile_c (CUDA events on the solver stream)
 PHASES = ["numeric_total", "solve_total", "factor_interior", "solve_interior", "refine_residual", "schur",
@@ -250,6 +250,15 @@ def dotprod_subdomain_dev(isub: int, vec1_ptr: int, vec2_ptr: int, lvec: int) ->
                                          C.byref(out))
     _check()
     return out.value
+
+
+def element_gradient_dev(nelem: int, nne: int, inet_ptr: int, ke0_ptr: int, per_element: bool, u_ptr: int,
+                         lam_ptr: int, grad_ptr: int):
+    """grad[e] = -lam_e^T K_e^0 u_e on device arrays (raw device addresses)."""
+    lib().bddcml_element_gradient_dev_c(_i(nelem), _i(nne), C.c_void_p(inet_ptr), C.c_void_p(ke0_ptr),
+                                        _i(1 if per_element else 0), C.c_void_p(u_ptr), C.c_void_p(lam_ptr),
+                                        C.c_void_p(grad_ptr))
+    _check()
 
 
 def release_device_memory():

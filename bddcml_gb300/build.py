@@ -21,6 +21,7 @@ SOURCES = [
     ("bddc_abi.cpp", "g++"),
     ("bddc_device.cu", "nvcc"),
     ("bddc_noalloc.cu", "nvcc"),
+    ("bddc_gradient.cu", "nvcc"),
 ]
 HEADERS = ["bddc_internal.hpp", "bddc_kernels.cuh", "bddc_df.cuh", "bddc_setup_kernels.cuh",
            "bddc_pcg_kernels.cuh", "bddc_tc.cuh"]

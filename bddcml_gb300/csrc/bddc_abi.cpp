@@ -354,6 +354,15 @@ void bddcml_dotprod_subdomain_dev_c(int* isub, const double* vec1, const double*
   });
 }
 
+void bddcml_element_gradient_dev_c(int* nelem, int* nne, const int* inet, const double* ke0, int* ke0_per_element,
+                                   const double* u, const double* lam, double* grad) {
+  guarded("bddcml_element_gradient_dev_c", [&] {
+    if (!nelem || !nne || !ke0_per_element) throw Error{ERR_ARGUMENT, "null size argument"};
+    Error err{BDDCML_OK, ""};
+    if (!device_element_gradient(*nelem, *nne, inet, ke0, *ke0_per_element != 0, u, lam, grad, err)) throw err;
+  });
+}
+
 void bddcml_release_device_memory_c(void) {
   guarded("bddcml_release_device_memory_c", [&] {
     Error err{BDDCML_OK, ""};

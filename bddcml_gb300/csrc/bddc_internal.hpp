@@ -172,6 +172,8 @@ void host_new_data(Solver& S);
 Device* device_create(Error& err);
 bool device_release_memory(Error& err);
 bool device_new_data(Solver& S, Error& err);
+bool device_element_gradient(int nelem, int nne, const int* inet, const double* ke0, bool per_element,
+                             const double* u, const double* lam, double* grad, Error& err);
 // largest subdomain interface the allocation-free dot product's fixed scratch holds
 constexpr int NOALLOC_MAX_IFACE = 65536;
 bool device_dotprod_noalloc(const int* iface_dofs, const double* weights, int nif, const double* v1,

@@ -237,3 +237,32 @@ def global_matrix_and_rhs(prob: Problem):
                       shape=(prob.ndof, prob.ndof))
     f = f / np.maximum(cnt, 1.0)   # rhs is a restriction of the global rhs (complete)
     return K, f, fixed
+
+
+def cube_connectivity(n_el_edge: int) -> np.ndarray:
+    """Global node numbers (= dof numbers, one dof per node) of the 8 nodes of
+    every element of the n_el_edge^3 cube grid, in global element order (x
+    fastest, the order of the kappa vector), node order as in box_subdomain."""
+    n = n_el_edge
+    nng = n + 1
+    ek, ej, ei = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+    n1 = (ei + ej * nng + ek * nng * nng).ravel()
+    sx, sy, sz = 1, nng, nng * nng
+    return np.stack([n1, n1 + sx, n1 + sx + sy, n1 + sy,
+                     n1 + sz, n1 + sx + sz, n1 + sx + sy + sz, n1 + sy + sz], axis=1).astype(np.int32)
+
+
+def smooth_target(n_el_edge: int, seed: int, modes: int = 8) -> np.ndarray:
+    """A seeded smooth nodal field (sum of `modes` random Fourier modes) on the
+    cube grid: the target u* of the differentiation example."""
+    rng = np.random.default_rng(seed)
+    n = n_el_edge
+    t = np.arange(n + 1) / n
+    z, y, x = np.meshgrid(t, t, t, indexing="ij")
+    u = np.zeros_like(x)
+    for _ in range(modes):
+        k = rng.integers(1, 4, size=3)
+        a = rng.standard_normal() * 0.01
+        ph = rng.uniform(0, 2 * np.pi, size=3)
+        u += a * np.sin(np.pi * k[0] * x + ph[0]) * np.sin(np.pi * k[1] * y + ph[1]) * np.sin(np.pi * k[2] * z + ph[2])
+    return u.ravel()

@@ -175,6 +175,19 @@ void bddcml_get_profile_c(double *ms, int *counts, int *lphase);
  * No counterpart in the reference. */
 void bddcml_release_device_memory_c(void);
 
+/* Per-element gradient of an objective J(u) with respect to element
+ * coefficients kappa_e, for K(kappa) = sum_e kappa_e K_e^0:
+ *     grad[e] = dJ/dkappa_e = - lambda_e^T K_e^0 u_e,
+ * where u is the solution and lambda the adjoint solution (K lambda = dJ/du
+ * with homogeneous Dirichlet values, e.g. from change_subdomain_data +
+ * setup_new_data + solve).  All arrays are device pointers: inet (nelem x nne
+ * global dof indices, 0-based), ke0 (one nne x nne row-major matrix, or one
+ * per element when *ke0_per_element != 0), u and lam (global vectors), grad
+ * (nelem).  nne <= 27.  Runs on the legacy default stream and waits for it.
+ * No counterpart in the reference. */
+void bddcml_element_gradient_dev_c(int *nelem, int *nne, const int *inet, const double *ke0,
+                                   int *ke0_per_element, const double *u, const double *lam, double *grad);
+
 /* The weighted dot product of bddcml_dotprod_subdomain_c for vectors that
  * already live in device memory (vec1, vec2: device pointers, length *lvec =
  * the subdomain's ndof, subdomain dof order); the result is written to the
