@@ -266,3 +266,98 @@ def smooth_target(n_el_edge: int, seed: int, modes: int = 8) -> np.ndarray:
         ph = rng.uniform(0, 2 * np.pi, size=3)
         u += a * np.sin(np.pi * k[0] * x + ph[0]) * np.sin(np.pi * k[1] * y + ph[1]) * np.sin(np.pi * k[2] * z + ph[2])
     return u.ravel()
+
+
+def q1_elasticity_reference_matrix(nu: float) -> np.ndarray:
+    """24 x 24 stiffness matrix of the unit Q1 hexahedron for an isotropic
+    material with E = 1, 2x2x2 Gauss integration, dofs ordered node by node
+    (u_x, u_y, u_z) with the node order of box_subdomain.  For an element of
+    edge h and modulus E the matrix is E * h * this."""
+    lam = nu / ((1 + nu) * (1 - 2 * nu))
+    mu = 1.0 / (2 * (1 + nu))
+    D = np.zeros((6, 6))
+    D[:3, :3] = lam
+    D[np.arange(3), np.arange(3)] += 2 * mu
+    D[3, 3] = D[4, 4] = D[5, 5] = mu
+    corners = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0],
+                        [0, 0, 1], [1, 0, 1], [1, 1, 1], [0, 1, 1]], dtype=float)
+    g = 0.5 / np.sqrt(3.0)
+    K = np.zeros((24, 24))
+    for gx in (0.5 - g, 0.5 + g):
+        for gy in (0.5 - g, 0.5 + g):
+            for gz in (0.5 - g, 0.5 + g):
+                dN = np.zeros((8, 3))
+                for a, (cx, cy, cz) in enumerate(corners):
+                    fx = gx if cx else 1 - gx
+                    fy = gy if cy else 1 - gy
+                    fz = gz if cz else 1 - gz
+                    sx = 1 if cx else -1
+                    sy = 1 if cy else -1
+                    sz = 1 if cz else -1
+                    dN[a] = [sx * fy * fz, sy * fx * fz, sz * fx * fy]
+                Bm = np.zeros((6, 24))
+                for a in range(8):
+                    Bm[0, 3 * a] = dN[a, 0]
+                    Bm[1, 3 * a + 1] = dN[a, 1]
+                    Bm[2, 3 * a + 2] = dN[a, 2]
+                    Bm[3, 3 * a] = dN[a, 1]
+                    Bm[3, 3 * a + 1] = dN[a, 0]
+                    Bm[4, 3 * a + 1] = dN[a, 2]
+                    Bm[4, 3 * a + 2] = dN[a, 1]
+                    Bm[5, 3 * a] = dN[a, 2]
+                    Bm[5, 3 * a + 2] = dN[a, 0]
+                K += 0.125 * Bm.T @ D @ Bm
+    return K
+
+
+def elasticity_box_subdomain(isub: int, lo, hi, n_el_edge: int, young: Optional[np.ndarray],
+                             ke_ref: np.ndarray) -> Subdomain:
+    """Linear elasticity on the element box [lo, hi) of the unit cube grid:
+    3 dofs per node, clamped at x = 0, unit body force in -z (lumped)."""
+    base = box_subdomain(isub, lo, hi, n_el_edge, None, q1_laplace_reference_matrix())
+    h = 1.0 / n_el_edge
+    nn, ne_ = base.nnods, base.nelems
+    inet_e = base.inet.reshape(ne_, 8).astype(np.int64)
+    edof = (3 * inet_e[:, :, None] + np.arange(3)[None, None, :]).reshape(ne_, 24)
+    pairs = [(i_, j_) for j_ in range(24) for i_ in range(j_ + 1)]
+    pi = np.array([p[0] for p in pairs])
+    pj = np.array([p[1] for p in pairs])
+    idof, jdof = edof[:, pi], edof[:, pj]
+    i_sp = np.minimum(idof, jdof).astype(np.int32).ravel()
+    j_sp = np.maximum(idof, jdof).astype(np.int32).ravel()
+    scale = h * (young[base.isegn] if young is not None else np.ones(ne_))
+    a_sp = (scale[:, None] * ke_ref[pi, pj][None, :]).ravel()
+    x0 = base.xyz[0] == 0.0
+    ifix = np.repeat(x0.astype(np.int32), 3)
+    ndofs = 3 * nn
+    # lumped unit body force in -z: every element adds -h^3/8 to the z dof of
+    # its nodes; the subdomain holds the global (complete) value, so count the
+    # elements around each node in the whole grid
+    ig = np.rint(base.xyz[0] / h).astype(int)
+    jg = np.rint(base.xyz[1] / h).astype(int)
+    kg = np.rint(base.xyz[2] / h).astype(int)
+    glob_cnt = np.ones(nn)
+    for ax in (ig, jg, kg):
+        glob_cnt *= np.where((ax == 0) | (ax == n_el_edge), 1.0, 2.0)
+    rhs = np.zeros(ndofs)
+    rhs[2::3] = -glob_cnt * h ** 3 / 8.0
+    rhs[ifix != 0] = 0.0
+    isvgvn = (3 * base.isngn[:, None].astype(np.int64) + np.arange(3)[None, :]).ravel().astype(np.int32)
+    return Subdomain(
+        isub=isub, nelems=ne_, nnods=nn, ndofs=ndofs, inet=base.inet, nnet=base.nnet,
+        nndf=np.full(nn, 3, dtype=np.int32), isngn=base.isngn, isvgvn=isvgvn, isegn=base.isegn,
+        xyz=base.xyz, ifix=ifix, fixv=np.zeros(ndofs), rhs=rhs, sol=np.zeros(ndofs),
+        i_sparse=i_sp, j_sparse=j_sp, a_sparse=a_sp)
+
+
+def elasticity_on_cube(num_el_per_sub_edge: int, num_sub_per_cube_edge: int, nu: float = 0.3,
+                       young: Optional[np.ndarray] = None) -> Problem:
+    """Q1 linear elasticity on the unit cube: clamped at x = 0, unit body force
+    in -z, cubic subdomains (the elasticity configuration at two levels)."""
+    n = num_el_per_sub_edge * num_sub_per_cube_edge
+    ke = q1_elasticity_reference_matrix(nu)
+    subs = [elasticity_box_subdomain(isub, lo, hi, n, young, ke)
+            for isub, (lo, hi) in enumerate(_sub_ranges_uniform(num_el_per_sub_edge, num_sub_per_cube_edge))]
+    nnod = (n + 1) ** 3
+    return Problem(name=f"elasticity_{n}^3_{num_sub_per_cube_edge}^3subs", nelem=n ** 3, nnod=nnod,
+                   ndof=3 * nnod, ndim=3, meshdim=3, subdomains=subs, n_el_edge=n, kappa=young)

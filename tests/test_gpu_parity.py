@@ -91,3 +91,17 @@ def test_solution_matches_direct_solve(built_lib):
     for precision in (0, 1):
         u, it, reason, cond, st = _run(prob, precision)
         assert np.linalg.norm(u - ud) / np.linalg.norm(ud) < 1e-7
+
+
+@pytest.mark.parametrize("ne,ns", [(3, 2), (4, 3)])
+@pytest.mark.parametrize("precision", [0, 1])
+def test_elasticity_parity(built_lib, oracle_mod, ne, ns, precision):
+    """Three dofs per node (Q1 elasticity, clamped at x = 0, body force)."""
+    from bddcml_gb300 import problems
+    prob = problems.elasticity_on_cube(ne, ns)
+    o, it_o, reason_o, cond_o, u_o = _oracle(oracle_mod, prob)
+    u, it, reason, cond, st = _run(prob, precision)
+    assert reason == reason_o == 0
+    assert abs(it - it_o) <= 2
+    tol = TOL_FP64 if precision == 0 else TOL_MIXED
+    assert np.linalg.norm(u - u_o) / np.linalg.norm(u_o) <= tol

@@ -129,3 +129,26 @@ def test_solve_defaults_report_unsupported_bicgstab(built_lib):
     with pytest.raises(B.BddcmlError):
         B.bddcml_setup_preconditioner(1, 0, 1, 1, 1, 0, 0, 0)  # no GPU here -> CUDA error after host setup
     B.bddcml_finalize()
+
+
+def test_host_coarse_space_equals_oracle_elasticity(built_lib, oracle_mod):
+    """Three dofs per node: corners carry three coarse dofs, edge and face
+    averages one per component (module_dd.f90:4298-4384)."""
+    import bddcml_gb300 as B
+    from bddcml_gb300 import problems
+    prob = problems.elasticity_on_cube(3, 2)
+    B.bddcml_init(2, [prob.nsub, 1], -1, 0, 0, 0, 0)
+    B.upload_problem(prob)
+    try:
+        B.bddcml_setup_preconditioner(1, 0, 1, 1, 1, 0, 0, 0)
+    except B.BddcmlError as e:  # no GPU in this container: the host part has run
+        assert e.code == 2
+    info = B.get_coarse_info()
+    o = oracle_mod.Oracle(prob)
+    o.setup(1, 1, 0)
+    assert info == o.stats()
+    assert info["ndofc"] == 3 * (info["ncorner"] + info["nedge"] + info["nface"])
+    for s in prob.subdomains:
+        w_o = o.weights(s.isub)
+        assert np.array_equal(w_o, B.get_interface_weights(s.isub, len(w_o)))
+    B.bddcml_finalize()

@@ -166,3 +166,17 @@ def test_oracle_adjoint_gradient_matches_finite_differences(oracle_mod):
         fd = (jp - jm) / (2 * eps)           # directional derivative along kappa * d
         an = float(np.dot(grad, kappa * d))
         assert abs(fd - an) <= 1e-6 * max(abs(fd), abs(an)), (fd, an)
+
+
+def test_oracle_elasticity_matches_direct(oracle_mod):
+    """Q1 linear elasticity (3 dofs per node, clamped face, body force)."""
+    from bddcml_gb300 import problems
+    from newdata_util import direct_solution
+    prob = problems.elasticity_on_cube(3, 2)
+    o = oracle_mod.Oracle(prob)
+    o.setup(1, 1, 0)
+    it, reason, cond = o.solve(1e-10, 300, 50)
+    assert reason == 0
+    u = o.global_solution()
+    ud = direct_solution(prob)
+    assert np.linalg.norm(u - ud) / np.linalg.norm(ud) < 1e-9
