@@ -308,15 +308,16 @@ def upload_problem(prob, numbase: int = 0, find_components_int: int = 1, neighbo
 
 
 def solve_problem(prob, precision: int = 1, tol: float = 1e-8, maxit: int = 500, ndecrmax: int = 50,
-                  weights_type: int = 0, numbase: int = 0, finalize: bool = True):
+                  weights_type: int = 0, numbase: int = 0, finalize: bool = True, method: int = 0):
     """init -> upload -> setup -> solve -> download (-> finalize) through the
     C ABI, the sequence of the reference example poisson_on_cube.f90:373-672.
+    method: 0 PCG, 1 BiCGSTAB, 2 steepest descent, -1 reference defaults.
     Returns (global solution, num_iter, reason, cond, stats)."""
     bddcml_init(2, [prob.nsub, 1], -1, 0, 0, numbase, 0)
     set_precision(precision)
     upload_problem(prob, numbase=numbase)
     bddcml_setup_preconditioner(prob.matrixtype, 0, 1, 1, 1, 0, 0, weights_type)
-    it, reason, cond = bddcml_solve(0, 0, tol, maxit, ndecrmax, 0, 0)
+    it, reason, cond = bddcml_solve(0, method, tol, maxit, ndecrmax, 0, 0)
     u = np.zeros(prob.ndof)
     for s in prob.subdomains:
         u[s.isvgvn] = bddcml_download_local_solution(s.isub + numbase, s.ndofs)

@@ -231,20 +231,18 @@ void bddcml_solve_c(int* comm_all, int* method, double* tol, int* maxit, int* nd
     Solver* S = need_solver("bddcml_solve_c");
     if (!S) return;
     if (!S->setup_done) throw Error{ERR_ARGUMENT, "preconditioner is not set up"};
-    int m = *method;
-    double t = 1e-6;   // module_bddcml.f90:515-520 defaults
-    int mi = 1000, nd = 30;
-    if (m == -1) {
-      throw Error{ERR_UNSUPPORTED, "the default Krylov method of the reference is BiCGSTAB, which is not implemented; "
-                                  "use method 0 (PCG)"};
-    }
-    if (m != 0) throw Error{ERR_UNSUPPORTED, "only method 0 (PCG) is implemented"};
-    t = *tol; mi = *maxit; nd = *ndecrmax;
+    // method -1 takes the reference defaults (module_bddcml.f90:515-520, 544-567):
+    // BiCGSTAB, tol 1e-6, maxit 1000, ndecrmax 30
+    int m = 1, mi = 1000, nd = 30;
+    double t = 1e-6;
+    if (*method != -1) { m = *method; t = *tol; mi = *maxit; nd = *ndecrmax; }
+    if (m == 5) throw Error{ERR_UNSUPPORTED, "method 5 (direct solve by backsubstitution) is not implemented"};
+    if (m < 0 || m > 2) throw Error{ERR_ARGUMENT, "unknown iterative method " + std::to_string(m)};
     if (mi < 1) throw Error{ERR_ARGUMENT, "maxit must be positive"};
     int it = 0, reason = 0;
     double cond = 1.0;
     Error err{0, ""};
-    if (!device_solve(*S, t, mi, nd, it, reason, cond, err)) throw err;
+    if (!device_solve(*S, m, t, mi, nd, it, reason, cond, err)) throw err;
     *num_iter = it;
     *converged_reason = reason;
     *condition_number = cond;

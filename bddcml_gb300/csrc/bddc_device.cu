@@ -202,6 +202,8 @@ class Device {
   void* nv_v1 = nullptr;
   void* nv_r = nullptr;
   long long* nv_off = nullptr;
+  // extra interface vectors of BiCGSTAB / steepest descent (allocated on first use)
+  double *kv = nullptr, *ky = nullptr, *ks = nullptr, *kt = nullptr, *krs = nullptr;
   int maxnbo = 0, maxw = 0, maxNR = 0;
   int nref = 0;
   Profiler prof;
@@ -217,6 +219,7 @@ class Device {
   }
   void release() {
     nv_v0 = nv_v1 = nv_r = nullptr;
+    kv = ky = ks = kt = krs = nullptr;
     nv_off = nullptr;
     for (void* q : owned) cudaFreeAsync(q, st);
     owned.clear();
@@ -907,8 +910,101 @@ static double lanczos_max_eig(const vector<double>& d, const vector<double>& e) 
   return 0.5 * (lo + hi);
 }
 
+// BiCGSTAB (method 1, module_krylov.f90:948-1505) and steepest descent
+// (method 2, module_krylov.f90:1508-1840) on the interface problem, with the
+// same Schur and BDDC operators as PCG.  r holds g - S x0 with the fixed
+// dofs zeroed, normrhs its weighted norm (> 0).  Host-driven: each scalar is
+// read back once per use.
 template <typename T>
-static bool solve_impl(Solver& S, double tol, int maxit, int ndecrmax, int& num_iter, int& reason, double& cond) {
+static void other_krylov(Solver& S, int method, double normrhs, double tol, int maxit, int ndecrmax, int& num_iter,
+                         int& reason) {
+  Device& D = *S.dev;
+  cudaStream_t st = D.st;
+  auto& own = D.owned;
+  if (!D.kv) {
+    D.kv = dalloc<double>(D.n, own); D.ky = dalloc<double>(D.n, own); D.ks = dalloc<double>(D.n, own);
+    D.kt = dalloc<double>(D.n, own); D.krs = dalloc<double>(D.n, own);
+  }
+  const int nb = (D.n + 255) / 256;
+  const size_t bytes = (size_t)D.n * sizeof(double);
+  auto dot = [&](const double* a, const double* b) {
+    k_dot<<<D.npart, RT, 0, st>>>(D.n, a, b, D.wsum, D.part);
+    CKL();
+    return host_sum_parts(D);
+  };
+  auto axpy = [&](double a, const double* x, double* y) {
+    k_axpy<<<nb, 256, 0, st>>>(D.n, a, x, y);
+    CKL();
+  };
+  auto copy = [&](const double* x, double* y) { CK(cudaMemcpyAsync(y, x, bytes, cudaMemcpyDeviceToDevice, st)); };
+  int ndecr = 0;
+  double lastres = 1.0;
+  num_iter = 0;
+  reason = -1;
+  if (method == 2) {  // steepest descent: z = M r, x += alpha z, r -= alpha S z
+    for (int iter = 1; iter <= maxit; ++iter) {
+      launch_pc<T>(D, D.r, D.z, nullptr);
+      launch_schur<T>(D, D.z, D.ap, false, nullptr, nullptr);
+      const double alpha = dot(D.r, D.z) / dot(D.z, D.ap);
+      axpy(alpha, D.z, D.x);
+      axpy(-alpha, D.ap, D.r);
+      k_zero_fixed<<<nb, 256, 0, st>>>(D.n, D.fixed, D.r);
+      CKL();
+      const double relres = std::sqrt(dot(D.r, D.r)) / normrhs;
+      S.relres_history.push_back(relres);
+      num_iter = iter;
+      if (relres < tol) { reason = 0; return; }
+      if (iter == maxit) { reason = -1; return; }
+      // the reference stops with an error here (module_krylov.f90:1801-1812)
+      if (relres < lastres) ndecr = 0;
+      else if (++ndecr >= ndecrmax) { reason = -2; return; }
+      lastres = relres;
+    }
+    return;
+  }
+  // BiCGSTAB with the shadow residual r~ = r0
+  double rhoold = 1.0, alpha = 1.0, omega = 1.0;
+  CK(cudaMemsetAsync(D.kv, 0, bytes, st));
+  CK(cudaMemsetAsync(D.p, 0, bytes, st));
+  copy(D.r, D.krs);
+  for (int iter = 1; iter <= maxit; ++iter) {
+    const double rho = dot(D.r, D.krs);
+    const double beta = rho * alpha / (rhoold * omega);
+    axpy(-omega, D.kv, D.p);  // p = r + beta (p - omega v)
+    k_axpby<<<nb, 256, 0, st>>>(D.n, 1.0, D.r, beta, D.p);
+    CKL();
+    launch_pc<T>(D, D.p, D.ky, nullptr);                   // y = M p
+    launch_schur<T>(D, D.ky, D.kv, false, nullptr, nullptr);  // v = S y
+    alpha = rho / dot(D.kv, D.krs);
+    axpy(alpha, D.ky, D.x);
+    copy(D.r, D.ks);  // s = r - alpha v
+    axpy(-alpha, D.kv, D.ks);
+    double relres = std::sqrt(dot(D.ks, D.ks)) / normrhs;
+    num_iter = iter;
+    if (relres < tol) { S.relres_history.push_back(relres); reason = 0; return; }
+    if (relres < lastres) ndecr = 0;
+    else if (++ndecr >= ndecrmax) { S.relres_history.push_back(relres); reason = -2; return; }
+    lastres = relres;
+    launch_pc<T>(D, D.ks, D.z, nullptr);                   // z = M s
+    launch_schur<T>(D, D.z, D.kt, false, nullptr, nullptr);  // t = S z
+    omega = dot(D.kt, D.ks) / dot(D.kt, D.kt);
+    axpy(omega, D.z, D.x);
+    copy(D.ks, D.r);  // r = s - omega t
+    axpy(-omega, D.kt, D.r);
+    relres = std::sqrt(dot(D.r, D.r)) / normrhs;
+    S.relres_history.push_back(relres);
+    if (relres < tol) { reason = 0; return; }
+    if (iter == maxit) { reason = -1; return; }
+    if (relres < lastres) ndecr = 0;
+    else if (++ndecr >= ndecrmax) { reason = -2; return; }
+    lastres = relres;
+    rhoold = rho;
+  }
+}
+
+template <typename T>
+static bool solve_impl(Solver& S, int method, double tol, int maxit, int ndecrmax, int& num_iter, int& reason,
+                       double& cond) {
   Device& D = *S.dev;
   cudaStream_t st = D.st;
   auto& own = D.owned;
@@ -942,21 +1038,44 @@ static bool solve_impl(Solver& S, double tol, int maxit, int ndecrmax, int& num_
   // r = g with fixed interface dofs zeroed (module_krylov.f90:222-236)
   k_assemble_plain<<<(D.n + 255) / 256, 256, 0, st>>>(D.n, D.own, D.grep, D.fixed, D.r);
   CKL();
-  k_dot<<<D.npart, RT, 0, st>>>(D.n, D.r, D.r, D.wsum, D.part);
-  CKL();
-  double normrhs2 = host_sum_parts(D);
-  num_iter = 0; reason = 0; cond = 1.0;
+  num_iter = 0; reason = 0; cond = method == 0 ? 1.0 : -1.0;
   S.relres_history.clear();
   bool postprocess = true;
-  if (normrhs2 == 0.0) {
-    postprocess = false;
-  } else {
+  bool stalled = false;  // steepest descent without decrease: an error in the reference
+  if (method != 0) {
+    // BiCGSTAB / steepest descent: normalised by the norm of r = g - S x0
+    // (module_krylov.f90:1065-1113, 1620-1662)
     launch_schur<T>(D, D.x, D.ap, true, nullptr, nullptr);
     k_axpy<<<(D.n + 255) / 256, 256, 0, st>>>(D.n, -1.0, D.ap, D.r);
     CKL();
     k_dot<<<D.npart, RT, 0, st>>>(D.n, D.r, D.r, D.wsum, D.part);
     CKL();
-  CKL();
+    const double normrhs = std::sqrt(host_sum_parts(D));
+    if (normrhs == 0.0) {
+      postprocess = false;
+    } else {
+      double tl = wall_time();
+      D.prof.begin(PH_PCG, st);
+      other_krylov<T>(S, method, normrhs, tol, maxit, ndecrmax, num_iter, reason);
+      D.prof.end(PH_PCG, st);
+      S.stats.t_iterations = wall_time() - tl;
+      stalled = method == 2 && reason == -2;
+      if (stalled) postprocess = false;
+    }
+  }
+  double normrhs2 = 0.0;
+  if (method == 0) {
+    k_dot<<<D.npart, RT, 0, st>>>(D.n, D.r, D.r, D.wsum, D.part);
+    CKL();
+    normrhs2 = host_sum_parts(D);
+    if (normrhs2 == 0.0) postprocess = false;
+  }
+  if (method == 0 && normrhs2 != 0.0) {
+    launch_schur<T>(D, D.x, D.ap, true, nullptr, nullptr);
+    k_axpy<<<(D.n + 255) / 256, 256, 0, st>>>(D.n, -1.0, D.ap, D.r);
+    CKL();
+    k_dot<<<D.npart, RT, 0, st>>>(D.n, D.r, D.r, D.wsum, D.part);
+    CKL();
     double normres0 = std::sqrt(host_sum_parts(D));
     if (normres0 == 0.0) {
       postprocess = false;
@@ -1047,6 +1166,9 @@ static bool solve_impl(Solver& S, double tol, int maxit, int ndecrmax, int& num_
   S.stats.t_solve = wall_time() - t0;
   S.stats.num_iter = num_iter;
   S.stats.launches_solve = (double)(g_launches - launches0);
+  if (stalled)
+    throw Error{ERR_NUMERIC, "steepest descent: residual did not decrease for " + std::to_string(ndecrmax) +
+                                 " iterations"};
   return true;
 }
 
@@ -1143,11 +1265,11 @@ bool device_new_data(Solver& S, Error& err) {
   return true;
 }
 
-bool device_solve(Solver& S, double tol, int maxit, int ndecrmax, int& num_iter, int& reason, double& cond,
-                  Error& err) {
+bool device_solve(Solver& S, int method, double tol, int maxit, int ndecrmax, int& num_iter, int& reason,
+                  double& cond, Error& err) {
   try {
-    if (S.dev->mixed) return solve_impl<float>(S, tol, maxit, ndecrmax, num_iter, reason, cond);
-    return solve_impl<double>(S, tol, maxit, ndecrmax, num_iter, reason, cond);
+    if (S.dev->mixed) return solve_impl<float>(S, method, tol, maxit, ndecrmax, num_iter, reason, cond);
+    return solve_impl<double>(S, method, tol, maxit, ndecrmax, num_iter, reason, cond);
   } catch (Error& e) {
     err = e;
     return false;

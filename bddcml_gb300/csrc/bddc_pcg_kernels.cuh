@@ -390,6 +390,18 @@ __global__ void k_axpy(int n, double a, const double* __restrict__ x, double* __
   if (g < n) y[g] += a * x[g];
 }
 
+// y = a x + b y
+__global__ void k_axpby(int n, double a, const double* __restrict__ x, double b, double* __restrict__ y) {
+  int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g < n) y[g] = a * x[g] + b * y[g];
+}
+
+// v = 0 at the fixed interface dofs (dd_fix_bc_interface_dual, module_dd.f90:3468-3505)
+__global__ void k_zero_fixed(int n, const int* __restrict__ fixed, double* __restrict__ v) {
+  int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g < n && fixed[g]) v[g] = 0.0;
+}
+
 // interior values u_o = v - X(:, 0:ni) x_s  (module_dd.f90:6811-6932): 64
 // rows per CTA, the gathered interface solution staged once in shared memory
 // as double-float, X read as its double-float pair

@@ -82,8 +82,13 @@ void bddcml_setup_preconditioner_c(int *matrixtype, int *use_defaults_int, int *
                                    int *weights_type);
 
 /* replaces bddcml_solve_c, src/bddcml_interface_c.h:37-39 (module_bddcml.f90:459-567).
- * method 0 (PCG) is implemented; -1 selects the reference defaults, whose
- * method is BiCGSTAB (module_bddcml.f90:515) and is reported unsupported. */
+ * method 0 PCG (with the Lanczos condition estimate), 1 BiCGSTAB, 2 steepest
+ * descent; -1 takes the reference defaults (module_bddcml.f90:515-520):
+ * BiCGSTAB, tol 1e-6, maxit 1000, ndecrmax 30, ignoring the passed values.
+ * condition_number is -1 for methods 1 and 2.  method 5 (direct solve) sets
+ * BDDCML_ERR_UNSUPPORTED, any other value BDDCML_ERR_ARGUMENT.  A steepest
+ * descent that stalls for ndecrmax iterations sets BDDCML_ERR_NUMERIC (the
+ * reference stops with an error there, module_krylov.f90:1801-1812). */
 void bddcml_solve_c(int *comm_all, int *method, double *tol, int *maxit, int *ndecrmax,
                     int *recycling_int, int *max_number_of_stored_vectors,
                     int *num_iter, int *converged_reason, double *condition_number);

@@ -26,6 +26,7 @@
 //   exchange (upload/download) ..... module_dd.f90:11236-11551
 //   BDDC apply ..................... module_levels.f90:3627-4346
 //   PCG + Lanczos estimate ......... module_krylov.f90:48-945, 2061-2118
+//   BiCGSTAB, steepest descent ..... module_krylov.f90:948-1505, 1508-1840
 //   coarse problem ................. module_levels.f90:3001-3170, 4029-4061
 //
 // The direct solver MUMPS is replaced by band Cholesky factorisations in the
@@ -1188,6 +1189,8 @@ static double tridiag_max_eig(const vector<double>& d, const vector<double>& e) 
   return 0.5 * (lo + hi);
 }
 
+static void postprocess(Oracle& o, vector<vector<double>>& x);
+
 int oracle_solve(void* h, double tol, int maxit, int ndecrmax, int* num_iter, int* converged_reason,
                  double* condition_number) {
   auto* o = static_cast<Oracle*>(h);
@@ -1251,7 +1254,15 @@ int oracle_solve(void* h, double tol, int maxit, int ndecrmax, int* num_iter, in
       *condition_number = 1.0;
     }
   }
-  // post-processing (module_levels.f90:4510-4576, module_dd.f90:6811-6932)
+  postprocess(*o, x);
+  return 0;
+}
+
+// interior values from the interface solution x
+// (module_levels.f90:4510-4576, module_dd.f90:6811-6932)
+static void postprocess(Oracle& oo, vector<vector<double>>& x) {
+  Oracle* o = &oo;
+  int nsub = o->nsub;
 #pragma omp parallel for schedule(dynamic) num_threads(o->nthreads)
   for (int s = 0; s < nsub; ++s) {
     auto& S = o->subs[s];
@@ -1271,6 +1282,105 @@ int oracle_solve(void* h, double tol, int maxit, int ndecrmax, int* num_iter, in
     for (int i = 0; i < S.ndofi; ++i) u[S.iivsvn[i]] += x[s][i];
     S.sol = u;
   }
+}
+
+// BiCGSTAB (method 1, module_krylov.f90:948-1505) and steepest descent
+// (method 2, module_krylov.f90:1508-1840); method -1 takes the defaults of
+// module_bddcml.f90:515-520 (BiCGSTAB, tol 1e-6, maxit 1000, ndecrmax 30).
+// Residuals are relative to the norm of r0 = g - S x0.  cond is -1: neither
+// method estimates it.  Returns 2 when steepest descent stalls for ndecrmax
+// iterations, which the reference treats as an error (module_krylov.f90:1801-1812).
+int oracle_solve_method(void* h, int method, double tol, int maxit, int ndecrmax, int* num_iter,
+                        int* converged_reason, double* condition_number) {
+  if (method == 0) return oracle_solve(h, tol, maxit, ndecrmax, num_iter, converged_reason, condition_number);
+  auto* o = static_cast<Oracle*>(h);
+  if (method == -1) { method = 1; tol = 1e-6; maxit = 1000; ndecrmax = 30; }
+  if (method != 1 && method != 2) { o->err = "unknown method"; return 1; }
+  if (!o->setup_done) { o->err = "setup not done"; return 1; }
+  const int nsub = o->nsub;
+  vector<vector<double>> x(nsub), r(nsub), v(nsub), z(nsub);
+  for (int s = 0; s < nsub; ++s) {
+    auto& S = o->subs[s];
+    vector<double> sol = S.sol;
+    if (S.bc_present) for (int i = 0; i < S.ndof; ++i) if (S.ifix[i]) sol[i] = S.fixv[i];
+    x[s].resize(S.ndofi);
+    for (int i = 0; i < S.ndofi; ++i) x[s][i] = sol[S.iivsvn[i]];
+    r[s] = S.g;
+  }
+  fix_bc_dual(*o, r);
+  sm_apply(*o, x, v);
+  for (int s = 0; s < nsub; ++s) for (size_t i = 0; i < r[s].size(); ++i) r[s][i] -= v[s][i];
+  fix_bc_dual(*o, r);
+  o->relres_hist.clear();
+  *num_iter = 0; *converged_reason = -1; *condition_number = -1.0;
+  const double normrhs = std::sqrt(dotw(*o, r, r));
+  if (normrhs == 0.0) { *converged_reason = 0; return 0; }
+  auto axpy = [&](double a, vector<vector<double>>& xx, vector<vector<double>>& yy) {
+    for (int s = 0; s < nsub; ++s) for (size_t i = 0; i < yy[s].size(); ++i) yy[s][i] += a * xx[s][i];
+  };
+  int ndecr = 0;
+  double lastres = 1.0;
+  if (method == 2) {
+    vector<vector<double>> az(nsub);
+    for (int iter = 1; iter <= maxit; ++iter) {
+      pc_apply(*o, r, z);
+      sm_apply(*o, z, az);
+      const double alpha = dotw(*o, r, z) / dotw(*o, z, az);
+      axpy(alpha, z, x);
+      axpy(-alpha, az, r);
+      fix_bc_dual(*o, r);
+      const double relres = std::sqrt(dotw(*o, r, r)) / normrhs;
+      o->relres_hist.push_back(relres);
+      *num_iter = iter;
+      if (relres < tol) { *converged_reason = 0; break; }
+      if (iter == maxit) { *converged_reason = -1; break; }
+      if (relres < lastres) ndecr = 0;
+      else if (++ndecr >= ndecrmax) {
+        *converged_reason = -2;
+        o->err = "steepest descent: residual did not decrease for ndecrmax iterations";
+        return 2;
+      }
+      lastres = relres;
+    }
+    postprocess(*o, x);
+    return 0;
+  }
+  vector<vector<double>> p(nsub), y(nsub), sv(nsub), t(nsub), rs = r;
+  for (int s = 0; s < nsub; ++s) { v[s].assign(r[s].size(), 0.0); p[s].assign(r[s].size(), 0.0); }
+  double rhoold = 1.0, alpha = 1.0, omega = 1.0;
+  for (int iter = 1; iter <= maxit; ++iter) {
+    const double rho = dotw(*o, r, rs);
+    const double beta = rho * alpha / (rhoold * omega);
+    for (int s = 0; s < nsub; ++s)
+      for (size_t i = 0; i < p[s].size(); ++i) p[s][i] = r[s][i] + beta * (p[s][i] - omega * v[s][i]);
+    pc_apply(*o, p, y);
+    sm_apply(*o, y, v);
+    alpha = rho / dotw(*o, v, rs);
+    axpy(alpha, y, x);
+    sv = r;
+    axpy(-alpha, v, sv);
+    double relres = std::sqrt(dotw(*o, sv, sv)) / normrhs;
+    *num_iter = iter;
+    if (relres < tol) { o->relres_hist.push_back(relres); *converged_reason = 0; break; }
+    if (relres < lastres) ndecr = 0;
+    else if (++ndecr >= ndecrmax) { o->relres_hist.push_back(relres); *converged_reason = -2; break; }
+    lastres = relres;
+    pc_apply(*o, sv, z);
+    sm_apply(*o, z, t);
+    omega = dotw(*o, t, sv) / dotw(*o, t, t);
+    axpy(omega, z, x);
+    r = sv;
+    axpy(-omega, t, r);
+    relres = std::sqrt(dotw(*o, r, r)) / normrhs;
+    o->relres_hist.push_back(relres);
+    if (relres < tol) { *converged_reason = 0; break; }
+    if (iter == maxit) { *converged_reason = -1; break; }
+    if (relres < lastres) ndecr = 0;
+    else if (++ndecr >= ndecrmax) { *converged_reason = -2; break; }
+    lastres = relres;
+    rhoold = rho;
+  }
+  postprocess(*o, x);
   return 0;
 }
 

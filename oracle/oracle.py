@@ -36,6 +36,8 @@ def lib():
         L.oracle_setup.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int]
         L.oracle_solve.argtypes = [C.c_void_p, C.c_double, C.c_int, C.c_int,
                                    C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_double)]
+        L.oracle_solve_method.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_int, C.c_int,
+                                          C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_double)]
         L.oracle_download.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int]
         L.oracle_stats.argtypes = [C.c_void_p, C.c_void_p]
         L.oracle_sub_stats.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
@@ -107,9 +109,11 @@ class Oracle:
         if rc != 0:
             raise RuntimeError(self.L.oracle_error(self.h).decode())
 
-    def solve(self, tol=1e-8, maxit=500, ndecrmax=50):
+    def solve(self, tol=1e-8, maxit=500, ndecrmax=50, method=0):
+        """method 0 PCG, 1 BiCGSTAB, 2 steepest descent, -1 reference defaults."""
         it, reason, cond = C.c_int(), C.c_int(), C.c_double()
-        rc = self.L.oracle_solve(self.h, tol, maxit, ndecrmax, C.byref(it), C.byref(reason), C.byref(cond))
+        rc = self.L.oracle_solve_method(self.h, method, tol, maxit, ndecrmax, C.byref(it), C.byref(reason),
+                                        C.byref(cond))
         if rc != 0:
             raise RuntimeError(self.L.oracle_error(self.h).decode())
         return it.value, reason.value, cond.value

@@ -180,3 +180,43 @@ def test_oracle_elasticity_matches_direct(oracle_mod):
     u = o.global_solution()
     ud = direct_solution(prob)
     assert np.linalg.norm(u - ud) / np.linalg.norm(ud) < 1e-9
+
+
+@pytest.mark.parametrize("method,tol", [(1, 1e-10), (2, 1e-9)])
+def test_oracle_bicgstab_and_steepest_descent_match_direct(oracle_mod, method, tol):
+    """BiCGSTAB (module_krylov.f90:948-1505) and steepest descent
+    (module_krylov.f90:1508-1840) from a non-zero initial guess (the Dirichlet
+    values) reach the direct solution; neither estimates a condition number."""
+    from bddcml_gb300 import problems
+    from newdata_util import changed_data, direct_solution
+    prob = changed_data(problems.poisson_on_cube(4, 3), seed=3)
+    o = oracle_mod.Oracle(prob)
+    o.setup(1, 1, 0)
+    it, reason, cond = o.solve(tol, 400, 50, method=method)
+    assert reason == 0 and cond == -1.0 and 0 < it < 400
+    u = o.global_solution()
+    ud = direct_solution(prob)
+    assert np.linalg.norm(u - ud) / np.linalg.norm(ud) < 1e3 * tol
+
+
+def test_oracle_default_method_is_bicgstab_with_default_parameters(oracle_mod):
+    """method -1 ignores the passed tol/maxit/ndecrmax (module_bddcml.f90:515-520)."""
+    from bddcml_gb300 import problems
+    prob = problems.poisson_on_cube(4, 3)
+    o = oracle_mod.Oracle(prob)
+    o.setup(1, 1, 0)
+    it_d, reason_d, cond_d = o.solve(1e-14, 2, 1, method=-1)
+    hist_d = o.relres_history()
+    o2 = oracle_mod.Oracle(prob)
+    o2.setup(1, 1, 0)
+    it_b, reason_b, _ = o2.solve(1e-6, 1000, 30, method=1)
+    assert (it_d, reason_d, cond_d) == (it_b, 0, -1.0) and reason_b == 0
+    assert hist_d[-1] < 1e-6 and np.allclose(hist_d, o2.relres_history(), rtol=0, atol=1e-15)
+
+
+def test_oracle_bicgstab_maxit_reason(oracle_mod):
+    from bddcml_gb300 import problems
+    o = oracle_mod.Oracle(problems.poisson_on_cube(5, 4))
+    o.setup(1, 1, 0)
+    it, reason, cond = o.solve(1e-14, 2, 50, method=1)
+    assert it == 2 and reason == -1
