@@ -217,6 +217,35 @@ def lognormal_kappa(n_el_edge: int, sigma: float, seed: int) -> np.ndarray:
     return np.exp(sigma * rng.standard_normal(n_el_edge ** 3))
 
 
+def channel_kappa(n_el_edge: int, nchannels: int = 20, width: int = 2, contrast: float = 1e4,
+                  sigma: float = 2.0, seed: int = 17) -> np.ndarray:
+    """Per-element coefficient exp(sigma * g), g iid N(0, 1) from `seed`, with
+    `nchannels` axis-aligned channels of coefficient `contrast` and a square
+    cross-section of `width` elements crossing the whole cube at random
+    positions (drawn from seed + 1).  Elements are numbered x fastest."""
+    kappa = np.exp(sigma * np.random.default_rng(seed).standard_normal(n_el_edge ** 3))
+    rng = np.random.default_rng(seed + 1)
+    k3 = kappa.reshape(n_el_edge, n_el_edge, n_el_edge)  # [z, y, x]
+    w = min(width, n_el_edge)
+    for _ in range(nchannels):
+        axis = int(rng.integers(0, 3))
+        p, q = (int(v) for v in rng.integers(0, n_el_edge - w + 1, size=2))
+        if axis == 0:      # along x: fixed (y, z)
+            k3[q:q + w, p:p + w, :] = contrast
+        elif axis == 1:    # along y: fixed (x, z)
+            k3[q:q + w, :, p:p + w] = contrast
+        else:              # along z: fixed (x, y)
+            k3[:, q:q + w, p:p + w] = contrast
+    return kappa
+
+
+def uniform_boxes(n_el_edge: int, nsub_edge: int):
+    """The nsub_edge^3 equal boxes of the cube (as poisson_on_cube splits it)."""
+    cuts = [round(k * n_el_edge / nsub_edge) for k in range(nsub_edge + 1)]
+    return [(np.array([cuts[i], cuts[j], cuts[k]]), np.array([cuts[i + 1], cuts[j + 1], cuts[k + 1]]))
+            for k in range(nsub_edge) for j in range(nsub_edge) for i in range(nsub_edge)]
+
+
 def global_matrix_and_rhs(prob: Problem):
     """Assembled global stiffness matrix and load vector with the Dirichlet
     rows/columns eliminated (scipy CSR), used as an independent check."""

@@ -219,6 +219,14 @@ struct Oracle {
   int ncorner = 0, nedge = 0, nface = 0, ndofc = 0;
   vector<double> coarse_chol;  // dense Cholesky of the coarse matrix
   vector<int> ncdof_of_cnode;  // nndfc
+  // adaptive face constraints (module_adaptivity.f90)
+  bool adaptive = false;
+  double adaptive_tau = 1.5;           // threshold_eigval_default, module_adaptivity.f90:30
+  vector<std::array<int, 3>> pairs;    // (face global cnode, isub, jsub), 0-based subdomains
+  vector<vector<double>> pair_eigs;    // largest eigenvalues per pair, descending
+  vector<int> pair_nadaptive;          // eigenvalues >= tau per pair
+  vector<int> face_ncdof;              // constraints per pair face after orthogonalisation
+  double adaptivity_est = -1.0;
   std::string err;
   // PCG results
   vector<double> relres_hist;
@@ -720,6 +728,163 @@ static void load_arithmetic_constraints(Sub& S, int itype) {
   }
 }
 
+// ================================================================ dense helpers for adaptivity
+// Symmetric eigen-decomposition of a (n x n, row-major, overwritten): Householder
+// reduction to tridiagonal form, then implicit QR steps with Wilkinson shifts
+// (the textbook method of LAPACK's DSYEV/DSYGV, used by module_adaptivity.f90
+// for dense eigenproblems).  Eigenvalues ascending in w; z(i, k) = z[i*n + k]
+// holds the k-th eigenvector.
+static void sym_eig(int n, vector<double>& a, vector<double>& w, vector<double>& z) {
+  z.assign((size_t)n * n, 0.0);
+  for (int i = 0; i < n; ++i) z[(size_t)i * n + i] = 1.0;
+  vector<double> v(n), p(n);
+  for (int k = 0; k + 2 < n; ++k) {
+    const int m = n - k - 1;  // size of the trailing block
+    double nx = 0.0;
+    for (int i = 0; i < m; ++i) nx += a[(size_t)(k + 1 + i) * n + k] * a[(size_t)(k + 1 + i) * n + k];
+    nx = std::sqrt(nx);
+    if (nx == 0.0) continue;
+    const double x0 = a[(size_t)(k + 1) * n + k];
+    const double alpha = x0 > 0 ? -nx : nx;
+    for (int i = 0; i < m; ++i) v[i] = a[(size_t)(k + 1 + i) * n + k];
+    v[0] -= alpha;
+    double nv = 0.0;
+    for (int i = 0; i < m; ++i) nv += v[i] * v[i];
+    nv = std::sqrt(nv);
+    if (nv == 0.0) continue;
+    for (int i = 0; i < m; ++i) v[i] /= nv;
+    // trailing block A <- H A H with H = I - 2 v v^T
+    double kk = 0.0;
+    for (int i = 0; i < m; ++i) {
+      double t = 0.0;
+      for (int j = 0; j < m; ++j) t += a[(size_t)(k + 1 + i) * n + k + 1 + j] * v[j];
+      p[i] = t;
+      kk += v[i] * t;
+    }
+    for (int i = 0; i < m; ++i) p[i] -= kk * v[i];
+    for (int i = 0; i < m; ++i)
+      for (int j = 0; j < m; ++j) a[(size_t)(k + 1 + i) * n + k + 1 + j] -= 2.0 * (v[i] * p[j] + p[i] * v[j]);
+    a[(size_t)(k + 1) * n + k] = a[(size_t)k * n + k + 1] = alpha;
+    for (int i = 1; i < m; ++i) a[(size_t)(k + 1 + i) * n + k] = a[(size_t)k * n + k + 1 + i] = 0.0;
+    // z <- z H on columns k+1 ..
+    for (int r = 0; r < n; ++r) {
+      double t = 0.0;
+      for (int j = 0; j < m; ++j) t += z[(size_t)r * n + k + 1 + j] * v[j];
+      for (int j = 0; j < m; ++j) z[(size_t)r * n + k + 1 + j] -= 2.0 * t * v[j];
+    }
+  }
+  vector<double> d(n), e(std::max(1, n - 1), 0.0);
+  for (int i = 0; i < n; ++i) d[i] = a[(size_t)i * n + i];
+  for (int i = 0; i + 1 < n; ++i) e[i] = a[(size_t)i * n + i + 1];
+  const double eps = 2.220446049250313e-16;
+  int hi = n - 1, guard = 0;
+  while (hi > 0) {
+    if (std::fabs(e[hi - 1]) <= eps * (std::fabs(d[hi - 1]) + std::fabs(d[hi]))) { e[hi - 1] = 0.0; --hi; continue; }
+    int lo = hi - 1;
+    while (lo > 0 && std::fabs(e[lo - 1]) > eps * (std::fabs(d[lo - 1]) + std::fabs(d[lo]))) --lo;
+    if (lo > 0) e[lo - 1] = 0.0;
+    if (++guard > 60 * n) throw std::runtime_error("symmetric eigen-decomposition did not converge");
+    // Wilkinson shift from the trailing 2x2 block
+    const double dl = 0.5 * (d[hi - 1] - d[hi]);
+    const double b = e[hi - 1];
+    const double mu = d[hi] - b * b / (dl + (dl >= 0 ? 1.0 : -1.0) * std::hypot(dl, b));
+    double x = d[lo] - mu, zz = e[lo];
+    for (int k = lo; k < hi; ++k) {
+      const double r = std::hypot(x, zz);
+      const double c = r == 0.0 ? 1.0 : x / r, sn = r == 0.0 ? 0.0 : zz / r;
+      if (k > lo) e[k - 1] = r;
+      const double ak = d[k], ak1 = d[k + 1], bk = e[k];
+      d[k] = c * c * ak + 2.0 * c * sn * bk + sn * sn * ak1;
+      d[k + 1] = sn * sn * ak - 2.0 * c * sn * bk + c * c * ak1;
+      e[k] = c * sn * (ak1 - ak) + (c * c - sn * sn) * bk;
+      if (k + 1 < hi) {  // bulge below the block
+        x = e[k];
+        zz = sn * e[k + 1];
+        e[k + 1] *= c;
+      }
+      for (int r2 = 0; r2 < n; ++r2) {
+        const double zk = z[(size_t)r2 * n + k], zk1 = z[(size_t)r2 * n + k + 1];
+        z[(size_t)r2 * n + k] = c * zk + sn * zk1;
+        z[(size_t)r2 * n + k + 1] = -sn * zk + c * zk1;
+      }
+    }
+  }
+  // sort ascending
+  vector<int> ord(n);
+  std::iota(ord.begin(), ord.end(), 0);
+  std::sort(ord.begin(), ord.end(), [&](int x1, int x2) { return d[x1] < d[x2]; });
+  w.resize(n);
+  vector<double> zs((size_t)n * n);
+  for (int k = 0; k < n; ++k) {
+    w[k] = d[ord[k]];
+    for (int r2 = 0; r2 < n; ++r2) zs[(size_t)r2 * n + k] = z[(size_t)r2 * n + ord[k]];
+  }
+  z.swap(zs);
+}
+
+// Householder QR with column pivoting of the nrow x ncol matrix m (column-major,
+// overwritten), then the first nvalid columns of Q, where nvalid counts the
+// leading |R_ii| >= 0.01 |R_11| (dd_orthogonalize_constraints, module_dd.f90:4637-4760,
+// DGEQP3 + DORGQR).  Returns Q (nrow x nvalid, column-major).
+static vector<double> pivoted_orthonormal_basis(int nrow, int ncol, vector<double> m, int& nvalid) {
+  const int kmax = std::min(nrow, ncol);
+  vector<vector<double>> refl;
+  vector<double> rdiag;
+  vector<int> piv(ncol);
+  std::iota(piv.begin(), piv.end(), 0);
+  for (int k = 0; k < kmax; ++k) {
+    int best = k;
+    double bn = -1.0;
+    for (int c = k; c < ncol; ++c) {
+      double t = 0.0;
+      for (int r = k; r < nrow; ++r) t += m[(size_t)c * nrow + r] * m[(size_t)c * nrow + r];
+      if (t > bn) { bn = t; best = c; }
+    }
+    if (best != k) {
+      for (int r = 0; r < nrow; ++r) std::swap(m[(size_t)k * nrow + r], m[(size_t)best * nrow + r]);
+      std::swap(piv[k], piv[best]);
+    }
+    double nx = std::sqrt(std::max(0.0, bn));
+    vector<double> v(nrow, 0.0);
+    if (nx == 0.0) { rdiag.push_back(0.0); refl.push_back(v); continue; }
+    const double x0 = m[(size_t)k * nrow + k];
+    const double alpha = x0 > 0 ? -nx : nx;
+    for (int r = k; r < nrow; ++r) v[r] = m[(size_t)k * nrow + r];
+    v[k] -= alpha;
+    double nv = 0.0;
+    for (int r = k; r < nrow; ++r) nv += v[r] * v[r];
+    nv = std::sqrt(nv);
+    if (nv > 0) for (int r = k; r < nrow; ++r) v[r] /= nv;
+    for (int c = k; c < ncol; ++c) {
+      double t = 0.0;
+      for (int r = k; r < nrow; ++r) t += v[r] * m[(size_t)c * nrow + r];
+      for (int r = k; r < nrow; ++r) m[(size_t)c * nrow + r] -= 2.0 * t * v[r];
+    }
+    rdiag.push_back(m[(size_t)k * nrow + k]);
+    refl.push_back(v);
+  }
+  nvalid = 0;
+  if (kmax > 0 && std::fabs(rdiag[0]) > 1e-12) {
+    const double th = 0.01 * std::fabs(rdiag[0]);
+    for (int i = 0; i < kmax; ++i) {
+      if (std::fabs(rdiag[i]) < th) break;
+      nvalid = i + 1;
+    }
+  }
+  vector<double> q((size_t)nrow * nvalid, 0.0);
+  for (int c = 0; c < nvalid; ++c) {
+    double* col = &q[(size_t)c * nrow];
+    col[c] = 1.0;
+    for (int k = nvalid - 1; k >= 0; --k) {
+      const auto& v = refl[k];
+      double t = 0.0;
+      for (int r = k; r < nrow; ++r) t += v[r] * col[r];
+      for (int r = k; r < nrow; ++r) col[r] -= 2.0 * t * v[r];
+    }
+  }
+  return q;
+}
+
 // ================================================================ API
 extern "C" {
 
@@ -818,6 +983,325 @@ static void build_exchange_lists(Oracle& o) {
   }
 }
 
+// global coarse dofs of every coarse node and the constraint rows of every
+// subdomain in CSR over its interface dofs (module_dd.f90:11011-11235, 5018-5144)
+static void number_constraints(Oracle& o) {
+  int ncnode = o.ncorner + o.nedge + o.nface;
+  o.ncdof_of_cnode.assign(ncnode, 0);
+  for (auto& S : o.subs)
+    for (auto& cn : S.cnodes) o.ncdof_of_cnode[cn.global_cnode - 1] = cn.ncdof;
+  vector<int> kdofc(ncnode + 1, 0);
+  for (int c = 0; c < ncnode; ++c) kdofc[c + 1] = kdofc[c] + o.ncdof_of_cnode[c];
+  o.ndofc = kdofc[ncnode];
+  for (auto& S : o.subs) {
+    S.crow_ptr.assign(1, 0); S.crow_col.clear(); S.crow_val.clear(); S.indrowc.clear();
+    for (auto& cn : S.cnodes) {
+      cn.igcdof.clear();
+      for (int d = 0; d < cn.ncdof; ++d) cn.igcdof.push_back(kdofc[cn.global_cnode - 1] + d + 1);
+      if (!cn.used) continue;
+      for (int r = 0; r < cn.ncdof; ++r) {
+        for (int v = 0; v < cn.nvar; ++v) {
+          double val = cn.matrix[(size_t)r * cn.nvar + v];
+          if (std::fabs(val) > 0.0) { S.crow_col.push_back(cn.ivsivn[v]); S.crow_val.push_back(val); }
+        }
+        S.crow_ptr.push_back((int)S.crow_col.size());
+        S.indrowc.push_back(cn.igcdof[r]);
+      }
+    }
+    S.nconstr = (int)S.indrowc.size();
+  }
+}
+
+static void coarse_space(Oracle& o);
+
+// explicit Schur complement of a subdomain, ndofi x ndofi row-major
+// (dd_prepare_explicit_schur; the same operator as dd_multiply_by_schur)
+static vector<double> dense_schur(Sub& S) {
+  const int ni = S.ndofi;
+  vector<vector<std::pair<int, double>>> a12c(ni);  // A_oi by interface column
+  for (int io = 0; io < S.ndofo; ++io)
+    for (int k = S.a12_ptr[io]; k < S.a12_ptr[io + 1]; ++k) a12c[S.a12_col[k]].push_back({io, S.a12_val[k]});
+  vector<double> sd((size_t)ni * ni, 0.0), aux(S.ndofo);
+  for (int c = 0; c < ni; ++c) {
+    for (int k = S.a22_ptr[c]; k < S.a22_ptr[c + 1]; ++k) sd[(size_t)S.a22_col[k] * ni + c] += S.a22_val[k];
+    if (S.ndofo == 0 || a12c[c].empty()) continue;
+    std::fill(aux.begin(), aux.end(), 0.0);
+    for (auto& e : a12c[c]) aux[e.first] = e.second;
+    S.a11.solve(aux.data());
+    for (int io = 0; io < S.ndofo; ++io)
+      for (int k = S.a12_ptr[io]; k < S.a12_ptr[io + 1]; ++k) sd[(size_t)S.a12_col[k] * ni + c] -= S.a12_val[k] * aux[io];
+  }
+  for (int r = 0; r < ni; ++r)
+    for (int c = r + 1; c < ni; ++c) {
+      double m = 0.5 * (sd[(size_t)r * ni + c] + sd[(size_t)c * ni + r]);
+      sd[(size_t)r * ni + c] = sd[(size_t)c * ni + r] = m;
+    }
+  return sd;
+}
+
+// M <- P M P with P = I - Q Q^T, Q (n x m) column-major orthonormal
+static void project_both(int n, vector<double>& M, const vector<double>& Q, int m) {
+  if (m == 0) return;
+  vector<double> mq((size_t)n * m, 0.0);  // M Q, row-major n x m
+  for (int r = 0; r < n; ++r)
+    for (int k = 0; k < m; ++k) {
+      double t = 0.0;
+      for (int c = 0; c < n; ++c) t += M[(size_t)r * n + c] * Q[(size_t)k * n + c];
+      mq[(size_t)r * m + k] = t;
+    }
+  vector<double> qmq((size_t)m * m, 0.0);  // Q^T M Q
+  for (int a = 0; a < m; ++a)
+    for (int b = 0; b < m; ++b) {
+      double t = 0.0;
+      for (int r = 0; r < n; ++r) t += Q[(size_t)a * n + r] * mq[(size_t)r * m + b];
+      qmq[(size_t)a * m + b] = t;
+    }
+  // P M P = M - MQ Q^T - Q (MQ)^T + Q (Q^T M Q) Q^T   (M symmetric)
+  vector<double> qq((size_t)n * m, 0.0);  // Q (Q^T M Q), row-major n x m
+  for (int r = 0; r < n; ++r)
+    for (int b = 0; b < m; ++b) {
+      double t = 0.0;
+      for (int a = 0; a < m; ++a) t += Q[(size_t)a * n + r] * qmq[(size_t)a * m + b];
+      qq[(size_t)r * m + b] = t;
+    }
+  for (int r = 0; r < n; ++r)
+    for (int c = 0; c < n; ++c) {
+      double t = 0.0;
+      for (int k = 0; k < m; ++k)
+        t += -mq[(size_t)r * m + k] * Q[(size_t)k * n + c] - Q[(size_t)k * n + r] * mq[(size_t)c * m + k] +
+             qq[(size_t)r * m + k] * Q[(size_t)k * n + c];
+      M[(size_t)r * n + c] += t;
+    }
+}
+
+// Adaptive face constraints (adaptivity_solve_eigenvectors, module_adaptivity.f90:296-2514,
+// with the pair operators of adaptivity_mvecmult, :2560-3023).  For each face shared by
+// subdomains i and j, on the space of both interfaces (n = ndofi_i + ndofi_j):
+//   D  = [C_i  -C_j] on the coarse dofs common to i and j; P the orthogonal projection onto null(D)
+//   E  = weighted average on the common dofs (weights rho_i/(rho_i + rho_j)), I - E zero elsewhere
+//   A  = P (I-E)^T S (I-E) P,   B = P S P + t (I - P),  S = diag(S_i, S_j), t = max |diag S|
+// and the largest min(10, ncommon_dofs - ncommon_coarse) eigenvalues of A v = lambda B v are
+// computed exactly (B restricted to its range: null(S) within null(D) carries no information).
+// Eigenvectors with lambda >= tau give constraints A v restricted to the face dofs; each face's
+// rows [arithmetic average; adaptive] are orthonormalised by pivoted QR with the 1 % rule
+// (dd_orthogonalize_constraints, module_dd.f90:4637-4760) and given to both subdomains.
+static void adaptivity(Oracle& o, const vector<vector<double>>& rho) {
+  const int nsub = o.nsub;
+  number_constraints(o);
+  vector<vector<double>> sd(nsub);
+  std::string errs;
+#pragma omp parallel for schedule(dynamic) num_threads(o.nthreads)
+  for (int s = 0; s < nsub; ++s) sd[s] = dense_schur(o.subs[s]);
+  // pairs = faces, ordered by global coarse node (dd_create_pairs, module_dd.f90:10785-11008)
+  std::map<int, vector<std::pair<int, int>>> faces;
+  for (int s = 0; s < nsub; ++s)
+    for (int c = 0; c < (int)o.subs[s].cnodes.size(); ++c)
+      if (o.subs[s].cnodes[c].itype == 1) faces[o.subs[s].cnodes[c].global_cnode].push_back({s, c});
+  o.pairs.clear();
+  vector<std::array<int, 2>> pcn;
+  for (auto& f : faces) {
+    if (f.second.size() != 2) throw std::runtime_error("a face not shared by exactly two subdomains");
+    o.pairs.push_back({f.first, f.second[0].first, f.second[1].first});
+    pcn.push_back({f.second[0].second, f.second[1].second});
+  }
+  const int npair = (int)o.pairs.size();
+  o.pair_eigs.assign(npair, {});
+  o.pair_nadaptive.assign(npair, 0);
+  o.face_ncdof.assign(npair, 0);
+  vector<vector<double>> cons(npair);  // adaptive rows over the face dofs of the first subdomain
+  vector<double> est_loc(npair, 0.0);
+#pragma omp parallel for schedule(dynamic) num_threads(o.nthreads)
+  for (int p = 0; p < npair; ++p) {
+    try {
+      const int si = o.pairs[p][1], sj = o.pairs[p][2];
+      Sub& A = o.subs[si];
+      Sub& Bq = o.subs[sj];
+      const int ni = A.ndofi, nj = Bq.ndofi, n = ni + nj;
+      // common interface dofs
+      std::unordered_map<int, int> jnode;
+      for (int i = 0; i < Bq.nnodi; ++i) jnode[Bq.isngn[Bq.iin[i]]] = i;
+      vector<std::array<int, 2>> cd;
+      vector<double> wa, wb;
+      for (int i = 0; i < A.nnodi; ++i) {
+        auto it = jnode.find(A.isngn[A.iin[i]]);
+        if (it == jnode.end()) continue;
+        for (int d = 0; d < A.nndf[A.iin[i]]; ++d) {
+          int a = A.kdofi[i] + d, b = ni + Bq.kdofi[it->second] + d;
+          double ra = rho[si][a], rb = rho[sj][b - ni];
+          cd.push_back({a, b});
+          wa.push_back(ra / (ra + rb));
+          wb.push_back(rb / (ra + rb));
+        }
+      }
+      // D^T columns: coarse dofs common to both
+      std::unordered_map<int, int> jrow;
+      for (int r = 0; r < Bq.nconstr; ++r) jrow[Bq.indrowc[r]] = r;
+      vector<vector<double>> dcol;
+      for (int r = 0; r < A.nconstr; ++r) {
+        auto it = jrow.find(A.indrowc[r]);
+        if (it == jrow.end()) continue;
+        vector<double> v(n, 0.0);
+        for (int k = A.crow_ptr[r]; k < A.crow_ptr[r + 1]; ++k) v[A.crow_col[k]] += A.crow_val[k];
+        for (int k = Bq.crow_ptr[it->second]; k < Bq.crow_ptr[it->second + 1]; ++k)
+          v[ni + Bq.crow_col[k]] -= Bq.crow_val[k];
+        dcol.push_back(v);
+      }
+      const int m = (int)dcol.size();
+      const int neig = std::min(10, (int)cd.size() - m);
+      if (neig <= 0) { est_loc[p] = 1.0; continue; }
+      // orthonormal basis of range(D^T): Gram-Schmidt, twice
+      vector<double> q;
+      int mq = 0;
+      for (auto& v : dcol) {
+        for (int pass = 0; pass < 2; ++pass)
+          for (int k = 0; k < mq; ++k) {
+            double t = 0.0;
+            for (int r = 0; r < n; ++r) t += q[(size_t)k * n + r] * v[r];
+            for (int r = 0; r < n; ++r) v[r] -= t * q[(size_t)k * n + r];
+          }
+        double nv = 0.0;
+        for (int r = 0; r < n; ++r) nv += v[r] * v[r];
+        nv = std::sqrt(nv);
+        if (nv < 1e-12) continue;
+        for (int r = 0; r < n; ++r) q.push_back(v[r] / nv);
+        ++mq;
+      }
+      // S = diag(S_i, S_j)
+      vector<double> Sm((size_t)n * n, 0.0);
+      for (int r = 0; r < ni; ++r)
+        for (int c = 0; c < ni; ++c) Sm[(size_t)r * n + c] = sd[si][(size_t)r * ni + c];
+      for (int r = 0; r < nj; ++r)
+        for (int c = 0; c < nj; ++c) Sm[(size_t)(ni + r) * n + ni + c] = sd[sj][(size_t)r * nj + c];
+      double t = 0.0;
+      for (int r = 0; r < n; ++r) t = std::max(t, std::fabs(Sm[(size_t)r * n + r]));
+      // A = P E^T S E P
+      vector<double> F((size_t)n * n, 0.0), Am((size_t)n * n, 0.0);
+      for (size_t k = 0; k < cd.size(); ++k) {
+        const int a = cd[k][0], b = cd[k][1];
+        for (int r = 0; r < n; ++r) {
+          F[(size_t)r * n + a] = (1.0 - wa[k]) * Sm[(size_t)r * n + a] - wa[k] * Sm[(size_t)r * n + b];
+          F[(size_t)r * n + b] = -wb[k] * Sm[(size_t)r * n + a] + (1.0 - wb[k]) * Sm[(size_t)r * n + b];
+        }
+      }
+      for (size_t k = 0; k < cd.size(); ++k) {
+        const int a = cd[k][0], b = cd[k][1];
+        for (int c = 0; c < n; ++c) {
+          Am[(size_t)a * n + c] = (1.0 - wa[k]) * F[(size_t)a * n + c] - wa[k] * F[(size_t)b * n + c];
+          Am[(size_t)b * n + c] = -wb[k] * F[(size_t)a * n + c] + (1.0 - wb[k]) * F[(size_t)b * n + c];
+        }
+      }
+      for (int r = 0; r < n; ++r)
+        for (int c = r + 1; c < n; ++c) {
+          double mm = 0.5 * (Am[(size_t)r * n + c] + Am[(size_t)c * n + r]);
+          Am[(size_t)r * n + c] = Am[(size_t)c * n + r] = mm;
+        }
+      project_both(n, Am, q, mq);
+      // B = P S P + t (I - P)
+      vector<double> Bm = Sm;
+      project_both(n, Bm, q, mq);
+      for (int k = 0; k < mq; ++k)  // I - P = Q Q^T
+        for (int r = 0; r < n; ++r)
+          for (int c = 0; c < n; ++c) Bm[(size_t)r * n + c] += t * q[(size_t)k * n + r] * q[(size_t)k * n + c];
+      // B = U diag(sig) U^T; keep sig > 1e-12 max; V = U_keep sig^-1/2; H = V^T A V
+      vector<double> sig, U;
+      vector<double> bcopy = Bm;
+      sym_eig(n, bcopy, sig, U);
+      const double smax = sig.empty() ? 0.0 : sig.back();
+      vector<int> keep;
+      for (int k = 0; k < n; ++k) if (sig[k] > 1e-12 * smax) keep.push_back(k);
+      const int nk = (int)keep.size();
+      vector<double> V((size_t)n * nk);
+      for (int r = 0; r < n; ++r)
+        for (int k = 0; k < nk; ++k) V[(size_t)r * nk + k] = U[(size_t)r * n + keep[k]] / std::sqrt(sig[keep[k]]);
+      vector<double> AV((size_t)n * nk, 0.0), H((size_t)nk * nk, 0.0);
+      for (int r = 0; r < n; ++r)
+        for (int c = 0; c < n; ++c) {
+          const double arc = Am[(size_t)r * n + c];
+          if (arc == 0.0) continue;
+          for (int k = 0; k < nk; ++k) AV[(size_t)r * nk + k] += arc * V[(size_t)c * nk + k];
+        }
+      for (int a = 0; a < nk; ++a)
+        for (int b = 0; b < nk; ++b) {
+          double tt = 0.0;
+          for (int r = 0; r < n; ++r) tt += V[(size_t)r * nk + a] * AV[(size_t)r * nk + b];
+          H[(size_t)a * nk + b] = tt;
+        }
+      for (int a = 0; a < nk; ++a)
+        for (int b = a + 1; b < nk; ++b) {
+          double mm = 0.5 * (H[(size_t)a * nk + b] + H[(size_t)b * nk + a]);
+          H[(size_t)a * nk + b] = H[(size_t)b * nk + a] = mm;
+        }
+      vector<double> lam, Y;
+      sym_eig(nk, H, lam, Y);
+      const int ne = std::min(neig, nk);
+      vector<double> ev(ne);
+      for (int k = 0; k < ne; ++k) ev[k] = lam[nk - 1 - k];
+      int nad = 0;
+      for (double l : ev) if (l >= o.adaptive_tau) ++nad;
+      est_loc[p] = ne > 0 ? (nad < ne ? ev[nad] : ev[nad - 1]) : 1.0;
+      o.pair_eigs[p] = ev;
+      o.pair_nadaptive[p] = nad;
+      // constraints A v over the face dofs of subdomain i
+      const Cnode& cf = A.cnodes[pcn[p][0]];
+      vector<double> rows((size_t)nad * cf.nvar, 0.0);
+      for (int k = 0; k < nad; ++k) {
+        const int col = nk - 1 - k;
+        vector<double> v(n, 0.0), av(n, 0.0);
+        for (int r = 0; r < n; ++r) {
+          double tt = 0.0;
+          for (int a = 0; a < nk; ++a) tt += V[(size_t)r * nk + a] * Y[(size_t)a * nk + col];
+          v[r] = tt;
+        }
+        for (int r = 0; r < n; ++r) {
+          double tt = 0.0;
+          for (int c = 0; c < n; ++c) tt += Am[(size_t)r * n + c] * v[c];
+          av[r] = tt;
+        }
+        for (int vv = 0; vv < cf.nvar; ++vv) rows[(size_t)k * cf.nvar + vv] = av[cf.ivsivn[vv]];
+      }
+      cons[p] = rows;
+    } catch (std::exception& e) {
+#pragma omp critical
+      errs = e.what();
+    }
+  }
+  if (!errs.empty()) throw std::runtime_error(errs);
+  o.adaptivity_est = -1.0;
+  for (double e : est_loc) o.adaptivity_est = std::max(o.adaptivity_est, e);
+  // load, orthonormalise and share the face constraints
+  for (int p = 0; p < npair; ++p) {
+    Sub& A = o.subs[o.pairs[p][1]];
+    Sub& Bq = o.subs[o.pairs[p][2]];
+    Cnode& ci = A.cnodes[pcn[p][0]];
+    Cnode& cj = Bq.cnodes[pcn[p][1]];
+    const int nvar = ci.nvar;
+    const int nad = o.pair_nadaptive[p];
+    const int ncol = ci.ncdof + nad;
+    vector<double> mcol((size_t)nvar * ncol);
+    for (int r = 0; r < ci.ncdof; ++r)
+      for (int v = 0; v < nvar; ++v) mcol[(size_t)r * nvar + v] = ci.matrix[(size_t)r * nvar + v];
+    for (int r = 0; r < nad; ++r)
+      for (int v = 0; v < nvar; ++v) mcol[(size_t)(ci.ncdof + r) * nvar + v] = cons[p][(size_t)r * nvar + v];
+    int nvalid = 0;
+    vector<double> qb = pivoted_orthonormal_basis(nvar, ncol, mcol, nvalid);
+    // face dof order of j by global dof
+    std::unordered_map<int, int> gpos;
+    for (int v = 0; v < cj.nvar; ++v) gpos[Bq.isvgvn[Bq.iivsvn[cj.ivsivn[v]]]] = v;
+    ci.matrix.assign((size_t)nvalid * nvar, 0.0);
+    cj.matrix.assign((size_t)nvalid * nvar, 0.0);
+    for (int r = 0; r < nvalid; ++r)
+      for (int v = 0; v < nvar; ++v) {
+        const double val = qb[(size_t)r * nvar + v];
+        ci.matrix[(size_t)r * nvar + v] = val;
+        cj.matrix[(size_t)r * nvar + gpos.at(A.isvgvn[A.iivsvn[ci.ivsivn[v]]])] = val;
+      }
+    ci.ncdof = cj.ncdof = nvalid;
+    ci.used = cj.used = nvalid > 0;
+    o.face_ncdof[p] = nvalid;
+  }
+  number_constraints(o);
+}
+
 int oracle_setup(void* h, int use_corner_constraints, int use_arithmetic_constraints, int weights_type) {
   auto* o = static_cast<Oracle*>(h);
   try {
@@ -891,30 +1375,7 @@ int oracle_setup(void* h, int use_corner_constraints, int use_arithmetic_constra
       if (use_corner_constraints) load_arithmetic_constraints(S, 3);
       if (use_arithmetic_constraints) { load_arithmetic_constraints(S, 2); load_arithmetic_constraints(S, 1); }
     }
-    int ncnode = o->ncorner + o->nedge + o->nface;
-    o->ncdof_of_cnode.assign(ncnode, 0);
-    for (auto& S : o->subs)
-      for (auto& cn : S.cnodes) o->ncdof_of_cnode[cn.global_cnode - 1] = cn.ncdof;
-    vector<int> kdofc(ncnode + 1, 0);
-    for (int c = 0; c < ncnode; ++c) kdofc[c + 1] = kdofc[c] + o->ncdof_of_cnode[c];
-    o->ndofc = kdofc[ncnode];
-    for (auto& S : o->subs) {
-      S.crow_ptr.assign(1, 0); S.crow_col.clear(); S.crow_val.clear(); S.indrowc.clear();
-      for (auto& cn : S.cnodes) {
-        cn.igcdof.clear();
-        for (int d = 0; d < cn.ncdof; ++d) cn.igcdof.push_back(kdofc[cn.global_cnode - 1] + d + 1);
-        if (!cn.used) continue;
-        for (int r = 0; r < cn.ncdof; ++r) {
-          for (int v = 0; v < cn.nvar; ++v) {
-            double val = cn.matrix[(size_t)r * cn.nvar + v];
-            if (std::fabs(val) > 0.0) { S.crow_col.push_back(cn.ivsivn[v]); S.crow_val.push_back(val); }
-          }
-          S.crow_ptr.push_back((int)S.crow_col.size());
-          S.indrowc.push_back(cn.igcdof[r]);
-        }
-      }
-      S.nconstr = (int)S.indrowc.size();
-    }
+    number_constraints(*o);
     // ---- per-subdomain factorisations (module_dd.f90:3983-4295, 5211-5799)
     std::string errs;
 #pragma omp parallel for schedule(dynamic) num_threads(o->nthreads)
@@ -969,6 +1430,48 @@ int oracle_setup(void* h, int use_corner_constraints, int use_arithmetic_constra
           if (cn.itype == 3 && cn.used)
             for (int v : cn.ivsivn) { int d = S.iivsvn[v]; S.aug.at(d, d) *= 2.0; }
         S.aug.factor();
+      } catch (std::exception& e) {
+#pragma omp critical
+        errs = e.what();
+      }
+    }
+    if (!errs.empty()) throw std::runtime_error(errs);
+    // ---- adaptive face constraints (module_levels.f90:2826-2938)
+    if (o->adaptive) adaptivity(*o, rho);
+    coarse_space(*o);
+    // ---- reduced rhs (module_dd.f90:6995-7257)
+    vector<vector<double>> g(nsub);
+#pragma omp parallel for schedule(dynamic) num_threads(o->nthreads)
+    for (int s = 0; s < nsub; ++s) {
+      auto& S = o->subs[s];
+      vector<double> rhs = S.rhs;
+      if (S.rhs_complete) for (int i = 0; i < S.ndofi; ++i) rhs[S.iivsvn[i]] *= S.wi[i];
+      if (S.bc_present) {
+        vector<double> bcw = S.bc;
+        for (int i = 0; i < S.ndofi; ++i) bcw[S.iivsvn[i]] *= S.wi[i];
+        for (int i = 0; i < S.ndof; ++i) { if (S.ifix[i]) rhs[i] = 0.0; rhs[i] += bcw[i]; }
+      }
+      S.solo.assign(S.ndofo, 0.0);
+      for (int i = 0; i < S.ndofo; ++i) S.solo[i] = rhs[S.iovsvn[i]];
+      if (S.ndofo > 0) S.a11.solve(S.solo.data());
+      g[s].assign(S.ndofi, 0.0);
+      for (int io = 0; io < S.ndofo; ++io)
+        for (int k = S.a12_ptr[io]; k < S.a12_ptr[io + 1]; ++k) g[s][S.a12_col[k]] += S.a12_val[k] * S.solo[io];
+      for (int i = 0; i < S.ndofi; ++i) g[s][i] = rhs[S.iivsvn[i]] - g[s][i];
+    }
+    comm_exchange_add(*o, g);
+    for (int s = 0; s < nsub; ++s) o->subs[s].g = g[s];
+    o->setup_done = true;
+  } catch (std::exception& e) {
+    o->err = e.what();
+    return 1;
+  }
+  return 0;
+}
+
+// coarse basis of one subdomain for its current constraints (module_dd.f90:5211-5799):
+// Y = A_r^-1 C^T, G = C Y, Phi = Y G^-1, coarse matrix Phi^T A Phi
+static void coarse_basis(Sub& S) {
         int nc = S.nconstr;
         S.yaug.assign((size_t)S.ndof * nc, 0.0);
         for (int c = 0; c < nc; ++c) {
@@ -1014,13 +1517,23 @@ int oracle_setup(void* h, int use_corner_constraints, int use_arithmetic_constra
             S.coarsem[(size_t)r * nc + c] = t;
           }
         }
+}
+
+// coarse bases of all subdomains, then the coarse problem
+// (module_levels.f90:3001-3170): assemble the upper triangle, factor
+static void coarse_space(Oracle& oo) {
+    Oracle* o = &oo;
+    std::string errs;
+#pragma omp parallel for schedule(dynamic) num_threads(o->nthreads)
+    for (int s = 0; s < o->nsub; ++s) {
+      try {
+        coarse_basis(o->subs[s]);
       } catch (std::exception& e) {
 #pragma omp critical
         errs = e.what();
       }
     }
     if (!errs.empty()) throw std::runtime_error(errs);
-    // ---- coarse problem (module_levels.f90:3001-3170): assemble upper triangle, factor
     int n = o->ndofc;
     o->coarse_chol.assign((size_t)n * n, 0.0);
     for (auto& S : o->subs) {
@@ -1036,34 +1549,6 @@ int oracle_setup(void* h, int use_corner_constraints, int use_arithmetic_constra
     for (int r = 0; r < n; ++r)
       for (int c = r + 1; c < n; ++c) o->coarse_chol[(size_t)r * n + c] = o->coarse_chol[(size_t)c * n + r];
     if (n > 0) dense_chol(o->coarse_chol, n, o->nthreads);
-    // ---- reduced rhs (module_dd.f90:6995-7257)
-    vector<vector<double>> g(nsub);
-#pragma omp parallel for schedule(dynamic) num_threads(o->nthreads)
-    for (int s = 0; s < nsub; ++s) {
-      auto& S = o->subs[s];
-      vector<double> rhs = S.rhs;
-      if (S.rhs_complete) for (int i = 0; i < S.ndofi; ++i) rhs[S.iivsvn[i]] *= S.wi[i];
-      if (S.bc_present) {
-        vector<double> bcw = S.bc;
-        for (int i = 0; i < S.ndofi; ++i) bcw[S.iivsvn[i]] *= S.wi[i];
-        for (int i = 0; i < S.ndof; ++i) { if (S.ifix[i]) rhs[i] = 0.0; rhs[i] += bcw[i]; }
-      }
-      S.solo.assign(S.ndofo, 0.0);
-      for (int i = 0; i < S.ndofo; ++i) S.solo[i] = rhs[S.iovsvn[i]];
-      if (S.ndofo > 0) S.a11.solve(S.solo.data());
-      g[s].assign(S.ndofi, 0.0);
-      for (int io = 0; io < S.ndofo; ++io)
-        for (int k = S.a12_ptr[io]; k < S.a12_ptr[io + 1]; ++k) g[s][S.a12_col[k]] += S.a12_val[k] * S.solo[io];
-      for (int i = 0; i < S.ndofi; ++i) g[s][i] = rhs[S.iivsvn[i]] - g[s][i];
-    }
-    comm_exchange_add(*o, g);
-    for (int s = 0; s < nsub; ++s) o->subs[s].g = g[s];
-    o->setup_done = true;
-  } catch (std::exception& e) {
-    o->err = e.what();
-    return 1;
-  }
-  return 0;
 }
 
 // y = S x per subdomain (module_dd.f90:6564-6699), then exchange
@@ -1454,6 +1939,39 @@ double oracle_dotprod_subdomain(void* h, int isub, const double* v1, const doubl
   for (int i = 0; i < S.ndofi; ++i) t += v1[S.iivsvn[i]] * S.wi[i] * v2[S.iivsvn[i]];
   for (int i = 0; i < S.ndofo; ++i) t += v1[S.iovsvn[i]] * v2[S.iovsvn[i]];
   return t;
+}
+
+// the dense symmetric eigensolver on its own (a: n x n row-major), for tests
+void oracle_sym_eig(int n, const double* a, double* w, double* z) {
+  vector<double> m(a, a + (size_t)n * n), wv, zv;
+  sym_eig(n, m, wv, zv);
+  std::copy(wv.begin(), wv.end(), w);
+  std::copy(zv.begin(), zv.end(), z);
+}
+
+void oracle_set_adaptive(void* h, int on, double tau) {
+  auto* o = static_cast<Oracle*>(h);
+  o->adaptive = on != 0;
+  o->adaptive_tau = tau;
+}
+
+// pairs of the last adaptive setup: per pair (face global cnode, isub, jsub, neig, nadaptive,
+// face constraints) in info (6 ints each) and its eigenvalues (10 per pair, descending,
+// unused entries 0); returns the number of pairs
+int oracle_adaptive_info(void* h, int* info, double* eigs, int maxpair, double* est) {
+  auto* o = static_cast<Oracle*>(h);
+  const int np = (int)o->pairs.size();
+  for (int p = 0; p < std::min(np, maxpair); ++p) {
+    info[6 * p + 0] = o->pairs[p][0];
+    info[6 * p + 1] = o->pairs[p][1];
+    info[6 * p + 2] = o->pairs[p][2];
+    info[6 * p + 3] = (int)o->pair_eigs[p].size();
+    info[6 * p + 4] = o->pair_nadaptive[p];
+    info[6 * p + 5] = o->face_ncdof[p];
+    for (int k = 0; k < 10; ++k) eigs[10 * p + k] = k < (int)o->pair_eigs[p].size() ? o->pair_eigs[p][k] : 0.0;
+  }
+  *est = o->adaptivity_est;
+  return np;
 }
 
 }  // extern "C"

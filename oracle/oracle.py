@@ -15,6 +15,16 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB = None
 
 
+def sym_eig(a):
+    """The oracle's dense symmetric eigensolver: (ascending eigenvalues, eigenvectors in columns)."""
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    n = a.shape[0]
+    w = np.zeros(n)
+    z = np.zeros((n, n))
+    lib().oracle_sym_eig(n, a.ctypes.data, w.ctypes.data, z.ctypes.data)
+    return w, z
+
+
 def build(force: bool = False) -> str:
     path = os.path.join(_HERE, "liboracle.so")
     src = os.path.join(_HERE, "bddc_oracle.cpp")
@@ -39,6 +49,9 @@ def lib():
         L.oracle_solve_method.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_int, C.c_int,
                                           C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_double)]
         L.oracle_download.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int]
+        L.oracle_set_adaptive.argtypes = [C.c_void_p, C.c_int, C.c_double]
+        L.oracle_adaptive_info.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
+        L.oracle_sym_eig.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
         L.oracle_stats.argtypes = [C.c_void_p, C.c_void_p]
         L.oracle_sub_stats.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
         L.oracle_relres_history.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
@@ -108,6 +121,23 @@ class Oracle:
         rc = self.L.oracle_setup(self.h, use_corner_constraints, use_arithmetic_constraints, weights_type)
         if rc != 0:
             raise RuntimeError(self.L.oracle_error(self.h).decode())
+
+    def set_adaptive(self, on=True, tau=1.5):
+        """Adaptive face constraints at the next setup (module_adaptivity.f90),
+        eigenvalue threshold tau."""
+        self.L.oracle_set_adaptive(self.h, int(on), float(tau))
+
+    def adaptive_info(self, maxpair=100000):
+        """Pairs of the last adaptive setup: dict with 'pairs' (face, isub, jsub),
+        'neig', 'nadaptive', 'face_ncdof' (arrays) and 'eigs' (npair x 10,
+        descending, zero-padded), plus the estimate 'est'."""
+        info = np.zeros(6 * maxpair, dtype=np.int32)
+        eigs = np.zeros(10 * maxpair)
+        est = C.c_double()
+        n = self.L.oracle_adaptive_info(self.h, info.ctypes.data, eigs.ctypes.data, maxpair, C.byref(est))
+        info = info[:6 * n].reshape(n, 6)
+        return {"pairs": info[:, :3].copy(), "neig": info[:, 3].copy(), "nadaptive": info[:, 4].copy(),
+                "face_ncdof": info[:, 5].copy(), "eigs": eigs[:10 * n].reshape(n, 10).copy(), "est": est.value}
 
     def solve(self, tol=1e-8, maxit=500, ndecrmax=50, method=0):
         """method 0 PCG, 1 BiCGSTAB, 2 steepest descent, -1 reference defaults."""

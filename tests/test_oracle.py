@@ -220,3 +220,63 @@ def test_oracle_bicgstab_maxit_reason(oracle_mod):
     o.setup(1, 1, 0)
     it, reason, cond = o.solve(1e-14, 2, 50, method=1)
     assert it == 2 and reason == -1
+
+
+def test_oracle_dense_eigensolver_matches_numpy(oracle_mod):
+    """The oracle's Householder + implicit-QR eigensolver (stands in for
+    LAPACK DSYEV/DSYGV of module_adaptivity.f90) on random and degenerate
+    symmetric matrices."""
+    rng = np.random.default_rng(4)
+    for n in (1, 3, 17, 64, 120):
+        a = rng.standard_normal((n, n))
+        a = a + a.T
+        w, z = oracle_mod.sym_eig(a)
+        assert np.abs(w - np.linalg.eigvalsh(a)).max() < 1e-12 * max(1.0, np.abs(w).max())
+        assert np.abs(z.T @ z - np.eye(n)).max() < 1e-12
+        assert np.abs(a @ z - z * w).max() < 1e-11 * max(1.0, np.abs(w).max())
+    w, z = oracle_mod.sym_eig(np.diag([3.0, 1.0, 1.0, 2.0]))
+    assert np.allclose(w, [1, 1, 2, 3])
+
+
+def _channel_problem():
+    from bddcml_gb300 import problems
+    kappa = problems.channel_kappa(15, nchannels=4, width=1, contrast=1e4, sigma=1.0, seed=17)
+    return problems.poisson_boxes(15, problems.uniform_boxes(15, 3), kappa=kappa)
+
+
+def test_oracle_adaptive_constraints(oracle_mod):
+    """Adaptive face constraints (module_adaptivity.f90:296-2514,
+    module_levels.f90:2826-2938) on a high-contrast channel problem with
+    rho-scaling: with an infinite threshold only the face rows are
+    orthonormalised, which leaves the preconditioner unchanged; with tau = 10
+    the largest pair eigenvalues above tau become constraints, the PCG
+    condition number falls below the pair estimate and the solution still
+    matches a direct solve."""
+    prob = _channel_problem()
+    ud = _direct(prob)
+    o0 = oracle_mod.Oracle(prob)
+    o0.setup(1, 1, 1)
+    it0, r0, cond0 = o0.solve(1e-10, 500, 50)
+    oi = oracle_mod.Oracle(prob)
+    oi.set_adaptive(True, 1e30)
+    oi.setup(1, 1, 1)
+    iti, ri, condi = oi.solve(1e-10, 500, 50)
+    info_i = oi.adaptive_info()
+    assert len(info_i["pairs"]) == 54 and info_i["nadaptive"].sum() == 0
+    assert (info_i["face_ncdof"] == 1).all()
+    assert abs(iti - it0) <= 1 and abs(condi - cond0) <= 1e-6 * cond0
+    oa = oracle_mod.Oracle(prob)
+    oa.set_adaptive(True, 10.0)
+    oa.setup(1, 1, 1)
+    ita, ra, conda = oa.solve(1e-10, 500, 50)
+    info = oa.adaptive_info()
+    assert ra == 0 and info["nadaptive"].sum() > 0
+    assert ita < 0.7 * it0 and conda < 0.1 * cond0
+    assert conda <= 1.05 * info["est"] and info["est"] < 10.0
+    eigs = info["eigs"]
+    for p in range(len(eigs)):
+        k = info["neig"][p]
+        assert (np.diff(eigs[p, :k]) <= 1e-12 * max(1.0, eigs[p, 0])).all()  # descending
+        assert info["nadaptive"][p] == (eigs[p, :k] >= 10.0).sum()
+    err = np.linalg.norm(oa.global_solution() - ud) / np.linalg.norm(ud)
+    assert err < 1e-9
