@@ -29,7 +29,8 @@ STAT_FIELDS = ["t_host_setup", "t_device_setup", "t_solve", "t_iterations", "t_p
                "ninterface", "precision", "h2d_bytes", "d2h_bytes", "t_upload", "t_host_assemble",
                "t_host_iface", "t_host_globs", "t_host_blocks", "refine1", "refine2",
                "flop_sweep_oo", "flop_sweep_s", "bytes_residual", "bytes_schur_apply", "bytes_pc_local",
-               "launches_setup", "launches_solve", "t_dev_alloc", "t_dev_h2d"]
+               "launches_setup", "launches_solve", "t_dev_alloc", "t_dev_h2d", "npair", "nadaptive",
+               "adapt_est", "t_adaptive", "lobpcg_resid", "lobpcg_iter"]
 
 EXPORTS = ["bddcml_init_c", "bddcml_upload_global_data_c", "bddcml_upload_subdomain_data_c",
            "bddcml_setup_preconditioner_c", "bddcml_solve_c", "bddcml_download_local_solution_c",
@@ -39,7 +40,8 @@ EXPORTS = ["bddcml_init_c", "bddcml_upload_global_data_c", "bddcml_upload_subdom
            "bddcml_get_last_error_c", "bddcml_set_precision_c", "bddcml_get_stats_c",
            "bddcml_get_residual_history_c", "bddcml_get_interface_weights_c", "bddcml_get_coarse_info_c",
            "bddcml_set_profiling_c", "bddcml_get_profile_c", "bddcml_release_device_memory_c",
-           "bddcml_dotprod_subdomain_dev_c", "bddcml_element_gradient_dev_c"]
+           "bddcml_dotprod_subdomain_dev_c", "bddcml_element_gradient_dev_c", "bddcml_set_adaptive_threshold_c",
+           "bddcml_get_adaptive_info_c"]
 
 # phases of bddcml_get_profile_c (CUDA events on the solver stream)
 PHASES = ["numeric_total", "solve_total", "factor_interior", "solve_interior", "refine_residual", "schur",
@@ -224,6 +226,28 @@ def get_stats() -> dict:
     return {k: buf[i] for i, k in enumerate(STAT_FIELDS[: n.value])}
 
 
+def set_adaptive_threshold(tau: float) -> None:
+    """Eigenvalue threshold of the adaptive face constraints (default 1.5)."""
+    lib().bddcml_set_adaptive_threshold_c(_d(tau))
+    _check()
+
+
+def get_adaptive_info() -> dict:
+    """Face pairs of the last adaptive setup: 'pairs' (npair x 2 subdomains),
+    'k' (eigenvalues computed per pair) and 'eigs' (npair x 10, descending)."""
+    n = C.c_int(0)
+    lib().bddcml_get_adaptive_info_c(None, None, C.byref(n))
+    _check()
+    pairs = np.zeros(3 * max(1, n.value), dtype=np.int32)
+    eigs = np.zeros(10 * max(1, n.value))
+    m = C.c_int(n.value)
+    lib().bddcml_get_adaptive_info_c(pairs.ctypes.data_as(C.POINTER(C.c_int)),
+                                     eigs.ctypes.data_as(C.POINTER(C.c_double)), C.byref(m))
+    _check()
+    pairs = pairs[:3 * n.value].reshape(n.value, 3)
+    return {"pairs": pairs[:, :2].copy(), "k": pairs[:, 2].copy(), "eigs": eigs[:10 * n.value].reshape(n.value, 10)}
+
+
 def get_residual_history() -> np.ndarray:
     n = C.c_int(0)
     lib().bddcml_get_residual_history_c(None, C.byref(n))
@@ -308,15 +332,19 @@ def upload_problem(prob, numbase: int = 0, find_components_int: int = 1, neighbo
 
 
 def solve_problem(prob, precision: int = 1, tol: float = 1e-8, maxit: int = 500, ndecrmax: int = 50,
-                  weights_type: int = 0, numbase: int = 0, finalize: bool = True, method: int = 0):
+                  weights_type: int = 0, numbase: int = 0, finalize: bool = True, method: int = 0,
+                  adaptive_tau=None):
     """init -> upload -> setup -> solve -> download (-> finalize) through the
     C ABI, the sequence of the reference example poisson_on_cube.f90:373-672.
     method: 0 PCG, 1 BiCGSTAB, 2 steepest descent, -1 reference defaults.
+    adaptive_tau: adaptive face constraints with this eigenvalue threshold.
     Returns (global solution, num_iter, reason, cond, stats)."""
     bddcml_init(2, [prob.nsub, 1], -1, 0, 0, numbase, 0)
     set_precision(precision)
     upload_problem(prob, numbase=numbase)
-    bddcml_setup_preconditioner(prob.matrixtype, 0, 1, 1, 1, 0, 0, weights_type)
+    if adaptive_tau is not None:
+        set_adaptive_threshold(adaptive_tau)
+    bddcml_setup_preconditioner(prob.matrixtype, 0, 1, 1, 1, 1 if adaptive_tau is not None else 0, 0, weights_type)
     it, reason, cond = bddcml_solve(0, method, tol, maxit, ndecrmax, 0, 0)
     u = np.zeros(prob.ndof)
     for s in prob.subdomains:

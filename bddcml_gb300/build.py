@@ -19,12 +19,13 @@ NVFLAGS = GENCODE + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fop
 SOURCES = [
     ("bddc_host.cpp", "g++"),
     ("bddc_abi.cpp", "g++"),
+    ("bddc_adaptive.cpp", "g++"),
     ("bddc_device.cu", "nvcc"),
     ("bddc_noalloc.cu", "nvcc"),
     ("bddc_gradient.cu", "nvcc"),
 ]
 HEADERS = ["bddc_internal.hpp", "bddc_kernels.cuh", "bddc_df.cuh", "bddc_setup_kernels.cuh",
-           "bddc_pcg_kernels.cuh", "bddc_tc.cuh"]
+           "bddc_pcg_kernels.cuh", "bddc_tc.cuh", "bddc_adaptive.cuh"]
 
 
 def _nvcc() -> str:

@@ -204,7 +204,10 @@ void bddcml_setup_preconditioner_c(int* matrixtype, int* use_defaults_int, int* 
       S->prm.use_user = *use_user_constraints_int != 0;
       S->prm.weights_type = *weights_type;
     }
-    if (S->prm.use_adaptive) throw Error{ERR_UNSUPPORTED, "adaptive constraints are not implemented"};
+    if (S->prm.use_adaptive && !S->prm.use_arith)  // an add-on to the arithmetic ones (module_levels.f90:2699-2700)
+      throw Error{ERR_UNSUPPORTED, "adaptive constraints need the arithmetic face constraints"};
+    if (S->prm.use_adaptive && S->prm.matrixtype != 1)
+      throw Error{ERR_UNSUPPORTED, "adaptive constraints are implemented for SPD matrices (matrixtype 1)"};
     if (S->prm.use_user) throw Error{ERR_UNSUPPORTED, "user constraints are not implemented"};
     double t0 = wall_time();
     S->stats = Stats{};
@@ -397,10 +400,38 @@ void bddcml_get_stats_c(double* stats, int* lstats) {
                   (double)S->prm.precision, q.h2d_bytes, q.d2h_bytes, q.t_upload, q.t_host_assemble,
                   q.t_host_iface, q.t_host_globs, q.t_host_blocks, q.refine1, q.refine2,
                   q.flop_sweep_oo, q.flop_sweep_s, q.bytes_residual, q.bytes_schur_apply, q.bytes_pc_local,
-                  q.launches_setup, q.launches_solve, q.t_dev_alloc, q.t_dev_h2d};
+                  q.launches_setup, q.launches_solve, q.t_dev_alloc, q.t_dev_h2d, (double)q.npair,
+                  (double)q.nadaptive, q.adapt_est, q.t_adaptive, q.lobpcg_resid, (double)q.lobpcg_iter};
     int n = std::min<int>(*lstats, (int)(sizeof(v) / sizeof(v[0])));
     for (int i = 0; i < n; ++i) stats[i] = v[i];
     *lstats = n;
+  });
+}
+
+void bddcml_set_adaptive_threshold_c(double* tau) {
+  guarded("bddcml_set_adaptive_threshold_c", [&] {
+    Solver* S = need_solver("bddcml_set_adaptive_threshold_c");
+    if (!S) return;
+    if (!(*tau > 0.0)) throw Error{ERR_ARGUMENT, "the adaptive threshold must be positive"};
+    S->prm.adaptive_tau = *tau;
+  });
+}
+
+void bddcml_get_adaptive_info_c(int* pairs, double* eigs, int* lpair) {
+  guarded("bddcml_get_adaptive_info_c", [&] {
+    Solver* S = need_solver("bddcml_get_adaptive_info_c");
+    if (!S) return;
+    const AdaptivePairs& P = S->adaptive_pairs;
+    const int n = std::min(*lpair, P.npair);
+    for (int p = 0; p < n; ++p) {
+      pairs[3 * p + 0] = P.si[p] + S->prm.numbase;
+      pairs[3 * p + 1] = P.sj[p] + S->prm.numbase;
+      pairs[3 * p + 2] = P.k[p];
+      for (int c = 0; c < AdaptivePairs::KMAX; ++c)
+        eigs[(size_t)p * AdaptivePairs::KMAX + c] =
+            c < P.k[p] ? S->adaptive_eigs[(size_t)p * AdaptivePairs::KMAX + c] : 0.0;
+    }
+    *lpair = P.npair;
   });
 }
 

@@ -11,8 +11,10 @@
 #include <numeric>
 #include <string>
 #include <type_traits>
+#include <unordered_map>
 #include <vector>
 
+#include "bddc_adaptive.cuh"
 #include "bddc_internal.hpp"
 #include "bddc_pcg_kernels.cuh"
 #include "bddc_tc.cuh"
@@ -154,6 +156,8 @@ class Device {
  public:
   cudaStream_t st = nullptr;
   std::vector<void*> owned;    // freed on destruction / re-setup
+  std::vector<void*> owned_pc; // the constraint-dependent part (rebuilt after adaptive constraints)
+  void* poolP = nullptr;       // factor precision: Srho factor and [Srho^-1 | Y]
   bool mixed = true;
   int nsub = 0;
   std::vector<DevSub> hs;
@@ -221,9 +225,14 @@ class Device {
     nv_v0 = nv_v1 = nv_r = nullptr;
     kv = ky = ks = kt = krs = nullptr;
     nv_off = nullptr;
+    release_pc();
     for (void* q : owned) cudaFreeAsync(q, st);
     owned.clear();
     maxit_alloc = 0;
+  }
+  void release_pc() {
+    for (void* q : owned_pc) cudaFreeAsync(q, st);
+    owned_pc.clear();
   }
 };
 
@@ -324,8 +333,19 @@ static void run_solve(Device& D, const BandDesc* bd, int nbatch, int maxnb, int 
   }
 }
 
+// FP32 flop of one forward + backward block-band sweep over ncol columns
+static double band_sweep_flop(int nb, int w, int ncol) {
+  double f = 0.0;
+  for (int k = 0; k < nb; ++k) f += 2.0 * NB * ncol * NB * ((std::min(k, w) + 1) + (std::min(w, nb - 1 - k) + 1));
+  return f;
+}
+
 template <typename T>
 static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk);
+template <typename T>
+static void setup_precond(Solver& S, Device& D);
+template <typename T>
+static void adaptive_constraints(Solver& S, Device& D);
 
 bool device_setup(Solver& S, Error& err) {
   Device& D = *S.dev;
@@ -344,13 +364,25 @@ bool device_setup(Solver& S, Error& err) {
       auto& b = blk[t];
       if (b.maxrow_oo > 96 || b.maxrow_oi > 95 || b.maxrow_io > 128 || b.maxrow_ii > 128)
         throw Error{ERR_UNSUPPORTED, "subdomain matrix rows longer than the staging buffers (96/128 entries)"};
-      if (S.subs[t].nconstr > 119) throw Error{ERR_UNSUPPORTED, "more than 119 constraints on a subdomain"};
       if (S.subs[t].ndofi == 0) throw Error{ERR_ARGUMENT, "subdomain without interface"};
     }
     S.stats.t_host_setup += wall_time() - t0;
     double t1 = wall_time();
-    if (D.mixed) setup_numeric<float>(S, D, blk);
-    else setup_numeric<double>(S, D, blk);
+    if (D.mixed) {
+      setup_numeric<float>(S, D, blk);
+      setup_precond<float>(S, D);
+      if (S.prm.use_adaptive) {
+        adaptive_constraints<float>(S, D);
+        setup_precond<float>(S, D);
+      }
+    } else {
+      setup_numeric<double>(S, D, blk);
+      setup_precond<double>(S, D);
+      if (S.prm.use_adaptive) {
+        adaptive_constraints<double>(S, D);
+        setup_precond<double>(S, D);
+      }
+    }
     vector<SubBlocks>().swap(S.blocks);
     // check device error flags
     int herr = 0;
@@ -377,68 +409,43 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
 
   // ---- sizes and offsets
   D.hs.assign(nsub, DevSub{});
-  long long oT = 0, oS = 0, oPC = 0, oSm = 0, oPan = 0;
-  vector<std::array<long long, 4>> poff(nsub, {0, 0, 0, 0});
-  int rep = 0, koo = 0, koi = 0, kio = 0, kii = 0, cptr = 0, coff = 0;
-  D.maxnbo = 0; D.maxw = 0; D.maxNR = 0; D.maxNI = 0; D.maxNO = 0; D.ncpmax = 4;
-  int maxnbi = 0, maxNRC = 0, maxnc = 0;
+  long long oT = 0, oS = 0, oPan = 0;
+  vector<std::array<long long, 2>> poff(nsub, {0, 0});
+  int rep = 0, koo = 0, koi = 0, kio = 0, kii = 0;
+  D.maxnbo = 0; D.maxw = 0; D.maxNR = 0; D.maxNI = 0; D.maxNO = 0;
   for (int t = 0; t < nsub; ++t) {
     auto& s = S.subs[t];
     auto& b = blk[t];
     DevSub d{};
-    d.no = s.ndofo; d.ni = s.ndofi; d.nc = s.nconstr;
-    d.ncp = roundup(std::max(1, d.nc), 4);
+    d.no = s.ndofo; d.ni = s.ndofi;
     d.NO = roundup(d.no, NB); d.NI = roundup(d.ni, NB);
     d.NR = roundup(d.ni + 1, TC_M);
-    d.NRC = roundup(d.NI + std::max(1, d.nc), TC_M);
     d.nbo = d.NO / NB; d.w = b.w; d.nbi = d.NI / NB; d.nref = D.nref;
     d.oL = oT; oT += (long long)d.nbo * (d.w + 1) * NB * NB;
     d.oLinv = oT; oT += (long long)d.nbo * NB * NB;
     d.oXc = oT; oT += (long long)(d.nref == 0 ? 1 : (d.nref == 1 ? 2 : 3)) * d.NO * d.NR;
-    d.oLs = oT; oT += (long long)d.nbi * d.nbi * NB * NB;
-    d.oLsinv = oT; oT += (long long)d.nbi * NB * NB;
-    d.oBs = oT; oT += (long long)d.NI * d.NRC;
     if (std::is_same_v<T, float>) {
       poff[t][0] = oPan; oPan += (long long)d.nbo * (d.w + 1) * 2 * TC_PCHUNK;
       poff[t][1] = oPan; oPan += (long long)d.nbo * (d.w + 1) * 2 * TC_PCHUNK;
-      poff[t][2] = oPan; oPan += (long long)d.nbi * d.nbi * 2 * TC_PCHUNK;
-      poff[t][3] = oPan; oPan += (long long)d.nbi * d.nbi * 2 * TC_PCHUNK;
     }
     d.oS = oS; oS += (long long)d.NI * d.NI;
-    d.oZ = oPC; oPC += (long long)d.NI * d.NI;
-    d.oPhi = oPC; oPC += (long long)d.NI * d.ncp;
-    d.oGinv = oSm; oSm += (long long)d.ncp * d.ncp;
-    d.oAc = oSm; oSm += (long long)d.ncp * d.ncp;
     d.rep = rep; rep += d.NI;
     d.koo = koo; koo += d.no + 1;
     d.koi = koi; koi += d.no + 1;
     d.kio = kio; kio += d.ni + 1;
     d.kii = kii; kii += d.ni + 1;
-    d.cptr = cptr; cptr += d.nc + 1;
-    d.coff = coff; coff += d.nc;
     d.rho = b.rho;
     D.hs[t] = d;
     D.maxnbo = std::max(D.maxnbo, d.nbo); D.maxw = std::max(D.maxw, d.w);
     D.maxNR = std::max(D.maxNR, d.NR); D.maxNI = std::max(D.maxNI, d.NI); D.maxNO = std::max(D.maxNO, d.NO);
-    D.ncpmax = std::max(D.ncpmax, d.ncp);
-    maxnbi = std::max(maxnbi, d.nbi); maxNRC = std::max(maxNRC, d.NRC); maxnc = std::max(maxnc, d.nc);
   }
   D.nrep = rep;
   {
-    auto sweep = [](int nb, int w, int ncol) {
-      double f = 0.0;
-      for (int k = 0; k < nb; ++k)
-        f += 2.0 * NB * ncol * NB * ((std::min(k, w) + 1) + (std::min(w, nb - 1 - k) + 1));
-      return f;
-    };
-    S.stats.flop_sweep_oo = S.stats.flop_sweep_s = S.stats.bytes_residual = 0;
-    S.stats.bytes_schur_apply = S.stats.bytes_pc_local = 0;
+    S.stats.flop_sweep_oo = S.stats.bytes_residual = S.stats.bytes_schur_apply = 0;
     for (auto& d : D.hs) {
-      S.stats.flop_sweep_oo += sweep(d.nbo, d.w, d.NR);
-      S.stats.flop_sweep_s += sweep(d.nbi, d.nbi - 1, d.NRC);
+      S.stats.flop_sweep_oo += band_sweep_flop(d.nbo, d.w, d.NR);
       S.stats.bytes_residual += (double)d.NO * d.NR * 4.0 * 3.0;
       S.stats.bytes_schur_apply += (double)d.ni * d.NI * 8.0 + d.ni * 16.0;
-      S.stats.bytes_pc_local += (double)d.ni * d.NI * sizeof(T) + (double)d.ni * d.ncp * sizeof(T) + d.ni * 24.0;
     }
   }
   S.stats.bytes_per_iteration = 0;
@@ -450,8 +457,6 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
   D.poolT = dalloc<T>(oT, own);
   float* ppool = std::is_same_v<T, float> ? dalloc<float>(oPan, own) : nullptr;
   D.poolS = D.mixed ? (void*)dalloc<float2>(oS, own) : (void*)dalloc<double>(oS, own);
-  D.poolPC = dalloc<T>(oPC, own);
-  D.small = dalloc<double>(oSm, own);
   D.err = dalloc<int>(1, own);
   S.stats.t_dev_alloc = wall_time() - tw0;
   CK(cudaMemsetAsync(D.err, 0, sizeof(int), st));
@@ -499,22 +504,6 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
          [](SubBlocks& b) -> vector<double>& { return b.io_val; }, D.kio);
   concat([](SubBlocks& b) -> vector<int>& { return b.ii_ptr; }, [](SubBlocks& b) -> vector<int>& { return b.ii_col; },
          [](SubBlocks& b) -> vector<double>& { return b.ii_val; }, D.kii);
-  {
-    vector<int> cp, cc, cm;
-    vector<double> cv;
-    for (int t = 0; t < nsub; ++t) {
-      auto& s = S.subs[t];
-      int base = (int)cc.size();
-      for (int q = 0; q <= s.nconstr; ++q) cp.push_back(base + s.c_ptr[q]);
-      cc.insert(cc.end(), s.c_col.begin(), s.c_col.end());
-      cv.insert(cv.end(), s.c_val.begin(), s.c_val.end());
-      cm.insert(cm.end(), s.indrowc.begin(), s.indrowc.end());
-    }
-    D.c_ptr = upload(cp, own, st);
-    D.c_col = upload(cc, own, st);
-    D.c_val = upload(cv, own, st);
-    D.cmap = upload(cm, own, st);
-  }
   // ---- interface vectors and owner lists
   D.n = S.ninterface;
   {
@@ -555,21 +544,6 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
     D.own.loc = upload(oloc, own, st);
     D.fixed = upload(S.iface_fixed, own, st);
     D.wsum = upload(S.iface_wsum, own, st);
-    // coarse dof owners
-    D.ndofc = S.ndofc;
-    vector<int> cptrv(D.ndofc + 1, 0), csub, cloc;
-    for (int t = 0; t < nsub; ++t) for (int q : S.subs[t].indrowc) cptrv[q + 1]++;
-    for (int q = 0; q < D.ndofc; ++q) cptrv[q + 1] += cptrv[q];
-    csub.resize(cptrv[D.ndofc]); cloc.resize(cptrv[D.ndofc]);
-    vector<int> cpos(cptrv.begin(), cptrv.end() - 1);
-    for (int t = 0; t < nsub; ++t)
-      for (int c = 0; c < S.subs[t].nconstr; ++c) {
-        int q = S.subs[t].indrowc[c];
-        csub[cpos[q]] = t; cloc[cpos[q]++] = c;
-      }
-    D.co_ptr = upload(cptrv, own, st);
-    D.co_sub = upload(csub, own, st);
-    D.co_loc = upload(cloc, own, st);
   }
   D.x = dalloc<double>(D.n, own); D.r = dalloc<double>(D.n, own); D.p = dalloc<double>(D.n, own);
   D.ap = dalloc<double>(D.n, own); D.z = dalloc<double>(D.n, own); D.g = dalloc<double>(D.n, own);
@@ -578,17 +552,12 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
   CK(cudaMemsetAsync(D.zrep, 0, D.nrep * sizeof(double), st));
   CK(cudaMemsetAsync(D.grep, 0, D.nrep * sizeof(double), st));
   D.nrb = (D.maxNI + AROWS - 1) / AROWS;
-  D.rcpart = dalloc<double>((size_t)nsub * D.nrb * D.ncpmax, own);
-  CK(cudaMemsetAsync(D.rcpart, 0, (size_t)nsub * D.nrb * D.ncpmax * sizeof(double), st));
-  D.rc = dalloc<double>(std::max(1, D.ndofc), own);
-  D.uc = dalloc<double>(std::max(1, D.ndofc), own);
   D.npart = std::min(MAXPART, std::max(1, (D.n + RT - 1) / RT));
   D.part = dalloc<double>(MAXPART, own);
   D.ctl = dalloc<PcgCtl>(1, own);
   D.scal = dalloc<double>(4, own);
 
   T* poolT = static_cast<T*>(D.poolT);
-  T* poolPC = static_cast<T*>(D.poolPC);
   if (D.mixed)
     CK(cudaFuncSetAttribute(k_schur_apply_df, cudaFuncAttributeMaxDynamicSharedMemorySize,
                             (int)(D.maxNI * sizeof(float2))));
@@ -701,6 +670,98 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
     CKL();
   }
   D.prof.end(PH_SCHUR, st);
+  // ---- assembled reduced rhs (module_dd.f90:7090-7135)
+  k_assemble_plain<<<(D.n + 255) / 256, 256, 0, st>>>(D.n, D.own, D.grep, nullptr, D.g);
+  CKL();
+  D.prof.end(PH_NUMERIC_TOTAL, st);
+}
+
+// The constraint-dependent part of the setup: Srho factor, [Srho^-1 | Y], G^-1,
+// Phi, Z, the local coarse matrices and the coarse problem.  Run after
+// setup_numeric, and again when adaptive constraints have changed C; each run
+// frees the previous one's buffers.
+template <typename T>
+static void setup_precond(Solver& S, Device& D) {
+  const int nsub = D.nsub;
+  cudaStream_t st = D.st;
+  D.release_pc();
+  auto& own = D.owned_pc;
+  long long oP = 0, oPC = 0, oSm = 0, oPan = 0;
+  vector<std::array<long long, 2>> poff(nsub, {0, 0});
+  int cptr = 0, coff = 0, maxnbi = 0, maxNRC = 0, maxnc = 0;
+  D.ncpmax = 4;
+  for (int t = 0; t < nsub; ++t) {
+    auto& s = S.subs[t];
+    if (s.nconstr > 119) throw Error{ERR_UNSUPPORTED, "more than 119 constraints on a subdomain"};
+    DevSub& d = D.hs[t];
+    d.nc = s.nconstr;
+    d.ncp = roundup(std::max(1, d.nc), 4);
+    d.NRC = roundup(d.NI + std::max(1, d.nc), TC_M);
+    d.oLs = oP; oP += (long long)d.nbi * d.nbi * NB * NB;
+    d.oLsinv = oP; oP += (long long)d.nbi * NB * NB;
+    d.oBs = oP; oP += (long long)d.NI * d.NRC;
+    if (std::is_same_v<T, float>) {
+      poff[t][0] = oPan; oPan += (long long)d.nbi * d.nbi * 2 * TC_PCHUNK;
+      poff[t][1] = oPan; oPan += (long long)d.nbi * d.nbi * 2 * TC_PCHUNK;
+    }
+    d.oZ = oPC; oPC += (long long)d.NI * d.NI;
+    d.oPhi = oPC; oPC += (long long)d.NI * d.ncp;
+    d.oGinv = oSm; oSm += (long long)d.ncp * d.ncp;
+    d.oAc = oSm; oSm += (long long)d.ncp * d.ncp;
+    d.cptr = cptr; cptr += d.nc + 1;
+    d.coff = coff; coff += d.nc;
+    D.ncpmax = std::max(D.ncpmax, d.ncp);
+    maxnbi = std::max(maxnbi, d.nbi); maxNRC = std::max(maxNRC, d.NRC); maxnc = std::max(maxnc, d.nc);
+  }
+  S.stats.flop_sweep_s = S.stats.bytes_pc_local = 0;
+  for (auto& d : D.hs) {
+    S.stats.flop_sweep_s += band_sweep_flop(d.nbi, d.nbi - 1, d.NRC);
+    S.stats.bytes_pc_local += (double)d.ni * d.NI * sizeof(T) + (double)d.ni * d.ncp * sizeof(T) + d.ni * 24.0;
+  }
+  T* poolP = dalloc<T>(oP, own);
+  D.poolP = poolP;
+  float* ppool = std::is_same_v<T, float> ? dalloc<float>(oPan, own) : nullptr;
+  D.poolPC = dalloc<T>(oPC, own);
+  T* poolPC = static_cast<T*>(D.poolPC);
+  D.small = dalloc<double>(oSm, own);
+  CK(cudaMemsetAsync(poolP, 0, oP * sizeof(T), st));
+  D.ds = upload(D.hs, own, st);
+  {
+    vector<int> cp, cc, cm;
+    vector<double> cv;
+    for (int t = 0; t < nsub; ++t) {
+      auto& s = S.subs[t];
+      int base = (int)cc.size();
+      for (int q = 0; q <= s.nconstr; ++q) cp.push_back(base + s.c_ptr[q]);
+      cc.insert(cc.end(), s.c_col.begin(), s.c_col.end());
+      cv.insert(cv.end(), s.c_val.begin(), s.c_val.end());
+      cm.insert(cm.end(), s.indrowc.begin(), s.indrowc.end());
+    }
+    D.c_ptr = upload(cp, own, st);
+    D.c_col = upload(cc, own, st);
+    D.c_val = upload(cv, own, st);
+    D.cmap = upload(cm, own, st);
+    // coarse dof owners
+    D.ndofc = S.ndofc;
+    vector<int> cptrv(D.ndofc + 1, 0), csub, cloc;
+    for (int t = 0; t < nsub; ++t) for (int q : S.subs[t].indrowc) cptrv[q + 1]++;
+    for (int q = 0; q < D.ndofc; ++q) cptrv[q + 1] += cptrv[q];
+    csub.resize(cptrv[D.ndofc]); cloc.resize(cptrv[D.ndofc]);
+    vector<int> cpos(cptrv.begin(), cptrv.end() - 1);
+    for (int t = 0; t < nsub; ++t)
+      for (int c = 0; c < S.subs[t].nconstr; ++c) {
+        int q = S.subs[t].indrowc[c];
+        csub[cpos[q]] = t; cloc[cpos[q]++] = c;
+      }
+    D.co_ptr = upload(cptrv, own, st);
+    D.co_sub = upload(csub, own, st);
+    D.co_loc = upload(cloc, own, st);
+  }
+  D.rcpart = dalloc<double>((size_t)nsub * D.nrb * D.ncpmax, own);
+  CK(cudaMemsetAsync(D.rcpart, 0, (size_t)nsub * D.nrb * D.ncpmax * sizeof(double), st));
+  D.rc = dalloc<double>(std::max(1, D.ndofc), own);
+  D.uc = dalloc<double>(std::max(1, D.ndofc), own);
+  D.prof.begin(PH_NUMERIC_TOTAL, st, true);
   // ---- preconditioner blocks: Srho factor, [Srho^-1 | Y], G^-1, Phi, Z, local coarse matrices
   vector<BandDesc> hbs(nsub);
   for (int t = 0; t < nsub; ++t) {
@@ -711,43 +772,43 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
   D.prof.begin(PH_SRHO_FACTOR, st);
   if constexpr (std::is_same_v<T, float>)
     k_fill_srho<T, float2><<<dim3(D.maxNI / 16, D.maxNI / 16, nsub), dim3(16, 16), 0, st>>>(
-        D.ds, static_cast<const float2*>(D.poolS), poolT, bd_s);
+        D.ds, static_cast<const float2*>(D.poolS), poolP, bd_s);
   else
     k_fill_srho<T, double><<<dim3(D.maxNI / 16, D.maxNI / 16, nsub), dim3(16, 16), 0, st>>>(
-        D.ds, reinterpret_cast<const double*>(D.poolS), poolT, bd_s);
+        D.ds, reinterpret_cast<const double*>(D.poolS), poolP, bd_s);
   CKL();
   if (maxnc > 0) {
-    k_add_penalty<T><<<dim3(maxnc, nsub), 256, 0, st>>>(D.ds, D.c_ptr, D.c_col, D.c_val, poolT, bd_s);
+    k_add_penalty<T><<<dim3(1, nsub), 256, 0, st>>>(D.ds, D.c_ptr, D.c_col, D.c_val, poolP, bd_s);
     CKL();
   }
-  run_factor<T>(D, bd_s, nsub, maxnbi, maxnbi - 1, poolT);
+  run_factor<T>(D, bd_s, nsub, maxnbi, maxnbi - 1, poolP);
   TcDesc* td_s = nullptr;
   if constexpr (std::is_same_v<T, float>) {
     vector<TcDesc> hts(nsub);
     for (int t = 0; t < nsub; ++t) {
       auto& d = D.hs[t];
-      hts[t] = TcDesc{d.nbi, d.nbi - 1, d.NRC, d.NI, d.oBs, poff[t][2], poff[t][3], -1};  // [I | C^T]
+      hts[t] = TcDesc{d.nbi, d.nbi - 1, d.NRC, d.NI, d.oBs, poff[t][0], poff[t][1], -1};  // [I | C^T]
     }
     td_s = upload(hts, own, st);
-    run_panels(D, bd_s, td_s, nsub, maxnbi, maxnbi - 1, poolT, ppool);
+    run_panels(D, bd_s, td_s, nsub, maxnbi, maxnbi - 1, poolP, ppool);
   }
   D.prof.end(PH_SRHO_FACTOR, st);
   D.prof.begin(PH_SRHO_SOLVE, st);
-  k_fill_rhs_srho<T><<<dim3((D.maxNI + 127) / 128, nsub), 128, 0, st>>>(D.ds, D.c_ptr, D.c_col, D.c_val, poolT);
+  k_fill_rhs_srho<T><<<dim3((D.maxNI + 127) / 128, nsub), 128, 0, st>>>(D.ds, D.c_ptr, D.c_col, D.c_val, poolP);
   CKL();
-  if constexpr (std::is_same_v<T, float>) run_solve_tc(D, td_s, nsub, maxnbi, maxNRC, ppool, poolT);
-  else run_solve<T>(D, bd_s, nsub, maxnbi, maxNRC, poolT, poolT);
+  if constexpr (std::is_same_v<T, float>) run_solve_tc(D, td_s, nsub, maxnbi, maxNRC, ppool, poolP);
+  else run_solve<T>(D, bd_s, nsub, maxnbi, maxNRC, poolP, poolP);
   D.prof.end(PH_SRHO_SOLVE, st);
   D.prof.begin(PH_PC_BLOCKS, st);
   {
     size_t smem = 2 * (size_t)std::max(1, maxnc) * std::max(1, maxnc) * sizeof(double);
     CK(cudaFuncSetAttribute(k_small_g<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_small_g<T><<<nsub, 256, smem, st>>>(D.ds, D.c_ptr, D.c_col, D.c_val, poolT, D.small, D.err);
+    k_small_g<T><<<nsub, 256, smem, st>>>(D.ds, D.c_ptr, D.c_col, D.c_val, poolP, D.small, D.err);
     CKL();
   }
-  k_phi<T><<<dim3((D.maxNI * D.ncpmax + 255) / 256, nsub), 256, 0, st>>>(D.ds, poolT, D.small, poolPC);
+  k_phi<T><<<dim3((D.maxNI * D.ncpmax + 255) / 256, nsub), 256, 0, st>>>(D.ds, poolP, D.small, poolPC);
   CKL();
-  k_z<T><<<dim3(D.maxNI / 16, D.maxNI / 16, nsub), dim3(16, 16), 0, st>>>(D.ds, poolT, poolPC);
+  k_z<T><<<dim3(D.maxNI / 16, D.maxNI / 16, nsub), dim3(16, 16), 0, st>>>(D.ds, poolP, poolPC);
   CKL();
   k_symmetrize<T><<<dim3(D.maxNI / 32, D.maxNI / 32, nsub), dim3(32, 8), 0, st>>>(D.ds, poolPC, 1);
   CKL();
@@ -818,11 +879,334 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
     D.cres = dalloc<double>(std::max(1, nc_g), own);
   }
   D.prof.end(PH_COARSE, st);
-  // ---- assembled reduced rhs (module_dd.f90:7090-7135)
-  k_assemble_plain<<<(D.n + 255) / 256, 256, 0, st>>>(D.n, D.own, D.grep, nullptr, D.g);
-  CKL();
   D.prof.end(PH_NUMERIC_TOTAL, st);
   CK(cudaStreamSynchronize(st));
+}
+
+// ------------------------------------------------------------ adaptive constraints
+// Batched LOBPCG over all face pairs (adaptivity_solve_eigenvectors,
+// module_adaptivity.f90:296-2514; 15 iterations as lobpcg_maxit, :38), then
+// the eigenvectors above the threshold become face constraints
+// (host_load_adaptive).  Uses S and the subdomain corrections Z of the
+// preconditioner built from the standard constraints.
+template <typename T>
+static void adaptive_constraints(Solver& S, Device& D) {
+  const double t0 = wall_time();
+  cudaStream_t st = D.st;
+  // null spaces of the floating subdomains' Schur complements: Phi times the null
+  // vectors of the local coarse matrix Phi^T S Phi
+  const int nsub = D.nsub;
+  vector<vector<double>> nulls(nsub);
+  {
+    long long nsm = 0;
+    for (auto& d : D.hs) nsm = std::max(nsm, d.oAc + (long long)d.ncp * d.ncp);
+    vector<double> hsmall(std::max<long long>(1, nsm));
+    CK(cudaMemcpyAsync(hsmall.data(), D.small, nsm * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    for (int t = 0; t < nsub; ++t) {
+      if (S.subs[t].bc_present || D.hs[t].nc == 0) continue;
+      const DevSub& d = D.hs[t];
+      int dn = 0;
+      vector<double> y = host_coarse_null_coefficients(d.nc, d.ncp, hsmall.data() + d.oAc, dn);
+      if (dn == 0) continue;
+      vector<T> phi((size_t)d.NI * d.ncp);
+      CK(cudaMemcpyAsync(phi.data(), static_cast<const T*>(D.poolPC) + d.oPhi, phi.size() * sizeof(T),
+                         cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+      vector<double>& nv = nulls[t];
+      nv.assign((size_t)d.ni * dn, 0.0);
+      for (int c = 0; c < dn; ++c) {
+        for (int r = 0; r < d.ni; ++r) {
+          double acc = 0.0;
+          for (int q = 0; q < d.nc; ++q) acc += (double)phi[(size_t)r * d.ncp + q] * y[(size_t)q * dn + c];
+          nv[(size_t)c * d.ni + r] = acc;
+        }
+        // orthonormalise against the previous columns (twice)
+        for (int pass = 0; pass < 2; ++pass)
+          for (int c2 = 0; c2 < c; ++c2) {
+            double tt = 0.0;
+            for (int r = 0; r < d.ni; ++r) tt += nv[(size_t)c2 * d.ni + r] * nv[(size_t)c * d.ni + r];
+            for (int r = 0; r < d.ni; ++r) nv[(size_t)c * d.ni + r] -= tt * nv[(size_t)c2 * d.ni + r];
+          }
+        double nn = 0.0;
+        for (int r = 0; r < d.ni; ++r) nn += nv[(size_t)c * d.ni + r] * nv[(size_t)c * d.ni + r];
+        nn = std::sqrt(nn);
+        for (int r = 0; r < d.ni; ++r) nv[(size_t)c * d.ni + r] = nn > 0 ? nv[(size_t)c * d.ni + r] / nn : 0.0;
+      }
+    }
+  }
+  AdaptivePairs P;
+  host_adaptive_pairs(S, P, nulls);
+  S.stats.npair = P.npair;
+  const int np = P.npair;
+  vector<double> eig((size_t)std::max(1, np) * AD_KM, 0.0), cons;
+  if (np > 0) {
+    std::vector<void*> tmp;  // freed at the end of this step
+    vector<PairDev> hp(np);
+    for (int p = 0; p < np; ++p) {
+      if (P.m[p] > AD_MAXM) throw Error{ERR_UNSUPPORTED, "more than 48 coarse dofs shared by a face pair"};
+      hp[p] = PairDev{P.si[p], P.sj[p], P.ni[p], P.n[p], P.m[p], P.k[p], P.cptr[p], P.cptr[p + 1], P.vo[p], P.qo[p]};
+    }
+    PairDev* pd = upload(hp, tmp, st);
+    double* dq = upload(P.q, tmp, st);
+    int* dca = upload(P.ca, tmp, st);
+    int* dcb = upload(P.cb, tmp, st);
+    double* dwa = upload(P.wa, tmp, st);
+    double* dwb = upload(P.wb, tmp, st);
+    const long long nvec = P.nvec;
+    double* va = dalloc<double>((size_t)AB_NBLK * nvec, tmp);
+    CK(cudaMemsetAsync(va, 0, (size_t)AB_NBLK * nvec * sizeof(double), st));
+    double* G = dalloc<double>((size_t)np * 2 * AD_NB * AD_NB, tmp);
+    CK(cudaMemsetAsync(G, 0, (size_t)np * 2 * AD_NB * AD_NB * sizeof(double), st));
+    double* C = dalloc<double>((size_t)np * AD_NB * AD_KM, tmp);
+    double* lam = dalloc<double>((size_t)np * AD_KM, tmp);
+    CK(cudaMemsetAsync(lam, 0, (size_t)np * AD_KM * sizeof(double), st));
+    // pair coarse problems for the preconditioner: K = assembled Phi^T S Phi of
+    // both subdomains over the union of their coarse dofs, regularised along
+    // the coarse values of null(S) within null(D), inverted on the host
+    vector<int> hnu(np), hmofs(np), hmap;
+    vector<long long> hkofs(np);
+    vector<double> hkinv;
+    {
+      long long nsm = 0;
+      for (auto& d : D.hs) nsm = std::max(nsm, d.oAc + (long long)d.ncp * d.ncp);
+      vector<double> hsmall(std::max<long long>(1, nsm));
+      CK(cudaMemcpyAsync(hsmall.data(), D.small, nsm * sizeof(double), cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+      vector<vector<int>> maps(np);
+      vector<vector<double>> kinv(np);
+      std::string errs;
+#pragma omp parallel for schedule(dynamic)
+      for (int p = 0; p < np; ++p) {
+        const Subdomain& A = S.subs[P.si[p]];
+        const Subdomain& Bs = S.subs[P.sj[p]];
+        const DevSub& di = D.hs[P.si[p]];
+        const DevSub& dj = D.hs[P.sj[p]];
+        std::unordered_map<int, int> pos;
+        vector<int>& mp = maps[p];
+        int nu = 0;
+        for (int qq = 0; qq < A.nconstr; ++qq) { pos[A.indrowc[qq]] = nu; mp.push_back(nu++); }
+        for (int qq = 0; qq < Bs.nconstr; ++qq) {
+          auto it = pos.find(Bs.indrowc[qq]);
+          if (it != pos.end()) mp.push_back(it->second);
+          else { pos[Bs.indrowc[qq]] = nu; mp.push_back(nu++); }
+        }
+        hnu[p] = nu;
+        if (nu > AD_NUMAX) {
+#pragma omp critical
+          errs = "more than 256 coarse dofs in a face pair";
+          continue;
+        }
+        vector<double> K((size_t)nu * nu, 0.0);
+        for (int a = 0; a < A.nconstr; ++a)
+          for (int b = 0; b < A.nconstr; ++b) K[(size_t)mp[a] * nu + mp[b]] += hsmall[di.oAc + (long long)a * di.ncp + b];
+        for (int a = 0; a < Bs.nconstr; ++a)
+          for (int b = 0; b < Bs.nconstr; ++b)
+            K[(size_t)mp[A.nconstr + a] * nu + mp[A.nconstr + b]] += hsmall[dj.oAc + (long long)a * dj.ncp + b];
+        double kmax = 0.0;
+        for (int a = 0; a < nu; ++a) kmax = std::max(kmax, K[(size_t)a * nu + a]);
+        for (int c = P.md[p]; c < P.m[p]; ++c) {  // coarse values y = C v of the null directions
+          const double* v = &P.q[P.qo[p] + (long long)c * P.n[p]];
+          vector<double> y(nu, 0.0);
+          for (int r = 0; r < A.nconstr; ++r) {
+            double t = 0.0;
+            for (int e = A.c_ptr[r]; e < A.c_ptr[r + 1]; ++e) t += A.c_val[e] * v[A.c_col[e]];
+            y[mp[r]] = t;
+          }
+          for (int r = 0; r < Bs.nconstr; ++r) {
+            double t = 0.0;
+            for (int e = Bs.c_ptr[r]; e < Bs.c_ptr[r + 1]; ++e) t += Bs.c_val[e] * v[P.ni[p] + Bs.c_col[e]];
+            y[mp[A.nconstr + r]] = t;
+          }
+          double yy = 0.0;
+          for (double x : y) yy += x * x;
+          if (yy > 0)
+            for (int a = 0; a < nu; ++a)
+              for (int b = 0; b < nu; ++b) K[(size_t)a * nu + b] += kmax * y[a] * y[b] / yy;
+        }
+        // Cholesky, then the explicit inverse
+        vector<double> L = K;
+        bool ok = true;
+        for (int j = 0; j < nu && ok; ++j) {
+          double sum = L[(size_t)j * nu + j];
+          for (int t = 0; t < j; ++t) sum -= L[(size_t)j * nu + t] * L[(size_t)j * nu + t];
+          if (!(sum > 1e-14 * kmax)) { ok = false; break; }
+          const double dj2 = std::sqrt(sum);
+          L[(size_t)j * nu + j] = dj2;
+          for (int i = j + 1; i < nu; ++i) {
+            double t = L[(size_t)i * nu + j];
+            for (int k2 = 0; k2 < j; ++k2) t -= L[(size_t)i * nu + k2] * L[(size_t)j * nu + k2];
+            L[(size_t)i * nu + j] = t / dj2;
+          }
+        }
+        vector<double>& Ki = kinv[p];
+        Ki.assign((size_t)nu * nu, 0.0);
+        if (!ok) continue;  // singular pair coarse problem: no coarse correction for this pair
+        for (int c = 0; c < nu; ++c) {
+          vector<double> x(nu, 0.0);
+          x[c] = 1.0;
+          for (int i = 0; i < nu; ++i) {
+            double t = x[i];
+            for (int k2 = 0; k2 < i; ++k2) t -= L[(size_t)i * nu + k2] * x[k2];
+            x[i] = t / L[(size_t)i * nu + i];
+          }
+          for (int i = nu - 1; i >= 0; --i) {
+            double t = x[i];
+            for (int k2 = i + 1; k2 < nu; ++k2) t -= L[(size_t)k2 * nu + i] * x[k2];
+            x[i] = t / L[(size_t)i * nu + i];
+          }
+          for (int i = 0; i < nu; ++i) Ki[(size_t)i * nu + c] = x[i];
+        }
+      }
+      if (!errs.empty()) throw Error{ERR_UNSUPPORTED, errs};
+      long long ko = 0;
+      for (int p = 0; p < np; ++p) {
+        hmofs[p] = (int)hmap.size();
+        hmap.insert(hmap.end(), maps[p].begin(), maps[p].end());
+        hkofs[p] = ko;
+        ko += (long long)hnu[p] * hnu[p];
+        hkinv.insert(hkinv.end(), kinv[p].begin(), kinv[p].end());
+      }
+    }
+    PairCoarse pcoarse{upload(hnu, tmp, st), upload(hmofs, tmp, st), upload(hmap, tmp, st), upload(hkofs, tmp, st),
+                       upload(hkinv, tmp, st)};
+    // column tables of the batched products: per subdomain, every pair column it takes part in
+    struct Tab { vector<int> ptr; vector<long long> in, out; int maxc = 0; ColTab dev{}; };
+    auto build = [&](std::initializer_list<std::pair<int, int>> io) {
+      Tab t;
+      vector<vector<long long>> in(nsub), out(nsub);
+      for (int p = 0; p < np; ++p)
+        for (int side = 0; side < 2; ++side) {
+          const int sub = side == 0 ? P.si[p] : P.sj[p];
+          const long long roff = side == 0 ? 0 : P.ni[p];
+          for (auto& pr : io)
+            for (int c = 0; c < P.k[p]; ++c) {
+              in[sub].push_back(pr.first * nvec + P.vo[p] + (long long)c * P.n[p] + roff);
+              out[sub].push_back(pr.second * nvec + P.vo[p] + (long long)c * P.n[p] + roff);
+            }
+        }
+      t.ptr.assign(nsub + 1, 0);
+      for (int s2 = 0; s2 < nsub; ++s2) {
+        t.ptr[s2 + 1] = t.ptr[s2] + (int)in[s2].size();
+        t.maxc = std::max(t.maxc, (int)in[s2].size());
+        t.in.insert(t.in.end(), in[s2].begin(), in[s2].end());
+        t.out.insert(t.out.end(), out[s2].begin(), out[s2].end());
+      }
+      t.dev.ptr = upload(t.ptr, tmp, st);
+      t.dev.in = upload(t.in, tmp, st);
+      t.dev.out = upload(t.out, tmp, st);
+      return t;
+    };
+    Tab tabX = build({{AB_T1, AB_T2}, {AB_X, AB_BX}});
+    Tab tabW = build({{AB_T1, AB_T2}, {AB_W, AB_BW}});
+    Tab tabZ = build({{AB_T1, AB_W}});
+    int maxn = 0;
+    for (int p = 0; p < np; ++p) maxn = std::max(maxn, P.n[p]);
+    const dim3 gpair(np);
+    auto gemm_s = [&](const Tab& t) {
+      if (t.maxc == 0) return;
+      dim3 g((D.maxNI + 63) / 64, (t.maxc + 63) / 64, nsub);
+      if (D.mixed)
+        k_ad_gemm<float2, false, double><<<g, 256, 0, st>>>(D.ds, static_cast<const float2*>(D.poolS), t.dev, va);
+      else
+        k_ad_gemm<double, false, double><<<g, 256, 0, st>>>(D.ds, static_cast<const double*>(D.poolS), t.dev, va);
+      CKL();
+    };
+    auto project = [&](int b0, int b1) {
+      k_ad_project<<<dim3(np, b1 >= 0 ? 2 : 1), 256, 0, st>>>(pd, dq, va, nvec, b0, b1);
+      CKL();
+    };
+    // (A b, B b) for a projected block b (X or W)
+    auto apply_ab = [&](int b, int ab, int bb, const Tab& t) {
+      (void)bb;
+      k_ad_ire<<<gpair, 256, 0, st>>>(pd, dca, dcb, dwa, dwb, va, nvec, b, AB_T1, 0);
+      CKL();
+      gemm_s(t);
+      k_ad_ire<<<gpair, 256, 0, st>>>(pd, dca, dcb, dwa, dwb, va, nvec, AB_T2, ab, 1);
+      CKL();
+      project(ab, bb);
+    };
+    auto rayleigh_ritz = [&](int nb) {
+      k_ad_gram<<<dim3(np, 6, 2), 256, 0, st>>>(pd, va, nvec, G, nb);
+      CKL();
+      k_ad_rr<<<np, 32, 0, st>>>(pd, G, C, lam, nb);
+      CKL();
+      k_ad_update<<<dim3(np, 3, (maxn + 127) / 128), 128, 0, st>>>(pd, va, nvec, C, nb);
+      CKL();
+    };
+    k_ad_random<<<gpair, 256, 0, st>>>(pd, va, nvec);
+    CKL();
+    project(AB_X, -1);
+    apply_ab(AB_X, AB_AX, AB_BX, tabX);
+    rayleigh_ritz(1);
+    const int maxit = 15;
+    for (int it = 1; it <= maxit; ++it) {
+      k_ad_residual<<<dim3(np, (maxn + 255) / 256), 256, 0, st>>>(pd, va, nvec, lam);
+      CKL();
+      // W = P Z P R
+      if (tabZ.maxc > 0) {
+        dim3 g((D.maxNI + 63) / 64, (tabZ.maxc + 63) / 64, nsub);
+        k_ad_gemm<T, true, float><<<g, 256, 0, st>>>(D.ds, static_cast<const T*>(D.poolPC), tabZ.dev, va);
+        CKL();
+      }
+      k_ad_coarse<T><<<dim3(np, AD_KM), 256, 0, st>>>(pd, pcoarse, D.ds, static_cast<const T*>(D.poolPC), va, nvec);
+      CKL();
+      project(AB_W, -1);
+      apply_ab(AB_W, AB_AW, AB_BW, tabW);
+      rayleigh_ritz(it == 1 ? 2 : 3);
+    }
+    S.stats.lobpcg_iter = maxit;
+    double* rn = dalloc<double>((size_t)np * AD_KM, tmp);
+    CK(cudaMemsetAsync(rn, 0, (size_t)np * AD_KM * sizeof(double), st));
+    k_ad_resnorm<<<dim3(np, AD_KM), 256, 0, st>>>(pd, va, nvec, lam, rn);
+    CKL();
+    vector<double> hrn((size_t)np * AD_KM);
+    CK(cudaMemcpyAsync(eig.data(), lam, eig.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(hrn.data(), rn, hrn.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    S.stats.lobpcg_resid = 0;
+    for (int p = 0; p < np; ++p)
+      for (int c = 0; c < P.k[p]; ++c)
+        if (eig[(size_t)p * AD_KM + c] >= S.prm.adaptive_tau)
+          S.stats.lobpcg_resid = std::max(S.stats.lobpcg_resid, hrn[(size_t)p * AD_KM + c]);
+    // A x of the selected eigenvectors
+    vector<long long> src, dst;
+    vector<int> len;
+    long long tot = 0;
+    double est = -1.0;
+    for (int p = 0; p < np; ++p) {
+      int nad = 0;
+      for (int c = 0; c < P.k[p]; ++c)
+        if (eig[(size_t)p * AD_KM + c] >= S.prm.adaptive_tau) {
+          src.push_back(AB_AX * nvec + P.vo[p] + (long long)c * P.n[p]);
+          dst.push_back(tot);
+          len.push_back(P.n[p]);
+          tot += P.n[p];
+          ++nad;
+        }
+      // estimate of the condition number (module_adaptivity.f90:2156-2170)
+      double el = 1.0;
+      if (P.k[p] > 0) el = nad < P.k[p] ? eig[(size_t)p * AD_KM + nad] : eig[(size_t)p * AD_KM + nad - 1];
+      est = std::max(est, el);
+    }
+    S.stats.adapt_est = est;
+    cons.assign(std::max<long long>(1, tot), 0.0);
+    if (!src.empty()) {
+      long long* dsrc = upload(src, tmp, st);
+      long long* ddst = upload(dst, tmp, st);
+      int* dlen = upload(len, tmp, st);
+      double* dout = dalloc<double>((size_t)tot, tmp);
+      k_ad_gather<<<(int)src.size(), 256, 0, st>>>(va, dsrc, ddst, dlen, dout);
+      CKL();
+      CK(cudaMemcpyAsync(cons.data(), dout, (size_t)tot * sizeof(double), cudaMemcpyDeviceToHost, st));
+    }
+    CK(cudaStreamSynchronize(st));
+    for (void* q : tmp) cudaFreeAsync(q, st);
+  }
+  S.adaptive_eigs = eig;
+  S.adaptive_pairs = P;
+  host_load_adaptive(S, P, eig, cons);
+  S.stats.t_adaptive = wall_time() - t0;
 }
 
 // ------------------------------------------------------------ PCG driver

@@ -330,6 +330,57 @@ void host_new_data(Solver& S) {
   host_interface_bc(S);
 }
 
+void host_constraint_rows(Solver& S) {
+  const int nsub = (int)S.subs.size();
+  const int ncnode = S.ncorner + S.nedge + S.nface;
+  vector<int> nndfc(ncnode, -1);
+  for (auto& s : S.subs)
+    for (auto& cn : s.cnodes) {
+      int& slot = nndfc[cn.global_number - 1];
+      if (slot >= 0 && slot != cn.ncdof) throw Error{ERR_NUMERIC, "inconsistent coarse node dof count"};
+      slot = cn.ncdof;
+    }
+  vector<int> kdofc(ncnode + 1, 0);
+  for (int c = 0; c < ncnode; ++c) kdofc[c + 1] = kdofc[c] + std::max(0, nndfc[c]);
+  S.ndofc = kdofc[ncnode];
+#pragma omp parallel for schedule(dynamic)
+  for (int t = 0; t < nsub; ++t) {
+    auto& s = S.subs[t];
+    s.c_ptr.assign(1, 0); s.c_col.clear(); s.c_val.clear(); s.indrowc.clear();
+    for (auto& cn : s.cnodes) {
+      if (!cn.used) continue;
+      if (!cn.matrix.empty()) {  // explicit rows
+        const int nv = (int)cn.idofi.size();
+        for (int d = 0; d < cn.ncdof; ++d) {
+          for (int v = 0; v < nv; ++v) {
+            const double val = cn.matrix[(size_t)d * nv + v];
+            if (val != 0.0) { s.c_col.push_back(cn.idofi[v]); s.c_val.push_back(val); }
+          }
+          s.c_ptr.push_back((int)s.c_col.size());
+          s.indrowc.push_back(kdofc[cn.global_number - 1] + d);
+        }
+      } else if (cn.itype == 3) {
+        for (int d = 0; d < cn.ncdof; ++d) {
+          s.c_col.push_back(cn.idofi[d]); s.c_val.push_back(1.0);
+          s.c_ptr.push_back((int)s.c_col.size());
+          s.indrowc.push_back(kdofc[cn.global_number - 1] + d);
+        }
+      } else {
+        for (int d = 0; d < cn.ncdof; ++d) {  // row d: ones on the d-th dof of every node
+          for (int i : cn.inodi) {
+            int nd = s.iin[i];
+            if (d < s.nndf[nd]) { s.c_col.push_back(s.kdofi[i] + d); s.c_val.push_back(1.0); }
+          }
+          s.c_ptr.push_back((int)s.c_col.size());
+          s.indrowc.push_back(kdofc[cn.global_number - 1] + d);
+        }
+      }
+    }
+    s.nconstr = (int)s.indrowc.size();
+  }
+  S.stats.ndofc = S.ndofc;
+}
+
 void host_setup(Solver& S) {
   int nsub = (int)S.subs.size();
   for (int t = 0; t < nsub; ++t)
@@ -623,8 +674,6 @@ void host_setup(Solver& S) {
   S.nface = number_entities(S.ncorner + S.nedge, face_gid, face_num);
 
   // ---- coarse nodes and constraints
-  int ncnode = S.ncorner + S.nedge + S.nface;
-  vector<int> nndfc(ncnode, -1);
 #pragma omp parallel for schedule(dynamic)
   for (int t = 0; t < nsub; ++t) {
     auto& s = S.subs[t];
@@ -651,40 +700,7 @@ void host_setup(Solver& S) {
     for (size_t e = 0; e < edges[t].size(); ++e) add(2, edge_num[t][e], edges[t][e], S.prm.use_arith);
     for (size_t f = 0; f < faces[t].size(); ++f) add(1, face_num[t][f], faces[t][f], S.prm.use_arith);
   }
-  for (auto& s : S.subs)
-    for (auto& cn : s.cnodes) {
-      int& slot = nndfc[cn.global_number - 1];
-      if (slot >= 0 && slot != cn.ncdof) throw Error{ERR_NUMERIC, "inconsistent coarse node dof count"};
-      slot = cn.ncdof;
-    }
-  vector<int> kdofc(ncnode + 1, 0);
-  for (int c = 0; c < ncnode; ++c) kdofc[c + 1] = kdofc[c] + std::max(0, nndfc[c]);
-  S.ndofc = kdofc[ncnode];
-#pragma omp parallel for schedule(dynamic)
-  for (int t = 0; t < nsub; ++t) {
-    auto& s = S.subs[t];
-    s.c_ptr.assign(1, 0); s.c_col.clear(); s.c_val.clear(); s.indrowc.clear();
-    for (auto& cn : s.cnodes) {
-      if (!cn.used) continue;
-      if (cn.itype == 3) {
-        for (int d = 0; d < cn.ncdof; ++d) {
-          s.c_col.push_back(cn.idofi[d]); s.c_val.push_back(1.0);
-          s.c_ptr.push_back((int)s.c_col.size());
-          s.indrowc.push_back(kdofc[cn.global_number - 1] + d);
-        }
-      } else {
-        for (int d = 0; d < cn.ncdof; ++d) {  // row d: ones on the d-th dof of every node
-          for (int i : cn.inodi) {
-            int nd = s.iin[i];
-            if (d < s.nndf[nd]) { s.c_col.push_back(s.kdofi[i] + d); s.c_val.push_back(1.0); }
-          }
-          s.c_ptr.push_back((int)s.c_col.size());
-          s.indrowc.push_back(kdofc[cn.global_number - 1] + d);
-        }
-      }
-    }
-    s.nconstr = (int)s.indrowc.size();
-  }
+  host_constraint_rows(S);
 
   // ---- unique interface dofs (by global dof id) and per-dof sharing lists
   vector<int> gdof_uniq(ndof_global, -1);
@@ -745,6 +761,7 @@ void host_setup(Solver& S) {
         if (den == 0.0) throw Error{ERR_NUMERIC, "zero denominator in interface weights"};
         s.wi[i] = pr.first / den;
       }
+      s.rhoi = rho[t];
     }
   }
   S.iface_fixed.assign(S.ninterface, 0);

@@ -39,6 +39,9 @@ struct CoarseNode {
   vector<int> idofi;      // interface dofs of the glob
   int ncdof = 0;          // number of constraint rows it contributes
   bool used = false;
+  // explicit rows (ncdof x idofi.size(), row-major) once the face constraints
+  // have been made adaptive; empty = the corner / arithmetic-average rows
+  vector<double> matrix;
 };
 
 struct Subdomain {
@@ -80,6 +83,7 @@ struct Subdomain {
   vector<int> bcx_tgt, bcx_src;
   vector<double> bcx_val;
   vector<double> wi;         // interface weights
+  vector<double> rhoi;       // coefficients the weights are built from (module_dd.f90:11660-11722)
   vector<int> uniq;          // interface dof -> unique interface index
   // interior ordering used for the band factor: perm[new] = index into iovsvn
   vector<int> operm;
@@ -97,6 +101,7 @@ struct Params {
   bool use_corner = true, use_arith = true, use_adaptive = false, use_user = false;
   int weights_type = 0;
   int matrixtype = 1;
+  double adaptive_tau = 1.5;  // eigenvalue threshold of adaptive constraints (module_adaptivity.f90:30)
 };
 
 struct Stats {
@@ -118,6 +123,26 @@ struct Stats {
   double bytes_pc_local = 0;    // one local preconditioner apply
   double launches_setup = 0, launches_solve = 0;  // kernel launches of the last set-up / solve
   double t_dev_alloc = 0, t_dev_h2d = 0;  // device set-up: allocations, staging + host->device copies
+  // adaptive face constraints
+  int npair = 0, nadaptive = 0, lobpcg_iter = 0;
+  double adapt_est = -1, t_adaptive = 0, lobpcg_resid = 0;
+};
+
+// Face pairs of the adaptive constraint search (module_adaptivity.f90): the
+// space of both interfaces of a face's two subdomains, n = ni + nj rows
+// (first subdomain's interface dofs, then the second's).
+struct AdaptivePairs {
+  static constexpr int KMAX = 10;  // neigvecx, module_adaptivity.f90:44
+  int npair = 0;
+  vector<int> si, sj, fi, fj;      // subdomains and the face coarse node in each
+  vector<int> ni, n, m, k;         // first interface size, pair size, Q columns, eigenvectors
+  vector<int> md;                  // columns of Q from D (the rest span null(S) within null(D))
+  vector<long long> vo, qo;        // offsets of the pair's vector block (n x KMAX) and of Q (n x m)
+  vector<int> cptr;                // common dofs of pair p: [cptr[p], cptr[p + 1])
+  vector<int> ca, cb;              // their rows in the pair space (cb counts from 0 of the pair)
+  vector<double> wa, wb;           // weights rho_a / (rho_a + rho_b), rho_b / (rho_a + rho_b)
+  vector<double> q;                // orthonormal basis of range(D^T), column-major per pair
+  long long nvec = 0, nq = 0;      // total rows x KMAX, total Q entries
 };
 
 // Per-subdomain matrix blocks in device-ready form (interior rows in the
@@ -152,7 +177,22 @@ struct Solver {
   bool profiling = false;
   double t_upload = 0;              // accumulated time inside the upload calls
   vector<SubBlocks> blocks;         // device-ready blocks, freed after upload
+  // last adaptive constraint search: the pairs and their eigenvalues (KMAX per pair)
+  AdaptivePairs adaptive_pairs;
+  vector<double> adaptive_eigs;
 };
+
+// adaptive face constraints, host part (bddc_adaptive.cpp)
+// nulls[s]: orthonormal basis of null(S_s) on the interface (ndofi x d_s, column-major; empty if none)
+void host_adaptive_pairs(const Solver& S, AdaptivePairs& P, const vector<vector<double>>& nulls);
+// null space coefficients of a local coarse matrix (nc x nc in an ld x ld array): the
+// eigenvectors with |eigenvalue| <= 1e-5 max |eigenvalue|, nc x d column-major
+vector<double> host_coarse_null_coefficients(int nc, int ld, const double* ac, int& d);
+// eig: npair x KMAX eigenvalues (descending); cons: for every pair the columns A x of the
+// eigenvectors with eigenvalue >= tau, n rows each, packed pair after pair
+void host_load_adaptive(Solver& S, const AdaptivePairs& P, const vector<double>& eig, const vector<double>& cons);
+// global coarse numbering and the constraint rows of every subdomain from its coarse nodes
+void host_constraint_rows(Solver& S);
 
 // host setup (bddc_host.cpp)
 void host_assemble_upper(vector<int>& ia, vector<int>& ja, vector<double>& a);

@@ -532,18 +532,21 @@ __global__ void k_add_penalty(const DevSub* __restrict__ ds, const int* __restri
                               const double* __restrict__ cval, T* __restrict__ pool, const BandDesc* __restrict__ bd) {
   const DevSub s = ds[blockIdx.y];
   const BandDesc d = bd[blockIdx.y];
-  const int r = blockIdx.x;
-  if (r >= s.nc) return;
   const int* p = cptr + s.cptr;
-  int q0 = p[r], n = p[r + 1] - q0;
-  double nrm = 0.0;
-  for (int q = 0; q < n; ++q) nrm += cval[q0 + q] * cval[q0 + q];
-  double sc = s.rho / nrm;
-  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
-    int a = e / n, b = e % n;
-    int i = ccol[q0 + a], j = ccol[q0 + b];
-    if (j > i) continue;
-    pool[band_block(d, i / NB, j / NB) + (i % NB) * NB + j % NB] += T(sc * cval[q0 + a] * cval[q0 + b]);
+  // rows one after the other: rows of one coarse node (several constraints on
+  // a face) share their entries, and a fixed order keeps the sum deterministic
+  for (int r = 0; r < s.nc; ++r) {
+    const int q0 = p[r], n = p[r + 1] - q0;
+    double nrm = 0.0;
+    for (int q = 0; q < n; ++q) nrm += cval[q0 + q] * cval[q0 + q];
+    const double sc = s.rho / nrm;
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+      int a = e / n, b = e % n;
+      int i = ccol[q0 + a], j = ccol[q0 + b];
+      if (j > i) continue;
+      pool[band_block(d, i / NB, j / NB) + (i % NB) * NB + j % NB] += T(sc * cval[q0 + a] * cval[q0 + b]);
+    }
+    __syncthreads();
   }
 }
 

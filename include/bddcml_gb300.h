@@ -180,6 +180,19 @@ void bddcml_get_profile_c(double *ms, int *counts, int *lphase);
  * No counterpart in the reference. */
 void bddcml_release_device_memory_c(void);
 
+/* Eigenvalue threshold tau of the adaptive face constraints (no counterpart in
+ * the reference, which fixes it at 1.5: threshold_eigval_default,
+ * module_adaptivity.f90:30).  Eigenvectors of the face-pair problems with
+ * eigenvalue >= tau become constraints.  Takes effect at the next
+ * bddcml_setup_preconditioner_c; tau must be positive (BDDCML_ERR_ARGUMENT). */
+void bddcml_set_adaptive_threshold_c(double *tau);
+
+/* Face pairs of the last adaptive setup (no counterpart in the reference):
+ * for p < min(*lpair, npair), pairs[3p..3p+2] = the two subdomains (numbase
+ * applied) and the number of computed eigenvalues k, eigs[10p..10p+9] the
+ * eigenvalues in descending order (zero beyond k).  *lpair returns npair. */
+void bddcml_get_adaptive_info_c(int *pairs, double *eigs, int *lpair);
+
 /* Per-element gradient of an objective J(u) with respect to element
  * coefficients kappa_e, for K(kappa) = sum_e kappa_e K_e^0:
  *     grad[e] = dJ/dkappa_e = - lambda_e^T K_e^0 u_e,

@@ -120,7 +120,7 @@ def test_errors_are_status_codes(built_lib):
     assert B.last_error()[0] == 4
 
 
-def test_solve_defaults_report_unsupported_bicgstab(built_lib):
+def test_setup_without_gpu_reports_an_error(built_lib):
     import bddcml_gb300 as B
     from bddcml_gb300 import problems
     prob = problems.poisson_on_cube(4, 2)
