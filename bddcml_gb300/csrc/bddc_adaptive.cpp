@@ -65,8 +65,11 @@ vector<double> host_coarse_null_coefficients(int nc, int ld, const double* ac, i
   for (double x : w) wmax = std::max(wmax, std::fabs(x));
   vector<double> y;
   d = 0;
+  // the tolerance of Octave's null() relaxed as in module_adaptivity.f90:1485-1489
+  // (n * max eigenvalue * 4 eps), with the 2^-44 accuracy of the products
+  const double tol = std::max(1, nc) * wmax * 4.0 * 5.7e-14;
   for (int k = 0; k < nc; ++k)
-    if (std::fabs(w[k]) <= 1e-5 * wmax) {
+    if (std::fabs(w[k]) <= tol) {
       for (int r = 0; r < nc; ++r) y.push_back(z[(size_t)r * nc + k]);
       ++d;
     }

@@ -216,6 +216,90 @@ __global__ void __launch_bounds__(256) k_ad_gemm(const DevSub* __restrict__ ds, 
   }
 }
 
+// The same batched product with S as the float2 pair hi + lo in double-float
+// arithmetic on the FP32 pipes (GB300's FP64 rate is a small fraction of its
+// FP32 rate): the input column is split into x_hi + x_lo, each multiply-add is
+// the exact product a_hi x_hi (a rounded product and its fma error) plus the
+// cross terms a_hi x_lo + a_lo x_hi, accumulated as an unevaluated sum
+// (s_hi, s_lo) with an error-free two-sum.  Accuracy about 2^-44 relative to
+// sum |a x|, FP64-like for these products.
+__device__ __forceinline__ void df_mac(float& sh, float& sl, float ah, float al, float bh, float bl) {
+  const float p = __fmul_rn(ah, bh);
+  const float e = __fmaf_rn(ah, bh, -p);
+  const float c = __fmaf_rn(ah, bl, __fmaf_rn(al, bh, e));
+  const float t = __fadd_rn(sh, p);
+  const float bp = __fsub_rn(t, sh);
+  const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+  sh = t;
+  sl = __fadd_rn(sl, __fadd_rn(err, c));
+}
+
+__global__ void __launch_bounds__(256) k_ad_gemm_df(const DevSub* __restrict__ ds, const float2* __restrict__ Spool,
+                                                    ColTab tab, double* __restrict__ va) {
+  const int s = blockIdx.z;
+  const DevSub d = ds[s];
+  const int r0 = blockIdx.x * 64;
+  const int cbeg = tab.ptr[s], ncol = tab.ptr[s + 1] - cbeg;
+  const int c0 = blockIdx.y * 64;
+  if (r0 >= d.ni || c0 >= ncol) return;
+  const float2* M = Spool + d.oS;
+  __shared__ float Ah[32][64 + 4], Al[32][64 + 4], Bh[32][64 + 4], Bl[32][64 + 4];
+  __shared__ long long inoff[64], outoff[64];
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  if (tid < 64) {
+    const bool ok = c0 + tid < ncol;
+    inoff[tid] = ok ? tab.in[cbeg + c0 + tid] : -1;
+    outoff[tid] = ok ? tab.out[cbeg + c0 + tid] : -1;
+  }
+  float sh[4][4], sl[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) { sh[i][j] = 0.f; sl[i][j] = 0.f; }
+  __syncthreads();
+  for (int k0 = 0; k0 < d.ni; k0 += 32) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int e = tid + 256 * i;
+      const int row = e >> 5, kk = e & 31;
+      const int gr = r0 + row, gk = k0 + kk;
+      float2 a = make_float2(0.f, 0.f);
+      if (gr < d.ni && gk < d.ni) a = M[(long long)gr * d.NI + gk];
+      Ah[kk][row] = a.x;
+      Al[kk][row] = a.y;
+      const long long io = inoff[row];  // row doubles as the column index of the B tile
+      const double x = (io >= 0 && gk < d.ni) ? va[io + gk] : 0.0;
+      const float xh = (float)x;
+      Bh[kk][row] = xh;
+      Bl[kk][row] = (float)(x - (double)xh);
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int kk = 0; kk < 32; ++kk) {
+      float ah[4], al[4], bh[4], bl[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) { ah[i] = Ah[kk][ty * 4 + i]; al[i] = Al[kk][ty * 4 + i]; }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) { bh[j] = Bh[kk][tx * 4 + j]; bl[j] = Bl[kk][tx * 4 + j]; }
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) df_mac(sh[i][j], sl[i][j], ah[i], al[i], bh[j], bl[j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int gr = r0 + ty * 4 + i;
+    if (gr >= d.ni) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const long long oo = outoff[tx * 4 + j];
+      if (oo >= 0) va[oo + gr] = (double)sh[i][j] + (double)sl[i][j];
+    }
+  }
+}
+
 // Gram blocks G_{A,B}[u][v] = basis_u^T image_v for u <= v < nb (basis X, W, Y;
 // images AX.. or BX..), k x k each, into G[p][which][NB][NB].
 // Grid (npair, 6, 2).
@@ -308,7 +392,8 @@ __device__ void ad_jacobi(double (*a)[33], double (*z)[33], int nn) {
 }
 
 // Rayleigh-Ritz on span(basis), nb blocks of k columns: SVQB on G_B (scaled
-// to unit diagonal, directions below 1e-10 of the largest dropped), then the
+// to unit diagonal, directions below 1e-8 of the largest dropped: below that
+// the Gram entries are at the noise level of the S products), then the
 // largest k eigenpairs of V^T G_A V.  C (nb k x k, row-major in C[p]) maps the
 // basis to the new X; lam receives the Ritz values (descending).  One warp per pair.
 __global__ void __launch_bounds__(32) k_ad_rr(const PairDev* __restrict__ pd, const double* __restrict__ G,
@@ -334,13 +419,13 @@ __global__ void __launch_bounds__(32) k_ad_rr(const PairDev* __restrict__ pd, co
     if (lane < nn) a[r][lane] *= dsc[r] * dsc[lane];
   __syncwarp();
   ad_jacobi(a, z, nn);
-  // keep the directions with sigma > 1e-10 max sigma
+  // keep the directions with sigma > 1e-8 max sigma
   if (lane == 0) {
     double smax = 0.0;
     for (int r = 0; r < nn; ++r) smax = fmax(smax, a[r][r]);
     int cnt = 0;
     for (int r = 0; r < nn; ++r)
-      if (a[r][r] > 1e-10 * smax && smax > 0.0) keep[cnt++] = r;
+      if (a[r][r] > 1e-8 * smax && smax > 0.0) keep[cnt++] = r;
     nkeep = cnt;
   }
   __syncwarp();

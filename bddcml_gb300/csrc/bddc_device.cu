@@ -893,45 +893,96 @@ template <typename T>
 static void adaptive_constraints(Solver& S, Device& D) {
   const double t0 = wall_time();
   cudaStream_t st = D.st;
-  // null spaces of the floating subdomains' Schur complements: Phi times the null
-  // vectors of the local coarse matrix Phi^T S Phi
+  // null spaces of the floating subdomains' Schur complements: Phi y for the
+  // null vectors y of Phi^T S Phi, formed with FP64-accurate S products (the
+  // null-space projection of module_adaptivity.f90:1180-1480, per subdomain)
   const int nsub = D.nsub;
   vector<vector<double>> nulls(nsub);
   {
-    long long nsm = 0;
-    for (auto& d : D.hs) nsm = std::max(nsm, d.oAc + (long long)d.ncp * d.ncp);
-    vector<double> hsmall(std::max<long long>(1, nsm));
-    CK(cudaMemcpyAsync(hsmall.data(), D.small, nsm * sizeof(double), cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    for (int t = 0; t < nsub; ++t) {
-      if (S.subs[t].bc_present || D.hs[t].nc == 0) continue;
-      const DevSub& d = D.hs[t];
-      int dn = 0;
-      vector<double> y = host_coarse_null_coefficients(d.nc, d.ncp, hsmall.data() + d.oAc, dn);
-      if (dn == 0) continue;
-      vector<T> phi((size_t)d.NI * d.ncp);
-      CK(cudaMemcpyAsync(phi.data(), static_cast<const T*>(D.poolPC) + d.oPhi, phi.size() * sizeof(T),
-                         cudaMemcpyDeviceToHost, st));
-      CK(cudaStreamSynchronize(st));
-      vector<double>& nv = nulls[t];
-      nv.assign((size_t)d.ni * dn, 0.0);
-      for (int c = 0; c < dn; ++c) {
-        for (int r = 0; r < d.ni; ++r) {
-          double acc = 0.0;
-          for (int q = 0; q < d.nc; ++q) acc += (double)phi[(size_t)r * d.ncp + q] * y[(size_t)q * dn + c];
-          nv[(size_t)c * d.ni + r] = acc;
+    vector<int> fl;
+    for (int t = 0; t < nsub; ++t)
+      if (!S.subs[t].bc_present && D.hs[t].nc > 0) fl.push_back(t);
+    if (!fl.empty()) {
+      std::vector<void*> tmp0;
+      // columns: Phi_s (converted to FP64) in, S Phi_s out
+      vector<long long> off(fl.size() + 1, 0);
+      for (size_t f = 0; f < fl.size(); ++f) off[f + 1] = off[f] + (long long)D.hs[fl[f]].ni * D.hs[fl[f]].nc;
+      const long long tot = off[fl.size()];
+      vector<double> hphi(tot);
+      {
+        vector<T> phi;
+        for (size_t f = 0; f < fl.size(); ++f) {
+          const DevSub& d = D.hs[fl[f]];
+          phi.resize((size_t)d.NI * d.ncp);
+          CK(cudaMemcpyAsync(phi.data(), static_cast<const T*>(D.poolPC) + d.oPhi, phi.size() * sizeof(T),
+                             cudaMemcpyDeviceToHost, st));
+          CK(cudaStreamSynchronize(st));
+          for (int c = 0; c < d.nc; ++c)
+            for (int r = 0; r < d.ni; ++r) hphi[off[f] + (long long)c * d.ni + r] = (double)phi[(size_t)r * d.ncp + c];
         }
-        // orthonormalise against the previous columns (twice)
-        for (int pass = 0; pass < 2; ++pass)
-          for (int c2 = 0; c2 < c; ++c2) {
-            double tt = 0.0;
-            for (int r = 0; r < d.ni; ++r) tt += nv[(size_t)c2 * d.ni + r] * nv[(size_t)c * d.ni + r];
-            for (int r = 0; r < d.ni; ++r) nv[(size_t)c * d.ni + r] -= tt * nv[(size_t)c2 * d.ni + r];
+      }
+      double* buf = dalloc<double>((size_t)2 * tot, tmp0);
+      CK(cudaMemcpyAsync(buf, hphi.data(), tot * sizeof(double), cudaMemcpyHostToDevice, st));
+      vector<int> tptr(nsub + 1, 0);
+      vector<long long> tin, tout;
+      int maxc = 0;
+      {
+        size_t f = 0;
+        for (int t = 0; t < nsub; ++t) {
+          if (f < fl.size() && fl[f] == t) {
+            const DevSub& d = D.hs[t];
+            for (int c = 0; c < d.nc; ++c) {
+              tin.push_back(off[f] + (long long)c * d.ni);
+              tout.push_back(tot + off[f] + (long long)c * d.ni);
+            }
+            maxc = std::max(maxc, d.nc);
+            ++f;
           }
-        double nn = 0.0;
-        for (int r = 0; r < d.ni; ++r) nn += nv[(size_t)c * d.ni + r] * nv[(size_t)c * d.ni + r];
-        nn = std::sqrt(nn);
-        for (int r = 0; r < d.ni; ++r) nv[(size_t)c * d.ni + r] = nn > 0 ? nv[(size_t)c * d.ni + r] / nn : 0.0;
+          tptr[t + 1] = (int)tin.size();
+        }
+      }
+      ColTab tab{upload(tptr, tmp0, st), upload(tin, tmp0, st), upload(tout, tmp0, st)};
+      dim3 g((D.maxNI + 63) / 64, (maxc + 63) / 64, nsub);
+      if (D.mixed) k_ad_gemm_df<<<g, 256, 0, st>>>(D.ds, static_cast<const float2*>(D.poolS), tab, buf);
+      else k_ad_gemm<double, false, double><<<g, 256, 0, st>>>(D.ds, static_cast<const double*>(D.poolS), tab, buf);
+      CKL();
+      vector<double> hsphi(tot);
+      CK(cudaMemcpyAsync(hsphi.data(), buf + tot, tot * sizeof(double), cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+      for (void* q : tmp0) cudaFreeAsync(q, st);
+#pragma omp parallel for schedule(dynamic)
+      for (int f = 0; f < (int)fl.size(); ++f) {
+        const DevSub& d = D.hs[fl[f]];
+        const double* ph = &hphi[off[f]];
+        const double* sp = &hsphi[off[f]];
+        vector<double> ac((size_t)d.nc * d.nc);
+        for (int a = 0; a < d.nc; ++a)
+          for (int b = 0; b < d.nc; ++b) {
+            double t2 = 0.0;
+            for (int r = 0; r < d.ni; ++r) t2 += ph[(long long)a * d.ni + r] * sp[(long long)b * d.ni + r];
+            ac[(size_t)a * d.nc + b] = t2;
+          }
+        int dn = 0;
+        vector<double> y = host_coarse_null_coefficients(d.nc, d.nc, ac.data(), dn);
+        vector<double>& nv = nulls[fl[f]];
+        nv.assign((size_t)d.ni * dn, 0.0);
+        for (int c = 0; c < dn; ++c) {
+          for (int r = 0; r < d.ni; ++r) {
+            double acc = 0.0;
+            for (int q = 0; q < d.nc; ++q) acc += ph[(long long)q * d.ni + r] * y[(size_t)q * dn + c];
+            nv[(size_t)c * d.ni + r] = acc;
+          }
+          for (int pass = 0; pass < 2; ++pass)
+            for (int c2 = 0; c2 < c; ++c2) {
+              double tt = 0.0;
+              for (int r = 0; r < d.ni; ++r) tt += nv[(size_t)c2 * d.ni + r] * nv[(size_t)c * d.ni + r];
+              for (int r = 0; r < d.ni; ++r) nv[(size_t)c * d.ni + r] -= tt * nv[(size_t)c2 * d.ni + r];
+            }
+          double nn = 0.0;
+          for (int r = 0; r < d.ni; ++r) nn += nv[(size_t)c * d.ni + r] * nv[(size_t)c * d.ni + r];
+          nn = std::sqrt(nn);
+          for (int r = 0; r < d.ni; ++r) nv[(size_t)c * d.ni + r] = nn > 0 ? nv[(size_t)c * d.ni + r] / nn : 0.0;
+        }
       }
     }
   }
@@ -1107,7 +1158,7 @@ static void adaptive_constraints(Solver& S, Device& D) {
       if (t.maxc == 0) return;
       dim3 g((D.maxNI + 63) / 64, (t.maxc + 63) / 64, nsub);
       if (D.mixed)
-        k_ad_gemm<float2, false, double><<<g, 256, 0, st>>>(D.ds, static_cast<const float2*>(D.poolS), t.dev, va);
+        k_ad_gemm_df<<<g, 256, 0, st>>>(D.ds, static_cast<const float2*>(D.poolS), t.dev, va);
       else
         k_ad_gemm<double, false, double><<<g, 256, 0, st>>>(D.ds, static_cast<const double*>(D.poolS), t.dev, va);
       CKL();

@@ -185,8 +185,8 @@ struct Solver {
 // adaptive face constraints, host part (bddc_adaptive.cpp)
 // nulls[s]: orthonormal basis of null(S_s) on the interface (ndofi x d_s, column-major; empty if none)
 void host_adaptive_pairs(const Solver& S, AdaptivePairs& P, const vector<vector<double>>& nulls);
-// null space coefficients of a local coarse matrix (nc x nc in an ld x ld array): the
-// eigenvectors with |eigenvalue| <= 1e-5 max |eigenvalue|, nc x d column-major
+// null space coefficients of a local coarse matrix Phi^T S Phi (nc x nc in an ld x ld array):
+// the eigenvectors with |eigenvalue| <= nc * max |eigenvalue| * 4 * 2^-44, nc x d column-major
 vector<double> host_coarse_null_coefficients(int nc, int ld, const double* ac, int& d);
 // eig: npair x KMAX eigenvalues (descending); cons: for every pair the columns A x of the
 // eigenvectors with eigenvalue >= tau, n rows each, packed pair after pair

@@ -239,6 +239,33 @@ def channel_kappa(n_el_edge: int, nchannels: int = 20, width: int = 2, contrast:
     return kappa
 
 
+def random_box_counts(n_el_edge: int, counts, lo_side: int, hi_side: int, seed: int):
+    """Tensor-product box partition with counts[a] boxes along axis a, side
+    lengths drawn uniformly in [lo_side, hi_side] and then adjusted (within the
+    bounds) to fill the grid exactly."""
+    rng = np.random.default_rng(seed)
+    cuts = []
+    for a in range(3):
+        m = counts[a]
+        if not (m * lo_side <= n_el_edge <= m * hi_side):
+            raise ValueError("side bounds cannot fill the grid")
+        side = rng.integers(lo_side, hi_side + 1, size=m)
+        while side.sum() != n_el_edge:
+            i = int(rng.integers(0, m))
+            if side.sum() > n_el_edge and side[i] > lo_side:
+                side[i] -= 1
+            elif side.sum() < n_el_edge and side[i] < hi_side:
+                side[i] += 1
+        cuts.append(np.concatenate([[0], np.cumsum(side)]))
+    boxes = []
+    for kz in range(counts[2]):
+        for ky in range(counts[1]):
+            for kx in range(counts[0]):
+                boxes.append((np.array([cuts[0][kx], cuts[1][ky], cuts[2][kz]]),
+                              np.array([cuts[0][kx + 1], cuts[1][ky + 1], cuts[2][kz + 1]])))
+    return boxes
+
+
 def uniform_boxes(n_el_edge: int, nsub_edge: int):
     """The nsub_edge^3 equal boxes of the cube (as poisson_on_cube splits it)."""
     cuts = [round(k * n_el_edge / nsub_edge) for k in range(nsub_edge + 1)]
