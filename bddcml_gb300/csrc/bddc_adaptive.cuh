@@ -360,15 +360,27 @@ __device__ void ad_jacobi(double (*a)[33], double (*z)[33], int nn) {
       off += __shfl_xor_sync(0xffffffffu, off, o);
       dg += __shfl_xor_sync(0xffffffffu, dg, o);
     }
-    if (off <= 1e-30 * dg || off == 0.0) break;
+    if (off <= 1e-28 * dg || off == 0.0) break;
     for (int p = 0; p < nn - 1; ++p)
       for (int q = p + 1; q < nn; ++q) {
-        const double apq = a[p][q];
-        if (apq == 0.0) continue;
-        const double app = a[p][p], aqq = a[q][q];
-        const double th = (aqq - app) / (2.0 * apq);
-        const double t = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
-        const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+        // rotation computed by lane 0 (FP64 divide and square roots are slow
+        // on this part) and broadcast; rotations of negligible entries skipped
+        double c = 1.0, s = 0.0;
+        int skip = 1;
+        if (lane == 0) {
+          const double apq = a[p][q], app = a[p][p], aqq = a[q][q];
+          if (fabs(apq) > 1e-16 * sqrt(fabs(app * aqq)) && apq != 0.0) {
+            const double th = (aqq - app) / (2.0 * apq);
+            const double t = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
+            c = 1.0 / sqrt(t * t + 1.0);
+            s = t * c;
+            skip = 0;
+          }
+        }
+        skip = __shfl_sync(0xffffffffu, skip, 0);
+        if (skip) continue;
+        c = __shfl_sync(0xffffffffu, c, 0);
+        s = __shfl_sync(0xffffffffu, s, 0);
         __syncwarp();
         if (lane < nn) {
           const double xp = a[p][lane], xq = a[q][lane];

@@ -893,6 +893,7 @@ template <typename T>
 static void adaptive_constraints(Solver& S, Device& D) {
   const double t0 = wall_time();
   cudaStream_t st = D.st;
+  D.prof.begin(PH_NUMERIC_TOTAL, st, true);  // part of the device setup time
   // null spaces of the floating subdomains' Schur complements: Phi y for the
   // null vectors y of Phi^T S Phi, formed with FP64-accurate S products (the
   // null-space projection of module_adaptivity.f90:1180-1480, per subdomain)
@@ -1257,6 +1258,7 @@ static void adaptive_constraints(Solver& S, Device& D) {
   S.adaptive_eigs = eig;
   S.adaptive_pairs = P;
   host_load_adaptive(S, P, eig, cons);
+  D.prof.end(PH_NUMERIC_TOTAL, st);
   S.stats.t_adaptive = wall_time() - t0;
 }
 
