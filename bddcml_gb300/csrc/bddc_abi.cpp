@@ -230,7 +230,7 @@ void bddcml_solve_c(int* comm_all, int* method, double* tol, int* maxit, int* nd
                     int* max_number_of_stored_vectors, int* num_iter, int* converged_reason,
                     double* condition_number) {
   guarded("bddcml_solve_c", [&] {
-    (void)comm_all; (void)recycling_int; (void)max_number_of_stored_vectors;
+    (void)comm_all;
     Solver* S = need_solver("bddcml_solve_c");
     if (!S) return;
     if (!S->setup_done) throw Error{ERR_ARGUMENT, "preconditioner is not set up"};
@@ -245,7 +245,15 @@ void bddcml_solve_c(int* comm_all, int* method, double* tol, int* maxit, int* nd
     int it = 0, reason = 0;
     double cond = 1.0;
     Error err{0, ""};
-    if (!device_solve(*S, m, t, mi, nd, it, reason, cond, err)) throw err;
+    // Krylov recycling is part of PCG only (module_bddcml.f90:544-567); the reference's
+    // defaults switch it off (module_bddcml.f90:519-520)
+    int rec = 0, maxvec = 0;
+    if (*method != -1 && m == 0) {
+      rec = *recycling_int;
+      maxvec = *max_number_of_stored_vectors;
+      if (rec && maxvec < 0) throw Error{ERR_ARGUMENT, "max_number_of_stored_vectors must not be negative"};
+    }
+    if (!device_solve(*S, m, t, mi, nd, rec, maxvec, it, reason, cond, err)) throw err;
     *num_iter = it;
     *converged_reason = reason;
     *condition_number = cond;

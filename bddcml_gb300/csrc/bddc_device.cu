@@ -208,6 +208,10 @@ class Device {
   long long* nv_off = nullptr;
   // extra interface vectors of BiCGSTAB / steepest descent (allocated on first use)
   double *kv = nullptr, *ky = nullptr, *ks = nullptr, *kt = nullptr, *krs = nullptr;
+  // Krylov recycling: basis V, W = S V (n x rc_cap each), its size on the device and here
+  double *rcV = nullptr, *rcW = nullptr, *rc_part = nullptr, *rc_coef = nullptr;
+  int* rc_nact_dev = nullptr;
+  int rc_cap = 0, rc_nact = 0;
   int maxnbo = 0, maxw = 0, maxNR = 0;
   int nref = 0;
   Profiler prof;
@@ -224,6 +228,9 @@ class Device {
   void release() {
     nv_v0 = nv_v1 = nv_r = nullptr;
     kv = ky = ks = kt = krs = nullptr;
+    rcV = rcW = rc_part = rc_coef = nullptr;
+    rc_nact_dev = nullptr;
+    rc_cap = rc_nact = 0;
     nv_off = nullptr;
     release_pc();
     for (void* q : owned) cudaFreeAsync(q, st);
@@ -1440,8 +1447,8 @@ static void other_krylov(Solver& S, int method, double normrhs, double tol, int 
 }
 
 template <typename T>
-static bool solve_impl(Solver& S, int method, double tol, int maxit, int ndecrmax, int& num_iter, int& reason,
-                       double& cond) {
+static bool solve_impl(Solver& S, int method, double tol, int maxit, int ndecrmax, int recycling, int maxvec,
+                       int& num_iter, int& reason, double& cond) {
   Device& D = *S.dev;
   cudaStream_t st = D.st;
   auto& own = D.owned;
@@ -1514,8 +1521,36 @@ static bool solve_impl(Solver& S, int method, double tol, int maxit, int ndecrma
     k_dot<<<D.npart, RT, 0, st>>>(D.n, D.r, D.r, D.wsum, D.part);
     CKL();
     double normres0 = std::sqrt(host_sum_parts(D));
-    if (normres0 == 0.0) {
-      postprocess = false;
+    const bool rc = recycling != 0 && (D.rc_cap > 0 || maxvec > 0);
+    if (rc && D.rc_cap == 0) {  // the basis keeps the capacity of the first recycling solve
+      D.rc_cap = maxvec;
+      D.rcV = dalloc<double>((size_t)D.n * maxvec, own);
+      D.rcW = dalloc<double>((size_t)D.n * maxvec, own);
+      D.rc_part = dalloc<double>((size_t)D.npart * maxvec, own);
+      D.rc_coef = dalloc<double>(maxvec, own);
+      D.rc_nact_dev = dalloc<int>(1, own);
+      CK(cudaMemsetAsync(D.rc_nact_dev, 0, sizeof(int), st));
+      D.rc_nact = 0;
+    }
+    bool projected_done = false;
+    if (rc && normres0 != 0.0 && D.rc_nact > 0) {
+      // x += V V^T r, r -= S V V^T r (module_krylov.f90:373-452)
+      k_rc_dots<<<D.npart, RT, 0, st>>>(D.n, D.rc_cap, D.rc_nact_dev, D.rcV, D.wsum, D.r, D.rc_part, nullptr);
+      k_rc_coef<<<1, 256, 0, st>>>(D.rc_cap, D.rc_nact_dev, D.rc_part, D.npart, D.rc_coef, nullptr);
+      CK(cudaMemsetAsync(D.z, 0, (size_t)D.n * sizeof(double), st));
+      k_rc_combine<<<D.npart, RT, 0, st>>>(D.n, D.rc_nact_dev, D.rcV, D.rc_coef, 1.0, D.z, nullptr);
+      CKL();
+      k_axpy<<<(D.n + 255) / 256, 256, 0, st>>>(D.n, 1.0, D.z, D.x);
+      CKL();
+      launch_schur<T>(D, D.z, D.ap, true, nullptr, nullptr);
+      k_axpy<<<(D.n + 255) / 256, 256, 0, st>>>(D.n, -1.0, D.ap, D.r);
+      CKL();
+      k_dot<<<D.npart, RT, 0, st>>>(D.n, D.r, D.r, D.wsum, D.part);
+      CKL();
+      if (std::sqrt(host_sum_parts(D)) / normres0 < tol) projected_done = true;  // no iteration needed
+    }
+    if (normres0 == 0.0 || projected_done) {
+      postprocess = normres0 != 0.0;
     } else {
       launch_pc<T>(D, D.r, D.p, nullptr);
       double rmp = host_sum_parts(D);
@@ -1529,8 +1564,20 @@ static bool solve_impl(Solver& S, int method, double tol, int maxit, int ndecrma
       int launched = 0;
       while (true) {
         for (int q = 0; q < chunk; ++q) {
+          if (rc)  // S-orthogonalise p against the stored directions, twice (krylov_orthogonalize_icgs)
+            for (int pass = 0; pass < 2; ++pass) {
+              k_rc_dots<<<D.npart, RT, 0, st>>>(D.n, D.rc_cap, D.rc_nact_dev, D.rcW, D.wsum, D.p, D.rc_part, D.ctl);
+              k_rc_coef<<<1, 256, 0, st>>>(D.rc_cap, D.rc_nact_dev, D.rc_part, D.npart, D.rc_coef, D.ctl);
+              k_rc_combine<<<D.npart, RT, 0, st>>>(D.n, D.rc_nact_dev, D.rcV, D.rc_coef, -1.0, D.p, D.ctl);
+              CKL();
+            }
           launch_schur<T>(D, D.p, D.ap, false, D.ctl, D.p);
           k_sc_alpha<<<1, RT, 0, st>>>(D.ctl, D.part, D.npart);
+          if (rc) {
+            k_rc_store<<<D.npart, RT, 0, st>>>(D.n, D.rc_cap, D.rc_nact_dev, D.p, D.ap, D.rcV, D.rcW, D.ctl);
+            k_rc_bump<<<1, 1, 0, st>>>(D.rc_cap, D.rc_nact_dev, D.ctl);
+            CKL();
+          }
           k_update_xr<<<D.npart, RT, 0, st>>>(D.n, D.ctl, D.x, D.r, D.p, D.ap, D.wsum, D.part);
           k_sc_res<<<1, RT, 0, st>>>(D.ctl, D.part, D.npart, D.hist);
           launch_pc<T>(D, D.r, D.z, D.ctl);
@@ -1545,6 +1592,10 @@ static bool solve_impl(Solver& S, int method, double tol, int maxit, int ndecrma
       }
       D.prof.end(PH_PCG, st);
       S.stats.t_iterations = wall_time() - tl;
+      if (rc) {
+        CK(cudaMemcpyAsync(&D.rc_nact, D.rc_nact_dev, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+      }
       PcgCtl c2 = *D.hctl;
       num_iter = c2.num_iter;
       reason = c2.reason;
@@ -1702,11 +1753,11 @@ bool device_new_data(Solver& S, Error& err) {
   return true;
 }
 
-bool device_solve(Solver& S, int method, double tol, int maxit, int ndecrmax, int& num_iter, int& reason,
-                  double& cond, Error& err) {
+bool device_solve(Solver& S, int method, double tol, int maxit, int ndecrmax, int recycling, int maxvec,
+                  int& num_iter, int& reason, double& cond, Error& err) {
   try {
-    if (S.dev->mixed) return solve_impl<float>(S, method, tol, maxit, ndecrmax, num_iter, reason, cond);
-    return solve_impl<double>(S, method, tol, maxit, ndecrmax, num_iter, reason, cond);
+    if (S.dev->mixed) return solve_impl<float>(S, method, tol, maxit, ndecrmax, recycling, maxvec, num_iter, reason, cond);
+    return solve_impl<double>(S, method, tol, maxit, ndecrmax, recycling, maxvec, num_iter, reason, cond);
   } catch (Error& e) {
     err = e;
     return false;

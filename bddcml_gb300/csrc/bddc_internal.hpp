@@ -220,7 +220,8 @@ bool device_dotprod_noalloc(const int* iface_dofs, const double* weights, int ni
                             const double* v2, int ndof, double* out, Error& err);
 void device_destroy(Device* d);
 bool device_setup(Solver& S, Error& err);
-bool device_solve(Solver& S, int method, double tol, int maxit, int ndecrmax, int& num_iter, int& reason, double& cond,
+bool device_solve(Solver& S, int method, double tol, int maxit, int ndecrmax, int recycling, int maxvec, int& num_iter,
+                  int& reason, double& cond,
                   Error& err);
 bool device_download(Solver& S, int isub, double* out, Error& err);
 void device_set_profiling(Device* d, bool on);

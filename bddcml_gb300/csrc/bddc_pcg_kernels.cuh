@@ -357,6 +357,72 @@ __global__ void __launch_bounds__(RT) k_update_p(int n, const PcgCtl* __restrict
   for (int g = blockIdx.x * RT + threadIdx.x; g < n; g += gridDim.x * RT) p[g] = z[g] + beta * p[g];
 }
 
+// ------------------------------------------------------- Krylov recycling
+// Stored S-orthonormal search directions V (n x cap, column-major) and
+// W = S V, nact of them in use (module_krylov.f90:33-43, 663-726).  Kernels
+// with a control block do nothing once the iteration has stopped.
+
+// partial weighted dots (basis_j, v)_w for j < nact: part[block * cap + j]
+__global__ void __launch_bounds__(RT) k_rc_dots(int n, int cap, const int* __restrict__ nact,
+                                                const double* __restrict__ basis, const double* __restrict__ wsum,
+                                                const double* __restrict__ v, double* __restrict__ part,
+                                                const PcgCtl* __restrict__ ctl) {
+  if (ctl && ctl->done) return;
+  __shared__ double sh[32];
+  const int na = *nact;
+  for (int j = 0; j < na; ++j) {
+    const double* b = basis + (long long)j * n;
+    double loc = 0.0;
+    for (int g = blockIdx.x * RT + threadIdx.x; g < n; g += gridDim.x * RT) loc += wsum[g] * b[g] * v[g];
+    const double t = block_reduce(loc, sh);
+    if (threadIdx.x == 0) part[blockIdx.x * cap + j] = t;
+  }
+}
+
+__global__ void k_rc_coef(int cap, const int* __restrict__ nact, const double* __restrict__ part, int npart,
+                          double* __restrict__ coef, const PcgCtl* __restrict__ ctl) {
+  if (ctl && ctl->done) return;
+  const int na = *nact;
+  for (int j = threadIdx.x; j < na; j += blockDim.x) {
+    double t = 0.0;
+    for (int b = 0; b < npart; ++b) t += part[b * cap + j];
+    coef[j] = t;
+  }
+}
+
+// v += sign * V coef
+__global__ void __launch_bounds__(RT) k_rc_combine(int n, const int* __restrict__ nact, const double* __restrict__ V,
+                                                   const double* __restrict__ coef, double sign, double* __restrict__ v,
+                                                   const PcgCtl* __restrict__ ctl) {
+  if (ctl && ctl->done) return;
+  const int na = *nact;
+  for (int g = blockIdx.x * RT + threadIdx.x; g < n; g += gridDim.x * RT) {
+    double t = 0.0;
+    for (int j = 0; j < na; ++j) t += V[(long long)j * n + g] * coef[j];
+    v[g] += sign * t;
+  }
+}
+
+// V(:, nact) = p / sqrt(pap), W(:, nact) = ap / sqrt(pap) while there is room
+__global__ void __launch_bounds__(RT) k_rc_store(int n, int cap, const int* __restrict__ nact,
+                                                 const double* __restrict__ p, const double* __restrict__ ap,
+                                                 double* __restrict__ V, double* __restrict__ W,
+                                                 const PcgCtl* __restrict__ ctl) {
+  if (ctl->done) return;
+  const int na = *nact;
+  if (na >= cap) return;
+  const double sc = 1.0 / sqrt(ctl->pap);
+  for (int g = blockIdx.x * RT + threadIdx.x; g < n; g += gridDim.x * RT) {
+    V[(long long)na * n + g] = sc * p[g];
+    W[(long long)na * n + g] = sc * ap[g];
+  }
+}
+
+__global__ void k_rc_bump(int cap, int* __restrict__ nact, const PcgCtl* __restrict__ ctl) {
+  if (ctl->done) return;
+  if (*nact < cap) *nact += 1;
+}
+
 // -------------------------------------------------------- helper kernels
 // v[g] = sum over holders of a replicated vector (reduced rhs assembly)
 __global__ void k_assemble_plain(int n, Owners own, const double* __restrict__ rep, const int* __restrict__ fixed,

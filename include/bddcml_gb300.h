@@ -85,7 +85,13 @@ void bddcml_setup_preconditioner_c(int *matrixtype, int *use_defaults_int, int *
  * method 0 PCG (with the Lanczos condition estimate), 1 BiCGSTAB, 2 steepest
  * descent; -1 takes the reference defaults (module_bddcml.f90:515-520):
  * BiCGSTAB, tol 1e-6, maxit 1000, ndecrmax 30, ignoring the passed values.
- * condition_number is -1 for methods 1 and 2.  method 5 (direct solve) sets
+ * condition_number is -1 for methods 1 and 2.  With method 0, recycling_int = 1
+ * keeps up to max_number_of_stored_vectors S-orthonormal search directions
+ * across solves (module_krylov.f90:313-484, 663-726): they project the initial
+ * residual of the next solve (after bddcml_setup_new_data_c) and every new
+ * direction is orthogonalised against them; the capacity is fixed by the first
+ * recycling solve and the basis is dropped at the next setup or at finalize.
+ * method 5 (direct solve) sets
  * BDDCML_ERR_UNSUPPORTED, any other value BDDCML_ERR_ARGUMENT.  A steepest
  * descent that stalls for ndecrmax iterations sets BDDCML_ERR_NUMERIC (the
  * reference stops with an error there, module_krylov.f90:1801-1812). */

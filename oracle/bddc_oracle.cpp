@@ -227,6 +227,9 @@ struct Oracle {
   vector<int> pair_nadaptive;          // eigenvalues >= tau per pair
   vector<int> face_ncdof;              // constraints per pair face after orthogonalisation
   double adaptivity_est = -1.0;
+  // Krylov recycling (module_krylov.f90:33-43): S-orthonormal search directions V and W = S V
+  vector<vector<vector<double>>> rcv, rcw;  // [basis vector][subdomain][interface dof]
+  int rc_cap = 0;
   std::string err;
   // PCG results
   vector<double> relres_hist;
@@ -1302,6 +1305,33 @@ static void adaptivity(Oracle& o, const vector<vector<double>>& rho) {
   number_constraints(o);
 }
 
+// reduced right-hand side g = f_i - A_io A_oo^-1 f_o, assembled (module_dd.f90:6995-7257)
+static void reduced_rhs(Oracle& oo) {
+    Oracle* o = &oo;
+    const int nsub = o->nsub;
+    vector<vector<double>> g(nsub);
+#pragma omp parallel for schedule(dynamic) num_threads(o->nthreads)
+    for (int s = 0; s < nsub; ++s) {
+      auto& S = o->subs[s];
+      vector<double> rhs = S.rhs;
+      if (S.rhs_complete) for (int i = 0; i < S.ndofi; ++i) rhs[S.iivsvn[i]] *= S.wi[i];
+      if (S.bc_present) {
+        vector<double> bcw = S.bc;
+        for (int i = 0; i < S.ndofi; ++i) bcw[S.iivsvn[i]] *= S.wi[i];
+        for (int i = 0; i < S.ndof; ++i) { if (S.ifix[i]) rhs[i] = 0.0; rhs[i] += bcw[i]; }
+      }
+      S.solo.assign(S.ndofo, 0.0);
+      for (int i = 0; i < S.ndofo; ++i) S.solo[i] = rhs[S.iovsvn[i]];
+      if (S.ndofo > 0) S.a11.solve(S.solo.data());
+      g[s].assign(S.ndofi, 0.0);
+      for (int io = 0; io < S.ndofo; ++io)
+        for (int k = S.a12_ptr[io]; k < S.a12_ptr[io + 1]; ++k) g[s][S.a12_col[k]] += S.a12_val[k] * S.solo[io];
+      for (int i = 0; i < S.ndofi; ++i) g[s][i] = rhs[S.iivsvn[i]] - g[s][i];
+    }
+    comm_exchange_add(*o, g);
+    for (int s = 0; s < nsub; ++s) o->subs[s].g = g[s];
+}
+
 int oracle_setup(void* h, int use_corner_constraints, int use_arithmetic_constraints, int weights_type) {
   auto* o = static_cast<Oracle*>(h);
   try {
@@ -1439,28 +1469,7 @@ int oracle_setup(void* h, int use_corner_constraints, int use_arithmetic_constra
     // ---- adaptive face constraints (module_levels.f90:2826-2938)
     if (o->adaptive) adaptivity(*o, rho);
     coarse_space(*o);
-    // ---- reduced rhs (module_dd.f90:6995-7257)
-    vector<vector<double>> g(nsub);
-#pragma omp parallel for schedule(dynamic) num_threads(o->nthreads)
-    for (int s = 0; s < nsub; ++s) {
-      auto& S = o->subs[s];
-      vector<double> rhs = S.rhs;
-      if (S.rhs_complete) for (int i = 0; i < S.ndofi; ++i) rhs[S.iivsvn[i]] *= S.wi[i];
-      if (S.bc_present) {
-        vector<double> bcw = S.bc;
-        for (int i = 0; i < S.ndofi; ++i) bcw[S.iivsvn[i]] *= S.wi[i];
-        for (int i = 0; i < S.ndof; ++i) { if (S.ifix[i]) rhs[i] = 0.0; rhs[i] += bcw[i]; }
-      }
-      S.solo.assign(S.ndofo, 0.0);
-      for (int i = 0; i < S.ndofo; ++i) S.solo[i] = rhs[S.iovsvn[i]];
-      if (S.ndofo > 0) S.a11.solve(S.solo.data());
-      g[s].assign(S.ndofi, 0.0);
-      for (int io = 0; io < S.ndofo; ++io)
-        for (int k = S.a12_ptr[io]; k < S.a12_ptr[io + 1]; ++k) g[s][S.a12_col[k]] += S.a12_val[k] * S.solo[io];
-      for (int i = 0; i < S.ndofi; ++i) g[s][i] = rhs[S.iivsvn[i]] - g[s][i];
-    }
-    comm_exchange_add(*o, g);
-    for (int s = 0; s < nsub; ++s) o->subs[s].g = g[s];
+    reduced_rhs(*o);
     o->setup_done = true;
   } catch (std::exception& e) {
     o->err = e.what();
@@ -1676,9 +1685,40 @@ static double tridiag_max_eig(const vector<double>& d, const vector<double>& e) 
 
 static void postprocess(Oracle& o, vector<vector<double>>& x);
 
+static int solve_pcg(Oracle* o, double tol, int maxit, int ndecrmax, bool recycling, int maxvec, int* num_iter,
+                     int* converged_reason, double* condition_number);
+
 int oracle_solve(void* h, double tol, int maxit, int ndecrmax, int* num_iter, int* converged_reason,
                  double* condition_number) {
+  return solve_pcg(static_cast<Oracle*>(h), tol, maxit, ndecrmax, false, 0, num_iter, converged_reason,
+                   condition_number);
+}
+
+// PCG with Krylov recycling (module_krylov.f90:313-484, 663-726): the stored
+// S-orthonormal directions V (W = S V) project the initial residual
+// (x += V V^T r, r -= S V V^T r) and every new direction is S-orthogonalised
+// against them by classical Gram-Schmidt twice (krylov_orthogonalize_icgs,
+// :1930-1961) before it is stored while there is room.
+int oracle_solve_recycling(void* h, double tol, int maxit, int ndecrmax, int recycling, int maxvec, int* num_iter,
+                           int* converged_reason, double* condition_number) {
+  return solve_pcg(static_cast<Oracle*>(h), tol, maxit, ndecrmax, recycling != 0, maxvec, num_iter,
+                   converged_reason, condition_number);
+}
+
+// new loads and initial guess of a subdomain after setup (bddcml_change_subdomain_data
+// with the same Dirichlet data), then the reduced rhs again
+int oracle_new_loads(void* h, int isub, const double* rhs, const double* sol) {
   auto* o = static_cast<Oracle*>(h);
+  if (!o->setup_done || isub < 0 || isub >= o->nsub) { o->err = "bad call"; return 1; }
+  auto& S = o->subs[isub];
+  S.rhs.assign(rhs, rhs + S.ndof);
+  S.sol.assign(sol, sol + S.ndof);
+  reduced_rhs(*o);
+  return 0;
+}
+
+static int solve_pcg(Oracle* o, double tol, int maxit, int ndecrmax, bool recycling, int maxvec, int* num_iter,
+                     int* converged_reason, double* condition_number) {
   if (!o->setup_done) { o->err = "setup not done"; return 1; }
   int nsub = o->nsub;
   vector<vector<double>> x(nsub), r(nsub), p(nsub), ap(nsub), z(nsub);
@@ -1703,14 +1743,51 @@ int oracle_solve(void* h, double tol, int maxit, int ndecrmax, int* num_iter, in
   if (normres0 == 0.0) return 0;
   vector<double> diag(maxit + 1, 0.0), subdiag(maxit, 0.0);
   int nw = 0;
-  if (normres0 != 0.0) {
+  if (recycling && o->rc_cap == 0) o->rc_cap = std::max(0, maxvec);
+  auto combine = [&](const vector<vector<vector<double>>>& basis, const vector<double>& c,
+                     vector<vector<double>>& out, double sign) {
+    for (size_t j = 0; j < c.size(); ++j)
+      for (int s = 0; s < nsub; ++s)
+        for (size_t i = 0; i < out[s].size(); ++i) out[s][i] += sign * c[j] * basis[j][s][i];
+  };
+  bool projected_done = false;
+  if (recycling && !o->rcv.empty()) {
+    // x += V V^T r, r -= S V V^T r (module_krylov.f90:373-452)
+    vector<double> c(o->rcv.size());
+    for (size_t j = 0; j < c.size(); ++j) c[j] = dotw(*o, o->rcv[j], r);
+    for (int s = 0; s < nsub; ++s) z[s].assign(r[s].size(), 0.0);
+    combine(o->rcv, c, z, 1.0);
+    for (int s = 0; s < nsub; ++s)
+      for (size_t i = 0; i < x[s].size(); ++i) x[s][i] += z[s][i];
+    sm_apply(*o, z, ap);
+    for (int s = 0; s < nsub; ++s)
+      for (size_t i = 0; i < r[s].size(); ++i) r[s][i] -= ap[s][i];
+    fix_bc_dual(*o, r);
+    const double relres = std::sqrt(dotw(*o, r, r)) / normres0;
+    if (relres < tol) projected_done = true;  // no iteration needed
+  }
+  if (normres0 != 0.0 && !projected_done) {
     pc_apply(*o, r, p);
     double rmp = dotw(*o, r, p);
     int ndecr = 0;
     double lastres = 1.0;
     for (int iter = 1; iter <= maxit; ++iter) {
+      if (recycling && !o->rcv.empty())
+        for (int pass = 0; pass < 2; ++pass) {  // p -= V W^T p, twice
+          vector<double> c(o->rcv.size());
+          for (size_t j = 0; j < c.size(); ++j) c[j] = dotw(*o, o->rcw[j], p);
+          combine(o->rcv, c, p, -1.0);
+        }
       sm_apply(*o, p, ap);
       double pap = dotw(*o, p, ap);
+      if (recycling && (int)o->rcv.size() < o->rc_cap) {
+        const double sc = 1.0 / std::sqrt(pap);
+        vector<vector<double>> v = p, w = ap;
+        for (int s = 0; s < nsub; ++s)
+          for (size_t i = 0; i < v[s].size(); ++i) { v[s][i] *= sc; w[s][i] *= sc; }
+        o->rcv.push_back(v);
+        o->rcw.push_back(w);
+      }
       double alpha = rmp / pap;
       for (int s = 0; s < nsub; ++s)
         for (size_t i = 0; i < x[s].size(); ++i) { x[s][i] += alpha * p[s][i]; r[s][i] -= alpha * ap[s][i]; }
@@ -1948,6 +2025,8 @@ void oracle_sym_eig(int n, const double* a, double* w, double* z) {
   std::copy(wv.begin(), wv.end(), w);
   std::copy(zv.begin(), zv.end(), z);
 }
+
+int oracle_recycling_size(void* h) { return (int)static_cast<Oracle*>(h)->rcv.size(); }
 
 void oracle_set_adaptive(void* h, int on, double tau) {
   auto* o = static_cast<Oracle*>(h);

@@ -50,6 +50,10 @@ def lib():
                                           C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_double)]
         L.oracle_download.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int]
         L.oracle_set_adaptive.argtypes = [C.c_void_p, C.c_int, C.c_double]
+        L.oracle_solve_recycling.argtypes = [C.c_void_p, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int,
+                                             C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_double)]
+        L.oracle_new_loads.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+        L.oracle_recycling_size.argtypes = [C.c_void_p]
         L.oracle_adaptive_info.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
         L.oracle_sym_eig.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
         L.oracle_stats.argtypes = [C.c_void_p, C.c_void_p]
@@ -120,6 +124,26 @@ class Oracle:
     def setup(self, use_corner_constraints=1, use_arithmetic_constraints=1, weights_type=0):
         rc = self.L.oracle_setup(self.h, use_corner_constraints, use_arithmetic_constraints, weights_type)
         if rc != 0:
+            raise RuntimeError(self.L.oracle_error(self.h).decode())
+
+    def solve_recycling(self, tol=1e-8, maxit=500, ndecrmax=50, recycling=True, maxvec=100):
+        """PCG with Krylov recycling; the stored basis persists between calls."""
+        it, reason, cond = C.c_int(), C.c_int(), C.c_double()
+        rc = self.L.oracle_solve_recycling(self.h, tol, maxit, ndecrmax, int(recycling), maxvec, C.byref(it),
+                                           C.byref(reason), C.byref(cond))
+        if rc != 0:
+            raise RuntimeError(self.L.oracle_error(self.h).decode())
+        return it.value, reason.value, cond.value
+
+    def recycling_size(self):
+        return self.L.oracle_recycling_size(self.h)
+
+    def new_loads(self, isub, rhs, sol=None):
+        """New loads and initial guess (default zero) of one subdomain (same
+        Dirichlet data) after setup."""
+        r = np.ascontiguousarray(rhs, dtype=np.float64)
+        x = np.zeros_like(r) if sol is None else np.ascontiguousarray(sol, dtype=np.float64)
+        if self.L.oracle_new_loads(self.h, isub, r.ctypes.data, x.ctypes.data) != 0:
             raise RuntimeError(self.L.oracle_error(self.h).decode())
 
     def set_adaptive(self, on=True, tau=1.5):

@@ -280,3 +280,35 @@ def test_oracle_adaptive_constraints(oracle_mod):
         assert info["nadaptive"][p] == (eigs[p, :k] >= 10.0).sum()
     err = np.linalg.norm(oa.global_solution() - ud) / np.linalg.norm(ud)
     assert err < 1e-9
+
+
+def test_oracle_krylov_recycling(oracle_mod):
+    """PCG with Krylov recycling (module_krylov.f90:313-484, 663-726) over
+    consecutive load cases on one preconditioner: every solution matches a
+    direct solve, the stored S-orthonormal basis grows by the iterations of
+    each solve up to its capacity, and solving the same loads again needs no
+    iteration after the projection."""
+    from bddcml_gb300 import problems
+    from newdata_util import direct_solution
+    prob = problems.poisson_boxes(15, problems.uniform_boxes(15, 3), kappa=problems.lognormal_kappa(15, 1.0, 3))
+    o = oracle_mod.Oracle(prob)
+    o.setup(1, 1, 1)
+    rng = np.random.default_rng(2)
+    its, total = [], 0
+    for case in range(3):
+        if case > 0:
+            load = rng.uniform(0.5, 1.5, prob.ndof)
+            for s in prob.subdomains:
+                s.rhs = np.where(s.ifix != 0, 0.0, load[s.isvgvn] / prob.n_el_edge ** 3)
+                o.new_loads(s.isub, s.rhs)
+        it, reason, cond = o.solve_recycling(1e-10, 300, 50, True, 40)
+        assert reason == 0
+        total += it
+        its.append(it)
+        assert o.recycling_size() == min(40, total)
+        ud = direct_solution(prob)
+        assert np.linalg.norm(o.global_solution() - ud) / np.linalg.norm(ud) < 1e-8
+    for s in prob.subdomains:  # the same loads again, from a zero initial guess
+        o.new_loads(s.isub, s.rhs)
+    it, reason, cond = o.solve_recycling(1e-10, 300, 50, True, 40)
+    assert reason == 0 and it <= 1
