@@ -182,6 +182,30 @@ def bddcml_download_local_solution(isub: int, lsols: int) -> np.ndarray:
     return out
 
 
+def bddcml_download_global_solution(lsol: int) -> np.ndarray:
+    """Global solution gathered from the subdomains (module_levels.f90:4617-4744)."""
+    out = np.zeros(lsol)
+    lib().bddcml_download_global_solution_c(out.ctypes.data_as(C.POINTER(C.c_double)), _i(lsol))
+    _check()
+    return out
+
+
+def bddcml_download_local_reactions(isub: int, lreas: int) -> np.ndarray:
+    """Reactions of one subdomain after a solve (module_dd.f90:1258-1374, 3364-3395)."""
+    out = np.zeros(lreas)
+    lib().bddcml_download_local_reactions_c(_i(isub), out.ctypes.data_as(C.POINTER(C.c_double)), _i(lreas))
+    _check()
+    return out
+
+
+def bddcml_download_global_reactions(lrea: int) -> np.ndarray:
+    """Global reactions gathered from the subdomains (module_levels.f90:4785-4914)."""
+    out = np.zeros(lrea)
+    lib().bddcml_download_global_reactions_c(out.ctypes.data_as(C.POINTER(C.c_double)), _i(lrea))
+    _check()
+    return out
+
+
 def bddcml_dotprod_subdomain(isub: int, vec1, vec2) -> float:
     a, pa = _pd(vec1)
     b, pb = _pd(vec2)

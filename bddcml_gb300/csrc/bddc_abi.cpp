@@ -254,6 +254,8 @@ void bddcml_solve_c(int* comm_all, int* method, double* tol, int* maxit, int* nd
       if (rec && maxvec < 0) throw Error{ERR_ARGUMENT, "max_number_of_stored_vectors must not be negative"};
     }
     if (!device_solve(*S, m, t, mi, nd, rec, maxvec, it, reason, cond, err)) throw err;
+    S->solved = true;
+    S->reactions_ready = false;
     *num_iter = it;
     *converged_reason = reason;
     *condition_number = cond;
@@ -271,19 +273,52 @@ void bddcml_download_local_solution_c(int* isub, double* sols, int* lsols) {
   });
 }
 
-void bddcml_download_global_solution_c(double*, int*) {
-  clear_error();
-  set_error(BDDCML_ERR_UNSUPPORTED, "bddcml_download_global_solution_c: global data is not implemented");
+// the global vector with every subdomain's values written at its global dofs,
+// subdomains in order (levels_get_global_solution, module_levels.f90:4617-4744)
+static void gather_global(const Solver& S, const vector<double> Subdomain::*field, double* out, int lout) {
+  if (lout != S.ndof_global) throw Error{ERR_ARGUMENT, "array length does not match the global dof count"};
+  std::fill(out, out + lout, 0.0);
+  for (auto& s : S.subs) {
+    const vector<double>& v = s.*field;
+    for (int i = 0; i < s.ndof; ++i) out[s.isvgvn[i]] = v[i];
+  }
 }
 
-void bddcml_download_local_reactions_c(int*, double*, int*) {
-  clear_error();
-  set_error(BDDCML_ERR_UNSUPPORTED, "bddcml_download_local_reactions_c: reactions are not implemented");
+static void need_reactions(Solver& S) {
+  if (!S.solved) throw Error{ERR_ARGUMENT, "reactions are available after bddcml_solve"};
+  if (!S.reactions_ready) {
+    host_reactions(S);
+    S.reactions_ready = true;
+  }
 }
 
-void bddcml_download_global_reactions_c(double*, int*) {
-  clear_error();
-  set_error(BDDCML_ERR_UNSUPPORTED, "bddcml_download_global_reactions_c: reactions are not implemented");
+void bddcml_download_global_solution_c(double* sol, int* lsol) {
+  guarded("bddcml_download_global_solution_c", [&] {
+    Solver* S = need_solver("bddcml_download_global_solution_c");
+    if (!S) return;
+    gather_global(*S, &Subdomain::sol, sol, *lsol);
+  });
+}
+
+void bddcml_download_local_reactions_c(int* isub, double* reas, int* lreas) {
+  guarded("bddcml_download_local_reactions_c", [&] {
+    Solver* S = need_solver("bddcml_download_local_reactions_c");
+    if (!S) return;
+    int t = sub_index(*S, *isub);
+    need_reactions(*S);
+    Subdomain& s = S->subs[t];
+    if (*lreas != s.ndof) throw Error{ERR_ARGUMENT, "lreas does not match the subdomain dof count"};
+    std::copy(s.rea.begin(), s.rea.end(), reas);
+  });
+}
+
+void bddcml_download_global_reactions_c(double* rea, int* lrea) {
+  guarded("bddcml_download_global_reactions_c", [&] {
+    Solver* S = need_solver("bddcml_download_global_reactions_c");
+    if (!S) return;
+    need_reactions(*S);
+    gather_global(*S, &Subdomain::rea, rea, *lrea);
+  });
 }
 
 void bddcml_change_global_data_c(int*, int*, double*, int*, double*, int*, double*, int*) {

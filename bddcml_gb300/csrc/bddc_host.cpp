@@ -330,6 +330,39 @@ void host_new_data(Solver& S) {
   host_interface_bc(S);
 }
 
+void host_reactions(Solver& S) {
+  const int nsub = (int)S.subs.size();
+#pragma omp parallel for schedule(dynamic)
+  for (int t = 0; t < nsub; ++t) {
+    auto& s = S.subs[t];
+    s.rea.assign(s.ndof, 0.0);
+    if (!s.bc_present) continue;
+    // symmetric product with the fixed-rows matrix (upper triangle stored)
+    for (size_t k = 0; k < s.fxr_v.size(); ++k) {
+      const int i = s.fxr_i[k], j = s.fxr_j[k];
+      s.rea[i] += s.fxr_v[k] * s.sol[j];
+      if (i != j) s.rea[j] += s.fxr_v[k] * s.sol[i];
+    }
+    if (!s.rhs_complete)
+      for (int i = 0; i < s.ndof; ++i) if (s.ifix[i]) s.rea[i] -= s.rhs[i];
+  }
+  // neighbours' interface values added (dd_comm_upload / swapdata / download)
+  vector<double> sum(S.ninterface, 0.0);
+  for (auto& s : S.subs)
+    if (s.bc_present)
+      for (int i = 0; i < s.ndofi; ++i) sum[s.uniq[i]] += s.rea[s.iivsvn[i]];
+  bool any = false;
+  for (auto& s : S.subs) any = any || s.bc_present;
+  if (!any) return;
+#pragma omp parallel for schedule(dynamic)
+  for (int t = 0; t < nsub; ++t) {
+    auto& s = S.subs[t];
+    for (int i = 0; i < s.ndofi; ++i) s.rea[s.iivsvn[i]] = sum[s.uniq[i]];
+    if (s.rhs_complete && s.bc_present)
+      for (int i = 0; i < s.ndof; ++i) if (s.ifix[i]) s.rea[i] -= s.rhs[i];
+  }
+}
+
 void host_constraint_rows(Solver& S) {
   const int nsub = (int)S.subs.size();
   const int ncnode = S.ncorner + S.nedge + S.nface;
@@ -410,8 +443,10 @@ void host_setup(Solver& S) {
       s.bcx_tgt.push_back(tgt); s.bcx_src.push_back(src); s.bcx_val.push_back(v);
     };
     vector<char> diag_fixed(s.ndof, 0);
+    s.fxr_i.clear(); s.fxr_j.clear(); s.fxr_v.clear();
     for (size_t k = 0; k < s.ia.size(); ++k) {
       int i = s.ia[k], j = s.ja[k];
+      if (s.ifix[i] || s.ifix[j]) { s.fxr_i.push_back(i); s.fxr_j.push_back(j); s.fxr_v.push_back(s.a[k]); }
       if (i != j) {
         if (s.ifix[i] && s.a[k] != 0.0 && !s.ifix[j]) record(j, i, -s.a[k]);
         if (s.ifix[j] && s.a[k] != 0.0 && !s.ifix[i]) record(i, j, -s.a[k]);

@@ -82,6 +82,11 @@ struct Subdomain {
   // fixed rows of the matrix for the same purpose, module_dd.f90:1081-1180)
   vector<int> bcx_tgt, bcx_src;
   vector<double> bcx_val;
+  // entries of the uploaded matrix in fixed rows or columns, kept before the
+  // elimination for the reactions (the fixed-rows matrix of module_dd.f90:1160-1211)
+  vector<int> fxr_i, fxr_j;
+  vector<double> fxr_v;
+  vector<double> rea;        // reactions after the last solve
   vector<double> wi;         // interface weights
   vector<double> rhoi;       // coefficients the weights are built from (module_dd.f90:11660-11722)
   vector<int> uniq;          // interface dof -> unique interface index
@@ -171,6 +176,8 @@ struct Solver {
   vector<double> iface_wsum;          // per unique dof: sum of subdomain weights
   bool setup_done = false;
   bool new_data_pending = false;  // changed subdomain data not yet through setup_new_data
+  bool solved = false;            // a solve has produced the subdomain solutions
+  bool reactions_ready = false;   // reactions computed for the last solve
   Device* dev = nullptr;
   Stats stats;
   vector<double> relres_history;
@@ -207,6 +214,9 @@ void host_reduced_rhs_inputs(const Subdomain& s, vector<double>& fo, vector<doub
 // new boundary values / loads after setup: recompute bc on every subdomain and
 // assemble it over the interface (module_levels.f90:855-903)
 void host_new_data(Solver& S);
+// reactions A_fixed u - f on every subdomain, assembled on the interface
+// (dd_compute_reactions, module_dd.f90:1258-1374)
+void host_reactions(Solver& S);
 
 // device (bddc_device.cu)
 Device* device_create(Error& err);

@@ -102,16 +102,23 @@ void bddcml_solve_c(int *comm_all, int *method, double *tol, int *maxit, int *nd
 /* replaces bddcml_download_local_solution_c, src/bddcml_interface_c.h:41 */
 void bddcml_download_local_solution_c(int *isub, double *sols, int *lsols);
 
-/* replaces bddcml_download_global_solution_c, src/bddcml_interface_c.h:43 (unsupported) */
+/* replaces bddcml_download_global_solution_c, src/bddcml_interface_c.h:43
+ * (module_levels.f90:4617-4744): every subdomain's solution written at its
+ * global dofs; *lsol must be the global dof count. */
 void bddcml_download_global_solution_c(double *sol, int *lsol);
 
-/* replaces bddcml_download_local_reactions_c, src/bddcml_interface_c.h:45 (unsupported) */
+/* replaces bddcml_download_local_reactions_c, src/bddcml_interface_c.h:45
+ * (module_dd.f90:1258-1374, 3364-3395): A_fixed u - f of the subdomain after a
+ * solve, A_fixed the uploaded entries in fixed rows and columns, values on
+ * shared dofs summed over the subdomains, the load subtracted on fixed dofs. */
 void bddcml_download_local_reactions_c(int *isub, double *reas, int *lreas);
 
-/* replaces bddcml_download_global_reactions_c, src/bddcml_interface_c.h:47 (unsupported) */
+/* replaces bddcml_download_global_reactions_c, src/bddcml_interface_c.h:47
+ * (module_levels.f90:4785-4914): the subdomains' reactions at their global dofs. */
 void bddcml_download_global_reactions_c(double *rea, int *lrea);
 
-/* replaces bddcml_change_global_data_c, src/bddcml_interface_c.h:49 (unsupported) */
+/* replaces bddcml_change_global_data_c, src/bddcml_interface_c.h:49; it needs data
+ * loaded by bddcml_upload_global_data_c, which is not implemented (unsupported) */
 void bddcml_change_global_data_c(int *ifix, int *lifix, double *fixv, int *lfixv, double *rhs, int *lrhs,
                                  double *sol, int *lsol);
 

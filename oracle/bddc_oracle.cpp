@@ -209,6 +209,8 @@ struct Sub {
   vector<double> g, solo;
   // full symmetric CSR of the whole (BC-eliminated) matrix
   vector<int> f_ptr, f_col; vector<double> f_val;
+  // fixed-rows matrix (upper triangle entries in a fixed row or column, before elimination)
+  vector<int> fx_i, fx_j; vector<double> fx_v;
 };
 
 struct Oracle {
@@ -1347,8 +1349,10 @@ int oracle_setup(void* h, int use_corner_constraints, int use_arithmetic_constra
       S.bc.assign(S.ndof, 0.0);
       if (S.bc_present) {
         vector<char> diag_fixed(S.ndof, 0);
+        S.fx_i.clear(); S.fx_j.clear(); S.fx_v.clear();
         for (size_t k = 0; k < S.ia.size(); ++k) {
           int i = S.ia[k], j = S.ja[k];
+          if (S.ifix[i] || S.ifix[j]) { S.fx_i.push_back(i); S.fx_j.push_back(j); S.fx_v.push_back(S.a[k]); }
           if (i != j) {
             if (S.ifix[i] && S.fixv[i] != 0.0 && S.a[k] != 0.0 && !S.ifix[j]) S.bc[j] -= S.a[k] * S.fixv[i];
             if (S.ifix[j] && S.fixv[j] != 0.0 && S.a[k] != 0.0 && !S.ifix[i]) S.bc[i] -= S.a[k] * S.fixv[j];
@@ -2024,6 +2028,40 @@ void oracle_sym_eig(int n, const double* a, double* w, double* z) {
   sym_eig(n, m, wv, zv);
   std::copy(wv.begin(), wv.end(), w);
   std::copy(zv.begin(), zv.end(), z);
+}
+
+// reactions of every subdomain after a solve (dd_compute_reactions, module_dd.f90:1258-1374):
+// rea = A_fixed u over the fixed-rows matrix, neighbours' interface values added, minus the
+// load on the fixed dofs; out receives subdomain isub's (ndof values)
+int oracle_reactions(void* h, int isub, double* out) {
+  auto* o = static_cast<Oracle*>(h);
+  const int nsub = o->nsub;
+  vector<vector<double>> rea(nsub), ri(nsub);
+  bool any = false;
+  for (int s = 0; s < nsub; ++s) {
+    auto& S = o->subs[s];
+    rea[s].assign(S.ndof, 0.0);
+    ri[s].assign(S.ndofi, 0.0);
+    if (!S.bc_present) continue;
+    any = true;
+    for (size_t k = 0; k < S.fx_v.size(); ++k) {
+      const int i = S.fx_i[k], j = S.fx_j[k];
+      rea[s][i] += S.fx_v[k] * S.sol[j];
+      if (i != j) rea[s][j] += S.fx_v[k] * S.sol[i];
+    }
+    if (!S.rhs_complete) for (int i = 0; i < S.ndof; ++i) if (S.ifix[i]) rea[s][i] -= S.rhs[i];
+    for (int i = 0; i < S.ndofi; ++i) ri[s][i] = rea[s][S.iivsvn[i]];
+  }
+  if (any) {
+    comm_exchange(*o, ri, false);
+    for (int s = 0; s < nsub; ++s) {
+      auto& S = o->subs[s];
+      for (int i = 0; i < S.ndofi; ++i) rea[s][S.iivsvn[i]] += ri[s][i];
+      if (S.rhs_complete && S.bc_present) for (int i = 0; i < S.ndof; ++i) if (S.ifix[i]) rea[s][i] -= S.rhs[i];
+    }
+  }
+  std::copy(rea[isub].begin(), rea[isub].end(), out);
+  return 0;
 }
 
 int oracle_recycling_size(void* h) { return (int)static_cast<Oracle*>(h)->rcv.size(); }

@@ -54,6 +54,7 @@ def lib():
                                              C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_double)]
         L.oracle_new_loads.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
         L.oracle_recycling_size.argtypes = [C.c_void_p]
+        L.oracle_reactions.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
         L.oracle_adaptive_info.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
         L.oracle_sym_eig.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
         L.oracle_stats.argtypes = [C.c_void_p, C.c_void_p]
@@ -134,6 +135,18 @@ class Oracle:
         if rc != 0:
             raise RuntimeError(self.L.oracle_error(self.h).decode())
         return it.value, reason.value, cond.value
+
+    def reactions(self, isub):
+        """Reactions of subdomain isub after a solve (ndofs values)."""
+        out = np.zeros(self.prob.subdomains[isub].ndofs)
+        self.L.oracle_reactions(self.h, isub, out.ctypes.data)
+        return out
+
+    def global_reactions(self):
+        r = np.zeros(self.prob.ndof)
+        for s in self.prob.subdomains:
+            r[s.isvgvn] = self.reactions(s.isub)
+        return r
 
     def recycling_size(self):
         return self.L.oracle_recycling_size(self.h)

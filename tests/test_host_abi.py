@@ -115,9 +115,12 @@ def test_errors_are_status_codes(built_lib):
         B.bddcml_setup_preconditioner(1, 0, 1, 1, 1, 1, 0, 0)  # adaptive constraints
     assert ei.value.code in (1, 4)
     B.bddcml_finalize()
-    # global-data entry points are reported unsupported, not aborted
-    B.lib().bddcml_download_global_solution_c(None, None)
+    # global-data loading is reported unsupported, not aborted
+    B.lib().bddcml_change_global_data_c(None, None, None, None, None, None, None, None)
     assert B.last_error()[0] == 4
+    # the global solution needs an initialised solver
+    B.lib().bddcml_download_global_solution_c(None, None)
+    assert B.last_error()[0] == 1
 
 
 def test_setup_without_gpu_reports_an_error(built_lib):

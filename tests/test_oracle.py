@@ -312,3 +312,35 @@ def test_oracle_krylov_recycling(oracle_mod):
         o.new_loads(s.isub, s.rhs)
     it, reason, cond = o.solve_recycling(1e-10, 300, 50, True, 40)
     assert reason == 0 and it <= 1
+
+
+def test_oracle_reactions_balance_the_loads(oracle_mod):
+    """Reactions (dd_compute_reactions, module_dd.f90:1258-1374) on the fixed
+    dofs are K u - f there.  The Q1 Laplace matrix has zero row sums, so they
+    sum to minus the total load; they also equal K u - f of the assembled
+    global system at every fixed dof."""
+    from bddcml_gb300 import problems
+    from newdata_util import changed_data
+    prob = changed_data(problems.poisson_on_cube(4, 3), seed=5)
+    o = oracle_mod.Oracle(prob)
+    o.setup(1, 1, 0)
+    it, reason, cond = o.solve(1e-12, 300, 50)
+    assert reason == 0
+    u = o.global_solution()
+    rea = o.global_reactions()
+    fixed = np.zeros(prob.ndof, dtype=bool)
+    f = np.zeros(prob.ndof)
+    for s in prob.subdomains:
+        fixed[s.isvgvn[s.ifix != 0]] = True
+        f[s.isvgvn] = s.rhs  # loads are given complete at shared dofs
+    import scipy.sparse as sp
+    rows, cols, vals = [], [], []
+    for s in prob.subdomains:
+        g = s.isvgvn
+        rows.append(g[s.i_sparse]); cols.append(g[s.j_sparse]); vals.append(s.a_sparse)
+        off = s.i_sparse != s.j_sparse
+        rows.append(g[s.j_sparse[off]]); cols.append(g[s.i_sparse[off]]); vals.append(s.a_sparse[off])
+    K = sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(prob.ndof, prob.ndof))
+    r_true = K @ u - f
+    assert np.abs(rea[fixed] - r_true[fixed]).max() <= 1e-9 * np.abs(r_true[fixed]).max()
+    assert abs(rea[fixed].sum() + f.sum()) <= 1e-9 * np.abs(f).sum()
