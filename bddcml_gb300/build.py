@@ -20,6 +20,7 @@ SOURCES = [
     ("bddc_host.cpp", "g++"),
     ("bddc_abi.cpp", "g++"),
     ("bddc_adaptive.cpp", "g++"),
+    ("bddc_levels.cpp", "g++"),
     ("bddc_device.cu", "nvcc"),
     ("bddc_noalloc.cu", "nvcc"),
     ("bddc_gradient.cu", "nvcc"),

@@ -71,18 +71,18 @@ void bddcml_init_c(int* nl, int* nsublev, int* lnsublev, int* nsub_loc_1, int* c
     if (*nl < 2) throw Error{ERR_ARGUMENT, "number of levels must be at least 2"};
     if (*lnsublev < *nl) throw Error{ERR_ARGUMENT, "lnsublev smaller than the number of levels"};
     if (nsublev[*nl - 1] != 1) throw Error{ERR_ARGUMENT, "number of subdomains at the last level must be 1"};
-    if (*nl > 2) throw Error{ERR_UNSUPPORTED, "only 2 levels are implemented"};
+    if (*nl > 3 || *nl < 2) throw Error{ERR_UNSUPPORTED, "2 or 3 levels are implemented"};
+    if (*nl == 3 && (nsublev[1] < 1 || nsublev[1] > nsublev[0]))
+      throw Error{ERR_ARGUMENT, "level-2 subdomain count must be between 1 and the level-1 count"};
     if (just_direct_solve_int && *just_direct_solve_int)
       throw Error{ERR_UNSUPPORTED, "the global direct solve (just_direct_solve) is not implemented"};
     if (*nsub_loc_1 != -1 && *nsub_loc_1 != nsublev[0])
       throw Error{ERR_ARGUMENT, "all subdomains live in this process: nsub_loc_1 must be -1 or nsublev[0]"};
-    if (g_solver) {
-      if (g_solver->dev) device_destroy(g_solver->dev);
-      g_solver.reset();
-    }
+    g_solver.reset();  // the solver destroys its device state
     auto S = std::make_unique<Solver>();
     S->prm.nlevels = *nl;
     S->prm.nsub = nsublev[0];
+    S->prm.nsub2 = *nl == 3 ? nsublev[1] : 1;
     S->prm.numbase = *numbase;
     S->prm.verbose = verbose_level ? *verbose_level : 0;
     S->subs.resize(nsublev[0]);
@@ -378,10 +378,7 @@ void bddcml_dotprod_subdomain_c(int* isub, double* vec1, int* lvec1, double* vec
 
 void bddcml_finalize_c(void) {
   guarded("bddcml_finalize_c", [&] {
-    if (g_solver) {
-      if (g_solver->dev) device_destroy(g_solver->dev);
-      g_solver.reset();
-    }
+    g_solver.reset();  // the solver destroys its device state
   });
 }
 

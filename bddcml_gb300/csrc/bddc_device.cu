@@ -8,6 +8,7 @@
 #include <cstdint>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <numeric>
 #include <string>
 #include <type_traits>
@@ -39,6 +40,22 @@ static long long g_launches = 0;
   } while (0)
 
 static inline int roundup(int x, int m) { return (x + m - 1) / m * m; }
+
+// Dynamic shared memory limits are per kernel and process, and several
+// solvers (the levels of a three-level setup) launch the same kernels: the
+// limit only ever grows to the largest request.
+template <typename K>
+static void raise_smem(K* kernel, size_t bytes) {
+  static std::unordered_map<const void*, size_t> done;
+  static std::mutex mu;
+  std::lock_guard<std::mutex> lk(mu);
+  size_t& cur = done[reinterpret_cast<const void*>(kernel)];
+  if (bytes <= cur) return;
+  cudaError_t e = cudaFuncSetAttribute(reinterpret_cast<const void*>(kernel),
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e != cudaSuccess) throw Error{ERR_CUDA, std::string("shared memory attribute: ") + cudaGetErrorString(e)};
+  cur = bytes;
+}
 
 // Phase timers: CUDA events recorded on the solver's stream.  The two totals
 // are always recorded; the per-phase and per-kernel slots only when profiling
@@ -212,6 +229,13 @@ class Device {
   double *rcV = nullptr, *rcW = nullptr, *rc_part = nullptr, *rc_coef = nullptr;
   int* rc_nact_dev = nullptr;
   int rc_cap = 0, rc_nact = 0;
+  // three levels: the level-2 problem (on level 1), and the maps of a level-2
+  // device between its layouts and the level-1 coarse dofs
+  bool own_stream = true;
+  Solver* lev2 = nullptr;
+  int *l2_mo = nullptr, *l2_mi = nullptr, *l2_mz = nullptr;
+  double* l2_wi = nullptr;
+  int l2_nfo = 0;
   int maxnbo = 0, maxw = 0, maxNR = 0;
   int nref = 0;
   Profiler prof;
@@ -221,9 +245,9 @@ class Device {
     if (hctl) cudaFreeHost(hctl);
     if (st) {
       cudaStreamSynchronize(st);
-      cudaStreamDestroy(st);
+      if (own_stream) cudaStreamDestroy(st);
     }
-    if (g_alloc_st == st) g_alloc_st = nullptr;
+    if (own_stream && g_alloc_st == st) g_alloc_st = nullptr;
   }
   void release() {
     nv_v0 = nv_v1 = nv_r = nullptr;
@@ -231,6 +255,9 @@ class Device {
     rcV = rcW = rc_part = rc_coef = nullptr;
     rc_nact_dev = nullptr;
     rc_cap = rc_nact = 0;
+    lev2 = nullptr;
+    l2_mo = l2_mi = l2_mz = nullptr;
+    l2_wi = nullptr;
     nv_off = nullptr;
     release_pc();
     for (void* q : owned) cudaFreeAsync(q, st);
@@ -261,6 +288,19 @@ Device* device_create(Error& err) {
   return d;
 }
 
+Device* device_create_on_stream(Device* parent, Error& err) {
+  auto* d = new Device;
+  d->st = parent->st;
+  d->own_stream = false;
+  if (cudaMallocHost(&d->hctl, sizeof(PcgCtl)) != cudaSuccess) {
+    err = Error{ERR_CUDA, "pinned allocation failed"};
+    d->st = nullptr;
+    delete d;
+    return nullptr;
+  }
+  return d;
+}
+
 bool device_release_memory(Error& err) {
   try {
     CK(cudaDeviceSynchronize());
@@ -279,7 +319,7 @@ void device_destroy(Device* d) { delete d; }
 template <typename T>
 static void run_factor(Device& D, const BandDesc* bd, int nbatch, int maxnb, int maxw, T* pool) {
   size_t smem = (2 * NB * (NB + 1) + 2 * SM_TILE) * sizeof(T);
-  CK(cudaFuncSetAttribute(k_chol_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  raise_smem(k_chol_diag<T>, smem);
   for (int k = 0; k < maxnb; ++k) {
     k_chol_diag<T><<<nbatch, NT, smem, D.st>>>(bd, pool, k, D.err);
     CKL();
@@ -353,10 +393,13 @@ template <typename T>
 static void setup_precond(Solver& S, Device& D);
 template <typename T>
 static void adaptive_constraints(Solver& S, Device& D);
+template <typename T>
+static void setup_level2(Solver& S, Device& D);
 
 bool device_setup(Solver& S, Error& err) {
   Device& D = *S.dev;
   try {
+    S.lev2.reset();  // the previous level-2 state shares this device's stream
     D.release();
     D.prof.reset();
     g_h2d_bytes = 0.0;
@@ -369,7 +412,8 @@ bool device_setup(Solver& S, Error& err) {
     vector<SubBlocks>& blk = S.blocks;
     for (int t = 0; t < nsub; ++t) {
       auto& b = blk[t];
-      if (b.maxrow_oo > 96 || b.maxrow_oi > 95 || b.maxrow_io > 128 || b.maxrow_ii > 128)
+      // the double-float residual and Schur kernels stage a row in shared memory
+      if (D.mixed && (b.maxrow_oo > 96 || b.maxrow_oi > 95 || b.maxrow_io > 128 || b.maxrow_ii > 128))
         throw Error{ERR_UNSUPPORTED, "subdomain matrix rows longer than the staging buffers (96/128 entries)"};
       if (S.subs[t].ndofi == 0) throw Error{ERR_ARGUMENT, "subdomain without interface"};
     }
@@ -382,6 +426,7 @@ bool device_setup(Solver& S, Error& err) {
         adaptive_constraints<float>(S, D);
         setup_precond<float>(S, D);
       }
+      if (S.prm.nlevels == 3) setup_level2<float>(S, D);
     } else {
       setup_numeric<double>(S, D, blk);
       setup_precond<double>(S, D);
@@ -389,6 +434,7 @@ bool device_setup(Solver& S, Error& err) {
         adaptive_constraints<double>(S, D);
         setup_precond<double>(S, D);
       }
+      if (S.prm.nlevels == 3) setup_level2<double>(S, D);
     }
     vector<SubBlocks>().swap(S.blocks);
     // check device error flags
@@ -566,14 +612,11 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
 
   T* poolT = static_cast<T*>(D.poolT);
   if (D.mixed)
-    CK(cudaFuncSetAttribute(k_schur_apply_df, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                            (int)(D.maxNI * sizeof(float2))));
+    raise_smem(k_schur_apply_df, D.maxNI * sizeof(float2));
   else
-    CK(cudaFuncSetAttribute(k_schur_apply_f64, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                            (int)(D.maxNI * sizeof(double))));
-  CK(cudaFuncSetAttribute(k_pc_local<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(D.maxNI * sizeof(T))));
-  CK(cudaFuncSetAttribute(k_post_df, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                          (int)((D.maxNI + 1) * sizeof(float2))));
+    raise_smem(k_schur_apply_f64, D.maxNI * sizeof(double));
+  raise_smem(k_pc_local<T>, D.maxNI * sizeof(T));
+  raise_smem(k_post_df, (D.maxNI + 1) * sizeof(float2));
   (void)ppool;
 
   // ---- interior band factor
@@ -809,7 +852,7 @@ static void setup_precond(Solver& S, Device& D) {
   D.prof.begin(PH_PC_BLOCKS, st);
   {
     size_t smem = 2 * (size_t)std::max(1, maxnc) * std::max(1, maxnc) * sizeof(double);
-    CK(cudaFuncSetAttribute(k_small_g<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    raise_smem(k_small_g<T>, smem);
     k_small_g<T><<<nsub, 256, smem, st>>>(D.ds, D.c_ptr, D.c_col, D.c_val, poolP, D.small, D.err);
     CKL();
   }
@@ -825,7 +868,9 @@ static void setup_precond(Solver& S, Device& D) {
   // ---- coarse problem (levels_prepare_last_level, module_levels.f90:3001-3170):
   // sparse FP64 matrix assembled on the device in a fixed order, factor and
   // explicit inverse in factor precision; the solve is refined in FP64.
-  {
+  if (S.prm.nlevels == 3) {  // the coarse problem is the level-2 problem (setup_level2)
+    D.cres = dalloc<double>(std::max(1, D.ndofc), own);
+  } else {
     int nc_g = D.ndofc;
     int nbc = std::max(2, (nc_g + TC_M - 1) / TC_M * 2);  // even number of 64-blocks: ld multiple of 128
     D.ldc = nbc * NB;
@@ -890,6 +935,83 @@ static void setup_precond(Solver& S, Device& D) {
   CK(cudaStreamSynchronize(st));
 }
 
+// Phi_s^T S_s Phi_s for the subdomains in `subs` (nc x nc, row-major), with
+// FP64-accurate S products (double-float on the float2 S in mixed precision);
+// Phi_s (ni x nc, column-major, FP64) returned in *phis when asked.  The setup's
+// local coarse matrices G^-1 - rho D^2 carry the FP32 error of the factors.
+template <typename T>
+static vector<vector<double>> coarse_energies(Device& D, const vector<int>& subs, vector<vector<double>>* phis) {
+  cudaStream_t st = D.st;
+  const int nsub = D.nsub;
+  vector<vector<double>> out(subs.size());
+  if (phis) phis->assign(subs.size(), {});
+  if (subs.empty()) return out;
+  std::vector<void*> tmp;
+  vector<long long> off(subs.size() + 1, 0);
+  for (size_t f = 0; f < subs.size(); ++f) off[f + 1] = off[f] + (long long)D.hs[subs[f]].ni * D.hs[subs[f]].nc;
+  const long long tot = off[subs.size()];
+  vector<double> hphi(std::max<long long>(1, tot));
+  {
+    vector<T> phi;
+    for (size_t f = 0; f < subs.size(); ++f) {
+      const DevSub& d = D.hs[subs[f]];
+      phi.resize((size_t)d.NI * d.ncp);
+      CK(cudaMemcpyAsync(phi.data(), static_cast<const T*>(D.poolPC) + d.oPhi, phi.size() * sizeof(T),
+                         cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+      for (int c = 0; c < d.nc; ++c)
+        for (int r = 0; r < d.ni; ++r) hphi[off[f] + (long long)c * d.ni + r] = (double)phi[(size_t)r * d.ncp + c];
+    }
+  }
+  double* buf = dalloc<double>((size_t)2 * std::max<long long>(1, tot), tmp);
+  CK(cudaMemcpyAsync(buf, hphi.data(), tot * sizeof(double), cudaMemcpyHostToDevice, st));
+  vector<int> tptr(nsub + 1, 0);
+  vector<long long> tin, tout;
+  int maxc = 0;
+  {
+    size_t f = 0;
+    vector<int> order(subs.size());
+    for (int t = 0; t < nsub; ++t) {
+      while (f < subs.size() && subs[f] == t) {
+        const DevSub& d = D.hs[t];
+        for (int c = 0; c < d.nc; ++c) {
+          tin.push_back(off[f] + (long long)c * d.ni);
+          tout.push_back(tot + off[f] + (long long)c * d.ni);
+        }
+        maxc = std::max(maxc, d.nc);
+        ++f;
+      }
+      tptr[t + 1] = (int)tin.size();
+    }
+  }
+  ColTab tab{upload(tptr, tmp, st), upload(tin, tmp, st), upload(tout, tmp, st)};
+  dim3 g((D.maxNI + 63) / 64, (maxc + 63) / 64, nsub);
+  if (D.mixed) k_ad_gemm_df<<<g, 256, 0, st>>>(D.ds, static_cast<const float2*>(D.poolS), tab, buf);
+  else k_ad_gemm<double, false, double><<<g, 256, 0, st>>>(D.ds, static_cast<const double*>(D.poolS), tab, buf);
+  CKL();
+  vector<double> hsphi(std::max<long long>(1, tot));
+  CK(cudaMemcpyAsync(hsphi.data(), buf + tot, tot * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  for (void* q : tmp) cudaFreeAsync(q, st);
+#pragma omp parallel for schedule(dynamic)
+  for (int f = 0; f < (int)subs.size(); ++f) {
+    const DevSub& d = D.hs[subs[f]];
+    const double* ph = &hphi[off[f]];
+    const double* sp = &hsphi[off[f]];
+    vector<double>& ac = out[f];
+    ac.assign((size_t)d.nc * d.nc, 0.0);
+    for (int a = 0; a < d.nc; ++a)
+      for (int b = 0; b < d.nc; ++b) {
+        double t2 = 0.0;
+        for (int r = 0; r < d.ni; ++r) t2 += ph[(long long)a * d.ni + r] * sp[(long long)b * d.ni + r];
+        ac[(size_t)a * d.nc + b] = t2;
+      }
+  }
+  if (phis)
+    for (size_t f = 0; f < subs.size(); ++f) (*phis)[f].assign(hphi.begin() + off[f], hphi.begin() + off[f + 1]);
+  return out;
+}
+
 // ------------------------------------------------------------ adaptive constraints
 // Batched LOBPCG over all face pairs (adaptivity_solve_eigenvectors,
 // module_adaptivity.f90:296-2514; 15 iterations as lobpcg_maxit, :38), then
@@ -910,87 +1032,32 @@ static void adaptive_constraints(Solver& S, Device& D) {
     vector<int> fl;
     for (int t = 0; t < nsub; ++t)
       if (!S.subs[t].bc_present && D.hs[t].nc > 0) fl.push_back(t);
-    if (!fl.empty()) {
-      std::vector<void*> tmp0;
-      // columns: Phi_s (converted to FP64) in, S Phi_s out
-      vector<long long> off(fl.size() + 1, 0);
-      for (size_t f = 0; f < fl.size(); ++f) off[f + 1] = off[f] + (long long)D.hs[fl[f]].ni * D.hs[fl[f]].nc;
-      const long long tot = off[fl.size()];
-      vector<double> hphi(tot);
-      {
-        vector<T> phi;
-        for (size_t f = 0; f < fl.size(); ++f) {
-          const DevSub& d = D.hs[fl[f]];
-          phi.resize((size_t)d.NI * d.ncp);
-          CK(cudaMemcpyAsync(phi.data(), static_cast<const T*>(D.poolPC) + d.oPhi, phi.size() * sizeof(T),
-                             cudaMemcpyDeviceToHost, st));
-          CK(cudaStreamSynchronize(st));
-          for (int c = 0; c < d.nc; ++c)
-            for (int r = 0; r < d.ni; ++r) hphi[off[f] + (long long)c * d.ni + r] = (double)phi[(size_t)r * d.ncp + c];
-        }
-      }
-      double* buf = dalloc<double>((size_t)2 * tot, tmp0);
-      CK(cudaMemcpyAsync(buf, hphi.data(), tot * sizeof(double), cudaMemcpyHostToDevice, st));
-      vector<int> tptr(nsub + 1, 0);
-      vector<long long> tin, tout;
-      int maxc = 0;
-      {
-        size_t f = 0;
-        for (int t = 0; t < nsub; ++t) {
-          if (f < fl.size() && fl[f] == t) {
-            const DevSub& d = D.hs[t];
-            for (int c = 0; c < d.nc; ++c) {
-              tin.push_back(off[f] + (long long)c * d.ni);
-              tout.push_back(tot + off[f] + (long long)c * d.ni);
-            }
-            maxc = std::max(maxc, d.nc);
-            ++f;
-          }
-          tptr[t + 1] = (int)tin.size();
-        }
-      }
-      ColTab tab{upload(tptr, tmp0, st), upload(tin, tmp0, st), upload(tout, tmp0, st)};
-      dim3 g((D.maxNI + 63) / 64, (maxc + 63) / 64, nsub);
-      if (D.mixed) k_ad_gemm_df<<<g, 256, 0, st>>>(D.ds, static_cast<const float2*>(D.poolS), tab, buf);
-      else k_ad_gemm<double, false, double><<<g, 256, 0, st>>>(D.ds, static_cast<const double*>(D.poolS), tab, buf);
-      CKL();
-      vector<double> hsphi(tot);
-      CK(cudaMemcpyAsync(hsphi.data(), buf + tot, tot * sizeof(double), cudaMemcpyDeviceToHost, st));
-      CK(cudaStreamSynchronize(st));
-      for (void* q : tmp0) cudaFreeAsync(q, st);
+    vector<vector<double>> phis;
+    vector<vector<double>> acs = coarse_energies<T>(D, fl, &phis);
 #pragma omp parallel for schedule(dynamic)
-      for (int f = 0; f < (int)fl.size(); ++f) {
-        const DevSub& d = D.hs[fl[f]];
-        const double* ph = &hphi[off[f]];
-        const double* sp = &hsphi[off[f]];
-        vector<double> ac((size_t)d.nc * d.nc);
-        for (int a = 0; a < d.nc; ++a)
-          for (int b = 0; b < d.nc; ++b) {
-            double t2 = 0.0;
-            for (int r = 0; r < d.ni; ++r) t2 += ph[(long long)a * d.ni + r] * sp[(long long)b * d.ni + r];
-            ac[(size_t)a * d.nc + b] = t2;
-          }
-        int dn = 0;
-        vector<double> y = host_coarse_null_coefficients(d.nc, d.nc, ac.data(), dn);
-        vector<double>& nv = nulls[fl[f]];
-        nv.assign((size_t)d.ni * dn, 0.0);
-        for (int c = 0; c < dn; ++c) {
-          for (int r = 0; r < d.ni; ++r) {
-            double acc = 0.0;
-            for (int q = 0; q < d.nc; ++q) acc += ph[(long long)q * d.ni + r] * y[(size_t)q * dn + c];
-            nv[(size_t)c * d.ni + r] = acc;
-          }
-          for (int pass = 0; pass < 2; ++pass)
-            for (int c2 = 0; c2 < c; ++c2) {
-              double tt = 0.0;
-              for (int r = 0; r < d.ni; ++r) tt += nv[(size_t)c2 * d.ni + r] * nv[(size_t)c * d.ni + r];
-              for (int r = 0; r < d.ni; ++r) nv[(size_t)c * d.ni + r] -= tt * nv[(size_t)c2 * d.ni + r];
-            }
-          double nn = 0.0;
-          for (int r = 0; r < d.ni; ++r) nn += nv[(size_t)c * d.ni + r] * nv[(size_t)c * d.ni + r];
-          nn = std::sqrt(nn);
-          for (int r = 0; r < d.ni; ++r) nv[(size_t)c * d.ni + r] = nn > 0 ? nv[(size_t)c * d.ni + r] / nn : 0.0;
+    for (int f = 0; f < (int)fl.size(); ++f) {
+      const DevSub& d = D.hs[fl[f]];
+      const double* ph = phis[f].data();
+      int dn = 0;
+      vector<double> y = host_coarse_null_coefficients(d.nc, d.nc, acs[f].data(), dn);
+      vector<double>& nv = nulls[fl[f]];
+      nv.assign((size_t)d.ni * dn, 0.0);
+      for (int c = 0; c < dn; ++c) {
+        for (int r = 0; r < d.ni; ++r) {
+          double acc = 0.0;
+          for (int q = 0; q < d.nc; ++q) acc += ph[(long long)q * d.ni + r] * y[(size_t)q * dn + c];
+          nv[(size_t)c * d.ni + r] = acc;
         }
+        for (int pass = 0; pass < 2; ++pass)
+          for (int c2 = 0; c2 < c; ++c2) {
+            double tt = 0.0;
+            for (int r = 0; r < d.ni; ++r) tt += nv[(size_t)c2 * d.ni + r] * nv[(size_t)c * d.ni + r];
+            for (int r = 0; r < d.ni; ++r) nv[(size_t)c * d.ni + r] -= tt * nv[(size_t)c2 * d.ni + r];
+          }
+        double nn = 0.0;
+        for (int r = 0; r < d.ni; ++r) nn += nv[(size_t)c * d.ni + r] * nv[(size_t)c * d.ni + r];
+        nn = std::sqrt(nn);
+        for (int r = 0; r < d.ni; ++r) nv[(size_t)c * d.ni + r] = nn > 0 ? nv[(size_t)c * d.ni + r] / nn : 0.0;
       }
     }
   }
@@ -1289,6 +1356,8 @@ static void launch_schur(Device& D, const double* vin, double* vout, bool zero_f
   CKL();
 }
 
+static void level2_apply(Device& D1, const double* rc, double* uc);
+
 template <typename T>
 static void launch_pc(Device& D, const double* rin, double* zout, const PcgCtl* ctl) {
   dim3 grid(D.nrb, D.nsub);
@@ -1298,7 +1367,12 @@ static void launch_pc(Device& D, const double* rin, double* zout, const PcgCtl* 
                                           D.rcpart, D.nrb, D.ncpmax, ctl);
   CKL();
   D.prof.end(PH_PC_LOCAL, D.st);
-  if (D.ndofc > 0) {
+  if (D.ndofc > 0 && D.lev2) {
+    k_coarse_gather<<<(D.ndofc + 255) / 256, 256, 0, D.st>>>(D.ndofc, D.co_ptr, D.co_sub, D.co_loc, D.ds, D.rcpart,
+                                                           D.nrb, D.ncpmax, D.rc, ctl);
+    CKL();
+    level2_apply(D, D.rc, D.uc);
+  } else if (D.ndofc > 0) {
     k_coarse_gather<<<(D.ndofc + 255) / 256, 256, 0, D.st>>>(D.ndofc, D.co_ptr, D.co_sub, D.co_loc, D.ds, D.rcpart,
                                                            D.nrb, D.ncpmax, D.rc, ctl);
     CKL();
@@ -1673,6 +1747,11 @@ void device_get_profile(Device* d, double* ms, int* cnt) {
 // the right-hand-side column of X, and g = f_i - A_io v is formed.  Factors,
 // Schur complements and preconditioner stay as they are.
 template <typename T>
+static void ensure_nv(Device& D);
+template <typename T>
+static void reduced_rhs_device(Device& D);
+
+template <typename T>
 static void new_data_impl(Solver& S) {
   Device& D = *S.dev;
   const int nsub = D.nsub;
@@ -1695,19 +1774,41 @@ static void new_data_impl(Solver& S) {
   CK(cudaMemcpyAsync(D.fo, fov.data(), nfo * sizeof(double), cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(D.fi, fir.data(), D.nrep * sizeof(double), cudaMemcpyHostToDevice, st));
   g_h2d_bytes += (double)(nfo + D.nrep) * sizeof(double);
-  if (!D.nv_v0) {
-    D.nv_v0 = dalloc<T>(nv, own);
-    D.nv_v1 = dalloc<T>(nv, own);
-    D.nv_r = dalloc<T>(nv, own);
-    D.nv_off = upload(voff, own, st);
-  }
+  (void)own; (void)nv; (void)voff;
+  ensure_nv<T>(D);
+  reduced_rhs_device<T>(D);
+  int herr = 0;
+  CK(cudaMemcpyAsync(&herr, D.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (herr) throw Error{ERR_NUMERIC, "device error flags " + std::to_string(herr) + " after new data"};
+}
+
+// one-vector interior solve buffers (allocated on first use)
+template <typename T>
+static void ensure_nv(Device& D) {
+  if (D.nv_v0) return;
+  vector<long long> voff(D.nsub);
+  long long nv = 0;
+  for (int t = 0; t < D.nsub; ++t) { voff[t] = nv; nv += D.hs[t].NO; }
+  D.nv_v0 = dalloc<T>(nv, D.owned);
+  D.nv_v1 = dalloc<T>(nv, D.owned);
+  D.nv_r = dalloc<T>(nv, D.owned);
+  D.nv_off = upload(voff, D.owned, D.st);
+}
+
+// the reduced rhs of the current D.fo / D.fi on the device (module_dd.f90:6995-7257):
+// the interior solve replaces the rhs column of X, grep = f_i - A_io X(:, ni)
+template <typename T>
+static void reduced_rhs_device(Device& D) {
+  const int nsub = D.nsub;
+  cudaStream_t st = D.st;
   T* v0 = static_cast<T*>(D.nv_v0);
   T* v1 = static_cast<T*>(D.nv_v1);
   T* rv = static_cast<T*>(D.nv_r);
   T* poolT = static_cast<T*>(D.poolT);
   const dim3 gv((D.maxNO + 127) / 128, nsub);
   const size_t smem = (size_t)(D.maxnbo * NB + 5 * NB) * sizeof(T);
-  CK(cudaFuncSetAttribute(k_band_solve1<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  raise_smem(k_band_solve1<T>, smem);
   auto solve1 = [&](T* x) {
     k_band_solve1<T><<<nsub, NT, smem, st>>>(D.bd_oo, poolT, x, D.nv_off);
     CKL();
@@ -1735,10 +1836,109 @@ static void new_data_impl(Solver& S) {
     k_reduced_rhs_f64<<<dim3((D.maxNI + 127) / 128, nsub), 128, 0, st>>>(D.ds, D.kio, poolT, D.fi, D.grep);
     CKL();
   }
-  int herr = 0;
-  CK(cudaMemcpyAsync(&herr, D.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+}
+
+// ------------------------------------------------------------ three levels
+// The level-1 coarse problem is solved approximately by one BDDC application on
+// level 2 (levels_corsub_standard_level + levels_solve_last_level +
+// levels_add_standard_level, module_levels.f90:3849-4250): interior solves of
+// the level-2 subdomains, the reduced rhs on the level-2 interface, the level-2
+// BDDC preconditioner (with the exact level-3 coarse solve), interior resolve.
+__global__ void k_l2_rhs(int nfo, const int* __restrict__ mo, int nrep, const int* __restrict__ mi,
+                         const double* __restrict__ wi, const double* __restrict__ rc, double* __restrict__ fo,
+                         double* __restrict__ fi) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g < nfo) fo[g] = rc[mo[g]];
+  if (g < nrep) fi[g] = mi[g] >= 0 ? wi[g] * rc[mi[g]] : 0.0;
+}
+
+__global__ void k_l2_out(int nfo, const int* __restrict__ mo, const double* __restrict__ uo, int nz,
+                         const int* __restrict__ mz, const double* __restrict__ z, double* __restrict__ uc) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g < nfo) uc[mo[g]] = uo[g];
+  if (g < nz) uc[mz[g]] = z[g];
+}
+
+static void level2_apply(Device& D1, const double* rc, double* uc) {
+  Solver& S2 = *D1.lev2;
+  Device& D2 = *S2.dev;
+  cudaStream_t st = D1.st;
+  const int n1 = std::max(D2.l2_nfo, D2.nrep);
+  k_l2_rhs<<<(n1 + 255) / 256, 256, 0, st>>>(D2.l2_nfo, D2.l2_mo, D2.nrep, D2.l2_mi, D2.l2_wi, rc, D2.fo, D2.fi);
+  CKL();
+  reduced_rhs_device<double>(D2);
+  k_assemble_plain<<<(D2.n + 255) / 256, 256, 0, st>>>(D2.n, D2.own, D2.grep, nullptr, D2.g);
+  CKL();
+  launch_pc<double>(D2, D2.g, D2.z, nullptr);
+  k_post_f64<<<dim3((D2.maxNO + 7) / 8, D2.nsub), 256, 0, st>>>(D2.ds, static_cast<const double*>(D2.poolT), D2.z,
+                                                                 D2.uniq, D2.uo, D2.uo_off);
+  CKL();
+  const int n2 = std::max(D2.l2_nfo, D2.n);
+  k_l2_out<<<(n2 + 255) / 256, 256, 0, st>>>(D2.l2_nfo, D2.l2_mo, D2.uo, D2.n, D2.l2_mz, D2.z, uc);
+  CKL();
+}
+
+template <typename T>
+static void setup_level2(Solver& S, Device& D) {
+  cudaStream_t st = D.st;
+  const int nsub = D.nsub;
+  // local coarse matrices of the level-1 subdomains
+  long long nsm = 0;
+  for (auto& d : D.hs) nsm = std::max(nsm, d.oAc + (long long)d.ncp * d.ncp);
+  vector<double> hsmall(std::max<long long>(1, nsm));
+  CK(cudaMemcpyAsync(hsmall.data(), D.small, nsm * sizeof(double), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
-  if (herr) throw Error{ERR_NUMERIC, "device error flags " + std::to_string(herr) + " after new data"};
+  vector<vector<double>> acs(nsub);
+  if (D.mixed) {  // Phi^T S Phi with FP64-accurate products: the level-2 element matrices
+    vector<int> all(nsub);
+    std::iota(all.begin(), all.end(), 0);
+    acs = coarse_energies<T>(D, all, nullptr);
+  } else {
+    for (int t = 0; t < nsub; ++t) {
+      const DevSub& d = D.hs[t];
+      acs[t].resize((size_t)d.nc * d.nc);
+      for (int r = 0; r < d.nc; ++r)
+        for (int c = 0; c < d.nc; ++c) acs[t][(size_t)r * d.nc + c] = hsmall[d.oAc + (long long)r * d.ncp + c];
+    }
+  }
+  S.lev2 = host_build_level2(S, acs, S.prm.nsub2);
+  Solver& S2 = *S.lev2;
+  host_setup(S2);
+  Error err{0, ""};
+  S2.dev = device_create_on_stream(&D, err);
+  if (!S2.dev) throw err;
+  // the nested setup keeps this level's transfer and launch counters
+  const double h2d = g_h2d_bytes, d2h = g_d2h_bytes;
+  const long long nl = g_launches;
+  const bool ok = device_setup(S2, err);
+  g_h2d_bytes += h2d;
+  g_d2h_bytes += d2h;
+  g_launches += nl;
+  if (!ok) throw err;
+  Device& D2 = *S2.dev;
+  ensure_nv<double>(D2);
+  long long nfo = 0;
+  for (auto& s2 : S2.subs) nfo += s2.ndofo;
+  D2.l2_nfo = (int)nfo;
+  vector<int> mo(std::max<long long>(1, nfo)), mi(std::max(1, D2.nrep), -1), mz(std::max(1, D2.n), 0);
+  vector<double> wi(std::max(1, D2.nrep), 0.0);
+  for (int t = 0; t < D2.nsub; ++t) {
+    const Subdomain& q = S2.subs[t];
+    const long long fo = D2.huo_off[t];
+    for (int k = 0; k < q.ndofo; ++k) mo[fo + k] = q.isvgvn[q.iovsvn[q.operm[k]]];
+    for (int i = 0; i < q.ndofi; ++i) {
+      const int g = q.isvgvn[q.iivsvn[i]];
+      mi[D2.hs[t].rep + i] = g;
+      wi[D2.hs[t].rep + i] = q.wi[i];
+      mz[q.uniq[i]] = g;
+    }
+  }
+  D2.l2_mo = upload(mo, D2.owned, st);
+  D2.l2_mi = upload(mi, D2.owned, st);
+  D2.l2_mz = upload(mz, D2.owned, st);
+  D2.l2_wi = upload(wi, D2.owned, st);
+  D.lev2 = &S2;
+  CK(cudaStreamSynchronize(st));
 }
 
 bool device_new_data(Solver& S, Error& err) {

@@ -7,7 +7,9 @@
 // elimination and weights.  Everything numeric after that runs on the GPU.
 #pragma once
 
+#include <array>
 #include <cstdint>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -99,6 +101,7 @@ struct Subdomain {
 struct Params {
   int nlevels = 2;
   int nsub = 0;
+  int nsub2 = 1;              // subdomains of level 2 (three levels)
   int numbase = 0;
   int verbose = 0;
   int precision = 1;          // 0 plain FP64, 1 mixed
@@ -187,6 +190,9 @@ struct Solver {
   // last adaptive constraint search: the pairs and their eigenvalues (KMAX per pair)
   AdaptivePairs adaptive_pairs;
   vector<double> adaptive_eigs;
+  // three levels: the level-2 problem (its own host data and device state)
+  std::unique_ptr<Solver> lev2;
+  ~Solver();
 };
 
 // adaptive face constraints, host part (bddc_adaptive.cpp)
@@ -200,6 +206,11 @@ vector<double> host_coarse_null_coefficients(int nc, int ld, const double* ac, i
 void host_load_adaptive(Solver& S, const AdaptivePairs& P, const vector<double>& eig, const vector<double>& cons);
 // global coarse numbering and the constraint rows of every subdomain from its coarse nodes
 void host_constraint_rows(Solver& S);
+
+// three-level BDDC (bddc_levels.cpp): division of the level-1 subdomains and the level-2
+// problem built from the level-1 coarse space; acs[s] = local coarse matrix of s (nc x nc)
+vector<int> host_level_division(const vector<std::array<double, 3>>& centroids, int ndim, int nparts);
+std::unique_ptr<Solver> host_build_level2(const Solver& S1, const vector<vector<double>>& acs, int nsub2);
 
 // host setup (bddc_host.cpp)
 void host_assemble_upper(vector<int>& ia, vector<int>& ja, vector<double>& a);
@@ -220,6 +231,7 @@ void host_reactions(Solver& S);
 
 // device (bddc_device.cu)
 Device* device_create(Error& err);
+Device* device_create_on_stream(Device* parent, Error& err);  // shares the parent's stream
 bool device_release_memory(Error& err);
 bool device_new_data(Solver& S, Error& err);
 bool device_element_gradient(int nelem, int nne, const int* inet, const double* ke0, bool per_element,

@@ -44,7 +44,10 @@ extern "C" {
 
 /* ------------------------------------------------ reference entry points */
 
-/* replaces bddcml_init_c, src/bddcml_interface_c.h:6-7 (module_bddcml.f90:36-101) */
+/* replaces bddcml_init_c, src/bddcml_interface_c.h:6-7 (module_bddcml.f90:36-101).
+ * nl = 2 or 3; with three levels nsublev = {subdomains, level-2 subdomains, 1}
+ * and the level-2 subdomains are formed by recursive coordinate bisection of
+ * the level-1 subdomain centroids (the reference divides with METIS). */
 void bddcml_init_c(int *nl, int *nsublev, int *lnsublev, int *nsub_loc_1, int *comm_init,
                    int *verbose_level, int *numbase, int *just_direct_solve_int);
 

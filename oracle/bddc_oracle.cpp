@@ -229,6 +229,11 @@ struct Oracle {
   vector<int> pair_nadaptive;          // eigenvalues >= tau per pair
   vector<int> face_ncdof;              // constraints per pair face after orthogonalisation
   double adaptivity_est = -1.0;
+  // three levels: the level-2 problem built from this level's coarse space
+  int nlevels = 2, nsub2 = 1;
+  int setup_corner = 1, setup_arith = 1, setup_weights = 0;
+  struct Oracle* lev2 = nullptr;
+  ~Oracle();
   // Krylov recycling (module_krylov.f90:33-43): S-orthonormal search directions V and W = S V
   vector<vector<vector<double>>> rcv, rcw;  // [basis vector][subdomain][interface dof]
   int rc_cap = 0;
@@ -1334,6 +1339,125 @@ static void reduced_rhs(Oracle& oo) {
     for (int s = 0; s < nsub; ++s) o->subs[s].g = g[s];
 }
 
+Oracle::~Oracle() { delete lev2; }
+
+// recursive coordinate bisection of the level-1 subdomain centroids into
+// nparts level-2 subdomains: split along the longest extent, halves by count
+// (ties by subdomain index); stands in for the METIS division of the reference
+static void rcb(vector<int> ids, int nparts, int first, const vector<std::array<double, 3>>& c, int ndim,
+                vector<int>& part) {
+  if (nparts <= 1 || ids.size() <= 1) {
+    for (int id : ids) part[id] = first;
+    return;
+  }
+  int axis = 0;
+  double best = -1.0;
+  for (int a = 0; a < ndim; ++a) {
+    double lo = 1e300, hi = -1e300;
+    for (int id : ids) { lo = std::min(lo, c[id][a]); hi = std::max(hi, c[id][a]); }
+    if (hi - lo > best * (1.0 + 1e-12)) { best = hi - lo; axis = a; }
+  }
+  std::stable_sort(ids.begin(), ids.end(), [&](int x, int y) {
+    return c[x][axis] != c[y][axis] ? c[x][axis] < c[y][axis] : x < y;
+  });
+  const int k1 = nparts / 2;
+  const size_t n1 = ids.size() * (size_t)k1 / (size_t)nparts;
+  rcb(vector<int>(ids.begin(), ids.begin() + n1), k1, first, c, ndim, part);
+  rcb(vector<int>(ids.begin() + n1, ids.end()), nparts - k1, first + k1, c, ndim, part);
+}
+
+extern "C" int oracle_setup(void* h, int use_corner_constraints, int use_arithmetic_constraints, int weights_type);
+
+// the level-2 problem (levels_prepare_standard_level, module_levels.f90:1297-3000):
+// nodes = level-1 coarse nodes (corner: its node, edge / face: mean of the glob's
+// nodes), elements = level-1 subdomains with their coarse matrices Phi^T A Phi
+static void build_level2(Oracle& o) {
+  const int nsub = o.nsub;
+  const int ndim = o.subs[0].ndim;
+  const int ncnode = o.ncorner + o.nedge + o.nface;
+  vector<int> ncd(ncnode, 0), kdc(ncnode, -1);
+  vector<std::array<double, 3>> xc(ncnode, {0.0, 0.0, 0.0}), cent(nsub, {0.0, 0.0, 0.0});
+  for (int s = 0; s < nsub; ++s) {
+    const Sub& S = o.subs[s];
+    for (int i = 0; i < S.nnod; ++i)
+      for (int d = 0; d < ndim; ++d) cent[s][d] += S.xyz[(size_t)d * S.nnod + i] / S.nnod;
+    for (const Cnode& cn : S.cnodes) {
+      if (!cn.used) continue;
+      const int g = cn.global_cnode - 1;
+      if (kdc[g] >= 0) continue;
+      ncd[g] = cn.ncdof;
+      kdc[g] = cn.igcdof[0] - 1;
+      for (int in : cn.insin)
+        for (int d = 0; d < ndim; ++d) xc[g][d] += S.xyz[(size_t)d * S.nnod + S.iin[in]] / (double)cn.insin.size();
+    }
+  }
+  vector<int> part(nsub, 0), ids(nsub);
+  std::iota(ids.begin(), ids.end(), 0);
+  rcb(ids, o.nsub2, 0, cent, ndim, part);
+  Oracle* o2 = new Oracle;
+  o2->nsub = o.nsub2;
+  o2->nthreads = o.nthreads;
+  o2->subs.resize(o.nsub2);
+  o.lev2 = o2;
+  for (int t2 = 0; t2 < o.nsub2; ++t2) {
+    vector<int> elems;
+    for (int s = 0; s < nsub; ++s) if (part[s] == t2) elems.push_back(s);
+    if (elems.empty()) throw std::runtime_error("empty level-2 subdomain");
+    std::map<int, int> loc;
+    for (int s : elems)
+      for (const Cnode& cn : o.subs[s].cnodes) if (cn.used) loc.emplace(cn.global_cnode - 1, 0);
+    int nn = 0, nd = 0;
+    vector<int> kd, isngn, nndf, isvgvn, isegn, inet, nnet, ia, ja;
+    vector<double> xyz, a;
+    for (auto& kv : loc) {
+      kv.second = nn++;
+      isngn.push_back(kv.first);
+      nndf.push_back(ncd[kv.first]);
+      kd.push_back(nd);
+      nd += ncd[kv.first];
+    }
+    isvgvn.resize(nd);
+    xyz.assign((size_t)nn * ndim, 0.0);
+    for (auto& kv : loc) {
+      for (int d = 0; d < ncd[kv.first]; ++d) isvgvn[kd[kv.second] + d] = kdc[kv.first] + d;
+      for (int d = 0; d < ndim; ++d) xyz[(size_t)d * nn + kv.second] = xc[kv.first][d];
+    }
+    for (int s : elems) {
+      const Sub& S = o.subs[s];
+      isegn.push_back(s);
+      vector<int> rowdof;
+      int cnt = 0;
+      for (const Cnode& cn : S.cnodes) {
+        if (!cn.used) continue;
+        const int l = loc.at(cn.global_cnode - 1);
+        inet.push_back(l);
+        ++cnt;
+        for (int d = 0; d < cn.ncdof; ++d) rowdof.push_back(kd[l] + d);
+      }
+      nnet.push_back(cnt);
+      const int nc = (int)rowdof.size();
+      for (int r = 0; r < nc; ++r)
+        for (int c = 0; c < nc; ++c) {
+          const int i = rowdof[r], j = rowdof[c];
+          if (i < j || r == c) {
+            ia.push_back(i);
+            ja.push_back(j);
+            a.push_back(r == c ? S.coarsem[(size_t)r * nc + r]
+                               : 0.5 * (S.coarsem[(size_t)r * nc + c] + S.coarsem[(size_t)c * nc + r]));
+          }
+        }
+    }
+    vector<int> ifix(nd, 0);
+    vector<double> zero(nd, 0.0);
+    if (oracle_upload(o2, t2, (int)elems.size(), nn, nd, ndim, inet.data(), (int)inet.size(), nnet.data(),
+                      nndf.data(), isngn.data(), isvgvn.data(), isegn.data(), xyz.data(), ifix.data(), zero.data(),
+                      zero.data(), 1, zero.data(), 1, (int)a.size(), ia.data(), ja.data(), a.data(), 1, 1) != 0)
+      throw std::runtime_error("level-2 upload: " + o2->err);
+  }
+  if (oracle_setup(o2, o.setup_corner, o.setup_arith, o.setup_weights) != 0)
+    throw std::runtime_error("level-2 setup: " + o2->err);
+}
+
 int oracle_setup(void* h, int use_corner_constraints, int use_arithmetic_constraints, int weights_type) {
   auto* o = static_cast<Oracle*>(h);
   try {
@@ -1473,6 +1597,13 @@ int oracle_setup(void* h, int use_corner_constraints, int use_arithmetic_constra
     // ---- adaptive face constraints (module_levels.f90:2826-2938)
     if (o->adaptive) adaptivity(*o, rho);
     coarse_space(*o);
+    // ---- level 2 of three (module_levels.f90:1297-3000)
+    o->setup_corner = use_corner_constraints;
+    o->setup_arith = use_arithmetic_constraints;
+    o->setup_weights = weights_type;
+    delete o->lev2;
+    o->lev2 = nullptr;
+    if (o->nlevels == 3) build_level2(*o);
     reduced_rhs(*o);
     o->setup_done = true;
   } catch (std::exception& e) {
@@ -1589,6 +1720,47 @@ static void sm_apply(Oracle& o, vector<vector<double>>& x, vector<vector<double>
   comm_exchange_add(o, y);
 }
 
+static void pc_apply(Oracle& o, vector<vector<double>>& r, vector<vector<double>>& z);
+
+// One BDDC application on level 2 for the level-1 coarse residual rc (global
+// coarse dofs, 0-based): interior solves of the level-2 subdomains, reduced rhs
+// on the level-2 interface (rhs given complete: interface values weighted),
+// the level-2 preconditioner, interior resolve (levels_corsub_standard_level,
+// levels_solve_last_level, levels_add_standard_level, module_levels.f90:3849-4250).
+static vector<double> level2_apply(Oracle& o2, const vector<double>& rc) {
+  const int nsub = o2.nsub;
+  vector<vector<double>> g(nsub), z(nsub), f(nsub), solo(nsub);
+  for (int s = 0; s < nsub; ++s) {
+    auto& S = o2.subs[s];
+    f[s].resize(S.ndof);
+    for (int d = 0; d < S.ndof; ++d) f[s][d] = rc[S.isvgvn[d]];
+    for (int i = 0; i < S.ndofi; ++i) f[s][S.iivsvn[i]] *= S.wi[i];
+    solo[s].assign(S.ndofo, 0.0);
+    for (int io = 0; io < S.ndofo; ++io) solo[s][io] = f[s][S.iovsvn[io]];
+    if (S.ndofo > 0) S.a11.solve(solo[s].data());
+    g[s].assign(S.ndofi, 0.0);
+    for (int io = 0; io < S.ndofo; ++io)
+      for (int k = S.a12_ptr[io]; k < S.a12_ptr[io + 1]; ++k) g[s][S.a12_col[k]] += S.a12_val[k] * solo[s][io];
+    for (int i = 0; i < S.ndofi; ++i) g[s][i] = f[s][S.iivsvn[i]] - g[s][i];
+  }
+  comm_exchange_add(o2, g);
+  pc_apply(o2, g, z);
+  vector<double> uc(rc.size(), 0.0);
+  for (int s = 0; s < nsub; ++s) {
+    auto& S = o2.subs[s];
+    vector<double> uo(S.ndofo);
+    for (int io = 0; io < S.ndofo; ++io) {
+      double t = 0.0;
+      for (int k = S.a12_ptr[io]; k < S.a12_ptr[io + 1]; ++k) t += S.a12_val[k] * z[s][S.a12_col[k]];
+      uo[io] = f[s][S.iovsvn[io]] - t;
+    }
+    if (S.ndofo > 0) S.a11.solve(uo.data());
+    for (int io = 0; io < S.ndofo; ++io) uc[S.isvgvn[S.iovsvn[io]]] = uo[io];
+    for (int i = 0; i < S.ndofi; ++i) uc[S.isvgvn[S.iivsvn[i]]] = z[s][i];
+  }
+  return uc;
+}
+
 // z = M r (module_levels.f90:3627-3703, 3707-3846, 4029-4061, 4252-4346)
 static void pc_apply(Oracle& o, vector<vector<double>>& r, vector<vector<double>>& z) {
   int n = o.ndofc;
@@ -1629,7 +1801,10 @@ static void pc_apply(Oracle& o, vector<vector<double>>& r, vector<vector<double>
     auto& S = o.subs[s];
     for (int c = 0; c < S.nconstr; ++c) rc[S.indrowc[c] - 1] += rcs[s][c];
   }
-  if (n > 0) dense_chol_solve(o.coarse_chol, n, rc.data());
+  if (n > 0) {
+    if (o.lev2) rc = level2_apply(*o.lev2, rc);
+    else dense_chol_solve(o.coarse_chol, n, rc.data());
+  }
 #pragma omp parallel for schedule(dynamic) num_threads(o.nthreads)
   for (int s = 0; s < o.nsub; ++s) {
     auto& S = o.subs[s];
@@ -2062,6 +2237,12 @@ int oracle_reactions(void* h, int isub, double* out) {
   }
   std::copy(rea[isub].begin(), rea[isub].end(), out);
   return 0;
+}
+
+void oracle_set_levels(void* h, int nlevels, int nsub2) {
+  auto* o = static_cast<Oracle*>(h);
+  o->nlevels = nlevels;
+  o->nsub2 = nsub2;
 }
 
 int oracle_recycling_size(void* h) { return (int)static_cast<Oracle*>(h)->rcv.size(); }

@@ -55,6 +55,7 @@ def lib():
         L.oracle_new_loads.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
         L.oracle_recycling_size.argtypes = [C.c_void_p]
         L.oracle_reactions.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+        L.oracle_set_levels.argtypes = [C.c_void_p, C.c_int, C.c_int]
         L.oracle_adaptive_info.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
         L.oracle_sym_eig.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
         L.oracle_stats.argtypes = [C.c_void_p, C.c_void_p]
@@ -135,6 +136,10 @@ class Oracle:
         if rc != 0:
             raise RuntimeError(self.L.oracle_error(self.h).decode())
         return it.value, reason.value, cond.value
+
+    def set_levels(self, nlevels=2, nsub2=1):
+        """Three-level BDDC with nsub2 level-2 subdomains at the next setup."""
+        self.L.oracle_set_levels(self.h, nlevels, nsub2)
 
     def reactions(self, isub):
         """Reactions of subdomain isub after a solve (ndofs values)."""
