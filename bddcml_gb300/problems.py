@@ -266,6 +266,24 @@ def random_box_counts(n_el_edge: int, counts, lo_side: int, hi_side: int, seed: 
     return boxes
 
 
+def inclusions_young(n_el_edge: int, volume_fraction: float = 0.1, rmin: float = 3.0, rmax: float = 6.0,
+                     e_matrix: float = 1.0, e_incl: float = 1e3, seed: int = 5) -> np.ndarray:
+    """Per-element Young's modulus: e_matrix with spherical inclusions of
+    e_incl (radius uniform in [rmin, rmax] elements, centres uniform in the
+    cube, drawn from `seed`) added until they hold `volume_fraction` of the
+    elements (element centres inside a sphere).  Elements are numbered x fastest."""
+    rng = np.random.default_rng(seed)
+    n = n_el_edge
+    c = (np.arange(n) + 0.5)
+    z, y, x = np.meshgrid(c, c, c, indexing="ij")
+    inside = np.zeros((n, n, n), dtype=bool)
+    while inside.mean() < volume_fraction:
+        cx, cy, cz = rng.uniform(0, n, size=3)
+        r = rng.uniform(rmin, rmax)
+        inside |= (x - cx) ** 2 + (y - cy) ** 2 + (z - cz) ** 2 <= r * r
+    return np.where(inside.ravel(), e_incl, e_matrix)
+
+
 def uniform_boxes(n_el_edge: int, nsub_edge: int):
     """The nsub_edge^3 equal boxes of the cube (as poisson_on_cube splits it)."""
     cuts = [round(k * n_el_edge / nsub_edge) for k in range(nsub_edge + 1)]

@@ -53,6 +53,10 @@ WORKLOADS = {
     # of sides 8..24 (6 x 5 x 10), rho-scaling, adaptive face constraints tau = 10
     "poisson_96^3_300boxes_channels_adaptive": ("channels", (96, (6, 5, 10)), 1, 10.0),
     "poisson_96^3_300boxes_channels": ("channels", (96, (6, 5, 10)), 1, None),
+    # 96^3 Q1 elasticity (E = 1, nu = 0.3) with 10 % of spherical inclusions of E = 1e3
+    # (radius 3..6, seed 5), clamped at x = 0, body force -z; 512 subdomains, three levels
+    # with 8 level-2 subdomains, rho-scaling; one right-hand side
+    "elasticity_96^3_512subs_3levels": ("elasticity", (12, 8, 8), 1, None),
 }
 DEFAULT_WORKLOAD = "poisson_128^3_512subs"
 
@@ -128,6 +132,9 @@ def make_problem(workload):
     kind, par, _, _ = WORKLOADS[workload]
     if kind == "cube":
         return problems.poisson_on_cube(*par)
+    if kind == "elasticity":
+        nes, nss, _ = par
+        return problems.elasticity_on_cube(nes, nss, nu=0.3, young=problems.inclusions_young(nes * nss))
     ne, counts = par
     kappa = problems.channel_kappa(ne, nchannels=20, width=2, contrast=1e4, sigma=2.0, seed=17)
     return problems.poisson_boxes(ne, problems.random_box_counts(ne, counts, 8, 24, seed=17), kappa=kappa)
@@ -136,9 +143,12 @@ def make_problem(workload):
 def e2e_solve(B, prob, precision, profile=False, workload=DEFAULT_WORKLOAD):
     """The reference-facing sequence through the C ABI with host buffers
     (poisson_on_cube.f90:373-672)."""
-    _, _, weights, tau = WORKLOADS[workload]
+    kind, par, weights, tau = WORKLOADS[workload]
     tp = [time.perf_counter()]
-    B.bddcml_init(2, [prob.nsub, 1], -1, 0, 0, 0, 0)
+    if kind == "elasticity":
+        B.bddcml_init(3, [prob.nsub, par[2], 1], -1, 0, 0, 0, 0)
+    else:
+        B.bddcml_init(2, [prob.nsub, 1], -1, 0, 0, 0, 0)
     B.set_precision(precision)
     if profile:
         B.set_profiling(True)
@@ -267,15 +277,18 @@ def run_gpu(args):
     roof["traffic"] = None
     all_roof = {k: phase_roofline(k, prof_p, st_p, hbm, tensor, peak_kind)
                 for k in ("solve_interior", "precond_solve", "refine_residual", "schur_apply", "precond_local")}
-    _, _, weights, tau = WORKLOADS[args.workload]
-    # the oracle solves the adaptive pair eigenproblems densely: far beyond a bounded sample at this size
-    cpu = None if (args.no_cpu_baseline or tau is not None) else cpu_baseline(prob, weights=weights)
+    kind, _, weights, tau = WORKLOADS[args.workload]
+    # the oracle solves the adaptive pair eigenproblems densely, and takes minutes on the
+    # three-level elasticity: both far beyond a bounded sample
+    cpu = None if (args.no_cpu_baseline or tau is not None or kind == "elasticity") else \
+        cpu_baseline(prob, weights=weights)
     out = {
         "metric": METRIC, "value": dev_mean, "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_mean * 1e3, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 factors / f64 Krylov",
-        "data": "synthetic (deterministic Poisson cube)" if WORKLOADS[args.workload][0] == "cube"
-        else "synthetic (seeded coefficients, channels and box partition)",
+        "data": {"cube": "synthetic (deterministic Poisson cube)",
+                 "channels": "synthetic (seeded coefficients, channels and box partition)",
+                 "elasticity": "synthetic (seeded spherical inclusions)"}[WORKLOADS[args.workload][0]],
         "config": {"workload": args.workload, "elements": prob.nelem, "subdomains": prob.nsub, "dofs": prob.ndof,
                    "precision": "mixed", "tol": 1e-8,
                    "constraints": "corners+edges+faces" + (f" + adaptive faces (tau {tau:g})" if tau else ""),
