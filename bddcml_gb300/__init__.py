@@ -41,7 +41,8 @@ EXPORTS = ["bddcml_init_c", "bddcml_upload_global_data_c", "bddcml_upload_subdom
            "bddcml_get_residual_history_c", "bddcml_get_interface_weights_c", "bddcml_get_coarse_info_c",
            "bddcml_set_profiling_c", "bddcml_get_profile_c", "bddcml_release_device_memory_c",
            "bddcml_dotprod_subdomain_dev_c", "bddcml_element_gradient_dev_c", "bddcml_set_adaptive_threshold_c",
-           "bddcml_get_adaptive_info_c"]
+           "bddcml_get_adaptive_info_c", "bddcml_upload_subdomain_rhs_batch_c", "bddcml_solve_batch_c",
+           "bddcml_download_local_solution_batch_c"]
 
 # phases of bddcml_get_profile_c (CUDA events on the solver stream)
 PHASES = ["numeric_total", "solve_total", "factor_interior", "solve_interior", "refine_residual", "schur",
@@ -228,6 +229,37 @@ def bddcml_change_subdomain_data(isub: int, ifix, fixv, rhs, is_rhs_complete: in
 def bddcml_setup_new_data():
     lib().bddcml_setup_new_data_c()
     _check()
+
+
+def bddcml_upload_subdomain_rhs_batch(isub: int, rhss, is_rhs_complete: int = 1):
+    """Batched loads of one subdomain: rhss is (nrhs, ndof), one load per row
+    (stored column-major as ndof x nrhs for the C call)."""
+    r = np.ascontiguousarray(np.atleast_2d(rhss), dtype=np.float64)
+    nrhs = r.shape[0]
+    lib().bddcml_upload_subdomain_rhs_batch_c(_i(isub), _i(nrhs), r.ctypes.data_as(C.POINTER(C.c_double)),
+                                              _i(r.size), _i(is_rhs_complete))
+    _check()
+
+
+def bddcml_solve_batch(nrhs: int, comm_all=0, method=0, tol=1e-8, maxit=1000, ndecrmax=30):
+    """PCG on the uploaded batch; returns per-column (num_iter, converged_reason, condition_number) arrays."""
+    it = np.zeros(nrhs, dtype=np.int32)
+    reason = np.zeros(nrhs, dtype=np.int32)
+    cond = np.zeros(nrhs)
+    lib().bddcml_solve_batch_c(_i(comm_all), _i(method), _d(tol), _i(maxit), _i(ndecrmax), _i(nrhs),
+                               it.ctypes.data_as(C.POINTER(C.c_int)), reason.ctypes.data_as(C.POINTER(C.c_int)),
+                               cond.ctypes.data_as(C.POINTER(C.c_double)))
+    _check()
+    return it, reason, cond
+
+
+def bddcml_download_local_solution_batch(isub: int, nrhs: int, ndof: int) -> np.ndarray:
+    """Solutions of the last batched solve for one subdomain, shape (nrhs, ndof)."""
+    out = np.zeros((nrhs, ndof))
+    lib().bddcml_download_local_solution_batch_c(_i(isub), _i(nrhs), out.ctypes.data_as(C.POINTER(C.c_double)),
+                                                 _i(out.size))
+    _check()
+    return out
 
 
 def bddcml_finalize():

@@ -26,7 +26,8 @@ SOURCES = [
     ("bddc_gradient.cu", "nvcc"),
 ]
 HEADERS = ["bddc_internal.hpp", "bddc_kernels.cuh", "bddc_df.cuh", "bddc_setup_kernels.cuh",
-           "bddc_pcg_kernels.cuh", "bddc_tc.cuh", "bddc_adaptive.cuh"]
+           "bddc_pcg_kernels.cuh", "bddc_tc.cuh", "bddc_adaptive.cuh", "bddc_batch_kernels.cuh",
+           "bddc_batch.cuh"]
 
 
 def _nvcc() -> str:

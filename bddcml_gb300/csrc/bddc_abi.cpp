@@ -262,6 +262,63 @@ void bddcml_solve_c(int* comm_all, int* method, double* tol, int* maxit, int* nd
   });
 }
 
+// ---------------------------------------------------------- batched loads
+// Extension: nrhs loads of the same set-up problem solved by one batched PCG.
+void bddcml_upload_subdomain_rhs_batch_c(int* isub, int* nrhs, double* rhss, int* lrhss, int* is_rhs_complete) {
+  guarded("bddcml_upload_subdomain_rhs_batch_c", [&] {
+    Solver* S = need_solver("bddcml_upload_subdomain_rhs_batch_c");
+    if (!S) return;
+    int t = sub_index(*S, *isub);
+    Subdomain& s = S->subs[t];
+    if (!s.loaded) throw Error{ERR_ARGUMENT, "the subdomain data must be uploaded first"};
+    if (*nrhs < 1 || *nrhs > 64) throw Error{ERR_ARGUMENT, "nrhs must be between 1 and 64"};
+    if ((long long)*lrhss != (long long)s.ndof * *nrhs) throw Error{ERR_ARGUMENT, "lrhss must be ndof * nrhs"};
+    s.rhs_batch.assign(rhss, rhss + *lrhss);
+    s.nrhs_batch = *nrhs;
+    s.rhs_batch_complete = is_rhs_complete && *is_rhs_complete != 0;
+  });
+}
+
+void bddcml_solve_batch_c(int* comm_all, int* method, double* tol, int* maxit, int* ndecrmax, int* nrhs,
+                          int* num_iter, int* converged_reason, double* condition_number) {
+  guarded("bddcml_solve_batch_c", [&] {
+    (void)comm_all;
+    Solver* S = need_solver("bddcml_solve_batch_c");
+    if (!S) return;
+    if (!S->setup_done) throw Error{ERR_ARGUMENT, "preconditioner is not set up"};
+    if (*method != 0) throw Error{ERR_UNSUPPORTED, "batched right-hand sides are solved by PCG (method 0) only"};
+    if (*maxit < 1) throw Error{ERR_ARGUMENT, "maxit must be positive"};
+    if (*nrhs < 1 || *nrhs > 64) throw Error{ERR_ARGUMENT, "nrhs must be between 1 and 64"};
+    for (auto& s : S->subs)
+      if (s.nrhs_batch != *nrhs)
+        throw Error{ERR_ARGUMENT, "every subdomain needs nrhs right-hand sides from bddcml_upload_subdomain_rhs_batch"};
+    vector<int> it, reason;
+    vector<double> cond;
+    Error err{0, ""};
+    S->batch_solved = 0;
+    if (!device_solve_batch(*S, *nrhs, *tol, *maxit, *ndecrmax, it, reason, cond, err)) throw err;
+    S->batch_solved = *nrhs;
+    for (int k = 0; k < *nrhs; ++k) {
+      num_iter[k] = it[k];
+      converged_reason[k] = reason[k];
+      condition_number[k] = cond[k];
+    }
+  });
+}
+
+void bddcml_download_local_solution_batch_c(int* isub, int* nrhs, double* sols, int* lsols) {
+  guarded("bddcml_download_local_solution_batch_c", [&] {
+    Solver* S = need_solver("bddcml_download_local_solution_batch_c");
+    if (!S) return;
+    if (S->batch_solved == 0 || *nrhs != S->batch_solved)
+      throw Error{ERR_ARGUMENT, "no batched solve with nrhs right-hand sides"};
+    int t = sub_index(*S, *isub);
+    Subdomain& s = S->subs[t];
+    if ((long long)*lsols != (long long)s.ndof * *nrhs) throw Error{ERR_ARGUMENT, "lsols must be ndof * nrhs"};
+    std::copy(s.sol_batch.begin(), s.sol_batch.end(), sols);
+  });
+}
+
 void bddcml_download_local_solution_c(int* isub, double* sols, int* lsols) {
   guarded("bddcml_download_local_solution_c", [&] {
     Solver* S = need_solver("bddcml_download_local_solution_c");

@@ -217,22 +217,7 @@ __global__ void __launch_bounds__(256) k_ad_gemm(const DevSub* __restrict__ ds, 
 }
 
 // The same batched product with S as the float2 pair hi + lo in double-float
-// arithmetic on the FP32 pipes (GB300's FP64 rate is a small fraction of its
-// FP32 rate): the input column is split into x_hi + x_lo, each multiply-add is
-// the exact product a_hi x_hi (a rounded product and its fma error) plus the
-// cross terms a_hi x_lo + a_lo x_hi, accumulated as an unevaluated sum
-// (s_hi, s_lo) with an error-free two-sum.  Accuracy about 2^-44 relative to
-// sum |a x|, FP64-like for these products.
-__device__ __forceinline__ void df_mac(float& sh, float& sl, float ah, float al, float bh, float bl) {
-  const float p = __fmul_rn(ah, bh);
-  const float e = __fmaf_rn(ah, bh, -p);
-  const float c = __fmaf_rn(ah, bl, __fmaf_rn(al, bh, e));
-  const float t = __fadd_rn(sh, p);
-  const float bp = __fsub_rn(t, sh);
-  const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bp)), __fsub_rn(p, bp));
-  sh = t;
-  sl = __fadd_rn(sl, __fadd_rn(err, c));
-}
+// arithmetic on the FP32 pipes (df_mac, bddc_df.cuh).
 
 __global__ void __launch_bounds__(256) k_ad_gemm_df(const DevSub* __restrict__ ds, const float2* __restrict__ Spool,
                                                     ColTab tab, double* __restrict__ va) {

@@ -1,0 +1,417 @@
+// Batched interface PCG: nrhs right-hand sides of one set-up problem solved
+// together (an extension of bddcml_solve; the reference solves one load per
+// call, module_bddcml.f90:505-600).  Every column runs the PCG of
+// module_krylov.f90:545-888 with its own scalars and stop test; the
+// subdomain applies of all columns are GEMMs (bddc_batch_kernels.cuh), so each
+// Schur complement, local preconditioner block and interior-resolve block is
+// read once per iteration for the whole batch.
+//
+// Included by bddc_device.cu after the Device class, whose buffers, setup
+// results and single-column routines (reduced_rhs_device, run_solve) it uses.
+
+namespace bddc {
+
+static unsigned blocks_for(long long cnt, int threads = 256) { return (unsigned)((cnt + threads - 1) / threads); }
+
+template <typename T>
+static void batch_prepare(Device& D, int nk, int lg, int maxit, int* shared_ndone, bool level2) {
+  BatchBufs& B = D.bt;
+  const int ldh = std::max(maxit + 2, 2);
+  if (B.nk == nk && B.ldh >= ldh && (shared_ndone == nullptr || B.ndone == shared_ndone)) return;
+  D.release_batch();
+  auto& mem = B.mem;
+  const long long n = D.n, nrep = D.nrep;
+  long long ncon = 0, nuo = 0, nbb = 0;
+  for (int t = 0; t < D.nsub; ++t) {
+    ncon = std::max(ncon, (long long)D.hs[t].coff + D.hs[t].nc);
+    nuo += D.hs[t].no;
+    nbb += D.hs[t].NO;
+  }
+  const long long nc = std::max(1, D.ndofc), ldc = std::max(1, D.ldc);
+  B.nk = nk;
+  B.lg = lg;
+  B.ldh = ldh;
+  B.x = dalloc<double>(n * nk, mem);
+  B.r = dalloc<double>(n * nk, mem);
+  B.p = dalloc<double>(n * nk, mem);
+  B.ap = dalloc<double>(n * nk, mem);
+  B.z = dalloc<double>(n * nk, mem);
+  B.yrep = dalloc<double>(nrep * nk, mem);
+  B.zrep = dalloc<double>(nrep * nk, mem);
+  B.grep = dalloc<double>(nrep * nk, mem);
+  B.rcs = dalloc<double>(std::max(1LL, ncon) * nk, mem);
+  B.rc = dalloc<double>(nc * nk, mem);
+  B.uc = dalloc<double>(nc * nk, mem);
+  B.cres = dalloc<double>(nc * nk, mem);
+  B.vo = dalloc<double>(std::max(1LL, nuo) * nk, mem);
+  B.part0 = dalloc<double>((long long)D.npart * nk, mem);
+  B.part1 = dalloc<double>((long long)D.npart * nk, mem);
+  B.part2 = dalloc<double>((long long)D.npart * nk, mem);
+  B.aux = dalloc<T>(nrep * nk, mem);
+  B.xs = dalloc<double>(nrep * nk, mem);  // float2 pairs or doubles: 8 bytes an entry either way
+  B.ucs = dalloc<T>(std::max(1LL, ncon) * nk, mem);
+  B.cbt = dalloc<T>(ldc * nk, mem);
+  B.ctl = dalloc<PcgCtl>(nk, mem);
+  B.ndone = shared_ndone ? shared_ndone : dalloc<int>(1, mem);
+  B.hist = dalloc<double>((long long)ldh * nk, mem);
+  B.diag = dalloc<double>((long long)ldh * nk, mem);
+  B.subdiag = dalloc<double>((long long)ldh * nk, mem);
+  if (level2) {
+    B.fi = dalloc<double>(nrep * nk, mem);
+    B.g = dalloc<double>(n * nk, mem);
+    B.bb = dalloc<double>(std::max(1LL, nbb) * BMAX, mem);
+    vector<long long> ro(D.nsub);
+    vector<BandDesc> bd(D.nsub);
+    long long o = 0;
+    for (int t = 0; t < D.nsub; ++t) {
+      ro[t] = o;
+      bd[t] = D.hbd_oo[t];
+      bd[t].ncol = BMAX;
+      bd[t].oB = o * BMAX;
+      o += D.hs[t].NO;
+    }
+    B.rowoff = upload(ro, mem, D.st);
+    B.bdB = upload(bd, mem, D.st);
+  }
+  // GEMM descriptors: Schur operator, [Z | Phi] with the coarse solution, interior resolve, coarse inverse
+  vector<GemmDesc> gs(D.nsub), gz(D.nsub), gx(D.nsub);
+  vector<long long> ro(D.nsub, 0);
+  {
+    long long o = 0;
+    for (int t = 0; t < D.nsub; ++t) { ro[t] = o; o += D.hs[t].NO; }
+  }
+  for (int t = 0; t < D.nsub; ++t) {
+    const DevSub& d = D.hs[t];
+    gs[t] = GemmDesc{d.oS, 0, d.rep, 0, d.rep, d.ni, d.ni, 0, d.NI, 0, 0};
+    gz[t] = GemmDesc{d.oZ, d.oPhi, d.rep, d.coff, d.rep, d.ni, d.ni, D.ndofc > 0 ? d.nc : 0, d.NI, d.ncp, 0};
+    gx[t] = GemmDesc{d.oXc, d.oXc + (long long)d.NO * d.NR, d.rep, 0, level2 ? ro[t] : D.huo_off[t],
+                     d.no, d.ni, 0, d.NR, 0, 0};
+  }
+  vector<GemmDesc> gc(1, GemmDesc{0, 0, 0, 0, 0, D.ndofc, D.ndofc, 0, D.ldc, 0, 0});
+  B.gS = upload(gs, mem, D.st);
+  B.gZ = upload(gz, mem, D.st);
+  B.gX = upload(gx, mem, D.st);
+  B.gC = upload(gc, mem, D.st);
+}
+
+// vout = sum_s R_s^T S_s R_s vin for every column; partial (dotvec, vout)_w into part
+template <typename T>
+static void batch_schur(Device& D, const double* vin, double* vout, bool zero_fixed, const double* dotvec,
+                        double* part) {
+  BatchBufs& B = D.bt;
+  cudaStream_t st = D.st;
+  const long long cnt = (long long)D.nrep << B.lg;
+  const dim3 grid((D.maxNI + GM - 1) / GM, D.nsub);
+  D.prof.begin(PH_SCHUR_APPLY, st);
+  if (D.mixed) {
+    kb_gather_df<<<blocks_for(cnt), 256, 0, st>>>(D.nrep, B.lg, D.uniq, 1.0, vin, static_cast<float2*>(B.xs), B.ndone);
+    CKL();
+    kb_gemm_df<false><<<grid, 256, 0, st>>>(B.gS, static_cast<const float*>(D.poolS),
+                                            static_cast<const float2*>(B.xs), B.nk, B.yrep, nullptr, B.nk, B.nk,
+                                            B.ndone);
+    CKL();
+  } else {
+    kb_gather_t<double><<<blocks_for(cnt), 256, 0, st>>>(D.nrep, B.lg, D.uniq, nullptr, 1.0, vin,
+                                                         static_cast<double*>(B.xs), B.ndone);
+    CKL();
+    kb_gemm_t<double><<<grid, 256, 0, st>>>(B.gS, static_cast<const double*>(D.poolS),
+                                            static_cast<const double*>(B.xs), nullptr, B.nk, B.yrep, nullptr, B.nk,
+                                            B.nk, B.ndone);
+    CKL();
+  }
+  D.prof.end(PH_SCHUR_APPLY, st);
+  kb_assemble_dot<<<D.npart, RT, 0, st>>>(D.n, B.lg, D.own, B.yrep, D.fixed, D.wsum, dotvec, vout, part, D.npart,
+                                          zero_fixed ? 1 : 0, B.ndone);
+  CKL();
+}
+
+static void batch_level2(Device& D1, const double* rc, double* uc);
+
+// zout = BDDC preconditioner applied to every column of rin; partial (rin, zout)_w into part
+template <typename T>
+static void batch_pc(Device& D, const double* rin, double* zout, double* part) {
+  BatchBufs& B = D.bt;
+  cudaStream_t st = D.st;
+  const int nk = B.nk, lg = B.lg;
+  const T* pc = static_cast<const T*>(D.poolPC);
+  T* aux = static_cast<T*>(B.aux);
+  T* ucs = static_cast<T*>(B.ucs);
+  D.prof.begin(PH_PC_LOCAL, st);
+  kb_gather_t<T><<<blocks_for((long long)D.nrep << lg), 256, 0, st>>>(D.nrep, lg, D.uniq, D.wrep, 1.0, rin, aux,
+                                                                      B.ndone);
+  CKL();
+  if (D.ndofc > 0) {
+    kb_phit<T><<<dim3(D.nsub, (D.ncpmax + 31) / 32), 256, 0, st>>>(D.ds, pc, aux, lg, B.rcs, B.ndone);
+    CKL();
+    kb_coarse_gather<<<blocks_for((long long)D.ndofc << lg), 256, 0, st>>>(D.ndofc, lg, D.co_ptr, D.co_sub,
+                                                                           D.co_loc, D.ds, B.rcs, B.rc, B.ndone);
+    CKL();
+    if (D.lev2) {
+      batch_level2(D, B.rc, B.uc);
+    } else {
+      // explicit coarse inverse with two FP64 refinement steps, as in the single-column path
+      const T* minv = static_cast<const T*>(D.cinv);
+      T* cb = static_cast<T*>(B.cbt);
+      const long long cc = (long long)D.ndofc << lg;
+      const dim3 gc((D.ndofc + GM - 1) / GM, 1);
+      kb_to_t<T><<<blocks_for(cc), 256, 0, st>>>(cc, B.rc, cb, nk, B.ndone);
+      CKL();
+      kb_gemm_t<T><<<gc, 256, 0, st>>>(B.gC, minv, cb, nullptr, nk, B.uc, nullptr, nk, nk, B.ndone);
+      CKL();
+      for (int rr = 0; rr < 2; ++rr) {
+        kb_coarse_res<<<blocks_for(cc), 256, 0, st>>>(D.ndofc, lg, D.ac_ptr, D.ac_col, D.ac_val, B.rc, B.uc, B.cres,
+                                                      B.ndone);
+        CKL();
+        kb_to_t<T><<<blocks_for(cc), 256, 0, st>>>(cc, B.cres, cb, nk, B.ndone);
+        CKL();
+        kb_gemm_t<T><<<gc, 256, 0, st>>>(B.gC, minv, cb, nullptr, nk, B.uc, B.uc, nk, nk, B.ndone);
+        CKL();
+      }
+    }
+    long long ncon = 0;
+    for (auto& d : D.hs) ncon = std::max(ncon, (long long)d.coff + d.nc);
+    kb_gather_uc<T><<<blocks_for(ncon << lg), 256, 0, st>>>(ncon, lg, D.cmap, B.uc, ucs, B.ndone);
+    CKL();
+  }
+  // zrep = Z_s aux_s + Phi_s uc_s in one product per subdomain
+  kb_gemm_t<T><<<dim3((D.maxNI + GM - 1) / GM, D.nsub), 256, 0, st>>>(B.gZ, pc, aux, ucs, nk, B.zrep, nullptr, nk,
+                                                                      nk, B.ndone);
+  CKL();
+  D.prof.end(PH_PC_LOCAL, st);
+  kb_assemble_z<<<D.npart, RT, 0, st>>>(D.n, lg, D.own, B.zrep, D.wrep, D.wsum, rin, zout, part, D.npart, B.ndone);
+  CKL();
+}
+
+// The level-1 coarse correction by one level-2 BDDC application per column
+// (the batched form of level2_apply): interior solves of the level-2
+// subdomains as a multi-column band solve, reduced rhs, level-2
+// preconditioner with the exact level-3 coarse solve, interior resolve.
+static void batch_level2(Device& D1, const double* rc, double* uc) {
+  Device& D2 = *D1.lev2->dev;
+  BatchBufs& B = D2.bt;
+  cudaStream_t st = D1.st;
+  const int nk = B.nk, lg = B.lg;
+  kb_l2_fill<<<dim3(blocks_for((long long)D2.maxNO * BMAX), D2.nsub), 256, 0, st>>>(
+      D2.ds, lg, B.rowoff, D2.uo_off, D2.l2_mo, rc, B.bb, B.ndone);
+  CKL();
+  kb_l2_fi<<<blocks_for((long long)D2.nrep << lg), 256, 0, st>>>(D2.nrep, lg, D2.l2_mi, D2.l2_wi, rc, B.fi, B.ndone);
+  CKL();
+  run_solve<double>(D2, B.bdB, D2.nsub, D2.maxnbo, BMAX, static_cast<const double*>(D2.poolT), B.bb);
+  kb_reduced_rhs<<<dim3(blocks_for((long long)D2.maxNI << lg), D2.nsub), 256, 0, st>>>(D2.ds, D2.kio, lg, B.rowoff,
+                                                                                       B.bb, B.fi, B.grep, B.ndone);
+  CKL();
+  kb_assemble_dot<<<D2.npart, RT, 0, st>>>(D2.n, lg, D2.own, B.grep, nullptr, nullptr, nullptr, B.g, nullptr,
+                                           D2.npart, 0, B.ndone);
+  CKL();
+  batch_pc<double>(D2, B.g, B.z, nullptr);
+  // interior resolve u_o = v - X z, in place in the band block
+  kb_gather_t<double><<<blocks_for((long long)D2.nrep << lg), 256, 0, st>>>(D2.nrep, lg, D2.uniq, nullptr, -1.0, B.z,
+                                                                            static_cast<double*>(B.xs), B.ndone);
+  CKL();
+  kb_gemm_t<double><<<dim3((D2.maxNO + GM - 1) / GM, D2.nsub), 256, 0, st>>>(
+      B.gX, static_cast<const double*>(D2.poolT), static_cast<const double*>(B.xs), nullptr, nk, B.bb, B.bb, BMAX, nk,
+      B.ndone);
+  CKL();
+  kb_l2_out_o<<<dim3(blocks_for((long long)D2.maxNO << lg), D2.nsub), 256, 0, st>>>(D2.ds, lg, B.rowoff, D2.uo_off,
+                                                                                   D2.l2_mo, B.bb, uc, B.ndone);
+  CKL();
+  kb_l2_out_i<<<blocks_for((long long)D2.n << lg), 256, 0, st>>>(D2.n, lg, D2.l2_mz, B.z, uc, B.ndone);
+  CKL();
+}
+
+template <typename T>
+static void new_data_impl(Solver& S);
+
+template <typename T>
+static void batch_solve_impl(Solver& S, int nrhs, double tol, int maxit, int ndecrmax, vector<int>& num_iter,
+                             vector<int>& reason, vector<double>& cond) {
+  Device& D = *S.dev;
+  cudaStream_t st = D.st;
+  const double t0 = wall_time();
+  int nk = 1, lg = 0;
+  while (nk < nrhs) { nk <<= 1; ++lg; }
+  batch_prepare<T>(D, nk, lg, maxit, nullptr, false);
+  if (D.lev2) batch_prepare<double>(*D.lev2->dev, nk, lg, 0, D.bt.ndone, true);
+  BatchBufs& B = D.bt;
+  const long long n = D.n, nrep = D.nrep;
+  long long nfo = 0;
+  for (auto& s : S.subs) nfo += s.ndofo;
+  // per-column reduced rhs g_k = f_i - A_io A_oo^-1 f_o and interior solutions
+  // A_oo^-1 f_o (module_dd.f90:6995-7257), one column at a time with the
+  // single-column interior solves and their refinement
+  ensure_nv<T>(D);
+  vector<double> hfo((size_t)std::max(1LL, nfo) * nrhs), hfi((size_t)std::max(1LL, nrep) * nrhs, 0.0);
+  {
+    vector<long long> fooff(D.nsub);
+    long long o = 0;
+    for (int t = 0; t < D.nsub; ++t) { fooff[t] = o; o += S.subs[t].ndofo; }
+#pragma omp parallel for schedule(dynamic)
+    for (int t = 0; t < D.nsub; ++t) {
+      const Subdomain& s = S.subs[t];
+      vector<double> fo, fi;
+      for (int k = 0; k < nrhs; ++k) {
+        host_reduced_rhs_inputs(s, s.rhs_batch.data() + (size_t)k * s.ndof, s.rhs_batch_complete, fo, fi);
+        std::copy(fo.begin(), fo.end(), hfo.begin() + (size_t)k * std::max(1LL, nfo) + fooff[t]);
+        std::copy(fi.begin(), fi.end(), hfi.begin() + (size_t)k * std::max(1LL, nrep) + D.hs[t].rep);
+      }
+    }
+  }
+  vector<void*> tmp;
+  double* dfo = dalloc<double>((long long)hfo.size(), tmp);
+  double* dfi = dalloc<double>((long long)hfi.size(), tmp);
+  CK(cudaMemcpyAsync(dfo, hfo.data(), hfo.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(dfi, hfi.data(), hfi.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+  g_h2d_bytes += (double)(hfo.size() + hfi.size()) * sizeof(double);
+  long long launches0 = g_launches;
+  D.prof.begin(PH_SOLVE_TOTAL, st, true);
+  CK(cudaMemsetAsync(B.grep, 0, (size_t)nrep * nk * sizeof(double), st));
+  CK(cudaMemsetAsync(B.vo, 0, (size_t)std::max(1LL, nfo) * nk * sizeof(double), st));
+  double* fo_keep = D.fo;
+  double* fi_keep = D.fi;
+  for (int k = 0; k < nrhs; ++k) {
+    D.fo = dfo + (size_t)k * std::max(1LL, nfo);
+    D.fi = dfi + (size_t)k * std::max(1LL, nrep);
+    reduced_rhs_device<T>(D);
+    kb_put_col<<<blocks_for(nrep), 256, 0, st>>>(nrep, lg, k, D.grep, B.grep);
+    CKL();
+    kb_put_vo<T><<<dim3((D.maxNO + 127) / 128, D.nsub), 128, 0, st>>>(
+        D.ds, lg, k, static_cast<const T*>(D.nv_v0), std::is_same_v<T, float> ? static_cast<const T*>(D.nv_v1) : nullptr,
+        D.nv_off, D.uo_off, B.vo);
+    CKL();
+  }
+  D.fo = fo_keep;
+  D.fi = fi_keep;
+  // initial guess: the fixed values at fixed interface dofs, zero elsewhere
+  bool x0_nonzero = false;
+  {
+    vector<double> x0(n, 0.0);
+    for (auto& s : S.subs)
+      for (int i = 0; i < s.ndofi; ++i) {
+        const int d = s.iivsvn[i];
+        if (s.bc_present && s.ifix[d] && s.fixv[d] != 0.0) {
+          x0[s.uniq[i]] = s.fixv[d];
+          x0_nonzero = true;
+        }
+      }
+    double* dx0 = dalloc<double>(n, tmp);
+    CK(cudaMemcpyAsync(dx0, x0.data(), n * sizeof(double), cudaMemcpyHostToDevice, st));
+    g_h2d_bytes += (double)n * sizeof(double);
+    kb_bcast<<<blocks_for(n << lg), 256, 0, st>>>((int)n, lg, dx0, B.x);
+    CKL();
+  }
+  CK(cudaMemsetAsync(B.ndone, 0, sizeof(int), st));
+  CK(cudaMemsetAsync(B.diag, 0, (size_t)B.ldh * nk * sizeof(double), st));
+  CK(cudaMemsetAsync(B.subdiag, 0, (size_t)B.ldh * nk * sizeof(double), st));
+  // r = g (zero at fixed dofs); (g, g); r -= S x0; (r, r); p = M r; (r, p)
+  kb_assemble_dot<<<D.npart, RT, 0, st>>>((int)n, lg, D.own, B.grep, D.fixed, D.wsum, nullptr, B.r, nullptr, D.npart,
+                                          1, nullptr);
+  CKL();
+  kb_dot<<<D.npart, RT, 0, st>>>((int)n, lg, B.r, B.r, D.wsum, B.part0, D.npart);
+  CKL();
+  if (x0_nonzero) {
+    batch_schur<T>(D, B.x, B.ap, true, nullptr, nullptr);
+    kb_axpy<<<blocks_for(n << lg), 256, 0, st>>>(n << lg, -1.0, B.ap, B.r);
+    CKL();
+  }
+  kb_dot<<<D.npart, RT, 0, st>>>((int)n, lg, B.r, B.r, D.wsum, B.part1, D.npart);
+  CKL();
+  batch_pc<T>(D, B.r, B.p, B.part2);
+  kb_init<<<nk, RT, 0, st>>>(B.ctl, B.part0, B.part1, B.part2, D.npart, tol, maxit, ndecrmax, nrhs, B.ndone);
+  CKL();
+  const double tl = wall_time();
+  D.prof.begin(PH_PCG, st);
+  const int chunk = 2;
+  int launched = 0, hdone = 0;
+  CK(cudaMemcpyAsync(&hdone, B.ndone, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  while (hdone < nk) {
+    for (int q = 0; q < chunk; ++q) {
+      batch_schur<T>(D, B.p, B.ap, false, B.p, B.part0);
+      kb_sc_alpha<<<nk, RT, 0, st>>>(B.ctl, B.part0, D.npart);
+      CKL();
+      kb_update_xr<<<D.npart, RT, 0, st>>>((int)n, lg, B.ctl, B.x, B.r, B.p, B.ap, D.wsum, B.part0, D.npart);
+      CKL();
+      kb_sc_res<<<nk, RT, 0, st>>>(B.ctl, B.part0, D.npart, B.hist, B.ldh, B.ndone);
+      CKL();
+      batch_pc<T>(D, B.r, B.z, B.part0);
+      kb_sc_beta<<<nk, RT, 0, st>>>(B.ctl, B.part0, D.npart, B.diag, B.subdiag, B.ldh);
+      CKL();
+      kb_update_p<<<blocks_for(n << lg), 256, 0, st>>>((int)n, lg, B.ctl, B.p, B.z);
+      CKL();
+    }
+    launched += chunk;
+    CK(cudaMemcpyAsync(&hdone, B.ndone, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (launched > maxit + chunk) break;
+  }
+  D.prof.end(PH_PCG, st);
+  S.stats.t_iterations = wall_time() - tl;
+  // interior values u_o = A_oo^-1 f_o - X x for every column (module_dd.f90:6811-6932)
+  D.prof.begin(PH_POST, st);
+  const dim3 gpost((D.maxNO + GM - 1) / GM, D.nsub);
+  if (D.mixed) {
+    kb_gather_df<<<blocks_for(nrep << lg), 256, 0, st>>>(nrep, lg, D.uniq, -1.0, B.x, static_cast<float2*>(B.xs),
+                                                         nullptr);
+    CKL();
+    kb_gemm_df<true><<<gpost, 256, 0, st>>>(B.gX, static_cast<const float*>(D.poolT),
+                                            static_cast<const float2*>(B.xs), nk, B.vo, B.vo, nk, nk, nullptr);
+    CKL();
+  } else {
+    kb_gather_t<double><<<blocks_for(nrep << lg), 256, 0, st>>>(nrep, lg, D.uniq, nullptr, -1.0, B.x,
+                                                                static_cast<double*>(B.xs), nullptr);
+    CKL();
+    kb_gemm_t<double><<<gpost, 256, 0, st>>>(B.gX, static_cast<const double*>(D.poolT),
+                                             static_cast<const double*>(B.xs), nullptr, nk, B.vo, B.vo, nk, nk,
+                                             nullptr);
+    CKL();
+  }
+  D.prof.end(PH_POST, st);
+  vector<double> hx((size_t)n * nk), hvo((size_t)std::max(1LL, nfo) * nk);
+  vector<PcgCtl> hc(nk);
+  vector<double> hdg((size_t)B.ldh * nk), hsd((size_t)B.ldh * nk);
+  CK(cudaMemcpyAsync(hx.data(), B.x, hx.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(hvo.data(), B.vo, hvo.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(hc.data(), B.ctl, nk * sizeof(PcgCtl), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(hdg.data(), B.diag, hdg.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(hsd.data(), B.subdiag, hsd.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+  g_d2h_bytes += (double)(hx.size() + hvo.size()) * sizeof(double);
+  CK(cudaStreamSynchronize(st));
+  D.prof.end(PH_SOLVE_TOTAL, st);
+  for (void* q : tmp) cudaFreeAsync(q, st);
+  const long long launches = g_launches - launches0;
+  num_iter.assign(nrhs, 0);
+  reason.assign(nrhs, 0);
+  cond.assign(nrhs, 1.0);
+  int maxiter = 0;
+  for (int k = 0; k < nrhs; ++k) {
+    const PcgCtl& c = hc[k];
+    num_iter[k] = c.done ? c.num_iter : maxit;
+    reason[k] = c.done ? c.reason : -1;
+    maxiter = std::max(maxiter, num_iter[k]);
+    const int nw = c.nw;
+    if (nw > 1) {
+      vector<double> dg(hdg.begin() + (size_t)k * B.ldh, hdg.begin() + (size_t)k * B.ldh + nw);
+      vector<double> sd(hsd.begin() + (size_t)k * B.ldh, hsd.begin() + (size_t)k * B.ldh + nw - 1);
+      cond[k] = lanczos_max_eig(dg, sd);
+    }
+  }
+  for (int t = 0; t < D.nsub; ++t) {
+    Subdomain& s = S.subs[t];
+    s.sol_batch.assign((size_t)s.ndof * nrhs, 0.0);
+    for (int k = 0; k < nrhs; ++k) {
+      double* u = s.sol_batch.data() + (size_t)k * s.ndof;
+      for (int q = 0; q < s.ndofo; ++q) u[s.iovsvn[s.operm[q]]] = hvo[((size_t)D.huo_off[t] + q) * nk + k];
+      for (int i = 0; i < s.ndofi; ++i) u[s.iivsvn[i]] = hx[(size_t)s.uniq[i] * nk + k];
+    }
+  }
+  D.prof.collect();
+  // the single-column state (reduced rhs of the subdomains' own loads) for later solves
+  new_data_impl<T>(S);
+  S.stats.h2d_bytes = g_h2d_bytes;
+  S.stats.d2h_bytes = g_d2h_bytes;
+  S.stats.t_solve = wall_time() - t0;
+  S.stats.num_iter = maxiter;
+  S.stats.launches_solve = (double)launches;
+}
+
+}  // namespace bddc

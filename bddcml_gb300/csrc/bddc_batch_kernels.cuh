@@ -1,0 +1,626 @@
+// Kernels of the batched interface PCG: nk right-hand sides of one assembled
+// problem advanced together, each with its own PCG recurrence (scalars, stop
+// test, Lanczos coefficients), so that every column follows the iteration of
+// krylov_bddcpcg (module_krylov.f90:545-888) for its own load.
+//
+// Layout: every batched vector is dof-major with the columns interleaved,
+// v[g * nk + k], nk a power of two <= 64.  A gather of one interface dof then
+// moves all columns in one coalesced segment, and the per-subdomain applies
+// (Schur operator, local preconditioner with the coarse correction, interior
+// resolve) become GEMMs that read each subdomain matrix once per iteration for
+// all columns instead of once per column.
+#pragma once
+
+#include "bddc_pcg_kernels.cuh"
+
+namespace bddc {
+
+constexpr int BMAX = 64;  // columns per batch: one GEMM column tile
+constexpr int GM = 64;    // GEMM rows per CTA
+constexpr int GK = 32;    // GEMM K chunk
+
+// One product of a batched GEMM:  out = addend + A1 B1 + A2 B2  (rows m).
+// A1 is m x k1 (row stride lda), A2 m x k2 (row stride lda2, optional);
+// B1 / B2 are row blocks of the B buffers starting at rows ob / ob2; the
+// result rows start at oo.  For double-float planes oA2 is the low plane.
+struct GemmDesc {
+  long long oA, oA2;
+  long long ob, ob2;
+  long long oo;
+  int m, k1, k2, lda, lda2, pad;
+};
+
+__device__ __forceinline__ bool batch_all_done(const int* ndone, int nk) { return ndone && *ndone >= nk; }
+
+// --------------------------------------------------------------- gathers
+// b[j][k] = split(sign * x[uniq[j]][k]) for replicated interface index j
+__global__ void kb_gather_df(long long nrep, int lg, const int* __restrict__ uniq, double sign,
+                             const double* __restrict__ x, float2* __restrict__ b, const int* __restrict__ ndone) {
+  const int nk = 1 << lg;
+  if (batch_all_done(ndone, nk)) return;
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (nrep << lg)) return;
+  const long long j = e >> lg;
+  const int k = (int)(e & (nk - 1));
+  const dfloat v = df_from_double(sign * x[((long long)uniq[j] << lg) + k]);
+  b[e] = make_float2(v.hi, v.lo);
+}
+
+// b[j][k] = T(sign * w[j] * x[uniq[j]][k])  (w optional)
+template <typename T>
+__global__ void kb_gather_t(long long nrep, int lg, const int* __restrict__ uniq, const double* __restrict__ w,
+                            double sign, const double* __restrict__ x, T* __restrict__ b,
+                            const int* __restrict__ ndone) {
+  const int nk = 1 << lg;
+  if (batch_all_done(ndone, nk)) return;
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (nrep << lg)) return;
+  const long long j = e >> lg;
+  const int k = (int)(e & (nk - 1));
+  double v = sign * x[((long long)uniq[j] << lg) + k];
+  if (w) v *= w[j];
+  b[e] = T(v);
+}
+
+// ---------------------------------------------------------------- GEMMs
+// Double-float product with FP64-class accuracy on the FP32 pipes (A stored as
+// (hi, lo) pairs, interleaved float2 or two planes; B pre-split float2):
+//   out[oo + r][c] = addend + sum_j A[r][j] B[ob + j][c],   c < nk.
+// 256 threads, 64 x 64 output tile, each thread rows ty + 16 i, columns
+// tx + 16 j (conflict-free shared-memory reads).
+template <bool PLANES>
+__global__ void __launch_bounds__(256) kb_gemm_df(const GemmDesc* __restrict__ gd, const float* __restrict__ A,
+                                                  const float2* __restrict__ B, int ldb, double* out,
+                                                  const double* addend, int ldo, int nk,
+                                                  const int* __restrict__ ndone) {
+  if (batch_all_done(ndone, nk)) return;
+  const GemmDesc d = gd[blockIdx.y];
+  const int r0 = blockIdx.x * GM;
+  if (r0 >= d.m) return;
+  __shared__ float Ah[GK][GM + 1], Al[GK][GM + 1], Bh[GK][BMAX], Bl[GK][BMAX];
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  float sh[4][4], sl[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) { sh[i][j] = 0.f; sl[i][j] = 0.f; }
+  for (int k0 = 0; k0 < d.k1; k0 += GK) {
+    if (!PLANES) {  // float2 pairs, two consecutive columns per 16-byte load
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int e = tid + 256 * i;
+        const int row = e >> 4, m2 = e & 15;
+        const int gr = r0 + row, gk = k0 + 2 * m2;
+        float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (gr < d.m && gk < d.k1) {
+          a = __ldg(reinterpret_cast<const float4*>(A + 2 * (d.oA + (long long)gr * d.lda + gk)));
+          if (gk + 1 >= d.k1) { a.z = 0.f; a.w = 0.f; }
+        }
+        Ah[2 * m2][row] = a.x;
+        Al[2 * m2][row] = a.y;
+        Ah[2 * m2 + 1][row] = a.z;
+        Al[2 * m2 + 1][row] = a.w;
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int e = tid + 256 * i;
+        const int row = e >> 5, kk = e & 31;
+        const int gr = r0 + row, gk = k0 + kk;
+        float h = 0.f, l = 0.f;
+        if (gr < d.m && gk < d.k1) {
+          const long long o = (long long)gr * d.lda + gk;
+          h = __ldg(A + d.oA + o);
+          l = __ldg(A + d.oA2 + o);
+        }
+        Ah[kk][row] = h;
+        Al[kk][row] = l;
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int e = tid + 256 * i;
+      const int kk = e >> 6, c = e & 63;
+      const int gk = k0 + kk;
+      float2 b = make_float2(0.f, 0.f);
+      if (gk < d.k1 && c < nk) b = B[(d.ob + gk) * ldb + c];
+      Bh[kk][c] = b.x;
+      Bl[kk][c] = b.y;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int kk = 0; kk < GK; ++kk) {
+      float ah[4], al[4], bh[4], bl[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) { ah[i] = Ah[kk][ty + 16 * i]; al[i] = Al[kk][ty + 16 * i]; }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) { bh[j] = Bh[kk][tx + 16 * j]; bl[j] = Bl[kk][tx + 16 * j]; }
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) df_mac(sh[i][j], sl[i][j], ah[i], al[i], bh[j], bl[j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int gr = r0 + ty + 16 * i;
+    if (gr >= d.m) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int c = tx + 16 * j;
+      if (c >= nk) continue;
+      const long long o = (d.oo + gr) * ldo + c;
+      const double v = (double)sh[i][j] + (double)sl[i][j];
+      out[o] = addend ? addend[o] + v : v;
+    }
+  }
+}
+
+// Product in the working precision T with T accumulation, two K segments:
+//   out[oo + r][c] = addend + sum_j A1[r][j] B1[ob + j][c] + sum_j A2[r][j] B2[ob2 + j][c]
+template <typename T>
+__global__ void __launch_bounds__(256) kb_gemm_t(const GemmDesc* __restrict__ gd, const T* __restrict__ A,
+                                                 const T* __restrict__ B1, const T* __restrict__ B2, int ldb,
+                                                 double* out, const double* addend, int ldo, int nk,
+                                                 const int* __restrict__ ndone) {
+  if (batch_all_done(ndone, nk)) return;
+  const GemmDesc d = gd[blockIdx.y];
+  const int r0 = blockIdx.x * GM;
+  if (r0 >= d.m) return;
+  __shared__ T As[GK][GM + 1], Bs[GK][BMAX];
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  T acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
+  const int kt = d.k1 + d.k2;
+  for (int k0 = 0; k0 < kt; k0 += GK) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int e = tid + 256 * i;
+      const int row = e >> 5, kk = e & 31;
+      const int gr = r0 + row, gk = k0 + kk;
+      T a = T(0);
+      if (gr < d.m) {
+        if (gk < d.k1) a = __ldg(A + d.oA + (long long)gr * d.lda + gk);
+        else if (gk < kt) a = __ldg(A + d.oA2 + (long long)gr * d.lda2 + (gk - d.k1));
+      }
+      As[kk][row] = a;
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int e = tid + 256 * i;
+      const int kk = e >> 6, c = e & 63;
+      const int gk = k0 + kk;
+      T b = T(0);
+      if (c < nk) {
+        if (gk < d.k1) b = B1[(d.ob + gk) * ldb + c];
+        else if (gk < kt) b = B2[(d.ob2 + gk - d.k1) * ldb + c];
+      }
+      Bs[kk][c] = b;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int kk = 0; kk < GK; ++kk) {
+      T a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] += a[i] * b[j];
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int gr = r0 + ty + 16 * i;
+    if (gr >= d.m) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int c = tx + 16 * j;
+      if (c >= nk) continue;
+      const long long o = (d.oo + gr) * ldo + c;
+      const double v = (double)acc[i][j];
+      out[o] = addend ? addend[o] + v : v;
+    }
+  }
+}
+
+// ------------------------------------------------- preconditioner pieces
+// coarse residual of each subdomain, rcs[coff + c][k] = sum_i Phi[i][c] aux[rep + i][k]
+// (dd_phisi_dual_apply, module_dd.f90:6126-6206); grid (nsub, ceil(ncpmax / 32))
+template <typename T>
+__global__ void __launch_bounds__(256) kb_phit(const DevSub* __restrict__ ds, const T* __restrict__ pcpool,
+                                               const T* __restrict__ aux, int lg, double* __restrict__ rcs,
+                                               const int* __restrict__ ndone) {
+  const int nk = 1 << lg;
+  if (batch_all_done(ndone, nk)) return;
+  const DevSub s = ds[blockIdx.x];
+  const int c0 = blockIdx.y * 32;
+  if (c0 >= s.nc) return;
+  __shared__ T as[32][BMAX];
+  __shared__ T ps[32][33];
+  const int tid = threadIdx.x, k = tid & (nk - 1), cl = tid >> lg, ncl = 256 >> lg;
+  T acc[8];
+#pragma unroll
+  for (int m = 0; m < 8; ++m) acc[m] = T(0);
+  for (int i0 = 0; i0 < s.ni; i0 += 32) {
+    for (int e = tid; e < 32 * nk; e += 256) {
+      const int ii = e >> lg, kk = e & (nk - 1);
+      as[ii][kk] = i0 + ii < s.ni ? aux[((long long)(s.rep + i0 + ii) << lg) + kk] : T(0);
+    }
+    for (int e = tid; e < 32 * 32; e += 256) {
+      const int ii = e >> 5, cc = e & 31;
+      ps[ii][cc] = (i0 + ii < s.ni && c0 + cc < s.nc) ? pcpool[s.oPhi + (long long)(i0 + ii) * s.ncp + c0 + cc] : T(0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+      const int c = cl + ncl * m;
+      if (c < 32)
+        for (int ii = 0; ii < 32; ++ii) acc[m] += ps[ii][c] * as[ii][k];
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int m = 0; m < 8; ++m) {
+    const int c = cl + ncl * m;
+    if (c < 32 && c0 + c < s.nc) rcs[((long long)(s.coff + c0 + c) << lg) + k] = (double)acc[m];
+  }
+}
+
+// rc[q][k] = sum over the subdomain constraints mapped to coarse dof q
+__global__ void kb_coarse_gather(int ndofc, int lg, const int* __restrict__ cptr, const int* __restrict__ csub,
+                                 const int* __restrict__ cloc, const DevSub* __restrict__ ds,
+                                 const double* __restrict__ rcs, double* __restrict__ rc,
+                                 const int* __restrict__ ndone) {
+  const int nk = 1 << lg;
+  if (batch_all_done(ndone, nk)) return;
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ((long long)ndofc << lg)) return;
+  const int q = (int)(e >> lg), k = (int)(e & (nk - 1));
+  double t = 0.0;
+  for (int p = cptr[q]; p < cptr[q + 1]; ++p) t += rcs[((long long)(ds[csub[p]].coff + cloc[p]) << lg) + k];
+  rc[e] = t;
+}
+
+// ucs[e][k] = T(uc[cmap[e]][k]): the coarse solution at each subdomain constraint
+template <typename T>
+__global__ void kb_gather_uc(long long ncon, int lg, const int* __restrict__ cmap, const double* __restrict__ uc,
+                             T* __restrict__ ucs, const int* __restrict__ ndone) {
+  const int nk = 1 << lg;
+  if (batch_all_done(ndone, nk)) return;
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (ncon << lg)) return;
+  ucs[e] = T(uc[((long long)cmap[e >> lg] << lg) + (e & (nk - 1))]);
+}
+
+template <typename T>
+__global__ void kb_to_t(long long cnt, const double* __restrict__ v, T* __restrict__ out, int nk,
+                        const int* __restrict__ ndone) {
+  if (batch_all_done(ndone, nk)) return;
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < cnt) out[e] = T(v[e]);
+}
+
+// res = rc - Ac uc with the sparse FP64 coarse matrix
+__global__ void kb_coarse_res(int n, int lg, const int* __restrict__ ptr, const int* __restrict__ col,
+                              const double* __restrict__ val, const double* __restrict__ rc,
+                              const double* __restrict__ uc, double* __restrict__ res, const int* __restrict__ ndone) {
+  const int nk = 1 << lg;
+  if (batch_all_done(ndone, nk)) return;
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ((long long)n << lg)) return;
+  const int i = (int)(e >> lg), k = (int)(e & (nk - 1));
+  double t = rc[e];
+  for (int q = ptr[i]; q < ptr[i + 1]; ++q) t -= val[q] * uc[((long long)col[q] << lg) + k];
+  res[e] = t;
+}
+
+// ------------------------------------------------ assembly and reductions
+// per-column block sums of the threads' partials (thread t holds column t % nk)
+__device__ __forceinline__ void col_partials(double v, int nk, double* sh, double* __restrict__ part, int npart) {
+  sh[threadIdx.x] = v;
+  __syncthreads();
+  for (int st = RT / 2; st >= nk; st >>= 1) {
+    if (threadIdx.x < st) sh[threadIdx.x] += sh[threadIdx.x + st];
+    __syncthreads();
+  }
+  if (threadIdx.x < nk) part[(long long)threadIdx.x * npart + blockIdx.x] = sh[threadIdx.x];
+}
+
+// out[g][k] = sum of the subdomain rows (zero at fixed dofs if asked);
+// partial (p, out)_w per column when p is given
+__global__ void __launch_bounds__(RT) kb_assemble_dot(int n, int lg, Owners own, const double* __restrict__ yrep,
+                                                      const int* __restrict__ fixed, const double* __restrict__ wsum,
+                                                      const double* __restrict__ p, double* __restrict__ out,
+                                                      double* __restrict__ part, int npart, int zero_fixed,
+                                                      const int* __restrict__ ndone) {
+  const int nk = 1 << lg;
+  if (batch_all_done(ndone, nk)) return;
+  __shared__ double sh[RT];
+  const int k = threadIdx.x & (nk - 1), rl = threadIdx.x >> lg, nrl = RT >> lg;
+  double loc = 0.0;
+  for (long long g = (long long)blockIdx.x * nrl + rl; g < n; g += (long long)gridDim.x * nrl) {
+    double v = 0.0;
+    for (int q = own.ptr[g]; q < own.ptr[g + 1]; ++q) v += yrep[((long long)own.rep[q] << lg) + k];
+    if (zero_fixed && fixed && fixed[g]) v = 0.0;
+    const long long e = (g << lg) + k;
+    out[e] = v;
+    if (p) loc += wsum[g] * p[e] * v;
+  }
+  if (part) col_partials(loc, nk, sh, part, npart);
+}
+
+// z[g][k] = sum_s w_s zrep_s (the coarse correction is already in zrep); partial (r, z)_w
+__global__ void __launch_bounds__(RT) kb_assemble_z(int n, int lg, Owners own, const double* __restrict__ zrep,
+                                                    const double* __restrict__ wrep, const double* __restrict__ wsum,
+                                                    const double* __restrict__ r, double* __restrict__ z,
+                                                    double* __restrict__ part, int npart,
+                                                    const int* __restrict__ ndone) {
+  const int nk = 1 << lg;
+  if (batch_all_done(ndone, nk)) return;
+  __shared__ double sh[RT];
+  const int k = threadIdx.x & (nk - 1), rl = threadIdx.x >> lg, nrl = RT >> lg;
+  double loc = 0.0;
+  for (long long g = (long long)blockIdx.x * nrl + rl; g < n; g += (long long)gridDim.x * nrl) {
+    double v = 0.0;
+    for (int q = own.ptr[g]; q < own.ptr[g + 1]; ++q) {
+      const int j = own.rep[q];
+      v += wrep[j] * zrep[((long long)j << lg) + k];
+    }
+    const long long e = (g << lg) + k;
+    z[e] = v;
+    loc += wsum[g] * r[e] * v;
+  }
+  if (part) col_partials(loc, nk, sh, part, npart);
+}
+
+// partial (a, b)_w per column
+__global__ void __launch_bounds__(RT) kb_dot(int n, int lg, const double* __restrict__ a, const double* __restrict__ b,
+                                             const double* __restrict__ wsum, double* __restrict__ part, int npart) {
+  const int nk = 1 << lg;
+  __shared__ double sh[RT];
+  const int k = threadIdx.x & (nk - 1), rl = threadIdx.x >> lg, nrl = RT >> lg;
+  double loc = 0.0;
+  for (long long g = (long long)blockIdx.x * nrl + rl; g < n; g += (long long)gridDim.x * nrl) {
+    const long long e = (g << lg) + k;
+    loc += wsum[g] * a[e] * b[e];
+  }
+  col_partials(loc, nk, sh, part, npart);
+}
+
+__global__ void kb_axpy(long long cnt, double a, const double* __restrict__ x, double* __restrict__ y) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < cnt) y[e] += a * x[e];
+}
+
+// x[g][k] = x0[g] for every column
+__global__ void kb_bcast(int n, int lg, const double* __restrict__ x0, double* __restrict__ x) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < ((long long)n << lg)) x[e] = x0[e >> lg];
+}
+
+// dst[i][k] = src[i] for one column k
+__global__ void kb_put_col(long long cnt, int lg, int k, const double* __restrict__ src, double* __restrict__ dst) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < cnt) dst[(i << lg) + k] = src[i];
+}
+
+// interior solution of one column's interior loads (v0 [+ v1]) into vo[uo_off + r][k]
+template <typename T>
+__global__ void kb_put_vo(const DevSub* __restrict__ ds, int lg, int k, const T* __restrict__ v0,
+                          const T* __restrict__ v1, const long long* __restrict__ voff,
+                          const long long* __restrict__ uo_off, double* __restrict__ vo) {
+  const DevSub s = ds[blockIdx.y];
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= s.no) return;
+  const long long o = voff[blockIdx.y] + r;
+  double v = (double)v0[o];
+  if (v1) v += (double)v1[o];
+  vo[((uo_off[blockIdx.y] + r) << lg) + k] = v;
+}
+
+// ---------------------------------------------------------------- scalars
+// per column: normres0 = |r|, rmp = (r, z); columns past nrhs, with a zero
+// reduced rhs or a zero initial residual stop at once
+__global__ void kb_init(PcgCtl* __restrict__ ctl, const double* __restrict__ pgg, const double* __restrict__ prr,
+                        const double* __restrict__ prz, int npart, double tol, int maxit, int ndecrmax, int nrhs,
+                        int* __restrict__ ndone) {
+  __shared__ double sh[32];
+  const int k = blockIdx.x;
+  const double gg = sum_parts(pgg + (long long)k * npart, npart, sh);
+  const double rr = sum_parts(prr + (long long)k * npart, npart, sh);
+  const double rz = sum_parts(prz + (long long)k * npart, npart, sh);
+  if (threadIdx.x == 0) {
+    PcgCtl c{};
+    c.normres0 = sqrt(rr);
+    c.rmp = rz;
+    c.tol = tol;
+    c.lastres = 1.0;
+    c.iter = 1;
+    c.maxit = maxit;
+    c.ndecrmax = ndecrmax;
+    if (k >= nrhs || gg == 0.0 || rr == 0.0) {
+      c.done = 1;
+      c.reason = 0;
+      c.num_iter = 0;
+      c.nw = 0;
+      atomicAdd(ndone, 1);
+    }
+    ctl[k] = c;
+  }
+}
+
+__global__ void kb_sc_alpha(PcgCtl* ctl, const double* __restrict__ part, int npart) {
+  PcgCtl* c = ctl + blockIdx.x;
+  if (c->done) return;
+  __shared__ double sh[32];
+  const double pap = sum_parts(part + (long long)blockIdx.x * npart, npart, sh);
+  if (threadIdx.x == 0) {
+    c->pap = pap;
+    if (!(pap > 0.0)) c->warn |= 1;
+    c->alpha = c->rmp / pap;
+  }
+}
+
+__global__ void kb_sc_res(PcgCtl* ctl, const double* __restrict__ part, int npart, double* __restrict__ hist,
+                          int ldh, int* __restrict__ ndone) {
+  PcgCtl* c = ctl + blockIdx.x;
+  if (c->done) return;
+  __shared__ double sh[32];
+  const double nr2 = sum_parts(part + (long long)blockIdx.x * npart, npart, sh);
+  if (threadIdx.x == 0) {
+    const int iter = c->iter;
+    c->normres2 = nr2;
+    const double relres = sqrt(nr2) / c->normres0;
+    c->relres = relres;
+    hist[(long long)blockIdx.x * ldh + iter - 1] = relres;
+    int stop = 0;
+    if (relres < c->tol) { stop = 1; c->reason = 0; }
+    else if (iter == c->maxit) { stop = 1; c->reason = -1; }
+    else {
+      if (relres < c->lastres) c->ndecr = 0;
+      else {
+        c->ndecr += 1;
+        if (c->ndecr >= c->ndecrmax) { stop = 1; c->reason = -2; }
+      }
+      c->lastres = relres;
+    }
+    if (stop) {
+      c->done = 1;
+      c->num_iter = iter;
+      c->nw = iter - 1;
+      atomicAdd(ndone, 1);
+    }
+  }
+}
+
+__global__ void kb_sc_beta(PcgCtl* ctl, const double* __restrict__ part, int npart, double* __restrict__ diag,
+                           double* __restrict__ subdiag, int ldd) {
+  PcgCtl* c = ctl + blockIdx.x;
+  if (c->done) return;
+  __shared__ double sh[32];
+  const double rmp = sum_parts(part + (long long)blockIdx.x * npart, npart, sh);
+  if (threadIdx.x == 0) {
+    if (!(rmp > 0.0)) c->warn |= 2;
+    const double beta = rmp / c->rmp;
+    c->beta = beta;
+    c->rmp = rmp;
+    const int iter = c->iter;
+    const double alpha = c->alpha;
+    double* dg = diag + (long long)blockIdx.x * ldd;
+    double* sd = subdiag + (long long)blockIdx.x * ldd;
+    dg[iter - 1] += 1.0 / alpha;
+    dg[iter] = beta / alpha;
+    sd[iter - 1] = beta >= 0.0 ? -sqrt(beta) / alpha : 0.0;
+    c->iter = iter + 1;
+  }
+}
+
+// x += alpha p, r -= alpha ap for the running columns; partial (r, r)_w
+__global__ void __launch_bounds__(RT) kb_update_xr(int n, int lg, const PcgCtl* __restrict__ ctl,
+                                                   double* __restrict__ x, double* __restrict__ r,
+                                                   const double* __restrict__ p, const double* __restrict__ ap,
+                                                   const double* __restrict__ wsum, double* __restrict__ part,
+                                                   int npart) {
+  const int nk = 1 << lg;
+  __shared__ double sh[RT];
+  const int k = threadIdx.x & (nk - 1), rl = threadIdx.x >> lg, nrl = RT >> lg;
+  const bool run = !ctl[k].done;
+  const double alpha = ctl[k].alpha;
+  double loc = 0.0;
+  if (run)
+    for (long long g = (long long)blockIdx.x * nrl + rl; g < n; g += (long long)gridDim.x * nrl) {
+      const long long e = (g << lg) + k;
+      x[e] += alpha * p[e];
+      const double rv = r[e] - alpha * ap[e];
+      r[e] = rv;
+      loc += wsum[g] * rv * rv;
+    }
+  col_partials(loc, nk, sh, part, npart);
+}
+
+__global__ void kb_update_p(int n, int lg, const PcgCtl* __restrict__ ctl, double* __restrict__ p,
+                            const double* __restrict__ z) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ((long long)n << lg)) return;
+  const PcgCtl& c = ctl[e & ((1 << lg) - 1)];
+  if (c.done) return;
+  p[e] = z[e] + c.beta * p[e];
+}
+
+// ------------------------------------------------------------ three levels
+// level-2 interior loads into the band right-hand-side block (row stride BMAX,
+// padding rows and columns zero): bb[rowoff + r][k] = rc[mo[uo_off + r]][k]
+__global__ void kb_l2_fill(const DevSub* __restrict__ ds, int lg, const long long* __restrict__ rowoff,
+                           const long long* __restrict__ uo_off, const int* __restrict__ mo,
+                           const double* __restrict__ rc, double* __restrict__ bb, const int* __restrict__ ndone) {
+  const int nk = 1 << lg;
+  if (batch_all_done(ndone, nk)) return;
+  const DevSub s = ds[blockIdx.y];
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (long long)s.NO * BMAX) return;
+  const int r = (int)(e / BMAX), k = (int)(e % BMAX);
+  double v = 0.0;
+  if (r < s.no && k < nk) v = rc[((long long)mo[uo_off[blockIdx.y] + r] << lg) + k];
+  bb[(rowoff[blockIdx.y] + r) * BMAX + k] = v;
+}
+
+// fi[j][k] = w_j rc[mi[j]][k] on the level-2 interface (zero where unmapped)
+__global__ void kb_l2_fi(int nrep, int lg, const int* __restrict__ mi, const double* __restrict__ wi,
+                         const double* __restrict__ rc, double* __restrict__ fi, const int* __restrict__ ndone) {
+  const int nk = 1 << lg;
+  if (batch_all_done(ndone, nk)) return;
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ((long long)nrep << lg)) return;
+  const int j = (int)(e >> lg), k = (int)(e & (nk - 1));
+  fi[e] = mi[j] >= 0 ? wi[j] * rc[((long long)mi[j] << lg) + k] : 0.0;
+}
+
+// grep = f_i - A_io v with v the interior solutions in the band block
+__global__ void kb_reduced_rhs(const DevSub* __restrict__ ds, CsrView kio, int lg, const long long* __restrict__ rowoff,
+                               const double* __restrict__ bb, const double* __restrict__ fi,
+                               double* __restrict__ grep, const int* __restrict__ ndone) {
+  const int nk = 1 << lg;
+  if (batch_all_done(ndone, nk)) return;
+  const DevSub s = ds[blockIdx.y];
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ((long long)s.ni << lg)) return;
+  const int i = (int)(e >> lg), k = (int)(e & (nk - 1));
+  const long long o = ((long long)(s.rep + i) << lg) + k;
+  double acc = fi[o];
+  const int* p = kio.ptr + s.kio;
+  const long long ro = rowoff[blockIdx.y];
+  for (int q = p[i]; q < p[i + 1]; ++q) acc -= kio.val[q] * bb[(ro + kio.col[q]) * BMAX + k];
+  grep[o] = acc;
+}
+
+// uc at the level-2 interior dofs (from the band block) and interface dofs (from z)
+__global__ void kb_l2_out_o(const DevSub* __restrict__ ds, int lg, const long long* __restrict__ rowoff,
+                            const long long* __restrict__ uo_off, const int* __restrict__ mo,
+                            const double* __restrict__ bb, double* __restrict__ uc, const int* __restrict__ ndone) {
+  const int nk = 1 << lg;
+  if (batch_all_done(ndone, nk)) return;
+  const DevSub s = ds[blockIdx.y];
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ((long long)s.no << lg)) return;
+  const int r = (int)(e >> lg), k = (int)(e & (nk - 1));
+  uc[((long long)mo[uo_off[blockIdx.y] + r] << lg) + k] = bb[(rowoff[blockIdx.y] + r) * BMAX + k];
+}
+
+__global__ void kb_l2_out_i(int n, int lg, const int* __restrict__ mz, const double* __restrict__ z,
+                            double* __restrict__ uc, const int* __restrict__ ndone) {
+  const int nk = 1 << lg;
+  if (batch_all_done(ndone, nk)) return;
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ((long long)n << lg)) return;
+  uc[((long long)mz[e >> lg] << lg) + (e & (nk - 1))] = z[e];
+}
+
+}  // namespace bddc

@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "bddc_adaptive.cuh"
+#include "bddc_batch_kernels.cuh"
 #include "bddc_internal.hpp"
 #include "bddc_pcg_kernels.cuh"
 #include "bddc_tc.cuh"
@@ -169,6 +170,26 @@ static T* upload(const std::vector<T>& v, std::vector<void*>& owned, cudaStream_
   return p;
 }
 
+// Device buffers of the batched solve (nk interleaved columns), allocated at
+// the first batched solve and kept until the next setup or a larger batch.
+struct BatchBufs {
+  int nk = 0, lg = 0, ldh = 0;
+  std::vector<void*> mem;
+  double *x = nullptr, *r = nullptr, *p = nullptr, *ap = nullptr, *z = nullptr;
+  double *yrep = nullptr, *zrep = nullptr, *grep = nullptr, *rcs = nullptr;
+  double *rc = nullptr, *uc = nullptr, *cres = nullptr, *vo = nullptr;
+  double *part0 = nullptr, *part1 = nullptr, *part2 = nullptr;
+  void *aux = nullptr, *xs = nullptr, *ucs = nullptr, *cbt = nullptr;  // working precision / split operands
+  PcgCtl* ctl = nullptr;
+  int* ndone = nullptr;  // finished columns (shared with the level-2 device)
+  double *hist = nullptr, *diag = nullptr, *subdiag = nullptr;
+  GemmDesc *gS = nullptr, *gZ = nullptr, *gX = nullptr, *gC = nullptr;
+  // level-2 device only: interior loads, assembled reduced rhs, band block
+  double *fi = nullptr, *g = nullptr, *bb = nullptr;
+  BandDesc* bdB = nullptr;
+  long long* rowoff = nullptr;
+};
+
 class Device {
  public:
   cudaStream_t st = nullptr;
@@ -238,6 +259,7 @@ class Device {
   int l2_nfo = 0;
   int maxnbo = 0, maxw = 0, maxNR = 0;
   int nref = 0;
+  BatchBufs bt;
   Profiler prof;
 
   ~Device() {
@@ -259,10 +281,15 @@ class Device {
     l2_mo = l2_mi = l2_mz = nullptr;
     l2_wi = nullptr;
     nv_off = nullptr;
+    release_batch();
     release_pc();
     for (void* q : owned) cudaFreeAsync(q, st);
     owned.clear();
     maxit_alloc = 0;
+  }
+  void release_batch() {
+    for (void* q : bt.mem) cudaFreeAsync(q, st);
+    bt = BatchBufs{};
   }
   void release_pc() {
     for (void* q : owned_pc) cudaFreeAsync(q, st);
@@ -734,6 +761,7 @@ template <typename T>
 static void setup_precond(Solver& S, Device& D) {
   const int nsub = D.nsub;
   cudaStream_t st = D.st;
+  D.release_batch();
   D.release_pc();
   auto& own = D.owned_pc;
   long long oP = 0, oPC = 0, oSm = 0, oPan = 0;
@@ -1939,6 +1967,24 @@ static void setup_level2(Solver& S, Device& D) {
   D2.l2_wi = upload(wi, D2.owned, st);
   D.lev2 = &S2;
   CK(cudaStreamSynchronize(st));
+}
+
+}  // namespace bddc
+
+#include "bddc_batch.cuh"
+
+namespace bddc {
+
+bool device_solve_batch(Solver& S, int nrhs, double tol, int maxit, int ndecrmax, vector<int>& num_iter,
+                        vector<int>& reason, vector<double>& cond, Error& err) {
+  try {
+    if (S.dev->mixed) batch_solve_impl<float>(S, nrhs, tol, maxit, ndecrmax, num_iter, reason, cond);
+    else batch_solve_impl<double>(S, nrhs, tol, maxit, ndecrmax, num_iter, reason, cond);
+  } catch (Error& e) {
+    err = e;
+    return false;
+  }
+  return true;
 }
 
 bool device_new_data(Solver& S, Error& err) {

@@ -63,6 +63,22 @@ struct dfacc {
   __device__ __forceinline__ double to_double() const { return (double)s + (double)c; }
 };
 
+// One multiply-add of a double-float product a * b (a = ah + al,
+// b = bh + bl) into the unevaluated sum (sh, sl): the exact product ah bh (a
+// rounded product and its fma error) plus the cross terms ah bl + al bh,
+// accumulated with an error-free two-sum.  Accuracy about 2^-44 relative to
+// sum |a b|, FP64-like for these products.
+__device__ __forceinline__ void df_mac(float& sh, float& sl, float ah, float al, float bh, float bl) {
+  const float p = __fmul_rn(ah, bh);
+  const float e = __fmaf_rn(ah, bh, -p);
+  const float c = __fmaf_rn(ah, bl, __fmaf_rn(al, bh, e));
+  const float t = __fadd_rn(sh, p);
+  const float bp = __fsub_rn(t, sh);
+  const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+  sh = t;
+  sl = __fadd_rn(sl, __fadd_rn(err, c));
+}
+
 __device__ __forceinline__ dfloat df_from_double(double v) {
   dfloat r;
   r.hi = (float)v;

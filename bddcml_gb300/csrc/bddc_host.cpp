@@ -826,10 +826,15 @@ void host_setup(Solver& S) {
 // reduced-rhs input: weighted rhs, Dirichlet rows zeroed, weighted bc added
 // (module_dd.f90:7040-7075 and sm_prepare_rhs, module_sm.f90:603-628)
 void host_reduced_rhs_inputs(const Subdomain& s, vector<double>& fo, vector<double>& fi) {
+  host_reduced_rhs_inputs(s, s.rhs.data(), s.rhs_complete, fo, fi);
+}
+
+void host_reduced_rhs_inputs(const Subdomain& s, const double* rhs, bool complete, vector<double>& fo,
+                             vector<double>& fi) {
   const int no = s.ndofo, ni = s.ndofi;
-  vector<double> f = s.rhs;
+  vector<double> f(rhs, rhs + s.ndof);
   vector<double> bcw = s.bc;
-  if (s.rhs_complete) for (int i = 0; i < ni; ++i) f[s.iivsvn[i]] *= s.wi[i];
+  if (complete) for (int i = 0; i < ni; ++i) f[s.iivsvn[i]] *= s.wi[i];
   for (int i = 0; i < ni; ++i) bcw[s.iivsvn[i]] *= s.wi[i];
   if (s.bc_present)
     for (int i = 0; i < s.ndof; ++i) { if (s.ifix[i]) f[i] = 0.0; f[i] += bcw[i]; }

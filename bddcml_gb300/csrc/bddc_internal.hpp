@@ -53,6 +53,10 @@ struct Subdomain {
   vector<double> xyz;  // column-major (nnod x ndim)
   vector<double> fixv, rhs, sol;
   bool rhs_complete = true;
+  // batched right-hand sides (ndof x nrhs_batch, column-major) and their solutions
+  vector<double> rhs_batch, sol_batch;
+  int nrhs_batch = 0;
+  bool rhs_batch_complete = true;
   int matrixtype = 1;
   vector<int> ia, ja;  // upper triangle (merged at setup)
   vector<double> a;
@@ -179,6 +183,7 @@ struct Solver {
   vector<double> iface_wsum;          // per unique dof: sum of subdomain weights
   bool setup_done = false;
   bool new_data_pending = false;  // changed subdomain data not yet through setup_new_data
+  int batch_solved = 0;           // right-hand sides of the last batched solve (0: none)
   bool solved = false;            // a solve has produced the subdomain solutions
   bool reactions_ready = false;   // reactions computed for the last solve
   Device* dev = nullptr;
@@ -222,6 +227,8 @@ void host_prepare_blocks(Subdomain& s, SubBlocks& b);
 // reduced-rhs inputs of a subdomain: weighted rhs with Dirichlet rows replaced by the
 // weighted eliminated contributions; fo in the band order of the interior, fi per interface dof
 void host_reduced_rhs_inputs(const Subdomain& s, vector<double>& fo, vector<double>& fi);
+void host_reduced_rhs_inputs(const Subdomain& s, const double* rhs, bool complete, vector<double>& fo,
+                             vector<double>& fi);
 // new boundary values / loads after setup: recompute bc on every subdomain and
 // assemble it over the interface (module_levels.f90:855-903)
 void host_new_data(Solver& S);
@@ -234,6 +241,10 @@ Device* device_create(Error& err);
 Device* device_create_on_stream(Device* parent, Error& err);  // shares the parent's stream
 bool device_release_memory(Error& err);
 bool device_new_data(Solver& S, Error& err);
+// PCG on nrhs batched right-hand sides (Subdomain::rhs_batch) together; the
+// solutions go to Subdomain::sol_batch, per-column results to the vectors
+bool device_solve_batch(Solver& S, int nrhs, double tol, int maxit, int ndecrmax, vector<int>& num_iter,
+                        vector<int>& reason, vector<double>& cond, Error& err);
 bool device_element_gradient(int nelem, int nne, const int* inet, const double* ke0, bool per_element,
                              const double* u, const double* lam, double* grad, Error& err);
 // largest subdomain interface the allocation-free dot product's fixed scratch holds

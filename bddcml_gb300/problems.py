@@ -435,3 +435,29 @@ def elasticity_on_cube(num_el_per_sub_edge: int, num_sub_per_cube_edge: int, nu:
     nnod = (n + 1) ** 3
     return Problem(name=f"elasticity_{n}^3_{num_sub_per_cube_edge}^3subs", nelem=n ** 3, nnod=nnod,
                    ndof=3 * nnod, ndim=3, meshdim=3, subdomains=subs, n_el_edge=n, kappa=young)
+
+
+def body_force_loads(prob: Problem, nrhs: int, seed: int = 5) -> list:
+    """nrhs load cases of an elasticity problem on the unit-cube grid: the lumped
+    body force in -z of every element (-h^3/8 per node) scaled by its own iid
+    N(0, 1) factor in each case.  Returns, per subdomain, an (nrhs, ndofs)
+    array of complete right-hand sides (global values at the subdomain dofs,
+    zero at fixed dofs)."""
+    n = prob.n_el_edge
+    h = 1.0 / n
+    nng = n + 1
+    rng = np.random.default_rng(seed)
+    out = [np.zeros((nrhs, s.ndofs)) for s in prob.subdomains]
+    for k in range(nrhs):
+        sc = rng.standard_normal(n ** 3).reshape(n, n, n)  # [z, y, x] = global element order
+        f = np.zeros((nng, nng, nng))
+        for dz in (0, 1):
+            for dy in (0, 1):
+                for dx in (0, 1):
+                    f[dz:dz + n, dy:dy + n, dx:dx + n] += sc
+        f = (-h ** 3 / 8.0) * f.ravel()
+        for s, o in zip(prob.subdomains, out):
+            r = o[k]
+            r[2::3] = f[s.isngn]
+            r[s.ifix != 0] = 0.0
+    return out

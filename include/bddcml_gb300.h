@@ -105,6 +105,26 @@ void bddcml_solve_c(int *comm_all, int *method, double *tol, int *maxit, int *nd
 /* replaces bddcml_download_local_solution_c, src/bddcml_interface_c.h:41 */
 void bddcml_download_local_solution_c(int *isub, double *sols, int *lsols);
 
+/* Batched loads (extension; the reference solves one load per bddcml_solve_c
+ * call and re-enters with change_subdomain_data + setup_new_data for the next).
+ * Uploads nrhs (1..64) right-hand sides of subdomain isub, rhss holding nrhs
+ * columns of ndof entries (column-major, *lrhss = ndof * nrhs); the fixed
+ * values, matrix and constraints are those of the set-up problem. */
+void bddcml_upload_subdomain_rhs_batch_c(int *isub, int *nrhs, double *rhss, int *lrhss, int *is_rhs_complete);
+
+/* Solves the uploaded batch by PCG (method 0; any other method sets
+ * BDDCML_ERR_UNSUPPORTED).  Every column runs the iteration of
+ * bddcml_solve_c with its own scalars and stop test (module_krylov.f90:545-888)
+ * from the zero initial guess (fixed values at fixed dofs); the subdomain
+ * applies of all columns run as one product per subdomain.  num_iter,
+ * converged_reason and condition_number receive nrhs entries each. */
+void bddcml_solve_batch_c(int *comm_all, int *method, double *tol, int *maxit, int *ndecrmax, int *nrhs,
+                          int *num_iter, int *converged_reason, double *condition_number);
+
+/* Solutions of the last batched solve for subdomain isub: nrhs columns of ndof
+ * entries, column-major (*lsols = ndof * nrhs). */
+void bddcml_download_local_solution_batch_c(int *isub, int *nrhs, double *sols, int *lsols);
+
 /* replaces bddcml_download_global_solution_c, src/bddcml_interface_c.h:43
  * (module_levels.f90:4617-4744): every subdomain's solution written at its
  * global dofs; *lsol must be the global dof count. */

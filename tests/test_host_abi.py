@@ -155,3 +155,33 @@ def test_host_coarse_space_equals_oracle_elasticity(built_lib, oracle_mod):
         w_o = o.weights(s.isub)
         assert np.array_equal(w_o, B.get_interface_weights(s.isub, len(w_o)))
     B.bddcml_finalize()
+
+
+def test_batch_upload_validation_without_gpu(built_lib):
+    """bddcml_upload_subdomain_rhs_batch_c checks its sizes on the host; the
+    batched solve and download refuse to run before a setup / batched solve."""
+    import bddcml_gb300 as B
+    from bddcml_gb300 import problems
+    prob = problems.poisson_on_cube(3, 2)
+    B.bddcml_init(2, [prob.nsub, 1], -1, 0, 0, 0, 0)
+    try:
+        B.upload_problem(prob)
+        s = prob.subdomains[0]
+        with pytest.raises(B.BddcmlError) as e:
+            B.bddcml_upload_subdomain_rhs_batch(s.isub, np.zeros((65, s.ndofs)))
+        assert e.value.code == 1
+        lib = B.lib()
+        r = np.zeros(2 * s.ndofs - 1)
+        lib.bddcml_upload_subdomain_rhs_batch_c(C.byref(C.c_int(s.isub)), C.byref(C.c_int(2)),
+                                                r.ctypes.data_as(C.POINTER(C.c_double)),
+                                                C.byref(C.c_int(r.size)), C.byref(C.c_int(1)))
+        assert B.last_error()[0] == 1
+        B.bddcml_upload_subdomain_rhs_batch(s.isub, np.ones((3, s.ndofs)))
+        with pytest.raises(B.BddcmlError) as e:
+            B.bddcml_solve_batch(3)
+        assert e.value.code == 1
+        with pytest.raises(B.BddcmlError) as e:
+            B.bddcml_download_local_solution_batch(s.isub, 3, s.ndofs)
+        assert e.value.code == 1
+    finally:
+        B.bddcml_finalize()
