@@ -13,6 +13,17 @@ namespace bddc {
 
 static unsigned blocks_for(long long cnt, int threads = 256) { return (unsigned)((cnt + threads - 1) / threads); }
 
+// out = addend + [A1 A2] [B1; B2] for every descriptor (kb_gemm_t), rows up to maxm
+template <typename T>
+static void gemm_t(Device& D, const GemmDesc* gd, int ndesc, int maxm, const T* A, const T* B1, const T* B2, int ldb,
+                   double* out, const double* addend, int ldo, int nk, const int* ndone) {
+  const size_t smem = GtCfg<T>::SMEM;
+  raise_smem(kb_gemm_t<T>, smem);
+  kb_gemm_t<T><<<dim3((maxm + GtCfg<T>::BM - 1) / GtCfg<T>::BM, ndesc), 256, smem, D.st>>>(gd, A, B1, B2, ldb, out,
+                                                                                          addend, ldo, nk, ndone);
+  CKL();
+}
+
 template <typename T>
 static void batch_prepare(Device& D, int nk, int lg, int maxit, int* shared_ndone, bool level2) {
   BatchBufs& B = D.bt;
@@ -88,6 +99,22 @@ static void batch_prepare(Device& D, int nk, int lg, int maxit, int* shared_ndon
                      d.no, d.ni, 0, d.NR, 0, 0};
   }
   vector<GemmDesc> gc(1, GemmDesc{0, 0, 0, 0, 0, D.ndofc, D.ndofc, 0, D.ldc, 0, 0});
+  // Phi^T per subdomain for the coarse-residual product
+  vector<GemmDesc> gp(D.nsub);
+  vector<long long> opt(D.nsub);
+  long long npt = 0;
+  for (int t = 0; t < D.nsub; ++t) {
+    const DevSub& d = D.hs[t];
+    opt[t] = npt;
+    gp[t] = GemmDesc{npt, 0, d.rep, 0, d.coff, d.nc, d.ni, 0, d.NI, 0, 0};
+    npt += (long long)d.ncp * d.NI;
+  }
+  B.phit = dalloc<T>(std::max(1LL, npt), mem);
+  B.gP = upload(gp, mem, D.st);
+  const long long* dopt = upload(opt, mem, D.st);
+  kb_phi_transpose<T><<<dim3(blocks_for((long long)D.ncpmax * D.maxNI), D.nsub), 256, 0, D.st>>>(
+      D.ds, static_cast<const T*>(D.poolPC), dopt, static_cast<T*>(B.phit));
+  CKL();
   B.gS = upload(gs, mem, D.st);
   B.gZ = upload(gz, mem, D.st);
   B.gX = upload(gx, mem, D.st);
@@ -114,10 +141,8 @@ static void batch_schur(Device& D, const double* vin, double* vout, bool zero_fi
     kb_gather_t<double><<<blocks_for(cnt), 256, 0, st>>>(D.nrep, B.lg, D.uniq, nullptr, 1.0, vin,
                                                          static_cast<double*>(B.xs), B.ndone);
     CKL();
-    kb_gemm_t<double><<<grid, 256, 0, st>>>(B.gS, static_cast<const double*>(D.poolS),
-                                            static_cast<const double*>(B.xs), nullptr, B.nk, B.yrep, nullptr, B.nk,
-                                            B.nk, B.ndone);
-    CKL();
+    gemm_t<double>(D, B.gS, D.nsub, D.maxNI, static_cast<const double*>(D.poolS), static_cast<const double*>(B.xs),
+                   nullptr, B.nk, B.yrep, nullptr, B.nk, B.nk, B.ndone);
   }
   D.prof.end(PH_SCHUR_APPLY, st);
   kb_assemble_dot<<<D.npart, RT, 0, st>>>(D.n, B.lg, D.own, B.yrep, D.fixed, D.wsum, dotvec, vout, part, D.npart,
@@ -141,8 +166,8 @@ static void batch_pc(Device& D, const double* rin, double* zout, double* part) {
                                                                       B.ndone);
   CKL();
   if (D.ndofc > 0) {
-    kb_phit<T><<<dim3(D.nsub, (D.ncpmax + 31) / 32), 256, 0, st>>>(D.ds, pc, aux, lg, B.rcs, B.ndone);
-    CKL();
+    gemm_t<T>(D, B.gP, D.nsub, D.ncpmax, static_cast<const T*>(B.phit), aux, nullptr, nk, B.rcs, nullptr, nk, nk,
+              B.ndone);
     kb_coarse_gather<<<blocks_for((long long)D.ndofc << lg), 256, 0, st>>>(D.ndofc, lg, D.co_ptr, D.co_sub,
                                                                            D.co_loc, D.ds, B.rcs, B.rc, B.ndone);
     CKL();
@@ -153,19 +178,16 @@ static void batch_pc(Device& D, const double* rin, double* zout, double* part) {
       const T* minv = static_cast<const T*>(D.cinv);
       T* cb = static_cast<T*>(B.cbt);
       const long long cc = (long long)D.ndofc << lg;
-      const dim3 gc((D.ndofc + GM - 1) / GM, 1);
       kb_to_t<T><<<blocks_for(cc), 256, 0, st>>>(cc, B.rc, cb, nk, B.ndone);
       CKL();
-      kb_gemm_t<T><<<gc, 256, 0, st>>>(B.gC, minv, cb, nullptr, nk, B.uc, nullptr, nk, nk, B.ndone);
-      CKL();
+      gemm_t<T>(D, B.gC, 1, D.ndofc, minv, cb, nullptr, nk, B.uc, nullptr, nk, nk, B.ndone);
       for (int rr = 0; rr < 2; ++rr) {
         kb_coarse_res<<<blocks_for(cc), 256, 0, st>>>(D.ndofc, lg, D.ac_ptr, D.ac_col, D.ac_val, B.rc, B.uc, B.cres,
                                                       B.ndone);
         CKL();
         kb_to_t<T><<<blocks_for(cc), 256, 0, st>>>(cc, B.cres, cb, nk, B.ndone);
         CKL();
-        kb_gemm_t<T><<<gc, 256, 0, st>>>(B.gC, minv, cb, nullptr, nk, B.uc, B.uc, nk, nk, B.ndone);
-        CKL();
+        gemm_t<T>(D, B.gC, 1, D.ndofc, minv, cb, nullptr, nk, B.uc, B.uc, nk, nk, B.ndone);
       }
     }
     long long ncon = 0;
@@ -174,9 +196,7 @@ static void batch_pc(Device& D, const double* rin, double* zout, double* part) {
     CKL();
   }
   // zrep = Z_s aux_s + Phi_s uc_s in one product per subdomain
-  kb_gemm_t<T><<<dim3((D.maxNI + GM - 1) / GM, D.nsub), 256, 0, st>>>(B.gZ, pc, aux, ucs, nk, B.zrep, nullptr, nk,
-                                                                      nk, B.ndone);
-  CKL();
+  gemm_t<T>(D, B.gZ, D.nsub, D.maxNI, pc, aux, ucs, nk, B.zrep, nullptr, nk, nk, B.ndone);
   D.prof.end(PH_PC_LOCAL, st);
   kb_assemble_z<<<D.npart, RT, 0, st>>>(D.n, lg, D.own, B.zrep, D.wrep, D.wsum, rin, zout, part, D.npart, B.ndone);
   CKL();
@@ -208,10 +228,8 @@ static void batch_level2(Device& D1, const double* rc, double* uc) {
   kb_gather_t<double><<<blocks_for((long long)D2.nrep << lg), 256, 0, st>>>(D2.nrep, lg, D2.uniq, nullptr, -1.0, B.z,
                                                                             static_cast<double*>(B.xs), B.ndone);
   CKL();
-  kb_gemm_t<double><<<dim3((D2.maxNO + GM - 1) / GM, D2.nsub), 256, 0, st>>>(
-      B.gX, static_cast<const double*>(D2.poolT), static_cast<const double*>(B.xs), nullptr, nk, B.bb, B.bb, BMAX, nk,
-      B.ndone);
-  CKL();
+  gemm_t<double>(D2, B.gX, D2.nsub, D2.maxNO, static_cast<const double*>(D2.poolT), static_cast<const double*>(B.xs),
+                 nullptr, nk, B.bb, B.bb, BMAX, nk, B.ndone);
   kb_l2_out_o<<<dim3(blocks_for((long long)D2.maxNO << lg), D2.nsub), 256, 0, st>>>(D2.ds, lg, B.rowoff, D2.uo_off,
                                                                                    D2.l2_mo, B.bb, uc, B.ndone);
   CKL();
@@ -228,7 +246,7 @@ static void batch_solve_impl(Solver& S, int nrhs, double tol, int maxit, int nde
   Device& D = *S.dev;
   cudaStream_t st = D.st;
   const double t0 = wall_time();
-  int nk = 1, lg = 0;
+  int nk = 4, lg = 2;  // at least 4 columns: the GEMM operand rows move in 16-byte pieces
   while (nk < nrhs) { nk <<= 1; ++lg; }
   batch_prepare<T>(D, nk, lg, maxit, nullptr, false);
   if (D.lev2) batch_prepare<double>(*D.lev2->dev, nk, lg, 0, D.bt.ndone, true);
@@ -360,10 +378,8 @@ static void batch_solve_impl(Solver& S, int nrhs, double tol, int maxit, int nde
     kb_gather_t<double><<<blocks_for(nrep << lg), 256, 0, st>>>(nrep, lg, D.uniq, nullptr, -1.0, B.x,
                                                                 static_cast<double*>(B.xs), nullptr);
     CKL();
-    kb_gemm_t<double><<<gpost, 256, 0, st>>>(B.gX, static_cast<const double*>(D.poolT),
-                                             static_cast<const double*>(B.xs), nullptr, nk, B.vo, B.vo, nk, nk,
-                                             nullptr);
-    CKL();
+    gemm_t<double>(D, B.gX, D.nsub, D.maxNO, static_cast<const double*>(D.poolT), static_cast<const double*>(B.xs),
+                   nullptr, nk, B.vo, B.vo, nk, nk, nullptr);
   }
   D.prof.end(PH_POST, st);
   vector<double> hx((size_t)n * nk), hvo((size_t)std::max(1LL, nfo) * nk);

@@ -159,65 +159,116 @@ __global__ void __launch_bounds__(256) kb_gemm_df(const GemmDesc* __restrict__ g
 
 // Product in the working precision T with T accumulation, two K segments:
 //   out[oo + r][c] = addend + sum_j A1[r][j] B1[ob + j][c] + sum_j A2[r][j] B2[ob2 + j][c]
+// BM x 64 output tile per CTA (256 threads, rows ty + 16 i, columns tx + 16 j),
+// K chunks of 32 streamed through a STAGES-deep cp.async ring so that the
+// operand loads of later chunks are in flight while a chunk is multiplied.
+// FP32 uses 128-row tiles; FP64 (a small fraction of the FP32 rate on this
+// part, and used for the small level-2 problem) 32-row tiles, for more CTAs.
+// Requires nk % 4 == 0 and 16-byte aligned rows (row strides and offsets
+// multiples of 16 / sizeof(T) elements); partial chunks are zero-filled.
+template <typename T>
+struct GtCfg {
+  static constexpr int BM = sizeof(T) == 4 ? 128 : 32;
+  static constexpr int RI = BM / 16;  // rows per thread
+  static constexpr int STAGES = sizeof(T) == 4 ? 4 : 3;
+  static constexpr int VEC = 16 / sizeof(T);  // elements per 16-byte copy
+  static constexpr int LDA = GK + VEC;        // padded row stride of the A tile
+  static constexpr int A_ELEMS = BM * LDA;
+  static constexpr int B_ELEMS = GK * BMAX;
+  static constexpr size_t SMEM = (size_t)STAGES * (A_ELEMS + B_ELEMS) * sizeof(T);
+};
+
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, int bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(
+                   static_cast<unsigned>(__cvta_generic_to_shared(dst))),
+               "l"(src), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) kb_gemm_t(const GemmDesc* __restrict__ gd, const T* __restrict__ A,
                                                  const T* __restrict__ B1, const T* __restrict__ B2, int ldb,
                                                  double* out, const double* addend, int ldo, int nk,
                                                  const int* __restrict__ ndone) {
+  using C = GtCfg<T>;
   if (batch_all_done(ndone, nk)) return;
   const GemmDesc d = gd[blockIdx.y];
-  const int r0 = blockIdx.x * GM;
+  const int r0 = blockIdx.x * C::BM;
   if (r0 >= d.m) return;
-  __shared__ T As[GK][GM + 1], Bs[GK][BMAX];
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T* As = reinterpret_cast<T*>(smraw);
+  T* Bs = As + C::STAGES * C::A_ELEMS;
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-  T acc[4][4];
+  const int n1 = (d.k1 + GK - 1) / GK, nch = n1 + (d.k2 + GK - 1) / GK;
+  auto load = [&](int c) {
+    const int buf = c % C::STAGES;
+    const bool seg1 = c < n1;
+    const int kb = seg1 ? c * GK : (c - n1) * GK;
+    const int K = seg1 ? d.k1 : d.k2;
+    const T* Ab = A + (seg1 ? d.oA : d.oA2);
+    const int lda = seg1 ? d.lda : d.lda2;
+    const T* Bb = seg1 ? B1 + d.ob * ldb : B2 + d.ob2 * ldb;
+    T* as = As + buf * C::A_ELEMS;
+    T* bs = Bs + buf * C::B_ELEMS;
+    constexpr int CPR = GK / C::VEC;  // 16-byte copies per A row
 #pragma unroll
-  for (int i = 0; i < 4; ++i)
+    for (int q = 0; q < C::BM * CPR / 256; ++q) {
+      const int e = tid + 256 * q;
+      const int row = e / CPR, kc = (e % CPR) * C::VEC;
+      const int gr = r0 + row, gk = kb + kc;
+      const int nb = (gr < d.m && gk < K) ? min(C::VEC, K - gk) * (int)sizeof(T) : 0;
+      const T* src = nb ? Ab + (long long)gr * lda + gk : Ab;
+      cp_async16(as + row * C::LDA + kc, src, nb);
+    }
+    constexpr int CPB = BMAX / C::VEC;  // 16-byte copies per B row
+#pragma unroll
+    for (int q = 0; q < GK * CPB / 256; ++q) {
+      const int e = tid + 256 * q;
+      const int row = e / CPB, cc = (e % CPB) * C::VEC;
+      const int gk = kb + row;
+      const int nb = (gk < K && cc < nk) ? 16 : 0;
+      const T* src = nb ? Bb + (long long)gk * ldb + cc : Bb;
+      cp_async16(bs + row * BMAX + cc, src, nb);
+    }
+  };
+  T acc[C::RI][4];
+#pragma unroll
+  for (int i = 0; i < C::RI; ++i)
 #pragma unroll
     for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
-  const int kt = d.k1 + d.k2;
-  for (int k0 = 0; k0 < kt; k0 += GK) {
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      const int e = tid + 256 * i;
-      const int row = e >> 5, kk = e & 31;
-      const int gr = r0 + row, gk = k0 + kk;
-      T a = T(0);
-      if (gr < d.m) {
-        if (gk < d.k1) a = __ldg(A + d.oA + (long long)gr * d.lda + gk);
-        else if (gk < kt) a = __ldg(A + d.oA2 + (long long)gr * d.lda2 + (gk - d.k1));
-      }
-      As[kk][row] = a;
-    }
-#pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      const int e = tid + 256 * i;
-      const int kk = e >> 6, c = e & 63;
-      const int gk = k0 + kk;
-      T b = T(0);
-      if (c < nk) {
-        if (gk < d.k1) b = B1[(d.ob + gk) * ldb + c];
-        else if (gk < kt) b = B2[(d.ob2 + gk - d.k1) * ldb + c];
-      }
-      Bs[kk][c] = b;
-    }
+  for (int st = 0; st < C::STAGES - 1; ++st) {
+    if (st < nch) load(st);
+    cp_async_commit();
+  }
+  for (int c = 0; c < nch; ++c) {
+    cp_async_wait<C::STAGES - 2>();
     __syncthreads();
+    if (c + C::STAGES - 1 < nch) load(c + C::STAGES - 1);
+    cp_async_commit();
+    const T* as = As + (c % C::STAGES) * C::A_ELEMS;
+    const T* bs = Bs + (c % C::STAGES) * C::B_ELEMS;
 #pragma unroll 4
     for (int kk = 0; kk < GK; ++kk) {
-      T a[4], b[4];
+      T a[C::RI], b[4];
 #pragma unroll
-      for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + 16 * i];
+      for (int i = 0; i < C::RI; ++i) a[i] = as[(ty + 16 * i) * C::LDA + kk];
 #pragma unroll
-      for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx + 16 * j];
+      for (int j = 0; j < 4; ++j) b[j] = bs[kk * BMAX + tx + 16 * j];
 #pragma unroll
-      for (int i = 0; i < 4; ++i)
+      for (int i = 0; i < C::RI; ++i)
 #pragma unroll
         for (int j = 0; j < 4; ++j) acc[i][j] += a[i] * b[j];
     }
-    __syncthreads();
   }
+  cp_async_wait<0>();
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
+  for (int i = 0; i < C::RI; ++i) {
     const int gr = r0 + ty + 16 * i;
     if (gr >= d.m) continue;
 #pragma unroll
@@ -272,6 +323,18 @@ __global__ void __launch_bounds__(256) kb_phit(const DevSub* __restrict__ ds, co
     const int c = cl + ncl * m;
     if (c < 32 && c0 + c < s.nc) rcs[((long long)(s.coff + c0 + c) << lg) + k] = (double)acc[m];
   }
+}
+
+// Phi^T of every subdomain (ncp x NI row-major at oT[s], padding zero), the
+// operand of the coarse-residual product rcs = Phi^T W r
+template <typename T>
+__global__ void kb_phi_transpose(const DevSub* __restrict__ ds, const T* __restrict__ pcpool,
+                                 const long long* __restrict__ oT, T* __restrict__ phit) {
+  const DevSub s = ds[blockIdx.y];
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (long long)s.ncp * s.NI) return;
+  const int c = (int)(e / s.NI), i = (int)(e % s.NI);
+  phit[oT[blockIdx.y] + e] = (c < s.nc && i < s.ni) ? pcpool[s.oPhi + (long long)i * s.ncp + c] : T(0);
 }
 
 // rc[q][k] = sum over the subdomain constraints mapped to coarse dof q

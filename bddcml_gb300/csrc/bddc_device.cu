@@ -183,7 +183,8 @@ struct BatchBufs {
   PcgCtl* ctl = nullptr;
   int* ndone = nullptr;  // finished columns (shared with the level-2 device)
   double *hist = nullptr, *diag = nullptr, *subdiag = nullptr;
-  GemmDesc *gS = nullptr, *gZ = nullptr, *gX = nullptr, *gC = nullptr;
+  GemmDesc *gS = nullptr, *gZ = nullptr, *gX = nullptr, *gC = nullptr, *gP = nullptr;
+  void* phit = nullptr;  // Phi^T per subdomain (working precision)
   // level-2 device only: interior loads, assembled reduced rhs, band block
   double *fi = nullptr, *g = nullptr, *bb = nullptr;
   BandDesc* bdB = nullptr;
