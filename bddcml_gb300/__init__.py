@@ -42,7 +42,7 @@ EXPORTS = ["bddcml_init_c", "bddcml_upload_global_data_c", "bddcml_upload_subdom
            "bddcml_set_profiling_c", "bddcml_get_profile_c", "bddcml_release_device_memory_c",
            "bddcml_dotprod_subdomain_dev_c", "bddcml_element_gradient_dev_c", "bddcml_set_adaptive_threshold_c",
            "bddcml_get_adaptive_info_c", "bddcml_upload_subdomain_rhs_batch_c", "bddcml_solve_batch_c",
-           "bddcml_download_local_solution_batch_c"]
+           "bddcml_download_local_solution_batch_c", "bddcml_set_batch_operator_c"]
 
 # phases of bddcml_get_profile_c (CUDA events on the solver stream)
 PHASES = ["numeric_total", "solve_total", "factor_interior", "solve_interior", "refine_residual", "schur",
@@ -251,6 +251,12 @@ def bddcml_solve_batch(nrhs: int, comm_all=0, method=0, tol=1e-8, maxit=1000, nd
                                cond.ctypes.data_as(C.POINTER(C.c_double)))
     _check()
     return it, reason, cond
+
+
+def set_batch_operator(mode: int) -> None:
+    """Batched Schur apply in mixed mode: 1 sliced bf16 tensor cores (default), 0 double-float SIMT."""
+    lib().bddcml_set_batch_operator_c(_i(mode))
+    _check()
 
 
 def bddcml_download_local_solution_batch(isub: int, nrhs: int, ndof: int) -> np.ndarray:

@@ -306,6 +306,15 @@ void bddcml_solve_batch_c(int* comm_all, int* method, double* tol, int* maxit, i
   });
 }
 
+void bddcml_set_batch_operator_c(int* mode) {
+  guarded("bddcml_set_batch_operator_c", [&] {
+    Solver* S = need_solver("bddcml_set_batch_operator_c");
+    if (!S) return;
+    if (*mode != 0 && *mode != 1) throw Error{ERR_ARGUMENT, "batch operator mode must be 0 or 1"};
+    S->prm.batch_operator = *mode;
+  });
+}
+
 void bddcml_download_local_solution_batch_c(int* isub, int* nrhs, double* sols, int* lsols) {
   guarded("bddcml_download_local_solution_batch_c", [&] {
     Solver* S = need_solver("bddcml_download_local_solution_batch_c");

@@ -24,11 +24,50 @@ static void gemm_t(Device& D, const GemmDesc* gd, int ndesc, int maxm, const T* 
   CKL();
 }
 
+// Slices of the Schur complements for the tensor-core apply (bddc_ozaki.cuh),
+// made once per batch setup from the float2 operator.
+static void batch_prepare_oz(Device& D) {
+  BatchBufs& B = D.bt;
+  auto& mem = B.mem;
+  vector<long long> soff(D.nsub), eoff(D.nsub), xoff(D.nsub);
+  long long ns = 0, ne = 0, nx = 0;
+  int maxrt = 0, maxch = 0;
+  for (int t = 0; t < D.nsub; ++t) {
+    const int ni = D.hs[t].ni;
+    const int nrt = (ni + OZ_M - 1) / OZ_M, nch = (ni + OZ_KC - 1) / OZ_KC;
+    soff[t] = ns; ns += (long long)nrt * nch * OZ_NS * OZ_AB;
+    eoff[t] = ne; ne += (long long)nrt * OZ_M;
+    xoff[t] = nx; nx += (long long)nch * OZ_BB;
+    maxrt = std::max(maxrt, nrt);
+    maxch = std::max(maxch, nch);
+  }
+  B.oz_nrt = maxrt;
+  B.oz_nch = maxch;
+  B.oz_s = dalloc<__nv_bfloat16>(std::max(1LL, ns), mem);
+  B.oz_x = dalloc<__nv_bfloat16>(std::max(1LL, nx), mem);
+  B.oz_erow = dalloc<int>(std::max(1LL, ne), mem);
+  B.oz_fcol = dalloc<int>((long long)D.nsub * BMAX, mem);
+  B.oz_soff = upload(soff, mem, D.st);
+  B.oz_eoff = upload(eoff, mem, D.st);
+  B.oz_xoff = upload(xoff, mem, D.st);
+  const float2* S = static_cast<const float2*>(D.poolS);
+  kb_oz_row_exp<<<dim3((maxrt * OZ_M + 7) / 8, D.nsub), 256, 0, D.st>>>(D.ds, S, B.oz_eoff, B.oz_erow);
+  CKL();
+  kb_oz_slice_s<<<dim3(maxrt * maxch, D.nsub), 256, 0, D.st>>>(D.ds, S, B.oz_soff, B.oz_eoff, B.oz_erow, B.oz_s);
+  CKL();
+  B.oz = true;
+}
+
 template <typename T>
-static void batch_prepare(Device& D, int nk, int lg, int maxit, int* shared_ndone, bool level2) {
+static void batch_prepare(Device& D, int nk, int lg, int maxit, int* shared_ndone, bool level2, int op = 0) {
   BatchBufs& B = D.bt;
   const int ldh = std::max(maxit + 2, 2);
-  if (B.nk == nk && B.ldh >= ldh && (shared_ndone == nullptr || B.ndone == shared_ndone)) return;
+  bool want_oz = false;
+  if (D.mixed && !level2 && op == 1) {
+    want_oz = true;
+    for (auto& d : D.hs) want_oz = want_oz && d.ni <= OZ_KMAX;
+  }
+  if (B.nk == nk && B.ldh >= ldh && (shared_ndone == nullptr || B.ndone == shared_ndone) && B.oz == want_oz) return;
   D.release_batch();
   auto& mem = B.mem;
   const long long n = D.n, nrep = D.nrep;
@@ -119,6 +158,7 @@ static void batch_prepare(Device& D, int nk, int lg, int maxit, int* shared_ndon
   B.gZ = upload(gz, mem, D.st);
   B.gX = upload(gx, mem, D.st);
   B.gC = upload(gc, mem, D.st);
+  if (want_oz) batch_prepare_oz(D);
 }
 
 // vout = sum_s R_s^T S_s R_s vin for every column; partial (dotvec, vout)_w into part
@@ -130,7 +170,18 @@ static void batch_schur(Device& D, const double* vin, double* vout, bool zero_fi
   const long long cnt = (long long)D.nrep << B.lg;
   const dim3 grid((D.maxNI + GM - 1) / GM, D.nsub);
   D.prof.begin(PH_SCHUR_APPLY, st);
-  if (D.mixed) {
+  if (B.oz) {
+    kb_oz_col_exp<<<D.nsub, 256, 0, st>>>(D.ds, B.lg, D.uniq, vin, B.oz_fcol, B.ndone);
+    CKL();
+    kb_oz_slice_x<<<dim3(B.oz_nch, D.nsub), 256, 0, st>>>(D.ds, B.lg, D.uniq, vin, B.oz_fcol, B.oz_xoff, B.oz_x,
+                                                          B.ndone);
+    CKL();
+    raise_smem(kb_schur_oz, OZ_SMEM);
+    kb_schur_oz<<<dim3(B.oz_nrt, D.nsub), OZ_THREADS, OZ_SMEM, st>>>(D.ds, B.oz_s, B.oz_soff, B.oz_eoff, B.oz_erow,
+                                                                    B.oz_x, B.oz_xoff, B.oz_fcol, B.yrep, B.nk, D.err,
+                                                                    B.ndone);
+    CKL();
+  } else if (D.mixed) {
     kb_gather_df<<<blocks_for(cnt), 256, 0, st>>>(D.nrep, B.lg, D.uniq, 1.0, vin, static_cast<float2*>(B.xs), B.ndone);
     CKL();
     kb_gemm_df<false><<<grid, 256, 0, st>>>(B.gS, static_cast<const float*>(D.poolS),
@@ -248,7 +299,7 @@ static void batch_solve_impl(Solver& S, int nrhs, double tol, int maxit, int nde
   const double t0 = wall_time();
   int nk = 4, lg = 2;  // at least 4 columns: the GEMM operand rows move in 16-byte pieces
   while (nk < nrhs) { nk <<= 1; ++lg; }
-  batch_prepare<T>(D, nk, lg, maxit, nullptr, false);
+  batch_prepare<T>(D, nk, lg, maxit, nullptr, false, S.prm.batch_operator);
   if (D.lev2) batch_prepare<double>(*D.lev2->dev, nk, lg, 0, D.bt.ndone, true);
   BatchBufs& B = D.bt;
   const long long n = D.n, nrep = D.nrep;
@@ -391,8 +442,14 @@ static void batch_solve_impl(Solver& S, int nrhs, double tol, int maxit, int nde
   CK(cudaMemcpyAsync(hdg.data(), B.diag, hdg.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(hsd.data(), B.subdiag, hsd.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
   g_d2h_bytes += (double)(hx.size() + hvo.size()) * sizeof(double);
+  int herr = 0;
+  CK(cudaMemcpyAsync(&herr, D.err, sizeof(int), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   D.prof.end(PH_SOLVE_TOTAL, st);
+  if (herr & DE_TIMEOUT) {
+    for (void* q : tmp) cudaFreeAsync(q, st);
+    throw Error{ERR_CUDA, "a bounded wait of the tensor-core Schur apply ran out"};
+  }
   for (void* q : tmp) cudaFreeAsync(q, st);
   const long long launches = g_launches - launches0;
   num_iter.assign(nrhs, 0);

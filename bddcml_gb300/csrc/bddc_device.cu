@@ -17,6 +17,7 @@
 
 #include "bddc_adaptive.cuh"
 #include "bddc_batch_kernels.cuh"
+#include "bddc_ozaki.cuh"
 #include "bddc_internal.hpp"
 #include "bddc_pcg_kernels.cuh"
 #include "bddc_tc.cuh"
@@ -185,6 +186,12 @@ struct BatchBufs {
   double *hist = nullptr, *diag = nullptr, *subdiag = nullptr;
   GemmDesc *gS = nullptr, *gZ = nullptr, *gX = nullptr, *gC = nullptr, *gP = nullptr;
   void* phit = nullptr;  // Phi^T per subdomain (working precision)
+  // sliced bf16 operands of the tensor-core Schur apply (mixed mode)
+  bool oz = false;
+  int oz_nrt = 0, oz_nch = 0;
+  __nv_bfloat16 *oz_s = nullptr, *oz_x = nullptr;
+  long long *oz_soff = nullptr, *oz_eoff = nullptr, *oz_xoff = nullptr;
+  int *oz_erow = nullptr, *oz_fcol = nullptr;
   // level-2 device only: interior loads, assembled reduced rhs, band block
   double *fi = nullptr, *g = nullptr, *bb = nullptr;
   BandDesc* bdB = nullptr;

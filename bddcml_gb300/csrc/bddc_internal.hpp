@@ -114,6 +114,7 @@ struct Params {
   int weights_type = 0;
   int matrixtype = 1;
   double adaptive_tau = 1.5;  // eigenvalue threshold of adaptive constraints (module_adaptivity.f90:30)
+  int batch_operator = 1;     // batched Schur apply in mixed mode: 0 double-float SIMT, 1 sliced bf16 tensor cores
 };
 
 struct Stats {

@@ -121,6 +121,15 @@ void bddcml_upload_subdomain_rhs_batch_c(int *isub, int *nrhs, double *rhss, int
 void bddcml_solve_batch_c(int *comm_all, int *method, double *tol, int *maxit, int *ndecrmax, int *nrhs,
                           int *num_iter, int *converged_reason, double *condition_number);
 
+/* Schur operator of the batched solve in mixed precision: 1 (default) slices
+ * S and every block of search directions into 6-bit integer pieces and
+ * multiplies them on the bf16 tensor cores with exact accumulation of the
+ * leading terms (FP64-class products; used when every subdomain has at most
+ * 3264 interface dofs, else mode 0); 0 multiplies the FP32 (hi, lo) pairs of S
+ * in double-float arithmetic on the FP32 pipes.  Takes effect at the next
+ * bddcml_solve_batch_c.  No counterpart in the reference. */
+void bddcml_set_batch_operator_c(int *mode);
+
 /* Solutions of the last batched solve for subdomain isub: nrhs columns of ndof
  * entries, column-major (*lsols = ndof * nrhs). */
 void bddcml_download_local_solution_batch_c(int *isub, int *nrhs, double *sols, int *lsols);
