@@ -107,21 +107,17 @@ static void batch_prepare(Device& D, int nk, int lg, int maxit, int* shared_ndon
   B.diag = dalloc<double>((long long)ldh * nk, mem);
   B.subdiag = dalloc<double>((long long)ldh * nk, mem);
   if (level2) {
+    B.fo = dalloc<double>(std::max(1LL, nuo) * nk, mem);
     B.fi = dalloc<double>(nrep * nk, mem);
     B.g = dalloc<double>(n * nk, mem);
     B.bb = dalloc<double>(std::max(1LL, nbb) * BMAX, mem);
     vector<long long> ro(D.nsub);
-    vector<BandDesc> bd(D.nsub);
     long long o = 0;
     for (int t = 0; t < D.nsub; ++t) {
       ro[t] = o;
-      bd[t] = D.hbd_oo[t];
-      bd[t].ncol = BMAX;
-      bd[t].oB = o * BMAX;
       o += D.hs[t].NO;
     }
     B.rowoff = upload(ro, mem, D.st);
-    B.bdB = upload(bd, mem, D.st);
   }
   // GEMM descriptors: Schur operator, [Z | Phi] with the coarse solution, interior resolve, coarse inverse
   vector<GemmDesc> gs(D.nsub), gz(D.nsub), gx(D.nsub);
@@ -158,6 +154,14 @@ static void batch_prepare(Device& D, int nk, int lg, int maxit, int* shared_ndon
   B.gZ = upload(gz, mem, D.st);
   B.gX = upload(gx, mem, D.st);
   B.gC = upload(gc, mem, D.st);
+  if (level2 && D.l2_ainv) {  // v = A_oo^-1 f_o: the interior solves of the level-2 subdomains
+    vector<GemmDesc> ga(D.nsub);
+    for (int t = 0; t < D.nsub; ++t) {
+      const DevSub& d = D.hs[t];
+      ga[t] = GemmDesc{D.l2_aoff[t], 0, D.huo_off[t], 0, ro[t], d.no, d.no, 0, d.NO, 0, 0};
+    }
+    B.gA = upload(ga, mem, D.st);
+  }
   if (want_oz) batch_prepare_oz(D);
 }
 
@@ -262,12 +266,12 @@ static void batch_level2(Device& D1, const double* rc, double* uc) {
   BatchBufs& B = D2.bt;
   cudaStream_t st = D1.st;
   const int nk = B.nk, lg = B.lg;
-  kb_l2_fill<<<dim3(blocks_for((long long)D2.maxNO * BMAX), D2.nsub), 256, 0, st>>>(
-      D2.ds, lg, B.rowoff, D2.uo_off, D2.l2_mo, rc, B.bb, B.ndone);
+  kb_l2_fo<<<blocks_for((long long)D2.l2_nfo << lg), 256, 0, st>>>(D2.l2_nfo, lg, D2.l2_mo, rc, B.fo, B.ndone);
   CKL();
   kb_l2_fi<<<blocks_for((long long)D2.nrep << lg), 256, 0, st>>>(D2.nrep, lg, D2.l2_mi, D2.l2_wi, rc, B.fi, B.ndone);
   CKL();
-  run_solve<double>(D2, B.bdB, D2.nsub, D2.maxnbo, BMAX, static_cast<const double*>(D2.poolT), B.bb);
+  // interior solves by the explicit inverses (one product per level-2 subdomain)
+  gemm_t<double>(D2, B.gA, D2.nsub, D2.maxNO, D2.l2_ainv, B.fo, nullptr, nk, B.bb, nullptr, BMAX, nk, B.ndone);
   kb_reduced_rhs<<<dim3(blocks_for((long long)D2.maxNI << lg), D2.nsub), 256, 0, st>>>(D2.ds, D2.kio, lg, B.rowoff,
                                                                                        B.bb, B.fi, B.grep, B.ndone);
   CKL();

@@ -619,20 +619,21 @@ __global__ void kb_update_p(int n, int lg, const PcgCtl* __restrict__ ctl, doubl
 }
 
 // ------------------------------------------------------------ three levels
-// level-2 interior loads into the band right-hand-side block (row stride BMAX,
-// padding rows and columns zero): bb[rowoff + r][k] = rc[mo[uo_off + r]][k]
-__global__ void kb_l2_fill(const DevSub* __restrict__ ds, int lg, const long long* __restrict__ rowoff,
-                           const long long* __restrict__ uo_off, const int* __restrict__ mo,
-                           const double* __restrict__ rc, double* __restrict__ bb, const int* __restrict__ ndone) {
+// identity right-hand side of every band system (row-major, ld = ncol)
+__global__ void k_band_identity(const BandDesc* __restrict__ bd, double* __restrict__ b) {
+  const BandDesc d = bd[blockIdx.y];
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < d.nb * NB && r < d.ncol) b[d.oB + (long long)r * d.ncol + r] = 1.0;
+}
+
+// level-2 interior loads fo[uo_off + r][k] = rc[mo[uo_off + r]][k]
+__global__ void kb_l2_fo(int nfo, int lg, const int* __restrict__ mo, const double* __restrict__ rc,
+                         double* __restrict__ fo, const int* __restrict__ ndone) {
   const int nk = 1 << lg;
   if (batch_all_done(ndone, nk)) return;
-  const DevSub s = ds[blockIdx.y];
   const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= (long long)s.NO * BMAX) return;
-  const int r = (int)(e / BMAX), k = (int)(e % BMAX);
-  double v = 0.0;
-  if (r < s.no && k < nk) v = rc[((long long)mo[uo_off[blockIdx.y] + r] << lg) + k];
-  bb[(rowoff[blockIdx.y] + r) * BMAX + k] = v;
+  if (e >= ((long long)nfo << lg)) return;
+  fo[e] = rc[((long long)mo[e >> lg] << lg) + (e & (nk - 1))];
 }
 
 // fi[j][k] = w_j rc[mi[j]][k] on the level-2 interface (zero where unmapped)

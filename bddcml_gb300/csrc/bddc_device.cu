@@ -192,9 +192,10 @@ struct BatchBufs {
   __nv_bfloat16 *oz_s = nullptr, *oz_x = nullptr;
   long long *oz_soff = nullptr, *oz_eoff = nullptr, *oz_xoff = nullptr;
   int *oz_erow = nullptr, *oz_fcol = nullptr;
-  // level-2 device only: interior loads, assembled reduced rhs, band block
-  double *fi = nullptr, *g = nullptr, *bb = nullptr;
-  BandDesc* bdB = nullptr;
+  // level-2 device only: interior loads, assembled reduced rhs, interior solutions (rows of
+  // BMAX columns)
+  double *fo = nullptr, *fi = nullptr, *g = nullptr, *bb = nullptr;
+  GemmDesc* gA = nullptr;
   long long* rowoff = nullptr;
 };
 
@@ -263,6 +264,8 @@ class Device {
   bool own_stream = true;
   Solver* lev2 = nullptr;
   int *l2_mo = nullptr, *l2_mi = nullptr, *l2_mz = nullptr;
+  double* l2_ainv = nullptr;       // explicit interior inverses A_oo^-1 (NO x NO per subdomain)
+  std::vector<long long> l2_aoff;  // their offsets
   double* l2_wi = nullptr;
   int l2_nfo = 0;
   int maxnbo = 0, maxw = 0, maxNR = 0;
@@ -287,6 +290,8 @@ class Device {
     rc_cap = rc_nact = 0;
     lev2 = nullptr;
     l2_mo = l2_mi = l2_mz = nullptr;
+    l2_ainv = nullptr;
+    l2_aoff.clear();
     l2_wi = nullptr;
     nv_off = nullptr;
     release_batch();
@@ -1968,6 +1973,28 @@ static void setup_level2(Solver& S, Device& D) {
       wi[D2.hs[t].rep + i] = q.wi[i];
       mz[q.uniq[i]] = g;
     }
+  }
+  // explicit interior inverses for the batched level-2 solves: A_oo X = I with the band factor
+  {
+    vector<BandDesc> bdi(D2.nsub);
+    long long na = 0;
+    int maxNO = 0;
+    D2.l2_aoff.assign(D2.nsub, 0);
+    for (int t = 0; t < D2.nsub; ++t) {
+      const DevSub& d2 = D2.hs[t];
+      D2.l2_aoff[t] = na;
+      bdi[t] = D2.hbd_oo[t];
+      bdi[t].ncol = d2.NO;
+      bdi[t].oB = na;
+      na += (long long)d2.NO * d2.NO;
+      maxNO = std::max(maxNO, d2.NO);
+    }
+    D2.l2_ainv = dalloc<double>(std::max(1LL, na), D2.owned);
+    CK(cudaMemsetAsync(D2.l2_ainv, 0, (size_t)std::max(1LL, na) * sizeof(double), st));
+    const BandDesc* dbi = upload(bdi, D2.owned, st);
+    k_band_identity<<<dim3((maxNO + 255) / 256, D2.nsub), 256, 0, st>>>(dbi, D2.l2_ainv);
+    CKL();
+    run_solve<double>(D2, dbi, D2.nsub, D2.maxnbo, maxNO, static_cast<const double*>(D2.poolT), D2.l2_ainv);
   }
   D2.l2_mo = upload(mo, D2.owned, st);
   D2.l2_mi = upload(mi, D2.owned, st);
