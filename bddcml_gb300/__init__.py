@@ -30,7 +30,8 @@ STAT_FIELDS = ["t_host_setup", "t_device_setup", "t_solve", "t_iterations", "t_p
                "t_host_iface", "t_host_globs", "t_host_blocks", "refine1", "refine2",
                "flop_sweep_oo", "flop_sweep_s", "bytes_residual", "bytes_schur_apply", "bytes_pc_local",
                "launches_setup", "launches_solve", "t_dev_alloc", "t_dev_h2d", "npair", "nadaptive",
-               "adapt_est", "t_adaptive", "lobpcg_resid", "lobpcg_iter"]
+               "adapt_est", "t_adaptive", "lobpcg_resid", "lobpcg_iter", "batch_bytes_schur",
+               "batch_flop_schur_mma", "batch_flop_schur", "batch_flop_pc", "batch_nk"]
 
 EXPORTS = ["bddcml_init_c", "bddcml_upload_global_data_c", "bddcml_upload_subdomain_data_c",
            "bddcml_setup_preconditioner_c", "bddcml_solve_c", "bddcml_download_local_solution_c",

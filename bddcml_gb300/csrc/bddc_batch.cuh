@@ -163,6 +163,41 @@ static void batch_prepare(Device& D, int nk, int lg, int maxit, int* shared_ndon
     B.gA = upload(ga, mem, D.st);
   }
   if (want_oz) batch_prepare_oz(D);
+  if (!level2) {  // multi-column interior solves of the loads and of the interior resolve
+    const int vld = D.mixed ? TC_M : NB;
+    const int ncomp = D.mixed ? 3 : 1;
+    vector<long long> vo(D.nsub);
+    long long nv = 0;
+    for (int t = 0; t < D.nsub; ++t) { vo[t] = nv; nv += (long long)ncomp * D.hs[t].NO * vld; }
+    B.vb = D.mixed ? (void*)dalloc<float>(std::max(1LL, nv), mem) : (void*)dalloc<double>(std::max(1LL, nv), mem);
+    B.voff = upload(vo, mem, D.st);
+    B.fin = dalloc<double>(std::max(1LL, nuo) * nk, mem);
+    B.ibuf = dalloc<double>(nrep * nk, mem);
+    if (D.mixed) {
+      vector<TcDesc> t0(D.nsub), t1(D.nsub), t2(D.nsub);
+      for (int t = 0; t < D.nsub; ++t) {
+        const long long comp = (long long)D.hs[t].NO * vld;
+        TcDesc c = D.htd_oo[t];
+        c.ncol = vld;
+        c.pad = 0;
+        c.oAcc = -1;
+        t0[t] = c; t0[t].oB = vo[t];
+        t1[t] = c; t1[t].oB = vo[t] + comp;
+        t2[t] = c; t2[t].oB = vo[t] + 2 * comp; t2[t].oAcc = vo[t] + comp;  // D2 is added into D1
+      }
+      B.tdv0 = upload(t0, mem, D.st);
+      B.tdv1 = upload(t1, mem, D.st);
+      B.tdv2 = upload(t2, mem, D.st);
+    } else {
+      vector<BandDesc> bv(D.nsub);
+      for (int t = 0; t < D.nsub; ++t) {
+        bv[t] = D.hbd_oo[t];
+        bv[t].ncol = vld;
+        bv[t].oB = vo[t];
+      }
+      B.bdv = upload(bv, mem, D.st);
+    }
+  }
 }
 
 // vout = sum_s R_s^T S_s R_s vin for every column; partial (dotvec, vout)_w into part
@@ -292,8 +327,31 @@ static void batch_level2(Device& D1, const double* rc, double* uc) {
   CKL();
 }
 
+// V = A_oo^-1 F for every column (F interleaved at the interior rows): the
+// tensor-core sweeps with two FP64-accurate refinement steps in mixed mode
+// (the scheme of the setup's interior solves), FP64 band solves in plain mode
 template <typename T>
-static void new_data_impl(Solver& S);
+static void batch_interior_solve(Device& D, const double* rhs) {
+  BatchBufs& B = D.bt;
+  cudaStream_t st = D.st;
+  const int vld = D.mixed ? TC_M : NB;
+  kb_v_fill<T><<<dim3(blocks_for((long long)D.maxNO * vld), D.nsub), 256, 0, st>>>(D.ds, B.lg, rhs, D.uo_off, B.voff,
+                                                                                  vld, static_cast<T*>(B.vb));
+  CKL();
+  if constexpr (std::is_same_v<T, float>) {
+    float* v = static_cast<float*>(B.vb);
+    run_solve_tc(D, B.tdv0, D.nsub, D.maxnbo, vld, D.ppool_oo, v, 3, false);
+    const dim3 gr((D.maxNO + 7) / 8, D.nsub);
+    kb_v_residual<<<gr, vld, 0, st>>>(D.ds, D.koo, B.lg, rhs, D.uo_off, B.voff, vld, v, 0, 1);
+    CKL();
+    run_solve_tc(D, B.tdv1, D.nsub, D.maxnbo, vld, D.ppool_oo, v, 3, false);
+    kb_v_residual<<<gr, vld, 0, st>>>(D.ds, D.koo, B.lg, rhs, D.uo_off, B.voff, vld, v, 1, 2);
+    CKL();
+    run_solve_tc(D, B.tdv2, D.nsub, D.maxnbo, vld, D.ppool_oo, v, 1, true);
+  } else {
+    run_solve<double>(D, B.bdv, D.nsub, D.maxnbo, vld, static_cast<const double*>(D.poolT), static_cast<double*>(B.vb));
+  }
+}
 
 template <typename T>
 static void batch_solve_impl(Solver& S, int nrhs, double tol, int maxit, int ndecrmax, vector<int>& num_iter,
@@ -306,14 +364,27 @@ static void batch_solve_impl(Solver& S, int nrhs, double tol, int maxit, int nde
   batch_prepare<T>(D, nk, lg, maxit, nullptr, false, S.prm.batch_operator);
   if (D.lev2) batch_prepare<double>(*D.lev2->dev, nk, lg, 0, D.bt.ndone, true);
   BatchBufs& B = D.bt;
+  {
+    double bs = 0, fm = 0, fs = 0, fp = 0;
+    for (auto& d : D.hs) {
+      const int nrt = (d.ni + OZ_M - 1) / OZ_M, nch = (d.ni + OZ_KC - 1) / OZ_KC;
+      bs += B.oz ? (double)nrt * nch * OZ_NS * OZ_AB * 2.0 : (double)d.ni * d.NI * (D.mixed ? 8.0 : 8.0);
+      fm += B.oz ? 2.0 * nrt * OZ_M * (double)nch * OZ_KC * BMAX * (OZ_NS * (OZ_NS + 1) / 2) : 0.0;
+      fs += 2.0 * d.ni * (double)d.ni * nk;
+      fp += 2.0 * d.ni * (double)(d.ni + 2 * d.nc) * nk;
+    }
+    S.stats.batch_bytes_schur = bs;
+    S.stats.batch_flop_schur_mma = fm;
+    S.stats.batch_flop_schur = fs;
+    S.stats.batch_flop_pc = fp;
+    S.stats.batch_nk = nk;
+  }
   const long long n = D.n, nrep = D.nrep;
   long long nfo = 0;
   for (auto& s : S.subs) nfo += s.ndofo;
-  // per-column reduced rhs g_k = f_i - A_io A_oo^-1 f_o and interior solutions
-  // A_oo^-1 f_o (module_dd.f90:6995-7257), one column at a time with the
-  // single-column interior solves and their refinement
-  ensure_nv<T>(D);
-  vector<double> hfo((size_t)std::max(1LL, nfo) * nrhs), hfi((size_t)std::max(1LL, nrep) * nrhs, 0.0);
+  // reduced rhs of every column g_k = f_i - A_io A_oo^-1 f_o (module_dd.f90:6995-7257)
+  // from one multi-column interior solve
+  vector<double> hfo((size_t)std::max(1LL, nfo) * nk, 0.0), hfi((size_t)nrep * nk, 0.0);
   {
     vector<long long> fooff(D.nsub);
     long long o = 0;
@@ -324,36 +395,25 @@ static void batch_solve_impl(Solver& S, int nrhs, double tol, int maxit, int nde
       vector<double> fo, fi;
       for (int k = 0; k < nrhs; ++k) {
         host_reduced_rhs_inputs(s, s.rhs_batch.data() + (size_t)k * s.ndof, s.rhs_batch_complete, fo, fi);
-        std::copy(fo.begin(), fo.end(), hfo.begin() + (size_t)k * std::max(1LL, nfo) + fooff[t]);
-        std::copy(fi.begin(), fi.end(), hfi.begin() + (size_t)k * std::max(1LL, nrep) + D.hs[t].rep);
+        for (int r = 0; r < s.ndofo; ++r) hfo[((size_t)fooff[t] + r) * nk + k] = fo[r];
+        for (int i = 0; i < s.ndofi; ++i) hfi[((size_t)D.hs[t].rep + i) * nk + k] = fi[i];
       }
     }
   }
   vector<void*> tmp;
-  double* dfo = dalloc<double>((long long)hfo.size(), tmp);
-  double* dfi = dalloc<double>((long long)hfi.size(), tmp);
-  CK(cudaMemcpyAsync(dfo, hfo.data(), hfo.size() * sizeof(double), cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(dfi, hfi.data(), hfi.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(B.fin, hfo.data(), hfo.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(B.ibuf, hfi.data(), hfi.size() * sizeof(double), cudaMemcpyHostToDevice, st));
   g_h2d_bytes += (double)(hfo.size() + hfi.size()) * sizeof(double);
   long long launches0 = g_launches;
   D.prof.begin(PH_SOLVE_TOTAL, st, true);
-  CK(cudaMemsetAsync(B.grep, 0, (size_t)nrep * nk * sizeof(double), st));
-  CK(cudaMemsetAsync(B.vo, 0, (size_t)std::max(1LL, nfo) * nk * sizeof(double), st));
-  double* fo_keep = D.fo;
-  double* fi_keep = D.fi;
-  for (int k = 0; k < nrhs; ++k) {
-    D.fo = dfo + (size_t)k * std::max(1LL, nfo);
-    D.fi = dfi + (size_t)k * std::max(1LL, nrep);
-    reduced_rhs_device<T>(D);
-    kb_put_col<<<blocks_for(nrep), 256, 0, st>>>(nrep, lg, k, D.grep, B.grep);
-    CKL();
-    kb_put_vo<T><<<dim3((D.maxNO + 127) / 128, D.nsub), 128, 0, st>>>(
-        D.ds, lg, k, static_cast<const T*>(D.nv_v0), std::is_same_v<T, float> ? static_cast<const T*>(D.nv_v1) : nullptr,
-        D.nv_off, D.uo_off, B.vo);
-    CKL();
-  }
-  D.fo = fo_keep;
-  D.fi = fi_keep;
+  const int vld = D.mixed ? TC_M : NB;
+  batch_interior_solve<T>(D, B.fin);
+  kb_v_grep<T><<<dim3(blocks_for((long long)D.maxNI << lg), D.nsub), 256, 0, st>>>(
+      D.ds, D.kio, lg, B.ibuf, B.voff, vld, static_cast<const T*>(B.vb), B.grep);
+  CKL();
+  kb_v_out<T><<<dim3(blocks_for((long long)D.maxNO << lg), D.nsub), 256, 0, st>>>(
+      D.ds, lg, B.voff, vld, static_cast<const T*>(B.vb), D.uo_off, B.vo);
+  CKL();
   // initial guess: the fixed values at fixed interface dofs, zero elsewhere
   bool x0_nonzero = false;
   {
@@ -419,15 +479,15 @@ static void batch_solve_impl(Solver& S, int nrhs, double tol, int maxit, int nde
   }
   D.prof.end(PH_PCG, st);
   S.stats.t_iterations = wall_time() - tl;
-  // interior values u_o = A_oo^-1 f_o - X x for every column (module_dd.f90:6811-6932)
+  // interior values u_o = A_oo^-1 f_o - X x for every column (module_dd.f90:6811-6932),
+  // X = A_oo^-1 A_oi from the setup
   D.prof.begin(PH_POST, st);
-  const dim3 gpost((D.maxNO + GM - 1) / GM, D.nsub);
   if (D.mixed) {
     kb_gather_df<<<blocks_for(nrep << lg), 256, 0, st>>>(nrep, lg, D.uniq, -1.0, B.x, static_cast<float2*>(B.xs),
                                                          nullptr);
     CKL();
-    kb_gemm_df<true><<<gpost, 256, 0, st>>>(B.gX, static_cast<const float*>(D.poolT),
-                                            static_cast<const float2*>(B.xs), nk, B.vo, B.vo, nk, nk, nullptr);
+    kb_gemm_df<true><<<dim3((D.maxNO + GM - 1) / GM, D.nsub), 256, 0, st>>>(
+        B.gX, static_cast<const float*>(D.poolT), static_cast<const float2*>(B.xs), nk, B.vo, B.vo, nk, nk, nullptr);
     CKL();
   } else {
     kb_gather_t<double><<<blocks_for(nrep << lg), 256, 0, st>>>(nrep, lg, D.uniq, nullptr, -1.0, B.x,
@@ -482,8 +542,6 @@ static void batch_solve_impl(Solver& S, int nrhs, double tol, int maxit, int nde
     }
   }
   D.prof.collect();
-  // the single-column state (reduced rhs of the subdomains' own loads) for later solves
-  new_data_impl<T>(S);
   S.stats.h2d_bytes = g_h2d_bytes;
   S.stats.d2h_bytes = g_d2h_bytes;
   S.stats.t_solve = wall_time() - t0;

@@ -469,24 +469,89 @@ __global__ void kb_bcast(int n, int lg, const double* __restrict__ x0, double* _
   if (e < ((long long)n << lg)) x[e] = x0[e >> lg];
 }
 
-// dst[i][k] = src[i] for one column k
-__global__ void kb_put_col(long long cnt, int lg, int k, const double* __restrict__ src, double* __restrict__ dst) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < cnt) dst[(i << lg) + k] = src[i];
+// ------------------------------------------- multi-column interior solves
+// Blocks V of NO rows x vld columns per subdomain at voff (row-major); the
+// right-hand sides are interleaved rows (fo_off + r) x nk.
+template <typename T>
+__global__ void kb_v_fill(const DevSub* __restrict__ ds, int lg, const double* __restrict__ rhs,
+                          const long long* __restrict__ fo_off, const long long* __restrict__ voff, int vld,
+                          T* __restrict__ v) {
+  const int nk = 1 << lg;
+  const DevSub s = ds[blockIdx.y];
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (long long)s.NO * vld) return;
+  const int r = (int)(e / vld), k = (int)(e % vld);
+  v[voff[blockIdx.y] + e] = (r < s.no && k < nk) ? T(rhs[((fo_off[blockIdx.y] + r) << lg) + k]) : T(0);
 }
 
-// interior solution of one column's interior loads (v0 [+ v1]) into vo[uo_off + r][k]
-template <typename T>
-__global__ void kb_put_vo(const DevSub* __restrict__ ds, int lg, int k, const T* __restrict__ v0,
-                          const T* __restrict__ v1, const long long* __restrict__ voff,
-                          const long long* __restrict__ uo_off, double* __restrict__ vo) {
+// component outc = F - A_oo (X0 [+ D1]) with FP64-accurate double-float sums,
+// stored as FP32 (the refinement residuals of the mixed-precision solves);
+// grid (ceil(maxNO / 8), nsub), vld threads (one per column), 8 rows per CTA
+__global__ void kb_v_residual(const DevSub* __restrict__ ds, CsrView koo, int lg, const double* __restrict__ rhs,
+                              const long long* __restrict__ fo_off, const long long* __restrict__ voff, int vld,
+                              float* __restrict__ v, int xpair, int outc) {
+  const int nk = 1 << lg;
   const DevSub s = ds[blockIdx.y];
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= s.no) return;
-  const long long o = voff[blockIdx.y] + r;
-  double v = (double)v0[o];
-  if (v1) v += (double)v1[o];
-  vo[((uo_off[blockIdx.y] + r) << lg) + k] = v;
+  const int k = threadIdx.x;
+  const long long comp = (long long)s.NO * vld;
+  const float* X0 = v + voff[blockIdx.y];
+  const float* X1 = X0 + comp;
+  float* out = v + voff[blockIdx.y] + outc * comp;
+  const int* p = koo.ptr + s.koo;
+  for (int r = blockIdx.x * 8; r < min(s.NO, blockIdx.x * 8 + 8); ++r) {
+    float res = 0.f;
+    if (r < s.no && k < nk) {
+      dfacc acc;
+      acc.add_df(df_from_double(rhs[((fo_off[blockIdx.y] + r) << lg) + k]));
+      for (int q = p[r]; q < p[r + 1]; ++q) {
+        const long long o = (long long)koo.col[q] * vld + k;
+        const dfloat a = df_from_double(-koo.val[q]);
+        if (xpair) acc.fma_df(a, dfloat{X0[o], X1[o]});
+        else acc.fma_df(a, X0[o]);
+      }
+      res = acc.value().hi;
+    }
+    out[(long long)r * vld + k] = res;
+  }
+}
+
+// value of the interior solution V[r][k]: the FP32 pair (X0, D1) or the FP64 block
+__device__ __forceinline__ double v_value(const float* v, long long comp, long long o) {
+  return (double)v[o] + (double)v[comp + o];
+}
+__device__ __forceinline__ double v_value(const double* v, long long, long long o) { return v[o]; }
+
+// grep[rep + i][k] = f_i - A_io V  (module_dd.f90:6995-7257), double-float sums
+template <typename T>
+__global__ void kb_v_grep(const DevSub* __restrict__ ds, CsrView kio, int lg, const double* __restrict__ fi,
+                          const long long* __restrict__ voff, int vld, const T* __restrict__ v,
+                          double* __restrict__ grep) {
+  const int nk = 1 << lg;
+  const DevSub s = ds[blockIdx.y];
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ((long long)s.ni << lg)) return;
+  const int i = (int)(e >> lg), k = (int)(e & (nk - 1));
+  const long long o = ((long long)(s.rep + i) << lg) + k;
+  const T* V = v + voff[blockIdx.y];
+  const long long comp = (long long)s.NO * vld;
+  dfacc acc;
+  acc.add_df(df_from_double(fi[o]));
+  const int* p = kio.ptr + s.kio;
+  for (int q = p[i]; q < p[i + 1]; ++q)
+    acc.fma_df(df_from_double(-kio.val[q]), df_from_double(v_value(V, comp, (long long)kio.col[q] * vld + k)));
+  grep[o] = acc.to_double();
+}
+
+// vo[uo_off + r][k] = V[r][k]
+template <typename T>
+__global__ void kb_v_out(const DevSub* __restrict__ ds, int lg, const long long* __restrict__ voff, int vld,
+                         const T* __restrict__ v, const long long* __restrict__ uo_off, double* __restrict__ vo) {
+  const int nk = 1 << lg;
+  const DevSub s = ds[blockIdx.y];
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ((long long)s.no << lg)) return;
+  const int r = (int)(e >> lg), k = (int)(e & (nk - 1));
+  vo[((uo_off[blockIdx.y] + r) << lg) + k] = v_value(v + voff[blockIdx.y], (long long)s.NO * vld, (long long)r * vld + k);
 }
 
 // ---------------------------------------------------------------- scalars

@@ -196,6 +196,13 @@ struct BatchBufs {
   // BMAX columns)
   double *fo = nullptr, *fi = nullptr, *g = nullptr, *bb = nullptr;
   GemmDesc* gA = nullptr;
+  // level 1: multi-column interior solves A_oo V = F (components X0, D1, D2 of
+  // NO x VB_COLS per subdomain in mixed mode, one FP64 block in plain mode)
+  void* vb = nullptr;
+  long long* voff = nullptr;
+  TcDesc *tdv0 = nullptr, *tdv1 = nullptr, *tdv2 = nullptr;
+  BandDesc* bdv = nullptr;
+  double *fin = nullptr, *ibuf = nullptr;  // staged loads (interior rows, interface rows) x nk
   long long* rowoff = nullptr;
 };
 
@@ -248,6 +255,8 @@ class Device {
   double* scal = nullptr;  // scratch scalar
   BandDesc* bd_oo = nullptr;
   std::vector<BandDesc> hbd_oo;
+  std::vector<TcDesc> htd_oo;  // tensor-core sweep descriptors of the interior systems (mixed)
+  float* ppool_oo = nullptr;   // their panels
   // one-vector interior solves for new loads after setup (allocated on first use)
   void* nv_v0 = nullptr;
   void* nv_v1 = nullptr;
@@ -294,6 +303,8 @@ class Device {
     l2_aoff.clear();
     l2_wi = nullptr;
     nv_off = nullptr;
+    htd_oo.clear();
+    ppool_oo = nullptr;
     release_batch();
     release_pc();
     for (void* q : owned) cudaFreeAsync(q, st);
@@ -681,6 +692,8 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
     }
     td_oo = upload(htd, own, st);
     run_panels(D, D.bd_oo, td_oo, nsub, D.maxnbo, D.maxw, poolT, ppool);
+    D.htd_oo = htd;
+    D.ppool_oo = ppool;
   }
   D.prof.end(PH_FACTOR_OO, st);
   // ---- interior solves [X | v] = A_oo^-1 [A_oi | f_o], refined in mixed precision

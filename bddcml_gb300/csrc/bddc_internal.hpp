@@ -128,6 +128,10 @@ struct Stats {
   double h2d_bytes = 0, d2h_bytes = 0;
   double t_upload = 0, t_host_assemble = 0, t_host_iface = 0, t_host_globs = 0, t_host_blocks = 0;
   double refine1 = 0, refine2 = 0;  // max |correction| / max |X| of refinement steps 1, 2
+  // batched solve, per Schur / preconditioner apply: operator bytes streamed, tensor-core
+  // flops executed (sliced operator), FP64-equivalent flops of S X, working-precision
+  // flops of the local preconditioner products, and the batch width
+  double batch_bytes_schur = 0, batch_flop_schur_mma = 0, batch_flop_schur = 0, batch_flop_pc = 0, batch_nk = 0;
   // algorithmic work per launch of the main phases (for roofline reporting)
   double flop_sweep_oo = 0;     // one forward + backward interior sweep, all subdomains (FP32 flop)
   double flop_sweep_s = 0;      // one forward + backward preconditioner-block sweep
