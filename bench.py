@@ -60,6 +60,9 @@ WORKLOADS = {
     # the same problem with 64 load cases (every element's body force scaled by
     # its own iid N(0, 1) factor per case, seed 5) solved by one batched PCG
     "elasticity_96^3_512subs_3levels_64rhs": ("elasticity", (12, 8, 8, 64), 1, None),
+    # the same subdomain size on 48^3 with 64 subdomains (8 level-2 subdomains): the
+    # small case of the batched kernels for parity runs and full profiler captures
+    "elasticity_48^3_64subs_3levels_64rhs": ("elasticity", (12, 4, 8, 64), 1, None),
 }
 DEFAULT_WORKLOAD = "poisson_128^3_512subs"
 
