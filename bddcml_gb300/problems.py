@@ -302,8 +302,9 @@ def global_matrix_and_rhs(prob: Problem):
     for s in prob.subdomains:
         g = s.isvgvn
         rows.append(g[s.i_sparse]); cols.append(g[s.j_sparse]); vals.append(s.a_sparse)
-        off = s.i_sparse != s.j_sparse
-        rows.append(g[s.j_sparse[off]]); cols.append(g[s.i_sparse[off]]); vals.append(s.a_sparse[off])
+        if prob.matrixtype != 0:  # upper-triangle storage of a symmetric matrix
+            off = s.i_sparse != s.j_sparse
+            rows.append(g[s.j_sparse[off]]); cols.append(g[s.i_sparse[off]]); vals.append(s.a_sparse[off])
         fixed[g[s.ifix != 0]] = True
         np.add.at(f, g, s.rhs)
         np.add.at(cnt, g, 1.0)
@@ -461,3 +462,45 @@ def body_force_loads(prob: Problem, nrhs: int, seed: int = 5) -> list:
             r[2::3] = f[s.isngn]
             r[s.ifix != 0] = 0.0
     return out
+
+
+def q1_convection_reference_matrix(b) -> np.ndarray:
+    """Galerkin convection matrix C[i][j] = int phi_i (b . grad phi_j) of the Q1
+    element [0,1]^3 (node order of q1_laplace_reference_matrix).  The trilinear
+    basis is a product of 1D hats, so every entry is a product of the 1D mass
+    matrix [[2,1],[1,2]]/6 and the 1D convection matrix [[-1,1],[-1,1]]/2 (rows:
+    test function, columns: derivative of the trial function); on an element
+    of size h the matrix scales with h^2."""
+    m1 = np.array([[2.0, 1.0], [1.0, 2.0]]) / 6.0
+    d1 = np.array([[-0.5, 0.5], [-0.5, 0.5]])
+    c = np.zeros((8, 8))
+    for i in range(8):
+        for j in range(8):
+            oi, oj = _NODE_OFFSETS[i], _NODE_OFFSETS[j]
+            f = [m1[oi[a], oj[a]] for a in range(3)]
+            g = [d1[oi[a], oj[a]] for a in range(3)]
+            c[i, j] = b[0] * g[0] * f[1] * f[2] + b[1] * f[0] * g[1] * f[2] + b[2] * f[0] * f[1] * g[2]
+    return c
+
+
+def convection_diffusion_on_cube(num_el_per_sub_edge: int, num_sub_per_cube_edge: int,
+                                 b=(10.0, 7.0, 4.0)) -> Problem:
+    """-Laplace(u) + b . grad(u) = 1 on the unit cube, u = 0 on the boundary,
+    Q1 hexahedra, cubic subdomains: a nonsymmetric problem (matrixtype 0).
+    Element matrices h K_laplace + h^2 C(b) are given in full (all 64 pairs),
+    as the reference expects for general matrices."""
+    n = num_el_per_sub_edge * num_sub_per_cube_edge
+    h = 1.0 / n
+    km = h * q1_laplace_reference_matrix() + h * h * q1_convection_reference_matrix(b)
+    subs = []
+    for isub, (lo, hi) in enumerate(_sub_ranges_uniform(num_el_per_sub_edge, num_sub_per_cube_edge)):
+        sd = box_subdomain(isub, lo, hi, n, None, q1_laplace_reference_matrix())
+        inet_e = sd.inet.reshape(sd.nelems, 8)
+        ii, jj = np.meshgrid(np.arange(8), np.arange(8), indexing="ij")
+        sd.i_sparse = inet_e[:, ii.ravel()].astype(np.int32).ravel()
+        sd.j_sparse = inet_e[:, jj.ravel()].astype(np.int32).ravel()
+        sd.a_sparse = np.tile(km[ii.ravel(), jj.ravel()], sd.nelems)
+        subs.append(sd)
+    return Problem(name=f"convection_diffusion_{n}^3_{num_sub_per_cube_edge}^3subs", nelem=n ** 3,
+                   nnod=(n + 1) ** 3, ndof=(n + 1) ** 3, ndim=3, meshdim=3, subdomains=subs,
+                   matrixtype=0, n_el_edge=n)

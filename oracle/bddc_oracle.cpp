@@ -129,6 +129,95 @@ static void dense_chol_solve(const vector<double>& l, int n, double* x) {
   }
 }
 
+// General band matrix (nonsymmetric, matrixtype 0): A(i,j) for |i-j| <= b at
+// v[i*(2b+1) + (j-i+b)], LU without pivoting in place (unit lower L, upper U).
+// MUMPS factors the reference's general subdomain matrices with pivoting
+// (module_mumps.f90:443-511); the test problems (convection-diffusion with cell
+// Peclet numbers below 1) are diagonally dominant, where no pivot is needed.
+struct BandLU {
+  int n = 0, b = 0;
+  vector<double> v;
+  double& at(int i, int j) { return v[(size_t)i * (2 * b + 1) + (j - i + b)]; }
+  double at(int i, int j) const { return v[(size_t)i * (2 * b + 1) + (j - i + b)]; }
+  void factor() {
+    for (int k = 0; k < n; ++k) {
+      const double piv = at(k, k);
+      if (!(std::fabs(piv) > 0.0)) throw std::runtime_error("band LU: zero pivot");
+      for (int i = k + 1; i <= std::min(n - 1, k + b); ++i) {
+        const double l = at(i, k) / piv;
+        at(i, k) = l;
+        if (l == 0.0) continue;
+        for (int j = k + 1; j <= std::min(n - 1, k + b); ++j) at(i, j) -= l * at(k, j);
+      }
+    }
+  }
+  void solve(double* x) const {  // L U x = rhs, in place
+    for (int i = 0; i < n; ++i) {
+      double t = x[i];
+      for (int j = std::max(0, i - b); j < i; ++j) t -= at(i, j) * x[j];
+      x[i] = t;
+    }
+    for (int i = n - 1; i >= 0; --i) {
+      double t = x[i];
+      for (int j = i + 1; j <= std::min(n - 1, i + b); ++j) t -= at(i, j) * x[j];
+      x[i] = t / at(i, i);
+    }
+  }
+  void solve_t(double* x) const {  // (L U)^T x = rhs: U^T then L^T, in place
+    for (int i = 0; i < n; ++i) {
+      double t = x[i];
+      for (int j = std::max(0, i - b); j < i; ++j) t -= at(j, i) * x[j];
+      x[i] = t / at(i, i);
+    }
+    for (int i = n - 1; i >= 0; --i) {
+      double t = x[i];
+      for (int j = i + 1; j <= std::min(n - 1, i + b); ++j) t -= at(j, i) * x[j];
+      x[i] = t;
+    }
+  }
+};
+
+// dense LU with partial pivoting (small general matrices: G = C A^-1 C^T and the
+// coarse matrix of a nonsymmetric problem), row-major n x n, in place
+static void dense_lu(vector<double>& a, int n, vector<int>& piv) {
+  piv.resize(n);
+  for (int k = 0; k < n; ++k) {
+    int p = k;
+    for (int i = k + 1; i < n; ++i)
+      if (std::fabs(a[(size_t)i * n + k]) > std::fabs(a[(size_t)p * n + k])) p = i;
+    piv[k] = p;
+    if (p != k)
+      for (int j = 0; j < n; ++j) std::swap(a[(size_t)k * n + j], a[(size_t)p * n + j]);
+    const double d = a[(size_t)k * n + k];
+    if (!(std::fabs(d) > 0.0)) throw std::runtime_error("dense LU: singular matrix");
+    for (int i = k + 1; i < n; ++i) {
+      const double l = a[(size_t)i * n + k] / d;
+      a[(size_t)i * n + k] = l;
+      for (int j = k + 1; j < n; ++j) a[(size_t)i * n + j] -= l * a[(size_t)k * n + j];
+    }
+  }
+}
+// x <- A^-1 x (trans = false) or A^-T x (trans = true) with the factors of dense_lu
+static void dense_lu_solve(const vector<double>& a, int n, const vector<int>& piv, double* x, bool trans) {
+  if (!trans) {
+    for (int k = 0; k < n; ++k) std::swap(x[k], x[piv[k]]);
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < i; ++j) x[i] -= a[(size_t)i * n + j] * x[j];
+    for (int i = n - 1; i >= 0; --i) {
+      for (int j = i + 1; j < n; ++j) x[i] -= a[(size_t)i * n + j] * x[j];
+      x[i] /= a[(size_t)i * n + i];
+    }
+  } else {
+    for (int i = 0; i < n; ++i) {
+      for (int j = 0; j < i; ++j) x[i] -= a[(size_t)j * n + i] * x[j];
+      x[i] /= a[(size_t)i * n + i];
+    }
+    for (int i = n - 1; i >= 0; --i)
+      for (int j = i + 1; j < n; ++j) x[i] -= a[(size_t)j * n + i] * x[j];
+    for (int k = n - 1; k >= 0; --k) std::swap(x[k], x[piv[k]]);
+  }
+}
+
 // COO sort + merge of duplicates (module_sm.f90:630-684 sm_assembly)
 static void coo_assemble(vector<int>& ia, vector<int>& ja, vector<double>& a) {
   size_t n = ia.size();
@@ -202,6 +291,14 @@ struct Sub {
   vector<int> a12_ptr, a12_col; vector<double> a12_val;  // CSR rows = interior, cols = interface
   vector<int> a22_ptr, a22_col; vector<double> a22_val;  // full symmetric CSR on interface
   Band aug;                 // A + corner shifts, full subdomain order
+  // matrixtype 0 (general): LU factors in place of the Cholesky factors, the
+  // interface-row block A_io, the dual basis from the adjoint problem
+  // (module_dd.f90:5687-5757) and the LU pivots of G
+  BandLU a11lu, auglu;
+  vector<int> a21_ptr, a21_col; vector<double> a21_val;  // CSR rows = interface, cols = interior
+  vector<double> ydual;     // ndof x nconstr: A_r^-T C^T
+  vector<double> phisi_dual;
+  vector<int> gpiv;
   vector<double> yaug;      // ndof x nconstr (column-major: yaug[c*ndof + i])
   vector<double> gchol;     // nconstr x nconstr Cholesky of C A_r^-1 C^T
   vector<double> phisi;     // ndofi x nconstr (column-major)
@@ -219,7 +316,8 @@ struct Oracle {
   vector<Sub> subs;
   bool setup_done = false;
   int ncorner = 0, nedge = 0, nface = 0, ndofc = 0;
-  vector<double> coarse_chol;  // dense Cholesky of the coarse matrix
+  vector<double> coarse_chol;  // dense Cholesky of the coarse matrix (LU for matrixtype 0)
+  vector<int> coarse_piv;
   vector<int> ncdof_of_cnode;  // nndfc
   // adaptive face constraints (module_adaptivity.f90)
   bool adaptive = false;
@@ -268,6 +366,19 @@ static void csr_mult(const vector<int>& ptr, const vector<int>& col, const vecto
     for (int k = ptr[i]; k < ptr[i + 1]; ++k) s += val[k] * x[col[k]];
     y[i] = s;
   }
+}
+
+// CSR rows of a general (matrixtype 0) COO matrix
+static void csr_from_full(int n, const vector<int>& ia, const vector<int>& ja, const vector<double>& a,
+                          vector<int>& ptr, vector<int>& col, vector<double>& val) {
+  vector<int> cnt(n + 1, 0);
+  for (size_t k = 0; k < ia.size(); ++k) cnt[ia[k] + 1]++;
+  for (int i = 0; i < n; ++i) cnt[i + 1] += cnt[i];
+  ptr = cnt;
+  col.assign(ptr[n], 0);
+  val.assign(ptr[n], 0.0);
+  vector<int> pos(ptr.begin(), ptr.end() - 1);
+  for (size_t k = 0; k < ia.size(); ++k) { col[pos[ia[k]]] = ja[k]; val[pos[ia[k]]++] = a[k]; }
 }
 
 // nodal components from the dual mesh graph (module_dd.f90:2516-2770):
@@ -938,13 +1049,38 @@ int oracle_upload(void* h, int isub, int nelem, int nnod, int ndof, int ndim,
   S.ia.assign(i_sparse, i_sparse + la);
   S.ja.assign(j_sparse, j_sparse + la);
   S.a.assign(a_sparse, a_sparse + la);
-  for (int k = 0; k < la; ++k)
-    if (S.ia[k] > S.ja[k]) { o->err = "only the upper triangle is expected"; return 2; }
+  if (matrixtype != 0)  // symmetric storage: upper triangle (module_levels.f90:748-752)
+    for (int k = 0; k < la; ++k)
+      if (S.ia[k] > S.ja[k]) { o->err = "only the upper triangle is expected"; return 2; }
   coo_assemble(S.ia, S.ja, S.a);
   S.bc_present = false;
   for (int i = 0; i < ndof; ++i) if (S.ifix[i] != 0) S.bc_present = true;
   nodal_components(S, find_components != 0, neighbouring);
   return 0;
+}
+
+// interior and augmented solves: Cholesky factors for symmetric matrices, LU for general ones
+static void a11_solve(const Sub& S, double* x) {
+  if (S.matrixtype == 0) S.a11lu.solve(x);
+  else S.a11.solve(x);
+}
+static void aug_solve(const Sub& S, double* x) {
+  if (S.matrixtype == 0) S.auglu.solve(x);
+  else S.aug.solve(x);
+}
+// yi += A_io xo (interface rows): from A_oi^T for symmetric matrices, the
+// interface rows themselves for general ones
+static void a21_apply_add(const Sub& S, const double* xo, double* yi) {
+  if (S.matrixtype == 0) {
+    for (int i = 0; i < S.ndofi; ++i) {
+      double t = 0.0;
+      for (int k = S.a21_ptr[i]; k < S.a21_ptr[i + 1]; ++k) t += S.a21_val[k] * xo[S.a21_col[k]];
+      yi[i] += t;
+    }
+  } else {
+    for (int io = 0; io < S.ndofo; ++io)
+      for (int k = S.a12_ptr[io]; k < S.a12_ptr[io + 1]; ++k) yi[S.a12_col[k]] += S.a12_val[k] * xo[io];
+  }
 }
 
 static void comm_exchange(Oracle& o, vector<vector<double>>& v, bool keep_own) {
@@ -1329,10 +1465,9 @@ static void reduced_rhs(Oracle& oo) {
       }
       S.solo.assign(S.ndofo, 0.0);
       for (int i = 0; i < S.ndofo; ++i) S.solo[i] = rhs[S.iovsvn[i]];
-      if (S.ndofo > 0) S.a11.solve(S.solo.data());
+      if (S.ndofo > 0) a11_solve(S, S.solo.data());
       g[s].assign(S.ndofi, 0.0);
-      for (int io = 0; io < S.ndofo; ++io)
-        for (int k = S.a12_ptr[io]; k < S.a12_ptr[io + 1]; ++k) g[s][S.a12_col[k]] += S.a12_val[k] * S.solo[io];
+      a21_apply_add(S, S.solo.data(), g[s].data());
       for (int i = 0; i < S.ndofi; ++i) g[s][i] = rhs[S.iivsvn[i]] - g[s][i];
     }
     comm_exchange_add(*o, g);
@@ -1372,6 +1507,7 @@ extern "C" int oracle_setup(void* h, int use_corner_constraints, int use_arithme
 // nodes = level-1 coarse nodes (corner: its node, edge / face: mean of the glob's
 // nodes), elements = level-1 subdomains with their coarse matrices Phi^T A Phi
 static void build_level2(Oracle& o) {
+
   const int nsub = o.nsub;
   const int ndim = o.subs[0].ndim;
   const int ncnode = o.ncorner + o.nedge + o.nface;
@@ -1459,6 +1595,14 @@ static void build_level2(Oracle& o) {
 }
 
 int oracle_setup(void* h, int use_corner_constraints, int use_arithmetic_constraints, int weights_type) {
+  {
+    auto* og = static_cast<Oracle*>(h);
+    const bool gen = !og->subs.empty() && og->subs[0].matrixtype == 0;
+    if (gen && (og->adaptive || og->nlevels == 3)) {
+      og->err = "adaptive constraints and three levels need a symmetric matrix";
+      return 1;
+    }
+  }
   auto* o = static_cast<Oracle*>(h);
   try {
     int nsub = o->nsub;
@@ -1474,11 +1618,13 @@ int oracle_setup(void* h, int use_corner_constraints, int use_arithmetic_constra
       if (S.bc_present) {
         vector<char> diag_fixed(S.ndof, 0);
         S.fx_i.clear(); S.fx_j.clear(); S.fx_v.clear();
+        const bool sym = S.matrixtype != 0;
         for (size_t k = 0; k < S.ia.size(); ++k) {
           int i = S.ia[k], j = S.ja[k];
-          if (S.ifix[i] || S.ifix[j]) { S.fx_i.push_back(i); S.fx_j.push_back(j); S.fx_v.push_back(S.a[k]); }
+          if (S.ifix[i] || (sym && S.ifix[j])) { S.fx_i.push_back(i); S.fx_j.push_back(j); S.fx_v.push_back(S.a[k]); }
           if (i != j) {
-            if (S.ifix[i] && S.fixv[i] != 0.0 && S.a[k] != 0.0 && !S.ifix[j]) S.bc[j] -= S.a[k] * S.fixv[i];
+            // a fixed row moves into the rhs only in symmetric storage (module_sm.f90:528-541)
+            if (sym && S.ifix[i] && S.fixv[i] != 0.0 && S.a[k] != 0.0 && !S.ifix[j]) S.bc[j] -= S.a[k] * S.fixv[i];
             if (S.ifix[j] && S.fixv[j] != 0.0 && S.a[k] != 0.0 && !S.ifix[i]) S.bc[i] -= S.a[k] * S.fixv[j];
             if (S.ifix[i] || S.ifix[j]) S.a[k] = 0.0;
           } else if (S.ifix[i]) {
@@ -1540,7 +1686,8 @@ int oracle_setup(void* h, int use_corner_constraints, int use_arithmetic_constra
     for (int s = 0; s < nsub; ++s) {
       try {
         auto& S = o->subs[s];
-        sym_csr_from_upper(S.ndof, S.ia, S.ja, S.a, S.f_ptr, S.f_col, S.f_val);
+        if (S.matrixtype == 0) csr_from_full(S.ndof, S.ia, S.ja, S.a, S.f_ptr, S.f_col, S.f_val);
+        else sym_csr_from_upper(S.ndof, S.ia, S.ja, S.a, S.f_ptr, S.f_col, S.f_val);
         // blocks
         vector<int> mo(S.ndof, -1), mi(S.ndof, -1);
         for (int i = 0; i < S.ndofo; ++i) mo[S.iovsvn[i]] = i;
@@ -1557,37 +1704,64 @@ int oracle_setup(void* h, int use_corner_constraints, int use_arithmetic_constra
           }
           S.a12_ptr[io + 1] = (int)S.a12_col.size();
         }
+        S.a21_ptr.assign(S.ndofi + 1, 0); S.a21_col.clear(); S.a21_val.clear();
         for (int ii = 0; ii < S.ndofi; ++ii) {
           int r = S.iivsvn[ii];
           for (int k = S.f_ptr[r]; k < S.f_ptr[r + 1]; ++k) {
             int c = S.f_col[k];
             if (mi[c] >= 0) { S.a22_col.push_back(mi[c]); S.a22_val.push_back(S.f_val[k]); }
+            else if (S.matrixtype == 0) { S.a21_col.push_back(mo[c]); S.a21_val.push_back(S.f_val[k]); }
           }
           S.a22_ptr[ii + 1] = (int)S.a22_col.size();
+          S.a21_ptr[ii + 1] = (int)S.a21_col.size();
         }
-        S.a11.n = S.ndofo; S.a11.b = b11;
-        S.a11.v.assign((size_t)S.ndofo * (b11 + 1), 0.0);
-        for (int io = 0; io < S.ndofo; ++io) {
-          int r = S.iovsvn[io];
-          for (int k = S.f_ptr[r]; k < S.f_ptr[r + 1]; ++k) {
-            int c = S.f_col[k];
-            if (mo[c] >= 0 && mo[c] <= io) S.a11.at(io, mo[c]) += S.f_val[k];
+        if (S.matrixtype == 0) {
+          S.a11lu.n = S.ndofo; S.a11lu.b = b11;
+          S.a11lu.v.assign((size_t)S.ndofo * (2 * b11 + 1), 0.0);
+          for (int io = 0; io < S.ndofo; ++io) {
+            int r = S.iovsvn[io];
+            for (int k = S.f_ptr[r]; k < S.f_ptr[r + 1]; ++k) {
+              int c = S.f_col[k];
+              if (mo[c] >= 0) S.a11lu.at(io, mo[c]) += S.f_val[k];
+            }
           }
+          if (S.ndofo > 0) S.a11lu.factor();
+        } else {
+          S.a11.n = S.ndofo; S.a11.b = b11;
+          S.a11.v.assign((size_t)S.ndofo * (b11 + 1), 0.0);
+          for (int io = 0; io < S.ndofo; ++io) {
+            int r = S.iovsvn[io];
+            for (int k = S.f_ptr[r]; k < S.f_ptr[r + 1]; ++k) {
+              int c = S.f_col[k];
+              if (mo[c] >= 0 && mo[c] <= io) S.a11.at(io, mo[c]) += S.f_val[k];
+            }
+          }
+          if (S.ndofo > 0) S.a11.factor();
         }
-        if (S.ndofo > 0) S.a11.factor();
         // augmented system: corner dofs shifted by their own diagonal
         int baug = 0;
         for (int r = 0; r < S.ndof; ++r)
           for (int k = S.f_ptr[r]; k < S.f_ptr[r + 1]; ++k) baug = std::max(baug, std::abs(r - S.f_col[k]));
-        S.aug.n = S.ndof; S.aug.b = baug;
-        S.aug.v.assign((size_t)S.ndof * (baug + 1), 0.0);
-        for (int r = 0; r < S.ndof; ++r)
-          for (int k = S.f_ptr[r]; k < S.f_ptr[r + 1]; ++k)
-            if (S.f_col[k] <= r) S.aug.at(r, S.f_col[k]) += S.f_val[k];
-        for (auto& cn : S.cnodes)
-          if (cn.itype == 3 && cn.used)
-            for (int v : cn.ivsivn) { int d = S.iivsvn[v]; S.aug.at(d, d) *= 2.0; }
-        S.aug.factor();
+        if (S.matrixtype == 0) {
+          S.auglu.n = S.ndof; S.auglu.b = baug;
+          S.auglu.v.assign((size_t)S.ndof * (2 * baug + 1), 0.0);
+          for (int r = 0; r < S.ndof; ++r)
+            for (int k = S.f_ptr[r]; k < S.f_ptr[r + 1]; ++k) S.auglu.at(r, S.f_col[k]) += S.f_val[k];
+          for (auto& cn : S.cnodes)
+            if (cn.itype == 3 && cn.used)
+              for (int v : cn.ivsivn) { int d = S.iivsvn[v]; S.auglu.at(d, d) *= 2.0; }
+          S.auglu.factor();
+        } else {
+          S.aug.n = S.ndof; S.aug.b = baug;
+          S.aug.v.assign((size_t)S.ndof * (baug + 1), 0.0);
+          for (int r = 0; r < S.ndof; ++r)
+            for (int k = S.f_ptr[r]; k < S.f_ptr[r + 1]; ++k)
+              if (S.f_col[k] <= r) S.aug.at(r, S.f_col[k]) += S.f_val[k];
+          for (auto& cn : S.cnodes)
+            if (cn.itype == 3 && cn.used)
+              for (int v : cn.ivsivn) { int d = S.iivsvn[v]; S.aug.at(d, d) *= 2.0; }
+          S.aug.factor();
+        }
       } catch (std::exception& e) {
 #pragma omp critical
         errs = e.what();
@@ -1617,11 +1791,20 @@ int oracle_setup(void* h, int use_corner_constraints, int use_arithmetic_constra
 // Y = A_r^-1 C^T, G = C Y, Phi = Y G^-1, coarse matrix Phi^T A Phi
 static void coarse_basis(Sub& S) {
         int nc = S.nconstr;
+        const bool gen = S.matrixtype == 0;
         S.yaug.assign((size_t)S.ndof * nc, 0.0);
         for (int c = 0; c < nc; ++c) {
           double* y = &S.yaug[(size_t)c * S.ndof];
           for (int k = S.crow_ptr[c]; k < S.crow_ptr[c + 1]; ++k) y[S.iivsvn[S.crow_col[k]]] += S.crow_val[k];
-          S.aug.solve(y);
+          aug_solve(S, y);
+        }
+        if (gen) {  // adjoint problem A^T for the dual basis (module_dd.f90:5687-5757)
+          S.ydual.assign((size_t)S.ndof * nc, 0.0);
+          for (int c = 0; c < nc; ++c) {
+            double* y = &S.ydual[(size_t)c * S.ndof];
+            for (int k = S.crow_ptr[c]; k < S.crow_ptr[c + 1]; ++k) y[S.iivsvn[S.crow_col[k]]] += S.crow_val[k];
+            S.auglu.solve_t(y);
+          }
         }
         S.gchol.assign((size_t)nc * nc, 0.0);
         for (int r = 0; r < nc; ++r)
@@ -1630,34 +1813,51 @@ static void coarse_basis(Sub& S) {
             for (int k = S.crow_ptr[r]; k < S.crow_ptr[r + 1]; ++k) t += S.crow_val[k] * S.yaug[(size_t)c * S.ndof + S.iivsvn[S.crow_col[k]]];
             S.gchol[(size_t)r * nc + c] = t;
           }
-        for (int r = 0; r < nc; ++r)
-          for (int c = r + 1; c < nc; ++c) {
-            double m = 0.5 * (S.gchol[(size_t)r * nc + c] + S.gchol[(size_t)c * nc + r]);
-            S.gchol[(size_t)r * nc + c] = S.gchol[(size_t)c * nc + r] = m;
-          }
-        if (nc > 0) dense_chol(S.gchol, nc);
-        // coarse basis: Phi = Y G^{-1}   (solve with RHS [0; I], module_dd.f90:5592-5607)
-        vector<double> phi((size_t)S.ndof * nc, 0.0);
-        for (int c = 0; c < nc; ++c) {
-          vector<double> e(nc, 0.0); e[c] = 1.0;
-          dense_chol_solve(S.gchol, nc, e.data());
-          for (int i = 0; i < S.ndof; ++i) {
-            double t = 0.0;
-            for (int q = 0; q < nc; ++q) t += S.yaug[(size_t)q * S.ndof + i] * e[q];
-            phi[(size_t)c * S.ndof + i] = t;
-          }
+        if (!gen) {
+          for (int r = 0; r < nc; ++r)
+            for (int c = r + 1; c < nc; ++c) {
+              double m = 0.5 * (S.gchol[(size_t)r * nc + c] + S.gchol[(size_t)c * nc + r]);
+              S.gchol[(size_t)r * nc + c] = S.gchol[(size_t)c * nc + r] = m;
+            }
+          if (nc > 0) dense_chol(S.gchol, nc);
+        } else if (nc > 0) {
+          dense_lu(S.gchol, nc, S.gpiv);
         }
+        // coarse basis: Phi = Y G^{-1}   (solve with RHS [0; I], module_dd.f90:5592-5607);
+        // for a general matrix also the dual basis Phi_dual = Y_dual G^{-T}
+        auto basis = [&](const vector<double>& y, bool trans) {
+          vector<double> phi((size_t)S.ndof * nc, 0.0);
+          for (int c = 0; c < nc; ++c) {
+            vector<double> e(nc, 0.0); e[c] = 1.0;
+            if (gen) dense_lu_solve(S.gchol, nc, S.gpiv, e.data(), trans);
+            else dense_chol_solve(S.gchol, nc, e.data());
+            for (int i = 0; i < S.ndof; ++i) {
+              double t = 0.0;
+              for (int q = 0; q < nc; ++q) t += y[(size_t)q * S.ndof + i] * e[q];
+              phi[(size_t)c * S.ndof + i] = t;
+            }
+          }
+          return phi;
+        };
+        vector<double> phi = basis(S.yaug, false);
+        vector<double> phid = gen ? basis(S.ydual, true) : phi;
         S.phisi.assign((size_t)S.ndofi * nc, 0.0);
         for (int c = 0; c < nc; ++c)
           for (int i = 0; i < S.ndofi; ++i) S.phisi[(size_t)c * S.ndofi + i] = phi[(size_t)c * S.ndof + S.iivsvn[i]];
-        // coarse matrix Phi^T A Phi
+        if (gen) {
+          S.phisi_dual.assign((size_t)S.ndofi * nc, 0.0);
+          for (int c = 0; c < nc; ++c)
+            for (int i = 0; i < S.ndofi; ++i)
+              S.phisi_dual[(size_t)c * S.ndofi + i] = phid[(size_t)c * S.ndof + S.iivsvn[i]];
+        }
+        // coarse matrix Phi_dual^T A Phi (Phi^T A Phi for symmetric matrices)
         S.coarsem.assign((size_t)nc * nc, 0.0);
         vector<double> aphi(S.ndof);
         for (int c = 0; c < nc; ++c) {
           csr_mult(S.f_ptr, S.f_col, S.f_val, &phi[(size_t)c * S.ndof], aphi.data(), S.ndof);
           for (int r = 0; r < nc; ++r) {
             double t = 0.0;
-            for (int i = 0; i < S.ndof; ++i) t += phi[(size_t)r * S.ndof + i] * aphi[i];
+            for (int i = 0; i < S.ndof; ++i) t += phid[(size_t)r * S.ndof + i] * aphi[i];
             S.coarsem[(size_t)r * nc + c] = t;
           }
         }
@@ -1680,8 +1880,15 @@ static void coarse_space(Oracle& oo) {
     if (!errs.empty()) throw std::runtime_error(errs);
     int n = o->ndofc;
     o->coarse_chol.assign((size_t)n * n, 0.0);
+    const bool gen = !o->subs.empty() && o->subs[0].matrixtype == 0;
     for (auto& S : o->subs) {
       int nc = S.nconstr;
+      if (gen) {  // all entries of the general local coarse matrices
+        for (int i = 0; i < nc; ++i)
+          for (int j = 0; j < nc; ++j)
+            o->coarse_chol[(size_t)(S.indrowc[i] - 1) * n + (S.indrowc[j] - 1)] += S.coarsem[(size_t)i * nc + j];
+        continue;
+      }
       for (int j = 0; j < nc; ++j)
         for (int i = 0; i <= j; ++i) {
           int gi = S.indrowc[i] - 1, gj = S.indrowc[j] - 1;
@@ -1689,6 +1896,10 @@ static void coarse_space(Oracle& oo) {
           int r = std::max(gi, gj), c = std::min(gi, gj);
           o->coarse_chol[(size_t)r * n + c] += v;
         }
+    }
+    if (gen) {
+      if (n > 0) dense_lu(o->coarse_chol, n, o->coarse_piv);
+      return;
     }
     for (int r = 0; r < n; ++r)
       for (int c = r + 1; c < n; ++c) o->coarse_chol[(size_t)r * n + c] = o->coarse_chol[(size_t)c * n + r];
@@ -1706,10 +1917,9 @@ static void sm_apply(Oracle& o, vector<vector<double>>& x, vector<vector<double>
       for (int k = S.a12_ptr[io]; k < S.a12_ptr[io + 1]; ++k) t += S.a12_val[k] * x[s][S.a12_col[k]];
       aux1[io] = t;
     }
-    if (S.ndofo > 0) S.a11.solve(aux1.data());
+    if (S.ndofo > 0) a11_solve(S, aux1.data());
     vector<double> aux2(S.ndofi, 0.0);
-    for (int io = 0; io < S.ndofo; ++io)
-      for (int k = S.a12_ptr[io]; k < S.a12_ptr[io + 1]; ++k) aux2[S.a12_col[k]] += S.a12_val[k] * aux1[io];
+    a21_apply_add(S, aux1.data(), aux2.data());
     y[s].assign(S.ndofi, 0.0);
     for (int i = 0; i < S.ndofi; ++i) {
       double t = 0.0;
@@ -1773,22 +1983,27 @@ static void pc_apply(Oracle& o, vector<vector<double>>& r, vector<vector<double>
     vector<double> aux(S.ndofi);
     for (int i = 0; i < S.ndofi; ++i) aux[i] = S.wi[i] * r[s][i];
     rcs[s].assign(nc, 0.0);
+    // restriction with the dual basis for a general matrix (dd_phisi_dual_apply, module_dd.f90:6126-6206)
+    const vector<double>& phr = S.matrixtype == 0 ? S.phisi_dual : S.phisi;
     for (int c = 0; c < nc; ++c) {
       double t = 0.0;
-      for (int i = 0; i < S.ndofi; ++i) t += S.phisi[(size_t)c * S.ndofi + i] * aux[i];
+      for (int i = 0; i < S.ndofi; ++i) t += phr[(size_t)c * S.ndofi + i] * aux[i];
       rcs[s][c] = t;
     }
     // constrained Neumann solve with interface RHS, interior zero
     vector<double> f(S.ndof, 0.0);
     for (int i = 0; i < S.ndofi; ++i) f[S.iivsvn[i]] = aux[i];
-    S.aug.solve(f.data());
+    aug_solve(S, f.data());
     vector<double> mu(nc, 0.0);
     for (int c = 0; c < nc; ++c) {
       double t = 0.0;
       for (int k = S.crow_ptr[c]; k < S.crow_ptr[c + 1]; ++k) t += S.crow_val[k] * f[S.iivsvn[S.crow_col[k]]];
       mu[c] = t;
     }
-    if (nc > 0) dense_chol_solve(S.gchol, nc, mu.data());
+    if (nc > 0) {
+      if (S.matrixtype == 0) dense_lu_solve(S.gchol, nc, S.gpiv, mu.data(), false);
+      else dense_chol_solve(S.gchol, nc, mu.data());
+    }
     z[s].assign(S.ndofi, 0.0);
     for (int i = 0; i < S.ndofi; ++i) {
       int d = S.iivsvn[i];
@@ -1803,6 +2018,7 @@ static void pc_apply(Oracle& o, vector<vector<double>>& r, vector<vector<double>
   }
   if (n > 0) {
     if (o.lev2) rc = level2_apply(*o.lev2, rc);
+    else if (!o.coarse_piv.empty()) dense_lu_solve(o.coarse_chol, n, o.coarse_piv, rc.data(), false);
     else dense_chol_solve(o.coarse_chol, n, rc.data());
   }
 #pragma omp parallel for schedule(dynamic) num_threads(o.nthreads)
@@ -2017,7 +2233,7 @@ static void postprocess(Oracle& oo, vector<vector<double>>& x) {
         for (int k = S.a12_ptr[io]; k < S.a12_ptr[io + 1]; ++k) t += S.a12_val[k] * x[s][S.a12_col[k]];
         aux1[io] = rhs[S.iovsvn[io]] - t;
       }
-      S.a11.solve(aux1.data());
+      a11_solve(S, aux1.data());
       for (int io = 0; io < S.ndofo; ++io) u[S.iovsvn[io]] += aux1[io];
     }
     for (int i = 0; i < S.ndofi; ++i) u[S.iivsvn[i]] += x[s][i];
@@ -2209,6 +2425,10 @@ void oracle_sym_eig(int n, const double* a, double* w, double* z) {
 // rea = A_fixed u over the fixed-rows matrix, neighbours' interface values added, minus the
 // load on the fixed dofs; out receives subdomain isub's (ndof values)
 int oracle_reactions(void* h, int isub, double* out) {
+  if (!static_cast<Oracle*>(h)->subs.empty() && static_cast<Oracle*>(h)->subs[0].matrixtype == 0) {
+    static_cast<Oracle*>(h)->err = "reactions are restated for symmetric storage only";
+    return 1;
+  }
   auto* o = static_cast<Oracle*>(h);
   const int nsub = o->nsub;
   vector<vector<double>> rea(nsub), ri(nsub);

@@ -344,3 +344,40 @@ def test_oracle_reactions_balance_the_loads(oracle_mod):
     r_true = K @ u - f
     assert np.abs(rea[fixed] - r_true[fixed]).max() <= 1e-9 * np.abs(r_true[fixed]).max()
     assert abs(rea[fixed].sum() + f.sum()) <= 1e-9 * np.abs(f).sum()
+
+
+@pytest.mark.parametrize("ne,ns,b", [(3, 2, (10.0, 7.0, 4.0)), (4, 3, (20.0, 10.0, 5.0)), (5, 2, (30.0, -12.0, 6.0))])
+def test_oracle_nonsymmetric_matches_direct(oracle_mod, ne, ns, b):
+    """matrixtype 0 (convection-diffusion, full element matrices): LU factors,
+    the dual coarse basis of the adjoint problem (module_dd.f90:5687-5757) for
+    the restriction, Phi_dual^T A Phi as local coarse matrix; BiCGSTAB matches
+    the direct solve of the assembled nonsymmetric system."""
+    from bddcml_gb300 import problems
+    from newdata_util import direct_solution
+    prob = problems.convection_diffusion_on_cube(ne, ns, b)
+    o = oracle_mod.Oracle(prob)
+    o.setup(1, 1, 0)
+    it, reason, _ = o.solve(1e-10, 500, 50, method=1)
+    u = o.global_solution()
+    ud = direct_solution(prob)
+    assert reason == 0 and it <= 20
+    assert np.linalg.norm(u - ud) / np.linalg.norm(ud) <= 1e-9
+
+
+def test_oracle_nonsymmetric_inhomogeneous_dirichlet(oracle_mod):
+    """Fixed columns of a general matrix go into the rhs, fixed rows do not
+    (module_sm.f90:528-560): nonzero boundary values match the direct solve."""
+    from bddcml_gb300 import problems
+    from newdata_util import direct_solution
+    prob = problems.convection_diffusion_on_cube(3, 2)
+    for s in prob.subdomains:
+        x = s.xyz
+        g = 1.0 + x[0] + 2.0 * x[1] * x[2]
+        s.fixv = np.where(s.ifix != 0, g, 0.0)
+    o = oracle_mod.Oracle(prob)
+    o.setup(1, 1, 0)
+    it, reason, _ = o.solve(1e-10, 500, 50, method=1)
+    u = o.global_solution()
+    ud = direct_solution(prob)
+    assert reason == 0
+    assert np.linalg.norm(u - ud) / np.linalg.norm(ud) <= 1e-9
