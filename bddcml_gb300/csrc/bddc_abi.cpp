@@ -148,8 +148,8 @@ void bddcml_upload_subdomain_data_c(int* nelem, int* nnod, int* ndof, int* ndim,
     s.rhs_complete = is_rhs_complete && *is_rhs_complete != 0;
     s.sol.assign(sol, sol + *ndofs);
     s.matrixtype = *matrixtype;
-    if (*matrixtype != 1 && *matrixtype != 2)
-      throw Error{ERR_UNSUPPORTED, "only symmetric matrices (matrixtype 1 or 2) are implemented"};
+    if (*matrixtype < 0 || *matrixtype > 2)
+      throw Error{ERR_ARGUMENT, "matrixtype must be 0 (general), 1 (SPD) or 2 (symmetric)"};
     // the triplets are most of the uploaded bytes: copy them with several
     // threads (first touch of the new buffers included)
     const int nla = *la, nd = *ndofs;
@@ -167,7 +167,7 @@ void bddcml_upload_subdomain_data_c(int* nelem, int* nnod, int* ndof, int* ndim,
       bad_order |= i > j;
       bad_range |= (i < 0) | (j >= nd);
     }
-    if (bad_order)
+    if (bad_order && *matrixtype != 0)  // module_levels.f90:748-752
       throw Error{ERR_ARGUMENT, "matrix in wrong format - only the upper triangle is expected for symmetric problems"};
     if (bad_range) throw Error{ERR_ARGUMENT, "matrix index out of range"};
     // assembly (merge of repeated entries) and mesh components are computed
@@ -209,6 +209,11 @@ void bddcml_setup_preconditioner_c(int* matrixtype, int* use_defaults_int, int* 
     if (S->prm.use_adaptive && S->prm.matrixtype != 1)
       throw Error{ERR_UNSUPPORTED, "adaptive constraints are implemented for SPD matrices (matrixtype 1)"};
     if (S->prm.use_user) throw Error{ERR_UNSUPPORTED, "user constraints are not implemented"};
+    for (auto& sd : S->subs)
+      if (sd.loaded && (sd.matrixtype == 0) != (S->prm.matrixtype == 0))
+        throw Error{ERR_ARGUMENT, "matrixtype differs from the one of the uploaded subdomain matrices"};
+    if (S->prm.matrixtype == 0 && S->prm.nlevels == 3)
+      throw Error{ERR_UNSUPPORTED, "three levels are implemented for symmetric matrices"};
     double t0 = wall_time();
     S->stats = Stats{};
     S->stats.t_upload = S->t_upload;
@@ -287,6 +292,7 @@ void bddcml_solve_batch_c(int* comm_all, int* method, double* tol, int* maxit, i
     if (!S) return;
     if (!S->setup_done) throw Error{ERR_ARGUMENT, "preconditioner is not set up"};
     if (*method != 0) throw Error{ERR_UNSUPPORTED, "batched right-hand sides are solved by PCG (method 0) only"};
+    if (S->prm.matrixtype == 0) throw Error{ERR_UNSUPPORTED, "batched solves need a symmetric matrix (PCG)"};
     if (*maxit < 1) throw Error{ERR_ARGUMENT, "maxit must be positive"};
     if (*nrhs < 1 || *nrhs > 64) throw Error{ERR_ARGUMENT, "nrhs must be between 1 and 64"};
     for (auto& s : S->subs)
@@ -352,6 +358,7 @@ static void gather_global(const Solver& S, const vector<double> Subdomain::*fiel
 
 static void need_reactions(Solver& S) {
   if (!S.solved) throw Error{ERR_ARGUMENT, "reactions are available after bddcml_solve"};
+  if (S.prm.matrixtype == 0) throw Error{ERR_UNSUPPORTED, "reactions are implemented for symmetric matrices"};
   if (!S.reactions_ready) {
     host_reactions(S);
     S.reactions_ready = true;

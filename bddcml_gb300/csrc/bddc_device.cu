@@ -255,6 +255,9 @@ class Device {
   double* scal = nullptr;  // scratch scalar
   BandDesc* bd_oo = nullptr;
   std::vector<BandDesc> hbd_oo;
+  bool general = false;         // matrixtype 0: LU factors and the dual coarse basis
+  BandDesc* bdu_oo = nullptr;   // U^T bands of the interior LU factors (general matrices)
+  std::vector<BandDesc> hbdu_oo;
   std::vector<TcDesc> htd_oo;  // tensor-core sweep descriptors of the interior systems (mixed)
   float* ppool_oo = nullptr;   // their panels
   // one-vector interior solves for new loads after setup (allocated on first use)
@@ -381,10 +384,27 @@ static void run_factor(Device& D, const BandDesc* bd, int nbatch, int maxnb, int
   }
 }
 
-// FP32 factors: panels for the tensor-core sweeps (after the factorisation)
+// block LU of general band matrices: L and U^T bands (k_lu_diag / k_lu_off)
+template <typename T>
+static void run_factor_lu(Device& D, const BandDesc* bl, const BandDesc* bu, int nbatch, int maxnb, int maxw,
+                          T* pool) {
+  size_t smem = (2 * NB * (NB + 1) + 2 * SM_TILE) * sizeof(T);
+  raise_smem(k_lu_diag<T>, smem);
+  for (int k = 0; k < maxnb; ++k) {
+    k_lu_diag<T><<<nbatch, NT, smem, D.st>>>(bl, bu, pool, k, D.err);
+    CKL();
+    if (maxw > 0) {
+      k_lu_off<T><<<dim3(maxw, nbatch), NT, 0, D.st>>>(bl, bu, pool, k);
+      CKL();
+    }
+  }
+}
+
+// FP32 factors: panels for the tensor-core sweeps (after the factorisation);
+// backward panels from bdb (U^T of a general matrix) when given
 static void run_panels(Device& D, const BandDesc* bd, const TcDesc* td, int nbatch, int maxnb, int maxw,
-                       const float* L, float* P) {
-  k_make_panels<<<dim3(maxw + 1, maxnb, nbatch), NT, 0, D.st>>>(bd, td, L, P);
+                       const float* L, float* P, const BandDesc* bdb = nullptr) {
+  k_make_panels<<<dim3(maxw + 1, maxnb, nbatch), NT, 0, D.st>>>(bd, td, L, P, bdb);
   CKL();
 }
 
@@ -419,14 +439,15 @@ static void run_solve_tc(Device& D, const TcDesc* td, int nbatch, int maxnb, int
 }
 
 template <typename T>
-static void run_solve(Device& D, const BandDesc* bd, int nbatch, int maxnb, int maxncol, const T* L, T* B) {
+static void run_solve(Device& D, const BandDesc* bd, int nbatch, int maxnb, int maxncol, const T* L, T* B,
+                      const BandDesc* bdb = nullptr) {
   dim3 grid(maxncol / NB, nbatch);
   for (int k = 0; k < maxnb; ++k) {
     k_trsm_fwd<T><<<grid, NT, 0, D.st>>>(bd, L, B, k);
     CKL();
   }
-  for (int k = maxnb - 1; k >= 0; --k) {
-    k_trsm_bwd<T><<<grid, NT, 0, D.st>>>(bd, L, B, k);
+  for (int k = maxnb - 1; k >= 0; --k) {  // backward with L^T, or with U (its transposed band) when bdb is given
+    k_trsm_bwd<T><<<grid, NT, 0, D.st>>>(bdb ? bdb : bd, L, B, k);
     CKL();
   }
 }
@@ -510,6 +531,7 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
   cudaStream_t st = D.st;
   auto& own = D.owned;
   D.nref = D.mixed ? 2 : 0;
+  D.general = S.prm.matrixtype == 0;
 
   // ---- sizes and offsets
   D.hs.assign(nsub, DevSub{});
@@ -527,6 +549,10 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
     d.nbo = d.NO / NB; d.w = b.w; d.nbi = d.NI / NB; d.nref = D.nref;
     d.oL = oT; oT += (long long)d.nbo * (d.w + 1) * NB * NB;
     d.oLinv = oT; oT += (long long)d.nbo * NB * NB;
+    if (D.general) {
+      d.oU = oT; oT += (long long)d.nbo * (d.w + 1) * NB * NB;
+      d.oUinv = oT; oT += (long long)d.nbo * NB * NB;
+    }
     d.oXc = oT; oT += (long long)(d.nref == 0 ? 1 : (d.nref == 1 ? 2 : 3)) * d.NO * d.NR;
     if (std::is_same_v<T, float>) {
       poff[t][0] = oPan; oPan += (long long)d.nbo * (d.w + 1) * 2 * TC_PCHUNK;
@@ -677,12 +703,25 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
     D.hbd_oo[t] = BandDesc{d.nbo, d.w, d.NR, 0, d.oL, d.oLinv, d.oXc};
   }
   D.bd_oo = upload(D.hbd_oo, own, st);
+  D.hbdu_oo.clear();
+  D.bdu_oo = nullptr;
+  if (D.general) {
+    D.hbdu_oo = D.hbd_oo;
+    for (int t = 0; t < nsub; ++t) { D.hbdu_oo[t].oL = D.hs[t].oU; D.hbdu_oo[t].oLinv = D.hs[t].oUinv; }
+    D.bdu_oo = upload(D.hbdu_oo, own, st);
+  }
   S.stats.t_dev_h2d = wall_time() - tw0 - S.stats.t_dev_alloc;
   D.prof.begin(PH_NUMERIC_TOTAL, st, true);
   D.prof.begin(PH_FACTOR_OO, st);
-  k_fill_band<T><<<dim3((D.maxNO + 127) / 128, nsub), 128, 0, st>>>(D.ds, D.koo, poolT, D.bd_oo);
-  CKL();
-  run_factor<T>(D, D.bd_oo, nsub, D.maxnbo, D.maxw, poolT);
+  if (D.general) {
+    k_fill_band_lu<T><<<dim3((D.maxNO + 127) / 128, nsub), 128, 0, st>>>(D.ds, D.koo, poolT, D.bd_oo, D.bdu_oo);
+    CKL();
+    run_factor_lu<T>(D, D.bd_oo, D.bdu_oo, nsub, D.maxnbo, D.maxw, poolT);
+  } else {
+    k_fill_band<T><<<dim3((D.maxNO + 127) / 128, nsub), 128, 0, st>>>(D.ds, D.koo, poolT, D.bd_oo);
+    CKL();
+    run_factor<T>(D, D.bd_oo, nsub, D.maxnbo, D.maxw, poolT);
+  }
   vector<TcDesc> htd(nsub);
   TcDesc* td_oo = nullptr;
   if constexpr (std::is_same_v<T, float>) {
@@ -691,7 +730,7 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
       htd[t] = TcDesc{d.nbo, d.w, d.NR, 0, d.oXc, poff[t][0], poff[t][1], -1};
     }
     td_oo = upload(htd, own, st);
-    run_panels(D, D.bd_oo, td_oo, nsub, D.maxnbo, D.maxw, poolT, ppool);
+    run_panels(D, D.bd_oo, td_oo, nsub, D.maxnbo, D.maxw, poolT, ppool, D.bdu_oo);
     D.htd_oo = htd;
     D.ppool_oo = ppool;
   }
@@ -701,7 +740,7 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
   k_fill_rhs<T><<<dim3((D.maxNO + 127) / 128, nsub), 128, 0, st>>>(D.ds, D.koi, D.fo, D.fo_off, poolT);
   CKL();
   if constexpr (std::is_same_v<T, float>) run_solve_tc(D, td_oo, nsub, D.maxnbo, D.maxNR, ppool, poolT);
-  else run_solve<T>(D, D.bd_oo, nsub, D.maxnbo, D.maxNR, poolT, poolT);
+  else run_solve<T>(D, D.bd_oo, nsub, D.maxnbo, D.maxNR, poolT, poolT, D.bdu_oo);
   D.prof.end(PH_SOLVE_OO, st);
   // Mixed precision: two refinement steps with FP64-accurate residuals.
   //   R0 = [A_oi | f_o] - A_oo X0 -> component 1, D1 = A_oo^-1 R0 in place (3xTF32)
@@ -761,16 +800,20 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
     k_schur_df<<<dim3(D.maxNI, nsub), 128, 0, st>>>(D.ds, D.kio, D.kii, reinterpret_cast<const float*>(poolT),
                                                     static_cast<float2*>(D.poolS), D.fi, D.grep);
     CKL();
-    k_symmetrize<float2><<<dim3(D.maxNI / 32, D.maxNI / 32, nsub), dim3(32, 8), 0, st>>>(
-        D.ds, static_cast<float2*>(D.poolS), 0);
-    CKL();
+    if (!D.general) {
+      k_symmetrize<float2><<<dim3(D.maxNI / 32, D.maxNI / 32, nsub), dim3(32, 8), 0, st>>>(
+          D.ds, static_cast<float2*>(D.poolS), 0);
+      CKL();
+    }
   } else {
     k_schur_f64<<<dim3(D.maxNI, nsub), 128, 0, st>>>(D.ds, D.kio, D.kii, reinterpret_cast<const double*>(poolT),
                                                      static_cast<double*>(D.poolS), D.fi, D.grep);
     CKL();
-    k_symmetrize<double><<<dim3(D.maxNI / 32, D.maxNI / 32, nsub), dim3(32, 8), 0, st>>>(
-        D.ds, static_cast<double*>(D.poolS), 0);
-    CKL();
+    if (!D.general) {
+      k_symmetrize<double><<<dim3(D.maxNI / 32, D.maxNI / 32, nsub), dim3(32, 8), 0, st>>>(
+          D.ds, static_cast<double*>(D.poolS), 0);
+      CKL();
+    }
   }
   D.prof.end(PH_SCHUR, st);
   // ---- assembled reduced rhs (module_dd.f90:7090-7135)
@@ -804,12 +847,19 @@ static void setup_precond(Solver& S, Device& D) {
     d.oLs = oP; oP += (long long)d.nbi * d.nbi * NB * NB;
     d.oLsinv = oP; oP += (long long)d.nbi * NB * NB;
     d.oBs = oP; oP += (long long)d.NI * d.NRC;
+    if (D.general) {
+      d.oLsU = oP; oP += (long long)d.nbi * d.nbi * NB * NB;
+      d.oLsUinv = oP; oP += (long long)d.nbi * NB * NB;
+      d.oYd = oP; oP += (long long)d.NI * d.ncp;
+    }
     if (std::is_same_v<T, float>) {
       poff[t][0] = oPan; oPan += (long long)d.nbi * d.nbi * 2 * TC_PCHUNK;
       poff[t][1] = oPan; oPan += (long long)d.nbi * d.nbi * 2 * TC_PCHUNK;
     }
     d.oZ = oPC; oPC += (long long)d.NI * d.NI;
     d.oPhi = oPC; oPC += (long long)d.NI * d.ncp;
+    d.oPhid = d.oPhi;
+    if (D.general) { d.oPhid = oPC; oPC += (long long)d.NI * d.ncp; }
     d.oGinv = oSm; oSm += (long long)d.ncp * d.ncp;
     d.oAc = oSm; oSm += (long long)d.ncp * d.ncp;
     d.cptr = cptr; cptr += d.nc + 1;
@@ -873,19 +923,40 @@ static void setup_precond(Solver& S, Device& D) {
     hbs[t] = BandDesc{d.nbi, d.nbi - 1, d.NRC, 0, d.oLs, d.oLsinv, d.oBs};
   }
   BandDesc* bd_s = upload(hbs, own, st);
-  D.prof.begin(PH_SRHO_FACTOR, st);
-  if constexpr (std::is_same_v<T, float>)
-    k_fill_srho<T, float2><<<dim3(D.maxNI / 16, D.maxNI / 16, nsub), dim3(16, 16), 0, st>>>(
-        D.ds, static_cast<const float2*>(D.poolS), poolP, bd_s);
-  else
-    k_fill_srho<T, double><<<dim3(D.maxNI / 16, D.maxNI / 16, nsub), dim3(16, 16), 0, st>>>(
-        D.ds, reinterpret_cast<const double*>(D.poolS), poolP, bd_s);
-  CKL();
-  if (maxnc > 0) {
-    k_add_penalty<T><<<dim3(1, nsub), 256, 0, st>>>(D.ds, D.c_ptr, D.c_col, D.c_val, poolP, bd_s);
-    CKL();
+  BandDesc* bdu_s = nullptr;  // U^T band of the general Srho factor
+  if (D.general) {
+    vector<BandDesc> hbu = hbs;
+    for (int t = 0; t < nsub; ++t) { hbu[t].oL = D.hs[t].oLsU; hbu[t].oLinv = D.hs[t].oLsUinv; }
+    bdu_s = upload(hbu, own, st);
   }
-  run_factor<T>(D, bd_s, nsub, maxnbi, maxnbi - 1, poolP);
+  D.prof.begin(PH_SRHO_FACTOR, st);
+  if (D.general) {
+    if constexpr (std::is_same_v<T, float>)
+      k_fill_srho_lu<T, float2><<<dim3(D.maxNI / 16, D.maxNI / 16, nsub), dim3(16, 16), 0, st>>>(
+          D.ds, static_cast<const float2*>(D.poolS), poolP, bd_s, bdu_s);
+    else
+      k_fill_srho_lu<T, double><<<dim3(D.maxNI / 16, D.maxNI / 16, nsub), dim3(16, 16), 0, st>>>(
+          D.ds, reinterpret_cast<const double*>(D.poolS), poolP, bd_s, bdu_s);
+    CKL();
+    if (maxnc > 0) {
+      k_add_penalty_lu<T><<<dim3(1, nsub), 256, 0, st>>>(D.ds, D.c_ptr, D.c_col, D.c_val, poolP, bd_s, bdu_s);
+      CKL();
+    }
+    run_factor_lu<T>(D, bd_s, bdu_s, nsub, maxnbi, maxnbi - 1, poolP);
+  } else {
+    if constexpr (std::is_same_v<T, float>)
+      k_fill_srho<T, float2><<<dim3(D.maxNI / 16, D.maxNI / 16, nsub), dim3(16, 16), 0, st>>>(
+          D.ds, static_cast<const float2*>(D.poolS), poolP, bd_s);
+    else
+      k_fill_srho<T, double><<<dim3(D.maxNI / 16, D.maxNI / 16, nsub), dim3(16, 16), 0, st>>>(
+          D.ds, reinterpret_cast<const double*>(D.poolS), poolP, bd_s);
+    CKL();
+    if (maxnc > 0) {
+      k_add_penalty<T><<<dim3(1, nsub), 256, 0, st>>>(D.ds, D.c_ptr, D.c_col, D.c_val, poolP, bd_s);
+      CKL();
+    }
+    run_factor<T>(D, bd_s, nsub, maxnbi, maxnbi - 1, poolP);
+  }
   TcDesc* td_s = nullptr;
   if constexpr (std::is_same_v<T, float>) {
     vector<TcDesc> hts(nsub);
@@ -894,28 +965,39 @@ static void setup_precond(Solver& S, Device& D) {
       hts[t] = TcDesc{d.nbi, d.nbi - 1, d.NRC, d.NI, d.oBs, poff[t][0], poff[t][1], -1};  // [I | C^T]
     }
     td_s = upload(hts, own, st);
-    run_panels(D, bd_s, td_s, nsub, maxnbi, maxnbi - 1, poolP, ppool);
+    run_panels(D, bd_s, td_s, nsub, maxnbi, maxnbi - 1, poolP, ppool, bdu_s);
   }
   D.prof.end(PH_SRHO_FACTOR, st);
   D.prof.begin(PH_SRHO_SOLVE, st);
   k_fill_rhs_srho<T><<<dim3((D.maxNI + 127) / 128, nsub), 128, 0, st>>>(D.ds, D.c_ptr, D.c_col, D.c_val, poolP);
   CKL();
   if constexpr (std::is_same_v<T, float>) run_solve_tc(D, td_s, nsub, maxnbi, maxNRC, ppool, poolP);
-  else run_solve<T>(D, bd_s, nsub, maxnbi, maxNRC, poolP, poolP);
+  else run_solve<T>(D, bd_s, nsub, maxnbi, maxNRC, poolP, poolP, bdu_s);
   D.prof.end(PH_SRHO_SOLVE, st);
   D.prof.begin(PH_PC_BLOCKS, st);
+  const int gen = D.general ? 1 : 0;
+  if (gen) {  // Y_dual = Srho^-T C^T for the dual coarse basis
+    k_ydual<T><<<dim3((D.maxNI * D.ncpmax + 255) / 256, nsub), 256, 0, st>>>(D.ds, D.c_ptr, D.c_col, D.c_val, poolP);
+    CKL();
+  }
   {
     size_t smem = 2 * (size_t)std::max(1, maxnc) * std::max(1, maxnc) * sizeof(double);
     raise_smem(k_small_g<T>, smem);
-    k_small_g<T><<<nsub, 256, smem, st>>>(D.ds, D.c_ptr, D.c_col, D.c_val, poolP, D.small, D.err);
+    k_small_g<T><<<nsub, 256, smem, st>>>(D.ds, D.c_ptr, D.c_col, D.c_val, poolP, D.small, D.err, gen);
     CKL();
   }
-  k_phi<T><<<dim3((D.maxNI * D.ncpmax + 255) / 256, nsub), 256, 0, st>>>(D.ds, poolP, D.small, poolPC);
+  k_phi<T><<<dim3((D.maxNI * D.ncpmax + 255) / 256, nsub), 256, 0, st>>>(D.ds, poolP, D.small, poolPC, 0);
   CKL();
-  k_z<T><<<dim3(D.maxNI / 16, D.maxNI / 16, nsub), dim3(16, 16), 0, st>>>(D.ds, poolP, poolPC);
+  if (gen) {
+    k_phi<T><<<dim3((D.maxNI * D.ncpmax + 255) / 256, nsub), 256, 0, st>>>(D.ds, poolP, D.small, poolPC, 1);
+    CKL();
+  }
+  k_z<T><<<dim3(D.maxNI / 16, D.maxNI / 16, nsub), dim3(16, 16), 0, st>>>(D.ds, poolP, poolPC, gen);
   CKL();
-  k_symmetrize<T><<<dim3(D.maxNI / 32, D.maxNI / 32, nsub), dim3(32, 8), 0, st>>>(D.ds, poolPC, 1);
-  CKL();
+  if (!gen) {
+    k_symmetrize<T><<<dim3(D.maxNI / 32, D.maxNI / 32, nsub), dim3(32, 8), 0, st>>>(D.ds, poolPC, 1);
+    CKL();
+  }
   D.prof.end(PH_PC_BLOCKS, st);
   D.prof.begin(PH_COARSE, st);
 
@@ -959,27 +1041,36 @@ static void setup_precond(Solver& S, Device& D) {
     BandDesc cb{nbc, nbc - 1, D.ldc, 0, 0, (long long)nbc * nbc * NB * NB,
                 (long long)nbc * nbc * NB * NB + (long long)nbc * NB * NB};
     size_t csize = (size_t)cb.oB + (size_t)D.ldc * D.ldc;
+    BandDesc cbu = cb;  // U^T band of a general coarse matrix, after the identity block
+    if (D.general) {
+      cbu.oL = (long long)csize;
+      cbu.oLinv = cbu.oL + (long long)nbc * nbc * NB * NB;
+      csize = (size_t)cbu.oLinv + (size_t)nbc * NB * NB;
+    }
     T* cpool = dalloc<T>(csize, own);
     CK(cudaMemsetAsync(cpool, 0, csize * sizeof(T), st));
+    vector<BandDesc> hcbu{cbu};
+    BandDesc* dcbu = D.general ? upload(hcbu, own, st) : nullptr;
     if (nc_g > 0) {
       k_coarse_assemble<T><<<nc_g, 128, 0, st>>>(nc_g, D.ac_ptr, D.ac_col, dcptr, dcontrib, D.small, D.ac_val,
-                                                  cpool, cb);
+                                                  cpool, cb, dcbu);
       CKL();
     }
     k_coarse_pad<T><<<(D.ldc + 255) / 256, 256, 0, st>>>(nc_g, D.ldc, cpool, cb);
     CKL();
     vector<BandDesc> hcb{cb};
     BandDesc* dcb = upload(hcb, own, st);
-    run_factor<T>(D, dcb, 1, nbc, nbc - 1, cpool);
+    if (D.general) run_factor_lu<T>(D, dcb, dcbu, 1, nbc, nbc - 1, cpool);
+    else run_factor<T>(D, dcb, 1, nbc, nbc - 1, cpool);
     if constexpr (std::is_same_v<T, float>) {
       // identity right-hand side needs a column count that is a multiple of the MMA tile
       vector<TcDesc> htc{TcDesc{nbc, nbc - 1, D.ldc, D.ldc, cb.oB, 0, (long long)nbc * nbc * 2 * TC_PCHUNK, -1}};
       TcDesc* tdc = upload(htc, own, st);
       float* cpan = dalloc<float>((size_t)2 * nbc * nbc * 2 * TC_PCHUNK, own);
-      run_panels(D, dcb, tdc, 1, nbc, nbc - 1, cpool, cpan);
+      run_panels(D, dcb, tdc, 1, nbc, nbc - 1, cpool, cpan, dcbu);
       run_solve_tc(D, tdc, 1, nbc, D.ldc, cpan, cpool);
     } else {
-      run_solve<T>(D, dcb, 1, nbc, D.ldc, cpool, cpool);
+      run_solve<T>(D, dcb, 1, nbc, D.ldc, cpool, cpool, dcbu);
     }
     D.cinv = cpool + cb.oB;
     D.cres = dalloc<double>(std::max(1, nc_g), own);
@@ -1864,7 +1955,7 @@ static void reduced_rhs_device(Device& D) {
   const size_t smem = (size_t)(D.maxnbo * NB + 5 * NB) * sizeof(T);
   raise_smem(k_band_solve1<T>, smem);
   auto solve1 = [&](T* x) {
-    k_band_solve1<T><<<nsub, NT, smem, st>>>(D.bd_oo, poolT, x, D.nv_off);
+    k_band_solve1<T><<<nsub, NT, smem, st>>>(D.bd_oo, poolT, x, D.nv_off, D.bdu_oo);
     CKL();
   };
   k_fill_vec1<T><<<gv, 128, 0, st>>>(D.ds, D.fo, D.fo_off, v0, D.nv_off);

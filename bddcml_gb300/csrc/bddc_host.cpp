@@ -132,10 +132,18 @@ void host_nodal_components(Subdomain& s) {
 }
 
 void full_symmetric_csr(const Subdomain& s, vector<int>& ptr, vector<int>& col, vector<double>& val) {
+  int n = s.ndof;
+  if (s.matrixtype == 0) {  // general matrix: the assembled triplets are the rows, sorted
+    ptr.assign(n + 1, 0);
+    for (size_t k = 0; k < s.ia.size(); ++k) ptr[s.ia[k] + 1]++;
+    for (int i = 0; i < n; ++i) ptr[i + 1] += ptr[i];
+    col.assign(s.ja.begin(), s.ja.end());
+    val.assign(s.a.begin(), s.a.end());
+    return;
+  }
   // the assembled upper triangle is sorted by (row, column): scanning it in
   // order appends the mirrored entries of every row in increasing column
   // order, and the row's own entries follow, so no row needs sorting
-  int n = s.ndof;
   ptr.assign(n + 1, 0);
   for (size_t k = 0; k < s.ia.size(); ++k) {
     ptr[s.ia[k] + 1]++;
@@ -444,11 +452,12 @@ void host_setup(Solver& S) {
     };
     vector<char> diag_fixed(s.ndof, 0);
     s.fxr_i.clear(); s.fxr_j.clear(); s.fxr_v.clear();
+    const bool sym = s.matrixtype != 0;  // general storage: only fixed columns feed the rhs
     for (size_t k = 0; k < s.ia.size(); ++k) {
       int i = s.ia[k], j = s.ja[k];
-      if (s.ifix[i] || s.ifix[j]) { s.fxr_i.push_back(i); s.fxr_j.push_back(j); s.fxr_v.push_back(s.a[k]); }
+      if (s.ifix[i] || (sym && s.ifix[j])) { s.fxr_i.push_back(i); s.fxr_j.push_back(j); s.fxr_v.push_back(s.a[k]); }
       if (i != j) {
-        if (s.ifix[i] && s.a[k] != 0.0 && !s.ifix[j]) record(j, i, -s.a[k]);
+        if (sym && s.ifix[i] && s.a[k] != 0.0 && !s.ifix[j]) record(j, i, -s.a[k]);
         if (s.ifix[j] && s.a[k] != 0.0 && !s.ifix[i]) record(i, j, -s.a[k]);
         if (s.ifix[i] || s.ifix[j]) s.a[k] = 0.0;
       } else if (s.ifix[i]) {

@@ -131,6 +131,8 @@ __global__ void __launch_bounds__(RT) k_assemble_dot(int n, Owners own, const do
 
 // --------------------------------------------------- preconditioner parts
 // z_s = Z_s (w_s .* r_s) and partial coarse residual Phi_s^T (w_s .* r_s)
+// (the dual basis Phi_dual for a general matrix, dd_phisi_dual_apply,
+// module_dd.f90:6126-6206; oPhid = oPhi for symmetric matrices)
 template <typename T>
 __global__ void __launch_bounds__(AT) k_pc_local(const DevSub* __restrict__ ds, const T* __restrict__ pcpool,
                                                  const double* __restrict__ r, const int* __restrict__ uniq,
@@ -157,7 +159,7 @@ __global__ void __launch_bounds__(AT) k_pc_local(const DevSub* __restrict__ ds, 
   // coarse residual partial over this CTA's rows
   for (int c = threadIdx.x; c < s.nc; c += AT) {
     double t = 0.0;
-    for (int rr = r0; rr < rend; ++rr) t += (double)pcpool[s.oPhi + (long long)rr * s.ncp + c] * (double)aux[rr];
+    for (int rr = r0; rr < rend; ++rr) t += (double)pcpool[s.oPhid + (long long)rr * s.ncp + c] * (double)aux[rr];
     rcpart[((long long)blockIdx.y * nrb + blockIdx.x) * ncpmax + c] = t;
   }
 }
@@ -218,7 +220,7 @@ template <typename T>
 __global__ void k_coarse_assemble(int n, const int* __restrict__ ptr, const int* __restrict__ col,
                                   const int* __restrict__ cptr, const long long* __restrict__ contrib,
                                   const double* __restrict__ small, double* __restrict__ val, T* __restrict__ fpool,
-                                  BandDesc d) {
+                                  BandDesc d, const BandDesc* __restrict__ du) {
   int i = blockIdx.x;
   if (i >= n) return;
   for (int q = ptr[i] + threadIdx.x; q < ptr[i + 1]; q += blockDim.x) {
@@ -226,7 +228,8 @@ __global__ void k_coarse_assemble(int n, const int* __restrict__ ptr, const int*
     for (int e = cptr[q]; e < cptr[q + 1]; ++e) t += small[contrib[e]];
     val[q] = t;
     int j = col[q];
-    if (j <= i) fpool[band_block(d, i / NB, j / NB) + (i % NB) * NB + j % NB] = T(t);
+    if (du) lu_slot<T>(d, *du, fpool, i, j) = T(t);  // general: L and U^T bands
+    else if (j <= i) fpool[band_block(d, i / NB, j / NB) + (i % NB) * NB + j % NB] = T(t);
   }
 }
 

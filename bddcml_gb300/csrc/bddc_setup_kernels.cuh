@@ -31,6 +31,10 @@ struct DevSub {
   int cptr;                // constraint row-pointer offset
   int coff;                // offset into per-constraint arrays (coarse map)
   double rho;              // penalty scale of the preconditioner block
+  // general (nonsymmetric) matrices: the transposed upper LU factors (Ut) of the
+  // interior and preconditioner blocks, the dual coarse basis input Y_dual and
+  // the dual basis Phi_dual (oPhid = oPhi for symmetric matrices)
+  long long oU, oUinv, oLsU, oLsUinv, oYd, oPhid;
 };
 
 // ------------------------------------------------------------ band factor
@@ -124,6 +128,160 @@ __device__ void chol_off_step(const BandDesc& d, T* __restrict__ pool, int k, in
 #pragma unroll
     for (int p = 0; p < 4; ++p) Aik[(ty * 4 + q) * NB + tx * 4 + p] = acc[q][p];
   __syncthreads();
+}
+
+// ------------------------------------------------------- band LU factor
+// Left-looking block LU without pivoting of a general block-band matrix held
+// in two lower block bands with the same shape: L (the diagonal block and the
+// lower blocks of A on entry, the unit lower factor on exit) and Ut (the
+// upper blocks of A transposed, Ut(i,k) = A(k,i)^T, on entry; U^T on exit).
+// Step k:
+//   diagonal: L_kk U_kk = A_kk - sum_{j<k} L_kj Ut_kj^T;  L_kk^-1 at L.oLinv, (U_kk^-1)^T at Ut.oLinv
+//   below:    L_ik  = (A_ik  - sum_{j<k} L_ij  Ut_kj^T) Ut.inv_kk^T     (= ... U_kk^-1)
+//             Ut_ik = (Ut_ik - sum_{j<k} Ut_ij L_kj^T)  L.inv_kk^T      (= (L_kk^-1 ...)^T)
+// The forward solve with L then runs the Cholesky forward kernels on the L
+// band, the backward solve with U the backward kernels on the Ut band (they
+// apply Ut_kk^-T = U_kk^-1 and Ut_ik^T = U_ki).  The reference hands general
+// matrices to MUMPS, which pivots (module_mumps.f90:443-511); block LU without
+// pivoting needs diagonally dominant enough blocks, and a zero or non-finite
+// pivot is reported in the error word.
+template <typename T>
+__device__ void lu_diag_step(const BandDesc& dl, const BandDesc& du, T* __restrict__ pool, int k,
+                             int* __restrict__ err, T* a, T* inv, T* smA, T* smB) {
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  T acc[4][4];
+  tile_zero(acc);
+  for (int j = max(0, k - dl.w); j < k; ++j)
+    tile_gemm<T, false, true>(acc, pool + band_block(dl, k, j), NB, pool + band_block(du, k, j), NB, NB, smA, smB);
+  const T* Akk = pool + band_block(dl, k, k);
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+#pragma unroll
+    for (int p = 0; p < 4; ++p) {
+      int r = ty * 4 + q, c = tx * 4 + p;
+      a[r * (NB + 1) + c] = Akk[r * NB + c] - acc[q][p];
+    }
+  __syncthreads();
+  for (int c = 0; c < NB; ++c) {
+    if (tid == 0) {
+      T v = a[c * (NB + 1) + c];
+      if (!(v == v) || v == T(0) || !(fabs((double)v) < 1e300)) {
+        atomicOr(err, (v != v) ? DE_NAN : DE_PIVOT);
+        a[c * (NB + 1) + c] = T(1);
+      }
+    }
+    __syncthreads();
+    const T dc = a[c * (NB + 1) + c];
+    for (int r = c + 1 + tid; r < NB; r += NT) a[r * (NB + 1) + c] /= dc;
+    __syncthreads();
+    for (int r = c + 1 + ty; r < NB; r += 16) {  // trailing update of the whole block
+      const T lr = a[r * (NB + 1) + c];
+      for (int q = c + 1 + tx; q < NB; q += 16) a[r * (NB + 1) + q] -= lr * a[c * (NB + 1) + q];
+    }
+    __syncthreads();
+  }
+  // L_kk^-1 (unit lower) by elimination on the identity
+  for (int e = tid; e < NB * NB; e += NT) {
+    const int r = e / NB, c = e % NB;
+    inv[r * (NB + 1) + c] = r == c ? T(1) : T(0);
+  }
+  __syncthreads();
+  for (int kk = 0; kk < NB; ++kk) {
+    for (int i = kk + 1 + ty; i < NB; i += 16) {
+      const T lik = a[i * (NB + 1) + kk];
+      for (int j = tx; j <= kk; j += 16) inv[i * (NB + 1) + j] -= lik * inv[kk * (NB + 1) + j];
+    }
+    __syncthreads();
+  }
+  T* Lkk = pool + band_block(dl, k, k);
+  T* Li = pool + dl.oLinv + (long long)k * NB * NB;
+  for (int e = tid; e < NB * NB; e += NT) {
+    const int r = e / NB, c = e % NB;
+    Lkk[e] = c < r ? a[r * (NB + 1) + c] : (c == r ? T(1) : T(0));
+    Li[e] = inv[r * (NB + 1) + c];
+  }
+  __syncthreads();
+  // U_kk^-1 (upper) by elimination on the identity from the last row up
+  for (int e = tid; e < NB * NB; e += NT) {
+    const int r = e / NB, c = e % NB;
+    inv[r * (NB + 1) + c] = r == c ? T(1) : T(0);
+  }
+  __syncthreads();
+  for (int kk = NB - 1; kk >= 0; --kk) {
+    const T dk = a[kk * (NB + 1) + kk];
+    for (int j = kk + tid; j < NB; j += NT) inv[kk * (NB + 1) + j] /= dk;
+    __syncthreads();
+    for (int i = ty; i < kk; i += 16) {
+      const T uik = a[i * (NB + 1) + kk];
+      for (int j = kk + tx; j < NB; j += 16) inv[i * (NB + 1) + j] -= uik * inv[kk * (NB + 1) + j];
+    }
+    __syncthreads();
+  }
+  T* Ukk = pool + band_block(du, k, k);
+  T* Ui = pool + du.oLinv + (long long)k * NB * NB;
+  for (int e = tid; e < NB * NB; e += NT) {
+    const int r = e / NB, c = e % NB;  // transposed: (r, c) holds entry (c, r)
+    Ukk[e] = c <= r ? a[c * (NB + 1) + r] : T(0);
+    Ui[e] = inv[c * (NB + 1) + r];
+  }
+}
+
+template <typename T>
+__device__ void lu_off_step(const BandDesc& dl, const BandDesc& du, T* __restrict__ pool, int k, int i, T* smA,
+                            T* smB) {
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  for (int part = 0; part < 2; ++part) {
+    // part 0: L_ik with (L row i, Ut row k, Ut.inv_kk); part 1: Ut_ik with (Ut row i, L row k, L.inv_kk)
+    const BandDesc& dr = part == 0 ? dl : du;
+    const BandDesc& dc = part == 0 ? du : dl;
+    T acc[4][4];
+    tile_zero(acc);
+    for (int j = max(0, i - dl.w); j < k; ++j)
+      tile_gemm<T, false, true>(acc, pool + band_block(dr, i, j), NB, pool + band_block(dc, k, j), NB, NB, smA, smB);
+    T* Aik = pool + band_block(dr, i, k);
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+      for (int p = 0; p < 4; ++p) Aik[(ty * 4 + q) * NB + tx * 4 + p] -= acc[q][p];
+    __syncthreads();
+    tile_zero(acc);
+    tile_gemm<T, false, true>(acc, Aik, NB, pool + dc.oLinv + (long long)k * NB * NB, NB, NB, smA, smB);
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+      for (int p = 0; p < 4; ++p) Aik[(ty * 4 + q) * NB + tx * 4 + p] = acc[q][p];
+    __syncthreads();
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(NT) k_lu_diag(const BandDesc* __restrict__ bl, const BandDesc* __restrict__ bu,
+                                                T* __restrict__ pool, int k, int* __restrict__ err) {
+  const BandDesc dl = bl[blockIdx.x], du = bu[blockIdx.x];
+  if (k >= dl.nb) return;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T* a = reinterpret_cast<T*>(smraw);
+  T* inv = a + NB * (NB + 1);
+  T* smA = inv + NB * (NB + 1);
+  lu_diag_step<T>(dl, du, pool, k, err, a, inv, smA, smA + SM_TILE);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(NT) k_lu_off(const BandDesc* __restrict__ bl, const BandDesc* __restrict__ bu,
+                                               T* __restrict__ pool, int k) {
+  const BandDesc dl = bl[blockIdx.y], du = bu[blockIdx.y];
+  const int i = k + 1 + blockIdx.x;
+  if (k >= dl.nb || i >= dl.nb || i - k > dl.w) return;
+  __shared__ __align__(16) T smA[SM_TILE];
+  __shared__ __align__(16) T smB[SM_TILE];
+  lu_off_step<T>(dl, du, pool, k, i, smA, smB);
+}
+
+// entry (r, c) of a general matrix into the L / Ut bands (diagonal blocks whole in L)
+template <typename T>
+__device__ __forceinline__ T& lu_slot(const BandDesc& dl, const BandDesc& du, T* pool, int r, int c) {
+  return (c / NB <= r / NB) ? pool[band_block(dl, r / NB, c / NB) + (r % NB) * NB + c % NB]
+                            : pool[band_block(du, c / NB, r / NB) + (c % NB) * NB + r % NB];
 }
 
 // one step for every system (one CTA per system)
@@ -234,6 +392,22 @@ __global__ void k_fill_band(const DevSub* __restrict__ ds, CsrView koo, T* __res
     int c = koo.col[q];
     if (c <= r) pool[band_block(d, r / NB, c / NB) + (r % NB) * NB + c % NB] = T(koo.val[q]);
   }
+}
+
+// general interior block into the L / Ut bands; padding rows get a unit diagonal
+template <typename T>
+__global__ void k_fill_band_lu(const DevSub* __restrict__ ds, CsrView koo, T* __restrict__ pool,
+                               const BandDesc* __restrict__ bl, const BandDesc* __restrict__ bu) {
+  const DevSub s = ds[blockIdx.y];
+  const BandDesc dl = bl[blockIdx.y], du = bu[blockIdx.y];
+  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= s.NO) return;
+  if (r >= s.no) {
+    pool[band_block(dl, r / NB, r / NB) + (r % NB) * NB + r % NB] = T(1);
+    return;
+  }
+  const int* ptr = koo.ptr + s.koo;
+  for (int q = ptr[r]; q < ptr[r + 1]; ++q) lu_slot<T>(dl, du, pool, r, koo.col[q]) = T(koo.val[q]);
 }
 
 // RHS of the interior solves: [A_oi | f_o | 0], NO x NR
@@ -550,6 +724,58 @@ __global__ void k_add_penalty(const DevSub* __restrict__ ds, const int* __restri
   }
 }
 
+// general Srho = S + rho * C~^T C~ into the L / Ut bands (every entry; unit
+// diagonal on the padding)
+template <typename T, typename ST>
+__global__ void k_fill_srho_lu(const DevSub* __restrict__ ds, const ST* __restrict__ Spool, T* __restrict__ pool,
+                               const BandDesc* __restrict__ bl, const BandDesc* __restrict__ bu) {
+  const DevSub s = ds[blockIdx.z];
+  const BandDesc dl = bl[blockIdx.z], du = bu[blockIdx.z];
+  int i = blockIdx.y * 16 + threadIdx.y, j = blockIdx.x * 16 + threadIdx.x;
+  if (i >= s.NI || j >= s.NI) return;
+  T v;
+  if (i < s.ni && j < s.ni) v = schur_entry<T, ST>(Spool + s.oS, (long long)i * s.NI + j);
+  else v = (i == j) ? T(1) : T(0);
+  lu_slot<T>(dl, du, pool, i, j) = v;
+}
+
+template <typename T>
+__global__ void k_add_penalty_lu(const DevSub* __restrict__ ds, const int* __restrict__ cptr,
+                                 const int* __restrict__ ccol, const double* __restrict__ cval, T* __restrict__ pool,
+                                 const BandDesc* __restrict__ bl, const BandDesc* __restrict__ bu) {
+  const DevSub s = ds[blockIdx.y];
+  const BandDesc dl = bl[blockIdx.y], du = bu[blockIdx.y];
+  const int* p = cptr + s.cptr;
+  for (int r = 0; r < s.nc; ++r) {  // rows in a fixed order (shared entries, deterministic sums)
+    const int q0 = p[r], n = p[r + 1] - q0;
+    double nrm = 0.0;
+    for (int q = 0; q < n; ++q) nrm += cval[q0 + q] * cval[q0 + q];
+    const double sc = s.rho / nrm;
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+      int a = e / n, b = e % n;
+      lu_slot<T>(dl, du, pool, ccol[q0 + a], ccol[q0 + b]) += T(sc * cval[q0 + a] * cval[q0 + b]);
+    }
+    __syncthreads();
+  }
+}
+
+// dual input Y_dual = Srho^-T C^T = V^T C^T from the explicit inverse V = Srho^-1
+// (the adjoint solve of module_dd.f90:5687-5757 without a transposed factor solve)
+template <typename T>
+__global__ void k_ydual(const DevSub* __restrict__ ds, const int* __restrict__ cptr, const int* __restrict__ ccol,
+                        const double* __restrict__ cval, T* __restrict__ pool) {
+  const DevSub s = ds[blockIdx.y];
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= s.NI * s.ncp) return;
+  const int i = e / s.ncp, c = e % s.ncp;
+  double t = 0.0;
+  if (c < s.nc && i < s.ni) {
+    const int* p = cptr + s.cptr;
+    for (int k = p[c]; k < p[c + 1]; ++k) t += cval[k] * (double)pool[s.oBs + (long long)ccol[k] * s.NRC + i];
+  }
+  pool[s.oYd + e] = T(t);
+}
+
 // RHS [I | C^T | 0] of the preconditioner solves
 template <typename T>
 __global__ void k_fill_rhs_srho(const DevSub* __restrict__ ds, const int* __restrict__ cptr,
@@ -568,7 +794,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_small_g(const DevSub* __restrict__ ds, const int* __restrict__ cptr,
                                                  const int* __restrict__ ccol, const double* __restrict__ cval,
                                                  const T* __restrict__ pool, double* __restrict__ small,
-                                                 int* __restrict__ err) {
+                                                 int* __restrict__ err, int general) {
   const DevSub s = ds[blockIdx.x];
   const int nc = s.nc, ld = max(1, s.nc);
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -582,6 +808,57 @@ __global__ void __launch_bounds__(256) k_small_g(const DevSub* __restrict__ ds, 
     g[r * ld + q] = t;
   }
   __syncthreads();
+  if (general) {
+    // G = C Y of a general matrix: Gauss-Jordan inverse with partial pivoting
+    __shared__ int pivrow;
+    for (int e = threadIdx.x; e < nc * nc; e += blockDim.x) inv[(e / nc) * ld + e % nc] = (e / nc == e % nc) ? 1.0 : 0.0;
+    __syncthreads();
+    for (int c = 0; c < nc; ++c) {
+      if (threadIdx.x == 0) {
+        int pr = c;
+        for (int r = c + 1; r < nc; ++r)
+          if (fabs(g[r * ld + c]) > fabs(g[pr * ld + c])) pr = r;
+        if (!(fabs(g[pr * ld + c]) > 0.0)) { atomicOr(err, DE_PIVOT); g[pr * ld + c] = 1.0; }
+        pivrow = pr;
+      }
+      __syncthreads();
+      const int pr = pivrow;
+      if (pr != c)
+        for (int q = threadIdx.x; q < nc; q += blockDim.x) {
+          double t = g[c * ld + q]; g[c * ld + q] = g[pr * ld + q]; g[pr * ld + q] = t;
+          t = inv[c * ld + q]; inv[c * ld + q] = inv[pr * ld + q]; inv[pr * ld + q] = t;
+        }
+      __syncthreads();
+      const double dinv = 1.0 / g[c * ld + c];
+      __syncthreads();
+      for (int q = threadIdx.x; q < nc; q += blockDim.x) { g[c * ld + q] *= dinv; inv[c * ld + q] *= dinv; }
+      __syncthreads();
+      for (int e = threadIdx.x; e < nc * nc; e += blockDim.x) {
+        const int r = e / nc, q = e % nc;
+        if (r == c) continue;
+        const double f = g[r * ld + c];
+        if (q != c) g[r * ld + q] -= f * g[c * ld + q];
+        inv[r * ld + q] -= f * inv[c * ld + q];
+      }
+      __syncthreads();
+      for (int r = threadIdx.x; r < nc; r += blockDim.x) if (r != c) g[r * ld + c] = 0.0;
+      __syncthreads();
+    }
+    double* Gi = small + s.oGinv;
+    double* Ac = small + s.oAc;
+    for (int e = threadIdx.x; e < s.ncp * s.ncp; e += blockDim.x) {
+      int r = e / s.ncp, q = e % s.ncp;
+      double t = (r < nc && q < nc) ? inv[r * ld + q] : 0.0;
+      Gi[e] = t;
+      if (r < nc && r == q) {  // Phi_dual^T S Phi = G^-1 - rho D^2 as for symmetric matrices
+        double nrm = 0.0;
+        for (int k = p[r]; k < p[r + 1]; ++k) nrm += cval[k] * cval[k];
+        t -= s.rho / nrm;
+      }
+      Ac[e] = t;
+    }
+    return;
+  }
   for (int e = threadIdx.x; e < nc * nc; e += blockDim.x) {
     int r = e / nc, q = e % nc;
     if (q > r) {
@@ -643,18 +920,23 @@ __global__ void __launch_bounds__(256) k_small_g(const DevSub* __restrict__ ds, 
 // Phi = Y Ginv  (NI x ncp, preconditioner precision)
 template <typename T>
 __global__ void k_phi(const DevSub* __restrict__ ds, const T* __restrict__ pool, const double* __restrict__ small,
-                      T* __restrict__ pcpool) {
+                      T* __restrict__ pcpool, int dual) {
   const DevSub s = ds[blockIdx.y];
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= s.NI * s.ncp) return;
   int i = e / s.ncp, c = e % s.ncp;
   double t = 0.0;
   if (c < s.nc && i < s.ni) {
-    const T* y = pool + s.oBs + (long long)i * s.NRC + s.NI;
     const double* gi = small + s.oGinv;
-    for (int q = 0; q < s.nc; ++q) t += (double)y[q] * gi[q * s.ncp + c];
+    if (dual) {  // Phi_dual = Y_dual G^-T
+      const T* y = pool + s.oYd + (long long)i * s.ncp;
+      for (int q = 0; q < s.nc; ++q) t += (double)y[q] * gi[c * s.ncp + q];
+    } else {     // Phi = Y G^-1
+      const T* y = pool + s.oBs + (long long)i * s.NRC + s.NI;
+      for (int q = 0; q < s.nc; ++q) t += (double)y[q] * gi[q * s.ncp + c];
+    }
   }
-  pcpool[s.oPhi + e] = T(t);
+  pcpool[(dual ? s.oPhid : s.oPhi) + e] = T(t);
 }
 
 // Z = Srho^-1 - Phi Y^T on the interface block (dense, preconditioner
@@ -662,16 +944,18 @@ __global__ void k_phi(const DevSub* __restrict__ ds, const T* __restrict__ pool,
 // memory
 constexpr int NCMAX = 120;
 template <typename T>
-__global__ void k_z(const DevSub* __restrict__ ds, const T* __restrict__ pool, T* __restrict__ pcpool) {
+__global__ void k_z(const DevSub* __restrict__ ds, const T* __restrict__ pool, T* __restrict__ pcpool, int general) {
   const DevSub s = ds[blockIdx.z];
   const int i0 = blockIdx.y * 16, j0 = blockIdx.x * 16;
   if (i0 >= s.NI || j0 >= s.NI) return;
   __shared__ T ph[16][NCMAX + 1], yy[16][NCMAX + 1];
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * 16 + tx;
+  // Z = V - Phi Y^T, with Y_dual in place of Y for a general matrix (Z = V - Y G^-1 Y_dual^T)
   for (int e = tid; e < 16 * s.nc; e += 256) {
     int r = e / s.nc, c = e % s.nc;
     ph[r][c] = pcpool[s.oPhi + (long long)(i0 + r) * s.ncp + c];
-    yy[r][c] = pool[s.oBs + (long long)(j0 + r) * s.NRC + s.NI + c];
+    yy[r][c] = general ? pool[s.oYd + (long long)(j0 + r) * s.ncp + c]
+                       : pool[s.oBs + (long long)(j0 + r) * s.NRC + s.NI + c];
   }
   __syncthreads();
   const int i = i0 + ty, j = j0 + tx;
@@ -694,8 +978,10 @@ __global__ void k_z(const DevSub* __restrict__ ds, const T* __restrict__ pool, T
 // Dynamic shared memory: (nb*NB + 5*NB) elements of T.
 template <typename T>
 __global__ void __launch_bounds__(NT) k_band_solve1(const BandDesc* __restrict__ bd, const T* __restrict__ pool,
-                                                    T* __restrict__ xv, const long long* __restrict__ xoff) {
+                                                    T* __restrict__ xv, const long long* __restrict__ xoff,
+                                                    const BandDesc* __restrict__ bdb = nullptr) {
   const BandDesc d = bd[blockIdx.x];
+  const BandDesc db = bdb ? bdb[blockIdx.x] : d;  // backward factor: U^T of a general matrix, else L
   if (d.nb == 0) return;
   extern __shared__ __align__(16) unsigned char smraw[];
   T* xs = reinterpret_cast<T*>(smraw);  // nb * NB
@@ -730,14 +1016,14 @@ __global__ void __launch_bounds__(NT) k_band_solve1(const BandDesc* __restrict__
   for (int k = d.nb - 1; k >= 0; --k) {
     T acc = T(0);  // sum_{i>k} L_ik^T x_i, rows of this thread's group
     for (int i = k + 1; i <= min(d.nb - 1, k + d.w); ++i) {
-      const T* L = pool + band_block(d, i, k);
+      const T* L = pool + band_block(db, i, k);
       for (int r = grp * 16; r < grp * 16 + 16; ++r) acc += L[r * NB + c] * xs[i * NB + r];
     }
     part[grp * NB + c] = acc;
     __syncthreads();
     if (tid < NB) ts[tid] = xs[k * NB + tid] - ((part[tid] + part[NB + tid]) + (part[2 * NB + tid] + part[3 * NB + tid]));
     __syncthreads();
-    const T* Li = pool + d.oLinv + (long long)k * NB * NB;
+    const T* Li = pool + db.oLinv + (long long)k * NB * NB;
     T a2 = T(0);  // x_k = Linv_kk^T t
     for (int r = grp * 16; r < grp * 16 + 16; ++r) a2 += Li[r * NB + c] * ts[r];
     part[grp * NB + c] = a2;

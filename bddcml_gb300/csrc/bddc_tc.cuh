@@ -453,17 +453,20 @@ constexpr size_t tc_smem_bytes() { return (size_t)TC_STAGES * (2 * TC_ACHUNK + T
 // i = k + ii, each written as two 32-wide K chunks in canonical hi/lo form.
 // grid (w+1, nb, batch), 256 threads; 64x64 SIMT products in FP32.
 __global__ void __launch_bounds__(NT) k_make_panels(const BandDesc* __restrict__ bd, const TcDesc* __restrict__ td,
-                                                    const float* __restrict__ lpool, float* __restrict__ ppool) {
-  const BandDesc d = bd[blockIdx.z];
+                                                    const float* __restrict__ lpool, float* __restrict__ ppool,
+                                                    const BandDesc* __restrict__ bdb = nullptr) {
+  const BandDesc d0 = bd[blockIdx.z];
+  const BandDesc d1 = bdb ? bdb[blockIdx.z] : d0;  // backward panels: U^T of a general matrix, else L
   const TcDesc t = td[blockIdx.z];
   const int k = blockIdx.y, jj = blockIdx.x;
-  if (k >= d.nb) return;
+  if (k >= d0.nb) return;
   __shared__ __align__(16) float smA[SM_TILE];
   __shared__ __align__(16) float smB[SM_TILE];
   __shared__ float tile[NB][NB + 1];
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-  const float* Li = lpool + d.oLinv + (long long)k * NB * NB;
   for (int dir = 0; dir < 2; ++dir) {
+    const BandDesc& d = dir == 0 ? d0 : d1;
+    const float* Li = lpool + d.oLinv + (long long)k * NB * NB;
     int nblk = dir == 0 ? (k - (k - min(k, d.w)) + 1) : (min(d.w, d.nb - 1 - k) + 1);
     if (jj >= nblk) continue;
     float acc[4][4];

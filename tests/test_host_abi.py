@@ -185,3 +185,26 @@ def test_batch_upload_validation_without_gpu(built_lib):
         assert e.value.code == 1
     finally:
         B.bddcml_finalize()
+
+
+def test_host_general_matrix_upload_and_coarse_space(built_lib, oracle_mod):
+    """matrixtype 0 uploads full element matrices (no upper-triangle check); the
+    coarse space does not depend on symmetry and equals the oracle's."""
+    import bddcml_gb300 as B
+    from bddcml_gb300 import problems
+    prob = problems.convection_diffusion_on_cube(3, 2)
+    B.bddcml_init(2, [prob.nsub, 1], -1, 0, 0, 0, 0)
+    try:
+        B.upload_problem(prob)
+        with pytest.raises(B.BddcmlError) as e:  # the uploads say general, the setup says SPD
+            B.bddcml_setup_preconditioner(1, 0, 1, 1, 1, 0, 0, 0)
+        assert e.value.code == 1
+        try:
+            B.bddcml_setup_preconditioner(0, 0, 1, 1, 1, 0, 0, 0)
+        except B.BddcmlError as e:  # no GPU in this container: the host part has run
+            assert e.code == 2
+        o = oracle_mod.Oracle(prob)
+        o.setup(1, 1, 0)
+        assert B.get_coarse_info() == o.stats()
+    finally:
+        B.bddcml_finalize()
