@@ -61,7 +61,11 @@ void bddcml_upload_global_data_c(int *nelem, int *nnod, int *ndof, int *ndim, in
                                  int *neighbouring, int *load_division_int);
 
 /* replaces bddcml_upload_subdomain_data_c, src/bddcml_interface_c.h:15-27
- * (module_bddcml.f90:186-356, module_levels.f90:615-782) */
+ * (module_bddcml.f90:186-356, module_levels.f90:615-782).  matrixtype 1 (SPD)
+ * and 2 (symmetric) take the upper triangle; 0 (general) takes all entries and
+ * is solved with LU factors and a dual coarse basis (use BiCGSTAB, method 1);
+ * three levels, adaptive constraints, batched loads and reactions need a
+ * symmetric matrix (BDDCML_ERR_UNSUPPORTED otherwise). */
 void bddcml_upload_subdomain_data_c(int *nelem, int *nnod, int *ndof, int *ndim, int *meshdim,
                                     int *isub, int *nelems, int *nnods, int *ndofs,
                                     int *inet, int *linet, int *nnet, int *lnnet, int *nndf, int *lnndf,
