@@ -43,7 +43,8 @@ EXPORTS = ["bddcml_init_c", "bddcml_upload_global_data_c", "bddcml_upload_subdom
            "bddcml_set_profiling_c", "bddcml_get_profile_c", "bddcml_release_device_memory_c",
            "bddcml_dotprod_subdomain_dev_c", "bddcml_element_gradient_dev_c", "bddcml_set_adaptive_threshold_c",
            "bddcml_get_adaptive_info_c", "bddcml_upload_subdomain_rhs_batch_c", "bddcml_solve_batch_c",
-           "bddcml_download_local_solution_batch_c", "bddcml_set_batch_operator_c"]
+           "bddcml_download_local_solution_batch_c", "bddcml_set_batch_operator_c",
+           "bddcml_upload_global_data_file_c"]
 
 # phases of bddcml_get_profile_c (CUDA events on the solver stream)
 PHASES = ["numeric_total", "solve_total", "factor_interior", "solve_interior", "refine_residual", "schur",
@@ -153,6 +154,25 @@ def bddcml_upload_subdomain_data(nelem, nnod, ndof, ndim, meshdim, isub, nelems,
         _i(is_rhs_complete), p_sol, _i(l_sol), _i(matrixtype), p_i, p_j, p_a, _i(la), _i(is_assembled),
         empty, _i(0), _i(0), empty, _i(0), _i(0), empty, _i(0),
         _i(find_components_int), _i(use_dual_mesh_graph_int), _i(neighbouring))
+    _check()
+
+
+def bddcml_upload_global_data_file(nelem, nnod, ndof, ndim, meshdim, inet, nnet, nndf, xyz, ifix, fixv, rhs, sol,
+                                   elm_file: str, neighbouring: int = 1, load_division_int: int = 0):
+    """Global loading with the element matrices in a Fortran unformatted file
+    (extension of module_levels.f90:422-612); xyz is (nnod, ndim)."""
+    i_, pi = _pi(inet)
+    nn, pnn = _pi(nnet)
+    nd, pnd = _pi(nndf)
+    xyz_f = np.ascontiguousarray(np.asarray(xyz, dtype=np.float64).T)  # column-major (nnod x ndim)
+    fx, pfx = _pi(ifix)
+    fv, pfv = _pd(fixv)
+    r, pr = _pd(rhs)
+    x, px = _pd(sol)
+    lib().bddcml_upload_global_data_file_c(
+        _i(nelem), _i(nnod), _i(ndof), _i(ndim), _i(meshdim), pi, _i(len(i_)), pnn, _i(len(nn)), pnd, _i(len(nd)),
+        xyz_f.ctypes.data_as(C.POINTER(C.c_double)), _i(nnod), _i(ndim), pfx, _i(len(fx)), pfv, _i(len(fv)),
+        pr, _i(len(r)), px, _i(len(x)), C.c_char_p(elm_file.encode()), _i(neighbouring), _i(load_division_int))
     _check()
 
 

@@ -21,6 +21,7 @@ SOURCES = [
     ("bddc_abi.cpp", "g++"),
     ("bddc_adaptive.cpp", "g++"),
     ("bddc_levels.cpp", "g++"),
+    ("bddc_global.cpp", "g++"),
     ("bddc_device.cu", "nvcc"),
     ("bddc_noalloc.cu", "nvcc"),
     ("bddc_gradient.cu", "nvcc"),

@@ -97,6 +97,50 @@ void bddcml_upload_global_data_c(int*, int*, int*, int*, int*, int*, int*, int*,
   set_error(BDDCML_ERR_UNSUPPORTED, "bddcml_upload_global_data_c: global data loading is not implemented");
 }
 
+void bddcml_upload_global_data_file_c(int* nelem, int* nnod, int* ndof, int* ndim, int* meshdim, int* inet,
+                                      int* linet, int* nnet, int* lnnet, int* nndf, int* lnndf, double* xyz,
+                                      int* lxyz1, int* lxyz2, int* ifix, int* lifix, double* fixv, int* lfixv,
+                                      double* rhs, int* lrhs, double* sol, int* lsol, const char* elm_file,
+                                      int* neighbouring, int* load_division_int) {
+  guarded("bddcml_upload_global_data_file_c", [&] {
+    Solver* S = need_solver("bddcml_upload_global_data_file_c");
+    if (!S) return;
+    if (load_division_int && *load_division_int)
+      throw Error{ERR_UNSUPPORTED, "loading a stored element division is not implemented"};
+    if (!elm_file) throw Error{ERR_ARGUMENT, "no element matrix file"};
+    for (auto& s : S->subs)
+      if (s.loaded) throw Error{ERR_ARGUMENT, "subdomain data were uploaded already"};
+    if (*lnnet != *nelem || *lnndf != *nnod || *lxyz1 != *nnod || *lxyz2 != *ndim || *lifix != *ndof ||
+        *lfixv != *ndof || *lrhs != *ndof || *lsol != *ndof)
+      throw Error{ERR_ARGUMENT, "array length does not match nelem/nnod/ndof/ndim"};
+    long long snn = 0, snd = 0;
+    for (int e = 0; e < *nelem; ++e) snn += nnet[e];
+    for (int n = 0; n < *nnod; ++n) snd += nndf[n];
+    if (snn != *linet) throw Error{ERR_ARGUMENT, "NNET does not sum up to LINET"};
+    if (snd != *ndof) throw Error{ERR_ARGUMENT, "NNDF does not sum up to NDOF"};
+    GlobalData& G = S->global;
+    G = GlobalData{};
+    G.nelem = *nelem; G.nnod = *nnod; G.ndof = *ndof; G.ndim = *ndim; G.meshdim = *meshdim;
+    G.neighbouring = neighbouring ? *neighbouring : 1;
+    const int nb = S->prm.numbase;
+    G.inet.resize(*linet);
+    for (int k = 0; k < *linet; ++k) {
+      G.inet[k] = inet[k] - nb;
+      if (G.inet[k] < 0 || G.inet[k] >= *nnod) throw Error{ERR_ARGUMENT, "INET entry out of range"};
+    }
+    G.nnet.assign(nnet, nnet + *nelem);
+    G.nndf.assign(nndf, nndf + *nnod);
+    G.xyz.assign(xyz, xyz + (size_t)(*nnod) * (*ndim));
+    G.ifix.assign(ifix, ifix + *ndof);
+    G.fixv.assign(fixv, fixv + *ndof);
+    G.rhs.assign(rhs, rhs + *ndof);
+    G.sol.assign(sol, sol + *ndof);
+    G.elm_file = elm_file;
+    G.present = true;
+    S->setup_done = false;
+  });
+}
+
 void bddcml_upload_subdomain_data_c(int* nelem, int* nnod, int* ndof, int* ndim, int* meshdim, int* isub,
                                     int* nelems, int* nnods, int* ndofs, int* inet, int* linet, int* nnet,
                                     int* lnnet, int* nndf, int* lnndf, int* isngn, int* lisngn, int* isvgvn,
@@ -217,6 +261,10 @@ void bddcml_setup_preconditioner_c(int* matrixtype, int* use_defaults_int, int* 
     double t0 = wall_time();
     S->stats = Stats{};
     S->stats.t_upload = S->t_upload;
+    if (S->global.present && !S->subs.empty() && !S->subs[0].loaded) {
+      host_localize_global(*S, *matrixtype);  // global loading: divide and localise now
+      for (auto& sd : S->subs) sd.matrixtype = *matrixtype;
+    }
     host_setup(*S);
     S->stats.t_host_setup = wall_time() - t0;
     if (!S->dev) {

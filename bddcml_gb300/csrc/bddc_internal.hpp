@@ -176,9 +176,20 @@ struct SubBlocks {
 
 class Device;  // GPU side (bddc_device.cu)
 
+// global mesh and data uploaded as a whole (levels_upload_global_data,
+// module_levels.f90:422-612), localised to the subdomains at setup
+struct GlobalData {
+  bool present = false;
+  int nelem = 0, nnod = 0, ndof = 0, ndim = 0, meshdim = 0, neighbouring = 1;
+  vector<int> inet, nnet, nndf, ifix;  // 0-based node numbers in inet
+  vector<double> xyz, fixv, rhs, sol;   // xyz column-major (nnod x ndim)
+  std::string elm_file;                 // Fortran unformatted element matrices, one record per element
+};
+
 struct Solver {
   Params prm;
   vector<Subdomain> subs;
+  GlobalData global;
   int nelem = 0, nnod = 0, ndof_global = 0;
   // coarse space
   int ncorner = 0, nedge = 0, nface = 0, ndofc = 0;
@@ -220,6 +231,9 @@ void host_constraint_rows(Solver& S);
 // three-level BDDC (bddc_levels.cpp): division of the level-1 subdomains and the level-2
 // problem built from the level-1 coarse space; acs[s] = local coarse matrix of s (nc x nc)
 vector<int> host_level_division(const vector<std::array<double, 3>>& centroids, int ndim, int nparts);
+// global data to subdomain data: element division, local numbering, element
+// matrices from the ELM file (bddc_global.cpp)
+void host_localize_global(Solver& S, int matrixtype);
 std::unique_ptr<Solver> host_build_level2(const Solver& S1, const vector<vector<double>>& acs, int nsub2);
 
 // host setup (bddc_host.cpp)

@@ -60,6 +60,24 @@ void bddcml_upload_global_data_c(int *nelem, int *nnod, int *ndof, int *ndim, in
                                  double *sol, int *lsol, int *idelm,
                                  int *neighbouring, int *load_division_int);
 
+/* Global loading for C callers (extension).  The arguments of
+ * bddcml_upload_global_data_c, except that the element matrices come from
+ * the file named by elm_file instead of an open Fortran unit: a Fortran
+ * unformatted sequential file (4-byte record markers) with one record
+ * "lelm, elm(1:lelm)" per element in element order, each matrix packed as the
+ * reference packs it (column by column, upper triangle for matrixtype 1/2,
+ * full for 0; sm_pmd_make_element_numbering, module_sm.f90:272-380).  rhs is
+ * the assembled global load.  At bddcml_setup_preconditioner_c the elements
+ * are divided into nsublev[0] subdomains by recursive coordinate bisection of
+ * their centroids (the reference uses METIS) and the data are localised;
+ * everything after that is the subdomain path.  load_division_int must be 0. */
+void bddcml_upload_global_data_file_c(int *nelem, int *nnod, int *ndof, int *ndim, int *meshdim,
+                                      int *inet, int *linet, int *nnet, int *lnnet, int *nndf, int *lnndf,
+                                      double *xyz, int *lxyz1, int *lxyz2,
+                                      int *ifix, int *lifix, double *fixv, int *lfixv,
+                                      double *rhs, int *lrhs, double *sol, int *lsol, const char *elm_file,
+                                      int *neighbouring, int *load_division_int);
+
 /* replaces bddcml_upload_subdomain_data_c, src/bddcml_interface_c.h:15-27
  * (module_bddcml.f90:186-356, module_levels.f90:615-782).  matrixtype 1 (SPD)
  * and 2 (symmetric) take the upper triangle; 0 (general) takes all entries and
