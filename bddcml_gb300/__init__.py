@@ -247,6 +247,16 @@ def bddcml_change_subdomain_data(isub: int, ifix, fixv, rhs, is_rhs_complete: in
     _check()
 
 
+def bddcml_change_global_data(ifix, fixv, rhs, sol):
+    """New global fixed values, loads and initial guess (globally loaded data)."""
+    i, pi = _pi(ifix)
+    f, pf = _pd(fixv)
+    r, pr = _pd(rhs)
+    x, px = _pd(sol)
+    lib().bddcml_change_global_data_c(pi, _i(len(i)), pf, _i(len(f)), pr, _i(len(r)), px, _i(len(x)))
+    _check()
+
+
 def bddcml_setup_new_data():
     lib().bddcml_setup_new_data_c()
     _check()

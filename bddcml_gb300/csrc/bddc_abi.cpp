@@ -442,9 +442,37 @@ void bddcml_download_global_reactions_c(double* rea, int* lrea) {
   });
 }
 
-void bddcml_change_global_data_c(int*, int*, double*, int*, double*, int*, double*, int*) {
-  clear_error();
-  set_error(BDDCML_ERR_UNSUPPORTED, "bddcml_change_global_data_c: global data is not implemented");
+// new fixed values, loads and initial guess of globally loaded data
+// (levels_change_global_data): restricted to the subdomains of the division
+// made at setup, as bddcml_change_subdomain_data_c does per subdomain
+void bddcml_change_global_data_c(int* ifix, int* lifix, double* fixv, int* lfixv, double* rhs, int* lrhs,
+                                 double* sol, int* lsol) {
+  guarded("bddcml_change_global_data_c", [&] {
+    Solver* S = need_solver("bddcml_change_global_data_c");
+    if (!S) return;
+    GlobalData& G = S->global;
+    if (!G.present)
+      throw Error{ERR_UNSUPPORTED, "global data must be loaded by bddcml_upload_global_data_file_c"};
+    if (!S->setup_done) throw Error{ERR_ARGUMENT, "data can be changed only after bddcml_setup_preconditioner"};
+    if (*lifix != G.ndof || *lfixv != G.ndof || *lrhs != G.ndof || *lsol != G.ndof)
+      throw Error{ERR_ARGUMENT, "array length does not match the global dof count"};
+    for (int q = 0; q < G.ndof; ++q)
+      if ((ifix[q] != 0) != (G.ifix[q] != 0))
+        throw Error{ERR_UNSUPPORTED, "the set of fixed dofs changed; that needs a new setup"};
+    G.fixv.assign(fixv, fixv + G.ndof);
+    G.rhs.assign(rhs, rhs + G.ndof);
+    G.sol.assign(sol, sol + G.ndof);
+    for (auto& s : S->subs) {
+      for (int q = 0; q < s.ndof; ++q) {
+        const int g = s.isvgvn[q];
+        s.fixv[q] = G.fixv[g];
+        s.rhs[q] = G.rhs[g];
+        s.sol[q] = G.sol[g];
+      }
+      s.rhs_complete = true;
+    }
+    S->new_data_pending = true;
+  });
 }
 
 void bddcml_change_subdomain_data_c(int* isub, int* ifix, int* lifix, double* fixv, int* lfixv, double* rhs,

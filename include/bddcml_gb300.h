@@ -171,8 +171,10 @@ void bddcml_download_local_reactions_c(int *isub, double *reas, int *lreas);
  * (module_levels.f90:4785-4914): the subdomains' reactions at their global dofs. */
 void bddcml_download_global_reactions_c(double *rea, int *lrea);
 
-/* replaces bddcml_change_global_data_c, src/bddcml_interface_c.h:49; it needs data
- * loaded by bddcml_upload_global_data_c, which is not implemented (unsupported) */
+/* replaces bddcml_change_global_data_c, src/bddcml_interface_c.h:49: new fixed
+ * values, loads and initial guess of data loaded by
+ * bddcml_upload_global_data_file_c (BDDCML_ERR_UNSUPPORTED otherwise), after
+ * setup and with the same fixed dofs; takes effect at bddcml_setup_new_data_c. */
 void bddcml_change_global_data_c(int *ifix, int *lifix, double *fixv, int *lfixv, double *rhs, int *lrhs,
                                  double *sol, int *lsol);
 

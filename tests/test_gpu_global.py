@@ -50,3 +50,34 @@ def test_global_convection_diffusion(built_lib, tmp_path):
     assert reason == 0
     ud = _direct(gp)
     assert np.linalg.norm(u - ud) / np.linalg.norm(ud) <= 1e-7
+
+
+def test_change_global_data(built_lib, tmp_path):
+    """bddcml_change_global_data_c + bddcml_setup_new_data_c on globally loaded
+    data (levels_change_global_data): new loads and nonzero boundary values."""
+    import bddcml_gb300 as B
+    from bddcml_gb300 import pmd
+    gp = pmd.poisson_global(8)
+    prefix = str(tmp_path / "p8")
+    pmd.write_problem(prefix, gp, [8, 1], tol=1e-10)
+    par, d = pmd.read_problem(prefix)
+    B.bddcml_init(2, [8, 1], -1, 0, 0, 0, 0)
+    try:
+        B.bddcml_upload_global_data_file(par["nelem"], par["nnod"], par["ndof"], 3, 3, d["inet"], d["nnet"],
+                                         d["nndf"], d["xyz"], d["ifix"], d["fixv"], d["rhs"], np.zeros(par["ndof"]),
+                                         prefix + ".ELM")
+        B.bddcml_setup_preconditioner(1, 0, 1, 1, 1, 0, 0, 0)
+        B.bddcml_solve(0, 0, 1e-10, 500, 50, 0, 0)
+        rng = np.random.default_rng(4)
+        x = gp.xyz
+        gp.fixv = np.where(gp.ifix != 0, 1.0 + x[:, 0] + x[:, 1] * x[:, 2], 0.0)
+        gp.rhs = np.where(gp.ifix != 0, 0.0, rng.uniform(0.5, 1.5, gp.ndof) / 8 ** 3)
+        B.bddcml_change_global_data(gp.ifix, gp.fixv, gp.rhs, np.zeros(gp.ndof))
+        B.bddcml_setup_new_data()
+        it, reason, _ = B.bddcml_solve(0, 0, 1e-10, 500, 50, 0, 0)
+        u = B.bddcml_download_global_solution(gp.ndof)
+    finally:
+        B.bddcml_finalize()
+    assert reason == 0
+    ud = _direct(gp)
+    assert np.linalg.norm(u - ud) / np.linalg.norm(ud) <= 1e-8

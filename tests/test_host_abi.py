@@ -114,10 +114,12 @@ def test_errors_are_status_codes(built_lib):
     with pytest.raises(B.BddcmlError) as ei:
         B.bddcml_setup_preconditioner(1, 0, 1, 1, 1, 1, 0, 0)  # adaptive constraints
     assert ei.value.code in (1, 4)
+    # changing global data without global loading is reported unsupported, not aborted
+    z = np.zeros(prob.ndof)
+    with pytest.raises(B.BddcmlError) as ei:
+        B.bddcml_change_global_data(np.zeros(prob.ndof, dtype=np.int32), z, z, z)
+    assert ei.value.code == 4
     B.bddcml_finalize()
-    # global-data loading is reported unsupported, not aborted
-    B.lib().bddcml_change_global_data_c(None, None, None, None, None, None, None, None)
-    assert B.last_error()[0] == 4
     # the global solution needs an initialised solver
     B.lib().bddcml_download_global_solution_c(None, None)
     assert B.last_error()[0] == 1
