@@ -58,6 +58,24 @@ static void batch_prepare_oz(Device& D) {
   B.oz = true;
 }
 
+// the FP32 products of the preconditioner: 3xTF32 tensor cores with the
+// sliced Schur operator (operator 1), FP32 SIMT otherwise
+template <typename T>
+static void gemm_pc(Device& D, const GemmDesc* gd, int ndesc, int maxm, const T* A, const T* B1, const T* B2, int ldb,
+                    double* out, const double* addend, int ldo, int nk, const int* ndone) {
+  if constexpr (std::is_same_v<T, float>) {
+    if (D.bt.oz) {
+      raise_smem(kb_gemm_tc3, GC_SMEM);
+      kb_gemm_tc3<<<dim3((maxm + TC_M - 1) / TC_M, ndesc), GC_THREADS, GC_SMEM, D.st>>>(gd, A, B1, B2, ldb, out,
+                                                                                        addend, ldo, nk, D.err,
+                                                                                        ndone);
+      CKL();
+      return;
+    }
+  }
+  gemm_t<T>(D, gd, ndesc, maxm, A, B1, B2, ldb, out, addend, ldo, nk, ndone);
+}
+
 template <typename T>
 static void batch_prepare(Device& D, int nk, int lg, int maxit, int* shared_ndone, bool level2, int op = 0) {
   BatchBufs& B = D.bt;
@@ -256,8 +274,8 @@ static void batch_pc(Device& D, const double* rin, double* zout, double* part) {
                                                                       B.ndone);
   CKL();
   if (D.ndofc > 0) {
-    gemm_t<T>(D, B.gP, D.nsub, D.ncpmax, static_cast<const T*>(B.phit), aux, nullptr, nk, B.rcs, nullptr, nk, nk,
-              B.ndone);
+    gemm_pc<T>(D, B.gP, D.nsub, D.ncpmax, static_cast<const T*>(B.phit), aux, nullptr, nk, B.rcs, nullptr, nk, nk,
+               B.ndone);
     kb_coarse_gather<<<blocks_for((long long)D.ndofc << lg), 256, 0, st>>>(D.ndofc, lg, D.co_ptr, D.co_sub,
                                                                            D.co_loc, D.ds, B.rcs, B.rc, B.ndone);
     CKL();
@@ -286,7 +304,7 @@ static void batch_pc(Device& D, const double* rin, double* zout, double* part) {
     CKL();
   }
   // zrep = Z_s aux_s + Phi_s uc_s in one product per subdomain
-  gemm_t<T>(D, B.gZ, D.nsub, D.maxNI, pc, aux, ucs, nk, B.zrep, nullptr, nk, nk, B.ndone);
+  gemm_pc<T>(D, B.gZ, D.nsub, D.maxNI, pc, aux, ucs, nk, B.zrep, nullptr, nk, nk, B.ndone);
   D.prof.end(PH_PC_LOCAL, st);
   kb_assemble_z<<<D.npart, RT, 0, st>>>(D.n, lg, D.own, B.zrep, D.wrep, D.wsum, rin, zout, part, D.npart, B.ndone);
   CKL();

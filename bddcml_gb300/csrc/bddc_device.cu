@@ -18,6 +18,7 @@
 #include "bddc_adaptive.cuh"
 #include "bddc_batch_kernels.cuh"
 #include "bddc_ozaki.cuh"
+#include "bddc_batch_tc.cuh"
 #include "bddc_internal.hpp"
 #include "bddc_pcg_kernels.cuh"
 #include "bddc_tc.cuh"
