@@ -58,22 +58,72 @@ static void batch_prepare_oz(Device& D) {
   B.oz = true;
 }
 
-// the FP32 products of the preconditioner: 3xTF32 tensor cores with the
-// sliced Schur operator (operator 1), FP32 SIMT otherwise
-template <typename T>
-static void gemm_pc(Device& D, const GemmDesc* gd, int ndesc, int maxm, const T* A, const T* B1, const T* B2, int ldb,
-                    double* out, const double* addend, int ldo, int nk, const int* ndone) {
-  if constexpr (std::is_same_v<T, float>) {
-    if (D.bt.oz) {
-      raise_smem(kb_gemm_tc3, GC_SMEM);
-      kb_gemm_tc3<<<dim3((maxm + TC_M - 1) / TC_M, ndesc), GC_THREADS, GC_SMEM, D.st>>>(gd, A, B1, B2, ldb, out,
-                                                                                        addend, ldo, nk, D.err,
-                                                                                        ndone);
-      CKL();
-      return;
-    }
+// A tiles and job lists of the 3xTF32 preconditioner products (bddc_batch_tc.cuh),
+// made once per batch setup: [Z | Phi] from the preconditioner pool, Phi^T from phit
+static void batch_prepare_tc(Device& D) {
+  BatchBufs& B = D.bt;
+  auto& mem = B.mem;
+  const bool coarse = D.ndofc > 0;
+  vector<long long> zoff(D.nsub), poff(D.nsub), boff(D.nsub);
+  vector<TcJob> jz, jp;
+  long long nz = 0, np = 0, nb = 0;
+  int mch1 = 0, mch2 = 0, maxz = 0, maxp = 0;
+  for (int t = 0; t < D.nsub; ++t) {
+    const DevSub& d = D.hs[t];
+    const int n1 = (d.ni + TC_KC - 1) / TC_KC, n2 = coarse ? (d.nc + TC_KC - 1) / TC_KC : 0;
+    mch1 = std::max(mch1, n1);
+    mch2 = std::max(mch2, n2);
+    boff[t] = nb;
+    nb += (long long)(n1 + n2) * GC_TILE;
+    const int nrz = (d.ni + TC_M - 1) / TC_M;
+    zoff[t] = nz;
+    for (int rt = 0; rt < nrz; ++rt)
+      jz.push_back(TcJob{nz + (long long)rt * (n1 + n2) * GC_TILE, boff[t], (long long)d.rep + rt * TC_M,
+                         std::min(TC_M, d.ni - rt * TC_M), n1 + n2});
+    nz += (long long)nrz * (n1 + n2) * GC_TILE;
+    maxz = std::max(maxz, nrz * (n1 + n2));
+    const int nrp = coarse ? (d.nc + TC_M - 1) / TC_M : 0;
+    poff[t] = np;
+    for (int rt = 0; rt < nrp; ++rt)
+      jp.push_back(TcJob{np + (long long)rt * n1 * GC_TILE, boff[t], (long long)d.coff + rt * TC_M,
+                         std::min(TC_M, d.nc - rt * TC_M), n1});
+    np += (long long)nrp * n1 * GC_TILE;
+    maxp = std::max(maxp, nrp * n1);
   }
-  gemm_t<T>(D, gd, ndesc, maxm, A, B1, B2, ldb, out, addend, ldo, nk, ndone);
+  B.tc_az = dalloc<float>(std::max(1LL, nz), mem);
+  B.tc_ap = dalloc<float>(std::max(1LL, np), mem);
+  B.tc_b = dalloc<float>(std::max(1LL, nb), mem);
+  B.tc_boff = upload(boff, mem, D.st);
+  B.tc_jz = upload(jz, mem, D.st);
+  B.tc_njz = (int)jz.size();
+  B.tc_jp = jp.empty() ? nullptr : upload(jp, mem, D.st);
+  B.tc_njp = (int)jp.size();
+  B.tc_mch1 = mch1;
+  B.tc_mch2 = mch2;
+  int dev = 0, nsm = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  B.tc_grid = std::max(1, nsm);
+  if (maxz > 0) {
+    kb_tile_a<<<dim3(maxz, D.nsub), 256, 0, D.st>>>(B.gZ, upload(zoff, mem, D.st),
+                                                     static_cast<const float*>(D.poolPC), B.tc_az);
+    CKL();
+  }
+  if (coarse && maxp > 0) {
+    kb_tile_a<<<dim3(maxp, D.nsub), 256, 0, D.st>>>(B.gP, upload(poff, mem, D.st),
+                                                     static_cast<const float*>(B.phit), B.tc_ap);
+    CKL();
+  }
+}
+
+// out rows of every job = A tile rows x the B chunks (kb_gemm_tc3)
+static void gemm_tc(Device& D, const TcJob* jobs, int njobs, const float* At, double* out, int nk,
+                    const int* ndone) {
+  if (njobs <= 0) return;
+  raise_smem(kb_gemm_tc3, GC_SMEM);
+  kb_gemm_tc3<<<std::min(njobs, D.bt.tc_grid), GC_THREADS, GC_SMEM, D.st>>>(jobs, njobs, At, D.bt.tc_b, out, nullptr,
+                                                                            nk, nk, D.err, ndone);
+  CKL();
 }
 
 template <typename T>
@@ -180,7 +230,10 @@ static void batch_prepare(Device& D, int nk, int lg, int maxit, int* shared_ndon
     }
     B.gA = upload(ga, mem, D.st);
   }
-  if (want_oz) batch_prepare_oz(D);
+  if (want_oz) {
+    batch_prepare_oz(D);
+    if constexpr (std::is_same_v<T, float>) batch_prepare_tc(D);
+  }
   if (!level2) {  // multi-column interior solves of the loads and of the interior resolve
     const int vld = D.mixed ? TC_M : NB;
     const int ncomp = D.mixed ? 3 : 1;
@@ -269,13 +322,24 @@ static void batch_pc(Device& D, const double* rin, double* zout, double* part) {
   const T* pc = static_cast<const T*>(D.poolPC);
   T* aux = static_cast<T*>(B.aux);
   T* ucs = static_cast<T*>(B.ucs);
+  // with the sliced Schur operator the FP32 products run on the tensor cores
+  // (3xTF32) from pre-tiled A and the split B chunks, else on the FP32 SIMT pipes
+  const bool tc = std::is_same_v<T, float> && B.tc_az != nullptr;
   D.prof.begin(PH_PC_LOCAL, st);
-  kb_gather_t<T><<<blocks_for((long long)D.nrep << lg), 256, 0, st>>>(D.nrep, lg, D.uniq, D.wrep, 1.0, rin, aux,
-                                                                      B.ndone);
+  if (tc) {
+    kb_tile_b<<<dim3(B.tc_mch1, D.nsub), 256, 0, st>>>(1, D.ds, B.tc_boff, lg, D.uniq, D.wrep, rin, B.tc_b,
+                                                        B.ndone);
+  } else {
+    kb_gather_t<T><<<blocks_for((long long)D.nrep << lg), 256, 0, st>>>(D.nrep, lg, D.uniq, D.wrep, 1.0, rin, aux,
+                                                                        B.ndone);
+  }
   CKL();
   if (D.ndofc > 0) {
-    gemm_pc<T>(D, B.gP, D.nsub, D.ncpmax, static_cast<const T*>(B.phit), aux, nullptr, nk, B.rcs, nullptr, nk, nk,
-               B.ndone);
+    if (tc)
+      gemm_tc(D, B.tc_jp, B.tc_njp, B.tc_ap, B.rcs, nk, B.ndone);
+    else
+      gemm_t<T>(D, B.gP, D.nsub, D.ncpmax, static_cast<const T*>(B.phit), aux, nullptr, nk, B.rcs, nullptr, nk, nk,
+                B.ndone);
     kb_coarse_gather<<<blocks_for((long long)D.ndofc << lg), 256, 0, st>>>(D.ndofc, lg, D.co_ptr, D.co_sub,
                                                                            D.co_loc, D.ds, B.rcs, B.rc, B.ndone);
     CKL();
@@ -298,13 +362,24 @@ static void batch_pc(Device& D, const double* rin, double* zout, double* part) {
         gemm_t<T>(D, B.gC, 1, D.ndofc, minv, cb, nullptr, nk, B.uc, B.uc, nk, nk, B.ndone);
       }
     }
-    long long ncon = 0;
-    for (auto& d : D.hs) ncon = std::max(ncon, (long long)d.coff + d.nc);
-    kb_gather_uc<T><<<blocks_for(ncon << lg), 256, 0, st>>>(ncon, lg, D.cmap, B.uc, ucs, B.ndone);
-    CKL();
+    if (tc) {
+      if (B.tc_mch2 > 0) {
+        kb_tile_b<<<dim3(B.tc_mch2, D.nsub), 256, 0, st>>>(2, D.ds, B.tc_boff, lg, D.cmap, nullptr, B.uc, B.tc_b,
+                                                            B.ndone);
+        CKL();
+      }
+    } else {
+      long long ncon = 0;
+      for (auto& d : D.hs) ncon = std::max(ncon, (long long)d.coff + d.nc);
+      kb_gather_uc<T><<<blocks_for(ncon << lg), 256, 0, st>>>(ncon, lg, D.cmap, B.uc, ucs, B.ndone);
+      CKL();
+    }
   }
-  // zrep = Z_s aux_s + Phi_s uc_s in one product per subdomain
-  gemm_pc<T>(D, B.gZ, D.nsub, D.maxNI, pc, aux, ucs, nk, B.zrep, nullptr, nk, nk, B.ndone);
+  // zrep = Z_s W_s r_s + Phi_s uc_s in one product per subdomain
+  if (tc)
+    gemm_tc(D, B.tc_jz, B.tc_njz, B.tc_az, B.zrep, nk, B.ndone);
+  else
+    gemm_t<T>(D, B.gZ, D.nsub, D.maxNI, pc, aux, ucs, nk, B.zrep, nullptr, nk, nk, B.ndone);
   D.prof.end(PH_PC_LOCAL, st);
   kb_assemble_z<<<D.npart, RT, 0, st>>>(D.n, lg, D.own, B.zrep, D.wrep, D.wsum, rin, zout, part, D.npart, B.ndone);
   CKL();

@@ -1,15 +1,28 @@
-// Batched working-precision product on the tensor cores (3xTF32, TMEM
+// Batched working-precision products on the tensor cores (3xTF32, TMEM
 // accumulation) for the FP32 preconditioner blocks of the batched solve:
-//   out[oo + r][c] = addend + sum_j A1[r][j] B1[ob + j][c] + sum_j A2[r][j] B2[ob2 + j][c],  c < nk
-// with the operands of kb_gemm_t<float> (GemmDesc).  One CTA per 128-row tile
-// of one product: MMA M = 128 (rows of A), N = 64 (columns), K = 8 per
-// instruction; each FP32 operand is split into TF32 hi + lo while staging and
-// D += a_lo b_hi + a_hi b_lo + a_hi b_hi (Ootomo and Yokota's 3xTF32, about
-// the accuracy of the FP32 SIMT product it replaces).  Warps 0-3 stage K
-// chunks of 32 into the canonical K-major layout (A rows read as 16-byte
-// pieces, eight threads per 128-byte row segment; the column block of B is
-// transposed on the way) and write the result; one thread of warp 4 issues the
-// MMAs.  Every wait is bounded and reports DE_TIMEOUT.
+//   out[o + r][c] = addend + sum_j A[r][j] B[j][c],   r < m, c < nk
+// for a list of jobs, each one 128-row tile of one subdomain product
+// ([Z | Phi] with [W r ; u_c], or Phi^T with W r).
+//
+// Operands are laid out for the kernel once:
+//  * A tiles (batch setup): every 128 x 32 chunk of A is one 16 KB block in
+//    the canonical K-major no-swizzle order of the MMA (rows and K beyond the
+//    matrix are zero), so one cp.async.bulk moves it;
+//  * B chunks (every application, kb_tile_b): the 32 x 64 chunk of the
+//    right-hand sides, split into TF32 hi and lo and transposed to the same
+//    order, 16 KB per chunk.
+// The A chunk is split into hi and lo in shared memory, in place, each thread
+// on its own 16-byte pieces, and D += a_lo b_hi + a_hi b_lo + a_hi b_hi
+// (Ootomo and Yokota's 3xTF32, the accuracy of an FP32 product).
+//
+// Persistent and warp-specialised, one CTA per SM over the job list:
+//   warp 8  (one thread) issues the bulk copies into a 4-stage ring,
+//   warps 0-3 split the A chunks,
+//   warp 9  (one thread) issues the MMAs into one of two TMEM accumulators,
+//   warps 4-7 read the finished accumulator and write the rows,
+// so the epilogue of one tile overlaps the main loop of the next.  Every
+// wait is bounded; a timeout sets DE_TIMEOUT, and the CTA waits (bounded) for
+// its copies and MMAs in flight before it frees TMEM and returns.
 #pragma once
 
 #include "bddc_batch_kernels.cuh"
@@ -17,47 +30,53 @@
 
 namespace bddc {
 
-constexpr int GC_STAGES = 2;         // canonical hi / lo operand stages read by the MMAs
-constexpr int GC_RAW = 4;            // raw FP32 chunks in flight (cp.async ring)
-constexpr int GC_AH = TC_M * TC_KC;   // floats of one A half (hi or lo) per stage
-constexpr int GC_BH = BMAX * TC_KC;   // floats of one B half
-constexpr int GC_THREADS = TC_THREADS + 32;
-constexpr int GC_RLA = TC_KC + 4;     // padded row of the raw A chunk (conflict-free column reads)
-constexpr int GC_RLB = BMAX + 8;      // padded K row of the raw B chunk
-constexpr int GC_RA = TC_M * GC_RLA, GC_RB = TC_KC * GC_RLB;
-constexpr size_t GC_SMEM =
-    ((size_t)GC_STAGES * (2 * GC_AH + 2 * GC_BH) + (size_t)GC_RAW * (GC_RA + GC_RB)) * sizeof(float) + 1024;
+// One 128-row output tile: A chunks at a, a + GC_TILE, ...; B chunks at b, ...
+struct TcJob {
+  long long a, b;  // float offsets of the first A chunk and of the first B chunk
+  long long o;     // output row of tile row 0
+  int m, nch;      // valid rows (<= TC_M), K chunks
+};
+
+constexpr int GC_STAGES = 4;
+constexpr int GC_TILE = TC_M * TC_KC;   // floats of one A chunk, or of one B chunk (hi | lo)
+constexpr int GC_BHALF = BMAX * TC_KC;  // floats of the hi (or lo) half of a B chunk
+constexpr int GC_STAGE = 3 * GC_TILE;   // A (split in place into hi) | A lo | B hi, lo
+constexpr int GC_THREADS = 320;
+constexpr int GC_PRODUCER = 8, GC_ISSUER = 9;  // warps
+constexpr size_t GC_SMEM = (size_t)GC_STAGES * GC_STAGE * sizeof(float) + 1024;
+static_assert(GC_BHALF * 2 == GC_TILE, "a B chunk is 64 columns x 32 K, hi and lo");
 
 __global__ void __launch_bounds__(GC_THREADS, 1)
-    kb_gemm_tc3(const GemmDesc* __restrict__ gd, const float* __restrict__ A, const float* __restrict__ B1,
-                const float* __restrict__ B2, int ldb, double* out, const double* addend, int ldo, int nk,
+    kb_gemm_tc3(const TcJob* __restrict__ jobs, int njobs, const float* __restrict__ At,
+                const float* __restrict__ Bt, double* out, const double* addend, int ldo, int nk,
                 int* __restrict__ err, const int* __restrict__ ndone) {
   if (batch_all_done(ndone, nk)) return;
-  const GemmDesc d = gd[blockIdx.y];
-  const int r0 = blockIdx.x * TC_M;
-  if (r0 >= d.m) return;
   extern __shared__ __align__(1024) unsigned char gc_raw[];
   float* smem = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(gc_raw) + 1023) & ~uintptr_t(1023));
-  float* sA = smem;                          // [stage][hi | lo][GC_AH]
-  float* sB = smem + GC_STAGES * 2 * GC_AH;  // [stage][hi | lo][GC_BH]
-  float* rA = sB + GC_STAGES * 2 * GC_BH;    // [raw stage][128 rows][GC_RLA] row-major
-  float* rB = rA + GC_RAW * GC_RA;           // [raw stage][32 K rows][GC_RLB] row-major
-  __shared__ __align__(8) uint64_t bar_a[GC_STAGES], bar_mma[GC_STAGES], bar_done;
+  __shared__ __align__(8) uint64_t bar_full[GC_STAGES], bar_split[GC_STAGES], bar_empty[GC_STAGES];
+  __shared__ __align__(8) uint64_t bar_acc_full[2], bar_acc_empty[2];
   __shared__ uint32_t tmem_base;
   __shared__ volatile int abort_flag;
-  __shared__ long long last_commit;
+  __shared__ long long last_load[GC_STAGES], last_mma;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int n1 = (d.k1 + TC_KC - 1) / TC_KC, nch = n1 + (d.k2 + TC_KC - 1) / TC_KC;
   if (tid == 0) {
-    for (int s = 0; s < GC_STAGES; ++s) { mbar_init(&bar_a[s], TC_THREADS); mbar_init(&bar_mma[s], 1); }
-    mbar_init(&bar_done, 1);
+    for (int s = 0; s < GC_STAGES; ++s) {
+      mbar_init(&bar_full[s], 1);
+      mbar_init(&bar_split[s], TC_THREADS);
+      mbar_init(&bar_empty[s], 1);
+      last_load[s] = -1;
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&bar_acc_full[b], 1);
+      mbar_init(&bar_acc_empty[b], TC_THREADS);
+    }
     abort_flag = 0;
-    last_commit = -1;
+    last_mma = -1;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
-                 "r"(BMAX));
+                 "r"(2 * BMAX));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   tc_fence_before();
@@ -65,149 +84,216 @@ __global__ void __launch_bounds__(GC_THREADS, 1)
   tc_fence_after();
   const uint32_t tmem = tmem_base;
 
-  if (warp == TC_THREADS / 32) {
+  if (warp == GC_PRODUCER) {
+    // ------------------------------------------------ bulk copies (one thread)
+    if (lane == 0) {
+      long long q = 0;
+      bool ok = true;
+      for (int j = blockIdx.x; j < njobs && ok; j += gridDim.x) {
+        const TcJob jb = jobs[j];
+        for (int c = 0; c < jb.nch; ++c, ++q) {
+          const int s = (int)(q % GC_STAGES);
+          const long long use = q / GC_STAGES;
+          if (abort_flag || (use > 0 && !mbar_wait(&bar_empty[s], (uint32_t)((use - 1) & 1)))) {
+            abort_flag = 1;
+            ok = false;
+            break;
+          }
+          float* st = smem + s * GC_STAGE;
+          mbar_expect_tx(&bar_full[s], 2 * GC_TILE * (uint32_t)sizeof(float));
+          bulk_g2s(st, At + jb.a + (long long)c * GC_TILE, GC_TILE * sizeof(float), &bar_full[s]);
+          bulk_g2s(st + 2 * GC_TILE, Bt + jb.b + (long long)c * GC_TILE, GC_TILE * sizeof(float), &bar_full[s]);
+          last_load[s] = q;
+        }
+      }
+    }
+  } else if (warp == GC_ISSUER) {
     // ------------------------------------------------ MMA issuer (one thread)
     if (lane == 0) {
       constexpr uint32_t idesc = tc_idesc(TC_M, BMAX);
-      for (int g = 0; g < nch; ++g) {
-        const int st = g % GC_STAGES;
-        if (!mbar_wait(&bar_a[st], (uint32_t)((g / GC_STAGES) & 1))) { abort_flag = 1; break; }
-        tc_fence_after();
-        const uint32_t a_hi = smem_u32(sA + (st * 2 + 0) * GC_AH), a_lo = smem_u32(sA + (st * 2 + 1) * GC_AH);
-        const uint32_t b_hi = smem_u32(sB + (st * 2 + 0) * GC_BH), b_lo = smem_u32(sB + (st * 2 + 1) * GC_BH);
-#pragma unroll
-        for (int kk = 0; kk < TC_KC / 8; ++kk) {
-          const uint32_t koff = kk * 2 * TC_LBO;
-          const uint32_t acc = (g > 0 || kk > 0) ? 1u : 0u;
-          mma_tf32(tmem, tc_desc(a_lo + koff), tc_desc(b_hi + koff), idesc, acc);
-          mma_tf32(tmem, tc_desc(a_hi + koff), tc_desc(b_lo + koff), idesc, 1u);
-          mma_tf32(tmem, tc_desc(a_hi + koff), tc_desc(b_hi + koff), idesc, 1u);
+      long long q = 0;
+      int t = 0;
+      for (int j = blockIdx.x; j < njobs; j += gridDim.x, ++t) {
+        const int nch = jobs[j].nch;
+        const int ab = t & 1;
+        if (abort_flag || (t >= 2 && !mbar_wait(&bar_acc_empty[ab], (uint32_t)((t / 2 - 1) & 1)))) {
+          abort_flag = 1;
+          break;
         }
-        mma_commit(&bar_mma[st]);
-        last_commit = g;
+        tc_fence_after();
+        const uint32_t dt = tmem + (uint32_t)(ab * BMAX);
+        bool ok = true;
+        for (int c = 0; c < nch; ++c, ++q) {
+          const int s = (int)(q % GC_STAGES);
+          if (abort_flag || !mbar_wait(&bar_split[s], (uint32_t)((q / GC_STAGES) & 1))) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t a_hi = smem_u32(smem + s * GC_STAGE), a_lo = a_hi + GC_TILE * 4;
+          const uint32_t b_hi = a_hi + 2 * GC_TILE * 4, b_lo = b_hi + GC_BHALF * 4;
+#pragma unroll
+          for (int kk = 0; kk < TC_KC / 8; ++kk) {
+            const uint32_t koff = kk * 2 * TC_LBO;
+            const uint32_t acc = (c > 0 || kk > 0) ? 1u : 0u;
+            mma_tf32(dt, tc_desc(a_lo + koff), tc_desc(b_hi + koff), idesc, acc);
+            mma_tf32(dt, tc_desc(a_hi + koff), tc_desc(b_lo + koff), idesc, 1u);
+            mma_tf32(dt, tc_desc(a_hi + koff), tc_desc(b_hi + koff), idesc, 1u);
+          }
+          mma_commit(&bar_empty[s]);
+          last_mma = q;
+        }
+        if (!ok) {
+          abort_flag = 1;
+          break;
+        }
+        mma_commit(&bar_acc_full[ab]);
       }
-      mma_commit(&bar_done);
+    }
+  } else if (warp < 4) {
+    // ------------------------------------------------ in-place TF32 split of the A chunks
+    long long q = 0;
+    bool ok = true;
+    for (int j = blockIdx.x; j < njobs && ok; j += gridDim.x) {
+      const int nch = jobs[j].nch;
+      for (int c = 0; c < nch; ++c, ++q) {
+        const int s = (int)(q % GC_STAGES);
+        if (abort_flag || !mbar_wait(&bar_full[s], (uint32_t)((q / GC_STAGES) & 1))) {
+          abort_flag = 1;
+          ok = false;
+          break;
+        }
+        float* ahi = smem + s * GC_STAGE;
+        float* alo = ahi + GC_TILE;
+#pragma unroll
+        for (int i = 0; i < GC_TILE / 4 / TC_THREADS; ++i) {
+          const int p = (tid + TC_THREADS * i) * 4;
+          const float4 x = *reinterpret_cast<const float4*>(ahi + p);
+          float4 h, l;
+          h.x = tf32_rna(x.x); l.x = tf32_rna(x.x - h.x);
+          h.y = tf32_rna(x.y); l.y = tf32_rna(x.y - h.y);
+          h.z = tf32_rna(x.z); l.z = tf32_rna(x.z - h.z);
+          h.w = tf32_rna(x.w); l.w = tf32_rna(x.w - h.w);
+          *reinterpret_cast<float4*>(ahi + p) = h;
+          *reinterpret_cast<float4*>(alo + p) = l;
+        }
+        fence_async_smem();
+        mbar_arrive(&bar_split[s]);
+      }
     }
   } else {
-    // ------------------------------------------------ staging + epilogue (128 threads)
-    // raw chunks move by cp.async (zero-filled outside the operands), GC_RAW - 1
-    // of them ahead of the one being split into the canonical hi / lo stages
-    auto load = [&](int g) {
-      const int rs = g % GC_RAW;
-      const bool seg1 = g < n1;
-      const int kb = seg1 ? g * TC_KC : (g - n1) * TC_KC;
-      const int K = seg1 ? d.k1 : d.k2;
-      const float* Ab = A + (seg1 ? d.oA : d.oA2);
-      const int lda = seg1 ? d.lda : d.lda2;
-      const float* Bb = seg1 ? B1 + d.ob * ldb : B2 + d.ob2 * ldb;
-#pragma unroll
-      for (int i = 0; i < 8; ++i) {  // A: row e >> 3, 16-byte piece e & 7
-        const int e = tid + TC_THREADS * i;
-        const int r = e >> 3, k = kb + (e & 7) * 4;
-        const int nb = (r0 + r < d.m && k < K) ? 4 * min(4, K - k) : 0;
-        const float* src = nb ? Ab + (long long)(r0 + r) * lda + k : Ab;
-        cp_async16(rA + rs * GC_RA + r * GC_RLA + (e & 7) * 4, src, nb);
+    // ------------------------------------------------ epilogue (warps 4-7 read TMEM lanes 32 (warp - 4) ..)
+    const int ew = warp - 4;
+    int t = 0;
+    for (int j = blockIdx.x; j < njobs; j += gridDim.x, ++t) {
+      const TcJob jb = jobs[j];
+      const int ab = t & 1;
+      if (abort_flag || !mbar_wait(&bar_acc_full[ab], (uint32_t)((t / 2) & 1))) {
+        abort_flag = 1;
+        break;
       }
-#pragma unroll
-      for (int i = 0; i < 4; ++i) {  // B: K row e >> 4, columns 4 (e & 15) .. +3
-        const int e = tid + TC_THREADS * i;
-        const int k = e >> 4, c = (e & 15) * 4;
-        const int nb = (kb + k < K && c < nk) ? 16 : 0;
-        const float* src = nb ? Bb + (long long)(kb + k) * ldb + c : Bb;
-        cp_async16(rB + rs * GC_RB + k * GC_RLB + c, src, nb);
-      }
-    };
-    auto split = [](float x, float& h, float& l) { h = tf32_rna(x); l = x - h; };
-    bool ok = true;
-#pragma unroll
-    for (int q = 0; q < GC_RAW - 1; ++q) {
-      if (q < nch) load(q);
-      cp_async_commit();
-    }
-    for (int g = 0; g < nch && ok; ++g) {
-      const int st = g % GC_STAGES, rs = g % GC_RAW;
-      cp_async_wait<GC_RAW - 2>();  // chunk g has landed (this thread's part)
-      // ... and everyone's; everyone has also finished splitting chunk g - 1,
-      // so its raw slot may take chunk g + GC_RAW - 1
-      asm volatile("bar.sync 1, %0;" ::"r"(TC_THREADS) : "memory");
-      if (g + GC_RAW - 1 < nch) load(g + GC_RAW - 1);
-      cp_async_commit();
-      if (g >= GC_STAGES &&
-          !mbar_wait(&bar_mma[st], (uint32_t)(((g - GC_STAGES) / GC_STAGES) & 1))) { abort_flag = 1; ok = false; break; }
-      float* ahi = sA + (st * 2 + 0) * GC_AH;
-      float* alo = sA + (st * 2 + 1) * GC_AH;
-      float* bhi = sB + (st * 2 + 0) * GC_BH;
-      float* blo = sB + (st * 2 + 1) * GC_BH;
-      const float* ra = rA + rs * GC_RA;
-      const float* rb = rB + rs * GC_RB;
-      // A: a quarter-warp takes 8 consecutive rows of one 16-byte column piece,
-      // so both the padded raw reads and the canonical stores are conflict-free
-#pragma unroll
-      for (int i = 0; i < 8; ++i) {
-        const int e = tid + TC_THREADS * i;
-        const int r = (e >> 6) * 8 + (e & 7), q = (e >> 3) & 7;
-        const float4 x = *reinterpret_cast<const float4*>(ra + r * GC_RLA + q * 4);
-        const int off = canon_off(r, q * 4);
-        float4 h, l;
-        split(x.x, h.x, l.x); split(x.y, h.y, l.y); split(x.z, h.z, l.z); split(x.w, h.w, l.w);
-        *reinterpret_cast<float4*>(ahi + off) = h;
-        *reinterpret_cast<float4*>(alo + off) = l;
-      }
-      // B (transposed): a warp takes 8 columns x 4 K rows, distinct banks for the
-      // padded raw reads and for the canonical stores
-      {
-        const int nlo = lane & 7, klo = lane >> 3;
-#pragma unroll
-        for (int i = 0; i < 16; ++i) {
-          const int blk = warp * 16 + i;  // 64 blocks of 8 columns x 4 K rows
-          const int n = (blk & 7) * 8 + nlo, k = (blk >> 3) * 4 + klo;
-          float h, l;
-          split(rb[k * GC_RLB + n], h, l);
-          bhi[canon_off(n, k)] = h;
-          blo[canon_off(n, k)] = l;
-        }
-      }
-      fence_async_smem();
-      mbar_arrive(&bar_a[st]);
-    }
-    cp_async_wait<0>();
-    // epilogue: row r0 + 32 warp + lane of the tile, 64 columns from TMEM
-    if (ok && !abort_flag && mbar_wait(&bar_done, 0u)) {
       tc_fence_after();
-      const int r = r0 + warp * 32 + lane;
-      const uint32_t trow = (uint32_t)(warp * 32) << 16;
-#pragma unroll 1
+      float v[BMAX];
+      const uint32_t ta = tmem + ((uint32_t)(ew * 32) << 16) + (uint32_t)(ab * BMAX);
+#pragma unroll
       for (int part = 0; part < BMAX / 16; ++part) {
-        float v[16];
-        tmem_ld16(tmem + trow + (uint32_t)(part * 16), v);
-        if (nch == 0)
+        float w[16];
+        tmem_ld16(ta + (uint32_t)(part * 16), w);
 #pragma unroll
-          for (int i = 0; i < 16; ++i) v[i] = 0.f;
-        if (r < d.m)
+        for (int i = 0; i < 16; ++i) v[part * 16 + i] = jb.nch > 0 ? w[i] : 0.f;
+      }
+      tc_fence_before();
+      mbar_arrive(&bar_acc_empty[ab]);  // the accumulator may take tile t + 2
+      const int r = ew * 32 + lane;
+      if (r < jb.m) {
+        double* orow = out + (jb.o + r) * ldo;
+        const double* arow = addend ? addend + (jb.o + r) * ldo : nullptr;
 #pragma unroll
-          for (int i = 0; i < 16; ++i) {
-            const int c = part * 16 + i;
-            if (c < nk) {
-              const long long o = (d.oo + r) * ldo + c;
-              out[o] = addend ? addend[o] + (double)v[i] : (double)v[i];
+        for (int c = 0; c < BMAX; c += 2)
+          if (c < nk) {
+            double2 y = make_double2((double)v[c], (double)v[c + 1]);
+            if (arow) {
+              y.x += arow[c];
+              y.y += arow[c + 1];
             }
+            *reinterpret_cast<double2*>(orow + c) = y;
           }
       }
-    } else {
-      abort_flag = 1;
     }
   }
-  // wind-down: after an abort, wait (bounded) for the MMAs in flight before freeing TMEM
+  // wind-down: after an abort, wait (bounded) for the copies and MMAs in flight before freeing TMEM
   __syncthreads();
   if (tid == 0 && abort_flag) {
-    const long long ql = last_commit;
-    if (ql >= 0) mbar_wait(&bar_mma[ql % GC_STAGES], (uint32_t)((ql / GC_STAGES) & 1));
+    for (int s = 0; s < GC_STAGES; ++s)
+      if (last_load[s] >= 0) mbar_wait(&bar_full[s], (uint32_t)((last_load[s] / GC_STAGES) & 1));
+    const long long qm = last_mma;
+    if (qm >= 0) mbar_wait(&bar_empty[qm % GC_STAGES], (uint32_t)((qm / GC_STAGES) & 1));
     atomicOr(err, DE_TIMEOUT);
   }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BMAX));
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * BMAX));
+}
+
+// A tiles of [A1 | A2] for every descriptor: tile (rt, ch) of descriptor y at
+// toff[y] + (rt * nch + ch) * GC_TILE, nch = ceil(k1 / 32) + ceil(k2 / 32).
+// One block per tile; each thread writes whole 16-byte pieces of the
+// canonical order (piece p holds row (p >> 6) * 8 + (p & 7), K 4 ((p >> 3) & 7) ..).
+__global__ void kb_tile_a(const GemmDesc* __restrict__ gd, const long long* __restrict__ toff,
+                          const float* __restrict__ A, float* __restrict__ At) {
+  const GemmDesc d = gd[blockIdx.y];
+  const int n1 = (d.k1 + TC_KC - 1) / TC_KC, nch = n1 + (d.k2 + TC_KC - 1) / TC_KC;
+  const int nrt = (d.m + TC_M - 1) / TC_M;
+  const int ti = blockIdx.x;
+  if (ti >= nrt * nch) return;
+  const int rt = ti / nch, ch = ti % nch;
+  const bool seg1 = ch < n1;
+  const int K = seg1 ? d.k1 : d.k2, kb = (seg1 ? ch : ch - n1) * TC_KC, lda = seg1 ? d.lda : d.lda2;
+  const float* Ab = A + (seg1 ? d.oA : d.oA2);
+  float4* dst = reinterpret_cast<float4*>(At + toff[blockIdx.y] + (long long)ti * GC_TILE);
+  for (int p = threadIdx.x; p < GC_TILE / 4; p += blockDim.x) {
+    const int r = rt * TC_M + (p >> 6) * 8 + (p & 7), k = kb + ((p >> 3) & 7) * 4;
+    float v[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) v[e] = (r < d.m && k + e < K) ? Ab[(long long)r * lda + k + e] : 0.f;
+    dst[p] = make_float4(v[0], v[1], v[2], v[3]);
+  }
+}
+
+// B chunks of one application: chunk ch of subdomain y at boff[y] + ch * GC_TILE,
+// TF32 hi then lo, each 64 columns x 32 K in the canonical order.
+//   seg 1 (chunks 0 .. ceil(ni / 32) - 1):   B[j][c] = w[rep + j] x[idx[rep + j]][c]
+//   seg 2 (the next ceil(nc / 32) chunks):   B[j][c] = x[idx[coff + j]][c]
+// Columns c >= nk and rows beyond the segment are zero.
+__global__ void kb_tile_b(int seg, const DevSub* __restrict__ ds, const long long* __restrict__ boff, int lg,
+                          const int* __restrict__ idx, const double* __restrict__ w, const double* __restrict__ x,
+                          float* __restrict__ Bt, const int* __restrict__ ndone) {
+  const int nk = 1 << lg;
+  if (batch_all_done(ndone, nk)) return;
+  const DevSub s = ds[blockIdx.y];
+  const int n1 = (s.ni + TC_KC - 1) / TC_KC;
+  const int K = seg == 1 ? s.ni : s.nc, base = seg == 1 ? s.rep : s.coff;
+  const int ch = blockIdx.x;
+  if (ch * TC_KC >= K) return;
+  __shared__ __align__(16) float sh[GC_TILE];
+  for (int e = threadIdx.x; e < GC_BHALF; e += blockDim.x) {
+    const int kk = e >> 6, c = e & 63;  // 64 consecutive threads read one row of x
+    const int j = ch * TC_KC + kk;
+    double v = 0.0;
+    if (j < K && c < nk) {
+      const int g = base + j;
+      v = x[((long long)idx[g] << lg) + c];
+      if (w) v *= w[g];
+    }
+    const float h = tf32_rna((float)v);
+    const int o = canon_off(c, kk);
+    sh[o] = h;
+    sh[GC_BHALF + o] = tf32_rna((float)(v - (double)h));
+  }
+  __syncthreads();
+  float4* dst = reinterpret_cast<float4*>(Bt + boff[blockIdx.y] + (long long)((seg == 1 ? 0 : n1) + ch) * GC_TILE);
+  for (int p = threadIdx.x; p < GC_TILE / 4; p += blockDim.x) dst[p] = reinterpret_cast<const float4*>(sh)[p];
 }
 
 }  // namespace bddc

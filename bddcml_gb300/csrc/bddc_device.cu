@@ -193,6 +193,12 @@ struct BatchBufs {
   __nv_bfloat16 *oz_s = nullptr, *oz_x = nullptr;
   long long *oz_soff = nullptr, *oz_eoff = nullptr, *oz_xoff = nullptr;
   int *oz_erow = nullptr, *oz_fcol = nullptr;
+  // 3xTF32 tensor-core preconditioner products (with the sliced Schur operator):
+  // A tiles of [Z | Phi] and of Phi^T, the B chunks of one application, job lists
+  float *tc_az = nullptr, *tc_ap = nullptr, *tc_b = nullptr;
+  long long* tc_boff = nullptr;
+  TcJob *tc_jz = nullptr, *tc_jp = nullptr;
+  int tc_njz = 0, tc_njp = 0, tc_grid = 0, tc_mch1 = 0, tc_mch2 = 0;
   // level-2 device only: interior loads, assembled reduced rhs, interior solutions (rows of
   // BMAX columns)
   double *fo = nullptr, *fi = nullptr, *g = nullptr, *bb = nullptr;
