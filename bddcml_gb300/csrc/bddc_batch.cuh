@@ -64,6 +64,18 @@ static void batch_prepare_tc(Device& D) {
   BatchBufs& B = D.bt;
   auto& mem = B.mem;
   const bool coarse = D.ndofc > 0;
+  int dev = 0, nsm = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  B.tc_grid = std::max(1, nsm);
+  // the Phi^T product has one tile per subdomain: split its K range so that
+  // the job list fills the SMs several times over
+  long long ncon = 0, nptile = 0;
+  for (auto& d : D.hs) {
+    ncon = std::max(ncon, (long long)d.coff + d.nc);
+    if (coarse) nptile += (d.nc + TC_M - 1) / TC_M;
+  }
+  const int ks = nptile > 0 ? (int)std::min<long long>(8, std::max<long long>(1, (8LL * nsm + nptile - 1) / nptile)) : 1;
   vector<long long> zoff(D.nsub), poff(D.nsub), boff(D.nsub);
   vector<TcJob> jz, jp;
   long long nz = 0, np = 0, nb = 0;
@@ -85,8 +97,11 @@ static void batch_prepare_tc(Device& D) {
     const int nrp = coarse ? (d.nc + TC_M - 1) / TC_M : 0;
     poff[t] = np;
     for (int rt = 0; rt < nrp; ++rt)
-      jp.push_back(TcJob{np + (long long)rt * n1 * GC_TILE, boff[t], (long long)d.coff + rt * TC_M,
-                         std::min(TC_M, d.nc - rt * TC_M), n1});
+      for (int h = 0; h < ks; ++h) {  // part h: chunks [c0, c1), rows in plane h
+        const int c0 = (int)((long long)n1 * h / ks), c1 = (int)((long long)n1 * (h + 1) / ks);
+        jp.push_back(TcJob{np + ((long long)rt * n1 + c0) * GC_TILE, boff[t] + (long long)c0 * GC_TILE,
+                           h * ncon + d.coff + rt * TC_M, std::min(TC_M, d.nc - rt * TC_M), c1 - c0});
+      }
     np += (long long)nrp * n1 * GC_TILE;
     maxp = std::max(maxp, nrp * n1);
   }
@@ -100,10 +115,9 @@ static void batch_prepare_tc(Device& D) {
   B.tc_njp = (int)jp.size();
   B.tc_mch1 = mch1;
   B.tc_mch2 = mch2;
-  int dev = 0, nsm = 0;
-  CK(cudaGetDevice(&dev));
-  CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  B.tc_grid = std::max(1, nsm);
+  B.tc_ks = ks;
+  B.tc_pstride = std::max(1LL, ncon) * B.nk;
+  B.tc_rcs = dalloc<double>(ks * B.tc_pstride, mem);
   if (maxz > 0) {
     kb_tile_a<<<dim3(maxz, D.nsub), 256, 0, D.st>>>(B.gZ, upload(zoff, mem, D.st),
                                                      static_cast<const float*>(D.poolPC), B.tc_az);
@@ -121,8 +135,8 @@ static void gemm_tc(Device& D, const TcJob* jobs, int njobs, const float* At, do
                     const int* ndone) {
   if (njobs <= 0) return;
   raise_smem(kb_gemm_tc3, GC_SMEM);
-  kb_gemm_tc3<<<std::min(njobs, D.bt.tc_grid), GC_THREADS, GC_SMEM, D.st>>>(jobs, njobs, At, D.bt.tc_b, out, nullptr,
-                                                                            nk, nk, D.err, ndone);
+  kb_gemm_tc3<<<std::min(njobs, D.bt.tc_grid), GC_THREADS, GC_SMEM, D.st>>>(jobs, njobs, At, D.bt.tc_b, out, nk, nk,
+                                                                            D.err, ndone);
   CKL();
 }
 
@@ -336,12 +350,14 @@ static void batch_pc(Device& D, const double* rin, double* zout, double* part) {
   CKL();
   if (D.ndofc > 0) {
     if (tc)
-      gemm_tc(D, B.tc_jp, B.tc_njp, B.tc_ap, B.rcs, nk, B.ndone);
+      gemm_tc(D, B.tc_jp, B.tc_njp, B.tc_ap, B.tc_rcs, nk, B.ndone);
     else
       gemm_t<T>(D, B.gP, D.nsub, D.ncpmax, static_cast<const T*>(B.phit), aux, nullptr, nk, B.rcs, nullptr, nk, nk,
                 B.ndone);
     kb_coarse_gather<<<blocks_for((long long)D.ndofc << lg), 256, 0, st>>>(D.ndofc, lg, D.co_ptr, D.co_sub,
-                                                                           D.co_loc, D.ds, B.rcs, B.rc, B.ndone);
+                                                                           D.co_loc, D.ds, tc ? B.tc_rcs : B.rcs,
+                                                                           B.rc, B.ndone, tc ? B.tc_ks : 1,
+                                                                           tc ? B.tc_pstride : 0);
     CKL();
     if (D.lev2) {
       batch_level2(D, B.rc, B.uc);

@@ -337,18 +337,22 @@ __global__ void kb_phi_transpose(const DevSub* __restrict__ ds, const T* __restr
   phit[oT[blockIdx.y] + e] = (c < s.nc && i < s.ni) ? pcpool[s.oPhi + (long long)i * s.ncp + c] : T(0);
 }
 
-// rc[q][k] = sum over the subdomain constraints mapped to coarse dof q
+// rc[q][k] = sum over the subdomain constraints mapped to coarse dof q (and
+// over the nparts partial planes of rcs, pstride apart, of a split-K product)
 __global__ void kb_coarse_gather(int ndofc, int lg, const int* __restrict__ cptr, const int* __restrict__ csub,
                                  const int* __restrict__ cloc, const DevSub* __restrict__ ds,
                                  const double* __restrict__ rcs, double* __restrict__ rc,
-                                 const int* __restrict__ ndone) {
+                                 const int* __restrict__ ndone, int nparts = 1, long long pstride = 0) {
   const int nk = 1 << lg;
   if (batch_all_done(ndone, nk)) return;
   const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= ((long long)ndofc << lg)) return;
   const int q = (int)(e >> lg), k = (int)(e & (nk - 1));
   double t = 0.0;
-  for (int p = cptr[q]; p < cptr[q + 1]; ++p) t += rcs[((long long)(ds[csub[p]].coff + cloc[p]) << lg) + k];
+  for (int p = cptr[q]; p < cptr[q + 1]; ++p) {
+    const long long o = ((long long)(ds[csub[p]].coff + cloc[p]) << lg) + k;
+    for (int h = 0; h < nparts; ++h) t += rcs[o + h * pstride];
+  }
   rc[e] = t;
 }
 

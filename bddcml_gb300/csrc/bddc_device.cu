@@ -199,6 +199,9 @@ struct BatchBufs {
   long long* tc_boff = nullptr;
   TcJob *tc_jz = nullptr, *tc_jp = nullptr;
   int tc_njz = 0, tc_njp = 0, tc_grid = 0, tc_mch1 = 0, tc_mch2 = 0;
+  int tc_ks = 1;                 // K parts of the Phi^T product, each writing its own plane of tc_rcs
+  long long tc_pstride = 0;      // doubles between the planes
+  double* tc_rcs = nullptr;
   // level-2 device only: interior loads, assembled reduced rhs, interior solutions (rows of
   // BMAX columns)
   double *fo = nullptr, *fi = nullptr, *g = nullptr, *bb = nullptr;
