@@ -140,8 +140,61 @@ static void gemm_tc(Device& D, const TcJob* jobs, int njobs, const float* At, do
   CKL();
 }
 
+// out = addend + A B with A as hi / lo float planes (oA, oA2) and B split float2 (kb_gemm_df)
+static void gemm_df(Device& D, const GemmDesc* gd, int ndesc, int maxm, const float* Ap, const float2* B, double* out,
+                    const double* addend, int ldo, int nk, const int* ndone) {
+  kb_gemm_df<true><<<dim3((maxm + GM - 1) / GM, ndesc), 256, 0, D.st>>>(gd, Ap, B, nk, out, addend, ldo, nk, ndone);
+  CKL();
+}
+
+// The level-2 operators as hi / lo planes for the double-float products, and
+// their descriptors (oA2 = the lo plane; [Z | Phi] as two single-segment products)
+static void batch_prepare_l2df(Device& D, const vector<GemmDesc>& ga, const vector<GemmDesc>& gz,
+                               const vector<GemmDesc>& gp, const vector<GemmDesc>& gx, long long npt, long long nuo) {
+  BatchBufs& B = D.bt;
+  auto& mem = B.mem;
+  auto extent = [](const vector<GemmDesc>& v, bool seg2) {
+    long long e = 0;
+    for (auto& d : v) {
+      if (d.m > 0 && d.k1 > 0) e = std::max(e, d.oA + (long long)(d.m - 1) * d.lda + d.k1);
+      if (seg2 && d.m > 0 && d.k2 > 0) e = std::max(e, d.oA2 + (long long)(d.m - 1) * d.lda2 + d.k2);
+    }
+    return e;
+  };
+  auto planes = [&](const double* src, long long n) {
+    float* p = dalloc<float>(2 * std::max(1LL, n), mem);
+    if (n > 0) {
+      kb_to_planes<<<blocks_for(n), 256, 0, D.st>>>(n, src, p);
+      CKL();
+    }
+    return p;
+  };
+  auto with_lo = [](vector<GemmDesc> v, long long e) {
+    for (auto& d : v) { d.oA2 = d.oA + e; d.k2 = 0; }
+    return v;
+  };
+  const long long ea = extent(ga, false), ez = extent(gz, true), et = extent(gx, false);
+  B.df_ainv = planes(D.l2_ainv, ea);
+  B.df_pc = planes(static_cast<const double*>(D.poolPC), ez);
+  B.df_phit = planes(static_cast<const double*>(B.phit), npt);
+  B.df_t = planes(static_cast<const double*>(D.poolT), et);
+  B.dA = upload(with_lo(ga, ea), mem, D.st);
+  B.dP = upload(with_lo(gp, npt), mem, D.st);
+  B.dX = upload(with_lo(gx, et), mem, D.st);
+  B.dZ1 = upload(with_lo(gz, ez), mem, D.st);
+  vector<GemmDesc> z2(gz.size());
+  for (size_t t = 0; t < gz.size(); ++t) {
+    const GemmDesc& d = gz[t];
+    z2[t] = GemmDesc{d.oA2, d.oA2 + ez, d.ob2, 0, d.oo, d.m, d.k2, 0, d.lda2, 0, 0};
+  }
+  B.dZ2 = upload(z2, mem, D.st);
+  B.df_fo = dalloc<float2>(std::max(1LL, nuo) * B.nk, mem);
+  B.l2df = true;
+}
+
 template <typename T>
-static void batch_prepare(Device& D, int nk, int lg, int maxit, int* shared_ndone, bool level2, int op = 0) {
+static void batch_prepare(Device& D, int nk, int lg, int maxit, int* shared_ndone, bool level2, int op = 0,
+                          bool l2df = false) {
   BatchBufs& B = D.bt;
   const int ldh = std::max(maxit + 2, 2);
   bool want_oz = false;
@@ -149,7 +202,9 @@ static void batch_prepare(Device& D, int nk, int lg, int maxit, int* shared_ndon
     want_oz = true;
     for (auto& d : D.hs) want_oz = want_oz && d.ni <= OZ_KMAX;
   }
-  if (B.nk == nk && B.ldh >= ldh && (shared_ndone == nullptr || B.ndone == shared_ndone) && B.oz == want_oz) return;
+  if (B.nk == nk && B.ldh >= ldh && (shared_ndone == nullptr || B.ndone == shared_ndone) && B.oz == want_oz &&
+      B.l2df == (level2 && l2df))
+    return;
   D.release_batch();
   auto& mem = B.mem;
   const long long n = D.n, nrep = D.nrep;
@@ -236,13 +291,15 @@ static void batch_prepare(Device& D, int nk, int lg, int maxit, int* shared_ndon
   B.gZ = upload(gz, mem, D.st);
   B.gX = upload(gx, mem, D.st);
   B.gC = upload(gc, mem, D.st);
+  vector<GemmDesc> ga;
   if (level2 && D.l2_ainv) {  // v = A_oo^-1 f_o: the interior solves of the level-2 subdomains
-    vector<GemmDesc> ga(D.nsub);
+    ga.resize(D.nsub);
     for (int t = 0; t < D.nsub; ++t) {
       const DevSub& d = D.hs[t];
       ga[t] = GemmDesc{D.l2_aoff[t], 0, D.huo_off[t], 0, ro[t], d.no, d.no, 0, d.NO, 0, 0};
     }
     B.gA = upload(ga, mem, D.st);
+    if (l2df) batch_prepare_l2df(D, ga, gz, gp, gx, npt, nuo);
   }
   if (want_oz) {
     batch_prepare_oz(D);
@@ -339,10 +396,17 @@ static void batch_pc(Device& D, const double* rin, double* zout, double* part) {
   // with the sliced Schur operator the FP32 products run on the tensor cores
   // (3xTF32) from pre-tiled A and the split B chunks, else on the FP32 SIMT pipes
   const bool tc = std::is_same_v<T, float> && B.tc_az != nullptr;
+  // the level-2 device of a mixed level 1 runs its products as double-float
+  const bool df = std::is_same_v<T, double> && B.l2df;
+  float2* auxf = static_cast<float2*>(B.aux);
+  float2* ucf = static_cast<float2*>(B.ucs);
   D.prof.begin(PH_PC_LOCAL, st);
   if (tc) {
     kb_tile_b<<<dim3(B.tc_mch1, D.nsub), 256, 0, st>>>(1, D.ds, B.tc_boff, lg, D.uniq, D.wrep, rin, B.tc_b,
                                                         B.ndone);
+  } else if (df) {
+    kb_gather_df<<<blocks_for((long long)D.nrep << lg), 256, 0, st>>>(D.nrep, lg, D.uniq, 1.0, rin, auxf, B.ndone,
+                                                                      D.wrep);
   } else {
     kb_gather_t<T><<<blocks_for((long long)D.nrep << lg), 256, 0, st>>>(D.nrep, lg, D.uniq, D.wrep, 1.0, rin, aux,
                                                                         B.ndone);
@@ -351,6 +415,8 @@ static void batch_pc(Device& D, const double* rin, double* zout, double* part) {
   if (D.ndofc > 0) {
     if (tc)
       gemm_tc(D, B.tc_jp, B.tc_njp, B.tc_ap, B.tc_rcs, nk, B.ndone);
+    else if (df)
+      gemm_df(D, B.dP, D.nsub, D.ncpmax, B.df_phit, auxf, B.rcs, nullptr, nk, nk, B.ndone);
     else
       gemm_t<T>(D, B.gP, D.nsub, D.ncpmax, static_cast<const T*>(B.phit), aux, nullptr, nk, B.rcs, nullptr, nk, nk,
                 B.ndone);
@@ -387,15 +453,22 @@ static void batch_pc(Device& D, const double* rin, double* zout, double* part) {
     } else {
       long long ncon = 0;
       for (auto& d : D.hs) ncon = std::max(ncon, (long long)d.coff + d.nc);
-      kb_gather_uc<T><<<blocks_for(ncon << lg), 256, 0, st>>>(ncon, lg, D.cmap, B.uc, ucs, B.ndone);
+      if (df)
+        kb_gather_df<<<blocks_for(ncon << lg), 256, 0, st>>>(ncon, lg, D.cmap, 1.0, B.uc, ucf, B.ndone);
+      else
+        kb_gather_uc<T><<<blocks_for(ncon << lg), 256, 0, st>>>(ncon, lg, D.cmap, B.uc, ucs, B.ndone);
       CKL();
     }
   }
   // zrep = Z_s W_s r_s + Phi_s uc_s in one product per subdomain
-  if (tc)
+  if (tc) {
     gemm_tc(D, B.tc_jz, B.tc_njz, B.tc_az, B.zrep, nk, B.ndone);
-  else
+  } else if (df) {
+    gemm_df(D, B.dZ1, D.nsub, D.maxNI, B.df_pc, auxf, B.zrep, nullptr, nk, nk, B.ndone);
+    if (D.ndofc > 0) gemm_df(D, B.dZ2, D.nsub, D.maxNI, B.df_pc, ucf, B.zrep, B.zrep, nk, nk, B.ndone);
+  } else {
     gemm_t<T>(D, B.gZ, D.nsub, D.maxNI, pc, aux, ucs, nk, B.zrep, nullptr, nk, nk, B.ndone);
+  }
   D.prof.end(PH_PC_LOCAL, st);
   kb_assemble_z<<<D.npart, RT, 0, st>>>(D.n, lg, D.own, B.zrep, D.wrep, D.wsum, rin, zout, part, D.npart, B.ndone);
   CKL();
@@ -415,7 +488,15 @@ static void batch_level2(Device& D1, const double* rc, double* uc) {
   kb_l2_fi<<<blocks_for((long long)D2.nrep << lg), 256, 0, st>>>(D2.nrep, lg, D2.l2_mi, D2.l2_wi, rc, B.fi, B.ndone);
   CKL();
   // interior solves by the explicit inverses (one product per level-2 subdomain)
-  gemm_t<double>(D2, B.gA, D2.nsub, D2.maxNO, D2.l2_ainv, B.fo, nullptr, nk, B.bb, nullptr, BMAX, nk, B.ndone);
+  if (B.l2df) {
+    long long nuo = 0;
+    for (auto& d : D2.hs) nuo += d.no;
+    kb_to_df<<<blocks_for(nuo << lg), 256, 0, st>>>(nuo << lg, B.fo, B.df_fo, B.ndone, nk);
+    CKL();
+    gemm_df(D2, B.dA, D2.nsub, D2.maxNO, B.df_ainv, B.df_fo, B.bb, nullptr, BMAX, nk, B.ndone);
+  } else {
+    gemm_t<double>(D2, B.gA, D2.nsub, D2.maxNO, D2.l2_ainv, B.fo, nullptr, nk, B.bb, nullptr, BMAX, nk, B.ndone);
+  }
   kb_reduced_rhs<<<dim3(blocks_for((long long)D2.maxNI << lg), D2.nsub), 256, 0, st>>>(D2.ds, D2.kio, lg, B.rowoff,
                                                                                        B.bb, B.fi, B.grep, B.ndone);
   CKL();
@@ -424,11 +505,19 @@ static void batch_level2(Device& D1, const double* rc, double* uc) {
   CKL();
   batch_pc<double>(D2, B.g, B.z, nullptr);
   // interior resolve u_o = v - X z, in place in the band block
-  kb_gather_t<double><<<blocks_for((long long)D2.nrep << lg), 256, 0, st>>>(D2.nrep, lg, D2.uniq, nullptr, -1.0, B.z,
-                                                                            static_cast<double*>(B.xs), B.ndone);
-  CKL();
-  gemm_t<double>(D2, B.gX, D2.nsub, D2.maxNO, static_cast<const double*>(D2.poolT), static_cast<const double*>(B.xs),
-                 nullptr, nk, B.bb, B.bb, BMAX, nk, B.ndone);
+  if (B.l2df) {
+    kb_gather_df<<<blocks_for((long long)D2.nrep << lg), 256, 0, st>>>(D2.nrep, lg, D2.uniq, -1.0, B.z,
+                                                                       static_cast<float2*>(B.xs), B.ndone);
+    CKL();
+    gemm_df(D2, B.dX, D2.nsub, D2.maxNO, B.df_t, static_cast<const float2*>(B.xs), B.bb, B.bb, BMAX, nk, B.ndone);
+  } else {
+    kb_gather_t<double><<<blocks_for((long long)D2.nrep << lg), 256, 0, st>>>(D2.nrep, lg, D2.uniq, nullptr, -1.0,
+                                                                              B.z, static_cast<double*>(B.xs),
+                                                                              B.ndone);
+    CKL();
+    gemm_t<double>(D2, B.gX, D2.nsub, D2.maxNO, static_cast<const double*>(D2.poolT),
+                   static_cast<const double*>(B.xs), nullptr, nk, B.bb, B.bb, BMAX, nk, B.ndone);
+  }
   kb_l2_out_o<<<dim3(blocks_for((long long)D2.maxNO << lg), D2.nsub), 256, 0, st>>>(D2.ds, lg, B.rowoff, D2.uo_off,
                                                                                    D2.l2_mo, B.bb, uc, B.ndone);
   CKL();
@@ -471,7 +560,7 @@ static void batch_solve_impl(Solver& S, int nrhs, double tol, int maxit, int nde
   int nk = 4, lg = 2;  // at least 4 columns: the GEMM operand rows move in 16-byte pieces
   while (nk < nrhs) { nk <<= 1; ++lg; }
   batch_prepare<T>(D, nk, lg, maxit, nullptr, false, S.prm.batch_operator);
-  if (D.lev2) batch_prepare<double>(*D.lev2->dev, nk, lg, 0, D.bt.ndone, true);
+  if (D.lev2) batch_prepare<double>(*D.lev2->dev, nk, lg, 0, D.bt.ndone, true, 0, D.mixed);
   BatchBufs& B = D.bt;
   {
     double bs = 0, fm = 0, fs = 0, fp = 0;

@@ -35,15 +35,37 @@ __device__ __forceinline__ bool batch_all_done(const int* ndone, int nk) { retur
 // --------------------------------------------------------------- gathers
 // b[j][k] = split(sign * x[uniq[j]][k]) for replicated interface index j
 __global__ void kb_gather_df(long long nrep, int lg, const int* __restrict__ uniq, double sign,
-                             const double* __restrict__ x, float2* __restrict__ b, const int* __restrict__ ndone) {
+                             const double* __restrict__ x, float2* __restrict__ b, const int* __restrict__ ndone,
+                             const double* __restrict__ w = nullptr) {
   const int nk = 1 << lg;
   if (batch_all_done(ndone, nk)) return;
   const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= (nrep << lg)) return;
   const long long j = e >> lg;
   const int k = (int)(e & (nk - 1));
-  const dfloat v = df_from_double(sign * x[((long long)uniq[j] << lg) + k]);
+  double t = sign * x[((long long)uniq[j] << lg) + k];
+  if (w) t *= w[j];
+  const dfloat v = df_from_double(t);
   b[e] = make_float2(v.hi, v.lo);
+}
+
+// b[e] = split(x[e]) for cnt entries (the batched operands of the double-float products)
+__global__ void kb_to_df(long long cnt, const double* __restrict__ x, float2* __restrict__ b,
+                         const int* __restrict__ ndone, int nk) {
+  if (batch_all_done(ndone, nk)) return;
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= cnt) return;
+  const dfloat v = df_from_double(x[e]);
+  b[e] = make_float2(v.hi, v.lo);
+}
+
+// a matrix pool of n doubles as two float planes: hi at [0, n), lo at [n, 2n)
+__global__ void kb_to_planes(long long n, const double* __restrict__ x, float* __restrict__ p) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const dfloat v = df_from_double(x[e]);
+  p[e] = v.hi;
+  p[n + e] = v.lo;
 }
 
 // b[j][k] = T(sign * w[j] * x[uniq[j]][k])  (w optional)

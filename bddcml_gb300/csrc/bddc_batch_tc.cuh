@@ -329,8 +329,8 @@ __global__ void kb_tile_a(const GemmDesc* __restrict__ gd, const long long* __re
 // TF32 hi then lo, each 64 columns x 32 K in the canonical order.
 //   seg 1 (chunks 0 .. ceil(ni / 32) - 1):   B[j][c] = w[rep + j] x[idx[rep + j]][c]
 //   seg 2 (the next ceil(nc / 32) chunks):   B[j][c] = x[idx[coff + j]][c]
-// Columns c >= nk and rows beyond the segment are zero.
-__global__ void kb_tile_b(int seg, const DevSub* __restrict__ ds, const long long* __restrict__ boff, int lg,
+// Columns c >= nk and rows beyond the segment are zero.  256 threads per block.
+__global__ void __launch_bounds__(256) kb_tile_b(int seg, const DevSub* __restrict__ ds, const long long* __restrict__ boff, int lg,
                           const int* __restrict__ idx, const double* __restrict__ w, const double* __restrict__ x,
                           float* __restrict__ Bt, const int* __restrict__ ndone) {
   const int nk = 1 << lg;
@@ -341,25 +341,34 @@ __global__ void kb_tile_b(int seg, const DevSub* __restrict__ ds, const long lon
   const int ch = blockIdx.x;
   if (ch * TC_KC >= K) return;
   __shared__ __align__(16) float sh[GC_TILE];
-  for (int e = threadIdx.x; e < GC_BHALF; e += blockDim.x) {
+  constexpr int PER = GC_BHALF / 256;  // elements per thread (blockDim.x == 256)
+  double v[PER];
+#pragma unroll
+  for (int i = 0; i < PER; ++i) {  // all loads in flight before the stores
     // a warp takes 8 columns x 4 K rows: 64-byte row pieces of x, and 32
     // distinct banks for the canonical stores
+    const int e = threadIdx.x + 256 * i;
     const int c = ((e >> 5) & 7) * 8 + (e & 7), kk = (e >> 8) * 4 + ((e >> 3) & 3);
     const int j = ch * TC_KC + kk;
-    double v = 0.0;
+    v[i] = 0.0;
     if (j < K && c < nk) {
       const int g = base + j;
-      v = x[((long long)idx[g] << lg) + c];
-      if (w) v *= w[g];
+      v[i] = x[((long long)idx[g] << lg) + c];
+      if (w) v[i] *= w[g];
     }
-    const float h = tf32_rna((float)v);
+  }
+#pragma unroll
+  for (int i = 0; i < PER; ++i) {
+    const int e = threadIdx.x + 256 * i;
+    const int c = ((e >> 5) & 7) * 8 + (e & 7), kk = (e >> 8) * 4 + ((e >> 3) & 3);
+    const float h = tf32_rna((float)v[i]);
     const int o = canon_off(c, kk);
     sh[o] = h;
-    sh[GC_BHALF + o] = tf32_rna((float)(v - (double)h));
+    sh[GC_BHALF + o] = tf32_rna((float)(v[i] - (double)h));
   }
   __syncthreads();
   float4* dst = reinterpret_cast<float4*>(Bt + boff[blockIdx.y] + (long long)((seg == 1 ? 0 : n1) + ch) * GC_TILE);
-  for (int p = threadIdx.x; p < GC_TILE / 4; p += blockDim.x) dst[p] = reinterpret_cast<const float4*>(sh)[p];
+  for (int p = threadIdx.x; p < GC_TILE / 4; p += 256) dst[p] = reinterpret_cast<const float4*>(sh)[p];
 }
 
 }  // namespace bddc

@@ -206,6 +206,12 @@ struct BatchBufs {
   // BMAX columns)
   double *fo = nullptr, *fi = nullptr, *g = nullptr, *bb = nullptr;
   GemmDesc* gA = nullptr;
+  // level-2 device under a mixed level 1: the products as double-float on the
+  // FP32 pipes (kb_gemm_df on hi / lo planes of the FP64 operators)
+  bool l2df = false;
+  float *df_ainv = nullptr, *df_pc = nullptr, *df_phit = nullptr, *df_t = nullptr;
+  GemmDesc *dA = nullptr, *dZ1 = nullptr, *dZ2 = nullptr, *dP = nullptr, *dX = nullptr;
+  float2* df_fo = nullptr;
   // level 1: multi-column interior solves A_oo V = F (components X0, D1, D2 of
   // NO x VB_COLS per subdomain in mixed mode, one FP64 block in plain mode)
   void* vb = nullptr;
