@@ -13,10 +13,10 @@
 //    order, 16 KB per chunk.
 // Each A chunk is split into TF32 hi and lo on its way into tensor memory.  A
 // B chunk is one canonical operand of 128 rows (b_hi in rows 0-63, b_lo in
-// rows 64-127), so two MMAs of N = 128 per K step, a_hi [b_hi | b_lo] and
-// a_lo [b_hi | b_lo], accumulate D_hi = a b_hi and D_lo = a b_lo, and the
-// epilogue adds the two halves in FP64 (Ootomo and Yokota's 3xTF32 with the
-// a_lo b_lo term kept: the accuracy of an FP32 product).
+// rows 64-127): per K step one MMA of N = 128, a_hi [b_hi | b_lo], and one of
+// N = 64, a_lo b_hi, accumulate D_hi = a b_hi and D_lo = a_hi b_lo, and the
+// epilogue adds the two halves in FP64 (Ootomo and Yokota's 3xTF32: the
+// accuracy of an FP32 product).
 //
 // Persistent and warp-specialised, one CTA per SM over the job list:
 //   warp 8  (one thread) moves A chunks into a ring of 9 slots (16 KB),
@@ -163,7 +163,8 @@ __global__ void __launch_bounds__(GC_THREADS, 1)
   } else if (warp == GC_ISSUER) {
     // ------------------------------------------------ MMA issuer (one thread)
     if (lane == 0) {
-      constexpr uint32_t idesc = tc_idesc(TC_M, GC_N);
+      constexpr uint32_t idesc = tc_idesc(TC_M, GC_N);      // a_hi [b_hi | b_lo]
+      constexpr uint32_t idesc_hi = tc_idesc(TC_M, BMAX);  // a_lo b_hi (rows 0-63 of the B chunk)
       long long q = 0;
       int t = 0;
       for (int j = blockIdx.x; j < njobs; j += gridDim.x, ++t) {
@@ -190,8 +191,8 @@ __global__ void __launch_bounds__(GC_THREADS, 1)
           for (int kk = 0; kk < TC_KC / 8; ++kk) {
             const uint32_t koff = kk * 2 * TC_LBO;
             const uint32_t acc = (c > 0 || kk > 0) ? 1u : 0u;
-            mma_tf32_ta(dt, a_lo + kk * 8, tc_desc(b + koff), idesc, acc);
-            mma_tf32_ta(dt, a_hi + kk * 8, tc_desc(b + koff), idesc, 1u);
+            mma_tf32_ta(dt, a_hi + kk * 8, tc_desc(b + koff), idesc, acc);
+            mma_tf32_ta(dt, a_lo + kk * 8, tc_desc(b + koff), idesc_hi, 1u);
           }
           mma_commit(&bar_bempty[sb]);
           mma_commit(&bar_a_empty[sa]);
