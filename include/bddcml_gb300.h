@@ -148,8 +148,10 @@ void bddcml_solve_batch_c(int *comm_all, int *method, double *tol, int *maxit, i
  * multiplies them on the bf16 tensor cores with exact accumulation of the
  * leading terms (FP64-class products; used when every subdomain has at most
  * 3264 interface dofs, else mode 0); 0 multiplies the FP32 (hi, lo) pairs of S
- * in double-float arithmetic on the FP32 pipes.  Takes effect at the next
- * bddcml_solve_batch_c.  No counterpart in the reference. */
+ * in double-float arithmetic on the FP32 pipes.  Mode 1 also runs the FP32
+ * preconditioner products as 3xTF32 on the tensor cores (mode 0: FP32 SIMT).
+ * Takes effect at the next bddcml_solve_batch_c.  No counterpart in the
+ * reference. */
 void bddcml_set_batch_operator_c(int *mode);
 
 /* Solutions of the last batched solve for subdomain isub: nrhs columns of ndof
