@@ -29,10 +29,10 @@
 //   warps 4-7 read the finished accumulator and write the rows,
 // so up to 144 KB of A stream from HBM per SM, the epilogue of one tile
 // overlaps the main loop of the next, and shared memory carries only the
-// landing copies, one read of A and the B operand reads.  A job may cover a K range of its tile (split K) and write its own
-// partial rows.  Every wait is bounded; a timeout sets DE_TIMEOUT, and the
-// CTA waits (bounded) for its copies and MMAs in flight before it frees TMEM
-// and returns.
+// landing copies, one read of A and the B operand reads.  A job may cover a K
+// range of its tile (split K) and write its own partial rows.  Every wait is
+// bounded; a timeout sets DE_TIMEOUT, and the CTA waits (bounded) for its
+// copies and MMAs in flight before it frees TMEM and returns.
 #pragma once
 
 #include "bddc_batch_kernels.cuh"
@@ -65,8 +65,22 @@ static_assert(GC_ACOL + GC_ABUF * 2 * TC_KC <= GC_TCOLS, "tensor memory columns"
 
 // 32 consecutive TMEM columns of this warp's 32 lanes from 32 registers per thread
 __device__ __forceinline__ void tmem_st32(uint32_t taddr, const float (&v)[32]) {
-  asm volatile("tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31, %32};" ::"r"(taddr),
-               "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])), "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])), "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])), "r"(__float_as_uint(v[8])), "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])), "r"(__float_as_uint(v[11])), "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])), "r"(__float_as_uint(v[14])), "r"(__float_as_uint(v[15])), "r"(__float_as_uint(v[16])), "r"(__float_as_uint(v[17])), "r"(__float_as_uint(v[18])), "r"(__float_as_uint(v[19])), "r"(__float_as_uint(v[20])), "r"(__float_as_uint(v[21])), "r"(__float_as_uint(v[22])), "r"(__float_as_uint(v[23])), "r"(__float_as_uint(v[24])), "r"(__float_as_uint(v[25])), "r"(__float_as_uint(v[26])), "r"(__float_as_uint(v[27])), "r"(__float_as_uint(v[28])), "r"(__float_as_uint(v[29])), "r"(__float_as_uint(v[30])), "r"(__float_as_uint(v[31]))
+  uint32_t u[32];
+#pragma unroll
+  for (int i = 0; i < 32; ++i) u[i] = __float_as_uint(v[i]);
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], "
+               "{%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16, "
+               "%17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31, %32};"
+               :
+               : "r"(taddr),
+               "r"(u[0]), "r"(u[1]), "r"(u[2]), "r"(u[3]),
+               "r"(u[4]), "r"(u[5]), "r"(u[6]), "r"(u[7]),
+               "r"(u[8]), "r"(u[9]), "r"(u[10]), "r"(u[11]),
+               "r"(u[12]), "r"(u[13]), "r"(u[14]), "r"(u[15]),
+               "r"(u[16]), "r"(u[17]), "r"(u[18]), "r"(u[19]),
+               "r"(u[20]), "r"(u[21]), "r"(u[22]), "r"(u[23]),
+               "r"(u[24]), "r"(u[25]), "r"(u[26]), "r"(u[27]),
+               "r"(u[28]), "r"(u[29]), "r"(u[30]), "r"(u[31])
                : "memory");
 }
 
