@@ -114,7 +114,8 @@ def _read_numbers(path: str):
 
 
 def read_par(prefix: str) -> dict:
-    lines = open(prefix + ".PAR").read().split("\n")
+    with open(prefix + ".PAR") as f:
+        lines = f.read().split("\n")
     w = lines[0].replace(",", " ").split()
     ndim, nsub, nelem, ndof, nnod, nnodc, linet = (int(x) for x in w[:7])
     tol, maxit, ndecrmax = float(w[7].replace("d", "e").replace("D", "e")), int(w[8]), int(w[9])

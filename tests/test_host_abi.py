@@ -13,7 +13,8 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def header_symbols():
-    src = open(os.path.join(ROOT, "include", "bddcml_gb300.h")).read()
+    with open(os.path.join(ROOT, "include", "bddcml_gb300.h")) as f:
+        src = f.read()
     return sorted(set(re.findall(r"^\s*(?:void|int)\s+(bddcml_\w+)\s*\(", src, re.M)))
 
 
@@ -30,7 +31,8 @@ def test_exports_every_header_symbol(built_lib):
 def test_reference_signatures_present():
     """Every function of the reference header src/bddcml_interface_c.h is
     declared with the same argument list."""
-    src = open(os.path.join(ROOT, "include", "bddcml_gb300.h")).read()
+    with open(os.path.join(ROOT, "include", "bddcml_gb300.h")) as f:
+        src = f.read()
     for name, nargs in [("bddcml_init_c", 8), ("bddcml_upload_global_data_c", 25),
                         ("bddcml_upload_subdomain_data_c", 50), ("bddcml_setup_preconditioner_c", 8),
                         ("bddcml_solve_c", 10), ("bddcml_download_local_solution_c", 3),

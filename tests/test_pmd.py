@@ -27,7 +27,8 @@ def test_problem_files_round_trip(tmp_path):
     assert np.array_equal(d["inet"], gp.inet) and np.array_equal(d["nnet"], gp.nnet)
     assert np.array_equal(d["ifix"], gp.ifix) and np.allclose(d["xyz"], gp.xyz, rtol=0, atol=1e-15)
     assert np.array_equal(d["rhs"], gp.rhs)
-    raw = open(prefix + ".ELM", "rb").read()
+    with open(prefix + ".ELM", "rb") as f:
+        raw = f.read()
     (n0,) = np.frombuffer(raw[:4], dtype="<i4")
     assert n0 == 4 + 8 * 64 and len(raw) == 27 * (8 + 4 + 8 * 64)
 
@@ -88,7 +89,10 @@ def test_global_loading_errors(built_lib, tmp_path):
                                              np.zeros(par["ndof"]), prefix + ".ELM", load_division_int=1)
         assert e.value.code == 4
         # a damaged element file is reported at setup
-        open(prefix + "_bad.ELM", "wb").write(open(prefix + ".ELM", "rb").read()[:-20])
+        with open(prefix + ".ELM", "rb") as f:
+            good = f.read()
+        with open(prefix + "_bad.ELM", "wb") as f:
+            f.write(good[:-20])
         B.bddcml_upload_global_data_file(par["nelem"], par["nnod"], par["ndof"], 3, 3, d["inet"], d["nnet"],
                                          d["nndf"], d["xyz"], d["ifix"], d["fixv"], d["rhs"], np.zeros(par["ndof"]),
                                          prefix + "_bad.ELM")
