@@ -25,12 +25,14 @@ namespace bddc {
 namespace {
 
 // one record of a Fortran unformatted sequential file written with 4-byte
-// record markers (gfortran's default): the payload length before and after
-bool read_record(std::FILE* f, vector<unsigned char>& buf) {
+// record markers (gfortran's default): the payload length before and after.
+// A payload longer than max_bytes is refused before anything is allocated.
+bool read_record(std::FILE* f, vector<unsigned char>& buf, size_t max_bytes) {
   unsigned char m[4];
   if (std::fread(m, 1, 4, f) != 4) return false;
   uint32_t n;
   std::memcpy(&n, m, 4);
+  if (n > max_bytes) return false;
   buf.resize(n);
   if (n && std::fread(buf.data(), 1, n, f) != n) return false;
   if (std::fread(m, 1, 4, f) != 4) return false;
@@ -120,7 +122,8 @@ void host_localize_global(Solver& S, int matrixtype) {
       for (int q = kdof[G.inet[k]]; q < kdof[G.inet[k] + 1]; ++q) kdofe.push_back(q);
     const int nve = (int)kdofe.size();
     const long long lelm_expected = matrixtype == 0 ? (long long)nve * nve : (long long)nve * (nve + 1) / 2;
-    if (!read_record(f, rec)) throw Error{ERR_ARGUMENT, "element matrix file ends early or is damaged"};
+    if (!read_record(f, rec, 4 + 8 * (size_t)lelm_expected))
+      throw Error{ERR_ARGUMENT, "element matrix file ends early or is damaged"};
     int lelm = 0;
     if (rec.size() >= 4) std::memcpy(&lelm, rec.data(), 4);
     if (lelm != lelm_expected || rec.size() != 4 + 8 * (size_t)lelm)

@@ -2,6 +2,8 @@
 .FVS, .RHS, .ELM; examples/bddcml_global.f90:223-362) and global loading
 (bddcml_upload_global_data_file_c): element-matrix packing order, file round
 trips, and the host-side division and localisation (no GPU needed)."""
+import struct
+
 import numpy as np
 import pytest
 
@@ -96,6 +98,19 @@ def test_global_loading_errors(built_lib, tmp_path):
         B.bddcml_upload_global_data_file(par["nelem"], par["nnod"], par["ndof"], 3, 3, d["inet"], d["nnet"],
                                          d["nndf"], d["xyz"], d["ifix"], d["fixv"], d["rhs"], np.zeros(par["ndof"]),
                                          prefix + "_bad.ELM")
+        with pytest.raises(B.BddcmlError) as e:
+            B.bddcml_setup_preconditioner(1, 0, 1, 1, 1, 0, 0, 0)
+        assert e.value.code == 1
+    finally:
+        B.bddcml_finalize()
+    # a record marker claiming a huge payload is refused before anything is allocated
+    B.bddcml_init(2, [2, 1], -1, 0, 0, 0, 0)
+    try:
+        with open(prefix + "_huge.ELM", "wb") as f:
+            f.write(struct.pack("<I", 0x7FFFFFF0) + good[4:])
+        B.bddcml_upload_global_data_file(par["nelem"], par["nnod"], par["ndof"], 3, 3, d["inet"], d["nnet"],
+                                         d["nndf"], d["xyz"], d["ifix"], d["fixv"], d["rhs"], np.zeros(par["ndof"]),
+                                         prefix + "_huge.ELM")
         with pytest.raises(B.BddcmlError) as e:
             B.bddcml_setup_preconditioner(1, 0, 1, 1, 1, 0, 0, 0)
         assert e.value.code == 1
