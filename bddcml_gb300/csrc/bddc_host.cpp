@@ -310,6 +310,7 @@ static void host_interface_bc(Solver& S) {
       for (int i = 0; i < S.subs[t].ndofi; ++i) { int u = S.subs[t].uniq[i]; osub[pos[u]] = t; oloc[pos[u]++] = i; }
   }
   vector<vector<double>> bci(nsub);
+#pragma omp parallel for schedule(dynamic)
   for (int t = 0; t < nsub; ++t) {
     auto& s = S.subs[t];
     bci[t].resize(s.ndofi);
@@ -628,26 +629,28 @@ void host_setup(Solver& S) {
   // ---- coarse numbering of a class of entities identified by a global node id:
   // owner = lowest subdomain index holding the node; numbers run over
   // subdomains in order, inside a subdomain in interface node order.
+  // (arrays indexed by global node id: num 0 = not numbered)
   auto number_entities = [&](int shift, const vector<vector<int>>& ent_gid, vector<vector<int>>& ent_num) {
-    std::unordered_map<int, int> num;
+    vector<int> num(nnod_global, 0);
+    vector<char> mine(nnod_global, 0);
     int next = 1;
     for (int t = 0; t < nsub; ++t) {
       auto& s = S.subs[t];
-      std::unordered_map<int, int> mine;
-      for (size_t e = 0; e < ent_gid[t].size(); ++e) mine.emplace(ent_gid[t][e], (int)e);
+      for (int g : ent_gid[t]) mine[g] = 1;
       for (int i = 0; i < s.nnodi; ++i) {
         int g = s.isngn[s.iin[i]];
-        if (!mine.count(g)) continue;
+        if (!mine[g]) continue;
         if (sh.sub[sh.ptr[g]] == t) num[g] = shift + next++;
       }
+      for (int g : ent_gid[t]) mine[g] = 0;
     }
     ent_num.resize(nsub);
     for (int t = 0; t < nsub; ++t) {
       ent_num[t].resize(ent_gid[t].size());
       for (size_t e = 0; e < ent_gid[t].size(); ++e) {
-        auto it = num.find(ent_gid[t][e]);
-        if (it == num.end()) throw Error{ERR_NUMERIC, "coarse entity without owner"};
-        ent_num[t][e] = it->second;
+        const int n = num[ent_gid[t][e]];
+        if (n == 0) throw Error{ERR_NUMERIC, "coarse entity without owner"};
+        ent_num[t][e] = n;
       }
     }
     return next - 1;
@@ -746,16 +749,19 @@ void host_setup(Solver& S) {
   }
   host_constraint_rows(S);
 
-  // ---- unique interface dofs (by global dof id) and per-dof sharing lists
+  // ---- unique interface dofs (numbered in ascending global dof id) and per-dof sharing lists
   vector<int> gdof_uniq(ndof_global, -1);
-  vector<int> gid_list;
   for (auto& s : S.subs)
-    for (int i = 0; i < s.ndofi; ++i) gid_list.push_back(s.isvgvn[s.iivsvn[i]]);
-  std::sort(gid_list.begin(), gid_list.end());
-  gid_list.erase(std::unique(gid_list.begin(), gid_list.end()), gid_list.end());
-  for (size_t k = 0; k < gid_list.size(); ++k) gdof_uniq[gid_list[k]] = (int)k;
-  S.ninterface = (int)gid_list.size();
-  for (auto& s : S.subs) {
+    for (int i = 0; i < s.ndofi; ++i) gdof_uniq[s.isvgvn[s.iivsvn[i]]] = -2;  // marks
+  {
+    int nu = 0;
+    for (int g = 0; g < ndof_global; ++g)
+      if (gdof_uniq[g] == -2) gdof_uniq[g] = nu++;
+    S.ninterface = nu;
+  }
+#pragma omp parallel for schedule(dynamic)
+  for (int t = 0; t < nsub; ++t) {
+    auto& s = S.subs[t];
     s.uniq.resize(s.ndofi);
     for (int i = 0; i < s.ndofi; ++i) s.uniq[i] = gdof_uniq[s.isvgvn[s.iivsvn[i]]];
   }
