@@ -258,6 +258,17 @@ def cpu_baseline(prob, nthreads=None, weights=0):
             "sample": f"full workload, one solve (upload + setup + PCG, {it} iterations)", "iterations": it}
 
 
+def replica_max(values, dist=None):
+    """Per-rank figures (lists of floats) -> their maximum over the ranks of the
+    process group (the replicas of `--gpus N`); the values themselves on one rank."""
+    if dist is None:
+        return [float(v) for v in values]
+    import torch
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t]
+
+
 def run_gpu(args):
     import bddcml_gb300 as B
     from bddcml_gb300 import build
@@ -289,13 +300,7 @@ def run_gpu(args):
         e2e_t.append(t)
         dev_t.append((prof["numeric_total"][0] + prof["solve_total"][0]) / 1e3)
     clocks = sampler.stop() if sampler else None
-    if dist:  # replicas: max over ranks
-        import torch
-        v = torch.tensor([statistics.mean(dev_t), statistics.mean(e2e_t)], dtype=torch.float64)
-        dist.all_reduce(v, op=dist.ReduceOp.MAX)
-        dev_mean, e2e_mean = float(v[0]), float(v[1])
-    else:
-        dev_mean, e2e_mean = statistics.mean(dev_t), statistics.mean(e2e_t)
+    dev_mean, e2e_mean = replica_max([statistics.mean(dev_t), statistics.mean(e2e_t)], dist)  # max over ranks
     # profiled run outside the timed region: per-phase device times
     _, _, _, _, st_p, prof_p, _ = e2e_solve(B, prob, 1, profile=True, workload=args.workload, loads=loads)
     fp64 = None

@@ -1,0 +1,44 @@
+"""The N > 1 path of bench.py: N independent replicas, one per rank, whose
+timings are combined as the maximum over the ranks (gloo, two processes on the
+CPU)."""
+import os
+import socket
+
+import pytest
+
+torch = pytest.importorskip("torch")
+import torch.distributed as dist  # noqa: E402
+import torch.multiprocessing as mp  # noqa: E402
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank_main(rank, world, port, out):
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        import bench
+        # each replica reports its own (device, end-to-end) times
+        got = bench.replica_max([1.0 + rank, 5.0 - rank], dist)
+        out[rank] = got
+    finally:
+        dist.destroy_process_group()
+
+
+def test_replica_timings_take_the_maximum_over_ranks():
+    world = 2
+    with mp.Manager() as m:
+        out = m.dict()
+        mp.spawn(_rank_main, args=(world, _free_port(), out), nprocs=world, join=True)
+        res = dict(out)
+    assert res[0] == res[1] == [2.0, 5.0]
+
+
+def test_replica_max_on_one_rank_is_identity():
+    import bench
+    assert bench.replica_max([0.25, 3]) == [0.25, 3.0]
