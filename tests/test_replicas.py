@@ -1,6 +1,7 @@
 """The N > 1 path of bench.py: N independent replicas, one per rank, whose
 timings are combined as the maximum over the ranks (gloo, two processes on the
 CPU)."""
+import json
 import os
 import socket
 
@@ -17,7 +18,7 @@ def _free_port():
         return s.getsockname()[1]
 
 
-def _rank_main(rank, world, port, out):
+def _rank_main(rank, world, port, outdir):
     os.environ["MASTER_ADDR"] = "127.0.0.1"
     os.environ["MASTER_PORT"] = str(port)
     dist.init_process_group("gloo", rank=rank, world_size=world)
@@ -25,17 +26,19 @@ def _rank_main(rank, world, port, out):
         import bench
         # each replica reports its own (device, end-to-end) times
         got = bench.replica_max([1.0 + rank, 5.0 - rank], dist)
-        out[rank] = got
+        with open(os.path.join(outdir, f"rank{rank}.json"), "w") as f:
+            json.dump(got, f)
     finally:
         dist.destroy_process_group()
 
 
-def test_replica_timings_take_the_maximum_over_ranks():
+def test_replica_timings_take_the_maximum_over_ranks(tmp_path):
     world = 2
-    with mp.Manager() as m:
-        out = m.dict()
-        mp.spawn(_rank_main, args=(world, _free_port(), out), nprocs=world, join=True)
-        res = dict(out)
+    mp.spawn(_rank_main, args=(world, _free_port(), str(tmp_path)), nprocs=world, join=True)
+    res = []
+    for r in range(world):
+        with open(tmp_path / f"rank{r}.json") as f:
+            res.append(json.load(f))
     assert res[0] == res[1] == [2.0, 5.0]
 
 
