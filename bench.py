@@ -222,6 +222,23 @@ def phase_roofline(phase, prof, st, hbm, tensor, peak_kind):
             "algorithmic_bytes": byts, "avg_launch_ms": ms / cnt, "peak_kind": peak_kind}
 
 
+def roofline_traffic(workload, phase, roof):
+    """DRAM bytes per launch of the roofline kernel, from the committed ncu
+    captures of smaller cases of the same kernels, scaled by the units processed
+    (full-size captures would exceed the capture size limit); None elsewhere."""
+    if workload == "poisson_128^3_512subs" and phase == "solve_interior":
+        # k_band_sweep_tc forward + backward sweep at 64^3 with 64 subdomains of 16^3
+        # (profiles/k_band_sweep_tc_k_residual_df_poisson64.md): 8x the subdomains
+        return 8 * (1.862084 + 1.174258 + 1.983205 + 1.174619) * 1e9, \
+            "ncu capture at 64^3 (64 subdomains of 16^3), x8 subdomains"
+    if phase == "schur_apply" and "algorithmic_bytes" in roof:
+        # kb_schur_oz at 48^3 (profiles/kb_schur_oz_elasticity48_64subs_64rhs.md):
+        # 4.675 GB read + 0.063 GB written for 4.5068 GB of slice bytes
+        return roof["algorithmic_bytes"] * (4.675 + 0.063) / 4.506779648, \
+            "ncu capture at 48^3 (64 subdomains), scaled by slice bytes"
+    return None, None
+
+
 def batch_schur_roofline(prof, st, hbm, tensor, peak_kind):
     """Batched Schur apply: the sliced operator (6-bit bf16 slices of S, made at
     the batch setup) is streamed once per apply for all columns, so the bound is
@@ -343,7 +360,9 @@ def run_gpu(args):
         dominant = max(cands, key=lambda k: prof_p[k][0])
         roof = phase_roofline(dominant, prof_p, st_p, hbm, tensor, peak_kind)
     roof["phase"] = dominant
-    roof["traffic"] = None
+    roof["traffic"], src = roofline_traffic(args.workload, dominant, roof)
+    if src:
+        roof["traffic_source"] = src
     all_roof = {k: phase_roofline(k, prof_p, st_p, hbm, tensor, peak_kind)
                 for k in ("solve_interior", "precond_solve", "refine_residual", "schur_apply", "precond_local")}
     kind, _, weights, tau = WORKLOADS[args.workload]
