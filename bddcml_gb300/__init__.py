@@ -44,7 +44,7 @@ EXPORTS = ["bddcml_init_c", "bddcml_upload_global_data_c", "bddcml_upload_subdom
            "bddcml_dotprod_subdomain_dev_c", "bddcml_element_gradient_dev_c", "bddcml_set_adaptive_threshold_c",
            "bddcml_get_adaptive_info_c", "bddcml_upload_subdomain_rhs_batch_c", "bddcml_solve_batch_c",
            "bddcml_download_local_solution_batch_c", "bddcml_set_batch_operator_c",
-           "bddcml_upload_global_data_file_c"]
+           "bddcml_upload_global_data_file_c", "bddcml_set_wait_limit_c"]
 
 # phases of bddcml_get_profile_c (CUDA events on the solver stream)
 PHASES = ["numeric_total", "solve_total", "factor_interior", "solve_interior", "refine_residual", "schur",
@@ -381,6 +381,12 @@ def element_gradient_dev(nelem: int, nne: int, inet_ptr: int, ke0_ptr: int, per_
 def release_device_memory():
     """Hand the pooled device memory that no solver uses back to the driver."""
     lib().bddcml_release_device_memory_c()
+    _check()
+
+
+def set_wait_limit(spins: int) -> None:
+    """Spin limit of the waits inside the tensor-core sweeps (0: default)."""
+    lib().bddcml_set_wait_limit_c(C.byref(C.c_longlong(int(spins))))
     _check()
 
 

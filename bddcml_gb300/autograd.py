@@ -20,8 +20,8 @@ import torch
 
 from . import problems
 from . import (bddcml_change_subdomain_data, bddcml_download_local_solution, bddcml_finalize, bddcml_init,
-               bddcml_setup_new_data, bddcml_setup_preconditioner, bddcml_solve, element_gradient_dev,
-               set_precision, upload_problem)
+               bddcml_setup_new_data, bddcml_setup_preconditioner, bddcml_solve, element_gradient_dev, get_profile,
+               get_stats, set_precision, set_profiling, upload_problem)
 
 
 class PoissonCube:
@@ -40,6 +40,16 @@ class PoissonCube:
         self.nelem = self.n ** 3
         self.ndof = (self.n + 1) ** 3
         self.last_iterations = None
+        # per-phase device timers of the solver during the next forward pass
+        # and its backward pass (bddcml_set_profiling_c)
+        self.profile = False
+        # after a backward pass: the library's CUDA-event totals and statistics
+        # of the forward and adjoint solves, the adjoint iterations and the
+        # gradient kernel's time
+        self.last_profile = None
+        self.last_stats = None
+        self.last_adjoint_iterations = None
+        self.last_gradient_ms = None
 
     def solve(self, kappa: torch.Tensor) -> torch.Tensor:
         """u(kappa) as a differentiable function of kappa (float64, nelem)."""
@@ -50,6 +60,8 @@ class PoissonCube:
         prob = problems.poisson_on_cube(self.ne, self.ns, kappa=kappa_np)
         bddcml_init(2, [prob.nsub, 1], -1, 0, 0, 0, 0)
         set_precision(self.precision)
+        if self.profile:
+            set_profiling(True)
         upload_problem(prob)
         bddcml_setup_preconditioner(1, 0, 1, 1, 1, 0, 0, 0)
         it, reason, _ = bddcml_solve(0, 0, self.tol, self.maxit, 50, 0, 0)
@@ -63,10 +75,14 @@ class PoissonCube:
             zero = np.zeros(s.ndofs)
             bddcml_change_subdomain_data(s.isub, s.ifix, zero, g[s.isvgvn], 1, zero)
         bddcml_setup_new_data()
-        _, reason, _ = bddcml_solve(0, 0, self.tol, self.maxit, 50, 0, 0)
+        it, reason, _ = bddcml_solve(0, 0, self.tol, self.maxit, 50, 0, 0)
         if reason != 0:
             raise RuntimeError(f"adjoint BDDC solve did not converge (reason {reason})")
-        return self._gather(prob)
+        self.last_adjoint_iterations = it
+        lam = self._gather(prob)
+        self.last_profile = get_profile()
+        self.last_stats = get_stats()
+        return lam
 
     @staticmethod
     def _gather(prob) -> np.ndarray:
@@ -80,8 +96,13 @@ class PoissonCube:
         lam = lam.to(self.device, torch.float64).contiguous()
         grad = torch.empty(self.nelem, dtype=torch.float64, device=self.device)
         torch.cuda.synchronize(self.device)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        ev[0].record()  # the kernel runs on the default stream, torch's current one here
         element_gradient_dev(self.nelem, 8, self.conn.data_ptr(), self.ke0.data_ptr(), False, u.data_ptr(),
                              lam.data_ptr(), grad.data_ptr())
+        ev[1].record()
+        ev[1].synchronize()
+        self.last_gradient_ms = ev[0].elapsed_time(ev[1])
         return grad
 
 

@@ -560,6 +560,13 @@ void bddcml_release_device_memory_c(void) {
   });
 }
 
+void bddcml_set_wait_limit_c(long long* spins) {
+  guarded("bddcml_set_wait_limit_c", [&] {
+    Error err{BDDCML_OK, ""};
+    if (!device_set_wait_limit(*spins, err)) throw err;
+  });
+}
+
 int bddcml_get_last_error_c(char* msg, int* lmsg) {
   if (msg && lmsg && *lmsg > 0) {
     int n = std::min<int>((int)g_msg.size(), *lmsg - 1);

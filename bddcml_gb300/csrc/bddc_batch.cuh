@@ -652,10 +652,13 @@ static void batch_solve_impl(Solver& S, int nrhs, double tol, int maxit, int nde
   const double tl = wall_time();
   D.prof.begin(PH_PCG, st);
   const int chunk = 2;
-  int launched = 0, hdone = 0;
+  int launched = 0, hdone = 0, herr = 0;
   CK(cudaMemcpyAsync(&hdone, B.ndone, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(&herr, D.err, sizeof(int), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
-  while (hdone < nk) {
+  // a bounded wait that ran out in a tensor-core kernel leaves its results
+  // unusable: stop at the next poll instead of iterating on them
+  while (hdone < nk && !(herr & DE_TIMEOUT)) {
     for (int q = 0; q < chunk; ++q) {
       batch_schur<T>(D, B.p, B.ap, false, B.p, B.part0);
       kb_sc_alpha<<<nk, RT, 0, st>>>(B.ctl, B.part0, D.npart);
@@ -672,6 +675,7 @@ static void batch_solve_impl(Solver& S, int nrhs, double tol, int maxit, int nde
     }
     launched += chunk;
     CK(cudaMemcpyAsync(&hdone, B.ndone, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&herr, D.err, sizeof(int), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     if (launched > maxit + chunk) break;
   }
@@ -704,13 +708,14 @@ static void batch_solve_impl(Solver& S, int nrhs, double tol, int maxit, int nde
   CK(cudaMemcpyAsync(hdg.data(), B.diag, hdg.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(hsd.data(), B.subdiag, hsd.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
   g_d2h_bytes += (double)(hx.size() + hvo.size()) * sizeof(double);
-  int herr = 0;
   CK(cudaMemcpyAsync(&herr, D.err, sizeof(int), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   D.prof.end(PH_SOLVE_TOTAL, st);
   if (herr & DE_TIMEOUT) {
     for (void* q : tmp) cudaFreeAsync(q, st);
-    throw Error{ERR_CUDA, "a bounded wait of the tensor-core Schur apply ran out"};
+    // reported once: the flag is cleared so that later calls start clean
+    CK(cudaMemsetAsync(D.err, 0, sizeof(int), st));
+    throw Error{ERR_NUMERIC, "a bounded wait of a tensor-core kernel of the batched solve ran out"};
   }
   for (void* q : tmp) cudaFreeAsync(q, st);
   const long long launches = g_launches - launches0;

@@ -22,6 +22,7 @@
 #include "bddc_internal.hpp"
 #include "bddc_pcg_kernels.cuh"
 #include "bddc_tc.cuh"
+#include "bddc_sweep.cuh"
 
 namespace bddc {
 
@@ -383,6 +384,20 @@ bool device_release_memory(Error& err) {
   return true;
 }
 
+// Spin limit of the waits of the tensor-core sweeps on the current device
+// (spins <= 0: the default).  For tests of the timeout path.
+bool device_set_wait_limit(long long spins, Error& err) {
+  try {
+    const long long v = spins > 0 ? spins : TC_SPIN_LIMIT;
+    CK(cudaMemcpyToSymbol(g_tc_wait_limit, &v, sizeof(v)));
+    CK(cudaDeviceSynchronize());
+  } catch (Error& e) {
+    err = e;
+    return false;
+  }
+  return true;
+}
+
 void device_destroy(Device* d) { delete d; }
 
 // ------------------------------------------------------------ band phases
@@ -431,17 +446,17 @@ static void run_panels(Device& D, const BandDesc* bd, const TcDesc* td, int nbat
 template <int PASSES, bool ACC>
 static void sweep_pair(Device& D, dim3 grid, const TcDesc* td, const float* P, float* B) {
   static bool attr = false;
-  const size_t smem = tc_smem_bytes();
+  const size_t smem = swt_smem_bytes();
   if (!attr) {  // both instances launched here need the large shared-memory window
-    CK(cudaFuncSetAttribute(k_band_sweep_tc<PASSES, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    CK(cudaFuncSetAttribute(k_band_sweep_tc<PASSES, false>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
-    CK(cudaFuncSetAttribute(k_band_sweep_tc<PASSES, ACC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    CK(cudaFuncSetAttribute(k_band_sweep_tc<PASSES, ACC>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    CK(cudaFuncSetAttribute(k_band_sweep_tm<PASSES, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_band_sweep_tm<PASSES, false>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    CK(cudaFuncSetAttribute(k_band_sweep_tm<PASSES, ACC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_band_sweep_tm<PASSES, ACC>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
     attr = true;
   }
-  k_band_sweep_tc<PASSES, false><<<grid, SW_THREADS, smem, D.st>>>(td, P, B, 0, D.err);
+  k_band_sweep_tm<PASSES, false><<<grid, SWT_THREADS, smem, D.st>>>(td, P, B, 0, D.err);
   CKL();
-  k_band_sweep_tc<PASSES, ACC><<<grid, SW_THREADS, smem, D.st>>>(td, P, B, 1, D.err);
+  k_band_sweep_tm<PASSES, ACC><<<grid, SWT_THREADS, smem, D.st>>>(td, P, B, 1, D.err);
   CKL();
 }
 
@@ -529,6 +544,11 @@ bool device_setup(Solver& S, Error& err) {
     int herr = 0;
     CK(cudaMemcpyAsync(&herr, D.err, sizeof(int), cudaMemcpyDeviceToHost, D.st));
     CK(cudaStreamSynchronize(D.st));
+    if (herr & DE_TIMEOUT) {
+      CK(cudaMemsetAsync(D.err, 0, sizeof(int), D.st));
+      throw Error{ERR_NUMERIC, "a bounded wait of a tensor-core kernel of the setup ran out (flags " +
+                                   std::to_string(herr) + ")"};
+    }
     if (herr) throw Error{ERR_NUMERIC, "non-positive pivot in a subdomain or coarse factorisation (flags " +
                                             std::to_string(herr) + ")"};
     D.prof.collect();
@@ -1937,11 +1957,16 @@ static void new_data_impl(Solver& S) {
   g_h2d_bytes += (double)(nfo + D.nrep) * sizeof(double);
   (void)own; (void)nv; (void)voff;
   ensure_nv<T>(D);
+  D.prof.begin(PH_NUMERIC_TOTAL, st, true);  // device part of setup_new_data
   reduced_rhs_device<T>(D);
+  D.prof.end(PH_NUMERIC_TOTAL, st);
   int herr = 0;
   CK(cudaMemcpyAsync(&herr, D.err, sizeof(int), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
-  if (herr) throw Error{ERR_NUMERIC, "device error flags " + std::to_string(herr) + " after new data"};
+  if (herr) {
+    CK(cudaMemsetAsync(D.err, 0, sizeof(int), st));  // reported once
+    throw Error{ERR_NUMERIC, "device error flags " + std::to_string(herr) + " after new data"};
+  }
 }
 
 // one-vector interior solve buffers (allocated on first use)

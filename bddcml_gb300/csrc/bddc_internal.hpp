@@ -259,6 +259,7 @@ void host_reactions(Solver& S);
 Device* device_create(Error& err);
 Device* device_create_on_stream(Device* parent, Error& err);  // shares the parent's stream
 bool device_release_memory(Error& err);
+bool device_set_wait_limit(long long spins, Error& err);
 bool device_new_data(Solver& S, Error& err);
 // PCG on nrhs batched right-hand sides (Subdomain::rhs_batch) together; the
 // solutions go to Subdomain::sol_batch, per-column results to the vectors

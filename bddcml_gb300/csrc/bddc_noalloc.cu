@@ -7,10 +7,16 @@
 //   [.., +4*NOALLOC_MAX_IFACE)      subdomain dof index of each interface dof (copied per call)
 //   [.., +8*NOALLOC_BLOCKS)         per-block partial sums
 //   then                            one double result, one unsigned ticket counter
-// The ticket counter must be zero when a call starts.  It is zero at load time
-// and the kernel's last block sets it back to zero.  Two calls that overlap in
-// time (several host threads, or work on several streams) share the scratch and
+// The ticket counter must be zero when a call starts: each call clears it on
+// its stream before the launch (a 4-byte memset, no allocation), so a launch
+// that failed part-way cannot leave it stale.  Two calls that overlap in time
+// (several host threads, or work on several streams) share the scratch and
 // race; callers must not overlap them.
+//
+// With CUDA's lazy module loading (the default since CUDA 12.2) this file's
+// module, and with it the scratch array, is loaded on a device by the first
+// call there (at cudaGetSymbolAddress).  That first call is the one that makes
+// the device allocation; later calls allocate nothing.
 #include <cstdint>
 #include <cstring>
 #include <string>
@@ -81,7 +87,7 @@ __global__ void __launch_bounds__(NOALLOC_THREADS) k_dot_subdomain(const double*
     double s = 0.0;
     for (int b = 0; b < (int)gridDim.x; ++b) s += reinterpret_cast<volatile double*>(part)[b];
     *result = s;
-    *ticket = 0u;  // ready for the next call
+    *ticket = 0u;
   }
 }
 
@@ -117,6 +123,8 @@ bool device_dotprod_noalloc(const int* iface_dofs, const double* weights, int ni
       e = cudaMemcpyAsync(scratch + OFF_IDX, iface_dofs, sizeof(int) * nif, cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return fail(ERR_CUDA, std::string("copy to scratch: ") + cudaGetErrorString(e));
   }
+  e = cudaMemsetAsync(scratch + OFF_TICKET, 0, sizeof(unsigned int), st);
+  if (e != cudaSuccess) return fail(ERR_CUDA, std::string("clear the ticket: ") + cudaGetErrorString(e));
   k_dot_subdomain<<<NOALLOC_BLOCKS, NOALLOC_THREADS, 0, st>>>(v1, v2, ndof, nif, scratch);
   e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaMemcpyAsync(out, scratch + OFF_RESULT, sizeof(double), cudaMemcpyDeviceToHost, st);

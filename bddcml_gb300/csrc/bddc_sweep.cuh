@@ -1,0 +1,409 @@
+// Block-band triangular sweeps on the tensor cores with the window operand in
+// tensor memory.
+//
+// The sweep is the one described in bddc_tc.cuh: for every system and every
+// 128-column tile of its right-hand side B (row-major FP32), block row k is
+//     B[k] = P_k  x  [window blocks of B]
+// with the precomputed panel P_k (forward: [-Linv_kk L_kj ... | Linv_kk],
+// backward: [Linv_kk^T | -Linv_kk^T L_ik^T ...]).  It replaces the interior
+// and preconditioner solves of MUMPS (dd_prepare_schur / dd_prepare_aug /
+// dd_solve_aug, module_dd.f90:4175-4295, 5211-5486, 5843-5932).
+//
+// The window (M = 128 columns of B by K) is the MMA's A operand and lives in
+// tensor memory: each of the 128 staging threads owns one column of the tile,
+// which is one TMEM lane, and writes the TF32 hi and lo parts of its column
+// there (tcgen05.st), so the MMAs read only the 64-row panel (the B operand,
+// 16 KB per 32-wide K chunk, moved by cp.async.bulk) from shared memory.
+// Block row k - 1, on which every step depends, never goes through global
+// memory on the critical path: the epilogue threads read it from the TMEM
+// accumulator, store it as the result and split it straight into the stages
+// of the next step's last two chunks.  The other window blocks (older solved
+// blocks and the right-hand-side block) do not depend on the previous step,
+// so the staging threads load them from global memory ahead of time and the
+// tensor core works on them while the epilogue of the previous step runs.
+//
+// Roles (320 threads, one CTA per SM):
+//   warps 0-3 and 4-7: two staging groups (each one thread per TMEM lane);
+//       group (jb & 1) stages every chunk of window block jb and writes the
+//       results of block jb (the epilogue), so a thread only ever reads back
+//       rows of its own column that it wrote itself;
+//   warp 8 (one thread): panel chunks into a ring of shared-memory slots;
+//   warp 9 (one thread): the MMAs, into one of two TMEM accumulators.
+// Precision: 3xTF32 (a_lo p_hi + a_hi p_lo + a_hi p_hi, FP32 accumulation),
+// or one TF32 product for a correction that is itself tiny (PASSES = 1).
+//
+// Every wait is bounded (limit g_tc_wait_limit, polled together with the
+// CTA's abort flag).  A wait that runs out sets the abort flag; the CTA then
+// waits (bounded by the full limit) for its bulk copies and MMAs in flight,
+// records DE_TIMEOUT in the error word, frees its tensor memory and returns.
+#pragma once
+
+#include "bddc_batch_tc.cuh"
+#include "bddc_tc.cuh"
+
+namespace bddc {
+
+constexpr int SWT_AST = 6;                       // TMEM stages of split window chunks
+constexpr int SWT_PST = 6;                       // shared-memory slots of panel chunks
+constexpr int SWT_GROUP = 128;                   // threads of one staging group
+constexpr int SWT_PRODUCER = 8, SWT_ISSUER = 9;  // warps
+constexpr int SWT_THREADS = 320;
+constexpr uint32_t SWT_ACOL = 2 * TC_N;  // TMEM column of stage 0, after the two accumulators
+constexpr uint32_t SWT_TCOLS = 512;
+static_assert(SWT_ACOL + SWT_AST * 2 * TC_KC <= SWT_TCOLS, "tensor memory columns");
+constexpr size_t swt_smem_bytes() { return (size_t)SWT_PST * TC_PCHUNK * sizeof(float) + 128; }
+
+// Spin limit of the sweeps' waits (the wind-down waits use TC_SPIN_LIMIT).
+// Settable for tests of the timeout path (bddcml_set_wait_limit_c).
+static __device__ long long g_tc_wait_limit = TC_SPIN_LIMIT;
+
+// bounded wait that also gives up when another thread of the CTA has aborted
+__device__ __forceinline__ bool swt_wait(uint64_t* bar, uint32_t parity, long long limit,
+                                         const volatile int* abort_flag) {
+  for (long long i = 0; i < limit; ++i) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((i & 63) == 63 && *abort_flag) return false;
+  }
+  return false;
+}
+
+// Window of block row k: forward blocks jlo .. k, backward k .. k + nblk - 1;
+// the panel index of block jb is jb - j0.  Forward sweeps of identity columns
+// start at row s0 and skip the zero blocks above it.
+struct SwWin {
+  int k, j0, jlo, nblk;
+};
+
+__device__ __forceinline__ SwWin sw_win(int dir, int nb, int w, int s0, int k) {
+  SwWin r;
+  r.k = k;
+  if (dir == 0) {
+    r.j0 = k - min(k, w);
+    r.jlo = max(r.j0, s0);
+    r.nblk = k - r.jlo + 1;
+  } else {
+    r.j0 = k;
+    r.jlo = k;
+    r.nblk = min(w, nb - 1 - k) + 1;
+  }
+  return r;
+}
+
+// chunk q of the window (two 32-row halves per block): the older solved
+// blocks first, then the right-hand-side block k, then the freshest block
+// (k - 1 forward, k + 1 backward), the only one that depends on the previous step
+__device__ __forceinline__ void sw_chunk(int dir, const SwWin& W, int q, int& jb, int& pq, bool& dep) {
+  const int p = q >> 1;
+  dep = false;
+  if (W.nblk == 1) {
+    jb = W.k;
+  } else if (p == W.nblk - 1) {
+    jb = dir == 0 ? W.k - 1 : W.k + 1;
+    dep = true;
+  } else if (p == W.nblk - 2) {
+    jb = W.k;
+  } else {
+    jb = dir == 0 ? W.jlo + p : W.k + 2 + p;
+  }
+  pq = 2 * (jb - W.j0) + (q & 1);
+}
+
+template <int PASSES, bool ACC>
+__global__ void __launch_bounds__(SWT_THREADS, 1)
+    k_band_sweep_tm(const TcDesc* __restrict__ td, const float* __restrict__ ppool, float* __restrict__ bpool,
+                    int dir, int* __restrict__ err) {
+  const TcDesc d = td[blockIdx.y];
+  const int c0 = blockIdx.x * TC_M;
+  if (c0 >= d.ncol || d.nb == 0) return;
+  const int ld = d.ncol;
+  float* B = bpool + d.oB;
+  const float* P = ppool + (dir == 0 ? d.oPf : d.oPb);
+  const uint32_t pbytes = (PASSES == 1 ? TC_PCHUNK / 2 : TC_PCHUNK) * 4;  // hi half first in a chunk
+  // a forward sweep of a tile inside the identity columns (pad = their
+  // count) starts at the tile's diagonal block row: the rows above stay zero
+  const int s0 = (dir == 0 && c0 + TC_M <= d.pad) ? c0 / NB : 0;
+  const int nsteps = d.nb - s0;
+  auto row_of = [&](int sidx) { return dir == 0 ? s0 + sidx : d.nb - 1 - sidx; };
+  const long long limit = g_tc_wait_limit;
+
+  extern __shared__ __align__(128) unsigned char swt_raw[];
+  float* sP = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(swt_raw) + 127) & ~uintptr_t(127));
+  __shared__ __align__(8) uint64_t bar_afull[SWT_AST], bar_aempty[SWT_AST];
+  __shared__ __align__(8) uint64_t bar_pfull[SWT_PST], bar_pfree[SWT_PST];
+  __shared__ __align__(8) uint64_t bar_accfull[2], bar_tfree[2];
+  __shared__ uint32_t tmem_base;
+  __shared__ volatile int abort_flag;
+  __shared__ long long last_pload[SWT_PST], last_mma;
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid == 0) {
+    for (int s = 0; s < SWT_AST; ++s) {
+      mbar_init(&bar_afull[s], SWT_GROUP);
+      mbar_init(&bar_aempty[s], 1);
+    }
+    for (int s = 0; s < SWT_PST; ++s) {
+      mbar_init(&bar_pfull[s], 1);
+      mbar_init(&bar_pfree[s], 1);
+      last_pload[s] = -1;
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&bar_accfull[b], 1);
+      mbar_init(&bar_tfree[b], SWT_GROUP);
+    }
+    abort_flag = 0;
+    last_mma = -1;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                 "r"(SWT_TCOLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_base;
+
+  if (warp == SWT_PRODUCER) {
+    // ------------------------------------------------ panel chunks (one thread)
+    if (lane == 0) {
+      long long g = 0;
+      bool ok = true;
+      for (int sidx = 0; sidx < nsteps && ok; ++sidx) {
+        const SwWin W = sw_win(dir, d.nb, d.w, s0, row_of(sidx));
+        for (int q = 0; q < 2 * W.nblk; ++q, ++g) {
+          const int s = (int)(g % SWT_PST);
+          const long long use = g / SWT_PST;
+          if (abort_flag || (use > 0 && !swt_wait(&bar_pfree[s], (uint32_t)((use - 1) & 1), limit, &abort_flag))) {
+            abort_flag = 1;
+            ok = false;
+            break;
+          }
+          int jb, pq;
+          bool dep;
+          sw_chunk(dir, W, q, jb, pq, dep);
+          mbar_expect_tx(&bar_pfull[s], pbytes);
+          bulk_g2s(sP + s * TC_PCHUNK, P + panel_chunk(0, d.w, W.k, pq), pbytes, &bar_pfull[s]);
+          last_pload[s] = g;
+        }
+      }
+    }
+  } else if (warp == SWT_ISSUER) {
+    // ------------------------------------------------ MMA issuer (one thread)
+    if (lane == 0) {
+      constexpr uint32_t idesc = tc_idesc(TC_M, TC_N);
+      long long g = 0;
+      bool ok = true;
+      for (int sidx = 0; sidx < nsteps && ok; ++sidx) {
+        const int b = sidx & 1;
+        if (abort_flag ||
+            (sidx >= 2 && !swt_wait(&bar_tfree[b], (uint32_t)(((sidx - 2) >> 1) & 1), limit, &abort_flag))) {
+          abort_flag = 1;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t dacc = tmem + (uint32_t)(b * TC_N);
+        const SwWin W = sw_win(dir, d.nb, d.w, s0, row_of(sidx));
+        const int nch = 2 * W.nblk;
+        for (int q = 0; q < nch; ++q, ++g) {
+          const int sa = (int)(g % SWT_AST), sp = (int)(g % SWT_PST);
+          if (!swt_wait(&bar_afull[sa], (uint32_t)((g / SWT_AST) & 1), limit, &abort_flag) ||
+              !swt_wait(&bar_pfull[sp], (uint32_t)((g / SWT_PST) & 1), limit, &abort_flag)) {
+            abort_flag = 1;
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t a_hi = tmem + SWT_ACOL + (uint32_t)(sa * 2 * TC_KC), a_lo = a_hi + TC_KC;
+          const uint32_t p_hi = smem_u32(sP + sp * TC_PCHUNK), p_lo = p_hi + TC_N * TC_KC * 4;
+#pragma unroll
+          for (int kk = 0; kk < TC_KC / 8; ++kk) {
+            const uint32_t koff = kk * 2 * TC_LBO;
+            const uint32_t acc = (q > 0 || kk > 0) ? 1u : 0u;
+            if (PASSES == 1) {
+              mma_tf32_ta(dacc, a_hi + kk * 8, tc_desc(p_hi + koff), idesc, acc);
+            } else {
+              mma_tf32_ta(dacc, a_lo + kk * 8, tc_desc(p_hi + koff), idesc, acc);
+              mma_tf32_ta(dacc, a_hi + kk * 8, tc_desc(p_lo + koff), idesc, 1u);
+              mma_tf32_ta(dacc, a_hi + kk * 8, tc_desc(p_hi + koff), idesc, 1u);
+            }
+          }
+          mma_commit(&bar_aempty[sa]);
+          mma_commit(&bar_pfree[sp]);
+          if (q == nch - 1) mma_commit(&bar_accfull[b]);
+          last_mma = g;
+        }
+      }
+    }
+  } else {
+    // ------------------------------------------------ staging groups and epilogue
+    const int G = warp >> 2;              // stages the chunks of the window blocks jb with (jb & 1) == G
+    const int r = tid & (SWT_GROUP - 1);  // column of the tile = TMEM lane
+    const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
+    float* col = B + c0 + r;
+    float* col_acc = (ACC && dir == 1 && d.oAcc >= 0) ? bpool + d.oAcc + c0 + r : nullptr;
+
+    // split one 32-row piece of this thread's column into the stage of chunk g
+    auto fill = [&](long long g, const float (&v)[TC_KC]) -> bool {
+      const int sa = (int)(g % SWT_AST);
+      const long long use = g / SWT_AST;
+      bool good = !abort_flag &&
+                  (use == 0 || swt_wait(&bar_aempty[sa], (uint32_t)((use - 1) & 1), limit, &abort_flag));
+      good = __all_sync(0xffffffffu, good);  // the TMEM stores below are warp-collective
+      if (!good) return false;
+      tc_fence_after();
+      float h[TC_KC], l[TC_KC];
+#pragma unroll
+      for (int t = 0; t < TC_KC; ++t) {
+        h[t] = tf32_rna(v[t]);
+        l[t] = tf32_rna(v[t] - h[t]);
+      }
+      const uint32_t ta = tmem + lane_base + SWT_ACOL + (uint32_t)(sa * 2 * TC_KC);
+      tmem_st32(ta, h);
+      if (PASSES != 1) tmem_st32(ta + TC_KC, l);
+      tmem_st_wait();
+      tc_fence_before();
+      mbar_arrive(&bar_afull[sa]);
+      return true;
+    };
+    // results of step se (block row k) from its accumulator to B; with gdep >= 0
+    // the two halves also become chunks gdep and gdep + 1 of the next step
+    auto epilogue = [&](int se, long long gdep) -> bool {
+      const int k = row_of(se), b = se & 1;
+      bool good = !abort_flag && swt_wait(&bar_accfull[b], (uint32_t)((se >> 1) & 1), limit, &abort_flag);
+      good = __all_sync(0xffffffffu, good);  // the TMEM loads below are warp-collective
+      if (!good) return false;
+      tc_fence_after();
+      // the row stride is made opaque so that the row offsets are formed here
+      // rather than kept live in registers across the sweep
+      long long lds = ld;
+      asm volatile("" : "+l"(lds));
+#pragma unroll 1
+      for (int h = 0; h < 2; ++h) {
+        float v[TC_KC];
+        {
+          float v0[16], v1[16];
+          tmem_ld16(tmem + lane_base + (uint32_t)(b * TC_N + h * TC_KC), v0);
+          tmem_ld16(tmem + lane_base + (uint32_t)(b * TC_N + h * TC_KC + 16), v1);
+#pragma unroll
+          for (int i = 0; i < 16; ++i) {
+            v[i] = v0[i];
+            v[16 + i] = v1[i];
+          }
+        }
+        float* dst = col + (long long)(k * NB + h * TC_KC) * lds;
+#pragma unroll
+        for (int i = 0; i < TC_KC; ++i) dst[(long long)i * lds] = v[i];
+        if (ACC && col_acc) {
+          float* dst2 = col_acc + (long long)(k * NB + h * TC_KC) * lds;
+          float a[TC_KC];
+#pragma unroll
+          for (int i = 0; i < TC_KC; ++i) a[i] = dst2[(long long)i * lds];
+#pragma unroll
+          for (int i = 0; i < TC_KC; ++i) dst2[(long long)i * lds] = a[i] + v[i];
+        }
+        if (gdep >= 0 && !fill(gdep + h, v)) return false;
+      }
+      tc_fence_before();
+      mbar_arrive(&bar_tfree[b]);  // the accumulator may take step se + 2
+      return true;
+    };
+    auto load = [&](int jb, int half, float (&v)[TC_KC]) {
+      const float* src = col + (long long)(jb * NB + half * TC_KC) * ld;
+#pragma unroll
+      for (int t = 0; t < TC_KC; ++t) v[t] = src[(long long)t * ld];
+    };
+    // this group's next chunk after chunk q of step sidx (sequence number g):
+    // its step ns (-1: none), block, half, sequence number and dependency flag
+    auto next_owned = [&](int sidx, int q, long long g, int& ns, long long& ng, int& njb, int& nhalf, bool& ndep) {
+      ns = sidx;
+      int nq = q + 1;
+      ng = g + 1;
+      while (ns < nsteps) {
+        const SwWin W = sw_win(dir, d.nb, d.w, s0, row_of(ns));
+        for (; nq < 2 * W.nblk; ++nq, ++ng) {
+          int pq;
+          sw_chunk(dir, W, nq, njb, pq, ndep);
+          if ((njb & 1) == G) {
+            nhalf = nq & 1;
+            return;
+          }
+        }
+        ++ns;
+        nq = 0;
+      }
+      ns = -1;
+    };
+
+    float vn[TC_KC];
+    long long gn = -1;  // sequence number of the chunk held in vn
+    long long g = 0;
+    bool ok = true;
+    for (int sidx = 0; sidx < nsteps && ok; ++sidx) {
+      const SwWin W = sw_win(dir, d.nb, d.w, s0, row_of(sidx));
+      const int nch = 2 * W.nblk;
+      // a window of one block (a block-diagonal band) does not read the previous
+      // step's results: they are written out here instead
+      if (sidx > 0 && W.nblk == 1 && (row_of(sidx - 1) & 1) == G && !epilogue(sidx - 1, -1)) {
+        ok = false;
+        break;
+      }
+      for (int q = 0; q < nch; ++q, ++g) {
+        int jb, pq;
+        bool dep;
+        sw_chunk(dir, W, q, jb, pq, dep);
+        if ((jb & 1) != G) continue;
+        if (dep) {  // both halves of the freshest block come from the previous step's epilogue
+          if (!epilogue(sidx - 1, g)) {
+            ok = false;
+            break;
+          }
+          ++q;
+          ++g;
+          continue;
+        }
+        float v[TC_KC];
+        if (gn == g) {
+#pragma unroll
+          for (int t = 0; t < TC_KC; ++t) v[t] = vn[t];
+        } else {
+          load(jb, q & 1, v);
+        }
+        // prefetch this group's next chunk unless it is a freshest block (made by the epilogue)
+        {
+          int ns, njb, nhalf;
+          long long ng;
+          bool ndep;
+          next_owned(sidx, q, g, ns, ng, njb, nhalf, ndep);
+          gn = -1;
+          if (ns >= 0 && !ndep) {
+            load(njb, nhalf, vn);
+            gn = ng;
+          }
+        }
+        if (!fill(g, v)) {
+          ok = false;
+          break;
+        }
+      }
+    }
+    // the last block row has no following step: the group that owns it writes it
+    if (ok && (row_of(nsteps - 1) & 1) == G && !epilogue(nsteps - 1, -1)) ok = false;
+    if (!ok) abort_flag = 1;
+  }
+  // wind-down: after an abort, wait (bounded) for the copies and MMAs in flight before freeing TMEM
+  __syncthreads();
+  if (tid == 0 && abort_flag) {
+    for (int s = 0; s < SWT_PST; ++s)
+      if (last_pload[s] >= 0) mbar_wait(&bar_pfull[s], (uint32_t)((last_pload[s] / SWT_PST) & 1));
+    const long long qm = last_mma;
+    if (qm >= 0) mbar_wait(&bar_aempty[qm % SWT_AST], (uint32_t)((qm / SWT_AST) & 1));
+    atomicOr(err, DE_TIMEOUT);
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(SWT_TCOLS));
+}
+
+}  // namespace bddc

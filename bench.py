@@ -36,9 +36,23 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+
+def visible_device_for_rank(local_rank, visible):
+    """The CUDA_VISIBLE_DEVICES value for one rank of a multi-rank launch: the
+    LOCAL_RANK-th entry of a list the launcher already set (so that a job given
+    GPUs 4,5 stays on them), else the bare local rank."""
+    if visible:
+        ids = [v.strip() for v in visible.split(",") if v.strip()]
+        if local_rank >= len(ids):
+            raise ValueError(f"LOCAL_RANK {local_rank} but CUDA_VISIBLE_DEVICES lists {len(ids)} GPUs")
+        return ids[local_rank]
+    return str(local_rank)
+
+
 # one process per GPU under torchrun: pin the GPU before any CUDA library loads
 if "LOCAL_RANK" in os.environ and int(os.environ.get("WORLD_SIZE", "1")) > 1:
-    os.environ["CUDA_VISIBLE_DEVICES"] = os.environ["LOCAL_RANK"]
+    os.environ["CUDA_VISIBLE_DEVICES"] = visible_device_for_rank(int(os.environ["LOCAL_RANK"]),
+                                                                 os.environ.get("CUDA_VISIBLE_DEVICES"))
 
 import numpy as np  # noqa: E402
 
@@ -63,6 +77,10 @@ WORKLOADS = {
     # the same subdomain size on 48^3 with 64 subdomains (8 level-2 subdomains): the
     # small case of the batched kernels for parity runs and full profiler captures
     "elasticity_48^3_64subs_3levels_64rhs": ("elasticity", (12, 4, 8, 64), 1, None),
+    # differentiation: 64^3 Poisson, 64 subdomains of 16^3, log-normal kappa (sigma 1,
+    # seed 3), J = 1/2 |u - u*|^2 with u* from 8 seeded Fourier modes (seed 4); one step
+    # = forward solve + adjoint solve + per-element gradient through torch.autograd
+    "poisson_64^3_64subs_gradient": ("gradient", (16, 4), 0, None),
 }
 DEFAULT_WORKLOAD = "poisson_128^3_512subs"
 
@@ -138,6 +156,8 @@ def make_problem(workload):
     kind, par, _, _ = WORKLOADS[workload]
     if kind == "cube":
         return problems.poisson_on_cube(*par)
+    if kind == "gradient":
+        return problems.poisson_on_cube(*par, kappa=problems.lognormal_kappa(par[0] * par[1], 1.0, seed=3))
     if kind == "elasticity":
         nes, nss = par[0], par[1]
         return problems.elasticity_on_cube(nes, nss, nu=0.3, young=problems.inclusions_young(nes * nss))
@@ -261,7 +281,9 @@ def batch_schur_roofline(prof, st, hbm, tensor, peak_kind):
 
 
 def cpu_baseline(prob, nthreads=None, weights=0):
-    """The CPU restatement (oracle/) on the same workload: upload + setup + solve."""
+    """The CPU restatement (oracle/) on the same workload: upload + setup + solve.
+    Returns the baseline record and the oracle's global solution (the parity
+    reference of the GPU solution)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as orc
     orc.build()
@@ -272,7 +294,36 @@ def cpu_baseline(prob, nthreads=None, weights=0):
     it, reason, cond = o.solve(1e-8, 1000, 1000)
     t = time.perf_counter() - t0
     return {"value": t, "unit": "s", "cores": nthreads, "kind": "port",
-            "sample": f"full workload, one solve (upload + setup + PCG, {it} iterations)", "iterations": it}
+            "sample": f"full workload, one solve (upload + setup + PCG, {it} iterations)", "iterations": it,
+            "note": "band-Cholesky restatement (A11 and the constrained local problem factored in band form in "
+                    "the subdomain's dof order), not the reference's MUMPS sparse LDL^T"}, \
+        (o.global_solution(), it, reason)
+
+
+def global_vector(prob, sols):
+    u = np.zeros(prob.ndof)
+    for s, v in zip(prob.subdomains, sols):
+        u[s.isvgvn] = v
+    return u
+
+
+def oracle_parity(prob, sols, it, reason, sols64, it64, oracle_result):
+    """GPU solutions (mixed, and plain FP64 when run) against the oracle's on
+    the same workload: iterations within +-2 and relative error <= 1e-7
+    (mixed) / 1e-8 (FP64), the bar of the path's specification."""
+    u_o, it_o, reason_o = oracle_result
+    nrm = np.linalg.norm(u_o)
+    out = {"iterations_oracle": int(it_o), "iterations": int(it), "converged_reason_oracle": int(reason_o),
+           "rel_err_vs_oracle": float(np.linalg.norm(global_vector(prob, sols) - u_o) / nrm),
+           "tolerance": 1e-7}
+    ok = reason == reason_o == 0 and abs(int(it) - int(it_o)) <= 2 and out["rel_err_vs_oracle"] <= 1e-7
+    if sols64 is not None:
+        out["fp64_iterations"] = int(it64)
+        out["fp64_rel_err_vs_oracle"] = float(np.linalg.norm(global_vector(prob, sols64) - u_o) / nrm)
+        out["fp64_tolerance"] = 1e-8
+        ok = ok and abs(int(it64) - int(it_o)) <= 2 and out["fp64_rel_err_vs_oracle"] <= 1e-8
+    out["ok"] = bool(ok)
+    return out
 
 
 def replica_max(values, dist=None):
@@ -368,8 +419,11 @@ def run_gpu(args):
     kind, _, weights, tau = WORKLOADS[args.workload]
     # the oracle solves the adaptive pair eigenproblems densely, and takes minutes on the
     # three-level elasticity: both far beyond a bounded sample
-    cpu = None if (args.no_cpu_baseline or tau is not None or kind == "elasticity") else \
-        cpu_baseline(prob, weights=weights)
+    cpu, parity = None, None
+    if not (args.no_cpu_baseline or tau is not None or kind == "elasticity"):
+        cpu, oracle_result = cpu_baseline(prob, weights=weights)
+        parity = oracle_parity(prob, sols, it, reason, sols64 if fp64 else None, fp64["iterations"] if fp64 else 0,
+                               oracle_result)
     out = {
         "metric": METRIC, "value": dev_mean, "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_mean * 1e3, "higher_is_better": False, "scaling": "weak",
@@ -392,6 +446,7 @@ def run_gpu(args):
         "gpu_launches": int(args.steps * (st["launches_setup"] + st["launches_solve"])),
         "gpu_launches_per_step": {"setup": int(st["launches_setup"]), "solve": int(st["launches_solve"])},
         "roofline": roof, "phase_rooflines": all_roof, "fp64_plain": fp64, "cpu_baseline": cpu,
+        "parity": parity,
         "refinement": {"max_correction_ratio_1": st_p["refine1"], "max_correction_ratio_2": st_p["refine2"]},
         "adaptive": None if tau is None else {k: st_p[k] for k in ("npair", "nadaptive", "adapt_est", "t_adaptive",
                                                                   "lobpcg_resid", "lobpcg_iter", "ndofc")},
@@ -403,6 +458,136 @@ def run_gpu(args):
     print(json.dumps(out))
     if dist:
         dist.destroy_process_group()
+    if parity is not None and not parity["ok"]:
+        print(f"parity with the oracle failed: {parity}", file=sys.stderr)
+        sys.exit(3)
+
+
+def run_gradient(args):
+    """Differentiation workload: dJ/dkappa through the torch.autograd binding
+    (forward BDDC solve, adjoint solve reusing the forward factors, per-element
+    gradient kernel).  `value` is the device time: the library's CUDA events of
+    the forward setup and solve and of the adjoint's new data and solve, plus
+    the gradient kernel.  `e2e` is the wall time of the user call from kappa in
+    pinned host memory to the gradient back in host memory.  Outside the timed
+    steps the gradient is compared with the oracle's forward + adjoint gradient
+    (same tolerance), and plain-FP64 solves to relres 1e-12 give central
+    differences along 32 seeded directions (step 1e-6)."""
+    import torch
+    import bddcml_gb300 as B
+    from bddcml_gb300 import build, problems
+    from bddcml_gb300.autograd import PoissonCube
+    build.build()
+    ne, ns = WORKLOADS[args.workload][1]
+    n = ne * ns
+    hbm, tensor, peak_kind = load_peaks()
+    kappa = problems.lognormal_kappa(n, 1.0, seed=3)
+    ustar = problems.smooth_target(n, seed=4)
+    k_host = torch.tensor(kappa, dtype=torch.float64).pin_memory()
+    us = torch.tensor(ustar, dtype=torch.float64, device="cuda")
+    op = PoissonCube(ne, ns, precision=1, tol=1e-8, maxit=1000)
+
+    def step(profile=False):
+        op.profile = profile
+        t0 = time.perf_counter()
+        k = k_host.to("cuda", non_blocking=True).requires_grad_(True)
+        u = op.solve(k)
+        J = 0.5 * torch.sum((u - us) ** 2)
+        J.backward()
+        g = k.grad.to("cpu")
+        t = time.perf_counter() - t0
+        dev = (op.last_profile["numeric_total"][0] + op.last_profile["solve_total"][0] + op.last_gradient_ms) / 1e3
+        return t, dev, u.detach(), g
+
+    for _ in range(args.warmup):
+        step()
+    sampler = ClockSampler()
+    sampler.start()
+    e2e_t, dev_t = [], []
+    for _ in range(args.steps):
+        t, dev, u, g = step()
+        e2e_t.append(t)
+        dev_t.append(dev)
+    clocks = sampler.stop()
+    dev_mean, e2e_mean = statistics.mean(dev_t), statistics.mean(e2e_t)
+    st = op.last_stats
+    it_f, it_a = op.last_iterations, op.last_adjoint_iterations
+    step(profile=True)
+    prof_p, st_p = op.last_profile, op.last_stats
+    dominant = max(SETUP_PHASES + ["pcg"], key=lambda k: prof_p[k][0])
+    roof = phase_roofline(dominant, prof_p, st_p, hbm, tensor, peak_kind)
+    if roof is None:
+        cands = [k for k in ("solve_interior", "precond_solve", "refine_residual", "schur_apply", "precond_local")
+                 if phase_roofline(k, prof_p, st_p, hbm, tensor, peak_kind)]
+        dominant = max(cands, key=lambda k: prof_p[k][0])
+        roof = phase_roofline(dominant, prof_p, st_p, hbm, tensor, peak_kind)
+    roof["phase"] = dominant
+    roof["traffic"] = None
+    # the oracle's forward + adjoint gradient at the same tolerance (CPU leg)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+    from oracle_gradient import oracle_gradient
+    orc.build()
+    nthreads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    u_o, g_o, it_fo, it_ao = oracle_gradient(orc, ne, ns, kappa, ustar, tol=1e-8, nthreads=nthreads,
+                                             with_iterations=True)
+    t_cpu = time.perf_counter() - t0
+    u_np, g_np = u.cpu().numpy(), g.numpy()
+    err_u = float(np.linalg.norm(u_np - u_o) / np.linalg.norm(u_o))
+    err_g = float(np.linalg.norm(g_np - g_o) / np.linalg.norm(g_o))
+    # central differences along 32 seeded directions, plain FP64 solves to relres 1e-12
+    fd_op = PoissonCube(ne, ns, precision=0, tol=1e-12, maxit=1000)
+    kt = torch.tensor(kappa, dtype=torch.float64, device="cuda")
+    kg = kt.clone().requires_grad_(True)
+    J = 0.5 * torch.sum((fd_op.solve(kg) - us) ** 2)
+    J.backward()
+    g_acc = kg.grad.cpu().numpy()
+    err_g64 = float(np.linalg.norm(g_np - g_acc) / np.linalg.norm(g_acc))
+    rng = np.random.default_rng(11)
+    eps, worst = 1e-6, 0.0
+    with torch.no_grad():
+        for _ in range(32):
+            d = rng.standard_normal(kappa.size)
+            dt = torch.tensor(d, dtype=torch.float64, device="cuda")
+            jp = 0.5 * torch.sum((fd_op.solve(kt * torch.exp(eps * dt)) - us) ** 2).item()
+            jm = 0.5 * torch.sum((fd_op.solve(kt * torch.exp(-eps * dt)) - us) ** 2).item()
+            fd = (jp - jm) / (2 * eps)
+            an = float(np.dot(g_acc, kappa * d))
+            worst = max(worst, abs(fd - an) / max(abs(fd), abs(an)))
+    B.bddcml_finalize()
+    parity = {"iterations": [int(it_f), int(it_a)], "iterations_oracle": [int(it_fo), int(it_ao)],
+              "rel_err_vs_oracle": err_u, "gradient_rel_err_vs_oracle": err_g, "tolerance": 1e-7,
+              "gradient_rel_diff_vs_fp64_tol1e-12": err_g64,
+              "fd_directions": 32, "fd_step": eps, "fd_worst_rel_diff": worst, "fd_tolerance": 1e-5,
+              "fd_solves": "plain FP64, relres 1e-12"}
+    parity["ok"] = bool(abs(it_f - it_fo) <= 2 and abs(it_a - it_ao) <= 2 and err_u <= 1e-7 and err_g <= 1e-7
+                        and worst <= 1e-5)
+    h2d = st["h2d_bytes"] + kappa.nbytes
+    d2h = st["d2h_bytes"] + kappa.nbytes
+    out = {
+        "metric": METRIC, "value": dev_mean, "unit": "s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dev_mean * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 factors / f64 Krylov", "data": "synthetic (seeded log-normal coefficients and target)",
+        "config": {"workload": args.workload, "elements": n ** 3, "subdomains": ns ** 3, "dofs": (n + 1) ** 3,
+                   "precision": "mixed", "tol": 1e-8, "objective": "1/2 |u - u*|^2",
+                   "gradient_entries": n ** 3,
+                   "step": "forward solve + adjoint solve (forward factors) + element gradient",
+                   "l2": "inputs larger than L2 (factors streamed per step)",
+                   "timing": "CUDA events of the library (setup, new data, solves) and of the gradient kernel "
+                             "(value); host wall clock around the autograd call (e2e)",
+                   "parallelism": "1 GPU, all subdomains resident"},
+        "e2e": {"value": e2e_mean, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(args.steps * (st["launches_setup"] + st["launches_solve"] + 1)),
+        "phases_ms": {k: v[0] for k, v in prof_p.items()}, "roofline": roof, "parity": parity,
+        "cpu_baseline": {"value": t_cpu, "unit": "s", "cores": nthreads, "kind": "port",
+                         "sample": "full workload: oracle forward + adjoint solve and gradient, one step"},
+        "clocks": clocks,
+    }
+    print(json.dumps(out))
+    if not parity["ok"]:
+        print(f"parity with the oracle failed: {parity}", file=sys.stderr)
+        sys.exit(3)
 
 
 def run_reference(args):
@@ -419,13 +604,22 @@ def run_reference(args):
         o.solve(1e-8, 500, 50)
     times, it = [], None
     nthreads = os.cpu_count() or 1
+    kind, par, _, _ = WORKLOADS[args.workload]
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        o = orc.Oracle(prob, nthreads=nthreads)
-        o.setup(1, 1, 0)
-        it, reason, cond = o.solve(1e-8, 500, 50)
+        if kind == "gradient":  # forward + adjoint solve and the element gradient
+            from bddcml_gb300 import problems
+            from oracle_gradient import oracle_gradient
+            n = par[0] * par[1]
+            _, _, it, _ = oracle_gradient(orc, par[0], par[1], problems.lognormal_kappa(n, 1.0, seed=3),
+                                          problems.smooth_target(n, seed=4), tol=1e-8, nthreads=nthreads,
+                                          with_iterations=True)
+        else:
+            o = orc.Oracle(prob, nthreads=nthreads)
+            o.setup(1, 1, 0)
+            it, reason, cond = o.solve(1e-8, 500, 50)
+            del o
         times.append(time.perf_counter() - t0)
-        del o
     v = statistics.mean(times)
     out = {"metric": METRIC, "value": v, "unit": "s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
@@ -435,8 +629,9 @@ def run_reference(args):
                             "sample": "full workload per step (upload + setup + PCG); warm-up steps on the 32^3 case"},
            "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
            "iterations": it,
-           "note": "CPU restatement of the reference algorithm (oracle/); the Fortran/MPI/MUMPS reference "
-                   "cannot be built on this image"}
+           "note": "CPU restatement of the reference algorithm (oracle/), with band Cholesky factors of A11 and "
+                   "of the constrained local problem in place of MUMPS's sparse LDL^T; the Fortran/MPI/MUMPS "
+                   "reference cannot be built on this image"}
     print(json.dumps(out))
 
 
@@ -452,6 +647,8 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif WORKLOADS[args.workload][0] == "gradient":
+        run_gradient(args)
     else:
         run_gpu(args)
 

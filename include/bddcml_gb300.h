@@ -251,6 +251,15 @@ void bddcml_get_profile_c(double *ms, int *counts, int *lphase);
  * No counterpart in the reference. */
 void bddcml_release_device_memory_c(void);
 
+/* Spin limit of every wait inside the tensor-core sweep kernels of the
+ * current device (*spins <= 0 restores the default, 2^26 polls).  A wait that
+ * runs out stops its kernel cleanly (bulk copies and MMAs in flight are
+ * drained, tensor memory is freed) and the setup fails with
+ * BDDCML_ERR_NUMERIC; the next setup starts clean.  Meant for testing that
+ * path with a tiny limit.  No counterpart in the reference, whose errors
+ * abort (module_utils.f90:296-298). */
+void bddcml_set_wait_limit_c(long long *spins);
+
 /* Eigenvalue threshold tau of the adaptive face constraints (no counterpart in
  * the reference, which fixes it at 1.5: threshold_eigval_default,
  * module_adaptivity.f90:30).  Eigenvectors of the face-pair problems with
@@ -288,14 +297,19 @@ void bddcml_element_gradient_dev_c(int *nelem, int *nne, const int *inet, const 
  * every GPU that loads the library keeps until the process exits.  It holds
  * subdomains with at most 65536 interface dofs; a larger interface is
  * rejected with BDDCML_ERR_ARGUMENT.  The array keeps the previous call's
- * contents; the one counter that must start at zero is reset by each call.  It is meant for callers that keep their
+ * contents; the one counter that must start at zero is cleared by each call
+ * before its kernel runs.  It is meant for callers that keep their
  * vectors on the GPU and may not allocate at that point: an application that
  * reserves all device memory up front, or one whose own allocator forbids
  * device allocations (and the implicit device synchronisation of cudaMalloc
  * and cudaFree) inside its time-stepping loop.
  *
  * The first call on each device looks up the scratch address
- * (cudaGetSymbolAddress), so make one call before any stream capture.  Work
+ * (cudaGetSymbolAddress).  Under CUDA's lazy module loading (the default since
+ * CUDA 12.2) that first call also loads the library's module on the device,
+ * which is when the static array is placed in device memory: make one call per
+ * device before any region where allocation is not allowed, and before any
+ * stream capture.  Later calls allocate nothing.  Work
  * runs on the legacy default stream; the vectors must be ready there.  Calls
  * must not overlap in time (several host threads, several streams): they share
  * the scratch and would race.  Needs a finished bddcml_setup_preconditioner_c. */

@@ -6,7 +6,7 @@ against the gradient assembled from CPU oracle forward + adjoint solves."""
 import numpy as np
 import pytest
 
-from gradient_util import oracle_gradient
+from oracle_gradient import oracle_gradient
 
 pytestmark = pytest.mark.gpu
 

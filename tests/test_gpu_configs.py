@@ -1,0 +1,295 @@
+"""GPU parity at the sizes of the benchmark configurations, through the C ABI,
+against the CPU oracle (restatement of krylov_bddcpcg, module_krylov.f90:765-809
+stop rule and reasons, and of the BDDC preconditioner of module_levels.f90).
+
+- C1: Poisson 32^3, 2 x 2 x 2 subdomains of 16^3 (the subdomain size of the
+  128^3 benchmark: a 64-row block band of about 5 blocks, 53 block rows), with
+  the configured load and with a seeded load.
+- C3 at an intermediate size: 32^3 with channels of 1e4 and a 3 x 3 x 3 box
+  partition with sides 8..16, rho-scaling, adaptive face constraints tau = 10.
+  (The oracle solves every face-pair pencil densely in FP64; at 48^3 that
+  takes more than twenty minutes.)
+- C4 at an intermediate size: 48^3 elasticity with 10 % of spherical
+  inclusions (E = 1e3), 64 subdomains of 12^3 (the subdomain size of the 96^3
+  configuration), three levels with 8 level-2 subdomains, rho-scaling; one
+  load, and a batch of 4 loads.
+- C5 at its size: 64^3 Poisson, 64 subdomains, log-normal kappa (sigma 1,
+  seed 3), J = 1/2 |u - u*|^2 with u* from 8 seeded Fourier modes; the adjoint
+  gradient against the oracle's forward + adjoint gradient and against central
+  differences on 32 random directions (step 1e-6).
+
+Tolerances as the path's specification states: iterations within +-2 of the
+oracle (+-1 per column for batches), solution relative error <= 1e-8 for the
+plain FP64 path and <= 1e-7 for the mixed path.
+"""
+import copy
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL = {0: 1e-8, 1: 1e-7}
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+# ---------------------------------------------------------------- C1
+def _random_load(prob, seed):
+    """The problem with a seeded N(0, 1) load at every free dof."""
+    g = np.random.default_rng(seed).standard_normal(prob.ndof)
+    p2 = copy.deepcopy(prob)
+    for s in p2.subdomains:
+        s.rhs = np.where(s.ifix != 0, 0.0, g[s.isvgvn])
+    return p2
+
+
+def _oracle_run(oracle_mod, prob):
+    o = oracle_mod.Oracle(prob)
+    o.setup(1, 1, 0)
+    it, reason, cond = o.solve(1e-8, 500, 50)
+    return it, reason, cond, o.global_solution()
+
+
+@pytest.fixture(scope="module")
+def c1(oracle_mod):
+    from bddcml_gb300 import problems
+    prob = problems.poisson_on_cube(16, 2)
+    prob_r = _random_load(prob, 3)
+    return prob, _oracle_run(oracle_mod, prob), prob_r, _oracle_run(oracle_mod, prob_r)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_c1_poisson_32cube_8subs(built_lib, c1, precision):
+    """C1 as configured (f = h^3 at every free node).  The load is symmetric
+    under the reflections of the cube that map the 2 x 2 x 2 partition onto
+    itself, and on that invariant subspace the BDDC preconditioner inverts S
+    exactly: the oracle converges in one iteration (relres 1e-14).  An FP32
+    perturbation of the preconditioner (mixed path) gives the residual parts
+    outside that subspace, where the spectrum is that of a generic load, so
+    the mixed path takes the iterations of a generic load (checked against the
+    oracle in the next test) and its condition estimate is the generic one."""
+    import bddcml_gb300 as B
+    from newdata_util import direct_solution
+    prob, (it_o, reason_o, cond_o, u_o), _, (it_r, _, cond_r, _) = c1
+    u, it, reason, cond, st = B.solve_problem(prob, precision=precision, tol=1e-8, maxit=500, ndecrmax=50)
+    err = _rel(u, u_o)
+    print(f"C1 precision {precision}: iterations {it} (oracle {it_o}; generic load {it_r}), cond {cond:.4f} "
+          f"(oracle {cond_o:.4f}; generic load {cond_r:.4f}), error vs oracle {err:.2e}")
+    assert reason == reason_o == 0
+    assert st["ndofc"] == 37  # 19 corners, 6 edges, 12 faces
+    assert err <= TOL[precision]
+    assert _rel(u, direct_solution(prob)) <= 1e-7
+    if precision == 0:
+        assert abs(it - it_o) <= 2
+    else:
+        assert it <= it_r + 2
+        assert it == 1 or abs(cond - cond_r) <= 0.05 * cond_r
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_c1_poisson_32cube_8subs_generic_load(built_lib, c1, precision):
+    """C1 mesh, partition and preconditioner with a seeded N(0, 1) load."""
+    import bddcml_gb300 as B
+    _, _, prob, (it_o, reason_o, cond_o, u_o) = c1
+    u, it, reason, cond, st = B.solve_problem(prob, precision=precision, tol=1e-8, maxit=500, ndecrmax=50)
+    err = _rel(u, u_o)
+    print(f"C1 generic load precision {precision}: iterations {it} (oracle {it_o}), cond {cond:.4f} "
+          f"(oracle {cond_o:.4f}), error vs oracle {err:.2e}")
+    assert reason == reason_o == 0
+    assert abs(it - it_o) <= 2
+    assert abs(cond - cond_o) <= 0.05 * cond_o
+    assert err <= TOL[precision]
+
+
+# ---------------------------------------------------------------- C3
+def _c3_problem():
+    from bddcml_gb300 import problems
+    ne = 32
+    kappa = problems.channel_kappa(ne, nchannels=8, width=2, contrast=1e4, sigma=2.0, seed=17)
+    return problems.poisson_boxes(ne, problems.random_box_counts(ne, (3, 3, 3), 8, 16, seed=17), kappa=kappa)
+
+
+@pytest.fixture(scope="module")
+def c3(oracle_mod):
+    prob = _c3_problem()
+    o = oracle_mod.Oracle(prob)
+    o.set_adaptive(True, 10.0)
+    o.setup(1, 1, 1)
+    it, reason, cond = o.solve(1e-8, 1000, 50)
+    return prob, it, reason, cond, o.global_solution(), o.adaptive_info()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_c3_channels_adaptive_32cube_27boxes(built_lib, c3, precision):
+    import bddcml_gb300 as B
+    prob, it_o, reason_o, cond_o, u_o, info_o = c3
+    u, it, reason, cond, st = B.solve_problem(prob, precision=precision, tol=1e-8, maxit=1000, ndecrmax=50,
+                                              weights_type=1, adaptive_tau=10.0)
+    err = _rel(u, u_o)
+    nad_o = int(info_o["nadaptive"].sum())
+    print(f"C3 precision {precision}: iterations {it} (oracle {it_o}), constraints {st['nadaptive']} "
+          f"(oracle {nad_o}), pairs {st['npair']}, error vs oracle {err:.2e}")
+    assert st["npair"] == len(info_o["pairs"])
+    assert st["nadaptive"] == nad_o
+    assert reason == reason_o == 0
+    assert abs(it - it_o) <= 2
+    assert err <= TOL[precision]
+
+
+# ---------------------------------------------------------------- C4
+C4_TOL_ERR = 1e-10  # solver tolerance of the error checks (see the test docstrings)
+
+
+def _c4_problem():
+    from bddcml_gb300 import problems
+    return problems.elasticity_on_cube(12, 4, nu=0.3, young=problems.inclusions_young(48))
+
+
+@pytest.fixture(scope="module")
+def c4(oracle_mod):
+    """Oracle runs of the subdomain loads and of 4 seeded load cases, each at
+    relres 1e-8 and 1e-10: {tol: (single, [columns])}."""
+    from bddcml_gb300 import problems
+    prob = _c4_problem()
+    loads = problems.body_force_loads(prob, 4, seed=5)
+    o = oracle_mod.Oracle(prob)
+    o.set_levels(3, 8)
+    o.setup(1, 1, 1)
+    out = {1e-8: [None, []], C4_TOL_ERR: [None, []]}
+    # every solve starts from the zero initial guess (a solve leaves its solution as the next guess)
+    for tol in out:
+        for s in prob.subdomains:
+            o.new_loads(s.isub, s.rhs)
+        it, reason, cond = o.solve(tol, 2000, 2000)
+        out[tol][0] = (it, reason, cond, o.global_solution())
+    for k in range(loads[0].shape[0]):
+        for tol in out:
+            for s, ld in zip(prob.subdomains, loads):
+                o.new_loads(s.isub, ld[k])
+            it, reason, cond = o.solve(tol, 2000, 2000)
+            out[tol][1].append((it, reason, o.global_solution()))
+    return prob, loads, out[1e-8], out[C4_TOL_ERR]
+
+
+def _c4_gpu(prob, precision, tol, loads=None):
+    import bddcml_gb300 as B
+    B.bddcml_init(3, [prob.nsub, 8, 1], -1, 0, 0, 0, 0)
+    try:
+        B.set_precision(precision)
+        B.upload_problem(prob)
+        B.bddcml_setup_preconditioner(1, 0, 1, 1, 1, 0, 0, 1)
+        if loads is None:
+            it, reason, cond = B.bddcml_solve(0, 0, tol, 2000, 2000, 0, 0)
+            u = np.zeros(prob.ndof)
+            for s in prob.subdomains:
+                u[s.isvgvn] = B.bddcml_download_local_solution(s.isub, s.ndofs)
+        else:
+            nrhs = loads[0].shape[0]
+            for s, ld in zip(prob.subdomains, loads):
+                B.bddcml_upload_subdomain_rhs_batch(s.isub, ld, 1)
+            it, reason, cond = B.bddcml_solve_batch(nrhs, 0, 0, tol, 2000, 2000)
+            u = np.zeros((nrhs, prob.ndof))
+            for s in prob.subdomains:
+                u[:, s.isvgvn] = B.bddcml_download_local_solution_batch(s.isub, nrhs, s.ndofs)
+    finally:
+        B.bddcml_finalize()
+    return u, it, reason, cond
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_c4_elasticity_48cube_3levels_one_load(built_lib, c4, precision):
+    """Iterations at the configured tolerance 1e-8.  The condition number is
+    about 670, so relres 1e-8 pins a solution only to a few 1e-6: the error
+    bound is checked on solves to relres 1e-10, where two solvers whose
+    iterates differ (FP32 preconditioner blocks) must still agree to 1e-7."""
+    prob, _, ((it_o, reason_o, cond_o, _), _), ((_, _, _, u_o), _) = c4
+    _, it, reason, cond = _c4_gpu(prob, precision, 1e-8)
+    u, _, reason2, _ = _c4_gpu(prob, precision, C4_TOL_ERR)
+    err = _rel(u, u_o)
+    print(f"C4 one load precision {precision}: iterations {it} (oracle {it_o}), cond {cond:.1f} "
+          f"(oracle {cond_o:.1f}), error vs oracle at relres {C4_TOL_ERR:g}: {err:.2e}")
+    assert reason == reason_o == 0 and reason2 == 0
+    assert abs(it - it_o) <= 2
+    assert err <= TOL[precision]
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_c4_elasticity_48cube_3levels_batch_of_4(built_lib, c4, precision):
+    prob, loads, (_, cols), (_, cols_e) = c4
+    _, it, reason, cond = _c4_gpu(prob, precision, 1e-8, loads)
+    u, _, reason2, _ = _c4_gpu(prob, precision, C4_TOL_ERR, loads)
+    errs = [_rel(u[k], cols_e[k][2]) for k in range(4)]
+    print(f"C4 batch precision {precision}: iterations {[int(i) for i in it]} (oracle {[c[0] for c in cols]}), "
+          f"errors vs oracle at relres {C4_TOL_ERR:g}: {['%.1e' % e for e in errs]}")
+    for k in range(4):
+        assert reason[k] == cols[k][1] == 0 and reason2[k] == 0
+        assert abs(int(it[k]) - cols[k][0]) <= 2
+        assert errs[k] <= TOL[precision]
+
+
+# ---------------------------------------------------------------- C5
+@pytest.fixture(scope="module")
+def c5(oracle_mod):
+    torch = pytest.importorskip("torch")
+    from bddcml_gb300 import problems
+    from oracle_gradient import oracle_gradient
+    n = 64
+    kappa = problems.lognormal_kappa(n, 1.0, seed=3)
+    ustar = problems.smooth_target(n, seed=4)
+    u_o, g_o = oracle_gradient(oracle_mod, 16, 4, kappa, ustar)
+    return torch, kappa, ustar, u_o, g_o
+
+
+def _c5_gradient(torch, precision, kappa, ustar):
+    from bddcml_gb300.autograd import PoissonCube
+    op = PoissonCube(16, 4, precision=precision, tol=1e-12)
+    k = torch.tensor(kappa, dtype=torch.float64, device="cuda").requires_grad_(True)
+    us = torch.tensor(ustar, dtype=torch.float64, device="cuda")
+    u = op.solve(k)
+    J = 0.5 * torch.sum((u - us) ** 2)
+    J.backward()
+    return op, us, u.detach().cpu().numpy(), k.grad.detach().cpu().numpy()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_c5_gradient_64cube_matches_oracle(built_lib, c5, precision):
+    torch, kappa, ustar, u_o, g_o = c5
+    _, _, u, g = _c5_gradient(torch, precision, kappa, ustar)
+    eu, eg = _rel(u, u_o), _rel(g, g_o)
+    print(f"C5 precision {precision}: solution error {eu:.2e}, gradient error {eg:.2e} vs oracle")
+    assert eu <= TOL[precision]
+    assert eg <= TOL[precision]
+
+
+def test_c5_gradient_64cube_finite_differences(built_lib, c5):
+    """Central differences of J along 32 seeded directions d (kappa scaled by
+    exp(+-1e-6 d)) against the adjoint gradient g . (kappa * d).  The solves
+    are plain FP64 to relres 1e-12: a difference quotient with step 1e-6
+    amplifies each solve's own error by 1e6, and the mixed path's FP32
+    preconditioner changes its iterates (not its limit) from one kappa to the
+    next, which leaves about 1e-4 of noise in the quotient (measured); the
+    mixed gradient itself is checked against the oracle above."""
+    torch, kappa, ustar, _, _ = c5
+    op, us, _, g = _c5_gradient(torch, 0, kappa, ustar)
+    rng = np.random.default_rng(11)
+    eps = 1e-6
+    kt = torch.tensor(kappa, dtype=torch.float64, device="cuda")
+    worst = 0.0
+    try:
+        with torch.no_grad():
+            for _ in range(32):
+                d = rng.standard_normal(kappa.size)
+                dt = torch.tensor(d, dtype=torch.float64, device="cuda")
+                jp = 0.5 * torch.sum((op.solve(kt * torch.exp(eps * dt)) - us) ** 2).item()
+                jm = 0.5 * torch.sum((op.solve(kt * torch.exp(-eps * dt)) - us) ** 2).item()
+                fd = (jp - jm) / (2 * eps)
+                an = float(np.dot(g, kappa * d))
+                worst = max(worst, abs(fd - an) / max(abs(fd), abs(an)))
+    finally:
+        import bddcml_gb300 as B
+        B.bddcml_finalize()
+    print(f"C5 finite differences: worst relative difference over 32 directions {worst:.2e}")
+    assert worst <= 1e-5

@@ -151,7 +151,7 @@ def test_oracle_adjoint_gradient_matches_finite_differences(oracle_mod):
     """The differentiation formula dJ/dkappa_e = -lambda_e^T K_e^0 u_e with the
     adjoint solve, against central differences of J = 1/2 |u - u*|^2."""
     from bddcml_gb300 import problems
-    from gradient_util import objective, oracle_gradient, oracle_solution
+    from oracle_gradient import objective, oracle_gradient, oracle_solution
     ne, ns = 3, 2
     n = ne * ns
     kappa = problems.lognormal_kappa(n, 1.0, seed=3)
@@ -161,8 +161,10 @@ def test_oracle_adjoint_gradient_matches_finite_differences(oracle_mod):
     eps = 1e-6
     for _ in range(4):
         d = rng.standard_normal(kappa.size)
-        jp = objective(oracle_solution(oracle_mod, problems.poisson_on_cube(ne, ns, kappa=kappa * np.exp(eps * d))), ustar)
-        jm = objective(oracle_solution(oracle_mod, problems.poisson_on_cube(ne, ns, kappa=kappa * np.exp(-eps * d))), ustar)
+        jp = objective(oracle_solution(oracle_mod, problems.poisson_on_cube(ne, ns, kappa=kappa * np.exp(eps * d)))[0],
+                       ustar)
+        jm = objective(oracle_solution(oracle_mod, problems.poisson_on_cube(ne, ns, kappa=kappa * np.exp(-eps * d)))[0],
+                       ustar)
         fd = (jp - jm) / (2 * eps)           # directional derivative along kappa * d
         an = float(np.dot(grad, kappa * d))
         assert abs(fd - an) <= 1e-6 * max(abs(fd), abs(an)), (fd, an)

@@ -45,3 +45,16 @@ def test_replica_timings_take_the_maximum_over_ranks(tmp_path):
 def test_replica_max_on_one_rank_is_identity():
     import bench
     assert bench.replica_max([0.25, 3]) == [0.25, 3.0]
+
+
+def test_rank_keeps_the_launchers_gpu_list():
+    """A rank takes the LOCAL_RANK-th GPU of a CUDA_VISIBLE_DEVICES list the
+    launcher set, and the bare local rank only when no list was set."""
+    import bench
+    assert bench.visible_device_for_rank(1, "4,5") == "5"
+    assert bench.visible_device_for_rank(0, " 4, 5") == "4"
+    assert bench.visible_device_for_rank(1, "GPU-aa,GPU-bb") == "GPU-bb"
+    assert bench.visible_device_for_rank(1, None) == "1"
+    assert bench.visible_device_for_rank(1, "") == "1"
+    with pytest.raises(ValueError):
+        bench.visible_device_for_rank(2, "4,5")

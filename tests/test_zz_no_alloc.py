@@ -33,6 +33,15 @@ def test_dotprod_dev_matches_host_entry_point(built_lib):
                 got = B.dotprod_subdomain_dev(isub, d1.data_ptr(), d2.data_ptr(), n)
                 scale = float(np.dot(np.abs(v1), np.abs(v2)))
                 assert abs(got - ref) <= 1e-12 * scale, (isub, got, ref)
+        # after the first call (which loads the static scratch on the device),
+        # further calls leave the free device memory unchanged
+        torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info()[0]
+        last = prob.nsub - 1  # d1 and d2 hold vectors of this subdomain
+        for _ in range(5):
+            B.dotprod_subdomain_dev(last, d1.data_ptr(), d2.data_ptr(), prob.subdomains[last].ndofs)
+        torch.cuda.synchronize()
+        assert torch.cuda.mem_get_info()[0] == free0
         with pytest.raises(B.BddcmlError):
             B.dotprod_subdomain_dev(0, d1.data_ptr(), d2.data_ptr(), prob.subdomains[0].ndofs + 1)
     finally:
