@@ -778,12 +778,13 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
   if constexpr (std::is_same_v<T, float>) run_solve_tc(D, td_oo, nsub, D.maxnbo, D.maxNR, ppool, poolT);
   else run_solve<T>(D, D.bd_oo, nsub, D.maxnbo, D.maxNR, poolT, poolT, D.bdu_oo);
   D.prof.end(PH_SOLVE_OO, st);
-  // Mixed precision: two refinement steps with FP64-accurate residuals.
-  //   R0 = [A_oi | f_o] - A_oo X0 -> component 1, D1 = A_oo^-1 R0 in place (3xTF32)
-  //   R1 = [A_oi | f_o] - A_oo (X0 + D1) -> component 2, D2 = A_oo^-1 R1 in place
-  //        with one TF32 pass (D2 is ~1e-10 of X, so its ~1e-3 relative error
-  //        stays far below the FP32 pair's resolution), added into D1 by the
-  //        backward sweep.
+  // Mixed precision: two refinement steps.
+  //   R0 = [A_oi | f_o] - A_oo X0, FP64-accurate (double-float) -> components 1
+  //        and 2, D1 = A_oo^-1 R0 in place in component 1 (3xTF32)
+  //   R1 = R0 - A_oo D1 in FP32 (R1 ~ 1e-5 R0, so FP32 rounding leaves it
+  //        within ~1 %) -> component 2, D2 = A_oo^-1 R1 in place with one TF32
+  //        pass (D2 is ~1e-10 of X, so its ~1 % error stays far below the FP32
+  //        pair's resolution), added into D1 by the backward sweep.
   // X is then the unnormalised FP32 pair (X0, D1 + D2) in components 0 and 1.
   int* dmax = nullptr;
   if (D.prof.on && D.mixed) {
@@ -795,8 +796,13 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
   if constexpr (std::is_same_v<T, float>) {
     for (int rr = 1; rr <= D.nref; ++rr) {
       D.prof.begin(PH_RESIDUAL, st);
-      k_residual_df<<<dim3((D.maxNO + RES_ROWS - 1) / RES_ROWS, nsub), 128, 0, st>>>(
-          D.ds, D.koo, D.koi, D.fo, D.fo_off, poolT, rr > 1 ? 1 : 0, rr);
+      if (rr == 1) {  // R0, kept in component 2 as well for the second residual
+        k_residual_df<<<dim3((D.maxNO + RES_ROWS - 1) / RES_ROWS, nsub), 128, 0, st>>>(
+            D.ds, D.koo, D.koi, D.fo, D.fo_off, poolT, 0, 1, D.nref >= 2 ? 2 : -1);
+      } else {        // R1 = R0 - A_oo D1 (FP32 suffices for the one-pass correction)
+        k_residual_update_f32<<<dim3((D.maxNO + RES_ROWS - 1) / RES_ROWS, nsub), 128, 0, st>>>(D.ds, D.koo,
+                                                                                              poolT, 1, 2);
+      }
       CKL();
       D.prof.end(PH_RESIDUAL, st);
       D.prof.begin(PH_SOLVE_OO, st);

@@ -15,7 +15,7 @@ namespace bddc {
 
 constexpr int NB = 64;      // tile edge
 constexpr int NT = 256;     // threads of the tile kernels (16 x 16, 4 x 4 outputs each)
-constexpr int KC = 16;      // K chunk of the SIMT tile product
+constexpr int KC = 32;      // K chunk of the SIMT tile product
 constexpr int KCS = NB + 4;  // row stride of a staged K chunk (spreads the transposing stores over banks)
 constexpr int SM_TILE = KC * KCS;  // elements of one staged operand chunk
 
@@ -50,24 +50,42 @@ __device__ __forceinline__ void load4(double (&v)[4], const double* p) {
 // --------------------------------------------------------------- SIMT tile
 // acc(4x4 per thread) += op(A) * op(B) over K (multiple of KC), 64 x 64 output.
 // A: !TA -> A[r*lda + k], TA -> A[k*lda + r];  B: !TB -> B[k*ldb + c], TB -> B[c*ldb + k]
+// The next K chunk is loaded into registers while the current one is used,
+// so only the first chunk's global-memory latency is exposed.
 template <typename T, bool TA, bool TB>
 __device__ __forceinline__ void tile_gemm(T (&acc)[4][4], const T* __restrict__ A, int lda,
                                           const T* __restrict__ B, int ldb, int K, T* smA, T* smB) {
+  constexpr int PER = KC * NB / NT;  // elements of each operand per thread and chunk
   const int tid = threadIdx.x;
   const int tx = tid & 15, ty = tid >> 4;
-  for (int k0 = 0; k0 < K; k0 += KC) {
-    // stage A chunk as smA[k][r], B chunk as smB[k][c]  (KC x 64 each)
-    for (int e = tid; e < KC * NB; e += NT) {
+  T ra[PER], rb[PER];
+  auto fetch = [&](int k0) {
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+      const int e = tid + i * NT;
       int r, k;
       if (!TA) { k = e % KC; r = e / KC; } else { r = e % NB; k = e / NB; }
-      T v = TA ? A[(long long)(k0 + k) * lda + r] : A[(long long)r * lda + k0 + k];
-      smA[k * KCS + r] = v;
+      ra[i] = TA ? A[(long long)(k0 + k) * lda + r] : A[(long long)r * lda + k0 + k];
       int c, kk;
       if (!TB) { c = e % NB; kk = e / NB; } else { kk = e % KC; c = e / KC; }
-      T u = TB ? B[(long long)c * ldb + k0 + kk] : B[(long long)(k0 + kk) * ldb + c];
-      smB[kk * KCS + c] = u;
+      rb[i] = TB ? B[(long long)c * ldb + k0 + kk] : B[(long long)(k0 + kk) * ldb + c];
+    }
+  };
+  fetch(0);
+  for (int k0 = 0; k0 < K; k0 += KC) {
+    // stage the chunk as smA[k][r], smB[k][c]  (KC x 64 each)
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+      const int e = tid + i * NT;
+      int r, k;
+      if (!TA) { k = e % KC; r = e / KC; } else { r = e % NB; k = e / NB; }
+      smA[k * KCS + r] = ra[i];
+      int c, kk;
+      if (!TB) { c = e % NB; kk = e / NB; } else { kk = e % KC; c = e / KC; }
+      smB[kk * KCS + c] = rb[i];
     }
     __syncthreads();
+    if (k0 + KC < K) fetch(k0 + KC);
 #pragma unroll
     for (int k = 0; k < KC; ++k) {
       T a[4], b[4];

@@ -10,7 +10,7 @@
    cases, used as regression pins of the oracle (the reference ships no
    solver goldens and cannot be built here).
 
-Usage: python tests/golden/make_fixtures.py [path-to-reference]
+Usage: python tests/golden/make_fixtures.py <path-to-reference-checkout>
 """
 import json
 import os
@@ -60,9 +60,9 @@ def oracle_cases():
 
 
 if __name__ == "__main__":
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    if os.path.isdir(ref):
-        with open(os.path.join(HERE, "reference_utils_known_answers.json"), "w") as f:
-            json.dump(parse_reference_utils(ref), f, indent=1)
+    if len(sys.argv) != 2 or not os.path.isdir(sys.argv[1]):
+        sys.exit("usage: make_fixtures.py <checkout of the reference sources>")
+    with open(os.path.join(HERE, "reference_utils_known_answers.json"), "w") as f:
+        json.dump(parse_reference_utils(sys.argv[1]), f, indent=1)
     with open(os.path.join(HERE, "oracle_small.json"), "w") as f:
         json.dump(oracle_cases(), f, indent=1)
