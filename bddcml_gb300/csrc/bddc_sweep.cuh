@@ -14,13 +14,14 @@
 // which is one TMEM lane, and writes the TF32 hi and lo parts of its column
 // there (tcgen05.st), so the MMAs read only the 64-row panel (the B operand,
 // 16 KB per 32-wide K chunk, moved by cp.async.bulk) from shared memory.
-// Block row k - 1, on which every step depends, never goes through global
-// memory on the critical path: the epilogue threads read it from the TMEM
+// The two freshest window blocks never go through global memory on the
+// critical path: the epilogue threads read a finished block row from the TMEM
 // accumulator, store it as the result and split it straight into the stages
-// of the next step's last two chunks.  The other window blocks (older solved
-// blocks and the right-hand-side block) do not depend on the previous step,
-// so the staging threads load them from global memory ahead of time and the
-// tensor core works on them while the epilogue of the previous step runs.
+// of the two following steps that read it.  The other window blocks (older
+// solved blocks and the right-hand-side block) do not depend on the previous
+// steps, so the staging threads load them from global memory ahead of time,
+// and the issue order (below) lets the tensor core work on them while the
+// epilogue of the previous step runs.
 //
 // Roles (320 threads, one CTA per SM):
 //   warps 0-3 and 4-7: two staging groups (each one thread per TMEM lane);
@@ -28,7 +29,7 @@
 //       results of block jb (the epilogue), so a thread only ever reads back
 //       rows of its own column that it wrote itself;
 //   warp 8 (one thread): panel chunks into a ring of shared-memory slots;
-//   warp 9 (one thread): the MMAs, into one of two TMEM accumulators.
+//   warp 9 (one thread): the MMAs, into one of three TMEM accumulators.
 // Precision: 3xTF32 (a_lo p_hi + a_hi p_lo + a_hi p_hi, FP32 accumulation),
 // or one TF32 product for a correction that is itself tiny (PASSES = 1).
 //
@@ -43,12 +44,13 @@
 
 namespace bddc {
 
-constexpr int SWT_AST = 6;                       // TMEM stages of split window chunks
+constexpr int SWT_AST = 5;                       // TMEM stages of split window chunks
+constexpr int SWT_NACC = 3;                      // TMEM accumulators (steps t, t + 1, t + 2)
 constexpr int SWT_PST = 6;                       // shared-memory slots of panel chunks
 constexpr int SWT_GROUP = 128;                   // threads of one staging group
 constexpr int SWT_PRODUCER = 8, SWT_ISSUER = 9;  // warps
 constexpr int SWT_THREADS = 320;
-constexpr uint32_t SWT_ACOL = 2 * TC_N;  // TMEM column of stage 0, after the two accumulators
+constexpr uint32_t SWT_ACOL = SWT_NACC * TC_N;  // TMEM column of stage 0, after the accumulators
 constexpr uint32_t SWT_TCOLS = 512;
 static_assert(SWT_ACOL + SWT_AST * 2 * TC_KC <= SWT_TCOLS, "tensor memory columns");
 constexpr size_t swt_smem_bytes() { return (size_t)SWT_PST * TC_PCHUNK * sizeof(float) + 128; }
@@ -67,11 +69,13 @@ __device__ __forceinline__ bool swt_wait(uint64_t* bar, uint32_t parity, long lo
   return false;
 }
 
-// Window of block row k: forward blocks jlo .. k, backward k .. k + nblk - 1;
-// the panel index of block jb is jb - j0.  Forward sweeps of identity columns
-// start at row s0 and skip the zero blocks above it.
+// Window of sweep step t (block row k): the blocks of "age" a = 0 .. nblk - 1,
+// age 0 being block k itself (the right-hand side) and age a the block solved
+// a steps earlier (forward k - a, backward k + a); the panel holds block jb at
+// position jb - j0.  Forward sweeps of identity columns start at row s0 and
+// skip the zero blocks above it.
 struct SwWin {
-  int k, j0, jlo, nblk;
+  int k, j0, nblk;
 };
 
 __device__ __forceinline__ SwWin sw_win(int dir, int nb, int w, int s0, int k) {
@@ -79,34 +83,36 @@ __device__ __forceinline__ SwWin sw_win(int dir, int nb, int w, int s0, int k) {
   r.k = k;
   if (dir == 0) {
     r.j0 = k - min(k, w);
-    r.jlo = max(r.j0, s0);
-    r.nblk = k - r.jlo + 1;
+    r.nblk = k - max(r.j0, s0) + 1;
   } else {
     r.j0 = k;
-    r.jlo = k;
     r.nblk = min(w, nb - 1 - k) + 1;
   }
   return r;
 }
 
-// chunk q of the window (two 32-row halves per block): the older solved
-// blocks first, then the right-hand-side block k, then the freshest block
-// (k - 1 forward, k + 1 backward), the only one that depends on the previous step
-__device__ __forceinline__ void sw_chunk(int dir, const SwWin& W, int q, int& jb, int& pq, bool& dep) {
-  const int p = q >> 1;
-  dep = false;
-  if (W.nblk == 1) {
-    jb = W.k;
-  } else if (p == W.nblk - 1) {
-    jb = dir == 0 ? W.k - 1 : W.k + 1;
-    dep = true;
-  } else if (p == W.nblk - 2) {
-    jb = W.k;
-  } else {
-    jb = dir == 0 ? W.jlo + p : W.k + 2 + p;
-  }
-  pq = 2 * (jb - W.j0) + (q & 1);
+// Issue order.  The chunks of step t (two 32-row halves per window block) fall
+// into three parts: A(t) = the blocks of age >= 3 and the right-hand side
+// (read from global memory), B(t) = the block of age 2 and C(t) = the block
+// of age 1 (both handed over by the epilogue of the step that made them).
+// "Macro step" t issues A(t), C(t - 1), B(t), so the MMAs of A(t) and B(t)
+// run while the epilogue of step t - 1 (which needs C(t - 1) complete) moves
+// that step's results out; the epilogue of step t - 2 supplies C(t - 1) and
+// B(t), which are adjacent in the order.  Steps use accumulators t mod 3.
+__device__ __forceinline__ int sw_nA(const SwWin& W) { return 2 * (1 + max(0, W.nblk - 3)); }
+__device__ __forceinline__ int sw_nB(const SwWin& W) { return W.nblk >= 3 ? 2 : 0; }
+__device__ __forceinline__ int sw_nC(const SwWin& W) { return W.nblk >= 2 ? 2 : 0; }
+
+// block of age a
+__device__ __forceinline__ int sw_block(int dir, const SwWin& W, int a) { return dir == 0 ? W.k - a : W.k + a; }
+
+// chunk q of part A: the oldest blocks first, the right-hand side last
+__device__ __forceinline__ int sw_A_block(int dir, const SwWin& W, int q) {
+  const int p = q >> 1, nold = max(0, W.nblk - 3);
+  return sw_block(dir, W, p < nold ? W.nblk - 1 - p : 0);
 }
+
+__device__ __forceinline__ int sw_pq(const SwWin& W, int jb, int half) { return 2 * (jb - W.j0) + half; }
 
 template <int PASSES, bool ACC>
 __global__ void __launch_bounds__(SWT_THREADS, 1)
@@ -123,14 +129,15 @@ __global__ void __launch_bounds__(SWT_THREADS, 1)
   // count) starts at the tile's diagonal block row: the rows above stay zero
   const int s0 = (dir == 0 && c0 + TC_M <= d.pad) ? c0 / NB : 0;
   const int nsteps = d.nb - s0;
-  auto row_of = [&](int sidx) { return dir == 0 ? s0 + sidx : d.nb - 1 - sidx; };
+  auto row_of = [&](int t) { return dir == 0 ? s0 + t : d.nb - 1 - t; };
+  auto win = [&](int t) { return sw_win(dir, d.nb, d.w, s0, row_of(t)); };
   const long long limit = g_tc_wait_limit;
 
   extern __shared__ __align__(128) unsigned char swt_raw[];
   float* sP = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(swt_raw) + 127) & ~uintptr_t(127));
   __shared__ __align__(8) uint64_t bar_afull[SWT_AST], bar_aempty[SWT_AST];
   __shared__ __align__(8) uint64_t bar_pfull[SWT_PST], bar_pfree[SWT_PST];
-  __shared__ __align__(8) uint64_t bar_accfull[2], bar_tfree[2];
+  __shared__ __align__(8) uint64_t bar_accfull[SWT_NACC], bar_tfree[SWT_NACC];
   __shared__ uint32_t tmem_base;
   __shared__ volatile int abort_flag;
   __shared__ long long last_pload[SWT_PST], last_mma;
@@ -146,7 +153,7 @@ __global__ void __launch_bounds__(SWT_THREADS, 1)
       mbar_init(&bar_pfree[s], 1);
       last_pload[s] = -1;
     }
-    for (int b = 0; b < 2; ++b) {
+    for (int b = 0; b < SWT_NACC; ++b) {
       mbar_init(&bar_accfull[b], 1);
       mbar_init(&bar_tfree[b], SWT_GROUP);
     }
@@ -164,62 +171,39 @@ __global__ void __launch_bounds__(SWT_THREADS, 1)
   tc_fence_after();
   const uint32_t tmem = tmem_base;
 
-  if (warp == SWT_PRODUCER) {
-    // ------------------------------------------------ panel chunks (one thread)
+  if (warp == SWT_PRODUCER || warp == SWT_ISSUER) {
     if (lane == 0) {
-      long long g = 0;
-      bool ok = true;
-      for (int sidx = 0; sidx < nsteps && ok; ++sidx) {
-        const SwWin W = sw_win(dir, d.nb, d.w, s0, row_of(sidx));
-        for (int q = 0; q < 2 * W.nblk; ++q, ++g) {
-          const int s = (int)(g % SWT_PST);
-          const long long use = g / SWT_PST;
-          if (abort_flag || (use > 0 && !swt_wait(&bar_pfree[s], (uint32_t)((use - 1) & 1), limit, &abort_flag))) {
-            abort_flag = 1;
-            ok = false;
-            break;
-          }
-          int jb, pq;
-          bool dep;
-          sw_chunk(dir, W, q, jb, pq, dep);
-          mbar_expect_tx(&bar_pfull[s], pbytes);
-          bulk_g2s(sP + s * TC_PCHUNK, P + panel_chunk(0, d.w, W.k, pq), pbytes, &bar_pfull[s]);
-          last_pload[s] = g;
-        }
-      }
-    }
-  } else if (warp == SWT_ISSUER) {
-    // ------------------------------------------------ MMA issuer (one thread)
-    if (lane == 0) {
+      const bool producer = warp == SWT_PRODUCER;
       constexpr uint32_t idesc = tc_idesc(TC_M, TC_N);
       long long g = 0;
       bool ok = true;
-      for (int sidx = 0; sidx < nsteps && ok; ++sidx) {
-        const int b = sidx & 1;
-        if (abort_flag ||
-            (sidx >= 2 && !swt_wait(&bar_tfree[b], (uint32_t)(((sidx - 2) >> 1) & 1), limit, &abort_flag))) {
-          abort_flag = 1;
-          break;
-        }
-        tc_fence_after();
-        const uint32_t dacc = tmem + (uint32_t)(b * TC_N);
-        const SwWin W = sw_win(dir, d.nb, d.w, s0, row_of(sidx));
-        const int nch = 2 * W.nblk;
-        for (int q = 0; q < nch; ++q, ++g) {
+      // one chunk of step t: panel chunk pq; first / last chunk of the step
+      auto chunk = [&](int t, int pq, bool first, bool last) -> bool {
+        if (producer) {
+          const int s = (int)(g % SWT_PST);
+          const long long use = g / SWT_PST;
+          if (abort_flag || (use > 0 && !swt_wait(&bar_pfree[s], (uint32_t)((use - 1) & 1), limit, &abort_flag)))
+            return false;
+          mbar_expect_tx(&bar_pfull[s], pbytes);
+          bulk_g2s(sP + s * TC_PCHUNK, P + panel_chunk(0, d.w, row_of(t), pq), pbytes, &bar_pfull[s]);
+          last_pload[s] = g;
+        } else {
+          const int b = t % SWT_NACC;
+          if (first && t >= SWT_NACC &&
+              !swt_wait(&bar_tfree[b], (uint32_t)(((t - SWT_NACC) / SWT_NACC) & 1), limit, &abort_flag))
+            return false;
           const int sa = (int)(g % SWT_AST), sp = (int)(g % SWT_PST);
           if (!swt_wait(&bar_afull[sa], (uint32_t)((g / SWT_AST) & 1), limit, &abort_flag) ||
-              !swt_wait(&bar_pfull[sp], (uint32_t)((g / SWT_PST) & 1), limit, &abort_flag)) {
-            abort_flag = 1;
-            ok = false;
-            break;
-          }
+              !swt_wait(&bar_pfull[sp], (uint32_t)((g / SWT_PST) & 1), limit, &abort_flag))
+            return false;
           tc_fence_after();
+          const uint32_t dacc = tmem + (uint32_t)(b * TC_N);
           const uint32_t a_hi = tmem + SWT_ACOL + (uint32_t)(sa * 2 * TC_KC), a_lo = a_hi + TC_KC;
           const uint32_t p_hi = smem_u32(sP + sp * TC_PCHUNK), p_lo = p_hi + TC_N * TC_KC * 4;
 #pragma unroll
           for (int kk = 0; kk < TC_KC / 8; ++kk) {
             const uint32_t koff = kk * 2 * TC_LBO;
-            const uint32_t acc = (q > 0 || kk > 0) ? 1u : 0u;
+            const uint32_t acc = (!first || kk > 0) ? 1u : 0u;
             if (PASSES == 1) {
               mma_tf32_ta(dacc, a_hi + kk * 8, tc_desc(p_hi + koff), idesc, acc);
             } else {
@@ -230,14 +214,35 @@ __global__ void __launch_bounds__(SWT_THREADS, 1)
           }
           mma_commit(&bar_aempty[sa]);
           mma_commit(&bar_pfree[sp]);
-          if (q == nch - 1) mma_commit(&bar_accfull[b]);
+          if (last) mma_commit(&bar_accfull[b]);
           last_mma = g;
         }
+        ++g;
+        return true;
+      };
+      for (int t = 0; t <= nsteps && ok; ++t) {
+        if (t < nsteps) {  // A(t)
+          const SwWin W = win(t);
+          const int n = sw_nA(W);
+          for (int q = 0; q < n && ok; ++q)
+            ok = chunk(t, sw_pq(W, sw_A_block(dir, W, q), q & 1), q == 0, W.nblk == 1 && q == n - 1);
+        }
+        if (t >= 1 && ok) {  // C(t - 1): the last chunks of step t - 1
+          const SwWin W = win(t - 1);
+          const int jb = sw_block(dir, W, 1);
+          for (int q = 0; q < sw_nC(W) && ok; ++q) ok = chunk(t - 1, sw_pq(W, jb, q), false, q == 1);
+        }
+        if (t < nsteps && ok) {  // B(t)
+          const SwWin W = win(t);
+          const int jb = sw_block(dir, W, 2);
+          for (int q = 0; q < sw_nB(W) && ok; ++q) ok = chunk(t, sw_pq(W, jb, q), false, false);
+        }
       }
+      if (!ok) abort_flag = 1;
     }
   } else {
     // ------------------------------------------------ staging groups and epilogue
-    const int G = warp >> 2;              // stages the chunks of the window blocks jb with (jb & 1) == G
+    const int G = warp >> 2;              // owns the window blocks jb with (jb & 1) == G
     const int r = tid & (SWT_GROUP - 1);  // column of the tile = TMEM lane
     const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
     float* col = B + c0 + r;
@@ -252,25 +257,27 @@ __global__ void __launch_bounds__(SWT_THREADS, 1)
       good = __all_sync(0xffffffffu, good);  // the TMEM stores below are warp-collective
       if (!good) return false;
       tc_fence_after();
-      float h[TC_KC], l[TC_KC];
-#pragma unroll
-      for (int t = 0; t < TC_KC; ++t) {
-        h[t] = tf32_rna(v[t]);
-        l[t] = tf32_rna(v[t] - h[t]);
-      }
       const uint32_t ta = tmem + lane_base + SWT_ACOL + (uint32_t)(sa * 2 * TC_KC);
+      float h[TC_KC];
+#pragma unroll
+      for (int i = 0; i < TC_KC; ++i) h[i] = tf32_rna(v[i]);
       tmem_st32(ta, h);
-      if (PASSES != 1) tmem_st32(ta + TC_KC, l);
+      if (PASSES != 1) {
+#pragma unroll
+        for (int i = 0; i < TC_KC; ++i) h[i] = tf32_rna(v[i] - tf32_rna(v[i]));
+        tmem_st32(ta + TC_KC, h);
+      }
       tmem_st_wait();
       tc_fence_before();
       mbar_arrive(&bar_afull[sa]);
       return true;
     };
-    // results of step se (block row k) from its accumulator to B; with gdep >= 0
-    // the two halves also become chunks gdep and gdep + 1 of the next step
-    auto epilogue = [&](int se, long long gdep) -> bool {
-      const int k = row_of(se), b = se & 1;
-      bool good = !abort_flag && swt_wait(&bar_accfull[b], (uint32_t)((se >> 1) & 1), limit, &abort_flag);
+    // results of step e (block row k) from its accumulator to B; each half
+    // also fills chunk gC + h of part C(e + 1) and chunk gB + h of part B(e + 2)
+    // when those are >= 0
+    auto epilogue = [&](int e, long long gC, long long gB) -> bool {
+      const int k = row_of(e), b = e % SWT_NACC;
+      bool good = !abort_flag && swt_wait(&bar_accfull[b], (uint32_t)((e / SWT_NACC) & 1), limit, &abort_flag);
       good = __all_sync(0xffffffffu, good);  // the TMEM loads below are warp-collective
       if (!good) return false;
       tc_fence_after();
@@ -291,6 +298,10 @@ __global__ void __launch_bounds__(SWT_THREADS, 1)
             v[16 + i] = v1[i];
           }
         }
+        if (h == 1) {  // both halves are in registers: the accumulator may take step e + 3
+          tc_fence_before();
+          mbar_arrive(&bar_tfree[b]);
+        }
         float* dst = col + (long long)(k * NB + h * TC_KC) * lds;
 #pragma unroll
         for (int i = 0; i < TC_KC; ++i) dst[(long long)i * lds] = v[i];
@@ -302,93 +313,95 @@ __global__ void __launch_bounds__(SWT_THREADS, 1)
 #pragma unroll
           for (int i = 0; i < TC_KC; ++i) dst2[(long long)i * lds] = a[i] + v[i];
         }
-        if (gdep >= 0 && !fill(gdep + h, v)) return false;
+        if (gC >= 0 && !fill(gC + h, v)) return false;
+        if (gB >= 0 && !fill(gB + h, v)) return false;
       }
-      tc_fence_before();
-      mbar_arrive(&bar_tfree[b]);  // the accumulator may take step se + 2
       return true;
     };
     auto load = [&](int jb, int half, float (&v)[TC_KC]) {
       const float* src = col + (long long)(jb * NB + half * TC_KC) * ld;
 #pragma unroll
-      for (int t = 0; t < TC_KC; ++t) v[t] = src[(long long)t * ld];
+      for (int i = 0; i < TC_KC; ++i) v[i] = src[(long long)i * ld];
     };
-    // this group's next chunk after chunk q of step sidx (sequence number g):
-    // its step ns (-1: none), block, half, sequence number and dependency flag
-    auto next_owned = [&](int sidx, int q, long long g, int& ns, long long& ng, int& njb, int& nhalf, bool& ndep) {
-      ns = sidx;
-      int nq = q + 1;
+    // The next chunk of this group after position (t, part A, chunk q): true
+    // with its block, half and sequence number when it is a chunk of part A
+    // (read from global memory); false when the group's next event is an
+    // epilogue (whose chunks it makes itself) or the sequence ends.  Every
+    // block that a part-A chunk reads was written by this group's own
+    // epilogue earlier in the order, so a prefetch never reads stale rows.
+    auto next_load = [&](int t, int q, long long g, int& njb, int& nhalf, long long& ng) -> bool {
       ng = g + 1;
-      while (ns < nsteps) {
-        const SwWin W = sw_win(dir, d.nb, d.w, s0, row_of(ns));
-        for (; nq < 2 * W.nblk; ++nq, ++ng) {
-          int pq;
-          sw_chunk(dir, W, nq, njb, pq, ndep);
-          if ((njb & 1) == G) {
-            nhalf = nq & 1;
-            return;
+      int qq = q + 1;
+      for (int tt = t; tt < nsteps; ++tt) {
+        const SwWin W = win(tt);
+        for (; qq < sw_nA(W); ++qq, ++ng) {
+          const int jb = sw_A_block(dir, W, qq);
+          if ((jb & 1) == G) {
+            njb = jb;
+            nhalf = qq & 1;
+            return true;
           }
         }
-        ++ns;
-        nq = 0;
+        // then part C(tt - 1), where the epilogue of step tt - 2 runs, and part B(tt)
+        if (tt >= 2 && (row_of(tt - 2) & 1) == G) return false;
+        if (tt >= 1) ng += sw_nC(win(tt - 1));
+        ng += sw_nB(W);
+        qq = 0;
       }
-      ns = -1;
+      return false;
     };
 
     float vn[TC_KC];
     long long gn = -1;  // sequence number of the chunk held in vn
     long long g = 0;
     bool ok = true;
-    for (int sidx = 0; sidx < nsteps && ok; ++sidx) {
-      const SwWin W = sw_win(dir, d.nb, d.w, s0, row_of(sidx));
-      const int nch = 2 * W.nblk;
-      // a window of one block (a block-diagonal band) does not read the previous
-      // step's results: they are written out here instead
-      if (sidx > 0 && W.nblk == 1 && (row_of(sidx - 1) & 1) == G && !epilogue(sidx - 1, -1)) {
-        ok = false;
-        break;
-      }
-      for (int q = 0; q < nch; ++q, ++g) {
-        int jb, pq;
-        bool dep;
-        sw_chunk(dir, W, q, jb, pq, dep);
-        if ((jb & 1) != G) continue;
-        if (dep) {  // both halves of the freshest block come from the previous step's epilogue
-          if (!epilogue(sidx - 1, g)) {
+    for (int t = 0; t <= nsteps && ok; ++t) {
+      if (t < nsteps) {  // A(t)
+        const SwWin W = win(t);
+        const int n = sw_nA(W);
+        for (int q = 0; q < n; ++q, ++g) {
+          const int jb = sw_A_block(dir, W, q);
+          if ((jb & 1) != G) continue;
+          float v[TC_KC];
+          if (gn == g) {
+#pragma unroll
+            for (int i = 0; i < TC_KC; ++i) v[i] = vn[i];
+          } else {
+            load(jb, q & 1, v);
+          }
+          {
+            int njb, nhalf;
+            long long ng;
+            gn = -1;
+            if (next_load(t, q, g, njb, nhalf, ng)) {
+              load(njb, nhalf, vn);
+              gn = ng;
+            }
+          }
+          if (!fill(g, v)) {
             ok = false;
             break;
           }
-          ++q;
-          ++g;
-          continue;
         }
-        float v[TC_KC];
-        if (gn == g) {
-#pragma unroll
-          for (int t = 0; t < TC_KC; ++t) v[t] = vn[t];
-        } else {
-          load(jb, q & 1, v);
-        }
-        // prefetch this group's next chunk unless it is a freshest block (made by the epilogue)
-        {
-          int ns, njb, nhalf;
-          long long ng;
-          bool ndep;
-          next_owned(sidx, q, g, ns, ng, njb, nhalf, ndep);
-          gn = -1;
-          if (ns >= 0 && !ndep) {
-            load(njb, nhalf, vn);
-            gn = ng;
-          }
-        }
-        if (!fill(g, v)) {
-          ok = false;
-          break;
-        }
+        if (!ok) break;
       }
+      long long gC = -1, gB = -1;
+      int nC = 0;
+      if (t >= 1) {  // C(t - 1)
+        nC = sw_nC(win(t - 1));
+        if (nC) gC = g;
+        g += nC;
+      }
+      if (t < nsteps) {  // B(t)
+        const int nB = sw_nB(win(t));
+        if (nB) gB = g;
+        g += nB;
+      }
+      // the epilogue of step t - 2 supplies C(t - 1) and B(t)
+      if (t >= 2 && (row_of(t - 2) & 1) == G && !epilogue(t - 2, gC, gB)) ok = false;
     }
-    // the last block row has no following step: the group that owns it writes it
-    if (ok && (row_of(nsteps - 1) & 1) == G && !epilogue(nsteps - 1, -1)) ok = false;
+    // the last step's results: written by the group that owns its block row
+    if (ok && nsteps >= 1 && (row_of(nsteps - 1) & 1) == G && !epilogue(nsteps - 1, -1, -1)) ok = false;
     if (!ok) abort_flag = 1;
   }
   // wind-down: after an abort, wait (bounded) for the copies and MMAs in flight before freeing TMEM
