@@ -29,7 +29,12 @@
 //       results of block jb (the epilogue), so a thread only ever reads back
 //       rows of its own column that it wrote itself;
 //   warp 8 (one thread): panel chunks into a ring of shared-memory slots;
-//   warp 9 (one thread): the MMAs, into one of three TMEM accumulators.
+//   warp 9, lane 0: the MMAs, into one of three TMEM accumulators;
+//   warp 9, lane 1: follows the MMA completions chunk by chunk (one phase of
+//       one stage barrier at a time) and publishes their count, which the
+//       staging threads wait on before they refill a stage.  The epilogue
+//       fills stages out of chunk order, and a parity wait on a barrier that
+//       is two phases behind would pass early; a count cannot.
 // Precision: 3xTF32 (a_lo p_hi + a_hi p_lo + a_hi p_hi, FP32 accumulation),
 // or one TF32 product for a correction that is itself tiny (PASSES = 1).
 //
@@ -58,6 +63,16 @@ constexpr size_t swt_smem_bytes() { return (size_t)SWT_PST * TC_PCHUNK * sizeof(
 // Spin limit of the sweeps' waits (the wind-down waits use TC_SPIN_LIMIT).
 // Settable for tests of the timeout path (bddcml_set_wait_limit_c).
 static __device__ long long g_tc_wait_limit = TC_SPIN_LIMIT;
+
+// release store / acquire load of a shared-memory counter
+__device__ __forceinline__ void smem_store_release(unsigned* p, unsigned v) {
+  asm volatile("st.release.cta.shared::cta.u32 [%0], %1;" ::"r"(smem_u32(p)), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned smem_load_acquire(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.cta.shared::cta.u32 %0, [%1];" : "=r"(v) : "r"(smem_u32(p)) : "memory");
+  return v;
+}
 
 // bounded wait that also gives up when another thread of the CTA has aborted
 __device__ __forceinline__ bool swt_wait(uint64_t* bar, uint32_t parity, long long limit,
@@ -89,6 +104,16 @@ __device__ __forceinline__ SwWin sw_win(int dir, int nb, int w, int s0, int k) {
     r.nblk = min(w, nb - 1 - k) + 1;
   }
   return r;
+}
+
+// Bounded wait until the counter reaches `target`.
+__device__ __forceinline__ bool swt_wait_count(const unsigned* counter, unsigned target, long long limit,
+                                               const volatile int* abort_flag) {
+  for (long long i = 0; i < limit; ++i) {
+    if (smem_load_acquire(counter) >= target) return true;
+    if ((i & 63) == 63 && *abort_flag) return false;
+  }
+  return false;
 }
 
 // Issue order.  The chunks of step t (two 32-row halves per window block) fall
@@ -141,6 +166,7 @@ __global__ void __launch_bounds__(SWT_THREADS, 1)
   __shared__ uint32_t tmem_base;
   __shared__ volatile int abort_flag;
   __shared__ long long last_pload[SWT_PST], last_mma;
+  __shared__ unsigned mma_done;  // chunks whose MMAs have completed, in order
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid == 0) {
@@ -159,6 +185,7 @@ __global__ void __launch_bounds__(SWT_THREADS, 1)
     }
     abort_flag = 0;
     last_mma = -1;
+    mma_done = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
@@ -171,7 +198,27 @@ __global__ void __launch_bounds__(SWT_THREADS, 1)
   tc_fence_after();
   const uint32_t tmem = tmem_base;
 
-  if (warp == SWT_PRODUCER || warp == SWT_ISSUER) {
+  // total number of chunks in the issue order
+  auto total_chunks = [&]() -> long long {
+    long long n = 0;
+    for (int t = 0; t < nsteps; ++t) {
+      const SwWin W = win(t);
+      n += sw_nA(W) + sw_nB(W) + sw_nC(W);
+    }
+    return n;
+  };
+
+  if (warp == SWT_ISSUER && lane == 1) {
+    // ------------------------------------------------ MMA completion tracker
+    const long long n = total_chunks();
+    for (long long g = 0; g < n; ++g) {
+      if (!swt_wait(&bar_aempty[g % SWT_AST], (uint32_t)((g / SWT_AST) & 1), limit, &abort_flag)) {
+        abort_flag = 1;
+        break;
+      }
+      smem_store_release(&mma_done, (unsigned)(g + 1));
+    }
+  } else if (warp == SWT_PRODUCER || warp == SWT_ISSUER) {
     if (lane == 0) {
       const bool producer = warp == SWT_PRODUCER;
       constexpr uint32_t idesc = tc_idesc(TC_M, TC_N);
@@ -251,9 +298,9 @@ __global__ void __launch_bounds__(SWT_THREADS, 1)
     // split one 32-row piece of this thread's column into the stage of chunk g
     auto fill = [&](long long g, const float (&v)[TC_KC]) -> bool {
       const int sa = (int)(g % SWT_AST);
-      const long long use = g / SWT_AST;
-      bool good = !abort_flag &&
-                  (use == 0 || swt_wait(&bar_aempty[sa], (uint32_t)((use - 1) & 1), limit, &abort_flag));
+      // the stage's previous chunk (g - SWT_AST) must be consumed
+      bool good = !abort_flag && (g < SWT_AST || swt_wait_count(&mma_done, (unsigned)(g - SWT_AST + 1), limit,
+                                                                &abort_flag));
       good = __all_sync(0xffffffffu, good);  // the TMEM stores below are warp-collective
       if (!good) return false;
       tc_fence_after();
@@ -409,8 +456,10 @@ __global__ void __launch_bounds__(SWT_THREADS, 1)
   if (tid == 0 && abort_flag) {
     for (int s = 0; s < SWT_PST; ++s)
       if (last_pload[s] >= 0) mbar_wait(&bar_pfull[s], (uint32_t)((last_pload[s] / SWT_PST) & 1));
-    const long long qm = last_mma;
-    if (qm >= 0) mbar_wait(&bar_aempty[qm % SWT_AST], (uint32_t)((qm / SWT_AST) & 1));
+    // the MMA completions not seen yet, one phase at a time (in order, so no
+    // parity wait can pass early)
+    for (long long g = mma_done; g <= last_mma; ++g)
+      if (!mbar_wait(&bar_aempty[g % SWT_AST], (uint32_t)((g / SWT_AST) & 1))) break;
     atomicOr(err, DE_TIMEOUT);
   }
   tc_fence_before();
