@@ -728,7 +728,7 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
     raise_smem(k_schur_apply_df, D.maxNI * sizeof(float2));
   else
     raise_smem(k_schur_apply_f64, D.maxNI * sizeof(double));
-  raise_smem(k_pc_local<T>, D.maxNI * sizeof(T));
+  raise_smem(k_pc_local<T>, D.maxNI * sizeof(typename PcVec<T>::type));
   raise_smem(k_post_df, (D.maxNI + 1) * sizeof(float2));
   (void)ppool;
 
@@ -1548,7 +1548,7 @@ static void level2_apply(Device& D1, const double* rc, double* uc);
 template <typename T>
 static void launch_pc(Device& D, const double* rin, double* zout, const PcgCtl* ctl) {
   dim3 grid(D.nrb, D.nsub);
-  size_t smem = (size_t)D.maxNI * sizeof(T);
+  size_t smem = (size_t)D.maxNI * sizeof(typename PcVec<T>::type);
   D.prof.begin(PH_PC_LOCAL, D.st);
   k_pc_local<T><<<grid, AT, smem, D.st>>>(D.ds, static_cast<const T*>(D.poolPC), rin, D.uniq, D.wrep, D.zrep,
                                           D.rcpart, D.nrb, D.ncpmax, ctl);

@@ -132,7 +132,25 @@ __global__ void __launch_bounds__(RT) k_assemble_dot(int n, Owners own, const do
 // --------------------------------------------------- preconditioner parts
 // z_s = Z_s (w_s .* r_s) and partial coarse residual Phi_s^T (w_s .* r_s)
 // (the dual basis Phi_dual for a general matrix, dd_phisi_dual_apply,
-// module_dd.f90:6126-6206; oPhid = oPhi for symmetric matrices)
+// module_dd.f90:6126-6206; oPhid = oPhi for symmetric matrices).
+//
+// With FP32 blocks (mixed precision) the blocks are exact FP32 numbers and the
+// products are formed to FP64 accuracy: w .* r is kept as a double-float pair
+// and each row sum is accumulated with error-free transformations.  The
+// preconditioner is then a fixed linear operator (the FP32 blocks) applied
+// without rounding noise: a product rounded to FP32 would add a relative
+// perturbation of ~1e-7 at every application, which delays the convergence of
+// the outer PCG on ill-conditioned problems (finite-precision CG behaves as if
+// its operator's eigenvalues were smeared by the size of such perturbations).
+template <typename T>
+struct PcVec {
+  using type = double;
+};
+template <>
+struct PcVec<float> {
+  using type = float2;  // (hi, lo) of an FP64 value
+};
+
 template <typename T>
 __global__ void __launch_bounds__(AT) k_pc_local(const DevSub* __restrict__ ds, const T* __restrict__ pcpool,
                                                  const double* __restrict__ r, const int* __restrict__ uniq,
@@ -143,23 +161,53 @@ __global__ void __launch_bounds__(AT) k_pc_local(const DevSub* __restrict__ ds, 
   const DevSub s = ds[blockIdx.y];
   const int r0 = blockIdx.x * AROWS;
   if (r0 >= s.ni) return;
+  using V = typename PcVec<T>::type;
   extern __shared__ __align__(16) unsigned char smraw[];
-  T* aux = reinterpret_cast<T*>(smraw);
-  for (int j = threadIdx.x; j < s.NI; j += AT) aux[j] = j < s.ni ? T(wrep[s.rep + j] * r[uniq[s.rep + j]]) : T(0);
+  V* aux = reinterpret_cast<V*>(smraw);
+  for (int j = threadIdx.x; j < s.NI; j += AT) {
+    const double x = j < s.ni ? wrep[s.rep + j] * r[uniq[s.rep + j]] : 0.0;
+    if constexpr (std::is_same_v<T, float>) {
+      const float hi = (float)x;
+      aux[j] = make_float2(hi, (float)(x - (double)hi));
+    } else {
+      aux[j] = x;
+    }
+  }
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int rend = min(r0 + AROWS, s.ni);
   for (int rr = r0 + warp; rr < rend; rr += AT / 32) {
     const T* row = pcpool + s.oZ + (long long)rr * s.NI;
-    T acc = T(0);
-    for (int j = lane; j < s.NI; j += 32) acc += __ldg(row + j) * aux[j];
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (lane == 0) zrep[s.rep + rr] = (double)acc;
+    if constexpr (std::is_same_v<T, float>) {
+      dfacc acc;
+      for (int j = lane; j < s.NI; j += 32) {
+        const float z = __ldg(row + j);
+        const float2 x = aux[j];
+        acc.fma_df(dfloat{x.x, x.y}, z);
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        dfacc other;
+        other.s = __shfl_xor_sync(0xffffffffu, acc.s, o);
+        other.c = __shfl_xor_sync(0xffffffffu, acc.c, o);
+        acc.merge(other);
+      }
+      if (lane == 0) zrep[s.rep + rr] = acc.to_double();
+    } else {
+      T acc = T(0);
+      for (int j = lane; j < s.NI; j += 32) acc += __ldg(row + j) * aux[j];
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+      if (lane == 0) zrep[s.rep + rr] = (double)acc;
+    }
   }
   // coarse residual partial over this CTA's rows
   for (int c = threadIdx.x; c < s.nc; c += AT) {
     double t = 0.0;
-    for (int rr = r0; rr < rend; ++rr) t += (double)pcpool[s.oPhid + (long long)rr * s.ncp + c] * (double)aux[rr];
+    for (int rr = r0; rr < rend; ++rr) {
+      double x;
+      if constexpr (std::is_same_v<T, float>) x = (double)aux[rr].x + (double)aux[rr].y;
+      else x = aux[rr];
+      t += (double)pcpool[s.oPhid + (long long)rr * s.ncp + c] * x;
+    }
     rcpart[((long long)blockIdx.y * nrb + blockIdx.x) * ncpmax + c] = t;
   }
 }
