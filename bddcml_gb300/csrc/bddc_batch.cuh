@@ -237,7 +237,7 @@ static void batch_prepare(Device& D, int nk, int lg, int maxit, int* shared_ndon
   B.aux = dalloc<T>(nrep * nk, mem);
   B.xs = dalloc<double>(nrep * nk, mem);  // float2 pairs or doubles: 8 bytes an entry either way
   B.ucs = dalloc<T>(std::max(1LL, ncon) * nk, mem);
-  B.cbt = dalloc<T>(ldc * nk, mem);
+  B.cbt = dalloc<double>(ldc * nk, mem);  // in the coarse inverse's precision (FP64 at most)
   B.ctl = dalloc<PcgCtl>(nk, mem);
   B.ndone = shared_ndone ? shared_ndone : dalloc<int>(1, mem);
   B.hist = dalloc<double>((long long)ldh * nk, mem);
@@ -429,20 +429,25 @@ static void batch_pc(Device& D, const double* rin, double* zout, double* part) {
       batch_level2(D, B.rc, B.uc);
     } else {
       // explicit coarse inverse with two FP64 refinement steps, as in the single-column path
-      const T* minv = static_cast<const T*>(D.cinv);
-      T* cb = static_cast<T*>(B.cbt);
-      const long long cc = (long long)D.ndofc << lg;
-      kb_to_t<T><<<blocks_for(cc), 256, 0, st>>>(cc, B.rc, cb, nk, B.ndone);
-      CKL();
-      gemm_t<T>(D, B.gC, 1, D.ndofc, minv, cb, nullptr, nk, B.uc, nullptr, nk, nk, B.ndone);
-      for (int rr = 0; rr < 2; ++rr) {
-        kb_coarse_res<<<blocks_for(cc), 256, 0, st>>>(D.ndofc, lg, D.ac_ptr, D.ac_col, D.ac_val, B.rc, B.uc, B.cres,
-                                                      B.ndone);
+      auto coarse = [&](auto tag) {
+        using TC = decltype(tag);
+        const TC* minv = static_cast<const TC*>(D.cinv);
+        TC* cb = static_cast<TC*>(B.cbt);
+        const long long cc = (long long)D.ndofc << lg;
+        kb_to_t<TC><<<blocks_for(cc), 256, 0, st>>>(cc, B.rc, cb, nk, B.ndone);
         CKL();
-        kb_to_t<T><<<blocks_for(cc), 256, 0, st>>>(cc, B.cres, cb, nk, B.ndone);
-        CKL();
-        gemm_t<T>(D, B.gC, 1, D.ndofc, minv, cb, nullptr, nk, B.uc, B.uc, nk, nk, B.ndone);
-      }
+        gemm_t<TC>(D, B.gC, 1, D.ndofc, minv, cb, nullptr, nk, B.uc, nullptr, nk, nk, B.ndone);
+        for (int rr = 0; rr < 2; ++rr) {
+          kb_coarse_res<<<blocks_for(cc), 256, 0, st>>>(D.ndofc, lg, D.ac_ptr, D.ac_col, D.ac_val, B.rc, B.uc,
+                                                        B.cres, B.ndone);
+          CKL();
+          kb_to_t<TC><<<blocks_for(cc), 256, 0, st>>>(cc, B.cres, cb, nk, B.ndone);
+          CKL();
+          gemm_t<TC>(D, B.gC, 1, D.ndofc, minv, cb, nullptr, nk, B.uc, B.uc, nk, nk, B.ndone);
+        }
+      };
+      if (D.coarse64) coarse(double{});
+      else coarse(T{});
     }
     if (tc) {
       if (B.tc_mch2 > 0) {

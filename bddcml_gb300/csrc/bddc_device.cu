@@ -255,7 +255,8 @@ class Device {
   double *yrep = nullptr, *zrep = nullptr, *grep = nullptr, *fi = nullptr, *fo = nullptr;
   long long* fo_off = nullptr;
   double *rcpart = nullptr, *rc = nullptr, *uc = nullptr, *cres = nullptr;
-  void* cinv = nullptr;            // explicit coarse inverse (factor precision), ldc x ldc
+  void* cinv = nullptr;            // explicit coarse inverse (factor precision, or FP64 with coarse64), ldc x ldc
+  bool coarse64 = false;           // the coarse factor and inverse are FP64 (FP32 factorisation broke down)
   int *ac_ptr = nullptr, *ac_col = nullptr;
   double* ac_val = nullptr;        // coarse matrix, FP64 CSR
   int ndofc = 0, ldc = 0, nrb = 0, ncpmax = 0, maxNI = 0, maxNO = 0;
@@ -410,6 +411,24 @@ static void run_factor(Device& D, const BandDesc* bd, int nbatch, int maxnb, int
     CKL();
     if (maxw > 0) {
       k_chol_off<T><<<dim3(maxw, nbatch), NT, 0, D.st>>>(bd, pool, k);
+      CKL();
+    }
+  }
+}
+
+// right-looking block Cholesky (k_chol_rl_*): for a few dense systems
+template <typename T>
+static void run_factor_rl(Device& D, const BandDesc* bd, int nbatch, int maxnb, int maxw, T* pool, int* err) {
+  size_t smem = (2 * NB * (NB + 1) + 2 * SM_TILE) * sizeof(T);
+  raise_smem(k_chol_rl_diag<T>, smem);
+  for (int k = 0; k < maxnb; ++k) {
+    k_chol_rl_diag<T><<<nbatch, NT, smem, D.st>>>(bd, pool, k, err);
+    CKL();
+    const int m = std::min(maxw, maxnb - 1 - k);
+    if (m > 0) {
+      k_chol_rl_panel<T><<<dim3(m, nbatch), NT, 0, D.st>>>(bd, pool, k);
+      CKL();
+      k_chol_rl_update<T><<<dim3(m * (m + 1) / 2, nbatch), NT, 0, D.st>>>(bd, pool, k);
       CKL();
     }
   }
@@ -864,6 +883,61 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
   D.prof.end(PH_NUMERIC_TOTAL, st);
 }
 
+// Coarse matrix (assembled from the local coarse matrices in a fixed order),
+// its block factor (right-looking for the symmetric case) and explicit
+// inverse, in precision TC.  Returns false if the symmetric factorisation met a
+// non-positive pivot.
+template <typename TC>
+static bool coarse_factor(Device& D, int nc_g, int nbc, const int* dcptr, const long long* dcontrib,
+                          vector<void*>& own) {
+  cudaStream_t st = D.st;
+  BandDesc cb{nbc, nbc - 1, D.ldc, 0, 0, (long long)nbc * nbc * NB * NB,
+              (long long)nbc * nbc * NB * NB + (long long)nbc * NB * NB};
+  size_t csize = (size_t)cb.oB + (size_t)D.ldc * D.ldc;
+  BandDesc cbu = cb;  // U^T band of a general coarse matrix, after the identity block
+  if (D.general) {
+    cbu.oL = (long long)csize;
+    cbu.oLinv = cbu.oL + (long long)nbc * nbc * NB * NB;
+    csize = (size_t)cbu.oLinv + (size_t)nbc * NB * NB;
+  }
+  TC* cpool = dalloc<TC>(csize, own);
+  CK(cudaMemsetAsync(cpool, 0, csize * sizeof(TC), st));
+  vector<BandDesc> hcbu{cbu};
+  BandDesc* dcbu = D.general ? upload(hcbu, own, st) : nullptr;
+  if (nc_g > 0) {
+    k_coarse_assemble<TC><<<nc_g, 128, 0, st>>>(nc_g, D.ac_ptr, D.ac_col, dcptr, dcontrib, D.small, D.ac_val, cpool,
+                                                cb, dcbu);
+    CKL();
+  }
+  k_coarse_pad<TC><<<(D.ldc + 255) / 256, 256, 0, st>>>(nc_g, D.ldc, cpool, cb);
+  CKL();
+  vector<BandDesc> hcb{cb};
+  BandDesc* dcb = upload(hcb, own, st);
+  if (D.general) {
+    run_factor_lu<TC>(D, dcb, dcbu, 1, nbc, nbc - 1, cpool);
+  } else {
+    int* cerr = dalloc<int>(1, own);
+    CK(cudaMemsetAsync(cerr, 0, sizeof(int), st));
+    run_factor_rl<TC>(D, dcb, 1, nbc, nbc - 1, cpool, cerr);
+    int herr = 0;
+    CK(cudaMemcpyAsync(&herr, cerr, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (herr) return false;
+  }
+  if constexpr (std::is_same_v<TC, float>) {
+    // identity right-hand side needs a column count that is a multiple of the MMA tile
+    vector<TcDesc> htc{TcDesc{nbc, nbc - 1, D.ldc, D.ldc, cb.oB, 0, (long long)nbc * nbc * 2 * TC_PCHUNK, -1}};
+    TcDesc* tdc = upload(htc, own, st);
+    float* cpan = dalloc<float>((size_t)2 * nbc * nbc * 2 * TC_PCHUNK, own);
+    run_panels(D, dcb, tdc, 1, nbc, nbc - 1, cpool, cpan, dcbu);
+    run_solve_tc(D, tdc, 1, nbc, D.ldc, cpan, cpool);
+  } else {
+    run_solve<TC>(D, dcb, 1, nbc, D.ldc, cpool, cpool, dcbu);
+  }
+  D.cinv = cpool + cb.oB;
+  return true;
+}
+
 // The constraint-dependent part of the setup: Srho factor, [Srho^-1 | Y], G^-1,
 // Phi, Z, the local coarse matrices and the coarse problem.  Run after
 // setup_numeric, and again when adaptive constraints have changed C; each run
@@ -1080,41 +1154,15 @@ static void setup_precond(Solver& S, Device& D) {
     int* dcptr = upload(acptr, own, st);
     long long* dcontrib = upload(acontrib, own, st);
     D.ac_val = dalloc<double>(acol.size(), own);
-    BandDesc cb{nbc, nbc - 1, D.ldc, 0, 0, (long long)nbc * nbc * NB * NB,
-                (long long)nbc * nbc * NB * NB + (long long)nbc * NB * NB};
-    size_t csize = (size_t)cb.oB + (size_t)D.ldc * D.ldc;
-    BandDesc cbu = cb;  // U^T band of a general coarse matrix, after the identity block
-    if (D.general) {
-      cbu.oL = (long long)csize;
-      cbu.oLinv = cbu.oL + (long long)nbc * nbc * NB * NB;
-      csize = (size_t)cbu.oLinv + (size_t)nbc * NB * NB;
+    // factor and explicit inverse in factor precision; an FP32 factorisation
+    // that meets a non-positive pivot (a coarse problem too ill-conditioned
+    // for FP32) is redone in FP64
+    D.coarse64 = false;
+    if (!coarse_factor<T>(D, nc_g, nbc, dcptr, dcontrib, own) && std::is_same_v<T, float>) {
+      D.coarse64 = true;
+      if (!coarse_factor<double>(D, nc_g, nbc, dcptr, dcontrib, own))
+        throw Error{ERR_NUMERIC, "non-positive pivot in the FP64 coarse factorisation"};
     }
-    T* cpool = dalloc<T>(csize, own);
-    CK(cudaMemsetAsync(cpool, 0, csize * sizeof(T), st));
-    vector<BandDesc> hcbu{cbu};
-    BandDesc* dcbu = D.general ? upload(hcbu, own, st) : nullptr;
-    if (nc_g > 0) {
-      k_coarse_assemble<T><<<nc_g, 128, 0, st>>>(nc_g, D.ac_ptr, D.ac_col, dcptr, dcontrib, D.small, D.ac_val,
-                                                  cpool, cb, dcbu);
-      CKL();
-    }
-    k_coarse_pad<T><<<(D.ldc + 255) / 256, 256, 0, st>>>(nc_g, D.ldc, cpool, cb);
-    CKL();
-    vector<BandDesc> hcb{cb};
-    BandDesc* dcb = upload(hcb, own, st);
-    if (D.general) run_factor_lu<T>(D, dcb, dcbu, 1, nbc, nbc - 1, cpool);
-    else run_factor<T>(D, dcb, 1, nbc, nbc - 1, cpool);
-    if constexpr (std::is_same_v<T, float>) {
-      // identity right-hand side needs a column count that is a multiple of the MMA tile
-      vector<TcDesc> htc{TcDesc{nbc, nbc - 1, D.ldc, D.ldc, cb.oB, 0, (long long)nbc * nbc * 2 * TC_PCHUNK, -1}};
-      TcDesc* tdc = upload(htc, own, st);
-      float* cpan = dalloc<float>((size_t)2 * nbc * nbc * 2 * TC_PCHUNK, own);
-      run_panels(D, dcb, tdc, 1, nbc, nbc - 1, cpool, cpan, dcbu);
-      run_solve_tc(D, tdc, 1, nbc, D.ldc, cpan, cpool);
-    } else {
-      run_solve<T>(D, dcb, 1, nbc, D.ldc, cpool, cpool, dcbu);
-    }
-    D.cinv = cpool + cb.oB;
     D.cres = dalloc<double>(std::max(1, nc_g), own);
   }
   D.prof.end(PH_COARSE, st);
@@ -1563,13 +1611,19 @@ static void launch_pc(Device& D, const double* rin, double* zout, const PcgCtl* 
     k_coarse_gather<<<(D.ndofc + 255) / 256, 256, 0, D.st>>>(D.ndofc, D.co_ptr, D.co_sub, D.co_loc, D.ds, D.rcpart,
                                                            D.nrb, D.ncpmax, D.rc, ctl);
     CKL();
-    const T* minv = static_cast<const T*>(D.cinv);
     int gb = (D.ndofc + 7) / 8;
-    k_coarse_gemv<T><<<gb, 256, 0, D.st>>>(D.ndofc, D.ldc, minv, D.rc, D.uc, 0, ctl);
+    auto gemv = [&](const double* v, int mode) {
+      if (D.coarse64)
+        k_coarse_gemv<double><<<gb, 256, 0, D.st>>>(D.ndofc, D.ldc, static_cast<const double*>(D.cinv), v, D.uc,
+                                                     mode, ctl);
+      else
+        k_coarse_gemv<T><<<gb, 256, 0, D.st>>>(D.ndofc, D.ldc, static_cast<const T*>(D.cinv), v, D.uc, mode, ctl);
+    };
+    gemv(D.rc, 0);
     for (int rr = 0; rr < 2; ++rr) {
       k_coarse_residual<<<(D.ndofc + 255) / 256, 256, 0, D.st>>>(D.ndofc, D.ac_ptr, D.ac_col, D.ac_val, D.rc, D.uc,
                                                                D.cres, ctl);
-      k_coarse_gemv<T><<<gb, 256, 0, D.st>>>(D.ndofc, D.ldc, minv, D.cres, D.uc, 1, ctl);
+      gemv(D.cres, 1);
     }
     CKL();
   }

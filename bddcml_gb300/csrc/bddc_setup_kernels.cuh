@@ -44,11 +44,11 @@ struct DevSub {
 // Shared memory of the diagonal step: a[NB][NB+1], inv[NB][NB+1], smA, smB.
 template <typename T>
 __device__ void chol_diag_step(const BandDesc& d, T* __restrict__ pool, int k, int* __restrict__ err, T* a, T* inv,
-                               T* smA, T* smB) {
+                               T* smA, T* smB, bool left = true) {
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   T acc[4][4];
   tile_zero(acc);
-  for (int j = max(0, k - d.w); j < k; ++j) {
+  for (int j = left ? max(0, k - d.w) : k; j < k; ++j) {
     const T* Lkj = pool + band_block(d, k, j);
     tile_gemm<T, false, true>(acc, Lkj, NB, Lkj, NB, NB, smA, smB);
   }
@@ -295,6 +295,67 @@ __global__ void __launch_bounds__(NT) k_chol_diag(const BandDesc* __restrict__ b
   T* inv = a + NB * (NB + 1);
   T* smA = inv + NB * (NB + 1);
   chol_diag_step<T>(d, pool, k, err, a, inv, smA, smA + SM_TILE);
+}
+
+// Right-looking steps (the trailing blocks already hold A minus the updates of
+// the earlier steps): the diagonal factor, then the panel L_ik = A_ik Linv_kk^T,
+// then the trailing update A_ij -= L_ik L_jk^T of every block pair k < j <= i,
+// one CTA per block (pair).  For one dense system (the coarse problem) this
+// spreads each step over many CTAs, where the left-looking steps leave a few
+// CTAs with long chains of block products.
+template <typename T>
+__global__ void __launch_bounds__(NT) k_chol_rl_diag(const BandDesc* __restrict__ bd, T* __restrict__ pool, int k,
+                                                     int* __restrict__ err) {
+  const BandDesc d = bd[blockIdx.x];
+  if (k >= d.nb) return;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T* a = reinterpret_cast<T*>(smraw);
+  T* inv = a + NB * (NB + 1);
+  T* smA = inv + NB * (NB + 1);
+  chol_diag_step<T>(d, pool, k, err, a, inv, smA, smA + SM_TILE, false);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(NT) k_chol_rl_panel(const BandDesc* __restrict__ bd, T* __restrict__ pool, int k) {
+  const BandDesc d = bd[blockIdx.y];
+  const int i = k + 1 + blockIdx.x;
+  if (k >= d.nb || i >= d.nb || i - k > d.w) return;
+  __shared__ __align__(16) T smA[SM_TILE];
+  __shared__ __align__(16) T smB[SM_TILE];
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  T acc[4][4];
+  tile_zero(acc);
+  T* Aik = pool + band_block(d, i, k);
+  tile_gemm<T, false, true>(acc, Aik, NB, pool + d.oLinv + (long long)k * NB * NB, NB, NB, smA, smB);
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+#pragma unroll
+    for (int p = 0; p < 4; ++p) Aik[(ty * 4 + q) * NB + tx * 4 + p] = acc[q][p];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(NT) k_chol_rl_update(const BandDesc* __restrict__ bd, T* __restrict__ pool, int k) {
+  const BandDesc d = bd[blockIdx.y];
+  if (k >= d.nb) return;
+  // block pair (i, j), k < j <= i, from the position in the lower triangle
+  const int p = blockIdx.x;
+  int ii = (int)((sqrt(8.0 * p + 1.0) - 1.0) * 0.5);
+  while ((ii + 1) * (ii + 2) / 2 <= p) ++ii;
+  while (ii * (ii + 1) / 2 > p) --ii;
+  const int jj = p - ii * (ii + 1) / 2;
+  const int i = k + 1 + ii, j = k + 1 + jj;
+  if (i >= d.nb || i - k > d.w || j - k > d.w) return;
+  __shared__ __align__(16) T smA[SM_TILE];
+  __shared__ __align__(16) T smB[SM_TILE];
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  T acc[4][4];
+  tile_zero(acc);
+  tile_gemm<T, false, true>(acc, pool + band_block(d, i, k), NB, pool + band_block(d, j, k), NB, NB, smA, smB);
+  T* Aij = pool + band_block(d, i, j);
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+#pragma unroll
+    for (int p2 = 0; p2 < 4; ++p2) Aij[(ty * 4 + q) * NB + tx * 4 + p2] -= acc[q][p2];
 }
 
 template <typename T>
