@@ -23,14 +23,14 @@
 // and the issue order (below) lets the tensor core work on them while the
 // epilogue of the previous step runs.
 //
-// Roles (320 threads, one CTA per SM):
+// Roles (352 threads, one CTA per SM):
 //   warps 0-3 and 4-7: two staging groups (each one thread per TMEM lane);
 //       group (jb & 1) stages every chunk of window block jb and writes the
 //       results of block jb (the epilogue), so a thread only ever reads back
 //       rows of its own column that it wrote itself;
 //   warp 8 (one thread): panel chunks into a ring of shared-memory slots;
-//   warp 9, lane 0: the MMAs, into one of three TMEM accumulators;
-//   warp 9, lane 1: follows the MMA completions chunk by chunk (one phase of
+//   warp 9 (one thread): the MMAs, into one of three TMEM accumulators;
+//   warp 10 (one thread): follows the MMA completions chunk by chunk (one phase of
 //       one stage barrier at a time) and publishes their count, which the
 //       staging threads wait on before they refill a stage.  The epilogue
 //       fills stages out of chunk order, and a parity wait on a barrier that
@@ -53,8 +53,8 @@ constexpr int SWT_AST = 5;                       // TMEM stages of split window 
 constexpr int SWT_NACC = 3;                      // TMEM accumulators (steps t, t + 1, t + 2)
 constexpr int SWT_PST = 6;                       // shared-memory slots of panel chunks
 constexpr int SWT_GROUP = 128;                   // threads of one staging group
-constexpr int SWT_PRODUCER = 8, SWT_ISSUER = 9;  // warps
-constexpr int SWT_THREADS = 320;
+constexpr int SWT_PRODUCER = 8, SWT_ISSUER = 9, SWT_TRACKER = 10;  // warps
+constexpr int SWT_THREADS = 352;
 constexpr uint32_t SWT_ACOL = SWT_NACC * TC_N;  // TMEM column of stage 0, after the accumulators
 constexpr uint32_t SWT_TCOLS = 512;
 static_assert(SWT_ACOL + SWT_AST * 2 * TC_KC <= SWT_TCOLS, "tensor memory columns");
@@ -112,6 +112,7 @@ __device__ __forceinline__ bool swt_wait_count(const unsigned* counter, unsigned
   for (long long i = 0; i < limit; ++i) {
     if (smem_load_acquire(counter) >= target) return true;
     if ((i & 63) == 63 && *abort_flag) return false;
+    __nanosleep(20);  // back off: spinning warps take issue slots from the working ones
   }
   return false;
 }
@@ -208,15 +209,17 @@ __global__ void __launch_bounds__(SWT_THREADS, 1)
     return n;
   };
 
-  if (warp == SWT_ISSUER && lane == 1) {
-    // ------------------------------------------------ MMA completion tracker
-    const long long n = total_chunks();
-    for (long long g = 0; g < n; ++g) {
-      if (!swt_wait(&bar_aempty[g % SWT_AST], (uint32_t)((g / SWT_AST) & 1), limit, &abort_flag)) {
-        abort_flag = 1;
-        break;
+  if (warp == SWT_TRACKER) {
+    // ------------------------------------------------ MMA completion tracker (one thread)
+    if (lane == 0) {
+      const long long n = total_chunks();
+      for (long long g = 0; g < n; ++g) {
+        if (!swt_wait(&bar_aempty[g % SWT_AST], (uint32_t)((g / SWT_AST) & 1), limit, &abort_flag)) {
+          abort_flag = 1;
+          break;
+        }
+        smem_store_release(&mma_done, (unsigned)(g + 1));
       }
-      smem_store_release(&mma_done, (unsigned)(g + 1));
     }
   } else if (warp == SWT_PRODUCER || warp == SWT_ISSUER) {
     if (lane == 0) {
