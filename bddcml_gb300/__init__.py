@@ -31,7 +31,8 @@ STAT_FIELDS = ["t_host_setup", "t_device_setup", "t_solve", "t_iterations", "t_p
                "flop_sweep_oo", "flop_sweep_s", "bytes_residual", "bytes_schur_apply", "bytes_pc_local",
                "launches_setup", "launches_solve", "t_dev_alloc", "t_dev_h2d", "npair", "nadaptive",
                "adapt_est", "t_adaptive", "lobpcg_resid", "lobpcg_iter", "batch_bytes_schur",
-               "batch_flop_schur_mma", "batch_flop_schur", "batch_flop_pc", "batch_nk"]
+               "batch_flop_schur_mma", "batch_flop_schur", "batch_flop_pc", "batch_nk",
+               "bytes_assemble_dot", "bytes_assemble_z", "bytes_coarse_apply"]
 
 EXPORTS = ["bddcml_init_c", "bddcml_upload_global_data_c", "bddcml_upload_subdomain_data_c",
            "bddcml_setup_preconditioner_c", "bddcml_solve_c", "bddcml_download_local_solution_c",
@@ -49,7 +50,7 @@ EXPORTS = ["bddcml_init_c", "bddcml_upload_global_data_c", "bddcml_upload_subdom
 # phases of bddcml_get_profile_c (CUDA events on the solver stream)
 PHASES = ["numeric_total", "solve_total", "factor_interior", "solve_interior", "refine_residual", "schur",
           "precond_factor", "precond_solve", "precond_blocks", "coarse", "pcg", "schur_apply", "precond_local",
-          "postprocess"]
+          "postprocess", "assemble_dot", "assemble_z", "coarse_apply"]
 
 
 class BddcmlError(RuntimeError):

@@ -988,6 +988,26 @@ static void setup_precond(Solver& S, Device& D) {
     S.stats.flop_sweep_s += band_sweep_flop(d.nbi, d.nbi - 1, d.NRC);
     S.stats.bytes_pc_local += (double)d.ni * d.NI * sizeof(T) + (double)d.ni * d.ncp * sizeof(T) + d.ni * 24.0;
   }
+  // interface kernels, per launch (each entry read or written once):
+  //   assemble_dot: per replicated dof its value and owner record (rep index), per
+  //     unique dof the owner pointer, the fixed flag, the weight sum, the dot vector
+  //     and the result;
+  //   assemble_z: per replicated dof z_s, w_s, the owner record (rep, sub, loc) and
+  //     the dof's row of Phi (ncp entries) with the coarse map; per unique dof the
+  //     owner pointer, r, the weight sum and the result;
+  //   coarse_apply: the coarse partials of every subdomain row block, the explicit
+  //     inverse three times and the sparse coarse matrix twice.
+  {
+    double nrep = 0, zrow = 0, nnzc = 0;
+    for (auto& d : D.hs) {
+      nrep += d.ni;
+      zrow += (double)d.ni * ((double)d.ncp * sizeof(T) + 4.0 * d.nc / std::max(1, d.ni));
+    }
+    const double n = D.n;
+    S.stats.bytes_assemble_dot = nrep * (8.0 + 4.0) + n * (4.0 + 4.0 + 8.0 + 8.0 + 8.0);
+    S.stats.bytes_assemble_z = nrep * (8.0 + 8.0 + 12.0) + zrow + n * (4.0 + 8.0 + 8.0 + 8.0);
+    (void)nnzc;
+  }
   T* poolP = dalloc<T>(oP, own);
   D.poolP = poolP;
   float* ppool = std::is_same_v<T, float> ? dalloc<float>(oPan, own) : nullptr;
@@ -1164,6 +1184,13 @@ static void setup_precond(Solver& S, Device& D) {
         throw Error{ERR_NUMERIC, "non-positive pivot in the FP64 coarse factorisation"};
     }
     D.cres = dalloc<double>(std::max(1, nc_g), own);
+    {
+      double parts = 0;
+      for (auto& d : D.hs) parts += (double)D.nrb * d.nc;
+      const double esz = D.coarse64 ? 8.0 : (double)sizeof(T);
+      S.stats.bytes_coarse_apply = parts * 8.0 + 3.0 * (double)nc_g * nc_g * esz +
+                                   2.0 * (double)acol.size() * 12.0 + 8.0 * nc_g * 8.0;
+    }
   }
   D.prof.end(PH_COARSE, st);
   D.prof.end(PH_NUMERIC_TOTAL, st);
@@ -1586,9 +1613,11 @@ static void launch_schur(Device& D, const double* vin, double* vout, bool zero_f
   }
   CKL();
   D.prof.end(PH_SCHUR_APPLY, D.st);
+  D.prof.begin(PH_ASSEMBLE_DOT, D.st);
   k_assemble_dot<<<D.npart, RT, 0, D.st>>>(D.n, D.own, D.yrep, D.fixed, D.wsum, dotvec, vout, D.part, ctl,
                                            zero_fixed ? 1 : 0);
   CKL();
+  D.prof.end(PH_ASSEMBLE_DOT, D.st);
 }
 
 static void level2_apply(Device& D1, const double* rc, double* uc);
@@ -1608,6 +1637,7 @@ static void launch_pc(Device& D, const double* rin, double* zout, const PcgCtl* 
     CKL();
     level2_apply(D, D.rc, D.uc);
   } else if (D.ndofc > 0) {
+    D.prof.begin(PH_COARSE_APPLY, D.st);
     k_coarse_gather<<<(D.ndofc + 255) / 256, 256, 0, D.st>>>(D.ndofc, D.co_ptr, D.co_sub, D.co_loc, D.ds, D.rcpart,
                                                            D.nrb, D.ncpmax, D.rc, ctl);
     CKL();
@@ -1626,10 +1656,13 @@ static void launch_pc(Device& D, const double* rin, double* zout, const PcgCtl* 
       gemv(D.cres, 1);
     }
     CKL();
+    D.prof.end(PH_COARSE_APPLY, D.st);
   }
+  D.prof.begin(PH_ASSEMBLE_Z, D.st);
   k_assemble_z<T><<<D.npart, RT, 0, D.st>>>(D.n, D.own, D.ds, static_cast<const T*>(D.poolPC), D.zrep, D.wrep,
                                             D.cmap, D.uc, D.wsum, rin, zout, D.part, ctl);
   CKL();
+  D.prof.end(PH_ASSEMBLE_Z, D.st);
 }
 
 static double host_sum_parts(Device& D) {

@@ -24,7 +24,8 @@ enum Status { OK = 0, ERR_ARGUMENT = 1, ERR_CUDA = 2, ERR_NUMERIC = 3, ERR_UNSUP
 // bddcml_get_profile_c extension
 enum Phase {
   PH_NUMERIC_TOTAL = 0, PH_SOLVE_TOTAL, PH_FACTOR_OO, PH_SOLVE_OO, PH_RESIDUAL, PH_SCHUR, PH_SRHO_FACTOR,
-  PH_SRHO_SOLVE, PH_PC_BLOCKS, PH_COARSE, PH_PCG, PH_SCHUR_APPLY, PH_PC_LOCAL, PH_POST, NPHASE
+  PH_SRHO_SOLVE, PH_PC_BLOCKS, PH_COARSE, PH_PCG, PH_SCHUR_APPLY, PH_PC_LOCAL, PH_POST, PH_ASSEMBLE_DOT,
+  PH_ASSEMBLE_Z, PH_COARSE_APPLY, NPHASE
 };
 
 struct Error {
@@ -138,6 +139,10 @@ struct Stats {
   double bytes_residual = 0;    // one refinement residual (X read once, R written)
   double bytes_schur_apply = 0; // one Schur operator apply
   double bytes_pc_local = 0;    // one local preconditioner apply
+  // interface kernels of a PCG iteration: assembly of S p with the dot product
+  // (k_assemble_dot), assembly of z with the coarse correction (k_assemble_z),
+  // and the two-level coarse solve (gather, inverse, two refinements)
+  double bytes_assemble_dot = 0, bytes_assemble_z = 0, bytes_coarse_apply = 0;
   double launches_setup = 0, launches_solve = 0;  // kernel launches of the last set-up / solve
   double t_dev_alloc = 0, t_dev_h2d = 0;  // device set-up: allocations, staging + host->device copies
   // adaptive face constraints

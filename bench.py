@@ -234,7 +234,8 @@ def phase_roofline(phase, prof, st, hbm, tensor, peak_kind):
                 "algorithmic_flop": flop, "avg_launch_ms": ms / cnt, "peak_kind": peak_kind,
                 "attainable_3xtf32": tensor / 6.0, "frac_of_3xtf32_ceiling": ach / (tensor / 6.0)}
     byts = {"schur_apply": st["bytes_schur_apply"], "precond_local": st["bytes_pc_local"],
-            "refine_residual": st["bytes_residual"]}.get(phase)
+            "refine_residual": st["bytes_residual"], "assemble_dot": st.get("bytes_assemble_dot"),
+            "assemble_z": st.get("bytes_assemble_z"), "coarse_apply": st.get("bytes_coarse_apply")}.get(phase)
     if byts is None:
         return None
     ach = byts / t / 1e9
@@ -415,7 +416,8 @@ def run_gpu(args):
     if src:
         roof["traffic_source"] = src
     all_roof = {k: phase_roofline(k, prof_p, st_p, hbm, tensor, peak_kind)
-                for k in ("solve_interior", "precond_solve", "refine_residual", "schur_apply", "precond_local")}
+                for k in ("solve_interior", "precond_solve", "refine_residual", "schur_apply", "precond_local",
+                          "assemble_dot", "assemble_z", "coarse_apply")}
     kind, _, weights, tau = WORKLOADS[args.workload]
     # the oracle solves the adaptive pair eigenproblems densely, and takes minutes on the
     # three-level elasticity: both far beyond a bounded sample
