@@ -32,7 +32,7 @@ STAT_FIELDS = ["t_host_setup", "t_device_setup", "t_solve", "t_iterations", "t_p
                "launches_setup", "launches_solve", "t_dev_alloc", "t_dev_h2d", "npair", "nadaptive",
                "adapt_est", "t_adaptive", "lobpcg_resid", "lobpcg_iter", "batch_bytes_schur",
                "batch_flop_schur_mma", "batch_flop_schur", "batch_flop_pc", "batch_nk",
-               "bytes_assemble_dot", "bytes_assemble_z", "bytes_coarse_apply"]
+               "bytes_assemble_dot", "bytes_assemble_z", "bytes_coarse_apply", "refine_steps"]
 
 EXPORTS = ["bddcml_init_c", "bddcml_upload_global_data_c", "bddcml_upload_subdomain_data_c",
            "bddcml_setup_preconditioner_c", "bddcml_solve_c", "bddcml_download_local_solution_c",

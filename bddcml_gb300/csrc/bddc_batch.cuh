@@ -548,9 +548,14 @@ static void batch_interior_solve(Device& D, const double* rhs) {
     kb_v_residual<<<gr, vld, 0, st>>>(D.ds, D.koo, B.lg, rhs, D.uo_off, B.voff, vld, v, 0, 1);
     CKL();
     run_solve_tc(D, B.tdv1, D.nsub, D.maxnbo, vld, D.ppool_oo, v, 3, false);
-    kb_v_residual<<<gr, vld, 0, st>>>(D.ds, D.koo, B.lg, rhs, D.uo_off, B.voff, vld, v, 1, 2);
-    CKL();
-    run_solve_tc(D, B.tdv2, D.nsub, D.maxnbo, vld, D.ppool_oo, v, 1, true);
+    // as many further corrections as the setup's interior solves of the same
+    // matrix needed: one one-pass correction for well-conditioned interiors,
+    // else 3xTF32 corrections
+    for (int step = 2; step <= D.refine_steps; ++step) {
+      kb_v_residual<<<gr, vld, 0, st>>>(D.ds, D.koo, B.lg, rhs, D.uo_off, B.voff, vld, v, 1, 2);
+      CKL();
+      run_solve_tc(D, B.tdv2, D.nsub, D.maxnbo, vld, D.ppool_oo, v, D.refine_onepass ? 1 : 3, true);
+    }
   } else {
     run_solve<double>(D, B.bdv, D.nsub, D.maxnbo, vld, static_cast<const double*>(D.poolT), static_cast<double*>(B.vb));
   }

@@ -257,6 +257,8 @@ class Device {
   double *rcpart = nullptr, *rc = nullptr, *uc = nullptr, *cres = nullptr;
   void* cinv = nullptr;            // explicit coarse inverse (factor precision, or FP64 with coarse64), ldc x ldc
   bool coarse64 = false;           // the coarse factor and inverse are FP64 (FP32 factorisation broke down)
+  int refine_steps = 2;            // refinement steps the interior solves of the setup took
+  bool refine_onepass = true;      // ... the last one a one-pass correction (well-conditioned interiors)
   int *ac_ptr = nullptr, *ac_col = nullptr;
   double* ac_val = nullptr;        // coarse matrix, FP64 CSR
   int ndofc = 0, ldc = 0, nrb = 0, ncpmax = 0, maxNI = 0, maxNO = 0;
@@ -463,7 +465,7 @@ static void run_panels(Device& D, const BandDesc* bd, const TcDesc* td, int nbat
 // forward + backward tensor-core sweep; passes 3 (3xTF32) or 1 (TF32); with
 // acc the backward sweep also adds its result into each system's oAcc block
 template <int PASSES, bool ACC>
-static void sweep_pair(Device& D, dim3 grid, const TcDesc* td, const float* P, float* B) {
+static void sweep_pair(Device& D, dim3 grid, const TcDesc* td, const float* P, float* B, int* maxabs) {
   static bool attr = false;
   const size_t smem = swt_smem_bytes();
   if (!attr) {  // both instances launched here need the large shared-memory window
@@ -473,19 +475,22 @@ static void sweep_pair(Device& D, dim3 grid, const TcDesc* td, const float* P, f
     CK(cudaFuncSetAttribute(k_band_sweep_tm<PASSES, ACC>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
     attr = true;
   }
-  k_band_sweep_tm<PASSES, false><<<grid, SWT_THREADS, smem, D.st>>>(td, P, B, 0, D.err);
+  k_band_sweep_tm<PASSES, false><<<grid, SWT_THREADS, smem, D.st>>>(td, P, B, 0, D.err, nullptr);
   CKL();
-  k_band_sweep_tm<PASSES, ACC><<<grid, SWT_THREADS, smem, D.st>>>(td, P, B, 1, D.err);
+  k_band_sweep_tm<PASSES, ACC><<<grid, SWT_THREADS, smem, D.st>>>(td, P, B, 1, D.err, maxabs);
   CKL();
 }
 
+// maxabs (optional, one int per system): the largest |result| of each
+// system, as FP32 bits, merged into the array by atomicMax
 static void run_solve_tc(Device& D, const TcDesc* td, int nbatch, int maxnb, int maxncol, const float* P, float* B,
-                         int passes = 3, bool acc = false) {
+                         int passes = 3, bool acc = false, int* maxabs = nullptr) {
   (void)maxnb;
   dim3 grid(maxncol / TC_M, nbatch);
-  if (passes == 3) sweep_pair<3, false>(D, grid, td, P, B);
-  else if (acc) sweep_pair<1, true>(D, grid, td, P, B);
-  else sweep_pair<1, false>(D, grid, td, P, B);
+  if (passes == 3 && acc) sweep_pair<3, true>(D, grid, td, P, B, maxabs);
+  else if (passes == 3) sweep_pair<3, false>(D, grid, td, P, B, maxabs);
+  else if (acc) sweep_pair<1, true>(D, grid, td, P, B, maxabs);
+  else sweep_pair<1, false>(D, grid, td, P, B, maxabs);
 }
 
 template <typename T>
@@ -791,69 +796,93 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
   }
   D.prof.end(PH_FACTOR_OO, st);
   // ---- interior solves [X | v] = A_oo^-1 [A_oi | f_o], refined in mixed precision
+  int* dmax = nullptr;  // mixed precision: per refinement step and system, max |result| as FP32 bits
+  if (std::is_same_v<T, float>) {
+    dmax = dalloc<int>((size_t)nsub * 8, own);
+    CK(cudaMemsetAsync(dmax, 0, (size_t)nsub * 8 * sizeof(int), st));
+  }
   D.prof.begin(PH_SOLVE_OO, st);
   k_fill_rhs<T><<<dim3((D.maxNO + 127) / 128, nsub), 128, 0, st>>>(D.ds, D.koi, D.fo, D.fo_off, poolT);
   CKL();
-  if constexpr (std::is_same_v<T, float>) run_solve_tc(D, td_oo, nsub, D.maxnbo, D.maxNR, ppool, poolT);
+  if constexpr (std::is_same_v<T, float>) run_solve_tc(D, td_oo, nsub, D.maxnbo, D.maxNR, ppool, poolT, 3, false, dmax);
   else run_solve<T>(D, D.bd_oo, nsub, D.maxnbo, D.maxNR, poolT, poolT, D.bdu_oo);
   D.prof.end(PH_SOLVE_OO, st);
-  // Mixed precision: two refinement steps.
-  //   R0 = [A_oi | f_o] - A_oo X0, FP64-accurate (double-float) -> components 1
-  //        and 2, D1 = A_oo^-1 R0 in place in component 1 (3xTF32)
-  //   R1 = R0 - A_oo D1 in FP32 (R1 ~ 1e-5 R0, so FP32 rounding leaves it
-  //        within ~1 %) -> component 2, D2 = A_oo^-1 R1 in place with one TF32
-  //        pass (D2 is ~1e-10 of X, so its ~1 % error stays far below the FP32
-  //        pair's resolution), added into D1 by the backward sweep.
-  // X is then the unnormalised FP32 pair (X0, D1 + D2) in components 0 and 1.
-  int* dmax = nullptr;
-  if (D.prof.on && D.mixed) {
-    dmax = dalloc<int>((size_t)nsub * 3, own);
-    CK(cudaMemsetAsync(dmax, 0, (size_t)nsub * 3 * sizeof(int), st));
-    k_comp_maxabs<<<dim3(64, nsub), 256, 0, st>>>(D.ds, reinterpret_cast<const float*>(poolT), 0, dmax);
-    CKL();
-  }
+  // Mixed precision: refinement with FP64-accurate residuals until the
+  // correction is negligible (iterative refinement in the sense of Wilkinson;
+  // each step contracts the error by about kappa(A_oo) eps_fp32):
+  //   R0 = [A_oi | f_o] - A_oo X0 in double-float -> component 1 (and 2),
+  //   D1 = A_oo^-1 R0 in place (3xTF32), r1 = max|D1| / max|X0|.
+  //   If r1 <= 1e-5 (well-conditioned interiors): R1 = R0 - A_oo D1 in FP32
+  //     (R1 ~ r1 R0, so FP32 rounding leaves it within ~1 %) -> component 2,
+  //     D2 = A_oo^-1 R1 with one TF32 pass, added into D1: the result is
+  //     accurate to ~r1^2 x 1e-2.
+  //   Otherwise: residuals of the pair X0 + D in double-float and 3xTF32
+  //     corrections added into D, until max|correction| / max|X0| <= 1e-13
+  //     (at most six steps).
+  // X is the unnormalised FP32 pair (X0, D) in components 0 and 1.
   if constexpr (std::is_same_v<T, float>) {
-    for (int rr = 1; rr <= D.nref; ++rr) {
-      D.prof.begin(PH_RESIDUAL, st);
-      if (rr == 1) {  // R0, kept in component 2 as well for the second residual
-        k_residual_df<<<dim3((D.maxNO + RES_ROWS - 1) / RES_ROWS, nsub), 128, 0, st>>>(
-            D.ds, D.koo, D.koi, D.fo, D.fo_off, poolT, 0, 1, D.nref >= 2 ? 2 : -1);
-      } else {        // R1 = R0 - A_oo D1 (FP32 suffices for the one-pass correction)
-        k_residual_update_f32<<<dim3((D.maxNO + RES_ROWS - 1) / RES_ROWS, nsub), 128, 0, st>>>(D.ds, D.koo,
-                                                                                              poolT, 1, 2);
+    auto ratio = [&](int slot) {
+      vector<int> hmax((size_t)nsub * 8);
+      CK(cudaMemcpyAsync(hmax.data(), dmax, hmax.size() * sizeof(int), cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+      float r = 0.f;
+      for (int t = 0; t < nsub; ++t) {
+        float x0, dd;
+        std::memcpy(&x0, &hmax[t], 4);
+        std::memcpy(&dd, &hmax[(size_t)slot * nsub + t], 4);
+        if (x0 > 0) r = std::max(r, dd / x0);
       }
+      return r;
+    };
+    auto tds = [&](int comp, int acc_comp) {
+      vector<TcDesc> h2 = htd;
+      for (int t = 0; t < nsub; ++t) {
+        const long long cs = (long long)D.hs[t].NO * D.hs[t].NR;
+        h2[t].oB = D.hs[t].oXc + comp * cs;
+        h2[t].oAcc = acc_comp >= 0 ? D.hs[t].oXc + acc_comp * cs : -1;
+      }
+      return upload(h2, own, st);
+    };
+    const dim3 gres((D.maxNO + RES_ROWS - 1) / RES_ROWS, nsub);
+    D.prof.begin(PH_RESIDUAL, st);
+    k_residual_df<<<gres, 128, 0, st>>>(D.ds, D.koo, D.koi, D.fo, D.fo_off, poolT, 0, 1, 2);
+    CKL();
+    D.prof.end(PH_RESIDUAL, st);
+    D.prof.begin(PH_SOLVE_OO, st);
+    run_solve_tc(D, tds(1, -1), nsub, D.maxnbo, D.maxNR, ppool, poolT, 3, false, dmax + nsub);
+    D.prof.end(PH_SOLVE_OO, st);
+    const float r1 = ratio(1);
+    float rl = r1;
+    int steps = 1;
+    if (r1 <= 1e-5f) {
+      D.prof.begin(PH_RESIDUAL, st);
+      k_residual_update_f32<<<gres, 128, 0, st>>>(D.ds, D.koo, poolT, 1, 2);
       CKL();
       D.prof.end(PH_RESIDUAL, st);
       D.prof.begin(PH_SOLVE_OO, st);
-      vector<TcDesc> h2 = htd;
-      for (int t = 0; t < nsub; ++t) {
-        const long long comp = (long long)D.hs[t].NO * D.hs[t].NR;
-        h2[t].oB = D.hs[t].oXc + rr * comp;
-        h2[t].oAcc = rr == 2 ? D.hs[t].oXc + comp : -1;  // D2 is added into D1
-      }
-      TcDesc* tdr = upload(h2, own, st);
-      run_solve_tc(D, tdr, nsub, D.maxnbo, D.maxNR, ppool, poolT, rr == 1 ? 3 : 1, rr == 2);
+      run_solve_tc(D, tds(2, 1), nsub, D.maxnbo, D.maxNR, ppool, poolT, 1, true, dmax + 2 * nsub);
       D.prof.end(PH_SOLVE_OO, st);
-      if (dmax && rr <= 2) {
-        k_comp_maxabs<<<dim3(64, nsub), 256, 0, st>>>(D.ds, poolT, rr, dmax + (size_t)rr * nsub);
+      rl = ratio(2);
+      steps = 2;
+    } else {
+      for (int step = 2; step <= 7 && rl > 1e-13f; ++step) {
+        D.prof.begin(PH_RESIDUAL, st);
+        k_residual_df<<<gres, 128, 0, st>>>(D.ds, D.koo, D.koi, D.fo, D.fo_off, poolT, 1, 2);
         CKL();
+        D.prof.end(PH_RESIDUAL, st);
+        D.prof.begin(PH_SOLVE_OO, st);
+        const int slot = std::min(step, 7);
+        run_solve_tc(D, tds(2, 1), nsub, D.maxnbo, D.maxNR, ppool, poolT, 3, true, dmax + (size_t)slot * nsub);
+        D.prof.end(PH_SOLVE_OO, st);
+        rl = ratio(slot);
+        steps = step;
       }
-    }
-  }
-  if (dmax) {
-    vector<int> hmax((size_t)nsub * 3);
-    CK(cudaMemcpyAsync(hmax.data(), dmax, hmax.size() * sizeof(int), cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    float r1 = 0.f, r2 = 0.f;
-    for (int t = 0; t < nsub; ++t) {
-      float x0, d1, d2;
-      std::memcpy(&x0, &hmax[t], 4);
-      std::memcpy(&d1, &hmax[nsub + t], 4);
-      std::memcpy(&d2, &hmax[2 * nsub + t], 4);
-      if (x0 > 0) { r1 = std::max(r1, d1 / x0); r2 = std::max(r2, d2 / x0); }
     }
     S.stats.refine1 = r1;
-    S.stats.refine2 = r2;
+    S.stats.refine2 = rl;
+    S.stats.refine_steps = steps;
+    D.refine_steps = steps;
+    D.refine_onepass = r1 <= 1e-5f;
   }
   // ---- Schur complements and the subdomain reduced rhs
   D.prof.begin(PH_SCHUR, st);
@@ -2100,11 +2129,14 @@ static void reduced_rhs_device(Device& D) {
     k_residual1_df<<<gv, 128, 0, st>>>(D.ds, D.koo, D.fo, D.fo_off, v0, nullptr, v1, D.nv_off);
     CKL();
     solve1(v1);
-    k_residual1_df<<<gv, 128, 0, st>>>(D.ds, D.koo, D.fo, D.fo_off, v0, v1, rv, D.nv_off);
-    CKL();
-    solve1(rv);
-    k_add_vec1<float><<<gv, 128, 0, st>>>(D.ds, rv, v1, D.nv_off);
-    CKL();
+    // as many further corrections as the setup's interior solves needed (at least one)
+    for (int step = 2; step <= std::max(2, D.refine_steps); ++step) {
+      k_residual1_df<<<gv, 128, 0, st>>>(D.ds, D.koo, D.fo, D.fo_off, v0, v1, rv, D.nv_off);
+      CKL();
+      solve1(rv);
+      k_add_vec1<float><<<gv, 128, 0, st>>>(D.ds, rv, v1, D.nv_off);
+      CKL();
+    }
     k_put_rhs_column<float><<<gv, 128, 0, st>>>(D.ds, poolT, v0, v1, D.nv_off);
     CKL();
     k_reduced_rhs_df<<<dim3((D.maxNI + 127) / 128, nsub), 128, 0, st>>>(D.ds, D.kio, poolT, D.fi, D.grep);

@@ -128,7 +128,8 @@ struct Stats {
   double setup_flops = 0;
   double h2d_bytes = 0, d2h_bytes = 0;
   double t_upload = 0, t_host_assemble = 0, t_host_iface = 0, t_host_globs = 0, t_host_blocks = 0;
-  double refine1 = 0, refine2 = 0;  // max |correction| / max |X| of refinement steps 1, 2
+  double refine1 = 0, refine2 = 0;  // max |correction| / max |X| of the first and the last refinement step
+  double refine_steps = 0;          // refinement steps of the interior solves
   // batched solve, per Schur / preconditioner apply: operator bytes streamed, tensor-core
   // flops executed (sliced operator), FP64-equivalent flops of S X, working-precision
   // flops of the local preconditioner products, and the batch width

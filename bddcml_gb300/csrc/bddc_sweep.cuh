@@ -143,7 +143,7 @@ __device__ __forceinline__ int sw_pq(const SwWin& W, int jb, int half) { return 
 template <int PASSES, bool ACC>
 __global__ void __launch_bounds__(SWT_THREADS, 1)
     k_band_sweep_tm(const TcDesc* __restrict__ td, const float* __restrict__ ppool, float* __restrict__ bpool,
-                    int dir, int* __restrict__ err) {
+                    int dir, int* __restrict__ err, int* __restrict__ maxabs) {
   const TcDesc d = td[blockIdx.y];
   const int c0 = blockIdx.x * TC_M;
   if (c0 >= d.ncol || d.nb == 0) return;
@@ -355,6 +355,13 @@ __global__ void __launch_bounds__(SWT_THREADS, 1)
         float* dst = col + (long long)(k * NB + h * TC_KC) * lds;
 #pragma unroll
         for (int i = 0; i < TC_KC; ++i) dst[(long long)i * lds] = v[i];
+        if (maxabs) {  // largest |result| of the system (non-negative FP32 bits order like integers)
+          float m = 0.f;
+#pragma unroll
+          for (int i = 0; i < TC_KC; ++i) m = fmaxf(m, fabsf(v[i]));
+          for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+          if (lane == 0) atomicMax(maxabs + blockIdx.y, __float_as_int(m));
+        }
         if (ACC && col_acc) {
           float* dst2 = col_acc + (long long)(k * NB + h * TC_KC) * lds;
           float a[TC_KC];

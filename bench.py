@@ -449,7 +449,8 @@ def run_gpu(args):
         "gpu_launches_per_step": {"setup": int(st["launches_setup"]), "solve": int(st["launches_solve"])},
         "roofline": roof, "phase_rooflines": all_roof, "fp64_plain": fp64, "cpu_baseline": cpu,
         "parity": parity,
-        "refinement": {"max_correction_ratio_1": st_p["refine1"], "max_correction_ratio_2": st_p["refine2"]},
+        "refinement": {"max_correction_ratio_first": st_p["refine1"], "max_correction_ratio_last": st_p["refine2"],
+                       "steps": int(st_p.get("refine_steps", 0))},
         "adaptive": None if tau is None else {k: st_p[k] for k in ("npair", "nadaptive", "adapt_est", "t_adaptive",
                                                                   "lobpcg_resid", "lobpcg_iter", "ndofc")},
         "host_ms": {k: 1e3 * st_p[k] for k in ("t_upload", "t_host_assemble", "t_host_iface", "t_host_globs",
