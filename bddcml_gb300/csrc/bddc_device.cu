@@ -522,6 +522,8 @@ template <typename T>
 static void adaptive_constraints(Solver& S, Device& D);
 template <typename T>
 static void setup_level2(Solver& S, Device& D);
+template <typename T>
+static vector<vector<double>> coarse_energies(Device& D, const vector<int>& subs, vector<vector<double>>* phis);
 
 bool device_setup(Solver& S, Error& err) {
   Device& D = *S.dev;
@@ -1208,7 +1210,29 @@ static void setup_precond(Solver& S, Device& D) {
     // for FP32) is redone in FP64
     D.coarse64 = false;
     if (!coarse_factor<T>(D, nc_g, nbc, dcptr, dcontrib, own) && std::is_same_v<T, float>) {
+      // The local coarse matrices G^-1 - rho D^2 come from FP32 factors and can
+      // lose their small eigenvalues to cancellation on ill-conditioned
+      // subdomains: take Phi^T S Phi with FP64-accurate products instead
+      // (the Galerkin form the level-2 problem also uses), and factor in FP64.
       D.coarse64 = true;
+      vector<int> all(nsub);
+      std::iota(all.begin(), all.end(), 0);
+      vector<vector<double>> acs = coarse_energies<T>(D, all, nullptr);
+      long long nsm = 0;
+      for (auto& d : D.hs) nsm = std::max(nsm, d.oAc + (long long)d.ncp * d.ncp);
+      vector<double> hsmall(std::max<long long>(1, nsm));
+      CK(cudaMemcpyAsync(hsmall.data(), D.small, nsm * sizeof(double), cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+      for (int t = 0; t < nsub; ++t) {
+        const DevSub& d = D.hs[t];
+        for (int r = 0; r < d.nc; ++r)
+          for (int c = 0; c < d.nc; ++c) {  // symmetric part
+            const double v = 0.5 * (acs[t][(size_t)r * d.nc + c] + acs[t][(size_t)c * d.nc + r]);
+            hsmall[d.oAc + (long long)r * d.ncp + c] = v;
+          }
+      }
+      CK(cudaMemcpyAsync(D.small, hsmall.data(), nsm * sizeof(double), cudaMemcpyHostToDevice, st));
+      CK(cudaStreamSynchronize(st));
       if (!coarse_factor<double>(D, nc_g, nbc, dcptr, dcontrib, own))
         throw Error{ERR_NUMERIC, "non-positive pivot in the FP64 coarse factorisation"};
     }
