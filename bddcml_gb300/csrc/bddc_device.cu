@@ -819,8 +819,8 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
   //     D2 = A_oo^-1 R1 with one TF32 pass, added into D1: the result is
   //     accurate to ~r1^2 x 1e-2.
   //   Otherwise: residuals of the pair X0 + D in double-float and 3xTF32
-  //     corrections added into D, until max|correction| / max|X0| <= 1e-13
-  //     (at most six steps).
+  //     corrections added into D, until max|correction| / max|X0| <= 1e-12
+  //     (at most 13 corrections).
   // X is the unnormalised FP32 pair (X0, D) in components 0 and 1.
   if constexpr (std::is_same_v<T, float>) {
     auto ratio = [&](int slot) {
@@ -867,16 +867,20 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
       rl = ratio(2);
       steps = 2;
     } else {
-      for (int step = 2; step <= 7 && rl > 1e-13f; ++step) {
+      // The contraction per step is about kappa(A_oo) u with u ~ 2^-21 for the
+      // 3xTF32 sweeps (two TF32 halves per operand, the lo x lo term dropped):
+      // interiors with kappa ~ 1e5 (stiff inclusions) contract by ~0.2 a step.
+      TcDesc* tdc = tds(2, 1);
+      for (int step = 2; step <= 14 && rl > 1e-12f; ++step) {
         D.prof.begin(PH_RESIDUAL, st);
         k_residual_df<<<gres, 128, 0, st>>>(D.ds, D.koo, D.koi, D.fo, D.fo_off, poolT, 1, 2);
         CKL();
         D.prof.end(PH_RESIDUAL, st);
         D.prof.begin(PH_SOLVE_OO, st);
-        const int slot = std::min(step, 7);
-        run_solve_tc(D, tds(2, 1), nsub, D.maxnbo, D.maxNR, ppool, poolT, 3, true, dmax + (size_t)slot * nsub);
+        CK(cudaMemsetAsync(dmax + 2 * nsub, 0, (size_t)nsub * sizeof(int), st));
+        run_solve_tc(D, tdc, nsub, D.maxnbo, D.maxNR, ppool, poolT, 3, true, dmax + 2 * nsub);
         D.prof.end(PH_SOLVE_OO, st);
-        rl = ratio(slot);
+        rl = ratio(2);
         steps = step;
       }
     }
