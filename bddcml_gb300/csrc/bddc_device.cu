@@ -467,17 +467,17 @@ static void run_panels(Device& D, const BandDesc* bd, const TcDesc* td, int nbat
 template <int PASSES, bool ACC>
 static void sweep_pair(Device& D, dim3 grid, const TcDesc* td, const float* P, float* B, int* maxabs) {
   static bool attr = false;
-  const size_t smem = swt_smem_bytes();
+  const size_t smem = tc_smem_bytes();
   if (!attr) {  // both instances launched here need the large shared-memory window
-    CK(cudaFuncSetAttribute(k_band_sweep_tm<PASSES, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    CK(cudaFuncSetAttribute(k_band_sweep_tm<PASSES, false>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
-    CK(cudaFuncSetAttribute(k_band_sweep_tm<PASSES, ACC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    CK(cudaFuncSetAttribute(k_band_sweep_tm<PASSES, ACC>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    CK(cudaFuncSetAttribute(k_band_sweep_tc<PASSES, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_band_sweep_tc<PASSES, false>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    CK(cudaFuncSetAttribute(k_band_sweep_tc<PASSES, ACC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_band_sweep_tc<PASSES, ACC>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
     attr = true;
   }
-  k_band_sweep_tm<PASSES, false><<<grid, SWT_THREADS, smem, D.st>>>(td, P, B, 0, D.err, nullptr);
+  k_band_sweep_tc<PASSES, false><<<grid, SW_THREADS, smem, D.st>>>(td, P, B, 0, D.err, nullptr);
   CKL();
-  k_band_sweep_tm<PASSES, ACC><<<grid, SWT_THREADS, smem, D.st>>>(td, P, B, 1, D.err, maxabs);
+  k_band_sweep_tc<PASSES, ACC><<<grid, SW_THREADS, smem, D.st>>>(td, P, B, 1, D.err, maxabs);
   CKL();
 }
 

@@ -60,9 +60,6 @@ constexpr uint32_t SWT_TCOLS = 512;
 static_assert(SWT_ACOL + SWT_AST * 2 * TC_KC <= SWT_TCOLS, "tensor memory columns");
 constexpr size_t swt_smem_bytes() { return (size_t)SWT_PST * TC_PCHUNK * sizeof(float) + 128; }
 
-// Spin limit of the sweeps' waits (the wind-down waits use TC_SPIN_LIMIT).
-// Settable for tests of the timeout path (bddcml_set_wait_limit_c).
-static __device__ long long g_tc_wait_limit = TC_SPIN_LIMIT;
 
 // release store / acquire load of a shared-memory counter
 __device__ __forceinline__ void smem_store_release(unsigned* p, unsigned v) {

@@ -67,11 +67,15 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 }
 
 // bounded wait: returns false after the spin limit
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  for (long long i = 0; i < TC_SPIN_LIMIT; ++i)
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long long limit = TC_SPIN_LIMIT) {
+  for (long long i = 0; i < limit; ++i)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
+
+// Spin limit of the sweeps' waits (their wind-down waits use TC_SPIN_LIMIT).
+// Settable for tests of the timeout path (bddcml_set_wait_limit_c).
+static __device__ long long g_tc_wait_limit = TC_SPIN_LIMIT;
 
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
@@ -213,9 +217,10 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
 template <int PASSES, bool ACC>
 __global__ void __launch_bounds__(SW_THREADS, 2)
     k_band_sweep_tc(const TcDesc* __restrict__ td, const float* __restrict__ ppool, float* __restrict__ bpool,
-                    int dir, int* __restrict__ err) {
+                    int dir, int* __restrict__ err, int* __restrict__ maxabs) {
   constexpr int passes = PASSES;
   const TcDesc d = td[blockIdx.y];
+  const long long limit = g_tc_wait_limit;
   const int c0 = blockIdx.x * TC_M;
   if (c0 >= d.ncol || d.nb == 0) return;
   const int ld = d.ncol;
@@ -277,11 +282,11 @@ __global__ void __launch_bounds__(SW_THREADS, 2)
         const int k = row_of(sidx), b = sidx & 1;
         const int nchunk = sweep_nchunk(dir, d.nb, d.w, k);
         const uint32_t dacc = tmem + (uint32_t)(b * TC_N);
-        if (sidx >= 2 && !mbar_wait(&bar_tfree[b], (uint32_t)(((sidx - 2) >> 1) & 1))) { abort_flag = 1; break; }
+        if (sidx >= 2 && !mbar_wait(&bar_tfree[b], (uint32_t)(((sidx - 2) >> 1) & 1), limit)) { abort_flag = 1; break; }
         for (int q = 0; q < nchunk; ++q, ++g) {
           const int st = (int)(g % TC_STAGES);
           const uint32_t ph = (uint32_t)((g / TC_STAGES) & 1);
-          if (!mbar_wait(&bar_a[st], ph) || !mbar_wait(&bar_p[st], ph)) { abort_flag = 1; break; }
+          if (!mbar_wait(&bar_a[st], ph, limit) || !mbar_wait(&bar_p[st], ph, limit)) { abort_flag = 1; break; }
           tma_pending[st] = -1;
           tc_fence_after();
           const uint32_t a_hi = smem_u32(sA + (st * 2 + 0) * TC_ACHUNK);
@@ -314,7 +319,7 @@ __global__ void __launch_bounds__(SW_THREADS, 2)
             const long long gn = g + 1;
             const int st2 = (int)(gn % TC_STAGES);
             if (gn >= TC_STAGES &&
-                !mbar_wait(&bar_mma[st2], (uint32_t)(((gn - TC_STAGES) / TC_STAGES) & 1))) { abort_flag = 1; break; }
+                !mbar_wait(&bar_mma[st2], (uint32_t)(((gn - TC_STAGES) / TC_STAGES) & 1), limit)) { abort_flag = 1; break; }
             issue_panel(st2, nk, sweep_chunk(dir, d.nb, d.w, nk, nq).pq, gn);
           }
         }
@@ -337,14 +342,18 @@ __global__ void __launch_bounds__(SW_THREADS, 2)
       asm volatile("" : "+l"(lds));
       float* dst = B + (long long)(k * NB) * lds + c0 + tid;
       float* dst2 = (ACC && dir == 1 && d.oAcc >= 0) ? bpool + d.oAcc + (long long)(k * NB) * lds + c0 + tid : nullptr;
-      if (!mbar_wait(&bar_acc[b], (uint32_t)((sr >> 1) & 1))) { abort_flag = 1; return false; }
+      if (!mbar_wait(&bar_acc[b], (uint32_t)((sr >> 1) & 1), limit)) { abort_flag = 1; return false; }
       tc_fence_after();
+      float vmax = 0.f;
 #pragma unroll
       for (int part = 0; part < TC_N / 16; ++part) {
         float vv[16];
         tmem_ld16(tmem + trow + (uint32_t)(b * TC_N + part * 16), vv);
 #pragma unroll
         for (int i = 0; i < 16; ++i) dst[(long long)(part * 16 + i) * lds] = vv[i];
+        if (maxabs)
+#pragma unroll
+          for (int i = 0; i < 16; ++i) vmax = fmaxf(vmax, fabsf(vv[i]));
         if (ACC && dst2) {
           float a[16];
 #pragma unroll
@@ -352,6 +361,10 @@ __global__ void __launch_bounds__(SW_THREADS, 2)
 #pragma unroll
           for (int i = 0; i < 16; ++i) dst2[(long long)(part * 16 + i) * lds] = a[i] + vv[i];
         }
+      }
+      if (maxabs) {  // largest |result| of the system (non-negative FP32 bits order like integers)
+        for (int o = 16; o > 0; o >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+        if (lane == 0) atomicMax(maxabs + blockIdx.y, __float_as_int(vmax));
       }
       tc_fence_before();
       mbar_arrive(&bar_tfree[b]);
@@ -397,7 +410,7 @@ __global__ void __launch_bounds__(SW_THREADS, 2)
         }
         const int st = (int)(g % TC_STAGES);
         if (g >= TC_STAGES &&
-            !mbar_wait(&bar_mma[st], (uint32_t)(((g - TC_STAGES) / TC_STAGES) & 1))) { abort_flag = 1; ok = false; break; }
+            !mbar_wait(&bar_mma[st], (uint32_t)(((g - TC_STAGES) / TC_STAGES) & 1), limit)) { abort_flag = 1; ok = false; break; }
         float* ahi = sA + (st * 2 + 0) * TC_ACHUNK;
         float* alo = sA + (st * 2 + 1) * TC_ACHUNK;
         if (passes == 1) {
