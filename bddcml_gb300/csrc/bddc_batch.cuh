@@ -543,18 +543,19 @@ static void batch_interior_solve(Device& D, const double* rhs) {
   CKL();
   if constexpr (std::is_same_v<T, float>) {
     float* v = static_cast<float*>(B.vb);
-    run_solve_tc(D, B.tdv0, D.nsub, D.maxnbo, vld, D.ppool_oo, v, 3, false);
+    run_solve_tc(D, B.tdv0, D.nsub, D.maxnbo, vld, D.ppool_oo, v, 3, 0);
     const dim3 gr((D.maxNO + 7) / 8, D.nsub);
     kb_v_residual<<<gr, vld, 0, st>>>(D.ds, D.koo, B.lg, rhs, D.uo_off, B.voff, vld, v, 0, 1);
     CKL();
-    run_solve_tc(D, B.tdv1, D.nsub, D.maxnbo, vld, D.ppool_oo, v, 3, false);
+    run_solve_tc(D, B.tdv1, D.nsub, D.maxnbo, vld, D.ppool_oo, v, 3, 0);
     // as many further corrections as the setup's interior solves of the same
     // matrix needed: one one-pass correction for well-conditioned interiors,
     // else 3xTF32 corrections
     for (int step = 2; step <= D.refine_steps; ++step) {
       kb_v_residual<<<gr, vld, 0, st>>>(D.ds, D.koo, B.lg, rhs, D.uo_off, B.voff, vld, v, 1, 2);
       CKL();
-      run_solve_tc(D, B.tdv2, D.nsub, D.maxnbo, vld, D.ppool_oo, v, D.refine_onepass ? 1 : 3, true);
+      run_solve_tc(D, B.tdv2, D.nsub, D.maxnbo, vld, D.ppool_oo, v, D.refine_onepass ? 1 : 3,
+                   D.refine_onepass ? 1 : 2);
     }
   } else {
     run_solve<double>(D, B.bdv, D.nsub, D.maxnbo, vld, static_cast<const double*>(D.poolT), static_cast<double*>(B.vb));

@@ -464,33 +464,35 @@ static void run_panels(Device& D, const BandDesc* bd, const TcDesc* td, int nbat
 // one launch per direction, one CTA per (system, 128-column tile)
 // forward + backward tensor-core sweep; passes 3 (3xTF32) or 1 (TF32); with
 // acc the backward sweep also adds its result into each system's oAcc block
-template <int PASSES, bool ACC>
+template <int PASSES, int ACC>
 static void sweep_pair(Device& D, dim3 grid, const TcDesc* td, const float* P, float* B, int* maxabs) {
   static bool attr = false;
   const size_t smem = tc_smem_bytes();
   if (!attr) {  // both instances launched here need the large shared-memory window
-    CK(cudaFuncSetAttribute(k_band_sweep_tc<PASSES, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    CK(cudaFuncSetAttribute(k_band_sweep_tc<PASSES, false>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    CK(cudaFuncSetAttribute(k_band_sweep_tc<PASSES, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_band_sweep_tc<PASSES, 0>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
     CK(cudaFuncSetAttribute(k_band_sweep_tc<PASSES, ACC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     CK(cudaFuncSetAttribute(k_band_sweep_tc<PASSES, ACC>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
     attr = true;
   }
-  k_band_sweep_tc<PASSES, false><<<grid, SW_THREADS, smem, D.st>>>(td, P, B, 0, D.err, nullptr);
+  k_band_sweep_tc<PASSES, 0><<<grid, SW_THREADS, smem, D.st>>>(td, P, B, 0, D.err, nullptr);
   CKL();
   k_band_sweep_tc<PASSES, ACC><<<grid, SW_THREADS, smem, D.st>>>(td, P, B, 1, D.err, maxabs);
   CKL();
 }
 
+// acc: 0 none, 1 add into oAcc, 2 add into the renormalised pair ending at oAcc
 // maxabs (optional, one int per system): the largest |result| of each
 // system, as FP32 bits, merged into the array by atomicMax
 static void run_solve_tc(Device& D, const TcDesc* td, int nbatch, int maxnb, int maxncol, const float* P, float* B,
-                         int passes = 3, bool acc = false, int* maxabs = nullptr) {
+                         int passes = 3, int acc = 0, int* maxabs = nullptr) {
   (void)maxnb;
   dim3 grid(maxncol / TC_M, nbatch);
-  if (passes == 3 && acc) sweep_pair<3, true>(D, grid, td, P, B, maxabs);
-  else if (passes == 3) sweep_pair<3, false>(D, grid, td, P, B, maxabs);
-  else if (acc) sweep_pair<1, true>(D, grid, td, P, B, maxabs);
-  else sweep_pair<1, false>(D, grid, td, P, B, maxabs);
+  if (passes == 3 && acc == 2) sweep_pair<3, 2>(D, grid, td, P, B, maxabs);
+  else if (passes == 3 && acc == 1) sweep_pair<3, 1>(D, grid, td, P, B, maxabs);
+  else if (passes == 3) sweep_pair<3, 0>(D, grid, td, P, B, maxabs);
+  else if (acc) sweep_pair<1, 1>(D, grid, td, P, B, maxabs);
+  else sweep_pair<1, 0>(D, grid, td, P, B, maxabs);
 }
 
 template <typename T>
@@ -806,7 +808,7 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
   D.prof.begin(PH_SOLVE_OO, st);
   k_fill_rhs<T><<<dim3((D.maxNO + 127) / 128, nsub), 128, 0, st>>>(D.ds, D.koi, D.fo, D.fo_off, poolT);
   CKL();
-  if constexpr (std::is_same_v<T, float>) run_solve_tc(D, td_oo, nsub, D.maxnbo, D.maxNR, ppool, poolT, 3, false, dmax);
+  if constexpr (std::is_same_v<T, float>) run_solve_tc(D, td_oo, nsub, D.maxnbo, D.maxNR, ppool, poolT, 3, 0, dmax);
   else run_solve<T>(D, D.bd_oo, nsub, D.maxnbo, D.maxNR, poolT, poolT, D.bdu_oo);
   D.prof.end(PH_SOLVE_OO, st);
   // Mixed precision: refinement with FP64-accurate residuals until the
@@ -851,7 +853,7 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
     CKL();
     D.prof.end(PH_RESIDUAL, st);
     D.prof.begin(PH_SOLVE_OO, st);
-    run_solve_tc(D, tds(1, -1), nsub, D.maxnbo, D.maxNR, ppool, poolT, 3, false, dmax + nsub);
+    run_solve_tc(D, tds(1, -1), nsub, D.maxnbo, D.maxNR, ppool, poolT, 3, 0, dmax + nsub);
     D.prof.end(PH_SOLVE_OO, st);
     const float r1 = ratio(1);
     float rl = r1;
@@ -862,7 +864,7 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
       CKL();
       D.prof.end(PH_RESIDUAL, st);
       D.prof.begin(PH_SOLVE_OO, st);
-      run_solve_tc(D, tds(2, 1), nsub, D.maxnbo, D.maxNR, ppool, poolT, 1, true, dmax + 2 * nsub);
+      run_solve_tc(D, tds(2, 1), nsub, D.maxnbo, D.maxNR, ppool, poolT, 1, 1, dmax + 2 * nsub);
       D.prof.end(PH_SOLVE_OO, st);
       rl = ratio(2);
       steps = 2;
@@ -878,7 +880,7 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
         D.prof.end(PH_RESIDUAL, st);
         D.prof.begin(PH_SOLVE_OO, st);
         CK(cudaMemsetAsync(dmax + 2 * nsub, 0, (size_t)nsub * sizeof(int), st));
-        run_solve_tc(D, tdc, nsub, D.maxnbo, D.maxNR, ppool, poolT, 3, true, dmax + 2 * nsub);
+        run_solve_tc(D, tdc, nsub, D.maxnbo, D.maxNR, ppool, poolT, 3, 2, dmax + 2 * nsub);
         D.prof.end(PH_SOLVE_OO, st);
         rl = ratio(2);
         steps = step;

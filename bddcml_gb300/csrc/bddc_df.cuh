@@ -29,7 +29,8 @@ struct dfacc {
     s = t;
     c += e;
   }
-  // += a * x with a, x double-float (a.lo*x.lo dropped, relative 2^-48)
+  // += a * x with a, x double-float (a.lo*x.lo dropped, relative 2^-48 when x
+  // is normalised, |x.lo| <= 2^-24 |x.hi|)
   __device__ __forceinline__ void fma_df(dfloat a, dfloat x) {
     float p = a.hi * x.hi;
     float e = fmaf(a.hi, x.hi, -p);

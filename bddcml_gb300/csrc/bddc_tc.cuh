@@ -214,7 +214,10 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
-template <int PASSES, bool ACC>
+// ACC: 0 none; 1 the backward sweep adds its result into the block at oAcc;
+// 2 likewise, into the FP32 pair (block at oAcc - one component, block at
+// oAcc) kept renormalised
+template <int PASSES, int ACC>
 __global__ void __launch_bounds__(SW_THREADS, 2)
     k_band_sweep_tc(const TcDesc* __restrict__ td, const float* __restrict__ ppool, float* __restrict__ bpool,
                     int dir, int* __restrict__ err, int* __restrict__ maxabs) {
@@ -358,8 +361,23 @@ __global__ void __launch_bounds__(SW_THREADS, 2)
           float a[16];
 #pragma unroll
           for (int i = 0; i < 16; ++i) a[i] = dst2[(long long)(part * 16 + i) * lds];
+          if (ACC == 2) {
+            // (X0, X1) += D as a renormalised pair: X0 + (X1 + D) by an
+            // error-free two-sum, so X1 stays below 2^-24 |X0| and the pair
+            // keeps 48 bits however many corrections it collects
+            float* dst0 = dst2 - (long long)d.nb * NB * lds;
 #pragma unroll
-          for (int i = 0; i < 16; ++i) dst2[(long long)(part * 16 + i) * lds] = a[i] + vv[i];
+            for (int i = 0; i < 16; ++i) {
+              const float x0 = dst0[(long long)(part * 16 + i) * lds];
+              const float y = a[i] + vv[i];
+              const float s = x0 + y, bb = s - x0;
+              dst0[(long long)(part * 16 + i) * lds] = s;
+              dst2[(long long)(part * 16 + i) * lds] = (x0 - (s - bb)) + (y - bb);
+            }
+          } else {
+#pragma unroll
+            for (int i = 0; i < 16; ++i) dst2[(long long)(part * 16 + i) * lds] = a[i] + vv[i];
+          }
         }
       }
       if (maxabs) {  // largest |result| of the system (non-negative FP32 bits order like integers)
