@@ -28,7 +28,7 @@ SOURCES = [
 ]
 HEADERS = ["bddc_internal.hpp", "bddc_kernels.cuh", "bddc_df.cuh", "bddc_setup_kernels.cuh",
            "bddc_pcg_kernels.cuh", "bddc_tc.cuh", "bddc_adaptive.cuh", "bddc_batch_kernels.cuh",
-           "bddc_batch.cuh", "bddc_ozaki.cuh", "bddc_batch_tc.cuh", "bddc_sweep.cuh"]
+           "bddc_batch.cuh", "bddc_ozaki.cuh", "bddc_batch_tc.cuh"]
 
 
 def _nvcc() -> str:

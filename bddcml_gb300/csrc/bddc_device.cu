@@ -22,7 +22,6 @@
 #include "bddc_internal.hpp"
 #include "bddc_pcg_kernels.cuh"
 #include "bddc_tc.cuh"
-#include "bddc_sweep.cuh"
 
 namespace bddc {
 
