@@ -32,7 +32,7 @@ STAT_FIELDS = ["t_host_setup", "t_device_setup", "t_solve", "t_iterations", "t_p
                "launches_setup", "launches_solve", "t_dev_alloc", "t_dev_h2d", "npair", "nadaptive",
                "adapt_est", "t_adaptive", "lobpcg_resid", "lobpcg_iter", "batch_bytes_schur",
                "batch_flop_schur_mma", "batch_flop_schur", "batch_flop_pc", "batch_nk",
-               "bytes_assemble_dot", "bytes_assemble_z", "bytes_coarse_apply", "refine_steps"]
+               "bytes_assemble_dot", "bytes_assemble_z", "bytes_coarse_apply", "refine_steps", "band_w"]
 
 EXPORTS = ["bddcml_init_c", "bddcml_upload_global_data_c", "bddcml_upload_subdomain_data_c",
            "bddcml_setup_preconditioner_c", "bddcml_solve_c", "bddcml_download_local_solution_c",
@@ -286,7 +286,10 @@ def bddcml_solve_batch(nrhs: int, comm_all=0, method=0, tol=1e-8, maxit=1000, nd
 
 
 def set_batch_operator(mode: int) -> None:
-    """Batched Schur apply in mixed mode: 1 sliced bf16 tensor cores (default), 0 double-float SIMT."""
+    """Products of the batched solve in mixed mode: -1 automatic (default), 0 SIMT
+    (double-float Schur apply, FP32 preconditioner), 1 sliced bf16 tensor-core Schur
+    apply with 3xTF32 preconditioner products, 2 sliced Schur apply and sliced
+    (exact) preconditioner products."""
     lib().bddcml_set_batch_operator_c(_i(mode))
     _check()
 

@@ -364,7 +364,7 @@ void bddcml_set_batch_operator_c(int* mode) {
   guarded("bddcml_set_batch_operator_c", [&] {
     Solver* S = need_solver("bddcml_set_batch_operator_c");
     if (!S) return;
-    if (*mode != 0 && *mode != 1) throw Error{ERR_ARGUMENT, "batch operator mode must be 0 or 1"};
+    if (*mode < -1 || *mode > 2) throw Error{ERR_ARGUMENT, "batch operator mode must be -1, 0, 1 or 2"};
     S->prm.batch_operator = *mode;
   });
 }
@@ -599,7 +599,7 @@ void bddcml_get_stats_c(double* stats, int* lstats) {
                   q.launches_setup, q.launches_solve, q.t_dev_alloc, q.t_dev_h2d, (double)q.npair,
                   (double)q.nadaptive, q.adapt_est, q.t_adaptive, q.lobpcg_resid, (double)q.lobpcg_iter,
                   q.batch_bytes_schur, q.batch_flop_schur_mma, q.batch_flop_schur, q.batch_flop_pc, q.batch_nk,
-                  q.bytes_assemble_dot, q.bytes_assemble_z, q.bytes_coarse_apply, q.refine_steps};
+                  q.bytes_assemble_dot, q.bytes_assemble_z, q.bytes_coarse_apply, q.refine_steps, q.band_w};
     int n = std::min<int>(*lstats, (int)(sizeof(v) / sizeof(v[0])));
     for (int i = 0; i < n; ++i) stats[i] = v[i];
     *lstats = n;

@@ -130,6 +130,121 @@ static void batch_prepare_tc(Device& D) {
   }
 }
 
+// Sliced preconditioner blocks for exact products (bddc_ozaki.cuh), made once
+// per batch setup: Z and Phi from the preconditioner pool, Phi^T from phit
+// (offsets opt), with their job lists.  The application reuses the Schur
+// apply's X slice buffers for w .* r and slices the coarse solution into ozp_u.
+static void batch_prepare_ozpc(Device& D, const vector<long long>& opt) {
+  BatchBufs& B = D.bt;
+  auto& mem = B.mem;
+  const int nsub = D.nsub;
+  const bool coarse = D.ndofc > 0;
+  int dev = 0, nsm = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  auto nchk = [](int k) { return (k + OZ_KC - 1) / OZ_KC; };
+  auto ntile = [](int m) { return (m + OZ_M - 1) / OZ_M; };
+  const long long blk = (long long)OZ_NA * OZ_AB;  // bf16 elements of one sliced 128 x 64 chunk
+  vector<OzMat> mpc, mpt;                          // from the preconditioner pool / from phit
+  vector<long long> sz(nsub, 0), sphi(nsub, 0), spt(nsub, 0), ez(nsub, 0), ephi(nsub, 0), ept(nsub, 0);
+  vector<long long> xo(nsub, 0), uo(nsub, 0);
+  long long ns = 0, ne = 0, nx = 0, nu = 0, ncon = 0, nptile = 0;
+  int nchu = 0, blk_pc = 0, rows_pc = 0, blk_pt = 0, rows_pt = 0;
+  for (int t = 0; t < nsub; ++t) {
+    const DevSub& d = D.hs[t];
+    ncon = std::max(ncon, (long long)d.coff + d.nc);
+    xo[t] = nx;  // the layout of the Schur apply's X slices (batch_prepare_oz)
+    nx += (long long)nchk(d.ni) * OZ_BB;
+    const int nc = coarse ? d.nc : 0;
+    uo[t] = nu;
+    nu += (long long)nchk(nc) * OZ_BB;
+    nchu = std::max(nchu, nchk(nc));
+    sz[t] = ns;
+    ns += (long long)ntile(d.ni) * nchk(d.ni) * blk;
+    ez[t] = ne;
+    ne += (long long)ntile(d.ni) * OZ_M;
+    mpc.push_back(OzMat{d.oZ, sz[t], ez[t], d.NI, d.ni, d.ni});
+    blk_pc = std::max(blk_pc, ntile(d.ni) * nchk(d.ni));
+    rows_pc = std::max(rows_pc, ntile(d.ni) * OZ_M);
+    if (nc > 0 && d.ni > 0) {
+      sphi[t] = ns;
+      ns += (long long)ntile(d.ni) * nchk(nc) * blk;
+      ephi[t] = ne;
+      ne += (long long)ntile(d.ni) * OZ_M;
+      mpc.push_back(OzMat{d.oPhi, sphi[t], ephi[t], d.ncp, d.ni, nc});
+      spt[t] = ns;
+      ns += (long long)ntile(nc) * nchk(d.ni) * blk;
+      ept[t] = ne;
+      ne += (long long)ntile(nc) * OZ_M;
+      mpt.push_back(OzMat{opt[t], spt[t], ept[t], d.NI, nc, d.ni});
+      blk_pt = std::max(blk_pt, ntile(nc) * nchk(d.ni));
+      rows_pt = std::max(rows_pt, ntile(nc) * OZ_M);
+      nptile += ntile(nc);
+    }
+  }
+  B.ozp_a = dalloc<__nv_bfloat16>(std::max(1LL, ns), mem);
+  B.ozp_erow = dalloc<int>(std::max(1LL, ne), mem);
+  B.ozp_u = dalloc<__nv_bfloat16>(std::max(1LL, nu), mem);
+  B.ozp_fu = dalloc<int>((long long)nsub * BMAX, mem);
+  B.ozp_uoff = upload(uo, mem, D.st);
+  B.ozp_nchu = nchu;
+  auto slice = [&](const vector<OzMat>& mats, const float* pool, int rows, int blocks) {
+    if (mats.empty() || blocks == 0) return;
+    const OzMat* dm = upload(mats, mem, D.st);
+    kb_oz_row_exp_a<<<dim3((rows + 7) / 8, (unsigned)mats.size()), 256, 0, D.st>>>(dm, pool, B.ozp_erow);
+    CKL();
+    kb_oz_slice_a<<<dim3(blocks, (unsigned)mats.size()), 256, 0, D.st>>>(dm, pool, B.ozp_erow, B.ozp_a);
+    CKL();
+  };
+  slice(mpc, static_cast<const float*>(D.poolPC), rows_pc, blk_pc);
+  slice(mpt, static_cast<const float*>(B.phit), rows_pt, blk_pt);
+  // Phi^T products split along K so that the job list fills the SMs several times over
+  const int ks = nptile > 0 ? (int)std::min<long long>(8, std::max<long long>(1, (8LL * nsm + nptile - 1) / nptile)) : 1;
+  vector<OzJob> jz, ju, jp;
+  for (int t = 0; t < nsub; ++t) {
+    const DevSub& d = D.hs[t];
+    const int nc = coarse ? d.nc : 0, n1 = nchk(d.ni);
+    for (int rt = 0; rt < ntile(d.ni); ++rt) {
+      const int m = std::min(OZ_M, d.ni - rt * OZ_M);
+      jz.push_back(OzJob{sz[t] + rt * n1 * blk, ez[t] + rt * OZ_M, xo[t], (long long)d.rep + rt * OZ_M, t * BMAX, m,
+                         n1, 0});
+      if (nc > 0)
+        ju.push_back(OzJob{sphi[t] + rt * nchk(nc) * blk, ephi[t] + rt * OZ_M, uo[t], (long long)d.rep + rt * OZ_M,
+                           t * BMAX, m, nchk(nc), 1});
+    }
+    if (nc > 0 && d.ni > 0)
+      for (int rt = 0; rt < ntile(nc); ++rt)
+        for (int h = 0; h < ks; ++h) {  // part h: chunks [c0, c1) into plane h
+          const int c0 = (int)((long long)n1 * h / ks), c1 = (int)((long long)n1 * (h + 1) / ks);
+          if (c1 > c0)
+            jp.push_back(OzJob{spt[t] + ((long long)rt * n1 + c0) * blk, ept[t] + rt * OZ_M, xo[t] + c0 * OZ_BB,
+                               h * ncon + d.coff + rt * OZ_M, t * BMAX, std::min(OZ_M, nc - rt * OZ_M), c1 - c0,
+                               0});
+        }
+  }
+  B.ozp_jz = jz.empty() ? nullptr : upload(jz, mem, D.st);
+  B.ozp_ju = ju.empty() ? nullptr : upload(ju, mem, D.st);
+  B.ozp_jp = jp.empty() ? nullptr : upload(jp, mem, D.st);
+  B.ozp_njz = (int)jz.size();
+  B.ozp_nju = (int)ju.size();
+  B.ozp_njp = (int)jp.size();
+  B.tc_ks = ks;
+  B.tc_pstride = std::max(1LL, ncon) * B.nk;
+  B.tc_rcs = dalloc<double>(ks * B.tc_pstride, mem);
+  // planes that no job writes (a subdomain with fewer K chunks than parts) stay zero
+  CK(cudaMemsetAsync(B.tc_rcs, 0, (size_t)ks * B.tc_pstride * sizeof(double), D.st));
+  B.ozpc = true;
+}
+
+// out rows of every job (+)= the sliced A tile x the X chunks (kb_gemm_oz)
+static void gemm_oz(Device& D, const OzJob* jobs, int njobs, const __nv_bfloat16* x, const int* fcol, double* out) {
+  if (njobs <= 0) return;
+  raise_smem(kb_gemm_oz, OZ_SMEM);
+  kb_gemm_oz<<<njobs, OZ_THREADS, OZ_SMEM, D.st>>>(jobs, D.bt.ozp_a, D.bt.ozp_erow, x, fcol, out, D.bt.nk, D.err,
+                                                   D.bt.ndone);
+  CKL();
+}
+
 // out rows of every job = A tile rows x the B chunks (kb_gemm_tc3)
 static void gemm_tc(Device& D, const TcJob* jobs, int njobs, const float* At, double* out, int nk,
                     const int* ndone) {
@@ -197,13 +312,20 @@ static void batch_prepare(Device& D, int nk, int lg, int maxit, int* shared_ndon
                           bool l2df = false) {
   BatchBufs& B = D.bt;
   const int ldh = std::max(maxit + 2, 2);
+  // mixed level 1: op 1 slices the Schur operator (bf16 tensor cores) and runs the
+  // preconditioner products as 3xTF32, op 2 slices both, op 0 runs both on the
+  // SIMT pipes; op -1 takes 2 for stiff interiors (those that needed the
+  // multi-step refinement), where rounding noise in the preconditioner costs
+  // outer iterations, and 1 otherwise
+  if (op < 0) op = D.refine_onepass ? 1 : 2;
   bool want_oz = false;
-  if (D.mixed && !level2 && op == 1) {
+  if (D.mixed && !level2 && op >= 1) {
     want_oz = true;
     for (auto& d : D.hs) want_oz = want_oz && d.ni <= OZ_KMAX;
   }
+  const bool want_ozpc = want_oz && op == 2;
   if (B.nk == nk && B.ldh >= ldh && (shared_ndone == nullptr || B.ndone == shared_ndone) && B.oz == want_oz &&
-      B.l2df == (level2 && l2df))
+      B.ozpc == want_ozpc && B.l2df == (level2 && l2df))
     return;
   D.release_batch();
   auto& mem = B.mem;
@@ -303,7 +425,10 @@ static void batch_prepare(Device& D, int nk, int lg, int maxit, int* shared_ndon
   }
   if (want_oz) {
     batch_prepare_oz(D);
-    if constexpr (std::is_same_v<T, float>) batch_prepare_tc(D);
+    if constexpr (std::is_same_v<T, float>) {
+      if (want_ozpc) batch_prepare_ozpc(D, opt);
+      else batch_prepare_tc(D);
+    }
   }
   if (!level2) {  // multi-column interior solves of the loads and of the interior resolve
     const int vld = D.mixed ? TC_M : NB;
@@ -352,10 +477,10 @@ static void batch_schur(Device& D, const double* vin, double* vout, bool zero_fi
   const dim3 grid((D.maxNI + GM - 1) / GM, D.nsub);
   D.prof.begin(PH_SCHUR_APPLY, st);
   if (B.oz) {
-    kb_oz_col_exp<<<D.nsub, 256, 0, st>>>(D.ds, B.lg, D.uniq, vin, B.oz_fcol, B.ndone);
+    kb_oz_col_exp<<<D.nsub, 256, 0, st>>>(D.ds, B.lg, 0, D.uniq, nullptr, vin, B.oz_fcol, B.ndone);
     CKL();
-    kb_oz_slice_x<<<dim3(B.oz_nch, D.nsub), 256, 0, st>>>(D.ds, B.lg, D.uniq, vin, B.oz_fcol, B.oz_xoff, B.oz_x,
-                                                          B.ndone);
+    kb_oz_slice_x<<<dim3(B.oz_nch, D.nsub), 256, 0, st>>>(D.ds, B.lg, 0, D.uniq, nullptr, vin, B.oz_fcol, B.oz_xoff,
+                                                          B.oz_x, B.ndone);
     CKL();
     raise_smem(kb_schur_oz, OZ_SMEM);
     kb_schur_oz<<<dim3(B.oz_nrt, D.nsub), OZ_THREADS, OZ_SMEM, st>>>(D.ds, B.oz_s, B.oz_soff, B.oz_eoff, B.oz_erow,
@@ -396,12 +521,19 @@ static void batch_pc(Device& D, const double* rin, double* zout, double* part) {
   // with the sliced Schur operator the FP32 products run on the tensor cores
   // (3xTF32) from pre-tiled A and the split B chunks, else on the FP32 SIMT pipes
   const bool tc = std::is_same_v<T, float> && B.tc_az != nullptr;
+  // or with sliced blocks: FP64-exact products on the bf16 tensor cores
+  const bool ozpc = std::is_same_v<T, float> && B.ozpc;
   // the level-2 device of a mixed level 1 runs its products as double-float
   const bool df = std::is_same_v<T, double> && B.l2df;
   float2* auxf = static_cast<float2*>(B.aux);
   float2* ucf = static_cast<float2*>(B.ucs);
   D.prof.begin(PH_PC_LOCAL, st);
-  if (tc) {
+  if (ozpc) {
+    kb_oz_col_exp<<<D.nsub, 256, 0, st>>>(D.ds, lg, 0, D.uniq, D.wrep, rin, B.oz_fcol, B.ndone);
+    CKL();
+    kb_oz_slice_x<<<dim3(B.oz_nch, D.nsub), 256, 0, st>>>(D.ds, lg, 0, D.uniq, D.wrep, rin, B.oz_fcol, B.oz_xoff,
+                                                          B.oz_x, B.ndone);
+  } else if (tc) {
     kb_tile_b<<<dim3(B.tc_mch1, D.nsub), 256, 0, st>>>(1, D.ds, B.tc_boff, lg, D.uniq, D.wrep, rin, B.tc_b,
                                                         B.ndone);
   } else if (df) {
@@ -413,7 +545,9 @@ static void batch_pc(Device& D, const double* rin, double* zout, double* part) {
   }
   CKL();
   if (D.ndofc > 0) {
-    if (tc)
+    if (ozpc)
+      gemm_oz(D, B.ozp_jp, B.ozp_njp, B.oz_x, B.oz_fcol, B.tc_rcs);
+    else if (tc)
       gemm_tc(D, B.tc_jp, B.tc_njp, B.tc_ap, B.tc_rcs, nk, B.ndone);
     else if (df)
       gemm_df(D, B.dP, D.nsub, D.ncpmax, B.df_phit, auxf, B.rcs, nullptr, nk, nk, B.ndone);
@@ -421,9 +555,10 @@ static void batch_pc(Device& D, const double* rin, double* zout, double* part) {
       gemm_t<T>(D, B.gP, D.nsub, D.ncpmax, static_cast<const T*>(B.phit), aux, nullptr, nk, B.rcs, nullptr, nk, nk,
                 B.ndone);
     kb_coarse_gather<<<blocks_for((long long)D.ndofc << lg), 256, 0, st>>>(D.ndofc, lg, D.co_ptr, D.co_sub,
-                                                                           D.co_loc, D.ds, tc ? B.tc_rcs : B.rcs,
-                                                                           B.rc, B.ndone, tc ? B.tc_ks : 1,
-                                                                           tc ? B.tc_pstride : 0);
+                                                                           D.co_loc, D.ds,
+                                                                           tc || ozpc ? B.tc_rcs : B.rcs, B.rc,
+                                                                           B.ndone, tc || ozpc ? B.tc_ks : 1,
+                                                                           tc || ozpc ? B.tc_pstride : 0);
     CKL();
     if (D.lev2) {
       batch_level2(D, B.rc, B.uc);
@@ -449,7 +584,15 @@ static void batch_pc(Device& D, const double* rin, double* zout, double* part) {
       if (D.coarse64) coarse(double{});
       else coarse(T{});
     }
-    if (tc) {
+    if (ozpc) {
+      if (B.ozp_nchu > 0) {
+        kb_oz_col_exp<<<D.nsub, 256, 0, st>>>(D.ds, lg, 1, D.cmap, nullptr, B.uc, B.ozp_fu, B.ndone);
+        CKL();
+        kb_oz_slice_x<<<dim3(B.ozp_nchu, D.nsub), 256, 0, st>>>(D.ds, lg, 1, D.cmap, nullptr, B.uc, B.ozp_fu,
+                                                                B.ozp_uoff, B.ozp_u, B.ndone);
+        CKL();
+      }
+    } else if (tc) {
       if (B.tc_mch2 > 0) {
         kb_tile_b<<<dim3(B.tc_mch2, D.nsub), 256, 0, st>>>(2, D.ds, B.tc_boff, lg, D.cmap, nullptr, B.uc, B.tc_b,
                                                             B.ndone);
@@ -466,7 +609,10 @@ static void batch_pc(Device& D, const double* rin, double* zout, double* part) {
     }
   }
   // zrep = Z_s W_s r_s + Phi_s uc_s in one product per subdomain
-  if (tc) {
+  if (ozpc) {
+    gemm_oz(D, B.ozp_jz, B.ozp_njz, B.oz_x, B.oz_fcol, B.zrep);
+    gemm_oz(D, B.ozp_ju, B.ozp_nju, B.ozp_u, B.ozp_fu, B.zrep);
+  } else if (tc) {
     gemm_tc(D, B.tc_jz, B.tc_njz, B.tc_az, B.zrep, nk, B.ndone);
   } else if (df) {
     gemm_df(D, B.dZ1, D.nsub, D.maxNI, B.df_pc, auxf, B.zrep, nullptr, nk, nk, B.ndone);

@@ -202,6 +202,16 @@ struct BatchBufs {
   int tc_ks = 1;                 // K parts of the Phi^T product, each writing its own plane of tc_rcs
   long long tc_pstride = 0;      // doubles between the planes
   double* tc_rcs = nullptr;
+  // or the preconditioner products with sliced blocks (bddc_ozaki.cuh): slices of
+  // Z, Phi and Phi^T, their row exponents, the sliced coarse solution of one
+  // application, and the job lists (Phi^T r into the tc_rcs planes, Z r, + Phi u_c)
+  bool ozpc = false;
+  __nv_bfloat16 *ozp_a = nullptr, *ozp_u = nullptr;
+  int *ozp_erow = nullptr, *ozp_fu = nullptr;
+  long long* ozp_uoff = nullptr;
+  int ozp_nchu = 0;
+  OzJob *ozp_jp = nullptr, *ozp_jz = nullptr, *ozp_ju = nullptr;
+  int ozp_njp = 0, ozp_njz = 0, ozp_nju = 0;
   // level-2 device only: interior loads, assembled reduced rhs, interior solutions (rows of
   // BMAX columns)
   double *fo = nullptr, *fi = nullptr, *g = nullptr, *bb = nullptr;
@@ -252,6 +262,8 @@ class Device {
   // vectors
   double *x = nullptr, *r = nullptr, *p = nullptr, *ap = nullptr, *z = nullptr, *g = nullptr;
   double *yrep = nullptr, *zrep = nullptr, *grep = nullptr, *fi = nullptr, *fo = nullptr;
+  double* zw = nullptr;  // weighted subdomain corrections w (z_s + Phi_s u_c) of one application
+  float2* cvdf = nullptr;  // the coarse-solve operand as double-float pairs (FP32 coarse inverse)
   long long* fo_off = nullptr;
   double *rcpart = nullptr, *rc = nullptr, *uc = nullptr, *cres = nullptr;
   void* cinv = nullptr;            // explicit coarse inverse (factor precision, or FP64 with coarse64), ldc x ldc
@@ -741,6 +753,7 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
   D.x = dalloc<double>(D.n, own); D.r = dalloc<double>(D.n, own); D.p = dalloc<double>(D.n, own);
   D.ap = dalloc<double>(D.n, own); D.z = dalloc<double>(D.n, own); D.g = dalloc<double>(D.n, own);
   D.yrep = dalloc<double>(D.nrep, own); D.zrep = dalloc<double>(D.nrep, own); D.grep = dalloc<double>(D.nrep, own);
+  D.zw = dalloc<double>(D.nrep, own);
   CK(cudaMemsetAsync(D.yrep, 0, D.nrep * sizeof(double), st));
   CK(cudaMemsetAsync(D.zrep, 0, D.nrep * sizeof(double), st));
   CK(cudaMemsetAsync(D.grep, 0, D.nrep * sizeof(double), st));
@@ -815,14 +828,12 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
   // each step contracts the error by about kappa(A_oo) eps_fp32):
   //   R0 = [A_oi | f_o] - A_oo X0 in double-float -> component 1 (and 2),
   //   D1 = A_oo^-1 R0 in place (3xTF32), r1 = max|D1| / max|X0|.
-  //   If r1 <= 1e-5 (well-conditioned interiors): R1 = R0 - A_oo D1 in FP32
-  //     (R1 ~ r1 R0, so FP32 rounding leaves it within ~1 %) -> component 2,
-  //     D2 = A_oo^-1 R1 with one TF32 pass, added into D1: the result is
-  //     accurate to ~r1^2 x 1e-2.
+  //   If r1 <= 1e-5 (well-conditioned interiors) X0 + D1 is accurate to about
+  //     r1^2 <= 1e-10 and the refinement stops.
   //   Otherwise: residuals of the pair X0 + D in double-float and 3xTF32
-  //     corrections added into D, until max|correction| / max|X0| <= 1e-12
-  //     (at most 13 corrections).
-  // X is the unnormalised FP32 pair (X0, D) in components 0 and 1.
+  //     corrections added into the pair (renormalised), until
+  //     max|correction| / max|X0| <= 1e-12 (at most 13 corrections).
+  // X is the FP32 pair (X0, D) in components 0 and 1.
   if constexpr (std::is_same_v<T, float>) {
     auto ratio = [&](int slot) {
       vector<int> hmax((size_t)nsub * 8);
@@ -858,15 +869,10 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
     float rl = r1;
     int steps = 1;
     if (r1 <= 1e-5f) {
-      D.prof.begin(PH_RESIDUAL, st);
-      k_residual_update_f32<<<gres, 128, 0, st>>>(D.ds, D.koo, poolT, 1, 2);
-      CKL();
-      D.prof.end(PH_RESIDUAL, st);
-      D.prof.begin(PH_SOLVE_OO, st);
-      run_solve_tc(D, tds(2, 1), nsub, D.maxnbo, D.maxNR, ppool, poolT, 1, 1, dmax + 2 * nsub);
-      D.prof.end(PH_SOLVE_OO, st);
-      rl = ratio(2);
-      steps = 2;
+      // Well-conditioned interiors (Poisson: r1 = 8e-6 at 16^3): a 3xTF32 solve
+      // is accurate to about r1 of its result, so the error left in X0 + D1 is
+      // about r1^2 <= 1e-10 of X, three orders below what the 1e-7 solution
+      // tolerance of the mixed path needs; no further correction is made.
     } else {
       // The contraction per step is about kappa(A_oo) u with u ~ 2^-21 for the
       // 3xTF32 sweeps (two TF32 halves per operand, the lo x lo term dropped):
@@ -1028,9 +1034,10 @@ static void setup_precond(Solver& S, Device& D) {
   //   assemble_dot: per replicated dof its value and owner record (rep index), per
   //     unique dof the owner pointer, the fixed flag, the weight sum, the dot vector
   //     and the result;
-  //   assemble_z: per replicated dof z_s, w_s, the owner record (rep, sub, loc) and
-  //     the dof's row of Phi (ncp entries) with the coarse map; per unique dof the
-  //     owner pointer, r, the weight sum and the result;
+  //   assemble_z: per replicated dof z_s, w_s, its row of Phi (ncp entries), the
+  //     weighted correction written and read back with its owner index, the
+  //     coarse map per constraint; per unique dof the owner pointer, r, the
+  //     weight sum and the result;
   //   coarse_apply: the coarse partials of every subdomain row block, the explicit
   //     inverse three times and the sparse coarse matrix twice.
   {
@@ -1041,7 +1048,7 @@ static void setup_precond(Solver& S, Device& D) {
     }
     const double n = D.n;
     S.stats.bytes_assemble_dot = nrep * (8.0 + 4.0) + n * (4.0 + 4.0 + 8.0 + 8.0 + 8.0);
-    S.stats.bytes_assemble_z = nrep * (8.0 + 8.0 + 12.0) + zrow + n * (4.0 + 8.0 + 8.0 + 8.0);
+    S.stats.bytes_assemble_z = nrep * (8.0 + 8.0 + 8.0 + 4.0 + 8.0) + zrow + n * (4.0 + 8.0 + 8.0 + 8.0);
     (void)nnzc;
   }
   T* poolP = dalloc<T>(oP, own);
@@ -1212,9 +1219,15 @@ static void setup_precond(Solver& S, Device& D) {
     D.ac_val = dalloc<double>(acol.size(), own);
     // factor and explicit inverse in factor precision; an FP32 factorisation
     // that meets a non-positive pivot (a coarse problem too ill-conditioned
-    // for FP32) is redone in FP64
+    // for FP32) is redone in FP64.  Interiors that needed the multi-step
+    // refinement (stiff inclusions) take the FP64 route at once: their FP32
+    // coarse data loses accuracy even when the FP32 factorisation goes through.
     D.coarse64 = false;
-    if (!coarse_factor<T>(D, nc_g, nbc, dcptr, dcontrib, own) && std::is_same_v<T, float>) {
+    const bool stiff = std::is_same_v<T, float> && !D.refine_onepass;
+    const bool factored = !stiff && coarse_factor<T>(D, nc_g, nbc, dcptr, dcontrib, own);
+    if (!factored && !std::is_same_v<T, float>)
+      throw Error{ERR_NUMERIC, "non-positive pivot in the FP64 coarse factorisation"};
+    if (!factored) {
       // The local coarse matrices G^-1 - rho D^2 come from FP32 factors and can
       // lose their small eigenvalues to cancellation on ill-conditioned
       // subdomains: take Phi^T S Phi with FP64-accurate products instead
@@ -1242,6 +1255,7 @@ static void setup_precond(Solver& S, Device& D) {
         throw Error{ERR_NUMERIC, "non-positive pivot in the FP64 coarse factorisation"};
     }
     D.cres = dalloc<double>(std::max(1, nc_g), own);
+    D.cvdf = dalloc<float2>(std::max(1, nc_g), own);
     {
       double parts = 0;
       for (auto& d : D.hs) parts += (double)D.nrb * d.nc;
@@ -1696,29 +1710,41 @@ static void launch_pc(Device& D, const double* rin, double* zout, const PcgCtl* 
     level2_apply(D, D.rc, D.uc);
   } else if (D.ndofc > 0) {
     D.prof.begin(PH_COARSE_APPLY, D.st);
+    // FP32 inverse: its operand also as double-float pairs (in vdf)
+    float2* vdf = (!D.coarse64 && std::is_same_v<T, float>) ? D.cvdf : nullptr;
     k_coarse_gather<<<(D.ndofc + 255) / 256, 256, 0, D.st>>>(D.ndofc, D.co_ptr, D.co_sub, D.co_loc, D.ds, D.rcpart,
-                                                           D.nrb, D.ncpmax, D.rc, ctl);
+                                                           D.nrb, D.ncpmax, D.rc, ctl, vdf);
     CKL();
     int gb = (D.ndofc + 7) / 8;
     auto gemv = [&](const double* v, int mode) {
       if (D.coarse64)
-        k_coarse_gemv<double><<<gb, 256, 0, D.st>>>(D.ndofc, D.ldc, static_cast<const double*>(D.cinv), v, D.uc,
-                                                     mode, ctl);
+        k_coarse_gemv<double><<<gb, 256, 0, D.st>>>(D.ndofc, D.ldc, static_cast<const double*>(D.cinv), v, nullptr,
+                                                     D.uc, mode, ctl);
       else
-        k_coarse_gemv<T><<<gb, 256, 0, D.st>>>(D.ndofc, D.ldc, static_cast<const T*>(D.cinv), v, D.uc, mode, ctl);
+        k_coarse_gemv<T><<<gb, 256, 0, D.st>>>(D.ndofc, D.ldc, static_cast<const T*>(D.cinv), v, vdf, D.uc, mode,
+                                               ctl);
     };
     gemv(D.rc, 0);
     for (int rr = 0; rr < 2; ++rr) {
       k_coarse_residual<<<(D.ndofc + 255) / 256, 256, 0, D.st>>>(D.ndofc, D.ac_ptr, D.ac_col, D.ac_val, D.rc, D.uc,
-                                                               D.cres, ctl);
+                                                               D.cres, ctl, vdf);
       gemv(D.cres, 1);
     }
     CKL();
     D.prof.end(PH_COARSE_APPLY, D.st);
   }
   D.prof.begin(PH_ASSEMBLE_Z, D.st);
-  k_assemble_z<T><<<D.npart, RT, 0, D.st>>>(D.n, D.own, D.ds, static_cast<const T*>(D.poolPC), D.zrep, D.wrep,
-                                            D.cmap, D.uc, D.wsum, rin, zout, D.part, ctl);
+  const size_t zsm = (size_t)D.ncpmax * sizeof(typename PcVec<T>::type) + (size_t)ZP_ROWS * (D.ncpmax + 1) * sizeof(T);
+  if (zsm <= 200 * 1024) {  // weighted corrections per subdomain row, then the sum per unique dof
+    raise_smem(k_zphi<T>, zsm);
+    k_zphi<T><<<dim3((D.maxNI + ZP_ROWS - 1) / ZP_ROWS, D.nsub), ZP_ROWS, zsm, D.st>>>(
+        D.ds, static_cast<const T*>(D.poolPC), D.zrep, D.wrep, D.cmap, D.ndofc > 0 ? D.uc : nullptr, D.zw, ctl);
+    CKL();
+    k_assemble_dot<<<D.npart, RT, 0, D.st>>>(D.n, D.own, D.zw, D.fixed, D.wsum, rin, zout, D.part, ctl, 0);
+  } else {  // very many constraints per subdomain: one pass per unique dof
+    k_assemble_z<T><<<D.npart, RT, 0, D.st>>>(D.n, D.own, D.ds, static_cast<const T*>(D.poolPC), D.zrep, D.wrep,
+                                              D.cmap, D.uc, D.wsum, rin, zout, D.part, ctl);
+  }
   CKL();
   D.prof.end(PH_ASSEMBLE_Z, D.st);
 }

@@ -158,11 +158,15 @@ void full_symmetric_csr(const Subdomain& s, vector<int>& ptr, vector<int>& col, 
   for (size_t k = 0; k < s.ia.size(); ++k) { int i = s.ia[k]; col[pos[i]] = s.ja[k]; val[pos[i]++] = s.a[k]; }
 }
 
-// Interior ordering for the band factor: natural order or reverse
-// Cuthill-McKee, whichever has the smaller half bandwidth.  The interior
-// graph is kept as flat arrays; neighbours of a visited node are queued by
-// increasing degree (stable, so ties keep the matrix order).
-void host_interior_ordering(Subdomain& s, const vector<int>& f_ptr, const vector<int>& f_col) {
+// Interior ordering for the band factor: natural order, natural order with
+// the uncoupled dofs (Dirichlet dofs whose rows and columns hold only the
+// diagonal) moved to the end, or reverse Cuthill-McKee, whichever has the
+// smallest half bandwidth.  The interior graph (nonzero entries only: the
+// removed rows and columns of fixed dofs stay in the pattern as zeros) is kept
+// as flat arrays; neighbours of a visited node are queued by increasing degree
+// (stable, so ties keep the matrix order).
+void host_interior_ordering(Subdomain& s, const vector<int>& f_ptr, const vector<int>& f_col,
+                            const vector<double>& f_val) {
   const int no = s.ndofo;
   vector<int> mo(s.ndof, -1);
   for (int i = 0; i < no; ++i) mo[s.iovsvn[i]] = i;
@@ -172,7 +176,7 @@ void host_interior_ordering(Subdomain& s, const vector<int>& f_ptr, const vector
     int r = s.iovsvn[i];
     for (int k = f_ptr[r]; k < f_ptr[r + 1]; ++k) {
       int c = mo[f_col[k]];
-      if (c >= 0 && c != i) gcol.push_back(c);
+      if (c >= 0 && c != i && f_val[k] != 0.0) gcol.push_back(c);
     }
     gptr[i + 1] = (int)gcol.size();
   }
@@ -188,6 +192,15 @@ void host_interior_ordering(Subdomain& s, const vector<int>& f_ptr, const vector
   vector<int> natural(no);
   std::iota(natural.begin(), natural.end(), 0);
   int bn = bandwidth(natural);
+  // a Dirichlet face of the subdomain interleaves uncoupled dofs with the
+  // coupled ones in natural order (16 x 15 x 15 instead of 15^3 interior nodes
+  // of a 16^3 subdomain): leave them out of the band
+  vector<int> coupled_first;
+  coupled_first.reserve(no);
+  for (int i = 0; i < no; ++i) if (deg(i) > 0) coupled_first.push_back(i);
+  for (int i = 0; i < no; ++i) if (deg(i) == 0) coupled_first.push_back(i);
+  const int bc = bandwidth(coupled_first);
+  if (bc < bn) { natural = coupled_first; bn = bc; }
   // reverse Cuthill-McKee, each component rooted at its first node of
   // minimum degree
   vector<int> rcm;
@@ -834,6 +847,8 @@ void host_setup(Solver& S) {
 #pragma omp parallel for schedule(dynamic)
   for (int t = 0; t < nsub; ++t) host_prepare_blocks(S.subs[t], S.blocks[t]);
   S.stats.t_host_blocks = wall_time() - tt;
+  S.stats.band_w = 0;
+  for (auto& b : S.blocks) S.stats.band_w = std::max(S.stats.band_w, (double)b.w);
 }
 
 // ---------------------------------------------------- device-ready blocks
@@ -864,7 +879,7 @@ void host_prepare_blocks(Subdomain& s, SubBlocks& b) {
   vector<int> fptr, fcol;
   vector<double> fval;
   full_symmetric_csr(s, fptr, fcol, fval);
-  host_interior_ordering(s, fptr, fcol);
+  host_interior_ordering(s, fptr, fcol, fval);
   int no = s.ndofo, ni = s.ndofi;
   vector<int> onew(s.ndof, -1), iidx(s.ndof, -1);
   for (int q = 0; q < no; ++q) onew[s.iovsvn[s.operm[q]]] = q;
@@ -873,9 +888,12 @@ void host_prepare_blocks(Subdomain& s, SubBlocks& b) {
                    vector<double>& val, int& maxrow) {
     ptr.assign(nrow + 1, 0);
     maxrow = 0;
+    // explicit zeros (the removed couplings of fixed dofs) are left out, so
+    // that they do not widen the band; diagonal entries are always kept
+    auto keep = [&](int d, int k) { return colmap[fcol[k]] >= 0 && (fval[k] != 0.0 || fcol[k] == d); };
     for (int r = 0; r < nrow; ++r) {
       int d = rowdof(r), cnt = 0;
-      for (int k = fptr[d]; k < fptr[d + 1]; ++k) cnt += colmap[fcol[k]] >= 0;
+      for (int k = fptr[d]; k < fptr[d + 1]; ++k) cnt += keep(d, k);
       ptr[r + 1] = ptr[r] + cnt;
       maxrow = std::max(maxrow, cnt);
     }
@@ -883,10 +901,8 @@ void host_prepare_blocks(Subdomain& s, SubBlocks& b) {
     val.resize(ptr[nrow]);
     for (int r = 0; r < nrow; ++r) {
       int d = rowdof(r), q = ptr[r];
-      for (int k = fptr[d]; k < fptr[d + 1]; ++k) {
-        int c = colmap[fcol[k]];
-        if (c >= 0) { col[q] = c; val[q++] = fval[k]; }
-      }
+      for (int k = fptr[d]; k < fptr[d + 1]; ++k)
+        if (keep(d, k)) { col[q] = colmap[fcol[k]]; val[q++] = fval[k]; }
     }
   };
   auto orow = [&](int r) { return s.iovsvn[s.operm[r]]; };

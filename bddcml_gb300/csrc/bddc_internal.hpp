@@ -115,7 +115,7 @@ struct Params {
   int weights_type = 0;
   int matrixtype = 1;
   double adaptive_tau = 1.5;  // eigenvalue threshold of adaptive constraints (module_adaptivity.f90:30)
-  int batch_operator = 1;     // batched Schur apply in mixed mode: 0 double-float SIMT, 1 sliced bf16 tensor cores
+  int batch_operator = -1;    // batched products in mixed mode (bddcml_set_batch_operator_c): -1 automatic, 0, 1, 2
 };
 
 struct Stats {
@@ -130,6 +130,7 @@ struct Stats {
   double t_upload = 0, t_host_assemble = 0, t_host_iface = 0, t_host_globs = 0, t_host_blocks = 0;
   double refine1 = 0, refine2 = 0;  // max |correction| / max |X| of the first and the last refinement step
   double refine_steps = 0;          // refinement steps of the interior solves
+  double band_w = 0;                // largest block bandwidth of the interior systems
   // batched solve, per Schur / preconditioner apply: operator bytes streamed, tensor-core
   // flops executed (sliced operator), FP64-equivalent flops of S X, working-precision
   // flops of the local preconditioner products, and the batch width
@@ -246,7 +247,8 @@ std::unique_ptr<Solver> host_build_level2(const Solver& S1, const vector<vector<
 void host_assemble_upper(vector<int>& ia, vector<int>& ja, vector<double>& a);
 void host_nodal_components(Subdomain& s);
 void host_setup(Solver& S);              // everything integer/geometric + BC + weights + constraints
-void host_interior_ordering(Subdomain& s, const vector<int>& f_ptr, const vector<int>& f_col);
+void host_interior_ordering(Subdomain& s, const vector<int>& f_ptr, const vector<int>& f_col,
+                            const vector<double>& f_val);
 void full_symmetric_csr(const Subdomain& s, vector<int>& ptr, vector<int>& col, vector<double>& val);
 void host_prepare_blocks(Subdomain& s, SubBlocks& b);
 // reduced-rhs inputs of a subdomain: weighted rhs with Dirichlet rows replaced by the

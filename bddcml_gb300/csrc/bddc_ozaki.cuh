@@ -1,4 +1,6 @@
-// Batched Schur apply Y = S X with FP64-class accuracy on the bf16 tensor
+// Batched Schur apply Y = S X (and, with the FP32 preconditioner blocks as A,
+// the preconditioner products of the batched solve; see the end of the file)
+// with FP64-class accuracy on the bf16 tensor
 // cores (tcgen05 kind::f16), by error-free slicing of both operands (Ozaki,
 // Ogita, Oishi and Rump, "Error-free transformations of matrix
 // multiplication by using fast routines of matrix multiplication and its
@@ -63,10 +65,11 @@ __device__ __forceinline__ void mma_bf16(uint32_t dtmem, uint64_t adesc, uint64_
       : "memory");
 }
 
-// OZ_NS slices of v = hi + lo, |v| <= 1: v ~ sum_s q_s 2^(-6 s), q_s integers
-__device__ __forceinline__ void oz_split(float hi, float lo, float (&q)[OZ_NS]) {
+// N slices of v = hi + lo, |v| <= 1: v ~ sum_s q_s 2^(-6 s), q_s integers
+template <int N>
+__device__ __forceinline__ void oz_split(float hi, float lo, float (&q)[N]) {
 #pragma unroll
-  for (int s = 0; s < OZ_NS; ++s) {
+  for (int s = 0; s < N; ++s) {
     hi *= 64.f;
     lo *= 64.f;
     const float r = rintf(hi);
@@ -131,17 +134,32 @@ __global__ void __launch_bounds__(256) kb_oz_slice_s(const DevSub* __restrict__ 
 }
 
 // ------------------------------------------------------ X slices (per apply)
-// fcol[sub * BMAX + k] = exponent of the largest |x| of column k on the subdomain's interface
-__global__ void __launch_bounds__(256) kb_oz_col_exp(const DevSub* __restrict__ ds, int lg,
-                                                     const int* __restrict__ uniq, const double* __restrict__ x,
-                                                     int* __restrict__ fcol, const int* __restrict__ ndone) {
+// The sliced vectors of a subdomain: mode 0 its interface (entries rep .. rep + ni,
+// the product's K range for S, Z and Phi^T), mode 1 its constraints (coff ..
+// coff + nc, the K range for Phi).  Entry j of column k is
+// w[base + j] * x[idx[base + j] * nk + k] (w omitted: 1).
+__device__ __forceinline__ void oz_range(const DevSub& d, int mode, int& base, int& cnt) {
+  base = mode ? d.coff : d.rep;
+  cnt = mode ? d.nc : d.ni;
+}
+
+// fcol[sub * BMAX + k] = exponent of the largest |entry| of column k
+__global__ void __launch_bounds__(256) kb_oz_col_exp(const DevSub* __restrict__ ds, int lg, int mode,
+                                                     const int* __restrict__ idx, const double* __restrict__ w,
+                                                     const double* __restrict__ x, int* __restrict__ fcol,
+                                                     const int* __restrict__ ndone) {
   const int nk = 1 << lg;
   if (batch_all_done(ndone, nk)) return;
   const DevSub d = ds[blockIdx.x];
+  int base, cnt;
+  oz_range(d, mode, base, cnt);
   __shared__ double sh[256];
   const int k = threadIdx.x & (nk - 1), rl = threadIdx.x >> lg, nrl = 256 >> lg;
   double m = 0.0;
-  for (int j = rl; j < d.ni; j += nrl) m = fmax(m, fabs(x[((long long)uniq[d.rep + j] << lg) + k]));
+  for (int j = rl; j < cnt; j += nrl) {
+    const double v = x[((long long)idx[base + j] << lg) + k];
+    m = fmax(m, fabs(w ? w[base + j] * v : v));
+  }
   sh[threadIdx.x] = m;
   __syncthreads();
   for (int st = 128; st >= nk; st >>= 1) {
@@ -153,22 +171,30 @@ __global__ void __launch_bounds__(256) kb_oz_col_exp(const DevSub* __restrict__ 
 
 // X chunk blocks of every subdomain: block c at xoff + c * OZ_BB, N row 64 s + k;
 // grid (max chunks, nsub), 256 threads
-__global__ void __launch_bounds__(256) kb_oz_slice_x(const DevSub* __restrict__ ds, int lg,
-                                                     const int* __restrict__ uniq, const double* __restrict__ x,
-                                                     const int* __restrict__ fcol, const long long* __restrict__ xoff,
+__global__ void __launch_bounds__(256) kb_oz_slice_x(const DevSub* __restrict__ ds, int lg, int mode,
+                                                     const int* __restrict__ idx, const double* __restrict__ w,
+                                                     const double* __restrict__ x, const int* __restrict__ fcol,
+                                                     const long long* __restrict__ xoff,
                                                      __nv_bfloat16* __restrict__ xl, const int* __restrict__ ndone) {
   const int nk = 1 << lg;
   if (batch_all_done(ndone, nk)) return;
   const DevSub d = ds[blockIdx.y];
+  int base, cnt;
+  oz_range(d, mode, base, cnt);
   const int c = blockIdx.x;
-  if (c * OZ_KC >= d.ni) return;
+  if (c * OZ_KC >= cnt) return;
   __shared__ double tile[OZ_KC][BMAX + 1];
   for (int e = threadIdx.x; e < OZ_KC * BMAX; e += 256) {
     const int j = e / BMAX, k = e % BMAX, gj = c * OZ_KC + j;
-    tile[j][k] = (k < nk && gj < d.ni) ? x[((long long)uniq[d.rep + gj] << lg) + k] : 0.0;
+    double v = 0.0;
+    if (k < nk && gj < cnt) {
+      v = x[((long long)idx[base + gj] << lg) + k];
+      if (w) v *= w[base + gj];
+    }
+    tile[j][k] = v;
   }
   __syncthreads();
-  __nv_bfloat16* base = xl + xoff[blockIdx.y] + (long long)c * OZ_BB;
+  __nv_bfloat16* out0 = xl + xoff[blockIdx.y] + (long long)c * OZ_BB;
   for (int task = threadIdx.x; task < BMAX * (OZ_KC / 8); task += 256) {
     const int k = task / (OZ_KC / 8), j0 = (task % (OZ_KC / 8)) * 8;
     const double sc = ldexp(1.0, -fcol[blockIdx.y * BMAX + k]);
@@ -184,23 +210,22 @@ __global__ void __launch_bounds__(256) kb_oz_slice_x(const DevSub* __restrict__ 
     }
 #pragma unroll
     for (int s = 0; s < OZ_NS; ++s)
-      *reinterpret_cast<uint4*>(base + oz_off(s * BMAX + k, j0)) = *reinterpret_cast<const uint4*>(out[s]);
+      *reinterpret_cast<uint4*>(out0 + oz_off(s * BMAX + k, j0)) = *reinterpret_cast<const uint4*>(out[s]);
   }
 }
 
 // ----------------------------------------------------------- the product
-// yrep[rep + r][k] = (S X)[r][k] for the rows of one 128-row tile of one
-// subdomain; grid (max row tiles, nsub), OZ_THREADS threads, OZ_SMEM bytes.
-__global__ void __launch_bounds__(OZ_THREADS, 1)
-    kb_schur_oz(const DevSub* __restrict__ ds, const __nv_bfloat16* __restrict__ sl,
-                const long long* __restrict__ soff, const long long* __restrict__ eoff, const int* __restrict__ erow,
-                const __nv_bfloat16* __restrict__ xl, const long long* __restrict__ xoff, const int* __restrict__ fcol,
-                double* __restrict__ yrep, int nk, int* __restrict__ err, const int* __restrict__ ndone) {
-  if (batch_all_done(ndone, nk)) return;
-  const DevSub d = ds[blockIdx.y];
-  const int rt = blockIdx.x, r0 = rt * OZ_M;
-  if (r0 >= d.ni) return;
-  const int nch = (d.ni + OZ_KC - 1) / OZ_KC;
+// One 128-row tile: out[r * nk + k] (+)= (A X)[r][k] for r < m, k < nk, with A
+// given as NSA slices per K chunk (block (c, s) at Sg + (c * NSA + s) * OZ_AB),
+// its row exponents erow[r], the X chunk blocks at Xg and the column
+// exponents fcol[k].  OZ_THREADS threads, OZ_SMEM bytes of dynamic shared
+// memory.  A with fewer slices than X (NSA < OZ_NS, e.g. FP32 data, exact in 5)
+// pairs every A slice with the X slices t <= OZ_NS - 1 - s as before.
+template <int NSA>
+__device__ __forceinline__ void oz_tile(const __nv_bfloat16* __restrict__ Sg, int nch,
+                                        const __nv_bfloat16* __restrict__ Xg, const int* __restrict__ erow,
+                                        const int* __restrict__ fcol, double* __restrict__ out, int m, int nk,
+                                        bool add, int* __restrict__ err) {
   extern __shared__ __align__(1024) unsigned char oz_raw[];
   unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(oz_raw) + 1023) & ~uintptr_t(1023));
   __nv_bfloat16* sB = reinterpret_cast<__nv_bfloat16*>(smem);  // [2][OZ_BB]
@@ -227,8 +252,6 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = tmem_base;
-  const __nv_bfloat16* Sg = sl + soff[blockIdx.y] + (long long)rt * nch * OZ_NS * OZ_AB;
-  const __nv_bfloat16* Xg = xl + xoff[blockIdx.y];
 
   if (warp == 4) {
     // ------------------------------------------------ copies (one thread)
@@ -240,12 +263,12 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         mbar_expect_tx(&bar_b[bb], OZ_BB * 2);
         bulk_g2s(sB + bb * OZ_BB, Xg + (long long)c * OZ_BB, OZ_BB * 2, &bar_b[bb]);
         b_issued = c + 1;
-        for (int s = 0; s < OZ_NS; ++s, ++g) {
+        for (int s = 0; s < NSA; ++s, ++g) {
           const int st = (int)(g % OZ_ASTAGES);
           if (g >= OZ_ASTAGES &&
               !mbar_wait(&bar_afree[st], (uint32_t)(((g - OZ_ASTAGES) / OZ_ASTAGES) & 1))) { abort_flag = 1; break; }
           mbar_expect_tx(&bar_a[st], OZ_AB * 2);
-          bulk_g2s(sA + st * OZ_AB, Sg + ((long long)c * OZ_NS + s) * OZ_AB, OZ_AB * 2, &bar_a[st]);
+          bulk_g2s(sA + st * OZ_AB, Sg + ((long long)c * NSA + s) * OZ_AB, OZ_AB * 2, &bar_a[st]);
           a_issued = g + 1;
         }
       }
@@ -258,23 +281,23 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         const int bb = c & 1;
         if (!mbar_wait(&bar_b[bb], (uint32_t)((c >> 1) & 1))) { abort_flag = 1; break; }
         const uint32_t b0 = smem_u32(sB + bb * OZ_BB);
-        for (int s = 0; s < OZ_NS; ++s, ++g) {
+        for (int s = 0; s < NSA; ++s, ++g) {
           const int st = (int)(g % OZ_ASTAGES);
           if (!mbar_wait(&bar_a[st], (uint32_t)((g / OZ_ASTAGES) & 1))) { abort_flag = 1; break; }
           tc_fence_after();
           const uint32_t a0 = smem_u32(sA + st * OZ_AB);
-          const int m = OZ_NS - s;  // X slices t = 0 .. m-1 pair with S slice s (s + t <= 7)
+          const int nt = OZ_NS - s;  // X slices t = 0 .. nt-1 pair with A slice s (s + t <= 7)
 #pragma unroll
           for (int k16 = 0; k16 < OZ_KC / 16; ++k16) {
             const uint32_t koff = k16 * 2 * TC_LBO;
             const uint32_t acc = (c > 0 || k16 > 0 || s > 0) ? 1u : 0u;
-            // t = 0..3 -> D_{s+t} at TMEM column 64 (s + t), N = 64 min(m, 4)
-            const int n1 = min(m, 4);
+            // t = 0..3 -> D_{s+t} at TMEM column 64 (s + t), N = 64 min(nt, 4)
+            const int n1 = min(nt, 4);
             mma_bf16(tmem + (uint32_t)(s * BMAX), tc_desc(a0 + koff), tc_desc(b0 + koff),
                      oz_idesc(OZ_M, n1 * BMAX), acc);
-            if (m > 4)
+            if (nt > 4)
               mma_bf16(tmem + (uint32_t)((s + 4) * BMAX), tc_desc(a0 + koff),
-                       tc_desc(b0 + koff + (uint32_t)(4 * BMAX / 8) * TC_SBO), oz_idesc(OZ_M, (m - 4) * BMAX), acc);
+                       tc_desc(b0 + koff + (uint32_t)(4 * BMAX / 8) * TC_SBO), oz_idesc(OZ_M, (nt - 4) * BMAX), acc);
           }
           mma_commit(&bar_afree[st]);
           mma_groups = g + 1;
@@ -290,8 +313,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     const uint32_t trow = (uint32_t)(warp * 32) << 16;
     if (mbar_wait(&bar_done, 0u) && !abort_flag) {
       tc_fence_after();
-      const int gr = r0 + r;
-      const int e = gr < d.ni ? erow[eoff[blockIdx.y] + gr] : 0;
+      const int e = r < m ? erow[r] : 0;
 #pragma unroll 1
       for (int cg = 0; cg < BMAX / 16; ++cg) {
         float sh[16], sl2[16];
@@ -310,13 +332,15 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
             sl2[i] += er;
           }
         }
-        if (gr < d.ni) {
+        if (r < m) {
 #pragma unroll
           for (int i = 0; i < 16; ++i) {
             const int k = cg * 16 + i;
-            if (k < nk)
-              yrep[((long long)(d.rep + gr)) * nk + k] =
-                  ldexp((double)sh[i] + (double)sl2[i], e + fcol[blockIdx.y * BMAX + k]);
+            if (k < nk) {
+              const double v = ldexp((double)sh[i] + (double)sl2[i], e + fcol[k]);
+              double* o = out + (long long)r * nk + k;
+              *o = add ? *o + v : v;
+            }
           }
         }
       }
@@ -337,6 +361,107 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
   __syncthreads();
   tc_fence_after();
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
+}
+
+// yrep[rep + r][k] = (S X)[r][k] for the rows of one 128-row tile of one
+// subdomain; grid (max row tiles, nsub), OZ_THREADS threads, OZ_SMEM bytes.
+__global__ void __launch_bounds__(OZ_THREADS, 1)
+    kb_schur_oz(const DevSub* __restrict__ ds, const __nv_bfloat16* __restrict__ sl,
+                const long long* __restrict__ soff, const long long* __restrict__ eoff, const int* __restrict__ erow,
+                const __nv_bfloat16* __restrict__ xl, const long long* __restrict__ xoff, const int* __restrict__ fcol,
+                double* __restrict__ yrep, int nk, int* __restrict__ err, const int* __restrict__ ndone) {
+  if (batch_all_done(ndone, nk)) return;
+  const DevSub d = ds[blockIdx.y];
+  const int rt = blockIdx.x, r0 = rt * OZ_M;
+  if (r0 >= d.ni) return;
+  const int nch = (d.ni + OZ_KC - 1) / OZ_KC;
+  oz_tile<OZ_NS>(sl + soff[blockIdx.y] + (long long)rt * nch * OZ_NS * OZ_AB, nch, xl + xoff[blockIdx.y],
+                 erow + eoff[blockIdx.y] + r0, fcol + blockIdx.y * BMAX, yrep + (long long)(d.rep + r0) * nk,
+                 min(OZ_M, d.ni - r0), nk, false, err);
+}
+
+// ------------------------------------------- FP32 matrices (preconditioner)
+// Exact products of the FP32 preconditioner blocks Z, Phi and Phi^T with the
+// FP64 vectors: the blocks are cut into OZ_NA slices and the vectors into
+// OZ_NS slices as for the Schur apply.  Every application is then the same
+// linear operator, without the rounding noise of FP32 products that delays the
+// outer PCG on ill-conditioned problems.  The slices of a row are scaled by
+// the row's largest entry, so seven 6-bit slices hold every FP32 entry down to
+// 2^-43 of it: a fixed (and almost symmetric) change of the blocks of at most
+// ni 2^-44 of the row's scale in a product.  Fewer slices leave a larger
+// asymmetric change: at 48^3 three-level elasticity with stiff inclusions the
+// batched mixed columns took +9 iterations over the oracle with five slices,
+// +5 with six and +3 with seven or eight.
+constexpr int OZ_NA = 7;
+
+// one sliced matrix: rows m, K range k, row-major FP32 source at src with
+// leading dimension ld; slice blocks at soff, row exponents at eoff
+struct OzMat {
+  long long src, soff, eoff;
+  int ld, m, k;
+};
+
+// erow[eoff + r] for r < m rounded up to the 128-row tile (padding rows 0);
+// warp per row, grid (rows / 8, matrices)
+__global__ void kb_oz_row_exp_a(const OzMat* __restrict__ mats, const float* __restrict__ pool,
+                                int* __restrict__ erow) {
+  const OzMat a = mats[blockIdx.y];
+  const int r = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (r >= (a.m + OZ_M - 1) / OZ_M * OZ_M) return;
+  float mx = 0.f;
+  if (r < a.m)
+    for (int j = lane; j < a.k; j += 32) mx = fmaxf(mx, fabsf(pool[a.src + (long long)r * a.ld + j]));
+  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if (lane == 0) erow[a.eoff + r] = oz_exp((double)mx);
+}
+
+// slice blocks ((rt * nch + c) * OZ_NA + s) * OZ_AB from soff; grid (tiles x chunks, matrices)
+__global__ void __launch_bounds__(256) kb_oz_slice_a(const OzMat* __restrict__ mats, const float* __restrict__ pool,
+                                                     const int* __restrict__ erow, __nv_bfloat16* __restrict__ sl) {
+  const OzMat a = mats[blockIdx.y];
+  const int nch = (a.k + OZ_KC - 1) / OZ_KC, nrt = (a.m + OZ_M - 1) / OZ_M;
+  if ((int)blockIdx.x >= nch * nrt) return;
+  const int rt = blockIdx.x / nch, c = blockIdx.x % nch;
+  __nv_bfloat16* base = sl + a.soff + ((long long)rt * nch + c) * OZ_NA * OZ_AB;
+  for (int task = threadIdx.x; task < OZ_M * (OZ_KC / 8); task += 256) {
+    const int r = task / (OZ_KC / 8), k0 = (task % (OZ_KC / 8)) * 8;
+    const int gr = rt * OZ_M + r;
+    const float sc = ldexpf(1.f, -erow[a.eoff + gr]);
+    __align__(16) __nv_bfloat16 out[OZ_NA][8];
+#pragma unroll
+    for (int kk = 0; kk < 8; ++kk) {
+      const int gk = c * OZ_KC + k0 + kk;
+      const float v = (gr < a.m && gk < a.k) ? pool[a.src + (long long)gr * a.ld + gk] : 0.f;
+      float q[OZ_NA];
+      oz_split(v * sc, 0.f, q);
+#pragma unroll
+      for (int s = 0; s < OZ_NA; ++s) out[s][kk] = __float2bfloat16_rn(q[s]);
+    }
+#pragma unroll
+    for (int s = 0; s < OZ_NA; ++s)
+      *reinterpret_cast<uint4*>(base + (long long)s * OZ_AB + oz_off(r, k0)) = *reinterpret_cast<const uint4*>(out[s]);
+  }
+}
+
+// one output tile of a sliced product
+struct OzJob {
+  long long a;    // first slice block of the tile's first K chunk (bf16 elements)
+  long long e;    // row exponent of tile row 0
+  long long x;    // first X chunk block (bf16 elements)
+  long long out;  // output row of tile row 0 (rows of nk doubles)
+  int f;          // column exponents at fcol + f
+  int m, nch;     // valid rows (<= OZ_M), K chunks (>= 1)
+  int add;        // 1: added to the output
+};
+
+// grid: one CTA per job; OZ_THREADS threads, OZ_SMEM bytes
+__global__ void __launch_bounds__(OZ_THREADS, 1)
+    kb_gemm_oz(const OzJob* __restrict__ jobs, const __nv_bfloat16* __restrict__ sl, const int* __restrict__ erow,
+               const __nv_bfloat16* __restrict__ xl, const int* __restrict__ fcol, double* __restrict__ out, int nk,
+               int* __restrict__ err, const int* __restrict__ ndone) {
+  if (batch_all_done(ndone, nk)) return;
+  const OzJob j = jobs[blockIdx.x];
+  oz_tile<OZ_NA>(sl + j.a, j.nch, xl + j.x, erow + j.e, fcol + j.f, out + j.out * nk, j.m, nk, j.add != 0, err);
 }
 
 }  // namespace bddc

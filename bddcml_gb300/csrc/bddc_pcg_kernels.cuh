@@ -213,10 +213,11 @@ __global__ void __launch_bounds__(AT) k_pc_local(const DevSub* __restrict__ ds, 
 }
 
 // r_c[q] = sum over the subdomain constraints mapped to coarse dof q
+// (also as a double-float pair in rdf when given, the operand of k_coarse_gemv<float>)
 __global__ void k_coarse_gather(int ndofc, const int* __restrict__ cptr, const int* __restrict__ csub,
                                 const int* __restrict__ cloc, const DevSub* __restrict__ ds,
                                 const double* __restrict__ rcpart, int nrb, int ncpmax, double* __restrict__ rc,
-                                const PcgCtl* __restrict__ ctl) {
+                                const PcgCtl* __restrict__ ctl, float2* __restrict__ rdf = nullptr) {
   if (ctl && ctl->done) return;
   int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= ndofc) return;
@@ -227,23 +228,49 @@ __global__ void k_coarse_gather(int ndofc, const int* __restrict__ cptr, const i
     for (int b = 0; b < nb; ++b) t += rcpart[((long long)s * nrb + b) * ncpmax + c];
   }
   rc[q] = t;
+  if (rdf) {
+    const dfloat v = df_from_double(t);
+    rdf[q] = make_float2(v.hi, v.lo);
+  }
 }
 
 // Coarse solve u_c = Ac^-1 r_c by an explicit inverse M of the coarse matrix
 // (factor precision) with FP64 refinement against the FP64 coarse matrix:
 //   u = M r;  repeat: u += M (r - Ac u).
 // mode 0: u = M v;  mode 1: u += M v  (warp per row, FP64 accumulation)
+// With an FP32 inverse the products M_ij v_j are formed exactly on the FP32
+// pipes, with v given as double-float pairs (vdf, written by the kernel that
+// produced v) and error-free sums, instead of in FP64, whose rate on this
+// part is a small fraction of FP32.
 template <typename T>
 __global__ void __launch_bounds__(256) k_coarse_gemv(int n, int ld, const T* __restrict__ m,
-                                                     const double* __restrict__ v, double* __restrict__ u, int mode,
+                                                     const double* __restrict__ v, const float2* __restrict__ vdf,
+                                                     double* __restrict__ u, int mode,
                                                      const PcgCtl* __restrict__ ctl) {
   if (ctl && ctl->done) return;
   int row = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   if (row >= n) return;
   const T* a = m + (long long)row * ld;
-  double t = 0.0;
-  for (int j = lane; j < n; j += 32) t += (double)a[j] * v[j];
-  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  double t;
+  if constexpr (std::is_same_v<T, float>) {
+    dfacc acc;
+#pragma unroll 4
+    for (int j = lane; j < n; j += 32) {
+      const float2 x = __ldg(vdf + j);
+      acc.fma_df(dfloat{x.x, x.y}, __ldg(a + j));
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      dfacc other;
+      other.s = __shfl_xor_sync(0xffffffffu, acc.s, o);
+      other.c = __shfl_xor_sync(0xffffffffu, acc.c, o);
+      acc.merge(other);
+    }
+    t = acc.to_double();
+  } else {
+    t = 0.0;
+    for (int j = lane; j < n; j += 32) t += (double)a[j] * v[j];
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  }
   if (lane == 0) u[row] = mode ? u[row] + t : t;
 }
 
@@ -251,13 +278,17 @@ __global__ void __launch_bounds__(256) k_coarse_gemv(int n, int ld, const T* __r
 __global__ void k_coarse_residual(int n, const int* __restrict__ ptr, const int* __restrict__ col,
                                   const double* __restrict__ val, const double* __restrict__ r,
                                   const double* __restrict__ u, double* __restrict__ res,
-                                  const PcgCtl* __restrict__ ctl) {
+                                  const PcgCtl* __restrict__ ctl, float2* __restrict__ rdf = nullptr) {
   if (ctl && ctl->done) return;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   double t = r[i];
   for (int q = ptr[i]; q < ptr[i + 1]; ++q) t -= val[q] * u[col[q]];
   res[i] = t;
+  if (rdf) {
+    const dfloat v = df_from_double(t);
+    rdf[i] = make_float2(v.hi, v.lo);
+  }
 }
 
 // deterministic assembly of the coarse matrix: every nonzero sums its
@@ -287,6 +318,58 @@ __global__ void k_coarse_pad(int n, int ld, T* __restrict__ fpool, BandDesc d) {
   if (i < ld) fpool[band_block(d, i / NB, i / NB) + (i % NB) * NB + i % NB] = T(1);
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k < ld) fpool[d.oB + (long long)k * ld + k] = T(1);  // identity right-hand side
+}
+
+// zw[rep + i] = w_i (z_s[i] + Phi_s[i, :] u_c|_s) for the interface rows of
+// every subdomain (the subdomain part of levels_add_first_level,
+// module_levels.f90:4252-4346); k_assemble_dot then sums them per unique dof.
+// grid (row tiles of ZP_ROWS, nsub); the tile of Phi (contiguous rows) is
+// staged through shared memory with coalesced loads, rows padded by one word.
+// With FP32 Phi the products are exact double-float sums on the FP32 pipes.
+constexpr int ZP_ROWS = 128;
+template <typename T>
+__global__ void __launch_bounds__(ZP_ROWS) k_zphi(const DevSub* __restrict__ ds, const T* __restrict__ pcpool,
+                                                  const double* __restrict__ zrep, const double* __restrict__ wrep,
+                                                  const int* __restrict__ cmap, const double* __restrict__ uc,
+                                                  double* __restrict__ zw, const PcgCtl* __restrict__ ctl) {
+  if (ctl && ctl->done) return;
+  const DevSub s = ds[blockIdx.y];
+  const int r0 = blockIdx.x * ZP_ROWS;
+  if (r0 >= s.ni) return;
+  using V = typename PcVec<T>::type;
+  extern __shared__ __align__(16) unsigned char zp_raw[];
+  V* us = reinterpret_cast<V*>(zp_raw);                  // u_c at the subdomain's constraints
+  T* tile = reinterpret_cast<T*>(us + s.ncp);             // rows x (ncp + 1)
+  const int nc = uc ? s.nc : 0, ldt = s.ncp + 1;
+  const int rows = min(ZP_ROWS, s.ni - r0);
+  for (int c = threadIdx.x; c < nc; c += ZP_ROWS) {
+    const double x = uc[cmap[s.coff + c]];
+    if constexpr (std::is_same_v<T, float>) {
+      const float hi = (float)x;
+      us[c] = make_float2(hi, (float)(x - (double)hi));
+    } else {
+      us[c] = x;
+    }
+  }
+  if (nc > 0) {
+    const T* src = pcpool + s.oPhi + (long long)r0 * s.ncp;
+    for (int e = threadIdx.x; e < rows * s.ncp; e += ZP_ROWS) tile[(e / s.ncp) * ldt + e % s.ncp] = __ldg(src + e);
+  }
+  __syncthreads();
+  const int r = threadIdx.x;
+  if (r >= rows) return;
+  const T* ph = tile + r * ldt;
+  double t;
+  if constexpr (std::is_same_v<T, float>) {
+    dfacc acc;
+    for (int c = 0; c < nc; ++c) acc.fma_df(dfloat{us[c].x, us[c].y}, ph[c]);
+    t = acc.to_double();
+  } else {
+    t = 0.0;
+    for (int c = 0; c < nc; ++c) t += ph[c] * us[c];
+  }
+  const long long o = (long long)s.rep + r0 + r;
+  zw[o] = wrep[o] * (zrep[o] + t);
 }
 
 // z[g] = sum_s w_s (z_s + Phi_s u_c|_s); partial (r, z)

@@ -598,60 +598,6 @@ __global__ void __launch_bounds__(128) k_residual_df(const DevSub* __restrict__ 
   }
 }
 
-// Second refinement residual from the first: R1 = R0 - A_oo D1 in FP32, with
-// R0 (component rcomp, overwritten by R1) the FP64-accurate first residual
-// rounded to FP32 and D1 (component dcomp) its solve.  R1 is about 1e-5 of R0
-// (the relative error of the 3xTF32 solve), so the FP32 rounding of R0 and of
-// the products (~6e-8 of R0) leaves R1 within about 1 % - enough for a
-// correction that is itself ~1e-10 of the solution and is solved with one
-// TF32 pass.  This replaces a second double-float residual of the pair X0 + D1.
-// One CTA per RES_ROWS rows; the rows' entries are staged in shared memory
-// and each thread owns groups of 4 adjacent columns.  Padding stays zero.
-__global__ void __launch_bounds__(128) k_residual_update_f32(const DevSub* __restrict__ ds, CsrView koo,
-                                                             float* __restrict__ pool, int dcomp, int rcomp) {
-  const DevSub s = ds[blockIdx.y];
-  const int r0 = blockIdx.x * RES_ROWS;
-  if (r0 >= s.no) return;
-  __shared__ int soff[RES_ROWS][RES_MAXNZ];
-  __shared__ float sval[RES_ROWS][RES_MAXNZ];
-  __shared__ int nnz[RES_ROWS];
-  const int nrow = min(RES_ROWS, s.no - r0);
-  const int tid = threadIdx.x;
-  const int* p = koo.ptr + s.koo;
-  if (tid < RES_ROWS) nnz[tid] = tid < nrow ? min(RES_MAXNZ, p[r0 + tid + 1] - p[r0 + tid]) : 0;
-  __syncthreads();
-  for (int rr = 0; rr < nrow; ++rr) {
-    const int r = r0 + rr;
-    for (int q = tid; q < nnz[rr]; q += blockDim.x) {
-      soff[rr][q] = koo.col[p[r] + q] * s.NR;
-      sval[rr][q] = (float)koo.val[p[r] + q];
-    }
-  }
-  __syncthreads();
-  const long long comp = (long long)s.NO * s.NR;
-  const float* Dv = pool + s.oXc + (long long)dcomp * comp;
-  float* R = pool + s.oXc + (long long)rcomp * comp;
-  const int ngrp = (s.ni + 1 + 3) / 4;  // columns past the rhs column are zero padding
-  for (int gidx = tid; gidx < ngrp; gidx += blockDim.x) {
-    const int c = 4 * gidx;
-    for (int rr = 0; rr < nrow; ++rr) {
-      float4* dst = reinterpret_cast<float4*>(R + (long long)(r0 + rr) * s.NR + c);
-      float4 acc = *dst;
-      const int n = nnz[rr];
-      for (int q = 0; q < n; ++q) {
-        const float a = sval[rr][q];
-        const float4 x = *reinterpret_cast<const float4*>(Dv + soff[rr][q] + c);
-        acc.x = fmaf(-a, x.x, acc.x);
-        acc.y = fmaf(-a, x.y, acc.y);
-        acc.z = fmaf(-a, x.z, acc.z);
-        acc.w = fmaf(-a, x.w, acc.w);
-      }
-      *dst = acc;
-    }
-  }
-}
-
-
 // largest |component| per subdomain (refinement diagnostics; FP32 bit patterns
 // of non-negative values order like integers)
 __global__ void k_comp_maxabs(const DevSub* __restrict__ ds, const float* __restrict__ pool, int comp_id,

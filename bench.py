@@ -247,11 +247,12 @@ def roofline_traffic(workload, phase, roof):
     """DRAM bytes per launch of the roofline kernel, from the committed ncu
     captures of smaller cases of the same kernels, scaled by the units processed
     (full-size captures would exceed the capture size limit); None elsewhere."""
-    if workload == "poisson_128^3_512subs" and phase == "solve_interior":
+    if workload == "poisson_128^3_512subs" and phase == "solve_interior" and "algorithmic_flop" in roof:
         # k_band_sweep_tc forward + backward sweep at 64^3 with 64 subdomains of 16^3
-        # (profiles/k_band_sweep_tc_k_residual_df_poisson64.md): 8x the subdomains
-        return 8 * (1.862084 + 1.174258 + 1.983205 + 1.174619) * 1e9, \
-            "ncu capture at 64^3 (64 subdomains of 16^3), x8 subdomains"
+        # (profiles/k_band_sweep_tc_poisson64.md): 6.151 GB for 3.756e11 flop, scaled by
+        # the algorithmic flop (block rows x window blocks x columns processed)
+        return (1.845567 + 1.173766 + 1.959529 + 1.172174) * 1e9 * roof["algorithmic_flop"] / 375641866240.0, \
+            "ncu capture at 64^3 (64 subdomains of 16^3), scaled by the sweeps' algorithmic flop"
     if phase == "schur_apply" and "algorithmic_bytes" in roof:
         # kb_schur_oz at 48^3 (profiles/kb_schur_oz_elasticity48_64subs_64rhs.md):
         # 4.675 GB read + 0.063 GB written for 4.5068 GB of slice bytes

@@ -143,15 +143,20 @@ void bddcml_upload_subdomain_rhs_batch_c(int *isub, int *nrhs, double *rhss, int
 void bddcml_solve_batch_c(int *comm_all, int *method, double *tol, int *maxit, int *ndecrmax, int *nrhs,
                           int *num_iter, int *converged_reason, double *condition_number);
 
-/* Schur operator of the batched solve in mixed precision: 1 (default) slices
- * S and every block of search directions into 6-bit integer pieces and
- * multiplies them on the bf16 tensor cores with exact accumulation of the
- * leading terms (FP64-class products; used when every subdomain has at most
- * 3264 interface dofs, else mode 0); 0 multiplies the FP32 (hi, lo) pairs of S
- * in double-float arithmetic on the FP32 pipes.  Mode 1 also runs the FP32
- * preconditioner products as 3xTF32 on the tensor cores (mode 0: FP32 SIMT).
- * Takes effect at the next bddcml_solve_batch_c.  No counterpart in the
- * reference. */
+/* Products of the batched solve in mixed precision.  Mode 1 slices S and every
+ * block of search directions into 6-bit integer pieces and multiplies them on
+ * the bf16 tensor cores with exact accumulation of the leading terms
+ * (FP64-class products; used when every subdomain has at most 3264 interface
+ * dofs, else mode 0), and runs the FP32 preconditioner products as 3xTF32 on
+ * the tensor cores.  Mode 2 also slices the FP32 preconditioner blocks (Z, Phi,
+ * Phi^T) and their FP64 operands, so that every preconditioner application is
+ * the same linear operator without rounding noise (which costs outer
+ * iterations on ill-conditioned problems).  Mode 0 multiplies the FP32 (hi, lo)
+ * pairs of S in double-float arithmetic and the preconditioner blocks in FP32
+ * on the FP32 pipes.  Mode -1 (the default) takes 2 when the setup's interior
+ * solves needed more than the two standard refinement steps (stiff
+ * subdomains) and 1 otherwise.  Takes effect at the next bddcml_solve_batch_c.
+ * No counterpart in the reference. */
 void bddcml_set_batch_operator_c(int *mode);
 
 /* Solutions of the last batched solve for subdomain isub: nrhs columns of ndof

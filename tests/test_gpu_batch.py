@@ -150,9 +150,11 @@ def test_batch_argument_errors(built_lib):
 
 @pytest.mark.parametrize("levels", [2, 3])
 def test_batch_operators_agree(built_lib, oracle_mod, levels):
-    """Mixed precision with the sliced bf16 tensor-core Schur apply (operator 1)
-    and the double-float SIMT apply (operator 0): both match the oracle per
-    column, and their solutions agree far below the solver tolerance."""
+    """Mixed precision with the double-float SIMT Schur apply (operator 0), the
+    sliced bf16 tensor-core Schur apply with 3xTF32 preconditioner products
+    (operator 1) and with sliced preconditioner products (operator 2): all
+    match the oracle per column, and their solutions agree far below the
+    solver tolerance."""
     from bddcml_gb300 import problems
     if levels == 2:
         prob, nsub2 = problems.poisson_boxes(15, problems.uniform_boxes(15, 3),
@@ -162,12 +164,13 @@ def test_batch_operators_agree(built_lib, oracle_mod, levels):
     loads = _loads(prob, 6, seed=31)
     ref, _ = _oracle_columns(oracle_mod, prob, loads, levels=levels, nsub2=nsub2)
     res = {}
-    for op in (0, 1):
+    for op in (0, 1, 2):
         u, it, reason, cond, _ = _batch_solve(prob, 1, loads, levels=levels, nsub2=nsub2, operator=op)
         _check(u, it, reason, ref, 1)
         res[op] = (u, it)
-    print(f"levels {levels}: iterations op0 {list(res[0][1])} op1 {list(res[1][1])}")
-    assert np.max(np.abs(res[0][1] - res[1][1])) <= 1
-    for k in range(len(loads)):
-        d = np.linalg.norm(res[0][0][k] - res[1][0][k]) / np.linalg.norm(res[0][0][k])
-        assert d <= 1e-8, (k, d)
+    print(f"levels {levels}: iterations " + " ".join(f"op{op} {list(res[op][1])}" for op in res))
+    for op in (1, 2):
+        assert np.max(np.abs(res[0][1] - res[op][1])) <= 1
+        for k in range(len(loads)):
+            d = np.linalg.norm(res[0][0][k] - res[op][0][k]) / np.linalg.norm(res[0][0][k])
+            assert d <= 1e-8, (op, k, d)
