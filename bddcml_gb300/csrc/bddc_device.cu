@@ -871,8 +871,9 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
     if (r1 <= 1e-5f) {
       // Well-conditioned interiors (Poisson: r1 = 8e-6 at 16^3): a 3xTF32 solve
       // is accurate to about r1 of its result, so the error left in X0 + D1 is
-      // about r1^2 <= 1e-10 of X, three orders below what the 1e-7 solution
-      // tolerance of the mixed path needs; no further correction is made.
+      // about r1^2 <= 1e-10 of X; with the amplification by the Schur
+      // complement's cancellation (a few hundred at 128^3) the solution stays
+      // within the 1e-7 tolerance of the mixed path; no further correction.
     } else {
       // The contraction per step is about kappa(A_oo) u with u ~ 2^-21 for the
       // 3xTF32 sweeps (two TF32 halves per operand, the lo x lo term dropped):
