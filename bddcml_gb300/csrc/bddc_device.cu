@@ -1172,12 +1172,14 @@ static void setup_precond(Solver& S, Device& D) {
     k_phi<T><<<dim3((D.maxNI * D.ncpmax + 255) / 256, nsub), 256, 0, st>>>(D.ds, poolP, D.small, poolPC, 1);
     CKL();
   }
-  k_z<T><<<dim3(D.maxNI / 16, D.maxNI / 16, nsub), dim3(16, 16), 0, st>>>(D.ds, poolP, poolPC, gen);
-  CKL();
-  if (!gen) {
-    k_symmetrize<T><<<dim3(D.maxNI / 32, D.maxNI / 32, nsub), dim3(32, 8), 0, st>>>(D.ds, poolPC, 1);
-    CKL();
+  if (gen) {
+    k_z<T><<<dim3(D.maxNI / 16, D.maxNI / 16, nsub), dim3(16, 16), 0, st>>>(D.ds, poolP, poolPC, gen);
+  } else {  // Z and its symmetrisation in one pass
+    const size_t zsm = (size_t)4 * 32 * (D.ncpmax + 1) * sizeof(T);
+    raise_smem(k_z_sym<T>, zsm);
+    k_z_sym<T><<<dim3(D.maxNI / 32, D.maxNI / 32, nsub), dim3(32, 8), zsm, st>>>(D.ds, poolP, poolPC, D.ncpmax);
   }
+  CKL();
   D.prof.end(PH_PC_BLOCKS, st);
   D.prof.begin(PH_COARSE, st);
 

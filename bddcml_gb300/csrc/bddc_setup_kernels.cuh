@@ -1030,6 +1030,61 @@ __global__ void k_z(const DevSub* __restrict__ ds, const T* __restrict__ pool, T
   pcpool[s.oZ + (long long)i * s.NI + j] = v;
 }
 
+// Symmetric matrices: Z = V - Phi Y^T and its symmetrisation (Z + Z^T) / 2 in
+// one pass.  One CTA per pair of 32 x 32 tiles (bi, bj), bj >= bi, forms both
+// T1 = Z[bi, bj] and T2 = Z[bj, bi] from V, Phi and Y staged in shared memory
+// and writes the average of T1 and T2^T to both places: the same values as
+// k_z followed by k_symmetrize, without the second pass over Z.  grid (NI/32,
+// NI/32, nsub), 32 x 8 threads, dynamic shared memory 4 * 32 * (ncpmax + 1)
+// elements of T (Phi and Y rows of both tiles).
+template <typename T>
+__global__ void __launch_bounds__(256) k_z_sym(const DevSub* __restrict__ ds, const T* __restrict__ pool,
+                                               T* __restrict__ pcpool, int ncpmax) {
+  const DevSub s = ds[blockIdx.z];
+  const int bi = blockIdx.y, bj = blockIdx.x;
+  if (bj < bi || bi * 32 >= s.NI || bj * 32 >= s.NI) return;  // padding tiles are written as zeros
+  extern __shared__ __align__(16) unsigned char zs_raw[];
+  const int ldc = ncpmax + 1;
+  T* phi_i = reinterpret_cast<T*>(zs_raw);
+  T* phi_j = phi_i + 32 * ldc;
+  T* y_i = phi_j + 32 * ldc;
+  T* y_j = y_i + 32 * ldc;
+  __shared__ T ta[32][33], tb[32][33];
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + tx;
+  const int i0 = bi * 32, j0 = bj * 32, nc = s.nc;
+  for (int e = tid; e < 32 * nc; e += 256) {
+    const int r = e / nc, c = e % nc;
+    phi_i[r * ldc + c] = pcpool[s.oPhi + (long long)(i0 + r) * s.ncp + c];
+    phi_j[r * ldc + c] = pcpool[s.oPhi + (long long)(j0 + r) * s.ncp + c];
+    y_i[r * ldc + c] = pool[s.oBs + (long long)(i0 + r) * s.NRC + s.NI + c];
+    y_j[r * ldc + c] = pool[s.oBs + (long long)(j0 + r) * s.NRC + s.NI + c];
+  }
+  for (int r = ty; r < 32; r += 8) {
+    ta[r][tx] = pool[s.oBs + (long long)(i0 + r) * s.NRC + j0 + tx];
+    tb[r][tx] = pool[s.oBs + (long long)(j0 + r) * s.NRC + i0 + tx];
+  }
+  __syncthreads();
+  for (int r = ty; r < 32; r += 8) {
+    T v1 = ta[r][tx], v2 = tb[r][tx];
+    for (int c = 0; c < nc; ++c) {
+      v1 -= phi_i[r * ldc + c] * y_j[tx * ldc + c];
+      v2 -= phi_j[r * ldc + c] * y_i[tx * ldc + c];
+    }
+    ta[r][tx] = v1;
+    tb[r][tx] = v2;
+  }
+  __syncthreads();
+  T* Z = pcpool + s.oZ;
+  for (int r = ty; r < 32; r += 8) {
+    const int gi = i0 + r, gj = j0 + tx;
+    if (gi < s.NI && gj < s.NI)
+      Z[(long long)gi * s.NI + gj] = (gi < s.ni && gj < s.ni) ? sym_avg(ta[r][tx], tb[tx][r]) : T(0);
+    const int hi = j0 + r, hj = i0 + tx;
+    if (bi != bj && hi < s.NI && hj < s.NI)
+      Z[(long long)hi * s.NI + hj] = (hi < s.ni && hj < s.ni) ? sym_avg(tb[r][tx], ta[tx][r]) : T(0);
+  }
+}
+
 // ---------------------------------------------------- one right-hand side
 // New loads after setup (bddcml_setup_new_data_c) need v = A_oo^-1 f_o and
 // g = f_i - A_io v per subdomain, with the factors already in place.

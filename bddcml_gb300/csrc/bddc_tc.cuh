@@ -34,7 +34,8 @@ constexpr int TC_M = 128;            // columns of B per CTA (MMA M)
 constexpr int TC_N = 64;             // output rows (MMA N)
 constexpr int TC_KC = 32;            // K chunk staged per pipeline stage
 constexpr int TC_THREADS = 128;
-constexpr int TC_STAGES = 2;
+constexpr int TC_STAGES = 2;             // window stages of the sweep
+constexpr int TC_PST = 3;                // panel stages of the sweep (copies two chunks ahead)
 constexpr int TC_PCHUNK = TC_N * TC_KC * 2;     // floats per panel chunk (hi + lo)
 constexpr int TC_ACHUNK = TC_M * TC_KC;         // floats per window-operand half (hi or lo)
 constexpr uint32_t TC_LBO = 128;                // bytes between K-adjacent core matrices
@@ -233,11 +234,12 @@ __global__ void __launch_bounds__(SW_THREADS, 2)
 
   extern __shared__ __align__(128) unsigned char sw_smem[];
   float* sA = reinterpret_cast<float*>(sw_smem);                // [stage][hi|lo][TC_ACHUNK]
-  float* sP = sA + TC_STAGES * 2 * TC_ACHUNK;                    // [stage][TC_PCHUNK]
-  __shared__ __align__(8) uint64_t bar_a[TC_STAGES], bar_p[TC_STAGES], bar_mma[TC_STAGES], bar_acc[2], bar_tfree[2];
+  float* sP = sA + TC_STAGES * 2 * TC_ACHUNK;                    // [panel stage][TC_PCHUNK]
+  __shared__ __align__(8) uint64_t bar_a[TC_STAGES], bar_mma[TC_STAGES], bar_acc[2], bar_tfree[2];
+  __shared__ __align__(8) uint64_t bar_p[TC_PST], bar_pfree[TC_PST];
   __shared__ uint32_t tmem_base;
   __shared__ volatile int abort_flag;
-  __shared__ long long last_commit, tma_pending[TC_STAGES];
+  __shared__ long long last_commit, tma_pending[TC_PST];
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   // a forward sweep of a tile inside the identity columns (pad = their
@@ -248,8 +250,11 @@ __global__ void __launch_bounds__(SW_THREADS, 2)
   if (tid == 0) {
     for (int s = 0; s < TC_STAGES; ++s) {
       mbar_init(&bar_a[s], TC_THREADS);
-      mbar_init(&bar_p[s], 1);
       mbar_init(&bar_mma[s], 1);
+    }
+    for (int s = 0; s < TC_PST; ++s) {
+      mbar_init(&bar_p[s], 1);
+      mbar_init(&bar_pfree[s], 1);
       tma_pending[s] = -1;
     }
     for (int b = 0; b < 2; ++b) {
@@ -279,7 +284,20 @@ __global__ void __launch_bounds__(SW_THREADS, 2)
         bulk_g2s(sP + st * TC_PCHUNK, P + panel_chunk(0, d.w, k, pq), pbytes, &bar_p[st]);
         tma_pending[st] = gg;
       };
-      issue_panel(0, row_of(0), sweep_chunk(dir, d.nb, d.w, row_of(0), 0).pq, 0);
+      // panel copies run TC_PST - 1 chunks ahead of the MMAs (cursor ps, pqi)
+      int ps = 0, pqi = 0;
+      long long gp = 0;
+      auto prefetch = [&]() -> bool {
+        if (ps >= nsteps) return true;
+        const int pst = (int)(gp % TC_PST);
+        if (gp >= TC_PST && !mbar_wait(&bar_pfree[pst], (uint32_t)(((gp - TC_PST) / TC_PST) & 1), limit)) return false;
+        const int kp = row_of(ps);
+        issue_panel(pst, kp, sweep_chunk(dir, d.nb, d.w, kp, pqi).pq, gp);
+        ++gp;
+        if (++pqi == sweep_nchunk(dir, d.nb, d.w, kp)) { pqi = 0; ++ps; }
+        return true;
+      };
+      for (int i = 0; i < TC_PST - 1; ++i) prefetch();
       long long g = 0;
       for (int sidx = 0; sidx < nsteps && !abort_flag; ++sidx) {
         const int k = row_of(sidx), b = sidx & 1;
@@ -287,14 +305,14 @@ __global__ void __launch_bounds__(SW_THREADS, 2)
         const uint32_t dacc = tmem + (uint32_t)(b * TC_N);
         if (sidx >= 2 && !mbar_wait(&bar_tfree[b], (uint32_t)(((sidx - 2) >> 1) & 1), limit)) { abort_flag = 1; break; }
         for (int q = 0; q < nchunk; ++q, ++g) {
-          const int st = (int)(g % TC_STAGES);
-          const uint32_t ph = (uint32_t)((g / TC_STAGES) & 1);
-          if (!mbar_wait(&bar_a[st], ph, limit) || !mbar_wait(&bar_p[st], ph, limit)) { abort_flag = 1; break; }
-          tma_pending[st] = -1;
+          const int st = (int)(g % TC_STAGES), pst = (int)(g % TC_PST);
+          if (!mbar_wait(&bar_a[st], (uint32_t)((g / TC_STAGES) & 1), limit) ||
+              !mbar_wait(&bar_p[pst], (uint32_t)((g / TC_PST) & 1), limit)) { abort_flag = 1; break; }
+          tma_pending[pst] = -1;
           tc_fence_after();
           const uint32_t a_hi = smem_u32(sA + (st * 2 + 0) * TC_ACHUNK);
           const uint32_t a_lo = smem_u32(sA + (st * 2 + 1) * TC_ACHUNK);
-          const uint32_t p_hi = smem_u32(sP + st * TC_PCHUNK);
+          const uint32_t p_hi = smem_u32(sP + pst * TC_PCHUNK);
           const uint32_t p_lo = p_hi + TC_N * TC_KC * 4;
           if (passes == 1) {
 #pragma unroll
@@ -313,18 +331,11 @@ __global__ void __launch_bounds__(SW_THREADS, 2)
             }
           }
           mma_commit(&bar_mma[st]);
+          mma_commit(&bar_pfree[pst]);
           if (q == nchunk - 1) mma_commit(&bar_acc[b]);
           last_commit = g;
-          // panel of the next chunk, once the stage it goes to is free
-          int nk = k, nq = q + 1;
-          if (nq == nchunk) { nk = sidx + 1 < nsteps ? row_of(sidx + 1) : -1; nq = 0; }
-          if (nk >= 0) {
-            const long long gn = g + 1;
-            const int st2 = (int)(gn % TC_STAGES);
-            if (gn >= TC_STAGES &&
-                !mbar_wait(&bar_mma[st2], (uint32_t)(((gn - TC_STAGES) / TC_STAGES) & 1), limit)) { abort_flag = 1; break; }
-            issue_panel(st2, nk, sweep_chunk(dir, d.nb, d.w, nk, nq).pq, gn);
-          }
+          // the panel TC_PST - 1 chunks ahead, once the stage it goes to is free
+          if (!prefetch()) { abort_flag = 1; break; }
         }
       }
     }
@@ -465,9 +476,9 @@ __global__ void __launch_bounds__(SW_THREADS, 2)
   __syncthreads();
   if (tid == 0 && abort_flag) {
     const long long ql = last_commit;
-    if (ql >= 0) mbar_wait(&bar_mma[ql % TC_STAGES], (uint32_t)((ql / TC_STAGES) & 1));
-    for (int s2 = 0; s2 < TC_STAGES; ++s2)
-      if (tma_pending[s2] >= 0) mbar_wait(&bar_p[s2], (uint32_t)((tma_pending[s2] / TC_STAGES) & 1));
+    if (ql >= 0) mbar_wait(&bar_pfree[ql % TC_PST], (uint32_t)((ql / TC_PST) & 1));
+    for (int s2 = 0; s2 < TC_PST; ++s2)
+      if (tma_pending[s2] >= 0) mbar_wait(&bar_p[s2], (uint32_t)((tma_pending[s2] / TC_PST) & 1));
     atomicOr(err, DE_TIMEOUT);
   }
   tc_fence_before();
@@ -476,7 +487,9 @@ __global__ void __launch_bounds__(SW_THREADS, 2)
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * TC_N));
 }
 
-constexpr size_t tc_smem_bytes() { return (size_t)TC_STAGES * (2 * TC_ACHUNK + TC_PCHUNK) * sizeof(float); }
+constexpr size_t tc_smem_bytes() {
+  return ((size_t)TC_STAGES * 2 * TC_ACHUNK + (size_t)TC_PST * TC_PCHUNK) * sizeof(float);
+}
 
 // ------------------------------------------------------------- panels
 // Builds the forward and backward panels of a block-band factor (FP32):
