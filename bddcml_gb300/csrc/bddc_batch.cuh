@@ -13,6 +13,61 @@ namespace bddc {
 
 static unsigned blocks_for(long long cnt, int threads = 256) { return (unsigned)((cnt + threads - 1) / threads); }
 
+// Launch-shape autotuner: for a key (kernel, device, problem sizes, batch
+// width) it times every candidate with CUDA events on the library stream (one
+// warm-up launch, then three timed launches) and keeps the fastest for the
+// rest of the process.  The candidates must all be valid launches.
+static int tune_pick(Device& D, const std::string& key, const vector<int>& cands,
+                     const std::function<void(int)>& run, float* best_ms = nullptr) {
+  static std::mutex mu;
+  static std::map<std::string, std::pair<int, float>> cache;
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  const std::string k = std::to_string(dev) + ":" + key;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(k);
+    if (it != cache.end()) {
+      if (best_ms) *best_ms = it->second.second;
+      return it->second.first;
+    }
+  }
+  int pick = cands.empty() ? 0 : cands[0];
+  float best = 0.f;
+  if (cands.size() > 1) {
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    best = 1e30f;
+    for (int c : cands) {
+      run(c);
+      CK(cudaEventRecord(e0, D.st));
+      for (int r = 0; r < 3; ++r) run(c);
+      CK(cudaEventRecord(e1, D.st));
+      CK(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, e0, e1));
+      if (ms < best) { best = ms; pick = c; }
+    }
+    CK(cudaEventDestroy(e0));
+    CK(cudaEventDestroy(e1));
+    best /= 3.f;
+  }
+  std::lock_guard<std::mutex> lk(mu);
+  cache[k] = {pick, best};
+  if (best_ms) *best_ms = best;
+  return pick;
+}
+
+// K-split candidates of a product whose job list has ntile row tiles with at
+// least minch K chunks each: 1, 2, 4, 8 parts, none with an empty part
+static vector<int> ksplit_candidates(int minch) {
+  vector<int> c;
+  for (int ks = 1; ks <= 8; ks *= 2)
+    if (ks == 1 || ks <= minch) c.push_back(ks);
+  return c;
+}
+
 // out = addend + [A1 A2] [B1; B2] for every descriptor (kb_gemm_t), rows up to maxm
 template <typename T>
 static void gemm_t(Device& D, const GemmDesc* gd, int ndesc, int maxm, const T* A, const T* B1, const T* B2, int ldb,
@@ -68,16 +123,17 @@ static void batch_prepare_tc(Device& D) {
   CK(cudaGetDevice(&dev));
   CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   B.tc_grid = std::max(1, nsm);
-  // the Phi^T product has one tile per subdomain: split its K range so that
-  // the job list fills the SMs several times over
-  long long ncon = 0, nptile = 0;
+  // the Phi^T product has one tile per subdomain: its K range is split into
+  // parts (each writing its own plane of tc_rcs) so that the job list fills the
+  // SMs; the number of parts is picked by the autotuner below
+  long long ncon = 0;
+  int minch = 1 << 30;
   for (auto& d : D.hs) {
     ncon = std::max(ncon, (long long)d.coff + d.nc);
-    if (coarse) nptile += (d.nc + TC_M - 1) / TC_M;
+    if (coarse && d.nc > 0) minch = std::min(minch, (d.ni + TC_KC - 1) / TC_KC);
   }
-  const int ks = nptile > 0 ? (int)std::min<long long>(8, std::max<long long>(1, (8LL * nsm + nptile - 1) / nptile)) : 1;
   vector<long long> zoff(D.nsub), poff(D.nsub), boff(D.nsub);
-  vector<TcJob> jz, jp;
+  vector<TcJob> jz;
   long long nz = 0, np = 0, nb = 0;
   int mch1 = 0, mch2 = 0, maxz = 0, maxp = 0;
   for (int t = 0; t < D.nsub; ++t) {
@@ -96,28 +152,34 @@ static void batch_prepare_tc(Device& D) {
     maxz = std::max(maxz, nrz * (n1 + n2));
     const int nrp = coarse ? (d.nc + TC_M - 1) / TC_M : 0;
     poff[t] = np;
-    for (int rt = 0; rt < nrp; ++rt)
-      for (int h = 0; h < ks; ++h) {  // part h: chunks [c0, c1), rows in plane h
-        const int c0 = (int)((long long)n1 * h / ks), c1 = (int)((long long)n1 * (h + 1) / ks);
-        jp.push_back(TcJob{np + ((long long)rt * n1 + c0) * GC_TILE, boff[t] + (long long)c0 * GC_TILE,
-                           h * ncon + d.coff + rt * TC_M, std::min(TC_M, d.nc - rt * TC_M), c1 - c0});
-      }
     np += (long long)nrp * n1 * GC_TILE;
     maxp = std::max(maxp, nrp * n1);
   }
+  auto make_jp = [&](int ks) {
+    vector<TcJob> jp;
+    for (int t = 0; t < D.nsub && coarse; ++t) {
+      const DevSub& d = D.hs[t];
+      const int n1 = (d.ni + TC_KC - 1) / TC_KC, nrp = (d.nc + TC_M - 1) / TC_M;
+      for (int rt = 0; rt < nrp; ++rt)
+        for (int h = 0; h < ks; ++h) {  // part h: chunks [c0, c1), rows in plane h
+          const int c0 = (int)((long long)n1 * h / ks), c1 = (int)((long long)n1 * (h + 1) / ks);
+          if (c1 > c0)
+            jp.push_back(TcJob{poff[t] + ((long long)rt * n1 + c0) * GC_TILE, boff[t] + (long long)c0 * GC_TILE,
+                               h * ncon + d.coff + rt * TC_M, std::min(TC_M, d.nc - rt * TC_M), c1 - c0});
+        }
+    }
+    return jp;
+  };
   B.tc_az = dalloc<float>(std::max(1LL, nz), mem);
   B.tc_ap = dalloc<float>(std::max(1LL, np), mem);
   B.tc_b = dalloc<float>(std::max(1LL, nb), mem);
   B.tc_boff = upload(boff, mem, D.st);
   B.tc_jz = upload(jz, mem, D.st);
   B.tc_njz = (int)jz.size();
-  B.tc_jp = jp.empty() ? nullptr : upload(jp, mem, D.st);
-  B.tc_njp = (int)jp.size();
   B.tc_mch1 = mch1;
   B.tc_mch2 = mch2;
-  B.tc_ks = ks;
   B.tc_pstride = std::max(1LL, ncon) * B.nk;
-  B.tc_rcs = dalloc<double>(ks * B.tc_pstride, mem);
+  B.tc_rcs = dalloc<double>(8 * B.tc_pstride, mem);  // room for the largest K split
   if (maxz > 0) {
     kb_tile_a<<<dim3(maxz, D.nsub), 256, 0, D.st>>>(B.gZ, upload(zoff, mem, D.st),
                                                      static_cast<const float*>(D.poolPC), B.tc_az);
@@ -128,6 +190,32 @@ static void batch_prepare_tc(Device& D) {
                                                      static_cast<const float*>(B.phit), B.tc_ap);
     CKL();
   }
+  // K split of the Phi^T product, timed on this batch's shapes
+  int ks = 1;
+  vector<TcJob> jp = make_jp(1);
+  if (coarse && !jp.empty()) {
+    vector<int> cands = ksplit_candidates(minch);
+    vector<TcJob*> lists(9, nullptr);
+    vector<int> counts(9, 0);
+    for (int c : cands) {
+      vector<TcJob> v = make_jp(c);
+      lists[c] = upload(v, mem, D.st);
+      counts[c] = (int)v.size();
+    }
+    const std::string key = "phit_tc3:" + std::to_string(D.nsub) + ":" + std::to_string(D.maxNI) + ":" +
+                            std::to_string(D.ncpmax) + ":" + std::to_string(B.nk);
+    raise_smem(kb_gemm_tc3, GC_SMEM);
+    ks = tune_pick(D, key, cands, [&](int c) {
+      kb_gemm_tc3<<<std::min(counts[c], B.tc_grid), GC_THREADS, GC_SMEM, D.st>>>(
+          lists[c], counts[c], B.tc_ap, B.tc_b, B.tc_rcs, B.nk, B.nk, D.err, nullptr);
+      CKL();
+    });
+    B.tc_jp = lists[ks];
+    B.tc_njp = counts[ks];
+  }
+  B.tc_ks = ks;
+  // planes that no job writes stay zero (the timing runs wrote into all of them)
+  CK(cudaMemsetAsync(B.tc_rcs, 0, (size_t)8 * B.tc_pstride * sizeof(double), D.st));
 }
 
 // Sliced preconditioner blocks for exact products (bddc_ozaki.cuh), made once
@@ -139,16 +227,13 @@ static void batch_prepare_ozpc(Device& D, const vector<long long>& opt) {
   auto& mem = B.mem;
   const int nsub = D.nsub;
   const bool coarse = D.ndofc > 0;
-  int dev = 0, nsm = 0;
-  CK(cudaGetDevice(&dev));
-  CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   auto nchk = [](int k) { return (k + OZ_KC - 1) / OZ_KC; };
   auto ntile = [](int m) { return (m + OZ_M - 1) / OZ_M; };
   const long long blk = (long long)OZ_NA * OZ_AB;  // bf16 elements of one sliced 128 x 64 chunk
   vector<OzMat> mpc, mpt;                          // from the preconditioner pool / from phit
   vector<long long> sz(nsub, 0), sphi(nsub, 0), spt(nsub, 0), ez(nsub, 0), ephi(nsub, 0), ept(nsub, 0);
   vector<long long> xo(nsub, 0), uo(nsub, 0);
-  long long ns = 0, ne = 0, nx = 0, nu = 0, ncon = 0, nptile = 0;
+  long long ns = 0, ne = 0, nx = 0, nu = 0, ncon = 0;
   int nchu = 0, blk_pc = 0, rows_pc = 0, blk_pt = 0, rows_pt = 0;
   for (int t = 0; t < nsub; ++t) {
     const DevSub& d = D.hs[t];
@@ -179,7 +264,6 @@ static void batch_prepare_ozpc(Device& D, const vector<long long>& opt) {
       mpt.push_back(OzMat{opt[t], spt[t], ept[t], d.NI, nc, d.ni});
       blk_pt = std::max(blk_pt, ntile(nc) * nchk(d.ni));
       rows_pt = std::max(rows_pt, ntile(nc) * OZ_M);
-      nptile += ntile(nc);
     }
   }
   B.ozp_a = dalloc<__nv_bfloat16>(std::max(1LL, ns), mem);
@@ -198,9 +282,7 @@ static void batch_prepare_ozpc(Device& D, const vector<long long>& opt) {
   };
   slice(mpc, static_cast<const float*>(D.poolPC), rows_pc, blk_pc);
   slice(mpt, static_cast<const float*>(B.phit), rows_pt, blk_pt);
-  // Phi^T products split along K so that the job list fills the SMs several times over
-  const int ks = nptile > 0 ? (int)std::min<long long>(8, std::max<long long>(1, (8LL * nsm + nptile - 1) / nptile)) : 1;
-  vector<OzJob> jz, ju, jp;
+  vector<OzJob> jz, ju;
   for (int t = 0; t < nsub; ++t) {
     const DevSub& d = D.hs[t];
     const int nc = coarse ? d.nc : 0, n1 = nchk(d.ni);
@@ -212,27 +294,58 @@ static void batch_prepare_ozpc(Device& D, const vector<long long>& opt) {
         ju.push_back(OzJob{sphi[t] + rt * nchk(nc) * blk, ephi[t] + rt * OZ_M, uo[t], (long long)d.rep + rt * OZ_M,
                            t * BMAX, m, nchk(nc), 1});
     }
-    if (nc > 0 && d.ni > 0)
-      for (int rt = 0; rt < ntile(nc); ++rt)
-        for (int h = 0; h < ks; ++h) {  // part h: chunks [c0, c1) into plane h
-          const int c0 = (int)((long long)n1 * h / ks), c1 = (int)((long long)n1 * (h + 1) / ks);
-          if (c1 > c0)
-            jp.push_back(OzJob{spt[t] + ((long long)rt * n1 + c0) * blk, ept[t] + rt * OZ_M, xo[t] + c0 * OZ_BB,
-                               h * ncon + d.coff + rt * OZ_M, t * BMAX, std::min(OZ_M, nc - rt * OZ_M), c1 - c0,
-                               0});
-        }
   }
+  // Phi^T products split along K (parts write separate planes of tc_rcs)
+  auto make_jp = [&](int ks) {
+    vector<OzJob> jp;
+    for (int t = 0; t < nsub; ++t) {
+      const DevSub& d = D.hs[t];
+      const int nc = coarse ? d.nc : 0, n1 = nchk(d.ni);
+      if (nc > 0 && d.ni > 0)
+        for (int rt = 0; rt < ntile(nc); ++rt)
+          for (int h = 0; h < ks; ++h) {  // part h: chunks [c0, c1) into plane h
+            const int c0 = (int)((long long)n1 * h / ks), c1 = (int)((long long)n1 * (h + 1) / ks);
+            if (c1 > c0)
+              jp.push_back(OzJob{spt[t] + ((long long)rt * n1 + c0) * blk, ept[t] + rt * OZ_M, xo[t] + c0 * OZ_BB,
+                                 h * ncon + d.coff + rt * OZ_M, t * BMAX, std::min(OZ_M, nc - rt * OZ_M), c1 - c0,
+                                 0});
+          }
+    }
+    return jp;
+  };
   B.ozp_jz = jz.empty() ? nullptr : upload(jz, mem, D.st);
   B.ozp_ju = ju.empty() ? nullptr : upload(ju, mem, D.st);
-  B.ozp_jp = jp.empty() ? nullptr : upload(jp, mem, D.st);
   B.ozp_njz = (int)jz.size();
   B.ozp_nju = (int)ju.size();
-  B.ozp_njp = (int)jp.size();
-  B.tc_ks = ks;
   B.tc_pstride = std::max(1LL, ncon) * B.nk;
-  B.tc_rcs = dalloc<double>(ks * B.tc_pstride, mem);
-  // planes that no job writes (a subdomain with fewer K chunks than parts) stay zero
-  CK(cudaMemsetAsync(B.tc_rcs, 0, (size_t)ks * B.tc_pstride * sizeof(double), D.st));
+  B.tc_rcs = dalloc<double>(8 * B.tc_pstride, mem);  // room for the largest K split
+  int ks = 1;
+  if (!make_jp(1).empty()) {  // K split of the Phi^T product, timed on this batch's shapes
+    int minch = 1 << 30;
+    for (auto& d : D.hs)
+      if (coarse && d.nc > 0 && d.ni > 0) minch = std::min(minch, nchk(d.ni));
+    vector<int> cands = ksplit_candidates(minch);
+    vector<OzJob*> lists(9, nullptr);
+    vector<int> counts(9, 0);
+    for (int c : cands) {
+      vector<OzJob> v = make_jp(c);
+      lists[c] = upload(v, mem, D.st);
+      counts[c] = (int)v.size();
+    }
+    const std::string key = "phit_oz:" + std::to_string(nsub) + ":" + std::to_string(D.maxNI) + ":" +
+                            std::to_string(D.ncpmax) + ":" + std::to_string(B.nk);
+    raise_smem(kb_gemm_oz, OZ_SMEM);
+    ks = tune_pick(D, key, cands, [&](int c) {
+      kb_gemm_oz<<<counts[c], OZ_THREADS, OZ_SMEM, D.st>>>(lists[c], B.ozp_a, B.ozp_erow, B.oz_x, B.oz_fcol,
+                                                           B.tc_rcs, B.nk, D.err, nullptr);
+      CKL();
+    });
+    B.ozp_jp = lists[ks];
+    B.ozp_njp = counts[ks];
+  }
+  B.tc_ks = ks;
+  // planes that no job writes stay zero (the timing runs wrote into all of them)
+  CK(cudaMemsetAsync(B.tc_rcs, 0, (size_t)8 * B.tc_pstride * sizeof(double), D.st));
   B.ozpc = true;
 }
 

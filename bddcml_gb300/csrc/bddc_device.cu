@@ -7,6 +7,8 @@
 #include <cstdio>
 #include <cstdint>
 #include <cstring>
+#include <functional>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <numeric>
