@@ -523,9 +523,17 @@ static void run_solve(Device& D, const BandDesc* bd, int nbatch, int maxnb, int 
 }
 
 // FP32 flop of one forward + backward block-band sweep over ncol columns
-static double band_sweep_flop(int nb, int w, int ncol) {
+// MMA work of one forward + backward sweep pair of k_band_sweep_tc, counting
+// the block rows each 128-column tile processes: a tile inside the pad leading
+// identity columns starts its forward sweep at its diagonal block row, and with
+// `lower` also ends its backward sweep there
+static double band_sweep_flop(int nb, int w, int ncol, int pad = 0, bool lower = false) {
   double f = 0.0;
-  for (int k = 0; k < nb; ++k) f += 2.0 * NB * ncol * NB * ((std::min(k, w) + 1) + (std::min(w, nb - 1 - k) + 1));
+  for (int c0 = 0; c0 < ncol; c0 += TC_M) {
+    const int s = c0 + TC_M <= pad ? c0 / NB : 0;
+    for (int k = s; k < nb; ++k) f += 2.0 * NB * TC_M * NB * (std::min(k, w) + 1);
+    for (int k = lower ? s : 0; k < nb; ++k) f += 2.0 * NB * TC_M * NB * (std::min(w, nb - 1 - k) + 1);
+  }
   return f;
 }
 
@@ -1030,7 +1038,7 @@ static void setup_precond(Solver& S, Device& D) {
   }
   S.stats.flop_sweep_s = S.stats.bytes_pc_local = 0;
   for (auto& d : D.hs) {
-    S.stats.flop_sweep_s += band_sweep_flop(d.nbi, d.nbi - 1, d.NRC);
+    S.stats.flop_sweep_s += band_sweep_flop(d.nbi, d.nbi - 1, d.NRC, d.NI, !D.general);
     S.stats.bytes_pc_local += (double)d.ni * d.NI * sizeof(T) + (double)d.ni * d.ncp * sizeof(T) + d.ni * 24.0;
   }
   // interface kernels, per launch (each entry read or written once):
@@ -1144,7 +1152,8 @@ static void setup_precond(Solver& S, Device& D) {
     vector<TcDesc> hts(nsub);
     for (int t = 0; t < nsub; ++t) {
       auto& d = D.hs[t];
-      hts[t] = TcDesc{d.nbi, d.nbi - 1, d.NRC, d.NI, d.oBs, poff[t][0], poff[t][1], -1};  // [I | C^T]
+      // [I | C^T]; Srho^-1 is symmetric, so only its lower triangle is formed
+      hts[t] = TcDesc{d.nbi, d.nbi - 1, d.NRC, d.NI, d.oBs, poff[t][0], poff[t][1], -1, D.general ? 0 : 1};
     }
     td_s = upload(hts, own, st);
     run_panels(D, bd_s, td_s, nsub, maxnbi, maxnbi - 1, poolP, ppool, bdu_s);

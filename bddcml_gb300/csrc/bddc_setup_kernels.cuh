@@ -1034,7 +1034,9 @@ __global__ void k_z(const DevSub* __restrict__ ds, const T* __restrict__ pool, T
 // one pass.  One CTA per pair of 32 x 32 tiles (bi, bj), bj >= bi, forms both
 // T1 = Z[bi, bj] and T2 = Z[bj, bi] from V, Phi and Y staged in shared memory
 // and writes the average of T1 and T2^T to both places: the same values as
-// k_z followed by k_symmetrize, without the second pass over Z.  grid (NI/32,
+// k_z followed by k_symmetrize, without the second pass over Z.  Only the
+// lower triangle of V = Srho^-1 is read (the sweeps form only that, up to the
+// 64-row diagonal blocks): V[bi, bj] = V[bj, bi]^T off the diagonal.  grid (NI/32,
 // NI/32, nsub), 32 x 8 threads, dynamic shared memory 4 * 32 * (ncpmax + 1)
 // elements of T (Phi and Y rows of both tiles).
 template <typename T>
@@ -1059,10 +1061,9 @@ __global__ void __launch_bounds__(256) k_z_sym(const DevSub* __restrict__ ds, co
     y_i[r * ldc + c] = pool[s.oBs + (long long)(i0 + r) * s.NRC + s.NI + c];
     y_j[r * ldc + c] = pool[s.oBs + (long long)(j0 + r) * s.NRC + s.NI + c];
   }
-  for (int r = ty; r < 32; r += 8) {
-    ta[r][tx] = pool[s.oBs + (long long)(i0 + r) * s.NRC + j0 + tx];
-    tb[r][tx] = pool[s.oBs + (long long)(j0 + r) * s.NRC + i0 + tx];
-  }
+  for (int r = ty; r < 32; r += 8) tb[r][tx] = pool[s.oBs + (long long)(j0 + r) * s.NRC + i0 + tx];
+  __syncthreads();
+  for (int r = ty; r < 32; r += 8) ta[r][tx] = bi == bj ? tb[r][tx] : tb[tx][r];
   __syncthreads();
   for (int r = ty; r < 32; r += 8) {
     T v1 = ta[r][tx], v2 = tb[r][tx];

@@ -148,6 +148,9 @@ struct TcDesc {
   long long oPf;     // forward panels in the panel pool
   long long oPb;     // backward panels
   long long oAcc;    // < 0, or a block (same shape as B) the backward sweep adds its result into
+  int lower = 0;     // 1: the result is a symmetric matrix's inverse on the identity columns, of which
+                     // only the lower triangle is wanted: backward sweeps of a tile inside them stop
+                     // at the tile's diagonal block row
 };
 
 // panel storage: block row k, chunk q at ((k * (w+1)*2) + q) * TC_PCHUNK
@@ -245,7 +248,10 @@ __global__ void __launch_bounds__(SW_THREADS, 2)
   // a forward sweep of a tile inside the identity columns (pad = their
   // count) starts at the tile's diagonal block row: the rows above stay zero
   const int s0 = (dir == 0 && c0 + TC_M <= d.pad) ? c0 / NB : 0;
-  const int nsteps = d.nb - s0;
+  // with `lower`, the backward sweep of such a tile stops at its diagonal block
+  // row: the rows above hold the upper triangle, which the caller does not read
+  const int s1 = (dir == 1 && d.lower && c0 + TC_M <= d.pad) ? c0 / NB : 0;
+  const int nsteps = d.nb - s0 - s1;
   auto row_of = [&](int sidx) { return dir == 0 ? s0 + sidx : d.nb - 1 - sidx; };
   if (tid == 0) {
     for (int s = 0; s < TC_STAGES; ++s) {
