@@ -431,6 +431,48 @@ static void run_factor(Device& D, const BandDesc* bd, int nbatch, int maxnb, int
   }
 }
 
+// Left-looking block Cholesky of FP32 band systems with the block products on
+// the tensor cores: per block step the update of column k (k_chol_upd_tc,
+// 3xTF32 from operand tiles made when each block was finished), the diagonal
+// factor and inverse, the panel below it, and the operand tiles of the new
+// column.  hbd: the host copies of the band descriptors (tile offsets).
+static void run_factor_tc(Device& D, const BandDesc* bd, const vector<BandDesc>& hbd, int nbatch, int maxnb, int maxw,
+                          float* pool) {
+  vector<long long> toff(nbatch);
+  long long nt = 0;
+  for (int t = 0; t < nbatch; ++t) {
+    toff[t] = nt;
+    nt += (long long)hbd[t].nb * (hbd[t].w + 1) * CU_TILE;
+  }
+  vector<void*> tmp;
+  float* tiles = dalloc<float>(std::max(1LL, nt), tmp);
+  float* zero = dalloc<float>(2 * CU_HALF, tmp);
+  CK(cudaMemsetAsync(zero, 0, 2 * CU_HALF * sizeof(float), D.st));
+  const long long* dtoff = upload(toff, tmp, D.st);
+  const size_t smem = (2 * NB * (NB + 1) + 2 * SM_TILE) * sizeof(float);
+  raise_smem(k_chol_rl_diag<float>, smem);
+  raise_smem(k_chol_upd_tc, CU_SMEM);
+  for (int k = 0; k < maxnb; ++k) {
+    if (k > 0 && maxw > 0) {
+      k_chol_upd_tc<<<dim3((maxw + 2) / 2, nbatch), CU_THREADS, CU_SMEM, D.st>>>(bd, pool, tiles, dtoff, zero, k,
+                                                                                   D.err);
+      CKL();
+    }
+    k_chol_rl_diag<float><<<nbatch, NT, smem, D.st>>>(bd, pool, k, D.err);
+    CKL();
+    const int m = std::min(maxw, maxnb - 1 - k);
+    if (m > 0) {
+      k_chol_rl_panel<float><<<dim3(m, nbatch), NT, 0, D.st>>>(bd, pool, k);
+      CKL();
+    }
+    if (k < maxnb - 1) {
+      k_chol_tile<<<dim3(maxw + 1, nbatch), 256, 0, D.st>>>(bd, pool, dtoff, tiles, k);
+      CKL();
+    }
+  }
+  for (void* q : tmp) cudaFreeAsync(q, D.st);
+}
+
 // right-looking block Cholesky (k_chol_rl_*): for a few dense systems
 template <typename T>
 static void run_factor_rl(Device& D, const BandDesc* bd, int nbatch, int maxnb, int maxw, T* pool, int* err) {
@@ -806,6 +848,11 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
   } else {
     k_fill_band<T><<<dim3((D.maxNO + 127) / 128, nsub), 128, 0, st>>>(D.ds, D.koo, poolT, D.bd_oo);
     CKL();
+    // SIMT FP32 products: the interior factor's rounding sets the first
+    // refinement ratio r1 (8e-6 at 16^3), and 3xTF32 block updates raise it
+    // (to 8.5e-6) together with the error left after the first correction
+    // (2.3e-8 -> 6e-8 of the oracle's solution at 128^3); the band updates
+    // are also too small (K <= 64 w) to gain from the tensor cores
     run_factor<T>(D, D.bd_oo, nsub, D.maxnbo, D.maxw, poolT);
   }
   vector<TcDesc> htd(nsub);
@@ -1145,7 +1192,8 @@ static void setup_precond(Solver& S, Device& D) {
       k_add_penalty<T><<<dim3(1, nsub), 256, 0, st>>>(D.ds, D.c_ptr, D.c_col, D.c_val, poolP, bd_s);
       CKL();
     }
-    run_factor<T>(D, bd_s, nsub, maxnbi, maxnbi - 1, poolP);
+    if constexpr (std::is_same_v<T, float>) run_factor_tc(D, bd_s, hbs, nsub, maxnbi, maxnbi - 1, poolP);
+    else run_factor<T>(D, bd_s, nsub, maxnbi, maxnbi - 1, poolP);
   }
   TcDesc* td_s = nullptr;
   if constexpr (std::is_same_v<T, float>) {

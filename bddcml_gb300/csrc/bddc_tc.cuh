@@ -560,4 +560,172 @@ __global__ void __launch_bounds__(NT) k_make_panels(const BandDesc* __restrict__
   }
 }
 
+// ------------------------------------------------- block Cholesky updates
+// Right-looking-free block Cholesky with the trailing products on the tensor
+// cores.  Step k of the left-looking factor needs, for the diagonal block and
+// every block below it in column k,
+//     C_ik = A_ik - sum_{j < k} L_ij L_kj^T        (i = k .. k + w)
+// which is a contraction over the K range of block columns j.  Each finished
+// block L_ij is stored once more as TF32 hi / lo operand tiles (k_chol_tile:
+// two 32-wide K chunks, each a 64-row canonical K-major hi part then lo part,
+// 8192 floats per block, at the block's band position), so that the update
+// streams ready operands with cp.async.bulk and runs 3xTF32 MMAs (a_lo b_hi,
+// a_hi b_lo, a_hi b_hi) with FP32 accumulation in TMEM.  One CTA updates two
+// blocks (i0, i0 + 1) of column k: their tiles of block column j land side by
+// side in shared memory as the M = 128 operand, the tile of L_kj is the N = 64
+// operand.  The diagonal factor, the panel L_ik = C_ik Linv_kk^T and the
+// tiling of the new column stay with k_chol_rl_diag / k_chol_rl_panel /
+// k_chol_tile.
+constexpr int CU_TILE = 4 * 2048;       // floats of one block's operand tiles (2 chunks x hi, lo)
+constexpr int CU_HALF = 2048;           // floats of one 64-row x 32 hi (or lo) part
+constexpr int CU_STAGES = 2;
+constexpr int CU_STAGE = 6 * CU_HALF;   // A hi (2 halves), A lo (2 halves), B hi, B lo
+constexpr int CU_THREADS = 192;         // warps 0-3 epilogue, 4 copies, 5 MMAs
+constexpr size_t CU_SMEM = (size_t)CU_STAGES * CU_STAGE * sizeof(float);
+
+__host__ __device__ __forceinline__ long long cu_tile(const BandDesc& d, long long toff, int i, int j) {
+  return toff + ((long long)i * (d.w + 1) + (j - i + d.w)) * CU_TILE;
+}
+
+// operand tiles of the blocks (i, k), i = k .. k + w, of every system; grid (w + 1, systems)
+__global__ void __launch_bounds__(256) k_chol_tile(const BandDesc* __restrict__ bd, const float* __restrict__ pool,
+                                                   const long long* __restrict__ toff, float* __restrict__ tiles,
+                                                   int k) {
+  const BandDesc d = bd[blockIdx.y];
+  const int i = k + blockIdx.x;
+  if (k >= d.nb || i >= d.nb || i - k > d.w) return;
+  const float* L = pool + band_block(d, i, k);
+  float* t = tiles + cu_tile(d, toff[blockIdx.y], i, k);
+  for (int e = threadIdx.x; e < NB * NB; e += 256) {
+    const int r = e / NB, c = e % NB;
+    const float v = L[e], h = tf32_rna(v);
+    float* dst = t + (c / TC_KC) * 2 * CU_HALF + canon_off(r, c % TC_KC);
+    dst[0] = h;
+    dst[CU_HALF] = v - h;
+  }
+}
+
+// C_ik = A_ik - sum_{j<k} L_ij L_kj^T for the block pair i0 = k + 2 blockIdx.x,
+// i0 + 1 of every system (blockIdx.y); in place in the band pool
+__global__ void __launch_bounds__(CU_THREADS, 1)
+    k_chol_upd_tc(const BandDesc* __restrict__ bd, float* __restrict__ pool, const float* __restrict__ tiles,
+                  const long long* __restrict__ toff, const float* __restrict__ zero_tile, int k,
+                  int* __restrict__ err) {
+  const BandDesc d = bd[blockIdx.y];
+  const int i0 = k + 2 * blockIdx.x;
+  if (k >= d.nb || i0 >= d.nb || i0 - k > d.w) return;
+  const bool two = i0 + 1 < d.nb && i0 + 1 - k <= d.w;
+  const int jlo = max(0, i0 - d.w), nch = 2 * (k - jlo);
+  if (nch <= 0) return;
+  const long long tb = toff[blockIdx.y];
+  const long long limit = g_tc_wait_limit;
+  extern __shared__ __align__(128) unsigned char cu_raw[];
+  float* sm = reinterpret_cast<float*>(cu_raw);
+  __shared__ __align__(8) uint64_t bar_full[CU_STAGES], bar_free[CU_STAGES], bar_done;
+  __shared__ uint32_t tmem_base;
+  __shared__ volatile int abort_flag;
+  __shared__ long long issued, mma_groups;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid == 0) {
+    for (int s = 0; s < CU_STAGES; ++s) { mbar_init(&bar_full[s], 1); mbar_init(&bar_free[s], 1); }
+    mbar_init(&bar_done, 1);
+    abort_flag = 0;
+    issued = mma_groups = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                 "r"(TC_N));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_base;
+  if (warp == 4) {
+    // ------------------------------------------------ copies (one thread)
+    if (lane == 0) {
+      constexpr uint32_t hb = CU_HALF * 4;
+      for (int q = 0; q < nch && !abort_flag; ++q) {
+        const int st = q % CU_STAGES, j = jlo + q / 2, c = q & 1;
+        if (q >= CU_STAGES && !mbar_wait(&bar_free[st], (uint32_t)(((q - CU_STAGES) / CU_STAGES) & 1), limit)) {
+          abort_flag = 1;
+          break;
+        }
+        float* dst = sm + st * CU_STAGE;
+        const float* a0 = tiles + cu_tile(d, tb, i0, j) + c * 2 * CU_HALF;
+        const float* a1 = (two && i0 + 1 - j <= d.w) ? tiles + cu_tile(d, tb, i0 + 1, j) + c * 2 * CU_HALF
+                                                     : zero_tile;
+        const float* b = tiles + cu_tile(d, tb, k, j) + c * 2 * CU_HALF;
+        mbar_expect_tx(&bar_full[st], 6 * hb);
+        bulk_g2s(dst + 0 * CU_HALF, a0, hb, &bar_full[st]);            // A hi, rows 0-63
+        bulk_g2s(dst + 1 * CU_HALF, a1, hb, &bar_full[st]);            // A hi, rows 64-127
+        bulk_g2s(dst + 2 * CU_HALF, a0 + CU_HALF, hb, &bar_full[st]);  // A lo
+        bulk_g2s(dst + 3 * CU_HALF, a1 + CU_HALF, hb, &bar_full[st]);
+        bulk_g2s(dst + 4 * CU_HALF, b, hb, &bar_full[st]);             // B hi
+        bulk_g2s(dst + 5 * CU_HALF, b + CU_HALF, hb, &bar_full[st]);   // B lo
+        issued = q + 1;
+      }
+    }
+  } else if (warp == 5) {
+    // ------------------------------------------------ MMAs (one thread)
+    if (lane == 0) {
+      constexpr uint32_t idesc = tc_idesc(TC_M, TC_N);
+      for (int q = 0; q < nch && !abort_flag; ++q) {
+        const int st = q % CU_STAGES;
+        if (!mbar_wait(&bar_full[st], (uint32_t)((q / CU_STAGES) & 1), limit)) { abort_flag = 1; break; }
+        tc_fence_after();
+        const uint32_t a_hi = smem_u32(sm + st * CU_STAGE), a_lo = a_hi + 2 * CU_HALF * 4;
+        const uint32_t b_hi = a_hi + 4 * CU_HALF * 4, b_lo = a_hi + 5 * CU_HALF * 4;
+#pragma unroll
+        for (int kk = 0; kk < TC_KC / 8; ++kk) {
+          const uint32_t koff = kk * 2 * TC_LBO;
+          mma_tf32(tmem, tc_desc(a_lo + koff), tc_desc(b_hi + koff), idesc, (q > 0 || kk > 0) ? 1u : 0u);
+          mma_tf32(tmem, tc_desc(a_hi + koff), tc_desc(b_lo + koff), idesc, 1u);
+          mma_tf32(tmem, tc_desc(a_hi + koff), tc_desc(b_hi + koff), idesc, 1u);
+        }
+        mma_commit(&bar_free[st]);
+        mma_groups = q + 1;
+      }
+      mma_commit(&bar_done);
+    }
+  } else {
+    // ------------------------------------------------ epilogue (128 threads)
+    const int m = warp * 32 + lane;  // TMEM lane = row of the block pair
+    const uint32_t trow = (uint32_t)(warp * 32) << 16;
+    if (mbar_wait(&bar_done, 0u, limit) && !abort_flag) {
+      tc_fence_after();
+      const int blk = i0 + (m >> 6);
+      float* A = (m < 64 || two) ? pool + band_block(d, blk, k) + (long long)(m & 63) * NB : nullptr;
+#pragma unroll 1
+      for (int part = 0; part < TC_N / 16; ++part) {
+        float v[16];
+        tmem_ld16(tmem + trow + (uint32_t)(part * 16), v);
+        if (A) {
+#pragma unroll
+          for (int t4 = 0; t4 < 4; ++t4) {
+            float4 a = *reinterpret_cast<float4*>(A + part * 16 + 4 * t4);
+            a.x -= v[4 * t4]; a.y -= v[4 * t4 + 1]; a.z -= v[4 * t4 + 2]; a.w -= v[4 * t4 + 3];
+            *reinterpret_cast<float4*>(A + part * 16 + 4 * t4) = a;
+          }
+        }
+      }
+    } else {
+      abort_flag = 1;
+    }
+  }
+  // wind-down: after an abort, wait (bounded) for copies and MMAs in flight before freeing TMEM
+  __syncthreads();
+  if (tid == 0 && abort_flag) {
+    const long long qi = issued, qm = mma_groups;
+    if (qm > 0) mbar_wait(&bar_free[(qm - 1) % CU_STAGES], (uint32_t)(((qm - 1) / CU_STAGES) & 1));
+    for (long long q = qm; q < qi; ++q) mbar_wait(&bar_full[q % CU_STAGES], (uint32_t)((q / CU_STAGES) & 1));
+    atomicOr(err, DE_TIMEOUT);
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_N));
+}
+
 }  // namespace bddc
