@@ -37,6 +37,108 @@ struct DevSub {
   long long oU, oUinv, oLsU, oLsUinv, oYd, oPhid;
 };
 
+// Cholesky factor and inverse of the 64 x 64 block in shared memory a (row
+// stride NB + 1; its lower triangle, the factor L on exit) and L^-1 into inv
+// (same stride, zero above the diagonal); NT = 256 threads.  Blocked in
+// 16-column panels so that a block step needs 25 block barriers instead of
+// the 320 of a column-by-column elimination:
+//   factor, per panel: the 16 x 16 diagonal block by one warp with shuffles
+//   (lane l owns row l), the rows below by forward substitution (a thread per
+//   row), the trailing lower triangle by a rank-16 update;
+//   inverse: the diagonal blocks' inverses column by column (warp p, lane j
+//   owns column j of block p), then the blocks below the diagonal by distance,
+//   Linv_pq = -Dinv_p sum_{m=q}^{p-1} L_pm Linv_mq.
+// A non-positive or NaN pivot sets DE_PIVOT / DE_NAN in err and is replaced by 1.
+template <typename T>
+__device__ void diag_factor_inverse(T* a, T* inv, T* tmp, int* __restrict__ err) {
+  constexpr int LD = NB + 1, PB = 16, NPB = NB / PB;
+  static_assert(NT == PB * PB, "one thread per element of a 16 x 16 block");
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, tx = tid & 15, ty = tid >> 4;
+  for (int p = 0; p < NPB; ++p) {
+    const int c0 = p * PB;
+    if (warp == 0) {
+      T row[PB];
+#pragma unroll
+      for (int k = 0; k < PB; ++k) row[k] = lane < PB ? a[(c0 + lane) * LD + c0 + k] : T(0);
+#pragma unroll
+      for (int j = 0; j < PB; ++j) {
+        T v = __shfl_sync(0xffffffffu, row[j], j);
+        if (!(v > T(0))) {
+          if (lane == 0) atomicOr(err, (v != v) ? DE_NAN : DE_PIVOT);
+          v = T(1);
+        }
+        const T dj = sqrt(v);
+        if (lane == j) row[j] = dj;
+        else if (lane > j) row[j] /= dj;
+#pragma unroll
+        for (int kk = j + 1; kk < PB; ++kk) {
+          const T lkj = __shfl_sync(0xffffffffu, row[j], kk);
+          if (lane >= kk && lane < PB) row[kk] -= row[j] * lkj;
+        }
+      }
+      if (lane < PB)
+#pragma unroll
+        for (int k = 0; k < PB; ++k)
+          if (k <= lane) a[(c0 + lane) * LD + c0 + k] = row[k];
+    }
+    __syncthreads();
+    for (int r = c0 + PB + tid; r < NB; r += NT) {  // rows below the diagonal block
+      T x[PB];
+#pragma unroll
+      for (int c = 0; c < PB; ++c) {
+        T t = a[r * LD + c0 + c];
+#pragma unroll
+        for (int k = 0; k < c; ++k) t -= x[k] * a[(c0 + c) * LD + c0 + k];
+        x[c] = t / a[(c0 + c) * LD + c0 + c];
+      }
+#pragma unroll
+      for (int c = 0; c < PB; ++c) a[r * LD + c0 + c] = x[c];
+    }
+    __syncthreads();
+    for (int r = c0 + PB + ty; r < NB; r += PB)  // rank-16 update of the trailing lower triangle
+      for (int q = c0 + PB + tx; q <= r; q += PB) {
+        T t = a[r * LD + q];
+#pragma unroll
+        for (int k = 0; k < PB; ++k) t -= a[r * LD + c0 + k] * a[q * LD + c0 + k];
+        a[r * LD + q] = t;
+      }
+    __syncthreads();
+  }
+  if (warp < NPB && lane < PB) {  // diagonal blocks of the inverse
+    const int c0 = warp * PB, j = lane;
+    T x[PB];
+#pragma unroll
+    for (int i = 0; i < PB; ++i) {
+      T t = i == j ? T(1) : T(0);
+#pragma unroll
+      for (int k = 0; k < i; ++k) t -= a[(c0 + i) * LD + c0 + k] * x[k];
+      x[i] = t / a[(c0 + i) * LD + c0 + i];
+    }
+#pragma unroll
+    for (int i = 0; i < PB; ++i) inv[(c0 + i) * LD + c0 + j] = x[i];
+  }
+  for (int e = tid; e < NB * NB; e += NT) {
+    const int r = e / NB, c = e % NB;
+    if (c / PB > r / PB) inv[r * LD + c] = T(0);
+  }
+  __syncthreads();
+  const int i = tid / PB, j = tid % PB;
+  for (int dd = 1; dd < NPB; ++dd)
+    for (int q = 0; q + dd < NPB; ++q) {
+      const int p = q + dd;
+      T t = T(0);
+      for (int m = q; m < p; ++m)
+#pragma unroll
+        for (int k = 0; k < PB; ++k) t += a[(p * PB + i) * LD + m * PB + k] * inv[(m * PB + k) * LD + q * PB + j];
+      tmp[i * (PB + 1) + j] = t;
+      __syncthreads();
+      T u = T(0);
+      for (int k = 0; k <= i; ++k) u += inv[(p * PB + i) * LD + p * PB + k] * tmp[k * (PB + 1) + j];
+      inv[(p * PB + i) * LD + q * PB + j] = -u;
+      __syncthreads();
+    }
+}
+
 // ------------------------------------------------------------ band factor
 // Left-looking block Cholesky of a block-band matrix, step k:
 //   diagonal: L_kk = chol(A_kk - sum_j L_kj L_kj^T), Linv_kk = L_kk^-1
@@ -61,44 +163,7 @@ __device__ void chol_diag_step(const BandDesc& d, T* __restrict__ pool, int k, i
       a[r * (NB + 1) + c] = Akk[r * NB + c] - acc[q][p];
     }
   __syncthreads();
-  for (int c = 0; c < NB; ++c) {
-    if (tid == 0) {
-      T v = a[c * (NB + 1) + c];
-      if (!(v > T(0))) {
-        atomicOr(err, (v != v) ? DE_NAN : DE_PIVOT);
-        v = T(1);
-      }
-      a[c * (NB + 1) + c] = sqrt(v);
-    }
-    __syncthreads();
-    T dc = a[c * (NB + 1) + c];
-    for (int r = c + 1 + tid; r < NB; r += NT) a[r * (NB + 1) + c] /= dc;
-    __syncthreads();
-    // trailing update of the lower triangle, 16 x 16 thread grid
-    for (int r = c + 1 + ty; r < NB; r += 16) {
-      const T lr = a[r * (NB + 1) + c];
-      for (int q = c + 1 + tx; q <= r; q += 16) a[r * (NB + 1) + q] -= lr * a[q * (NB + 1) + c];
-    }
-    __syncthreads();
-  }
-  // inverse of the lower triangular factor by elimination on the identity:
-  // row k of the inverse is final once scaled, then it is eliminated from the
-  // rows below, all (row, column) pairs of a step in parallel
-  for (int e = tid; e < NB * NB; e += NT) {
-    const int r = e / NB, c = e % NB;
-    inv[r * (NB + 1) + c] = r == c ? T(1) : T(0);
-  }
-  __syncthreads();
-  for (int k = 0; k < NB; ++k) {
-    const T dk = a[k * (NB + 1) + k];
-    for (int j = tid; j <= k; j += NT) inv[k * (NB + 1) + j] /= dk;
-    __syncthreads();
-    for (int i = k + 1 + ty; i < NB; i += 16) {
-      const T lik = a[i * (NB + 1) + k];
-      for (int j = tx; j <= k; j += 16) inv[i * (NB + 1) + j] -= lik * inv[k * (NB + 1) + j];
-    }
-    __syncthreads();
-  }
+  diag_factor_inverse<T>(a, inv, smA, err);
   T* Lkk = pool + band_block(d, k, k);
   T* Li = pool + d.oLinv + (long long)k * NB * NB;
   for (int e = tid; e < NB * NB; e += NT) {
