@@ -893,25 +893,32 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
   //     max|correction| / max|X0| <= 1e-12 (at most 13 corrections).
   // X is the FP32 pair (X0, D) in components 0 and 1.
   if constexpr (std::is_same_v<T, float>) {
-    auto ratio = [&](int slot) {
+    // per-subdomain max|correction| / max|X0| of slot `slot`
+    auto ratios = [&](int slot) {
       vector<int> hmax((size_t)nsub * 8);
       CK(cudaMemcpyAsync(hmax.data(), dmax, hmax.size() * sizeof(int), cudaMemcpyDeviceToHost, st));
       CK(cudaStreamSynchronize(st));
-      float r = 0.f;
+      vector<float> r(nsub, 0.f);
       for (int t = 0; t < nsub; ++t) {
         float x0, dd;
         std::memcpy(&x0, &hmax[t], 4);
         std::memcpy(&dd, &hmax[(size_t)slot * nsub + t], 4);
-        if (x0 > 0) r = std::max(r, dd / x0);
+        if (x0 > 0) r[t] = dd / x0;
       }
       return r;
     };
-    auto tds = [&](int comp, int acc_comp) {
+    auto ratio = [&](int slot) {
+      const vector<float> r = ratios(slot);
+      return nsub ? *std::max_element(r.begin(), r.end()) : 0.f;
+    };
+    // sweep descriptors for components (comp, acc_comp); systems with act[t] == 0 are skipped
+    auto tds = [&](int comp, int acc_comp, const vector<char>* act = nullptr) {
       vector<TcDesc> h2 = htd;
       for (int t = 0; t < nsub; ++t) {
         const long long cs = (long long)D.hs[t].NO * D.hs[t].NR;
         h2[t].oB = D.hs[t].oXc + comp * cs;
         h2[t].oAcc = acc_comp >= 0 ? D.hs[t].oXc + acc_comp * cs : -1;
+        if (act && !(*act)[t]) h2[t].nb = 0;
       }
       return upload(h2, own, st);
     };
@@ -936,17 +943,32 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
       // The contraction per step is about kappa(A_oo) u with u ~ 2^-21 for the
       // 3xTF32 sweeps (two TF32 halves per operand, the lo x lo term dropped):
       // interiors with kappa ~ 1e5 (stiff inclusions) contract by ~0.2 a step.
-      TcDesc* tdc = tds(2, 1);
+      // A subdomain whose correction has dropped below 1e-12 of its solution
+      // leaves the loop (its residual and sweeps are skipped): the stiff ones
+      // take all the steps, the others two or three.
+      vector<char> act(nsub, 1);
+      const vector<float> rr1 = ratios(1);
+      for (int t = 0; t < nsub; ++t) act[t] = rr1[t] > 1e-12f;
+      vector<int> hact(nsub);
+      int* dact = dalloc<int>(std::max(1, nsub), own);
       for (int step = 2; step <= 14 && rl > 1e-12f; ++step) {
+        for (int t = 0; t < nsub; ++t) hact[t] = act[t];
+        CK(cudaMemcpyAsync(dact, hact.data(), (size_t)nsub * sizeof(int), cudaMemcpyHostToDevice, st));
         D.prof.begin(PH_RESIDUAL, st);
-        k_residual_df<<<gres, 128, 0, st>>>(D.ds, D.koo, D.koi, D.fo, D.fo_off, poolT, 1, 2);
+        k_residual_df<<<gres, 128, 0, st>>>(D.ds, D.koo, D.koi, D.fo, D.fo_off, poolT, 1, 2, -1, dact);
         CKL();
         D.prof.end(PH_RESIDUAL, st);
         D.prof.begin(PH_SOLVE_OO, st);
         CK(cudaMemsetAsync(dmax + 2 * nsub, 0, (size_t)nsub * sizeof(int), st));
-        run_solve_tc(D, tdc, nsub, D.maxnbo, D.maxNR, ppool, poolT, 3, 2, dmax + 2 * nsub);
+        run_solve_tc(D, tds(2, 1, &act), nsub, D.maxnbo, D.maxNR, ppool, poolT, 3, 2, dmax + 2 * nsub);
         D.prof.end(PH_SOLVE_OO, st);
-        rl = ratio(2);
+        const vector<float> r = ratios(2);
+        rl = 0.f;
+        for (int t = 0; t < nsub; ++t)
+          if (act[t]) {
+            rl = std::max(rl, r[t]);
+            if (r[t] <= 1e-12f) act[t] = 0;
+          }
         steps = step;
       }
     }

@@ -563,7 +563,9 @@ constexpr int RES_MAXNZ = 96;
 __global__ void __launch_bounds__(128) k_residual_df(const DevSub* __restrict__ ds, CsrView koo, CsrView koi,
                                                      const double* __restrict__ fo,
                                                      const long long* __restrict__ fo_off, float* __restrict__ pool,
-                                                     int xpair, int outcomp, int copycomp = -1) {
+                                                     int xpair, int outcomp, int copycomp = -1,
+                                                     const int* __restrict__ active = nullptr) {
+  if (active && !active[blockIdx.y]) return;  // a system whose refinement has converged
   const DevSub s = ds[blockIdx.y];
   const int r0 = blockIdx.x * RES_ROWS;
   if (r0 >= s.NO) return;
