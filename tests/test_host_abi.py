@@ -212,3 +212,23 @@ def test_host_general_matrix_upload_and_coarse_space(built_lib, oracle_mod):
         assert B.get_coarse_info() == o.stats()
     finally:
         B.bddcml_finalize()
+
+
+def test_interior_band_of_dirichlet_subdomains(built_lib):
+    """The fixed dofs of a Dirichlet face are interior dofs whose couplings were
+    removed (explicit zeros); the interior ordering leaves them out of the band,
+    so every 16^3 subdomain of the cube, with or without Dirichlet faces, has
+    block bandwidth 4 (64-row blocks over 15^3 coupled nodes) instead of 5."""
+    import bddcml_gb300 as B
+    from bddcml_gb300 import problems
+    prob = problems.poisson_on_cube(16, 3)  # corner, edge, face and interior subdomains
+    B.bddcml_init(2, [prob.nsub, 1], -1, 0, 0, 0, 0)
+    try:
+        B.upload_problem(prob)
+        try:
+            B.bddcml_setup_preconditioner(1, 0, 1, 1, 1, 0, 0, 0)
+        except B.BddcmlError as e:  # no GPU in this container: the host part has run
+            assert e.code == 2
+        assert B.get_stats()["band_w"] == 4
+    finally:
+        B.bddcml_finalize()
