@@ -40,7 +40,7 @@ double wall_time() {
 // a row, repeated columns are summed in that order (as a stable sort followed
 // by a merge would), and the distinct columns of each short row are then
 // sorted.  Scratch buffers are per thread and reused across subdomains.
-void host_assemble_upper(vector<int>& ia, vector<int>& ja, vector<double>& a) {
+void host_assemble_upper(rawvec<int>& ia, rawvec<int>& ja, rawvec<double>& a) {
   static thread_local vector<int> ptr, col, slot;
   static thread_local vector<double> val;
   const size_t n = ia.size();
@@ -144,15 +144,18 @@ void full_symmetric_csr(const Subdomain& s, vector<int>& ptr, vector<int>& col, 
   // the assembled upper triangle is sorted by (row, column): scanning it in
   // order appends the mirrored entries of every row in increasing column
   // order, and the row's own entries follow, so no row needs sorting
+  // (every slot of col and val is written below: resize, so that buffers a
+  // caller reuses are not cleared first)
   ptr.assign(n + 1, 0);
   for (size_t k = 0; k < s.ia.size(); ++k) {
     ptr[s.ia[k] + 1]++;
     if (s.ia[k] != s.ja[k]) ptr[s.ja[k] + 1]++;
   }
   for (int i = 0; i < n; ++i) ptr[i + 1] += ptr[i];
-  col.assign(ptr[n], 0);
-  val.assign(ptr[n], 0.0);
-  vector<int> pos(ptr.begin(), ptr.end() - 1);
+  col.resize(ptr[n]);
+  val.resize(ptr[n]);
+  static thread_local vector<int> pos;
+  pos.assign(ptr.begin(), ptr.end() - 1);
   for (size_t k = 0; k < s.ia.size(); ++k)
     if (s.ia[k] != s.ja[k]) { int j = s.ja[k]; col[pos[j]] = s.ia[k]; val[pos[j]++] = s.a[k]; }
   for (size_t k = 0; k < s.ia.size(); ++k) { int i = s.ia[k]; col[pos[i]] = s.ja[k]; val[pos[i]++] = s.a[k]; }
@@ -876,41 +879,70 @@ void host_reduced_rhs_inputs(const Subdomain& s, const double* rhs, bool complet
 
 void host_prepare_blocks(Subdomain& s, SubBlocks& b) {
   constexpr int NB = 64;
-  vector<int> fptr, fcol;
-  vector<double> fval;
+  // the full matrix is scratch: one set of buffers per thread, reused across subdomains
+  static thread_local vector<int> fptr, fcol;
+  static thread_local vector<double> fval;
   full_symmetric_csr(s, fptr, fcol, fval);
   host_interior_ordering(s, fptr, fcol, fval);
   int no = s.ndofo, ni = s.ndofi;
   vector<int> onew(s.ndof, -1), iidx(s.ndof, -1);
   for (int q = 0; q < no; ++q) onew[s.iovsvn[s.operm[q]]] = q;
   for (int i = 0; i < ni; ++i) iidx[s.iivsvn[i]] = i;
-  auto build = [&](int nrow, auto rowdof, const vector<int>& colmap, vector<int>& ptr, vector<int>& col,
-                   vector<double>& val, int& maxrow) {
-    ptr.assign(nrow + 1, 0);
-    maxrow = 0;
-    // explicit zeros (the removed couplings of fixed dofs) are left out, so
-    // that they do not widen the band; diagonal entries are always kept
-    auto keep = [&](int d, int k) { return colmap[fcol[k]] >= 0 && (fval[k] != 0.0 || fcol[k] == d); };
+  // the rows of one dof set (interior rows in the band order, or interface
+  // rows) split by column into the interior block and the interface block in
+  // one pass; each block keeps the row's column order.  Explicit zeros (the
+  // removed couplings of fixed dofs) are left out, so that they do not widen
+  // the band; diagonal entries are always kept.
+  struct Out {
+    vector<int>* ptr;
+    vector<int>* col;
+    vector<double>* val;
+    int* maxrow;
+  };
+  auto build = [&](int nrow, auto rowdof, Out o, Out i) {
+    o.ptr->assign(nrow + 1, 0);
+    i.ptr->assign(nrow + 1, 0);
+    *o.maxrow = 0;
+    *i.maxrow = 0;
     for (int r = 0; r < nrow; ++r) {
-      int d = rowdof(r), cnt = 0;
-      for (int k = fptr[d]; k < fptr[d + 1]; ++k) cnt += keep(d, k);
-      ptr[r + 1] = ptr[r] + cnt;
-      maxrow = std::max(maxrow, cnt);
+      int d = rowdof(r), co = 0, ci = 0;
+      for (int k = fptr[d]; k < fptr[d + 1]; ++k) {
+        const int c = fcol[k];
+        if (fval[k] != 0.0 || c == d) {
+          co += onew[c] >= 0;
+          ci += iidx[c] >= 0;
+        }
+      }
+      (*o.ptr)[r + 1] = (*o.ptr)[r] + co;
+      (*i.ptr)[r + 1] = (*i.ptr)[r] + ci;
+      *o.maxrow = std::max(*o.maxrow, co);
+      *i.maxrow = std::max(*i.maxrow, ci);
     }
-    col.resize(ptr[nrow]);
-    val.resize(ptr[nrow]);
+    o.col->resize((*o.ptr)[nrow]);
+    o.val->resize((*o.ptr)[nrow]);
+    i.col->resize((*i.ptr)[nrow]);
+    i.val->resize((*i.ptr)[nrow]);
+    int* oc = o.col->data();
+    int* ic = i.col->data();
+    double* ov = o.val->data();
+    double* iv = i.val->data();
     for (int r = 0; r < nrow; ++r) {
-      int d = rowdof(r), q = ptr[r];
-      for (int k = fptr[d]; k < fptr[d + 1]; ++k)
-        if (keep(d, k)) { col[q] = colmap[fcol[k]]; val[q++] = fval[k]; }
+      int d = rowdof(r), qo = (*o.ptr)[r], qi = (*i.ptr)[r];
+      for (int k = fptr[d]; k < fptr[d + 1]; ++k) {
+        const int c = fcol[k];
+        if (fval[k] != 0.0 || c == d) {
+          if (onew[c] >= 0) { oc[qo] = onew[c]; ov[qo++] = fval[k]; }
+          if (iidx[c] >= 0) { ic[qi] = iidx[c]; iv[qi++] = fval[k]; }
+        }
+      }
     }
   };
   auto orow = [&](int r) { return s.iovsvn[s.operm[r]]; };
   auto irow = [&](int r) { return s.iivsvn[r]; };
-  build(no, orow, onew, b.oo_ptr, b.oo_col, b.oo_val, b.maxrow_oo);
-  build(no, orow, iidx, b.oi_ptr, b.oi_col, b.oi_val, b.maxrow_oi);
-  build(ni, irow, onew, b.io_ptr, b.io_col, b.io_val, b.maxrow_io);
-  build(ni, irow, iidx, b.ii_ptr, b.ii_col, b.ii_val, b.maxrow_ii);
+  build(no, orow, Out{&b.oo_ptr, &b.oo_col, &b.oo_val, &b.maxrow_oo},
+        Out{&b.oi_ptr, &b.oi_col, &b.oi_val, &b.maxrow_oi});
+  build(ni, irow, Out{&b.io_ptr, &b.io_col, &b.io_val, &b.maxrow_io},
+        Out{&b.ii_ptr, &b.ii_col, &b.ii_val, &b.maxrow_ii});
   b.w = 0;
   for (int r = 0; r < no; ++r)
     for (int k = b.oo_ptr[r]; k < b.oo_ptr[r + 1]; ++k)

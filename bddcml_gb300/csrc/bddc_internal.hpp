@@ -11,11 +11,30 @@
 #include <cstdint>
 #include <memory>
 #include <string>
+#include <utility>
 #include <vector>
 
 namespace bddc {
 
 using std::vector;
+
+// allocator whose resize leaves new elements uninitialised: the uploaded
+// triplets are written once by a parallel copy, and a zero fill before it
+// would be a second serial pass over the largest input
+template <class T>
+struct NoInitAllocator : std::allocator<T> {
+  template <class U>
+  struct rebind { using other = NoInitAllocator<U>; };
+  NoInitAllocator() = default;
+  template <class U>
+  NoInitAllocator(const NoInitAllocator<U>&) noexcept {}
+  template <class U>
+  void construct(U* p) noexcept { ::new ((void*)p) U; }
+  template <class U, class... A>
+  void construct(U* p, A&&... a) { ::new ((void*)p) U(std::forward<A>(a)...); }
+};
+template <class T>
+using rawvec = std::vector<T, NoInitAllocator<T>>;
 
 // status codes (mirror include/bddcml_gb300.h)
 enum Status { OK = 0, ERR_ARGUMENT = 1, ERR_CUDA = 2, ERR_NUMERIC = 3, ERR_UNSUPPORTED = 4, ERR_MEMORY = 5 };
@@ -59,8 +78,8 @@ struct Subdomain {
   int nrhs_batch = 0;
   bool rhs_batch_complete = true;
   int matrixtype = 1;
-  vector<int> ia, ja;  // upper triangle (merged at setup)
-  vector<double> a;
+  rawvec<int> ia, ja;  // upper triangle (merged at setup)
+  rawvec<double> a;
   bool loaded = false;
   bool assembled = false;
   bool find_components = true;
@@ -244,7 +263,7 @@ void host_localize_global(Solver& S, int matrixtype);
 std::unique_ptr<Solver> host_build_level2(const Solver& S1, const vector<vector<double>>& acs, int nsub2);
 
 // host setup (bddc_host.cpp)
-void host_assemble_upper(vector<int>& ia, vector<int>& ja, vector<double>& a);
+void host_assemble_upper(rawvec<int>& ia, rawvec<int>& ja, rawvec<double>& a);
 void host_nodal_components(Subdomain& s);
 void host_setup(Solver& S);              // everything integer/geometric + BC + weights + constraints
 void host_interior_ordering(Subdomain& s, const vector<int>& f_ptr, const vector<int>& f_col,
