@@ -209,7 +209,7 @@ void bddcml_upload_subdomain_data_c(int* nelem, int* nnod, int* ndof, int* ndim,
       ja[k] = j;
       av[k] = a_sparse[k];
       bad_order |= i > j;
-      bad_range |= (i < 0) | (j >= nd);
+      bad_range |= (i < 0) | (i >= nd) | (j < 0) | (j >= nd);  // both bounds: general storage has i > j
     }
     if (bad_order && *matrixtype != 0)  // module_levels.f90:748-752
       throw Error{ERR_ARGUMENT, "matrix in wrong format - only the upper triangle is expected for symmetric problems"};

@@ -127,6 +127,30 @@ def test_errors_are_status_codes(built_lib):
     assert B.last_error()[0] == 1
 
 
+def test_general_matrix_indices_checked_on_both_bounds(built_lib):
+    """General storage (matrixtype 0) allows row > column, so a row index past
+    ndofs or a negative column index must be caught by the range check itself."""
+    import bddcml_gb300 as B
+    from bddcml_gb300 import problems
+    prob = problems.convection_diffusion_on_cube(3, 2)
+    s = prob.subdomains[0]
+    B.bddcml_init(2, [prob.nsub, 1], -1, 0, 0, 0, 0)
+    try:
+        for which, value in (("i", s.ndofs), ("j", -1)):
+            bi, bj = s.i_sparse.copy(), s.j_sparse.copy()
+            (bi if which == "i" else bj)[7] = value
+            with pytest.raises(B.BddcmlError) as ei:
+                B.bddcml_upload_subdomain_data(prob.nelem, prob.nnod, prob.ndof, 3, 3, 0, s.nelems, s.nnods,
+                                               s.ndofs, s.inet, s.nnet, s.nndf, s.isngn, s.isvgvn, s.isegn, s.xyz,
+                                               s.ifix, s.fixv, s.rhs, 1, s.sol, 0, bi, bj, s.a_sparse, 0)
+            assert ei.value.code == 1 and "out of range" in str(ei.value)
+        B.bddcml_upload_subdomain_data(prob.nelem, prob.nnod, prob.ndof, 3, 3, 0, s.nelems, s.nnods, s.ndofs,
+                                       s.inet, s.nnet, s.nndf, s.isngn, s.isvgvn, s.isegn, s.xyz, s.ifix, s.fixv,
+                                       s.rhs, 1, s.sol, 0, s.i_sparse, s.j_sparse, s.a_sparse, 0)
+    finally:
+        B.bddcml_finalize()
+
+
 def test_setup_without_gpu_reports_an_error(built_lib):
     import bddcml_gb300 as B
     from bddcml_gb300 import problems
