@@ -817,18 +817,20 @@ void host_setup(Solver& S) {
         throw Error{ERR_UNSUPPORTED, "weights_type " + std::to_string(S.prm.weights_type) + " is not implemented"};
       }
     }
-#pragma omp parallel for schedule(dynamic)
+    int zero_den = 0;  // an exception may not leave the parallel loop: flag, then throw
+#pragma omp parallel for schedule(dynamic) reduction(| : zero_den)
     for (int t = 0; t < nsub; ++t) {
       auto& s = S.subs[t];
       s.wi.resize(s.ndofi);
       for (int i = 0; i < s.ndofi; ++i) {
         auto pr = neighbour_sum(t, i, [&](int a, int b) { return rho[a][b]; });
         double den = pr.first + pr.second;
-        if (den == 0.0) throw Error{ERR_NUMERIC, "zero denominator in interface weights"};
-        s.wi[i] = pr.first / den;
+        zero_den |= den == 0.0;
+        s.wi[i] = den == 0.0 ? 0.0 : pr.first / den;
       }
       s.rhoi = rho[t];
     }
+    if (zero_den) throw Error{ERR_NUMERIC, "zero denominator in interface weights"};
   }
   S.iface_fixed.assign(S.ninterface, 0);
   S.iface_wsum.assign(S.ninterface, 0.0);

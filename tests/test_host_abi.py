@@ -151,6 +151,24 @@ def test_general_matrix_indices_checked_on_both_bounds(built_lib):
         B.bddcml_finalize()
 
 
+def test_zero_weight_denominator_is_a_status(built_lib):
+    """Stiffness weights (weights_type 1) of a subdomain whose matrix was negated
+    cancel those of its neighbour on the dofs the two share alone: the setup
+    reports a numeric error (status 3) instead of aborting the process."""
+    import bddcml_gb300 as B
+    from bddcml_gb300 import problems
+    prob = problems.poisson_on_cube(2, 2)
+    prob.subdomains[0].a_sparse = -prob.subdomains[0].a_sparse
+    B.bddcml_init(2, [prob.nsub, 1], -1, 0, 0, 0, 0)
+    try:
+        B.upload_problem(prob)
+        with pytest.raises(B.BddcmlError) as ei:
+            B.bddcml_setup_preconditioner(1, 0, 1, 1, 1, 0, 0, 1)
+        assert ei.value.code == 3 and "zero denominator" in str(ei.value)
+    finally:
+        B.bddcml_finalize()
+
+
 def test_setup_without_gpu_reports_an_error(built_lib):
     import bddcml_gb300 as B
     from bddcml_gb300 import problems
