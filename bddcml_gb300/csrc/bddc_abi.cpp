@@ -169,22 +169,36 @@ void bddcml_upload_subdomain_data_c(int* nelem, int* nnod, int* ndof, int* ndim,
         *lsol != *ndofs)
       throw Error{ERR_ARGUMENT, "array length does not match nelems/nnods/ndofs/ndim"};
     long sum_nnet = 0;
-    for (int e = 0; e < *nelems; ++e) sum_nnet += nnet[e];
+    for (int e = 0; e < *nelems; ++e) {
+      if (nnet[e] < 0) throw Error{ERR_ARGUMENT, "negative NNET entry"};
+      sum_nnet += nnet[e];
+    }
     if (sum_nnet != *linet) throw Error{ERR_ARGUMENT, "NNET does not sum up to LINET"};
     long sum_nndf = 0;
-    for (int i = 0; i < *nnods; ++i) sum_nndf += nndf[i];
+    for (int i = 0; i < *nnods; ++i) {
+      if (nndf[i] < 0) throw Error{ERR_ARGUMENT, "negative NNDF entry"};
+      sum_nndf += nndf[i];
+    }
     if (sum_nndf != *ndofs) throw Error{ERR_ARGUMENT, "NNDF does not sum up to NDOFS"};
     s.nelem = *nelems; s.nnod = *nnods; s.ndof = *ndofs; s.ndim = *ndim;
+    // local node numbers index the subdomain's nodes, global numbers index
+    // tables over all subdomains: both are checked before they are used
+    int bad_index = 0;
     s.inet.resize(*linet);
-    for (int k = 0; k < *linet; ++k) s.inet[k] = inet[k] - nb;
+    for (int k = 0; k < *linet; ++k) {
+      s.inet[k] = inet[k] - nb;
+      bad_index |= (s.inet[k] < 0) | (s.inet[k] >= *nnods);
+    }
     s.nnet.assign(nnet, nnet + *nelems);
     s.nndf.assign(nndf, nndf + *nnods);
     s.isngn.resize(*nnods);
-    for (int i = 0; i < *nnods; ++i) s.isngn[i] = isngn[i] - nb;
+    for (int i = 0; i < *nnods; ++i) { s.isngn[i] = isngn[i] - nb; bad_index |= s.isngn[i] < 0; }
     s.isvgvn.resize(*ndofs);
-    for (int i = 0; i < *ndofs; ++i) s.isvgvn[i] = isvgvn[i] - nb;
+    for (int i = 0; i < *ndofs; ++i) { s.isvgvn[i] = isvgvn[i] - nb; bad_index |= s.isvgvn[i] < 0; }
     s.isegn.resize(*nelems);
-    for (int e = 0; e < *nelems; ++e) s.isegn[e] = isegn[e] - nb;
+    for (int e = 0; e < *nelems; ++e) { s.isegn[e] = isegn[e] - nb; bad_index |= s.isegn[e] < 0; }
+    if (bad_index)
+      throw Error{ERR_ARGUMENT, "INET entry outside the subdomain's nodes, or a negative global index"};
     s.xyz.assign(xyz, xyz + (size_t)(*nnods) * (*ndim));
     s.ifix.assign(ifix, ifix + *ndofs);
     s.fixv.assign(fixv, fixv + *ndofs);

@@ -22,6 +22,7 @@
 #include <cmath>
 #include <map>
 #include <numeric>
+#include <omp.h>
 #include <stdexcept>
 #include <functional>
 #include <unordered_map>
@@ -119,7 +120,7 @@ void host_nodal_components(Subdomain& s) {
       for (int k = kinet[e]; k < kinet[e + 1]; ++k)
         for (int q = nptr[s.inet[k]]; q < nptr[s.inet[k] + 1]; ++q) {
           int f = nel[q];
-          if (f != e && cnt[f]++ == 0) touched.push_back(f);
+          if (f != e && !ec[f] && cnt[f]++ == 0) touched.push_back(f);  // labelled elements stay as they are
         }
       for (int f : touched) {
         if (cnt[f] >= thr && !ec[f]) { ec[f] = nc; stack.push_back(f); }
@@ -255,21 +256,37 @@ struct Sharing {
   int count(int g) const { return ptr[g + 1] - ptr[g]; }
 };
 
+// Each thread owns a contiguous range of global node ids and scans every
+// subdomain in ascending order, so each node's list is in ascending subdomain
+// order whatever the thread count.
 Sharing build_sharing(const Solver& S, int nnod_global) {
   Sharing sh;
   sh.ptr.assign(nnod_global + 1, 0);
-  for (auto& s : S.subs)
-    for (int g : s.isngn) sh.ptr[g + 1]++;
-  for (int g = 0; g < nnod_global; ++g) sh.ptr[g + 1] += sh.ptr[g];
-  sh.sub.resize(sh.ptr[nnod_global]);
-  sh.loc.resize(sh.ptr[nnod_global]);
-  vector<int> pos(sh.ptr.begin(), sh.ptr.end() - 1);
-  for (int t = 0; t < (int)S.subs.size(); ++t) {
-    auto& s = S.subs[t];
-    for (int i = 0; i < s.nnod; ++i) {
-      int g = s.isngn[i];
-      sh.sub[pos[g]] = t;
-      sh.loc[pos[g]++] = i;
+  const int nsub = (int)S.subs.size();
+#pragma omp parallel
+  {
+    const int nt = omp_get_num_threads(), th = omp_get_thread_num();
+    const int g0 = (int)((long)nnod_global * th / nt), g1 = (int)((long)nnod_global * (th + 1) / nt);
+    for (int t = 0; t < nsub; ++t)
+      for (int g : S.subs[t].isngn)
+        if (g >= g0 && g < g1) sh.ptr[g + 1]++;
+#pragma omp barrier
+#pragma omp single
+    {
+      for (int g = 0; g < nnod_global; ++g) sh.ptr[g + 1] += sh.ptr[g];
+      sh.sub.resize(sh.ptr[nnod_global]);
+      sh.loc.resize(sh.ptr[nnod_global]);
+    }
+    vector<int> pos(sh.ptr.begin() + g0, sh.ptr.begin() + g1);
+    for (int t = 0; t < nsub; ++t) {
+      const auto& s = S.subs[t];
+      for (int i = 0; i < s.nnod; ++i) {
+        const int g = s.isngn[i];
+        if (g < g0 || g >= g1) continue;
+        int& q = pos[g - g0];
+        sh.sub[q] = t;
+        sh.loc[q++] = i;
+      }
     }
   }
   return sh;

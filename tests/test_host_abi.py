@@ -274,3 +274,80 @@ def test_interior_band_of_dirichlet_subdomains(built_lib):
         assert B.get_stats()["band_w"] == 4
     finally:
         B.bddcml_finalize()
+
+
+def _merged_subdomain(parts, isub):
+    """One subdomain holding the elements of several box subdomains (local
+    numbering in ascending global node id)."""
+    from bddcml_gb300 import problems
+    g = np.unique(np.concatenate([s.isngn for s in parts]))
+    n = len(g)
+
+    def loc(s, a):
+        return np.searchsorted(g, s.isngn[a]).astype(np.int32)
+    xyz, ifix, rhs = np.zeros((3, n)), np.zeros(n, np.int32), np.zeros(n)
+    for s in parts:
+        idx = loc(s, np.arange(s.nnods))
+        xyz[:, idx], ifix[idx], rhs[idx] = s.xyz, s.ifix, s.rhs
+    cat = np.concatenate
+    return problems.Subdomain(
+        isub=isub, nelems=sum(s.nelems for s in parts), nnods=n, ndofs=n, inet=cat([loc(s, s.inet) for s in parts]),
+        nnet=cat([s.nnet for s in parts]), nndf=np.ones(n, np.int32), isngn=g.astype(np.int32),
+        isvgvn=g.astype(np.int32), isegn=cat([s.isegn for s in parts]), xyz=xyz, ifix=ifix, fixv=np.zeros(n),
+        rhs=rhs, sol=np.zeros(n), i_sparse=cat([loc(s, s.i_sparse) for s in parts]),
+        j_sparse=cat([loc(s, s.j_sparse) for s in parts]), a_sparse=cat([s.a_sparse for s in parts]))
+
+
+def test_host_coarse_space_of_disconnected_subdomains(built_lib, oracle_mod):
+    """The 27 boxes of a 6^3 cube regrouped by (x + y + z) parity and z layer:
+    most subdomains are boxes that touch only along edges, so their dual mesh
+    graph (elements sharing 3 nodes) falls into up to 5 components.  Globs are
+    split by component (module_dd.f90:2680-2720, 9160-9175); the coarse space
+    and the weights equal the oracle's."""
+    import bddcml_gb300 as B
+    from bddcml_gb300 import problems
+    prob = problems.poisson_on_cube(2, 3)
+    groups = {}
+    for k, s in enumerate(prob.subdomains):
+        groups.setdefault(((k % 3 + (k // 3) % 3 + k // 9) % 2, k // 9), []).append(s)
+    prob.subdomains = [_merged_subdomain(v, i) for i, v in enumerate(groups.values())]
+    B.bddcml_init(2, [prob.nsub, 1], -1, 0, 0, 0, 0)
+    try:
+        B.upload_problem(prob)
+        try:
+            B.bddcml_setup_preconditioner(1, 0, 1, 1, 1, 0, 0, 0)
+        except B.BddcmlError as e:  # no GPU in this container: the host part has run
+            assert e.code == 2
+        info = B.get_coarse_info()
+        o = oracle_mod.Oracle(prob)
+        o.setup(1, 1, 0)
+        assert info == o.stats()
+        assert info["nedge"] > 0 and info["ncorner"] > 8 * prob.nsub
+        for s in prob.subdomains:
+            w_o = o.weights(s.isub)
+            assert np.array_equal(w_o, B.get_interface_weights(s.isub, len(w_o)))
+    finally:
+        B.bddcml_finalize()
+
+
+def test_mesh_indices_checked_at_upload(built_lib):
+    """INET must index the subdomain's own nodes and the global numbers must not
+    be negative: a bad entry is a status 1 at upload, not a bad access at setup."""
+    import bddcml_gb300 as B
+    from bddcml_gb300 import problems
+    prob = problems.poisson_on_cube(3, 2)
+    s = prob.subdomains[0]
+    B.bddcml_init(2, [prob.nsub, 1], -1, 0, 0, 0, 0)
+    try:
+        for field, k, value in (("inet", 5, s.nnods), ("inet", 0, -1), ("isngn", 3, -1), ("isvgvn", 2, -4)):
+            arrs = {f: getattr(s, f).copy() for f in ("inet", "isngn", "isvgvn")}
+            arrs[field][k] = value
+            with pytest.raises(B.BddcmlError) as ei:
+                B.bddcml_upload_subdomain_data(prob.nelem, prob.nnod, prob.ndof, 3, 3, 0, s.nelems, s.nnods,
+                                               s.ndofs, arrs["inet"], s.nnet, s.nndf, arrs["isngn"],
+                                               arrs["isvgvn"], s.isegn, s.xyz, s.ifix, s.fixv, s.rhs, 1, s.sol, 1,
+                                               s.i_sparse, s.j_sparse, s.a_sparse, 0)
+            assert ei.value.code == 1, field
+        B.upload_problem(prob)
+    finally:
+        B.bddcml_finalize()
