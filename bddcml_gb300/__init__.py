@@ -88,6 +88,33 @@ def _pd(a):
     return a, a.ctypes.data_as(C.POINTER(C.c_double))
 
 
+def _ci(a):
+    """a as a C-contiguous int32 array (no copy when it is one already)."""
+    if type(a) is np.ndarray and a.dtype == np.int32 and a.flags.c_contiguous:
+        return a
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _cd(a):
+    """a as a C-contiguous float64 array (no copy when it is one already)."""
+    if type(a) is np.ndarray and a.dtype == np.float64 and a.flags.c_contiguous:
+        return a
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+_EMPTY = np.zeros(1)
+_upload_c = None
+
+
+def _upload_fn():
+    """bddcml_upload_subdomain_data_c with its 50 pointer arguments declared as
+    addresses (a prototype of its own: the library's attribute keeps no argtypes)."""
+    global _upload_c
+    if _upload_c is None:
+        _upload_c = C.CFUNCTYPE(None, *([C.c_void_p] * 50))(("bddcml_upload_subdomain_data_c", lib()))
+    return _upload_c
+
+
 def last_error():
     buf = C.create_string_buffer(1024)
     code = lib().bddcml_get_last_error_c(buf, _i(1024))
@@ -126,35 +153,30 @@ def bddcml_upload_subdomain_data(nelem, nnod, ndof, ndim, meshdim, isub, nelems,
             xyzf = np.ascontiguousarray(xyz.T).ravel()
     else:
         xyzf = xyz
-    keep = []
+    # every argument is a pointer: arrays by their data address, the scalars
+    # as consecutive entries of one int32 array (one ctypes conversion per call
+    # instead of one object per argument; the call is made once per subdomain)
+    inet, nnet, nndf, isngn, isvgvn, isegn, ifix, i_sparse, j_sparse = (
+        _ci(a) for a in (inet, nnet, nndf, isngn, isvgvn, isegn, ifix, i_sparse, j_sparse))
+    xyzf, fixv, rhs, sol, a_sparse = (_cd(a) for a in (xyzf, fixv, rhs, sol, a_sparse))
+    sc = np.array([nelem, nnod, ndof, ndim, meshdim, isub, nelems, nnods, ndofs,            # 0-8
+                   len(inet), len(nnet), len(nndf), len(isngn), len(isvgvn), len(isegn),   # 9-14
+                   nnods, ndim, len(ifix), len(fixv), len(rhs), is_rhs_complete, len(sol),  # 15-21
+                   matrixtype, len(i_sparse), is_assembled, 0, find_components_int,        # 22-26
+                   use_dual_mesh_graph_int, neighbouring], dtype=np.int32)                 # 27-28
+    s0 = sc.ctypes.data
 
-    def P(a, f):
-        arr, ptr = f(a)
-        keep.append(arr)
-        return ptr, len(arr)
-
-    p_inet, l_inet = P(inet, _pi)
-    p_nnet, l_nnet = P(nnet, _pi)
-    p_nndf, l_nndf = P(nndf, _pi)
-    p_isngn, l_isngn = P(isngn, _pi)
-    p_isvgvn, l_isvgvn = P(isvgvn, _pi)
-    p_isegn, l_isegn = P(isegn, _pi)
-    p_xyz, _ = P(xyzf, _pd)
-    p_ifix, l_ifix = P(ifix, _pi)
-    p_fixv, l_fixv = P(fixv, _pd)
-    p_rhs, l_rhs = P(rhs, _pd)
-    p_sol, l_sol = P(sol, _pd)
-    p_i, la = P(i_sparse, _pi)
-    p_j, _ = P(j_sparse, _pi)
-    p_a, _ = P(a_sparse, _pd)
-    empty = (C.c_double * 1)()
-    lib().bddcml_upload_subdomain_data_c(
-        _i(nelem), _i(nnod), _i(ndof), _i(ndim), _i(meshdim), _i(isub), _i(nelems), _i(nnods), _i(ndofs),
-        p_inet, _i(l_inet), p_nnet, _i(l_nnet), p_nndf, _i(l_nndf), p_isngn, _i(l_isngn), p_isvgvn, _i(l_isvgvn),
-        p_isegn, _i(l_isegn), p_xyz, _i(nnods), _i(ndim), p_ifix, _i(l_ifix), p_fixv, _i(l_fixv), p_rhs, _i(l_rhs),
-        _i(is_rhs_complete), p_sol, _i(l_sol), _i(matrixtype), p_i, p_j, p_a, _i(la), _i(is_assembled),
-        empty, _i(0), _i(0), empty, _i(0), _i(0), empty, _i(0),
-        _i(find_components_int), _i(use_dual_mesh_graph_int), _i(neighbouring))
+    def s(k):
+        return s0 + 4 * k
+    e = _EMPTY.ctypes.data
+    _upload_fn()(
+        s(0), s(1), s(2), s(3), s(4), s(5), s(6), s(7), s(8),
+        inet.ctypes.data, s(9), nnet.ctypes.data, s(10), nndf.ctypes.data, s(11), isngn.ctypes.data, s(12),
+        isvgvn.ctypes.data, s(13), isegn.ctypes.data, s(14), xyzf.ctypes.data, s(15), s(16), ifix.ctypes.data,
+        s(17), fixv.ctypes.data, s(18), rhs.ctypes.data, s(19), s(20), sol.ctypes.data, s(21), s(22),
+        i_sparse.ctypes.data, j_sparse.ctypes.data, a_sparse.ctypes.data, s(23), s(24),
+        e, s(25), s(25), e, s(25), s(25), e, s(25),
+        s(26), s(27), s(28))
     _check()
 
 

@@ -120,7 +120,7 @@ void host_nodal_components(Subdomain& s) {
       for (int k = kinet[e]; k < kinet[e + 1]; ++k)
         for (int q = nptr[s.inet[k]]; q < nptr[s.inet[k] + 1]; ++q) {
           int f = nel[q];
-          if (f != e && !ec[f] && cnt[f]++ == 0) touched.push_back(f);  // labelled elements stay as they are
+          if (f != e && cnt[f]++ == 0) touched.push_back(f);
         }
       for (int f : touched) {
         if (cnt[f] >= thr && !ec[f]) { ec[f] = nc; stack.push_back(f); }
