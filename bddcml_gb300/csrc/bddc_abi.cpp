@@ -168,63 +168,99 @@ void bddcml_upload_subdomain_data_c(int* nelem, int* nnod, int* ndof, int* ndim,
         *lxyz2 != *ndim || *lisvgvn != *ndofs || *lifix != *ndofs || *lfixv != *ndofs || *lrhs != *ndofs ||
         *lsol != *ndofs)
       throw Error{ERR_ARGUMENT, "array length does not match nelems/nnods/ndofs/ndim"};
+    // the sizes are copied to locals: the loops below store ints, which the
+    // compiler would otherwise have to assume may overwrite *nelems and friends
+    const int ne = *nelems, nn = *nnods, nd = *ndofs, nin = *linet;
     long sum_nnet = 0;
-    for (int e = 0; e < *nelems; ++e) {
+    for (int e = 0; e < ne; ++e) {
       if (nnet[e] < 0) throw Error{ERR_ARGUMENT, "negative NNET entry"};
       sum_nnet += nnet[e];
     }
-    if (sum_nnet != *linet) throw Error{ERR_ARGUMENT, "NNET does not sum up to LINET"};
+    if (sum_nnet != nin) throw Error{ERR_ARGUMENT, "NNET does not sum up to LINET"};
     long sum_nndf = 0;
-    for (int i = 0; i < *nnods; ++i) {
+    for (int i = 0; i < nn; ++i) {
       if (nndf[i] < 0) throw Error{ERR_ARGUMENT, "negative NNDF entry"};
       sum_nndf += nndf[i];
     }
-    if (sum_nndf != *ndofs) throw Error{ERR_ARGUMENT, "NNDF does not sum up to NDOFS"};
-    s.nelem = *nelems; s.nnod = *nnods; s.ndof = *ndofs; s.ndim = *ndim;
-    // local node numbers index the subdomain's nodes, global numbers index
-    // tables over all subdomains: both are checked before they are used
-    int bad_index = 0;
-    s.inet.resize(*linet);
-    for (int k = 0; k < *linet; ++k) {
-      s.inet[k] = inet[k] - nb;
-      bad_index |= (s.inet[k] < 0) | (s.inet[k] >= *nnods);
-    }
-    s.nnet.assign(nnet, nnet + *nelems);
-    s.nndf.assign(nndf, nndf + *nnods);
-    s.isngn.resize(*nnods);
-    for (int i = 0; i < *nnods; ++i) { s.isngn[i] = isngn[i] - nb; bad_index |= s.isngn[i] < 0; }
-    s.isvgvn.resize(*ndofs);
-    for (int i = 0; i < *ndofs; ++i) { s.isvgvn[i] = isvgvn[i] - nb; bad_index |= s.isvgvn[i] < 0; }
-    s.isegn.resize(*nelems);
-    for (int e = 0; e < *nelems; ++e) { s.isegn[e] = isegn[e] - nb; bad_index |= s.isegn[e] < 0; }
-    if (bad_index)
-      throw Error{ERR_ARGUMENT, "INET entry outside the subdomain's nodes, or a negative global index"};
-    s.xyz.assign(xyz, xyz + (size_t)(*nnods) * (*ndim));
-    s.ifix.assign(ifix, ifix + *ndofs);
-    s.fixv.assign(fixv, fixv + *ndofs);
-    s.rhs.assign(rhs, rhs + *ndofs);
-    s.rhs_complete = is_rhs_complete && *is_rhs_complete != 0;
-    s.sol.assign(sol, sol + *ndofs);
-    s.matrixtype = *matrixtype;
+    if (sum_nndf != nd) throw Error{ERR_ARGUMENT, "NNDF does not sum up to NDOFS"};
+    s.nelem = ne; s.nnod = nn; s.ndof = nd; s.ndim = *ndim;
     if (*matrixtype < 0 || *matrixtype > 2)
       throw Error{ERR_ARGUMENT, "matrixtype must be 0 (general), 1 (SPD) or 2 (symmetric)"};
-    // the triplets are most of the uploaded bytes: copy them with several
-    // threads (first touch of the new buffers included)
-    const int nla = *la, nd = *ndofs;
+    s.matrixtype = *matrixtype;
+    s.rhs_complete = is_rhs_complete && *is_rhs_complete != 0;
+    // Every array is copied in one parallel region, each loop split over the
+    // threads: the triplets are most of the bytes, and the mesh arrays of a
+    // large subdomain are too many for one thread's share of the memory
+    // bandwidth.  Index arrays are shifted to 0-based and checked: local node
+    // numbers must index the subdomain's nodes, global numbers (which index
+    // tables over all subdomains) must not be negative.
+    const int nla = *la;
+    const long nxyz = (long)nn * (*ndim);
+    s.inet.resize(nin); s.nnet.resize(ne); s.nndf.resize(nn);
+    s.isngn.resize(nn); s.isvgvn.resize(nd); s.isegn.resize(ne);
+    s.xyz.resize(nxyz); s.ifix.resize(nd); s.fixv.resize(nd); s.rhs.resize(nd); s.sol.resize(nd);
     s.ia.resize(nla); s.ja.resize(nla); s.a.resize(nla);
+    int* pinet = s.inet.data();
+    int* pnnet = s.nnet.data();
+    int* pnndf = s.nndf.data();
+    int* pisngn = s.isngn.data();
+    int* pisvgvn = s.isvgvn.data();
+    int* pisegn = s.isegn.data();
+    int* pifix = s.ifix.data();
+    double* pxyz = s.xyz.data();
+    double* pfixv = s.fixv.data();
+    double* prhs = s.rhs.data();
+    double* psol = s.sol.data();
     int* ia = s.ia.data();
     int* ja = s.ja.data();
     double* av = s.a.data();
-    int bad_order = 0, bad_range = 0;
-#pragma omp parallel for schedule(static) reduction(| : bad_order, bad_range) if (nla > 65536)
-    for (int k = 0; k < nla; ++k) {
-      int i = i_sparse[k] - nb, j = j_sparse[k] - nb;
-      ia[k] = i;
-      ja[k] = j;
-      av[k] = a_sparse[k];
-      bad_order |= i > j;
-      bad_range |= (i < 0) | (i >= nd) | (j < 0) | (j >= nd);  // both bounds: general storage has i > j
+    int bad_index = 0, bad_order = 0, bad_range = 0;
+#pragma omp parallel reduction(| : bad_index, bad_order, bad_range) if (nla > 65536)
+    {
+#pragma omp for schedule(static) nowait
+      for (int k = 0; k < nin; ++k) {
+        const int v = inet[k] - nb;
+        pinet[k] = v;
+        bad_index |= (v < 0) | (v >= nn);
+      }
+#pragma omp for schedule(static) nowait
+      for (int i = 0; i < nn; ++i) {
+        const int v = isngn[i] - nb;
+        pisngn[i] = v;
+        pnndf[i] = nndf[i];
+        bad_index |= v < 0;
+      }
+#pragma omp for schedule(static) nowait
+      for (int i = 0; i < nd; ++i) {
+        const int v = isvgvn[i] - nb;
+        pisvgvn[i] = v;
+        bad_index |= v < 0;
+        pifix[i] = ifix[i];
+        pfixv[i] = fixv[i];
+        prhs[i] = rhs[i];
+        psol[i] = sol[i];
+      }
+#pragma omp for schedule(static) nowait
+      for (int e = 0; e < ne; ++e) {
+        const int v = isegn[e] - nb;
+        pisegn[e] = v;
+        pnnet[e] = nnet[e];
+        bad_index |= v < 0;
+      }
+#pragma omp for schedule(static) nowait
+      for (long k = 0; k < nxyz; ++k) pxyz[k] = xyz[k];
+#pragma omp for schedule(static) nowait
+      for (int k = 0; k < nla; ++k) {
+        const int i = i_sparse[k] - nb, j = j_sparse[k] - nb;
+        ia[k] = i;
+        ja[k] = j;
+        av[k] = a_sparse[k];
+        bad_order |= i > j;
+        bad_range |= (i < 0) | (i >= nd) | (j < 0) | (j >= nd);  // both bounds: general storage has i > j
+      }
     }
+    if (bad_index)
+      throw Error{ERR_ARGUMENT, "INET entry outside the subdomain's nodes, or a negative global index"};
     if (bad_order && *matrixtype != 0)  // module_levels.f90:748-752
       throw Error{ERR_ARGUMENT, "matrix in wrong format - only the upper triangle is expected for symmetric problems"};
     if (bad_range) throw Error{ERR_ARGUMENT, "matrix index out of range"};
