@@ -142,24 +142,43 @@ void full_symmetric_csr(const Subdomain& s, vector<int>& ptr, vector<int>& col, 
     val.assign(s.a.begin(), s.a.end());
     return;
   }
-  // the assembled upper triangle is sorted by (row, column): scanning it in
+  // The assembled upper triangle is sorted by (row, column): scanning it in
   // order appends the mirrored entries of every row in increasing column
-  // order, and the row's own entries follow, so no row needs sorting
-  // (every slot of col and val is written below: resize, so that buffers a
-  // caller reuses are not cleared first)
+  // order, and the row's own entries (its run of equal ia, copied whole)
+  // follow, so no row needs sorting.  Every slot of col and val is written:
+  // resize, so that buffers a caller reuses are not cleared first.
+  const int* ia = s.ia.data();
+  const int* ja = s.ja.data();
+  const double* av = s.a.data();
+  const size_t m = s.ia.size();
+  static thread_local vector<int> ustart, ulen;  // each row's run in the upper triangle
+  ustart.assign(n, 0);
+  ulen.assign(n, 0);
   ptr.assign(n + 1, 0);
-  for (size_t k = 0; k < s.ia.size(); ++k) {
-    ptr[s.ia[k] + 1]++;
-    if (s.ia[k] != s.ja[k]) ptr[s.ja[k] + 1]++;
+  for (size_t k = 0; k < m;) {
+    const int r = ia[k];
+    size_t e = k;
+    while (e < m && ia[e] == r) {
+      ptr[ja[e] + 1] += ja[e] != r;  // the mirrored entry lands in row ja
+      ++e;
+    }
+    ptr[r + 1] += (int)(e - k);
+    ustart[r] = (int)k;
+    ulen[r] = (int)(e - k);
+    k = e;
   }
   for (int i = 0; i < n; ++i) ptr[i + 1] += ptr[i];
   col.resize(ptr[n]);
   val.resize(ptr[n]);
   static thread_local vector<int> pos;
   pos.assign(ptr.begin(), ptr.end() - 1);
-  for (size_t k = 0; k < s.ia.size(); ++k)
-    if (s.ia[k] != s.ja[k]) { int j = s.ja[k]; col[pos[j]] = s.ia[k]; val[pos[j]++] = s.a[k]; }
-  for (size_t k = 0; k < s.ia.size(); ++k) { int i = s.ia[k]; col[pos[i]] = s.ja[k]; val[pos[i]++] = s.a[k]; }
+  for (size_t k = 0; k < m; ++k)
+    if (ia[k] != ja[k]) { int j = ja[k]; col[pos[j]] = ia[k]; val[pos[j]++] = av[k]; }
+  for (int r = 0; r < n; ++r) {
+    const int k0 = ustart[r], k1 = k0 + ulen[r];
+    std::copy(ja + k0, ja + k1, col.begin() + pos[r]);
+    std::copy(av + k0, av + k1, val.begin() + pos[r]);
+  }
 }
 
 // Interior ordering for the band factor: natural order, natural order with
