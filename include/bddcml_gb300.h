@@ -83,7 +83,11 @@ void bddcml_upload_global_data_file_c(int *nelem, int *nnod, int *ndof, int *ndi
  * and 2 (symmetric) take the upper triangle; 0 (general) takes all entries and
  * is solved with LU factors and a dual coarse basis (use BiCGSTAB, method 1);
  * three levels, adaptive constraints, batched loads and reactions need a
- * symmetric matrix (BDDCML_ERR_UNSUPPORTED otherwise). */
+ * symmetric matrix (BDDCML_ERR_UNSUPPORTED otherwise).  Indices are checked
+ * after the numbase shift: INET within [0, nnods), ISNGN / ISVGVN / ISEGN not
+ * negative, both matrix indices within [0, ndofs), and row <= column for
+ * matrixtype 1 and 2.  A failed check sets BDDCML_ERR_ARGUMENT and leaves the
+ * subdomain not loaded, so the call can be repeated with corrected data. */
 void bddcml_upload_subdomain_data_c(int *nelem, int *nnod, int *ndof, int *ndim, int *meshdim,
                                     int *isub, int *nelems, int *nnods, int *ndofs,
                                     int *inet, int *linet, int *nnet, int *lnnet, int *nndf, int *lnndf,
