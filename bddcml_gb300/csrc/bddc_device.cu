@@ -737,31 +737,31 @@ static void setup_numeric(Solver& S, Device& D, vector<SubBlocks>& blk) {
     std::unique_ptr<double[]> val(new double[std::max<long long>(1, co[nsub])]);
 #pragma omp parallel for schedule(dynamic)
     for (int t = 0; t < nsub; ++t) {
-      vector<int>& p = get_ptr(blk[t]);
-      vector<int>& c = get_col(blk[t]);
-      vector<double>& v = get_val(blk[t]);
+      auto& p = get_ptr(blk[t]);
+      auto& c = get_col(blk[t]);
+      auto& v = get_val(blk[t]);
       const int base = (int)co[t];
       for (size_t i = 0; i < p.size(); ++i) ptr[po[t] + i] = base + p[i];
       if (!c.empty()) {
         std::memcpy(col.get() + co[t], c.data(), c.size() * sizeof(int));
         std::memcpy(val.get() + co[t], v.data(), v.size() * sizeof(double));
       }
-      vector<int>().swap(p);
-      vector<int>().swap(c);
-      vector<double>().swap(v);
+      std::decay_t<decltype(p)>().swap(p);
+      std::decay_t<decltype(c)>().swap(c);
+      std::decay_t<decltype(v)>().swap(v);
     }
     view.ptr = upload(ptr.get(), (size_t)po[nsub], own, st);
     view.col = upload(col.get(), (size_t)co[nsub], own, st);
     view.val = upload(val.get(), (size_t)co[nsub], own, st);
   };
-  concat([](SubBlocks& b) -> vector<int>& { return b.oo_ptr; }, [](SubBlocks& b) -> vector<int>& { return b.oo_col; },
-         [](SubBlocks& b) -> vector<double>& { return b.oo_val; }, D.koo);
-  concat([](SubBlocks& b) -> vector<int>& { return b.oi_ptr; }, [](SubBlocks& b) -> vector<int>& { return b.oi_col; },
-         [](SubBlocks& b) -> vector<double>& { return b.oi_val; }, D.koi);
-  concat([](SubBlocks& b) -> vector<int>& { return b.io_ptr; }, [](SubBlocks& b) -> vector<int>& { return b.io_col; },
-         [](SubBlocks& b) -> vector<double>& { return b.io_val; }, D.kio);
-  concat([](SubBlocks& b) -> vector<int>& { return b.ii_ptr; }, [](SubBlocks& b) -> vector<int>& { return b.ii_col; },
-         [](SubBlocks& b) -> vector<double>& { return b.ii_val; }, D.kii);
+  concat([](SubBlocks& b) -> vector<int>& { return b.oo_ptr; }, [](SubBlocks& b) -> rawvec<int>& { return b.oo_col; },
+         [](SubBlocks& b) -> rawvec<double>& { return b.oo_val; }, D.koo);
+  concat([](SubBlocks& b) -> vector<int>& { return b.oi_ptr; }, [](SubBlocks& b) -> rawvec<int>& { return b.oi_col; },
+         [](SubBlocks& b) -> rawvec<double>& { return b.oi_val; }, D.koi);
+  concat([](SubBlocks& b) -> vector<int>& { return b.io_ptr; }, [](SubBlocks& b) -> rawvec<int>& { return b.io_col; },
+         [](SubBlocks& b) -> rawvec<double>& { return b.io_val; }, D.kio);
+  concat([](SubBlocks& b) -> vector<int>& { return b.ii_ptr; }, [](SubBlocks& b) -> rawvec<int>& { return b.ii_col; },
+         [](SubBlocks& b) -> rawvec<double>& { return b.ii_val; }, D.kii);
   // ---- interface vectors and owner lists
   D.n = S.ninterface;
   {

@@ -933,8 +933,8 @@ void host_prepare_blocks(Subdomain& s, SubBlocks& b) {
   // the band; diagonal entries are always kept.
   struct Out {
     vector<int>* ptr;
-    vector<int>* col;
-    vector<double>* val;
+    rawvec<int>* col;
+    rawvec<double>* val;
     int* maxrow;
   };
   auto build = [&](int nrow, auto rowdof, Out o, Out i) {

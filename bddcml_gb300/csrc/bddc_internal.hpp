@@ -192,8 +192,9 @@ struct AdaptivePairs {
 // band-reducing order): A_oo, A_oi, A_io, A_ii as CSR, the reduced-rhs inputs
 // and the band width of A_oo in 64-row blocks.
 struct SubBlocks {
-  vector<int> oo_ptr, oo_col, oi_ptr, oi_col, io_ptr, io_col, ii_ptr, ii_col;
-  vector<double> oo_val, oi_val, io_val, ii_val;
+  vector<int> oo_ptr, oi_ptr, io_ptr, ii_ptr;
+  rawvec<int> oo_col, oi_col, io_col, ii_col;  // written once by the row split: no zero fill
+  rawvec<double> oo_val, oi_val, io_val, ii_val;
   vector<double> fo, fi;  // interior rhs (new order), interface rhs (weighted)
   int w = 0;
   double rho = 1.0;
