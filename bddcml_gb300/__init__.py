@@ -122,8 +122,8 @@ def last_error():
 
 
 def _check():
-    code, msg = last_error()
-    if code != 0:
+    if lib().bddcml_get_last_error_c(None, None) != 0:  # status only; the message on failure
+        code, msg = last_error()
         raise BddcmlError(code, msg)
 
 
