@@ -20,7 +20,6 @@
 #include <array>
 #include <chrono>
 #include <cmath>
-#include <map>
 #include <numeric>
 #include <omp.h>
 #include <stdexcept>
@@ -313,21 +312,43 @@ Sharing build_sharing(const Solver& S, int nnod_global) {
 
 // sharing signature of a node as seen from subdomain t: for every other
 // subdomain holding the node (ascending), its index, its component of the node
-// and t's own component (module_dd.f90:9160-9175 globsubs)
-using Sig = vector<std::array<int, 3>>;
-
-Sig signature(const Solver& S, const Sharing& sh, int t, int g) {
-  Sig sig;
-  int mycomp = 0;
-  for (int q = sh.ptr[g]; q < sh.ptr[g + 1]; ++q)
-    if (sh.sub[q] == t) mycomp = S.subs[t].comp[sh.loc[q]];
-  for (int q = sh.ptr[g]; q < sh.ptr[g + 1]; ++q) {
-    int u = sh.sub[q];
-    if (u == t) continue;
-    sig.push_back({u, S.subs[u].comp[sh.loc[q]], mycomp});
+// and t's own component (module_dd.f90:9160-9175 globsubs).  The signatures of
+// all interface nodes of a subdomain are kept flat: node i's entries are
+// e[p[i]] .. e[p[i + 1]].
+struct SigTable {
+  vector<int> p;
+  vector<std::array<int, 3>> e;
+  int size(int i) const { return p[i + 1] - p[i]; }
+  bool equal(int a, int b) const {
+    return std::equal(e.begin() + p[a], e.begin() + p[a + 1], e.begin() + p[b], e.begin() + p[b + 1]);
   }
-  return sig;
+  bool less(int a, int b) const {
+    return std::lexicographical_compare(e.begin() + p[a], e.begin() + p[a + 1], e.begin() + p[b],
+                                        e.begin() + p[b + 1]);
+  }
+};
+
+SigTable signatures(const Solver& S, const Sharing& sh, int t) {
+  const Subdomain& s = S.subs[t];
+  SigTable st;
+  st.p.assign(s.nnodi + 1, 0);
+  st.e.reserve((size_t)s.nnodi * 2);
+  for (int i = 0; i < s.nnodi; ++i) {
+    const int g = s.isngn[s.iin[i]];
+    int mycomp = 0;
+    for (int q = sh.ptr[g]; q < sh.ptr[g + 1]; ++q)
+      if (sh.sub[q] == t) mycomp = s.comp[sh.loc[q]];
+    for (int q = sh.ptr[g]; q < sh.ptr[g + 1]; ++q) {
+      const int u = sh.sub[q];
+      if (u == t) continue;
+      st.e.push_back({u, S.subs[u].comp[sh.loc[q]], mycomp});
+    }
+    st.p[i + 1] = (int)st.e.size();
+  }
+  return st;
 }
+
+using Sig = vector<std::array<int, 3>>;
 
 struct SigHash {
   size_t operator()(const Sig& s) const {
@@ -336,6 +357,25 @@ struct SigHash {
     return h;
   }
 };
+
+// nodes grouped by equal signature, each group in visiting order, the groups
+// in the order of their first node (the lookup key is one reused buffer)
+vector<vector<int>> group_by_signature(const SigTable& st, const vector<int>& nodes) {
+  std::unordered_map<Sig, int, SigHash> first;
+  Sig key;
+  vector<vector<int>> groups;
+  for (int i : nodes) {
+    key.assign(st.e.begin() + st.p[i], st.e.begin() + st.p[i + 1]);
+    auto it = first.find(key);
+    if (it == first.end()) {
+      first.emplace(key, (int)groups.size());
+      groups.push_back({i});
+    } else {
+      groups[it->second].push_back(i);
+    }
+  }
+  return groups;
+}
 
 }  // namespace
 
@@ -565,37 +605,35 @@ void host_setup(Solver& S) {
   // ---- pass 1: glob classification and corner selection, per subdomain
   vector<char> corner_node(nnod_global, 0);  // union of all subdomains' corner choices
   vector<vector<int>> pass1_corners(nsub);
+  vector<SigTable> sigt(nsub);  // kept for pass 2: the components do not change in between
   int meshdim = S.subs.empty() ? 3 : S.subs[0].ndim;
 #pragma omp parallel for schedule(dynamic)
   for (int t = 0; t < nsub; ++t) {
     auto& s = S.subs[t];
     int nnodi = s.nnodi;
-    vector<Sig> sig(nnodi);
-    for (int i = 0; i < nnodi; ++i) sig[i] = signature(S, sh, t, s.isngn[s.iin[i]]);
+    sigt[t] = signatures(S, sh, t);
+    const SigTable& st = sigt[t];
     vector<int> type(nnodi, 0);
     {
-      std::unordered_map<Sig, int, SigHash> first;  // signature -> first node
-      vector<int> size(nnodi, 0), head(nnodi, -1);
-      for (int i = 0; i < nnodi; ++i) {
-        auto it = first.find(sig[i]);
-        if (it == first.end()) { first.emplace(sig[i], i); head[i] = i; }
-        else head[i] = it->second;
-        size[head[i]]++;
-      }
-      for (int i = 0; i < nnodi; ++i) {
-        int h = head[i];
-        if (sig[i].size() == 1) type[i] = 1;
-        else type[i] = size[h] > 1 ? 2 : 3;
-      }
+      vector<int> all(nnodi);
+      std::iota(all.begin(), all.end(), 0);
+      for (const auto& grp : group_by_signature(st, all))
+        for (int i : grp) type[i] = st.size(i) == 1 ? 1 : (grp.size() > 1 ? 2 : 3);
     }
     if (S.prm.use_corner) {
       // per neighbour sharing a face: up to four extreme points of each
       // component of the shared node set (module_dd.f90:10017-10327)
-      for (int u : s.adj) {
+      // nodes shared with each neighbour (its position in s.adj), in node order
+      vector<vector<std::pair<int, int>>> shared(s.adj.size());  // (global id, inodi)
+      for (int i = 0; i < nnodi; ++i)
+        for (int q = st.p[i]; q < st.p[i + 1]; ++q) {
+          const size_t k = std::lower_bound(s.adj.begin(), s.adj.end(), st.e[q][0]) - s.adj.begin();
+          shared[k].emplace_back(s.isngn[s.iin[i]], i);
+        }
+      for (size_t ka = 0; ka < s.adj.size(); ++ka) {
+        const int u = s.adj[ka];
         // shared nodes with u, ascending global id
-        vector<std::pair<int, int>> shn;  // (global id, inodi)
-        for (int i = 0; i < nnodi; ++i)
-          for (auto& e : sig[i]) if (e[0] == u) { shn.emplace_back(s.isngn[s.iin[i]], i); break; }
+        vector<std::pair<int, int>>& shn = shared[ka];
         std::sort(shn.begin(), shn.end());
         bool face = false;
         for (auto& p : shn) if (type[p.second] == 1) { face = true; break; }
@@ -604,15 +642,15 @@ void host_setup(Solver& S) {
         vector<int> myc(m), adc(m);
         for (int q = 0; q < m; ++q) {
           int i = shn[q].second;
-          for (auto& e : sig[i]) if (e[0] == u) { adc[q] = e[1]; myc[q] = e[2]; }
+          for (int r = st.p[i]; r < st.p[i + 1]; ++r)
+            if (st.e[r][0] == u) { adc[q] = st.e[r][1]; myc[q] = st.e[r][2]; }
         }
-        auto renumber = [](vector<int>& v) {
-          std::map<int, int> mp;
-          for (int x : v) mp[x] = 0;
-          int k = 0;
-          for (auto& kv : mp) kv.second = ++k;
-          for (int& x : v) x = mp[x];
-          return k;
+        auto renumber = [](vector<int>& v) {  // values -> their rank among the distinct values, from 1
+          vector<int> u(v);
+          std::sort(u.begin(), u.end());
+          u.erase(std::unique(u.begin(), u.end()), u.end());
+          for (int& x : v) x = (int)(std::lower_bound(u.begin(), u.end(), x) - u.begin()) + 1;
+          return (int)u.size();
         };
         renumber(myc);
         int nadc = renumber(adc);
@@ -725,20 +763,17 @@ void host_setup(Solver& S) {
 #pragma omp parallel for schedule(dynamic)
   for (int t = 0; t < nsub; ++t) {
     auto& s = S.subs[t];
-    std::unordered_map<Sig, int, SigHash> eidx, fidx;
-    for (int i = 0; i < s.nnodi; ++i) {
-      int g = s.isngn[s.iin[i]];
-      if (corner_node[g]) continue;
-      Sig sg = signature(S, sh, t, g);
-      if (sg.size() > 1) {
-        auto it = eidx.find(sg);
-        if (it == eidx.end()) { eidx.emplace(sg, (int)edges[t].size()); edges[t].push_back({i}); }
-        else edges[t][it->second].push_back(i);
-      } else {
-        auto it = fidx.find(sg);
-        if (it == fidx.end()) { fidx.emplace(sg, (int)faces[t].size()); faces[t].push_back({i}); }
-        else faces[t][it->second].push_back(i);
+    {
+      // non-corner nodes shared by more than one other subdomain form edges,
+      // the others faces; one glob per signature
+      vector<int> en, fn;
+      for (int i = 0; i < s.nnodi; ++i) {
+        if (corner_node[s.isngn[s.iin[i]]]) continue;
+        (sigt[t].size(i) > 1 ? en : fn).push_back(i);
       }
+      edges[t] = group_by_signature(sigt[t], en);
+      faces[t] = group_by_signature(sigt[t], fn);
+      SigTable().e.swap(sigt[t].e);
     }
     if (s.bc_present) {  // remove_bc_nodes on the first level (module_levels.f90:2233-2237)
       auto strip = [&](vector<vector<int>>& globs) {
