@@ -310,6 +310,40 @@ Sharing build_sharing(const Solver& S, int nnod_global) {
   return sh;
 }
 
+// Holders of each unique interface dof in ascending subdomain order: those of
+// u are osub / oloc (subdomain, interface index) [optr[u], optr[u + 1]).  Each
+// thread owns a range of unique dofs and scans every subdomain in order.
+void owner_lists(const Solver& S, vector<int>& optr, vector<int>& osub, vector<int>& oloc) {
+  const int n = S.ninterface, nsub = (int)S.subs.size();
+  optr.assign(n + 1, 0);
+#pragma omp parallel
+  {
+    const int nt = omp_get_num_threads(), th = omp_get_thread_num();
+    const int u0 = (int)((long)n * th / nt), u1 = (int)((long)n * (th + 1) / nt);
+    for (int t = 0; t < nsub; ++t)
+      for (int u : S.subs[t].uniq)
+        if (u >= u0 && u < u1) optr[u + 1]++;
+#pragma omp barrier
+#pragma omp single
+    {
+      for (int u = 0; u < n; ++u) optr[u + 1] += optr[u];
+      osub.resize(optr[n]);
+      oloc.resize(optr[n]);
+    }
+    vector<int> pos(optr.begin() + u0, optr.begin() + u1);
+    for (int t = 0; t < nsub; ++t) {
+      const vector<int>& uq = S.subs[t].uniq;
+      for (int i = 0; i < (int)uq.size(); ++i) {
+        const int u = uq[i];
+        if (u < u0 || u >= u1) continue;
+        int& q = pos[u - u0];
+        osub[q] = t;
+        oloc[q++] = i;
+      }
+    }
+  }
+}
+
 // sharing signature of a node as seen from subdomain t: for every other
 // subdomain holding the node (ascending), its index, its component of the node
 // and t's own component (module_dd.f90:9160-9175 globsubs).  The signatures of
@@ -392,15 +426,8 @@ static void host_replay_bc(Subdomain& s) {
 // ascending subdomain order (upload / swap / download, module_dd.f90:1200-1255)
 static void host_interface_bc(Solver& S) {
   const int nsub = (int)S.subs.size();
-  vector<int> optr(S.ninterface + 1, 0);
-  for (auto& s : S.subs) for (int u : s.uniq) optr[u + 1]++;
-  for (int u = 0; u < S.ninterface; ++u) optr[u + 1] += optr[u];
-  vector<int> osub(optr[S.ninterface]), oloc(optr[S.ninterface]);
-  {
-    vector<int> pos(optr.begin(), optr.end() - 1);
-    for (int t = 0; t < nsub; ++t)
-      for (int i = 0; i < S.subs[t].ndofi; ++i) { int u = S.subs[t].uniq[i]; osub[pos[u]] = t; oloc[pos[u]++] = i; }
-  }
+  vector<int> optr, osub, oloc;
+  owner_lists(S, optr, osub, oloc);
   vector<vector<double>> bci(nsub);
 #pragma omp parallel for schedule(dynamic)
   for (int t = 0; t < nsub; ++t) {
@@ -838,13 +865,36 @@ void host_setup(Solver& S) {
 
   // ---- unique interface dofs (numbered in ascending global dof id) and per-dof sharing lists
   vector<int> gdof_uniq(ndof_global, -1);
-  for (auto& s : S.subs)
-    for (int i = 0; i < s.ndofi; ++i) gdof_uniq[s.isvgvn[s.iivsvn[i]]] = -2;  // marks
-  {
-    int nu = 0;
-    for (int g = 0; g < ndof_global; ++g)
-      if (gdof_uniq[g] == -2) gdof_uniq[g] = nu++;
-    S.ninterface = nu;
+#pragma omp parallel for schedule(dynamic)
+  for (int t = 0; t < nsub; ++t) {
+    const auto& s = S.subs[t];
+    for (int i = 0; i < s.ndofi; ++i) {
+      const int g = s.isvgvn[s.iivsvn[i]];
+#pragma omp atomic write
+      gdof_uniq[g] = -2;  // marks (several subdomains mark a shared dof)
+    }
+  }
+  {  // marked dofs numbered in ascending global id: per-thread counts of contiguous id ranges, then offsets
+    vector<int> cnt(omp_get_max_threads() + 1, 0);
+    int nused = 1;
+#pragma omp parallel num_threads((int)cnt.size() - 1)
+    {
+      const int nt = omp_get_num_threads(), th = omp_get_thread_num();
+      const int g0 = (int)((long)ndof_global * th / nt), g1 = (int)((long)ndof_global * (th + 1) / nt);
+      int c = 0;
+      for (int g = g0; g < g1; ++g) c += gdof_uniq[g] == -2;
+      cnt[th + 1] = c;
+#pragma omp barrier
+#pragma omp single
+      {
+        for (int q = 0; q < nt; ++q) cnt[q + 1] += cnt[q];
+        nused = nt;
+      }
+      int nu = cnt[th];
+      for (int g = g0; g < g1; ++g)
+        if (gdof_uniq[g] == -2) gdof_uniq[g] = nu++;
+    }
+    S.ninterface = cnt[nused];
   }
 #pragma omp parallel for schedule(dynamic)
   for (int t = 0; t < nsub; ++t) {
@@ -853,15 +903,8 @@ void host_setup(Solver& S) {
     for (int i = 0; i < s.ndofi; ++i) s.uniq[i] = gdof_uniq[s.isvgvn[s.iivsvn[i]]];
   }
   // owners of each unique dof, ascending subdomain
-  vector<int> optr(S.ninterface + 1, 0);
-  for (auto& s : S.subs) for (int u : s.uniq) optr[u + 1]++;
-  for (int u = 0; u < S.ninterface; ++u) optr[u + 1] += optr[u];
-  vector<int> osub(optr[S.ninterface]), oloc(optr[S.ninterface]);
-  {
-    vector<int> pos(optr.begin(), optr.end() - 1);
-    for (int t = 0; t < nsub; ++t)
-      for (int i = 0; i < S.subs[t].ndofi; ++i) { int u = S.subs[t].uniq[i]; osub[pos[u]] = t; oloc[pos[u]++] = i; }
-  }
+  vector<int> optr, osub, oloc;
+  owner_lists(S, optr, osub, oloc);
   // own value plus the other holders' values in ascending order (the
   // upload / swap / download sum of module_dd.f90:11236-11551)
   auto neighbour_sum = [&](int t, int i, const std::function<double(int, int)>& val) {
