@@ -45,7 +45,7 @@ EXPORTS = ["bddcml_init_c", "bddcml_upload_global_data_c", "bddcml_upload_subdom
            "bddcml_dotprod_subdomain_dev_c", "bddcml_element_gradient_dev_c", "bddcml_set_adaptive_threshold_c",
            "bddcml_get_adaptive_info_c", "bddcml_upload_subdomain_rhs_batch_c", "bddcml_solve_batch_c",
            "bddcml_download_local_solution_batch_c", "bddcml_set_batch_operator_c",
-           "bddcml_upload_global_data_file_c", "bddcml_set_wait_limit_c"]
+           "bddcml_upload_global_data_file_c", "bddcml_set_wait_limit_c", "bddcml_get_setup_digest_c"]
 
 # phases of bddcml_get_profile_c (CUDA events on the solver stream)
 PHASES = ["numeric_total", "solve_total", "factor_interior", "solve_interior", "refine_residual", "schur",
@@ -438,6 +438,14 @@ def get_coarse_info() -> dict:
     _check()
     keys = ["ncorner", "nedge", "nface", "ndofc", "sum_ndofi", "sum_ndofo"]
     return {k: int(buf[i]) for i, k in enumerate(keys)}
+
+
+def get_setup_digest() -> int:
+    """64-bit digest of the host-side setup results (independent of the thread count)."""
+    d = C.c_ulonglong(0)
+    lib().bddcml_get_setup_digest_c(C.byref(d))
+    _check()
+    return d.value
 
 
 # ------------------------------------------------------------ convenience

@@ -726,6 +726,40 @@ void bddcml_get_profile_c(double* ms, int* counts, int* lphase) {
   });
 }
 
+void bddcml_get_setup_digest_c(unsigned long long* digest) {
+  guarded("bddcml_get_setup_digest_c", [&] {
+    Solver* S = need_solver("bddcml_get_setup_digest_c");
+    if (!S) return;
+    if (!digest) throw Error{ERR_ARGUMENT, "null argument"};
+    // FNV-1a over the bytes of every host-side setup result, in subdomain order
+    unsigned long long h = 1469598103934665603ull;
+    auto bytes = [&h](const void* p, size_t n) {
+      const unsigned char* c = static_cast<const unsigned char*>(p);
+      for (size_t i = 0; i < n; ++i) { h ^= c[i]; h *= 1099511628211ull; }
+    };
+    auto arr = [&](const auto& v) {
+      const unsigned long long n = v.size();
+      bytes(&n, sizeof n);
+      if (n) bytes(v.data(), n * sizeof(v[0]));
+    };
+    auto val = [&](const auto& x) { bytes(&x, sizeof x); };
+    for (const auto& s : S->subs) {
+      arr(s.ia); arr(s.ja); arr(s.a); arr(s.comp);
+      arr(s.iin); arr(s.kdofi); arr(s.iivsvn); arr(s.iovsvn); arr(s.adj);
+      for (const auto& cn : s.cnodes) {
+        val(cn.itype); val(cn.global_number); arr(cn.inodi); arr(cn.idofi); val(cn.ncdof); val(cn.used);
+        arr(cn.matrix);
+      }
+      arr(s.c_ptr); arr(s.c_col); arr(s.c_val); arr(s.indrowc);
+      arr(s.bc); arr(s.bcx_tgt); arr(s.bcx_src); arr(s.bcx_val); arr(s.fxr_i); arr(s.fxr_j); arr(s.fxr_v);
+      arr(s.wi); arr(s.uniq); arr(s.operm); val(s.band);
+    }
+    int v[] = {S->ncorner, S->nedge, S->nface, S->ndofc, S->ninterface};
+    bytes(v, sizeof v);
+    *digest = h;
+  });
+}
+
 void bddcml_get_coarse_info_c(int* out, int* lout) {
   guarded("bddcml_get_coarse_info_c", [&] {
     Solver* S = need_solver("bddcml_get_coarse_info_c");

@@ -243,6 +243,15 @@ void bddcml_get_interface_weights_c(int *isub, double *wi, int *lwi);
  * module_levels.f90:2240-2300 (printed there, returned here). */
 void bddcml_get_coarse_info_c(int *out, int *lout);
 
+/* 64-bit digest (FNV-1a) of every host-side setup result: the assembled
+ * subdomain matrices, mesh components, interface and interior dof lists,
+ * coarse nodes and constraint rows, eliminated Dirichlet values, weights,
+ * unique interface numbering and interior orderings.  The host setup runs on
+ * all host threads with fixed orders of work, so the digest does not depend
+ * on the thread count.  Available after the host part of
+ * bddcml_setup_preconditioner_c.  No counterpart in the reference. */
+void bddcml_get_setup_digest_c(unsigned long long *digest);
+
 /* Switches the per-phase CUDA-event timers on (1) or off (0).  The two totals
  * (numeric setup, solve) are always timed.  No counterpart in the reference
  * (its verbosity-2 profiling prints wall times, module_bddcml.f90:91-93). */

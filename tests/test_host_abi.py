@@ -351,3 +351,45 @@ def test_mesh_indices_checked_at_upload(built_lib):
         B.upload_problem(prob)
     finally:
         B.bddcml_finalize()
+
+
+_DIGEST_RUN = r"""
+import sys
+sys.path.insert(0, sys.argv[1])
+import bddcml_gb300 as B
+from bddcml_gb300 import problems
+case = sys.argv[2]
+if case == "uneven":
+    prob = problems.poisson_boxes(24, problems.random_box_partition(24, 5, 10, seed=17),
+                                  kappa=problems.lognormal_kappa(24, 1.0, seed=2))
+    weights = 1
+else:
+    prob = problems.elasticity_on_cube(8, 2, nu=0.3, young=problems.inclusions_young(16))
+    weights = 0
+B.bddcml_init(2, [prob.nsub, 1], -1, 0, 0, 0, 0)
+B.upload_problem(prob)
+try:
+    B.bddcml_setup_preconditioner(1, 0, 1, 1, 1, 0, 0, weights)
+except B.BddcmlError as e:
+    assert e.code == 2, e  # no GPU: the host part has run
+print(B.get_setup_digest())
+B.bddcml_finalize()
+"""
+
+
+@pytest.mark.parametrize("case", ["uneven", "elasticity"])
+def test_host_setup_independent_of_thread_count(built_lib, case):
+    """Every host-side setup result (assembled matrices, components, globs,
+    constraints, eliminated values, weights, numbering, orderings) is bit for bit
+    the same with 1, 3 and 8 OpenMP threads: the parallel steps split work by
+    subdomain or by ranges of global ids and keep the serial orders."""
+    import subprocess
+    import sys
+    digests = set()
+    for nt in (1, 3, 8):
+        env = dict(os.environ, OMP_NUM_THREADS=str(nt))
+        out = subprocess.run([sys.executable, "-c", _DIGEST_RUN, ROOT, case], env=env, capture_output=True,
+                             text=True, timeout=300)
+        assert out.returncode == 0, out.stderr[-2000:]
+        digests.add(out.stdout.strip().splitlines()[-1])
+    assert len(digests) == 1, digests
