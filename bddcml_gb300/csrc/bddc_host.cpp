@@ -748,29 +748,43 @@ void host_setup(Solver& S) {
   // subdomains in order, inside a subdomain in interface node order.
   // (arrays indexed by global node id: num 0 = not numbered)
   auto number_entities = [&](int shift, const vector<vector<int>>& ent_gid, vector<vector<int>>& ent_num) {
-    vector<int> num(nnod_global, 0);
-    vector<char> mine(nnod_global, 0);
-    int next = 1;
+    // the entities each subdomain owns, in its interface node order; then
+    // offsets over the subdomains, and the numbers
+    vector<vector<int>> owned(nsub);
+    vector<int> off(nsub + 1, 0);
+#pragma omp parallel for schedule(dynamic)
     for (int t = 0; t < nsub; ++t) {
       auto& s = S.subs[t];
+      static thread_local vector<char> mine;  // marks of t's entities, cleared after use
+      if ((int)mine.size() < nnod_global) mine.assign(nnod_global, 0);
       for (int g : ent_gid[t]) mine[g] = 1;
       for (int i = 0; i < s.nnodi; ++i) {
-        int g = s.isngn[s.iin[i]];
-        if (!mine[g]) continue;
-        if (sh.sub[sh.ptr[g]] == t) num[g] = shift + next++;
+        const int g = s.isngn[s.iin[i]];
+        if (mine[g] && sh.sub[sh.ptr[g]] == t) owned[t].push_back(g);
       }
       for (int g : ent_gid[t]) mine[g] = 0;
+      off[t + 1] = (int)owned[t].size();
+    }
+    for (int t = 0; t < nsub; ++t) off[t + 1] += off[t];
+    vector<int> num(nnod_global, 0);
+#pragma omp parallel for schedule(dynamic)
+    for (int t = 0; t < nsub; ++t) {
+      int next = shift + 1 + off[t];
+      for (int g : owned[t]) num[g] = next++;
     }
     ent_num.resize(nsub);
+    int orphan = 0;
+#pragma omp parallel for schedule(dynamic) reduction(| : orphan)
     for (int t = 0; t < nsub; ++t) {
       ent_num[t].resize(ent_gid[t].size());
       for (size_t e = 0; e < ent_gid[t].size(); ++e) {
         const int n = num[ent_gid[t][e]];
-        if (n == 0) throw Error{ERR_NUMERIC, "coarse entity without owner"};
+        orphan |= n == 0;
         ent_num[t][e] = n;
       }
     }
-    return next - 1;
+    if (orphan) throw Error{ERR_NUMERIC, "coarse entity without owner"};
+    return off[nsub];
   };
 
   // corners of each subdomain, ascending global id
@@ -839,8 +853,14 @@ void host_setup(Solver& S) {
   for (int t = 0; t < nsub; ++t) {
     auto& s = S.subs[t];
     s.cnodes.clear();
-    std::unordered_map<int, int> inodi_of;
-    for (int i = 0; i < s.nnodi; ++i) inodi_of.emplace(s.isngn[s.iin[i]], i);
+    // interface node of each corner (corner_gid[t] is ascending)
+    const vector<int>& cg = corner_gid[t];
+    vector<int> corner_inodi(cg.size(), -1);
+    for (int i = 0; i < s.nnodi; ++i) {
+      const int g = s.isngn[s.iin[i]];
+      auto it = std::lower_bound(cg.begin(), cg.end(), g);
+      if (it != cg.end() && *it == g) corner_inodi[it - cg.begin()] = i;
+    }
     auto add = [&](int itype, int num, const vector<int>& nodes, bool used) {
       CoarseNode cn;
       cn.itype = itype;
@@ -854,10 +874,11 @@ void host_setup(Solver& S) {
       }
       cn.ncdof = used ? (itype == 3 ? s.nndf[s.iin[nodes[0]]] : ncd) : 0;
       cn.used = used;
-      s.cnodes.push_back(cn);
+      s.cnodes.push_back(std::move(cn));
     };
+    s.cnodes.reserve(corner_gid[t].size() + edges[t].size() + faces[t].size());
     for (size_t c = 0; c < corner_gid[t].size(); ++c)
-      add(3, corner_num[t][c], {inodi_of.at(corner_gid[t][c])}, S.prm.use_corner);
+      add(3, corner_num[t][c], {corner_inodi[c]}, S.prm.use_corner);
     for (size_t e = 0; e < edges[t].size(); ++e) add(2, edge_num[t][e], edges[t][e], S.prm.use_arith);
     for (size_t f = 0; f < faces[t].size(); ++f) add(1, face_num[t][f], faces[t][f], S.prm.use_arith);
   }
